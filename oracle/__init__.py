@@ -1,0 +1,339 @@
+"""FP64 CPU oracle for the LBM hot path (test infrastructure only).
+
+This package is the correctness checker.  The CUDA product path never imports
+it; only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
+``--impl reference`` legs of ``bench.py`` use it.
+
+* ``lbm_oracle.c``   -- plain-C FP64 restatement of the reference time step
+  (Init, Collision/ConvLBM, Streaming, MacroProp, IBLBM, ...), each function
+  citing the reference ``lbm.cpp`` lines it follows.
+* ``build_ref.sh``   -- recipe that compiles the reference's own ``lbm.cpp``
+  (unmodified, where it lies) with ``ref_config.h`` + ``ref_harness.cpp`` into
+  ``oracle/_ref/``; used to pin the restatement (``tests/golden``).
+
+This module loads the restatement with ctypes and builds the benchmark cases
+(3D cavity, channel with an immersed sphere, 2D IBM cylinder) as numpy-backed
+lattices.  Arrays are indexed ``[k, j, i]`` (x fastest), ghost layers
+included.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liblbm_oracle.so")
+
+TYPE_F, TYPE_S, TYPE_OUT, TYPE_IN, TYPE_P, TYPE_L, TYPE_OUTZG = 0, 1, 2, 3, 4, 5, 8
+
+# D3Q19 in the reference order (LBM.h:542-552)
+CX19 = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
+CY19 = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1])
+CZ19 = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1])
+W19 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+REF_PI = 3.14159265
+
+
+def build(force: bool = False) -> str:
+    """Compile lbm_oracle.c into oracle/_build/liblbm_oracle.so (gcc, OpenMP)."""
+    src = os.path.join(HERE, "lbm_oracle.c")
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
+        return LIB
+    os.makedirs(BUILD, exist_ok=True)
+    tmp = LIB + ".tmp%d" % os.getpid()
+    cmd = ["gcc", "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", src, "-o", tmp, "-lm"]
+    subprocess.check_call(cmd)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def build_ref(*variants: str) -> None:
+    """Run the reference-literal recipe (no-op when the reference tree is absent)."""
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), *variants])
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(LIB)
+        vp, d, i, l = C.c_void_p, C.c_double, C.c_int, C.c_long
+        L.orc_create.restype = vp
+        L.orc_create.argtypes = [i, i, i, i, d]
+        L.orc_free.argtypes = [vp]
+        L.orc_enable_thermal.argtypes = [vp, d, d, d, d, d]
+        L.orc_ncell.restype = l
+        L.orc_ncell.argtypes = [vp]
+        L.orc_types.restype = C.POINTER(C.c_uint8)
+        L.orc_types.argtypes = [vp]
+        L.orc_field.restype = C.POINTER(C.c_double)
+        L.orc_field.argtypes = [vp, i]
+        L.orc_set_body_force.argtypes = [vp, d, d, d]
+        L.orc_feq.restype = d
+        L.orc_feq.argtypes = [vp, d, d, d, d, i]
+        L.orc_init.argtypes = [vp]
+        L.orc_collide.restype = l
+        L.orc_collide.argtypes = [vp]
+        L.orc_stream.argtypes = [vp]
+        L.orc_macro.restype = l
+        L.orc_macro.argtypes = [vp]
+        L.orc_step_plain.restype = l
+        L.orc_step_plain.argtypes = [vp, i]
+        L.orc_kernel.restype = d
+        L.orc_kernel.argtypes = [d]
+        L.orc_ibm_step.argtypes = [vp, vp, vp, C.POINTER(d), C.POINTER(d)]
+        L.orc_step_ibm.restype = l
+        L.orc_step_ibm.argtypes = [vp, vp, vp, C.POINTER(d), C.POINTER(d)]
+        L.orc_fibonacci_sphere.argtypes = [i, d, C.POINTER(d)] + [C.POINTER(d)] * 7
+        L.orc_body_step.argtypes = [vp, vp, d, C.POINTER(d)]
+        L.orc_nusselt_volume.restype = d
+        L.orc_nusselt_volume.argtypes = [vp, d, d]
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Markers(C.Structure):
+    """Mirror of ``orc_markers``; numpy arrays own the memory."""
+
+    _fields_ = [("n", C.c_int)] + [
+        (nm, C.POINTER(C.c_double))
+        for nm in ("x", "y", "z", "nx", "ny", "nz", "ds", "udx", "udy", "udz", "ubx", "uby", "ubz",
+                   "Fbx", "Fby", "Fbz", "Td", "Tb", "Qb")
+    ]
+
+    def __init__(self, n: int):
+        super().__init__()
+        self.n = n
+        self.arrays = {}
+        for nm, _ in self._fields_[1:]:
+            a = np.zeros(n)
+            self.arrays[nm] = a
+            setattr(self, nm, _dp(a))
+
+    def __getitem__(self, nm):
+        return self.arrays[nm]
+
+
+class IbmOpts(C.Structure):
+    """Mirror of ``orc_ibm_opts``."""
+
+    _fields_ = [("box_lo", C.c_int * 3), ("box_hi", C.c_int * 3), ("m_max", C.c_int),
+                ("lit_sign", C.c_int), ("rho_mode", C.c_int), ("thermal", C.c_int),
+                ("use_avg_density", C.c_int), ("vsolid", C.c_double),
+                ("vcm_new", C.c_double * 3), ("vcm_old", C.c_double * 3)]
+
+
+class Body(C.Structure):
+    """Mirror of ``orc_body``."""
+
+    _fields_ = [("xc", C.c_double * 3), ("v", C.c_double * 3), ("om", C.c_double * 3),
+                ("rho_ratio", C.c_double), ("vol", C.c_double), ("inertia", C.c_double),
+                ("grav", C.c_double * 3)]
+
+
+class Lattice:
+    """An FP64 lattice of (nx+2)(ny+2)(nz+2) cells, ghost layers included."""
+
+    def __init__(self, q: int, nx: int, ny: int, nz: int, tau: float):
+        self.L = lib()
+        self.q, self.nx, self.ny, self.nz, self.tau = q, nx, ny, nz, tau
+        self.h = self.L.orc_create(q, nx, ny, nz, tau)
+        self.shape = (nz + 2, ny + 2, nx + 2)
+        self.n = int(self.L.orc_ncell(self.h))
+        self.thermal = False
+
+    def __del__(self):
+        try:
+            if self.h:
+                self.L.orc_free(self.h)
+                self.h = None
+        except Exception:
+            pass
+
+    def enable_thermal(self, tau_g: float, T0: float = 0.0, gbeta=(0.0, 0.0, 0.0)):
+        self.L.orc_enable_thermal(self.h, tau_g, T0, *gbeta)
+        self.thermal = True
+
+    def _view(self, which: int, comps: int = 1) -> np.ndarray:
+        p = self.L.orc_field(self.h, which)
+        a = np.ctypeslib.as_array(p, shape=(comps * self.n,))
+        if comps == 1:
+            return a.reshape(self.shape)
+        return a.reshape((comps,) + self.shape)
+
+    @property
+    def types(self) -> np.ndarray:
+        p = self.L.orc_types(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.n,)).reshape(self.shape)
+
+    rho = property(lambda s: s._view(0))
+    ux = property(lambda s: s._view(1))
+    uy = property(lambda s: s._view(2))
+    uz = property(lambda s: s._view(3))
+    Fx = property(lambda s: s._view(4))
+    Fy = property(lambda s: s._view(5))
+    Fz = property(lambda s: s._view(6))
+    f = property(lambda s: s._view(7, s.q))
+    fs = property(lambda s: s._view(8, s.q))
+    T = property(lambda s: s._view(9))
+    g = property(lambda s: s._view(10, 7))
+    gs = property(lambda s: s._view(11, 7))
+
+    def set_body_force(self, fx, fy, fz):
+        self.L.orc_set_body_force(self.h, fx, fy, fz)
+
+    def init(self):
+        self.L.orc_init(self.h)
+
+    def step_plain(self, n: int) -> int:
+        return int(self.L.orc_step_plain(self.h, n))
+
+    def collide(self) -> int:
+        return int(self.L.orc_collide(self.h))
+
+    def stream(self):
+        self.L.orc_stream(self.h)
+
+    def macro(self) -> int:
+        return int(self.L.orc_macro(self.h))
+
+    def interior(self, a: np.ndarray) -> np.ndarray:
+        return a[1:-1, 1:-1, 1:-1] if self.nz > 1 or a.shape[0] > 1 else a
+
+    def ibm_step(self, mk: Markers, op: IbmOpts, center) -> np.ndarray:
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        out = np.zeros(7)
+        self.L.orc_ibm_step(self.h, C.byref(mk), C.byref(op), _dp(c), _dp(out))
+        return out
+
+    def step_ibm(self, mk: Markers, op: IbmOpts, center) -> np.ndarray:
+        c = np.ascontiguousarray(center, dtype=np.float64)
+        out = np.zeros(7)
+        self.L.orc_step_ibm(self.h, C.byref(mk), C.byref(op), _dp(c), _dp(out))
+        return out
+
+
+# --------------------------------------------------------------------------
+# Case builders
+# --------------------------------------------------------------------------
+
+def cavity(n: int, tau: float = 0.8, lid: float = 0.05, ny: int | None = None, nz: int | None = None) -> Lattice:
+    """D3Q19 lid-driven cavity: ghost walls TYPE_S, the ghost plane j = Ny+1
+    moving with u = (lid, 0, 0) (Couette top-wall convention,
+    lbm.cpp:1548-1551); rho = 1, u = 0 inside, f = feq."""
+    nx = n
+    ny = n if ny is None else ny
+    nz = n if nz is None else nz
+    lat = Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_S
+    t[1:-1, 1:-1, 1:-1] = TYPE_F
+    lat.ux[:, -1, :] = lid
+    lat.init()
+    return lat
+
+
+def channel(nx: int, ny: int, nz: int, tau: float, u_in: float = 0.05, outlet: int = TYPE_OUTZG) -> Lattice:
+    """D3Q19 channel: inlet ghost plane x = 0 (TYPE_IN, equilibrium at u_in),
+    outlet ghost plane x = nx+1 (zero-gradient by default), halfway
+    bounce-back walls on the y and z ghost planes (walls take the edges).
+    Initial state: rho = 1, u = (u_in, 0, 0) everywhere (lbm.cpp:1804-1818)."""
+    lat = Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    t[:, :, 0] = TYPE_IN
+    t[:, :, -1] = outlet
+    t[:, 0, :] = TYPE_S
+    t[:, -1, :] = TYPE_S
+    t[0, :, :] = TYPE_S
+    t[-1, :, :] = TYPE_S
+    fluidlike = t != TYPE_S
+    lat.ux[fluidlike] = u_in
+    lat.init()
+    return lat
+
+
+def fibonacci_sphere(n: int, diameter: float, center) -> Markers:
+    mk = Markers(n)
+    c = np.ascontiguousarray(center, dtype=np.float64)
+    a = mk.arrays
+    lib().orc_fibonacci_sphere(n, diameter / 2.0, _dp(c), _dp(a["x"]), _dp(a["y"]), _dp(a["z"]),
+                               _dp(a["nx"]), _dp(a["ny"]), _dp(a["nz"]), _dp(a["ds"]))
+    return mk
+
+
+def sphere_box(center, diameter: float, lat: Lattice) -> tuple:
+    """Eulerian node box covering every marker stencil: [floor(c - R) - 2,
+    ceil(c + R) + 2], clamped to the lattice (ghosts included)."""
+    R = diameter / 2.0
+    lo, hi = [], []
+    lims = (lat.nx + 1, lat.ny + 1, lat.nz + 1)
+    for a in range(3):
+        lo.append(max(0, int(np.floor(center[a] - R)) - 2))
+        hi.append(min(lims[a], int(np.ceil(center[a] + R)) + 2))
+    return lo, hi
+
+
+def ibm_opts(lo, hi, m_max: int, lit_sign: int = 0, rho_mode: int = 0, thermal: int = 0) -> IbmOpts:
+    op = IbmOpts()
+    for a in range(3):
+        op.box_lo[a] = lo[a]
+        op.box_hi[a] = hi[a]
+    op.m_max = m_max
+    op.lit_sign = lit_sign
+    op.rho_mode = rho_mode
+    op.thermal = thermal
+    op.use_avg_density = 0
+    return op
+
+
+def cylinder_markers_literal(nodes: int, D: float, cx: float, cy: float) -> Markers:
+    """Generate_Cylinder_Marker (lbm.cpp:1857-1877) + Normal_Marker
+    (lbm.cpp:1048-1069) + ds (main.cpp:123-131), restated."""
+    mk = Markers(nodes)
+    a = mk.arrays
+    r = D / 2.0
+    i = np.arange(nodes)
+    a["x"][:] = r * np.cos(2 * REF_PI / nodes * i) + cx + 0.5
+    a["y"][:] = r * np.sin(2 * REF_PI / nodes * i) + cy + 0.5
+    a["z"][:] = 1.0
+    x2 = np.roll(a["x"], -1)
+    y2 = np.roll(a["y"], -1)
+    ddx, ddy = x2 - a["x"], y2 - a["y"]
+    norm = np.sqrt(ddx ** 2 + ddy ** 2 + 0.0 ** 2)
+    tx, ty = ddx / norm, ddy / norm
+    a["nx"][:] = ty * 1 - 0.0 * 0
+    a["ny"][:] = 0.0 * 0 - tx * 1
+    a["nz"][:] = tx * 0 - ty * 0
+    a["ds"][:] = np.sqrt((a["x"] - x2) ** 2 + (a["y"] - y2) ** 2 + 0.0)
+    return mk
+
+
+def read_ref_dump(path: str, NX: int, NY: int, NZ: int, nfields: int, steps: int = 0, nodes: int = 0):
+    """Read a dump written by ref_harness.cpp."""
+    raw = np.fromfile(path, dtype=np.float64)
+    n = NX * NY * NZ
+    fields = raw[: nfields * n].reshape(nfields, NZ, NY, NX)
+    rest = raw[nfields * n:]
+    out = {"fields": fields}
+    if steps:
+        out["cl"] = rest[:steps]
+        out["cd"] = rest[steps: 2 * steps]
+        out["markers"] = rest[2 * steps: 2 * steps + 8 * nodes].reshape(nodes, 8)
+    return out
+
+
+if __name__ == "__main__":  # pragma: no cover
+    print(build(force="--force" in sys.argv))

@@ -1,0 +1,45 @@
+#!/bin/sh
+# Recipe for the reference-literal oracle: compiles the reference's own
+# lbm.cpp, unmodified and where it lies, against oracle/ref_config.h (which
+# replaces the compile-time configuration block of LBM.h) and the Vector3d
+# stand-in under oracle/shim, with the batch driver oracle/ref_harness.cpp.
+# Outputs go to oracle/_ref/ only.  Needs the reference tree (REF, default
+# /root/reference); without it this script does nothing and exits 0.
+#
+# usage: oracle/build_ref.sh [variant ...]
+#   cavity:N[:TAU]            D3Q19 cavity, N^3 interior
+#   cylinder:NX:NY:D:NODES:M  D2Q9 implicit IBM cylinder
+set -e
+HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${REF:-/root/reference}
+OUT="$HERE/_ref"
+if [ ! -f "$REF/lbm.cpp" ]; then
+    echo "build_ref: no reference tree at $REF, skipped"
+    exit 0
+fi
+mkdir -p "$OUT"
+[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5
+CXX=${CXX:-g++}
+FLAGS="-O2 -fopenmp -ffp-contract=off -w -include $HERE/ref_config.h -I$HERE/shim -I$REF"
+pids=""
+for v in "$@"; do
+    kind=$(echo "$v" | cut -d: -f1)
+    case "$kind" in
+    cavity)
+        n=$(echo "$v" | cut -d: -f2); tau=$(echo "$v" | cut -d: -f3); [ -z "$tau" ] && tau=0.8
+        exe="$OUT/ref_cavity_${n}_${tau}"
+        $CXX $FLAGS -DREF_CAVITY -DREF_NX=$n -DREF_NY=$n -DREF_NZ=$n -DREF_TAU=$tau \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    cylinder)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        nodes=$(echo "$v" | cut -d: -f5); mm=$(echo "$v" | cut -d: -f6)
+        exe="$OUT/ref_cylinder_${nx}_${ny}_${d}_${nodes}_${mm}"
+        $CXX $FLAGS -DREF_CYLINDER -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    *) echo "unknown variant $v"; exit 2 ;;
+    esac
+done
+for p in $pids; do wait $p; done
+echo "build_ref: done -> $OUT"

@@ -1,0 +1,85 @@
+/* ref_config.h -- compile-time configuration for the reference-literal
+ * oracle build.  It is force-included (g++ -include) ahead of the reference
+ * sources; it defines DEFINES_H, so the configuration block of the
+ * reference's LBM.h (LBM.h:9-517) is skipped and these values are used
+ * instead.  Everything after that block (lattice tables, LATTICE, LBM,
+ * MARKER and all of lbm.cpp) is the reference's own code, unmodified.
+ *
+ * Two variants, chosen with -D:
+ *   REF_CAVITY    D3Q19 box with ghost walls (the 3D lid-driven cavity).  The
+ *                 Sphere_BB case flag is used only to select the reference's
+ *                 3D code paths; the harness sets the geometry itself.
+ *   REF_CYLINDER  D2Q9 implicit IBM cylinder (the shipped default case),
+ *                 shrunk to test size.
+ * Sizes come from REF_NX/REF_NY/REF_NZ/REF_TAU (and REF_D, REF_NODES,
+ * REF_MMAX for the cylinder).
+ */
+#include <cmath>
+#include <iostream>
+#include <string>
+#include <vector>
+using namespace std;
+
+#define DEFINES_H
+
+static const double PI = 3.14159265;  // LBM.h:74
+#define rho0 1.0
+#define dt 1.0
+#define dx 1.0
+#define dy 1.0
+#define dz 1.0
+static const double cs2 = pow(dx, 2) / (3 * pow(dt, 2));
+#define p0 rho0 *cs2
+#define Conventional_LBM
+
+#define TYPE_F 0
+#define TYPE_S 1
+#define TYPE_OUT 2
+#define TYPE_IN 3
+#define TYPE_P 4
+#define TYPE_L 5
+#define TYPE_T 6
+#define TYPE_Q 7
+
+#if defined REF_CAVITY
+#define Sphere_BB
+#define MOMENTUM_EXCHANGE_ALGORITHM
+#define D3Q19
+#define Re 200.0
+static const double D = 20;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = REF_NZ;
+static const double u_max = 0.1;
+static double center_x = dx * (Nx / 5.0);
+static double center_y = dy * (Ny / 2.0);
+static double center_z = dz * (Nz / 2.0);
+static const double tau = REF_TAU;
+static const double nu = cs2 * (tau - 0.5);
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_CYLINDER
+#define IBM
+#define Implicit_Diffuse_Interface_Scheme
+#define Cylinder_IBM
+#define Volume_Force
+#define D2Q9
+#define Re 40.0
+static const double D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static const double u_max = 0.1;
+static double center_x = dx * (Nx / 5.0);
+static double center_y = dy * (Ny / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+static const int number_nodes = REF_NODES;
+static const int level_marker = 1;
+static int m_max = REF_MMAX;
+static const double Vsolid = PI * D * D * 0.25;
+#define T_OUT 30000
+#define Nt 10
+#else
+#error "define REF_CAVITY or REF_CYLINDER"
+#endif

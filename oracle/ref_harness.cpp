@@ -1,0 +1,113 @@
+// ref_harness.cpp -- driver for the reference-literal oracle build.
+//
+// Test infrastructure only.  It replaces main.cpp (which has a VTK/CSV output
+// cadence and an interactive prompt) with a batch driver that
+//   - builds the geometry through the reference's public LBM::fluid array
+//     (the cavity) or the reference's own setup functions (the cylinder),
+//   - runs the reference's own Init / Collision / Streaming / MacroProp and
+//     IBLBM in the order of main.cpp:195-221,
+//   - times only the step loop (wall clock), and
+//   - dumps rho, u (and F, Cl, Cd for the IBM case) as raw doubles,
+//     x fastest, ghost layers included.
+#include "LBM.h"
+
+#include <omp.h>
+
+#include <cstdio>
+#include <cstdlib>
+#include <vector>
+
+static void dump_field(LBM &lb, FILE *fp, int which) {
+    int NX = Nx + 2, NY = Ny + 2, NZ = Nz + 2;
+    std::vector<double> buf((size_t)NX * NY * NZ);
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++) {
+                LATTICE &c = lb.fluid[i][j][k];
+                double v = 0;
+                switch (which) {
+                case 0: v = c.density; break;
+                case 1: v = c.ux; break;
+                case 2: v = c.uy; break;
+                case 3: v = c.uz; break;
+                case 4: v = c.F[0]; break;
+                case 5: v = c.F[1]; break;
+                case 6: v = c.F[2]; break;
+                }
+                buf[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = v;
+            }
+    fwrite(buf.data(), sizeof(double), buf.size(), fp);
+}
+
+int main(int argc, char **argv) {
+    if (argc < 3) {
+        fprintf(stderr, "usage: %s steps out.bin [lid_velocity]\n", argv[0]);
+        return 2;
+    }
+    int steps = atoi(argv[1]);
+    const char *out = argv[2];
+#if defined REF_CAVITY
+    double lid = argc > 3 ? atof(argv[3]) : 0.05;
+    LBM lb(Nx, Ny, Nz, tau);
+    for (int i = 0; i <= Nx + 1; i++)
+        for (int j = 0; j <= Ny + 1; j++)
+            for (int k = 0; k <= Nz + 1; k++) {
+                bool ghost = i == 0 || i == Nx + 1 || j == 0 || j == Ny + 1 || k == 0 || k == Nz + 1;
+                lb.fluid[i][j][k].type = ghost ? TYPE_S : TYPE_F;
+                // moving lid: the whole ghost plane j = Ny+1 (Couette "top wall"
+                // convention, lbm.cpp:1548-1551)
+                if (j == Ny + 1) lb.fluid[i][j][k].ux = lid;
+            }
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int s = 1; s <= steps; s++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+    fclose(fp);
+    double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
+    printf("{\"case\": \"cavity\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
+           Nx, steps, t1 - t0, mlups, omp_get_max_threads());
+#elif defined REF_CYLINDER
+    LBM lb = main_setup_Cylinder_IBM();
+    std::vector<MARKER> marker(number_nodes);
+    Generate_Cylinder_Marker(marker);
+    // arc-length weights as main.cpp:123-131 computes them
+    std::vector<double> ds;
+    for (int i = 0; i < number_nodes; i++) {
+        int j = (i + 1) % number_nodes;
+        double ddx = marker[i].x - marker[j].x, ddy = marker[i].y - marker[j].y, ddz = marker[i].z - marker[j].z;
+        ds.push_back(sqrt(pow(ddx, 2) + pow(ddy, 2) + pow(ddz, 2)));
+    }
+    double V_CM[3] = {0, 0, 0};
+    std::vector<double> CL, CD;
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int step = 1; step <= steps; step++) {
+        IBLBM(lb, marker, ds, CL, CD, V_CM, step * dt);
+        lb.Collision();
+        lb.Streaming();
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 7; w++) dump_field(lb, fp, w);
+    fwrite(CL.data(), sizeof(double), CL.size(), fp);
+    fwrite(CD.data(), sizeof(double), CD.size(), fp);
+    for (int n = 0; n < number_nodes; n++) {
+        double v[8] = {marker[n].x, marker[n].y, marker[n].z, marker[n].normal[0], marker[n].normal[1],
+                       marker[n].normal[2], ds[n], 0.0};
+        fwrite(v, sizeof(double), 8, fp);
+    }
+    fclose(fp);
+    double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
+    printf("{\"case\": \"cylinder\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
+           Nx, steps, t1 - t0, mlups, omp_get_max_threads());
+#endif
+    return 0;
+}
