@@ -1,0 +1,320 @@
+#!/usr/bin/env python3
+"""Benchmark: MLUPS of the LBM time step on one GB300, with the HBM roofline.
+
+Workload (the single-GPU headline case): D3Q19 BGK channel 256x128x128,
+equilibrium inlet u = (0.05, 0, 0), zero-gradient outlet, bounce-back y/z
+walls, a fixed sphere of diameter 20 at (64, 64, 64) carrying 1257 Fibonacci
+markers, implicit direct-forcing IBM (m_max = 5, 4-point Peskin delta, Guo
+forcing), tau = 0.53 (Re = 100).  Synthetic: the state is initialised to the
+inflow equilibrium; there is no dataset.
+
+One bench "step" = 10 lattice time steps (the reference's output cadence,
+Nt = 10 in LBM.h).  `value` is MLUPS = interior cells x time steps / device
+seconds for the FP16-storage form (shifted populations, FP32 arithmetic),
+timed with CUDA events on the solver's stream; the plain FP32 form is
+reported beside it.  `e2e` is the same metric through the C ABI with host
+buffers: per bench step the marker set is uploaded from pinned host memory
+and the rho/u fields (FP32) plus the force history are read back.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+--impl reference times the CPU implementation of the path on the host cores
+(the FP64 restatement: the reference itself has no 3D IBM, so it cannot run
+this workload) and prints the same JSON line with "impl": "reference".
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX, NY, NZ = 256, 128, 128
+TAU = 0.53
+U_IN = 0.05
+DIAM = 20.0
+CENTER = (64.0, 64.0, 64.0)
+N_MARKERS = 1257
+M_MAX = 5
+LBM_PER_STEP = 10
+BYTES_PER_CELL = {"f32": 152, "f16": 76, "bf16": 76}
+METRIC = "MLUPS (D3Q19 IBM sphere channel 256x128x128, FP16-store)"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_summary():
+    p = os.path.join(ROOT, "profiles", "k_step_traffic.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            return json.load(f)
+    return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", "clocks_bench.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        if not self.proc or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            p = [x.strip() for x in line.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                smax.append(float(p[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, p[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        loaded = [s for s in sm if s > 0.5 * max(sm)] or sm
+        return {"sm_mhz": statistics.median(loaded), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def make_solver(pkg, orc, storage: str):
+    s = pkg.Solver(pkg.channel_config(NX, NY, NZ, TAU, u_in=U_IN, storage=storage))
+    s.init()
+    mk = orc.fibonacci_sphere(N_MARKERS, DIAM, CENTER)
+    xyz = np.ascontiguousarray(np.stack([mk["x"], mk["y"], mk["z"]]))
+    ds = np.ascontiguousarray(mk["ds"])
+    s.set_markers(xyz, ds, DIAM / 2.0, CENTER, m_max=M_MAX)
+    return s, xyz, ds
+
+
+def kernel_launches_per_lbm_step():
+    return 1 + 2 * M_MAX + 2  # fused collide-stream, m_max x (interp, spread), band collide, finish
+
+
+def run_gpu(args):
+    import __graft_entry__ as ge
+
+    rank, world, local = dist_env()
+    pkg = ge.load_package()
+    import oracle as orc
+
+    pkg.load()
+    ncell = NX * NY * NZ
+    results = {}
+    peak, peak_kind = measured_peak()
+    clocks = ClockSampler(local)
+    with clocks:
+        for storage in ("f32", "f16"):
+            s, xyz, ds = make_solver(pkg, orc, storage)
+            for _ in range(args.warmup):
+                s.step(LBM_PER_STEP)
+            s.sync()
+            nsteps = args.steps * LBM_PER_STEP
+            total_ms, fused_ms = s.step_profiled(nsteps)
+            st = s.status()
+            mlups = ncell * nsteps / (total_ms * 1e-3) / 1e6
+            fused_avg_ms = fused_ms / nsteps
+            achieved = BYTES_PER_CELL[storage] * ncell / (fused_avg_ms * 1e-3) / 1e9
+            results[storage] = dict(mlups=mlups, ms_per_step=total_ms / args.steps, fused_ms=fused_avg_ms,
+                                    achieved_gbs=achieved, status=st)
+            s.close()
+    # end-to-end through the C ABI with host buffers (FP16 form)
+    import ctypes as C
+
+    s, xyz, ds = make_solver(pkg, orc, "f16")
+    L = pkg.load()
+    nf = 4
+    host = C.c_void_p()
+    pkg.check(L.lbmgpu_host_alloc(nf * ncell * 4, C.byref(host)))
+    xyz_p = C.c_void_p()
+    pkg.check(L.lbmgpu_host_alloc(xyz.nbytes + ds.nbytes, C.byref(xyz_p)))
+    hx = np.ctypeslib.as_array(C.cast(xyz_p, C.POINTER(C.c_double)), shape=(xyz.size + ds.size,))
+    hx[: xyz.size] = xyz.ravel()
+    hx[xyz.size:] = ds
+    ic = pkg.IbmConfig()
+    ic.n_markers, ic.m_max, ic.radius = N_MARKERS, M_MAX, DIAM / 2.0
+    for a in range(3):
+        ic.center[a] = CENTER[a]
+    fbuf = np.zeros((LBM_PER_STEP, 8))
+    nout = C.c_int()
+    dp = C.POINTER(C.c_double)
+
+    def e2e_step():
+        pkg.check(L.lbmgpu_set_markers(s.h, C.byref(ic), C.cast(xyz_p, dp),
+                                       C.cast(xyz_p.value + xyz.nbytes, dp), None))
+        pkg.check(L.lbmgpu_step(s.h, LBM_PER_STEP))
+        pkg.check(L.lbmgpu_download_all_f32(s.h, host))
+        pkg.check(L.lbmgpu_get_forces(s.h, fbuf.ctypes.data_as(dp), LBM_PER_STEP, C.byref(nout)))
+
+    for _ in range(args.warmup):
+        e2e_step()
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    s.sync()
+    e2e_s = time.perf_counter() - t0
+    e2e_mlups = ncell * args.steps * LBM_PER_STEP / e2e_s / 1e6
+    h2d = xyz.nbytes + ds.nbytes + 3 * N_MARKERS * 4
+    d2h = nf * ncell * 4 + LBM_PER_STEP * 8 * 8
+    L.lbmgpu_host_free(host)
+    L.lbmgpu_host_free(xyz_p)
+    s.close()
+    return results, dict(value=e2e_mlups, h2d=h2d, d2h=d2h), clocks.summary(), (peak, peak_kind)
+
+
+def cpu_baseline_sample(threads: int | None = None):
+    """FP64 restatement (oracle) on the same workload, a bounded sample of
+    lattice steps, all host threads."""
+    import oracle as orc
+
+    orc.build()
+    if threads:
+        os.environ["OMP_NUM_THREADS"] = str(threads)
+    t0 = time.perf_counter()
+    lat = None
+    lat, mk, hist, body = orc.sphere_case(NX, NY, NZ, TAU, DIAM, CENTER, N_MARKERS, M_MAX, U_IN, steps=1)
+    setup = time.perf_counter() - t0
+    # time further steps on the same lattice
+    R = DIAM / 2.0
+    lo, hi = orc.sphere_box(CENTER, DIAM, lat)
+    op = orc.ibm_opts(lo, hi, M_MAX)
+    n = 0
+    t1 = time.perf_counter()
+    while n < 3 or (time.perf_counter() - t1 < 12.0 and n < 40):
+        lat.step_ibm(mk, op, CENTER)
+        n += 1
+    dt_s = time.perf_counter() - t1
+    cores = os.cpu_count() or 1
+    return dict(value=NX * NY * NZ * n / dt_s / 1e6, unit="MLUPS", cores=cores, kind="port",
+                sample="%d lattice steps of the 256x128x128 IBM sphere channel, FP64 oracle (OpenMP, %d threads); "
+                       "the reference has no 3D IBM, so its restatement stands in" % (n, cores),
+                setup_s=setup)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = dist_env()
+    if args.warmup < 3:
+        args.warmup = 3
+    cfg = {"workload": "ibm_sphere_channel_256x128x128", "grid": [NX, NY, NZ], "tau": TAU, "u_in": U_IN,
+           "sphere_diameter": DIAM, "markers": N_MARKERS, "m_max": M_MAX, "lbm_steps_per_bench_step": LBM_PER_STEP,
+           "storage": "f16 (shifted populations)", "l2": "inputs larger than L2 (319 MB FP16, 638 MB FP32 A/B)",
+           "replicas": world}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        cb = cpu_baseline_sample()
+        line = {"metric": METRIC, "value": cb["value"], "unit": "MLUPS", "n_gpus": args.gpus, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": NX * NY * NZ * LBM_PER_STEP / (cb["value"] * 1e6) * 1e3,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic", "config": cfg, "impl": "reference",
+                "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")},
+                "e2e": {"value": cb["value"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    res, e2e, clk, (peak, peak_kind) = run_gpu(args)
+    vals = {k: v["mlups"] for k, v in res.items()}
+    ms = res["f16"]["ms_per_step"]
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    if rank != 0:
+        return
+    value = NX * NY * NZ * LBM_PER_STEP / (ms * 1e-3) / 1e6 * world
+    tr = traffic_summary()
+    r16 = res["f16"]
+    roof = {"bound": "hbm", "kernel": "k_step (fused collide-stream)", "achieved": r16["achieved_gbs"],
+            "peak": peak, "unit": "GB/s", "frac": r16["achieved_gbs"] / peak, "peak_kind": peak_kind,
+            "algorithmic_bytes_per_cell": BYTES_PER_CELL["f16"], "fused_ms_per_launch": r16["fused_ms"],
+            "traffic": tr.get("f16", {}).get("bytes_per_launch")}
+    line = {"metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": cfg,
+            "roofline": roof,
+            "fp32_plain": {"value": vals["f32"], "unit": "MLUPS", "achieved_gbs": res["f32"]["achieved_gbs"],
+                           "frac": res["f32"]["achieved_gbs"] / peak, "fused_ms_per_launch": res["f32"]["fused_ms"],
+                           "traffic": tr.get("f32", {}).get("bytes_per_launch")},
+            "fp16_over_fp32": vals["f16"] / vals["f32"],
+            "e2e": {"value": e2e["value"], "unit": "MLUPS", "h2d_bytes_per_step": e2e["h2d"],
+                    "d2h_bytes_per_step": e2e["d2h"]},
+            "gpu_launches": kernel_launches_per_lbm_step() * LBM_PER_STEP * args.steps,
+            "clocks": clk, "status": {k: v["status"] for k, v in res.items()}}
+    if not args.no_cpu_baseline:
+        cb = cpu_baseline_sample()
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,180 @@
+/*
+ * lbmgpu.h -- C ABI of the GB300 LBM time-step library (liblbmgpu.so).
+ *
+ * Plain C types only (no CUDA or torch types).  The entry points replace the
+ * hot path of the reference's LBM class and IBM driver
+ * (DestinyFlow01/Lattice-Boltzmann-Method---Graduate-FSI-):
+ *
+ *   reference                                   here
+ *   LBM::LBM(Nx,Ny,Nz,tau)        LBM.h:630    lbmgpu_config_from_types + lbmgpu_create
+ *   fluid[i][j][k].type / ux..    LBM.h:558-597 (geometry)  lbmgpu_config_from_types
+ *   LBM::Init                     lbm.cpp:31   lbmgpu_init / lbmgpu_init_fields
+ *   LBM::Collision + Streaming    lbm.cpp:60,182  lbmgpu_step (fused)
+ *   LBM::MacroProp                lbm.cpp:657  fused into lbmgpu_step; read back
+ *                                              with lbmgpu_download
+ *   IBLBM (markers, ds, Cl, Cd)   lbm.cpp:1135 lbmgpu_set_markers (+ forcing inside
+ *                                              lbmgpu_step), lbmgpu_get_forces
+ *   terminate() on bad state      lbm.cpp:116,774  lbmgpu_status (never aborts)
+ *
+ * Conventions.  Interior cells only on the device; host arrays passed to or
+ * returned by the ABI are x-fastest: index i + nx*(j + ny*k) for interior
+ * cell (i+1, j+1, k+1) of the reference's fluid[Nx+2][Ny+2][Nz+2] array.
+ * Geometry arrays given to lbmgpu_config_from_types include the ghost layers:
+ * index i + (nx+2)*(j + (ny+2)*k) for fluid[i][j][k].
+ *
+ * Every call returns an lbm_status; lbmgpu_last_error() gives a message for
+ * the calling thread.  A handle owns one CUDA stream; calls on one handle are
+ * not re-entrant, distinct handles are independent.
+ */
+#ifndef LBMGPU_H
+#define LBMGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum lbm_status {
+    LBM_OK = 0,
+    LBM_ERR_INVALID = 1,     /* bad argument or configuration */
+    LBM_ERR_CUDA = 2,        /* CUDA runtime error */
+    LBM_ERR_NOMEM = 3,       /* device or host allocation failed */
+    LBM_ERR_DIVERGED = 4,    /* device status word reports an invalid state */
+    LBM_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
+    LBM_ERR_STATE = 6,       /* call out of order (e.g. step before init) */
+    LBM_ERR_UNSUPPORTED = 7  /* geometry this build does not handle */
+} lbm_status;
+
+/* Population storage formats.  F16/BF16 store f - w (shifted) and compute in FP32. */
+enum { LBM_STORE_F32 = 0, LBM_STORE_F16 = 1, LBM_STORE_BF16 = 2 };
+
+/* Kind of one box face (its ghost layer).  Reference cell types (LBM.h:505-515):
+ * TYPE_S -> WALL, TYPE_IN -> INLET, TYPE_OUT -> OUTLET_EQ (populations from the
+ * ghost keep the initial equilibrium, as in the reference), TYPE_F ghost layers
+ * on both faces of an axis -> PERIODIC.  OUTLET_ZG (zero-gradient) is new. */
+enum { LBM_FACE_WALL = 0, LBM_FACE_INLET = 1, LBM_FACE_OUTLET_EQ = 2, LBM_FACE_OUTLET_ZG = 3, LBM_FACE_PERIODIC = 4 };
+
+/* Thermal condition on a WALL face. */
+enum { LBM_TWALL_ADIABATIC = 0, LBM_TWALL_DIRICHLET = 1 };
+
+/* Fields for lbmgpu_download*. */
+enum { LBM_FIELD_RHO = 0, LBM_FIELD_UX = 1, LBM_FIELD_UY = 2, LBM_FIELD_UZ = 3, LBM_FIELD_T = 4 };
+
+/* Device status bits (lbmgpu_status). */
+enum {
+    LBM_STATUS_RHO_RANGE = 1,   /* rho outside (0, 100) or NaN: lbm.cpp:772-775 */
+    LBM_STATUS_BAND_EDGE = 2,   /* an IBM stencil reached outside the band/interior */
+    LBM_STATUS_NONFINITE_FORCE = 4
+};
+
+typedef struct lbm_face {
+    int kind;          /* LBM_FACE_* */
+    int thermal_kind;  /* LBM_TWALL_* for walls */
+    double rho;        /* inlet/outlet-equilibrium density */
+    double u[3];       /* wall velocity, or inlet/outlet-equilibrium velocity */
+    double T;          /* inlet temperature or Dirichlet wall temperature */
+} lbm_face;
+
+typedef struct lbm_config {
+    int nx, ny, nz;       /* interior cells (Nx, Ny, Nz) */
+    double tau;           /* BGK relaxation time */
+    int storage;          /* LBM_STORE_* */
+    lbm_face faces[6];    /* x-, x+, y-, y+, z-, z+ */
+    double rho0;          /* uniform initial density (lbmgpu_init) */
+    double u0[3];         /* uniform initial velocity */
+    double body_force[3]; /* uniform body force (e.g. -dp/dx, lbm.cpp:800-801) */
+    int thermal;          /* 1: D3Q7 temperature population */
+    double tau_g;         /* thermal relaxation time, 0.5 + alpha / (1/4) */
+    double T_init;        /* uniform initial temperature */
+    double T_ref;         /* Boussinesq reference temperature T0 */
+    double gbeta[3];      /* Boussinesq: F += gbeta * (T - T0)  (lbm.cpp:804-805) */
+    int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
+    int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
+} lbm_config;
+
+typedef struct lbm_ibm_config {
+    int n_markers;
+    int m_max;            /* implicit forcing iterations (lbm.cpp:1311) */
+    int literal_sign;     /* 1: force -Fm but velocity +Fm/2rho (lbm.cpp:1347-1352) */
+    int free_body;        /* 0: fixed/prescribed, 1: FP64 Newton-Euler (Kempe-Froehlich internal fluid) */
+    int thermal;          /* 1: also force the temperature to T_body */
+    double radius;        /* body radius (band size and rigid body) */
+    double center[3];     /* body centre, reference node coordinates */
+    double density_ratio; /* rho_s / rho_f */
+    double volume;        /* V_s */
+    double inertia;       /* I_p = 2/5 rho_s V_s R^2 for a sphere */
+    double gravity[3];
+    double velocity[3];   /* initial body velocity */
+    double T_body;        /* marker temperature for the thermal IBM */
+    int free_dofs;        /* free body: bits 0-2 translation x,y,z, bits 3-5 rotation; 0 = all six */
+} lbm_ibm_config;
+
+typedef struct lbm_handle lbm_handle;
+
+/* Derive a configuration from the reference's per-cell description
+ * (fluid[i][j][k].type and the ghost velocities/densities/temperatures),
+ * arrays of (nx+2)(ny+2)(nz+2) entries, x fastest; u/rho/T may be NULL.
+ * Fails with LBM_ERR_UNSUPPORTED if solids lie inside the domain or a face
+ * is not uniform.  Periodic axes (TYPE_F ghost layers) are mapped to an
+ * interior of N+2 cells, as the reference wraps over N+2 (lbm.cpp:187-189). */
+lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const uint8_t *types, const double *rho,
+                                    const double *ux, const double *uy, const double *uz, const double *T,
+                                    lbm_config *out);
+
+lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out);
+lbm_status lbmgpu_destroy(lbm_handle *h);
+
+/* LBM::Init (lbm.cpp:31-57): f = feq(rho0, u0) (third order), g = geq(T_init). */
+lbm_status lbmgpu_init(lbm_handle *h);
+/* LBM::Init from per-cell fields (interior, x fastest); T may be NULL. */
+lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const double *ux, const double *uy, const double *uz,
+                              const double *T);
+
+/* IBLBM set-up (lbm.cpp:1135-1167): markers xyz ([3][n], reference node
+ * coordinates), weights ds ([n]), desired velocities udes ([3][n], NULL =
+ * the body velocity). */
+lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *ds,
+                              const double *udes);
+
+/* Advance n reference iterations (IBLBM -> Collision -> Streaming, or
+ * Collision -> Streaming -> MacroProp).  Asynchronous on the handle's stream. */
+lbm_status lbmgpu_step(lbm_handle *h, int nsteps);
+
+/* Same, with CUDA events on the handle's stream: total device time of the
+ * n steps and the summed device time of the fused collide-stream kernel. */
+lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms);
+
+/* MacroProp moments of the current state (rho, u = (sum f c + F/2)/rho, T),
+ * interior cells, x fastest. */
+lbm_status lbmgpu_download(lbm_handle *h, int field, double *host);
+lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host);
+/* All of rho, ux, uy, uz (and T if thermal) in one export, FP32, [field][cells]. */
+lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host);
+
+/* IBM force history, oldest first: per step {Fx, Fy, Fz, Tx, Ty, Tz, heat,
+ * step}, where F = sum over forcing iterations of -F_m ds_m (the reference's
+ * Drag/Lift accumulators, lbm.cpp:1322-1323).  *n_out = entries written. */
+lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+/* Rigid body: {xc[3], v[3], omega[3]}. */
+lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]);
+/* Marker positions [3][n]. */
+lbm_status lbmgpu_get_markers(lbm_handle *h, double *xyz);
+
+lbm_status lbmgpu_status(lbm_handle *h, uint32_t *flags);
+lbm_status lbmgpu_sync(lbm_handle *h);
+lbm_status lbmgpu_steps_done(lbm_handle *h, long long *steps);
+lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes);
+
+/* Page-locked host buffers for fast host<->device copies. */
+lbm_status lbmgpu_host_alloc(size_t bytes, void **ptr);
+lbm_status lbmgpu_host_free(void *ptr);
+
+const char *lbmgpu_last_error(void);
+int lbmgpu_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* LBMGPU_H */

@@ -1,0 +1,292 @@
+"""Python mirror of the liblbmgpu C ABI (include/lbmgpu.h), for tests and the bench.
+
+The product is the C-ABI shared library ``liblbmgpu.so`` built from
+``csrc/`` (CUDA for sm_103a) and its C++ host facade ``csrc/facade``; this
+module only binds the ABI with ctypes.  There is no CPU fallback: if the
+library is missing or no GPU is visible, the solver calls fail loudly.
+
+Names follow the reference's LBM class (DestinyFlow01/
+Lattice-Boltzmann-Method---Graduate-FSI-, LBM.h:620-664): ``Solver.init``
+is LBM::Init, ``Solver.step`` is one Collision + Streaming (+ MacroProp, or
+IBLBM first when markers are set), ``Solver.download`` reads the MacroProp
+moments.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liblbmgpu.so")
+
+STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
+STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
+FACE_WALL, FACE_INLET, FACE_OUTLET_EQ, FACE_OUTLET_ZG, FACE_PERIODIC = 0, 1, 2, 3, 4
+TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
+FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
+STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE = 1, 2, 4
+
+# Every symbol include/lbmgpu.h declares.
+ABI_SYMBOLS = [
+    "lbmgpu_config_from_types", "lbmgpu_create", "lbmgpu_destroy", "lbmgpu_init", "lbmgpu_init_fields",
+    "lbmgpu_set_markers", "lbmgpu_step", "lbmgpu_step_profiled", "lbmgpu_download", "lbmgpu_download_f32",
+    "lbmgpu_download_all_f32", "lbmgpu_get_forces", "lbmgpu_get_body", "lbmgpu_get_markers", "lbmgpu_status",
+    "lbmgpu_sync", "lbmgpu_steps_done", "lbmgpu_device_bytes", "lbmgpu_host_alloc", "lbmgpu_host_free",
+    "lbmgpu_last_error", "lbmgpu_abi_version",
+]
+
+
+class Face(C.Structure):
+    _fields_ = [("kind", C.c_int), ("thermal_kind", C.c_int), ("rho", C.c_double), ("u", C.c_double * 3),
+                ("T", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("tau", C.c_double), ("storage", C.c_int),
+                ("faces", Face * 6), ("rho0", C.c_double), ("u0", C.c_double * 3),
+                ("body_force", C.c_double * 3), ("thermal", C.c_int), ("tau_g", C.c_double),
+                ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
+                ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int)]
+
+
+class IbmConfig(C.Structure):
+    _fields_ = [("n_markers", C.c_int), ("m_max", C.c_int), ("literal_sign", C.c_int), ("free_body", C.c_int),
+                ("thermal", C.c_int), ("radius", C.c_double), ("center", C.c_double * 3),
+                ("density_ratio", C.c_double), ("volume", C.c_double), ("inertia", C.c_double),
+                ("gravity", C.c_double * 3), ("velocity", C.c_double * 3), ("T_body", C.c_double),
+                ("free_dofs", C.c_int)]
+
+
+class LbmError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__("lbmgpu status %d: %s" % (status, msg))
+        self.status = status
+
+
+_lib = None
+
+
+def load(path: str | None = None):
+    """Load liblbmgpu.so (raises if it was not built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise OSError("liblbmgpu.so not built at %s (run __graft_entry__.build())" % p)
+    L = C.CDLL(p)
+    vp, i, d = C.c_void_p, C.c_int, C.c_double
+    dp = C.POINTER(C.c_double)
+    L.lbmgpu_last_error.restype = C.c_char_p
+    L.lbmgpu_abi_version.restype = i
+    L.lbmgpu_config_from_types.argtypes = [i, i, i, d, C.POINTER(C.c_uint8), dp, dp, dp, dp, dp, C.POINTER(Config)]
+    L.lbmgpu_create.argtypes = [C.POINTER(Config), C.POINTER(vp)]
+    L.lbmgpu_destroy.argtypes = [vp]
+    L.lbmgpu_init.argtypes = [vp]
+    L.lbmgpu_init_fields.argtypes = [vp, dp, dp, dp, dp, dp]
+    L.lbmgpu_set_markers.argtypes = [vp, C.POINTER(IbmConfig), dp, dp, dp]
+    L.lbmgpu_step.argtypes = [vp, i]
+    L.lbmgpu_step_profiled.argtypes = [vp, i, dp, dp]
+    L.lbmgpu_download.argtypes = [vp, i, dp]
+    L.lbmgpu_download_f32.argtypes = [vp, i, C.POINTER(C.c_float)]
+    L.lbmgpu_download_all_f32.argtypes = [vp, vp]
+    L.lbmgpu_get_forces.argtypes = [vp, dp, i, C.POINTER(i)]
+    L.lbmgpu_get_body.argtypes = [vp, dp]
+    L.lbmgpu_get_markers.argtypes = [vp, dp]
+    L.lbmgpu_status.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.lbmgpu_sync.argtypes = [vp]
+    L.lbmgpu_steps_done.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.lbmgpu_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.lbmgpu_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
+    L.lbmgpu_host_free.argtypes = [vp]
+    for nm in ABI_SYMBOLS:
+        fn = getattr(L, nm)
+        if fn.restype is None and nm not in ("lbmgpu_last_error", "lbmgpu_abi_version"):
+            fn.restype = i
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        raise LbmError(status, load().lbmgpu_last_error().decode())
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0.0, 0.0), body=(0.0, 0.0, 0.0),
+                thermal=False, tau_g=0.0, T_init=0.0, T_ref=0.0, gbeta=(0.0, 0.0, 0.0), block=(0, 0),
+                graph_steps=0) -> Config:
+    c = Config()
+    c.nx, c.ny, c.nz, c.tau = nx, ny, nz, tau
+    c.storage = STORAGE[storage] if isinstance(storage, str) else storage
+    for f in range(6):
+        spec = (faces or {}).get(f, {"kind": FACE_WALL})
+        c.faces[f].kind = spec.get("kind", FACE_WALL)
+        c.faces[f].thermal_kind = spec.get("thermal_kind", TWALL_ADIABATIC)
+        c.faces[f].rho = spec.get("rho", 1.0)
+        for a in range(3):
+            c.faces[f].u[a] = spec.get("u", (0.0, 0.0, 0.0))[a]
+        c.faces[f].T = spec.get("T", 0.0)
+    c.rho0 = rho0
+    for a in range(3):
+        c.u0[a] = u0[a]
+        c.body_force[a] = body[a]
+        c.gbeta[a] = gbeta[a]
+    c.thermal = 1 if thermal else 0
+    c.tau_g, c.T_init, c.T_ref = tau_g, T_init, T_ref
+    c.block_x, c.block_y = block
+    c.graph_steps = graph_steps
+    return c
+
+
+def cavity_config(n, tau=0.8, lid=0.05, storage="f32", ny=None, nz=None, **kw) -> Config:
+    """Lid-driven cavity: walls on every face, the y+ face moving with (lid, 0, 0)."""
+    faces = {f: {"kind": FACE_WALL} for f in range(6)}
+    faces[3] = {"kind": FACE_WALL, "u": (lid, 0.0, 0.0)}
+    return make_config(n, ny or n, nz or n, tau, storage, faces, **kw)
+
+
+def channel_config(nx, ny, nz, tau, u_in=0.05, storage="f32", outlet=FACE_OUTLET_ZG, thermal=False, T_in=0.0,
+                   **kw) -> Config:
+    """Channel: equilibrium inlet at x-, outlet at x+, bounce-back walls on y and z."""
+    faces = {0: {"kind": FACE_INLET, "u": (u_in, 0.0, 0.0), "rho": 1.0, "T": T_in},
+             1: {"kind": outlet, "u": (u_in, 0.0, 0.0), "rho": 1.0, "T": T_in}}
+    for f in (2, 3, 4, 5):
+        faces[f] = {"kind": FACE_WALL}
+    return make_config(nx, ny, nz, tau, storage, faces, u0=(u_in, 0.0, 0.0), thermal=thermal, T_init=T_in, **kw)
+
+
+class Solver:
+    """One device-resident solve (an lbm_handle)."""
+
+    def __init__(self, cfg: Config):
+        self.L = load()
+        self.cfg = cfg
+        self.h = C.c_void_p()
+        check(self.L.lbmgpu_create(C.byref(cfg), C.byref(self.h)))
+        self.shape = (cfg.nz, cfg.ny, cfg.nx)
+        self.ncell = cfg.nx * cfg.ny * cfg.nz
+        self.n_markers = 0
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.lbmgpu_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self, fields=None):
+        if fields is None:
+            check(self.L.lbmgpu_init(self.h))
+        else:
+            arrs = [np.ascontiguousarray(a, dtype=np.float64).ravel() for a in fields]
+            T = _dp(arrs[4]) if len(arrs) > 4 and arrs[4] is not None else None
+            check(self.L.lbmgpu_init_fields(self.h, _dp(arrs[0]), _dp(arrs[1]), _dp(arrs[2]), _dp(arrs[3]), T))
+
+    def set_markers(self, xyz, ds, radius, center, m_max=5, literal_sign=False, free_body=False, udes=None,
+                    density_ratio=0.0, volume=0.0, inertia=0.0, gravity=(0, 0, 0), velocity=(0, 0, 0),
+                    thermal=False, T_body=0.0, free_dofs=0):
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64)
+        ds = np.ascontiguousarray(ds, dtype=np.float64)
+        n = ds.shape[0]
+        ic = IbmConfig()
+        ic.n_markers, ic.m_max, ic.literal_sign, ic.free_body = n, m_max, int(literal_sign), int(free_body)
+        ic.thermal = int(thermal)
+        ic.radius = radius
+        for a in range(3):
+            ic.center[a] = center[a]
+            ic.gravity[a] = gravity[a]
+            ic.velocity[a] = velocity[a]
+        ic.density_ratio, ic.volume, ic.inertia, ic.T_body = density_ratio, volume, inertia, T_body
+        ic.free_dofs = free_dofs
+        ud = None
+        if udes is not None:
+            udes = np.ascontiguousarray(udes, dtype=np.float64)
+            ud = _dp(udes)
+        check(self.L.lbmgpu_set_markers(self.h, C.byref(ic), _dp(xyz), _dp(ds), ud))
+        self.n_markers = n
+
+    def step(self, n: int = 1):
+        check(self.L.lbmgpu_step(self.h, int(n)))
+
+    def step_profiled(self, n: int):
+        tot, fused = C.c_double(), C.c_double()
+        check(self.L.lbmgpu_step_profiled(self.h, int(n), C.byref(tot), C.byref(fused)))
+        return tot.value, fused.value
+
+    def sync(self):
+        check(self.L.lbmgpu_sync(self.h))
+
+    def download(self, field: int) -> np.ndarray:
+        out = np.empty(self.ncell, dtype=np.float64)
+        check(self.L.lbmgpu_download(self.h, field, _dp(out)))
+        return out.reshape(self.shape)
+
+    def download_f32(self, field: int) -> np.ndarray:
+        out = np.empty(self.ncell, dtype=np.float32)
+        check(self.L.lbmgpu_download_f32(self.h, field, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return out.reshape(self.shape)
+
+    def moments(self) -> dict:
+        nf = 5 if self.cfg.thermal else 4
+        out = np.empty(nf * self.ncell, dtype=np.float32)
+        check(self.L.lbmgpu_download_all_f32(self.h, out.ctypes.data_as(C.c_void_p)))
+        out = out.reshape((nf,) + self.shape)
+        d = {"rho": out[0], "ux": out[1], "uy": out[2], "uz": out[3]}
+        if nf == 5:
+            d["T"] = out[4]
+        return d
+
+    def forces(self, max_steps: int = 1 << 16) -> np.ndarray:
+        out = np.zeros((max_steps, 8))
+        n = C.c_int()
+        check(self.L.lbmgpu_get_forces(self.h, _dp(out), max_steps, C.byref(n)))
+        return out[: n.value]
+
+    def body(self) -> np.ndarray:
+        out = np.zeros(9)
+        check(self.L.lbmgpu_get_body(self.h, _dp(out)))
+        return out
+
+    def markers(self) -> np.ndarray:
+        out = np.zeros(3 * self.n_markers)
+        check(self.L.lbmgpu_get_markers(self.h, _dp(out)))
+        return out.reshape(3, self.n_markers)
+
+    def status(self) -> int:
+        v = C.c_uint32()
+        st = self.L.lbmgpu_status(self.h, C.byref(v))
+        if st not in (0, 4):
+            check(st)
+        return v.value
+
+    def steps_done(self) -> int:
+        v = C.c_longlong()
+        check(self.L.lbmgpu_steps_done(self.h, C.byref(v)))
+        return v.value
+
+    def device_bytes(self) -> int:
+        v = C.c_size_t()
+        check(self.L.lbmgpu_device_bytes(self.h, C.byref(v)))
+        return v.value
+
+
+def config_from_types(nx, ny, nz, tau, types, rho=None, ux=None, uy=None, uz=None, T=None) -> Config:
+    """Reference-style geometry (fluid[..].type incl. ghosts, x fastest) -> Config."""
+    L = load()
+    t = np.ascontiguousarray(types, dtype=np.uint8).ravel()
+    arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (rho, ux, uy, uz, T)]
+    ptrs = [None if a is None else _dp(a) for a in arrs]
+    cfg = Config()
+    check(L.lbmgpu_config_from_types(nx, ny, nz, tau, t.ctypes.data_as(C.POINTER(C.c_uint8)), *ptrs,
+                                     C.byref(cfg)))
+    return cfg

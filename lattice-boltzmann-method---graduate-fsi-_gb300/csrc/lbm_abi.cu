@@ -1,0 +1,738 @@
+// lbm_abi.cu -- the extern "C" layer (include/lbmgpu.h): handles, device
+// memory, boundary-class tables, step sequencing and CUDA-graph replay.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbmgpu.h"
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+using namespace lbmk;
+
+static thread_local std::string g_err;
+
+static lbm_status fail(lbm_status s, const std::string &msg) {
+    g_err = msg;
+    return s;
+}
+
+#define CUDA_TRY(expr)                                                                                    \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+struct lbm_handle {
+    lbm_config cfg;
+    StepParams P;
+    cudaStream_t s = nullptr;
+    size_t esize = 4;
+    void *f[2] = {nullptr, nullptr};
+    void *g[2] = {nullptr, nullptr};
+    int cur = 0;
+    float *mom = nullptr;
+    float *band = nullptr;
+    DevState *ds = nullptr;
+    bool inited = false;
+    long long steps = 0;
+    // IBM
+    bool ibm = false;
+    lbm_ibm_config icfg;
+    MarkerDev mk;
+    BodyParams bp;
+    double *hist = nullptr;
+    long long hist_cap = 1 << 16;
+    // graphs
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int gsteps = 16;
+    int tx = 128, ty = 2;
+    size_t dev_bytes = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> evpool;
+};
+
+// ---------------------------------------------------------------------------
+// Boundary classes
+// ---------------------------------------------------------------------------
+static double feq3_host(double rho, const double u[3], int l) {
+    const double cu = cx(l) * u[0] + cy(l) * u[1] + cz(l) * u[2];
+    const double usq = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const double cs2 = 1.0 / 3.0;
+    return rho * wd(l) *
+           (1 + cu / cs2 + cu * cu / (2 * cs2 * cs2) - usq / (2 * cs2) + cu * cu * cu / (6 * cs2 * cs2 * cs2) -
+            cu * usq / (2 * cs2 * cs2));
+}
+
+static int face_priority(int kind) {
+    switch (kind) {
+    case LBM_FACE_WALL: return 4;
+    case LBM_FACE_INLET: return 3;
+    case LBM_FACE_OUTLET_EQ: return 2;
+    case LBM_FACE_OUTLET_ZG: return 1;
+    }
+    return 0;
+}
+
+// Faces crossed by offset d from a cell of class cls (non-periodic axes).
+static int crossed_faces(int cls, const int d[3], int periodic, int faces_out[3]) {
+    int n = 0;
+    for (int a = 0; a < 3; a++) {
+        if (periodic & (1 << a)) continue;
+        if (d[a] < 0 && (cls & (1 << (2 * a)))) faces_out[n++] = 2 * a;
+        if (d[a] > 0 && (cls & (1 << (2 * a + 1)))) faces_out[n++] = 2 * a + 1;
+    }
+    return n;
+}
+
+// The ghost cell reached across faces fs[0..n): highest-priority kind wins;
+// for walls the velocity is that of a moving wall face among them (the last
+// in x-, x+, y-, y+, z-, z+ order), else zero.
+static int resolve_ghost(const lbm_config &c, const int *fs, int n, int *face_idx, double uw[3]) {
+    int best = -1, bp = -1;
+    for (int i = 0; i < n; i++) {
+        int p = face_priority(c.faces[fs[i]].kind);
+        if (p > bp) { bp = p; best = fs[i]; }
+    }
+    *face_idx = best;
+    uw[0] = uw[1] = uw[2] = 0.0;
+    if (best >= 0 && c.faces[best].kind == LBM_FACE_WALL) {
+        for (int i = 0; i < n; i++) {
+            const lbm_face &f = c.faces[fs[i]];
+            if (f.kind != LBM_FACE_WALL) continue;
+            if (f.u[0] != 0 || f.u[1] != 0 || f.u[2] != 0) { uw[0] = f.u[0]; uw[1] = f.u[1]; uw[2] = f.u[2]; }
+        }
+    }
+    return best >= 0 ? c.faces[best].kind : -1;
+}
+
+static void build_classes(const lbm_config &c, StepParams &P) {
+    for (int cls = 0; cls < 64; cls++) {
+        ClassEntry e;
+        memset(&e, 0, sizeof(e));
+        // wall velocity of a cell of this class: mean over its moving wall
+        // neighbours (Determine_Wall_Velocity, lbm.cpp:941-962)
+        double uwall[3] = {0, 0, 0};
+        int num = 0;
+        for (int l = 0; l < Q; l++) {
+            int d[3] = {cx(l), cy(l), cz(l)}, fs[3], fi;
+            int n = crossed_faces(cls, d, P.periodic, fs);
+            if (!n) continue;
+            double uw[3];
+            int kind = resolve_ghost(c, fs, n, &fi, uw);
+            if (kind == LBM_FACE_WALL && (uw[0] != 0 || uw[1] != 0 || uw[2] != 0)) {
+                uwall[0] += uw[0]; uwall[1] += uw[1]; uwall[2] += uw[2];
+                num++;
+            }
+        }
+        if (num) { uwall[0] /= num; uwall[1] /= num; uwall[2] /= num; }
+        for (int l = 0; l < Q; l++) {
+            int d[3] = {-cx(l), -cy(l), -cz(l)}, fs[3], fi;
+            int n = crossed_faces(cls, d, P.periodic, fs);
+            if (!n) continue;
+            double uw[3];
+            int kind = resolve_ghost(c, fs, n, &fi, uw);
+            const lbm_face &F = c.faces[fi];
+            if (kind == LBM_FACE_WALL) {
+                e.bb |= 1u << l;
+                // f_l(x) = f*_opp(l)(x) - 2 w (u_w . c_opp) / cs^2 (lbm.cpp:274)
+                e.val[l] = (float)(6.0 * wd(l) * (uwall[0] * cx(l) + uwall[1] * cy(l) + uwall[2] * cz(l)));
+                if (l < QT && F.thermal_kind == LBM_TWALL_DIRICHLET) {
+                    e.tdir |= 1u << l;
+                    e.tval[l] = (float)(2.0 * (l == 0 ? 0.25 : 0.125) * F.T);
+                }
+            } else if (kind == LBM_FACE_INLET || kind == LBM_FACE_OUTLET_EQ) {
+                e.eq |= 1u << l;
+                e.val[l] = (float)(feq3_host(F.rho, F.u, l) - wd(l));
+                if (l < QT) {
+                    const double cu = cx(l) * F.u[0] + cy(l) * F.u[1] + cz(l) * F.u[2];
+                    e.tval[l] = (float)((l == 0 ? 0.25 : 0.125) * F.T * (1.0 + 4.0 * cu));
+                }
+            } else if (kind == LBM_FACE_OUTLET_ZG) {
+                e.zg |= 1u << l;
+            }
+        }
+        P.cls[cls] = e;
+    }
+}
+
+static void choose_block(lbm_handle *h) {
+    int nx = h->cfg.nx;
+    int tx = h->cfg.block_x, ty = h->cfg.block_y;
+    if (tx <= 0) tx = nx >= 128 ? 128 : (nx >= 64 ? 64 : 32);
+    if (ty <= 0) ty = std::max(1, 256 / tx);
+    if (tx % 32 != 0) tx = ((tx + 31) / 32) * 32;
+    h->tx = tx;
+    h->ty = ty;
+}
+
+// ---------------------------------------------------------------------------
+// Creation
+// ---------------------------------------------------------------------------
+extern "C" int lbmgpu_abi_version(void) { return 1; }
+
+extern "C" const char *lbmgpu_last_error(void) { return g_err.c_str(); }
+
+extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const uint8_t *types,
+                                               const double *rho, const double *ux, const double *uy,
+                                               const double *uz, const double *T, lbm_config *out) {
+    if (!types || !out || nx < 1 || ny < 1 || nz < 1) return fail(LBM_ERR_INVALID, "config_from_types: bad arguments");
+    const int NX = nx + 2, NY = ny + 2, NZ = nz + 2;
+    auto at = [&](int i, int j, int k) { return (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k); };
+    lbm_config c;
+    memset(&c, 0, sizeof(c));
+    c.tau = tau;
+    c.rho0 = 1.0;
+    // interior must be fluid
+    for (int k = 1; k <= nz; k++)
+        for (int j = 1; j <= ny; j++)
+            for (int i = 1; i <= nx; i++)
+                if (types[at(i, j, k)] != 0)
+                    return fail(LBM_ERR_UNSUPPORTED, "config_from_types: non-fluid cell inside the domain");
+    // face planes (without edges): uniform type and state
+    const int lim[3] = {nx, ny, nz};
+    int periodic_axis[3] = {0, 0, 0};
+    for (int f = 0; f < 6; f++) {
+        int a = f / 2, side = f % 2;
+        int fixed = side ? lim[a] + 1 : 0;
+        int b = (a + 1) % 3, cc = (a + 2) % 3;
+        int kind0 = -1;
+        double st[5] = {0, 0, 0, 0, 0};
+        for (int p = 1; p <= lim[b]; p++)
+            for (int q = 1; q <= lim[cc]; q++) {
+                int ijk[3];
+                ijk[a] = fixed;
+                ijk[b] = p;
+                ijk[cc] = q;
+                size_t id = at(ijk[0], ijk[1], ijk[2]);
+                int t = types[id];
+                double s[5] = {rho ? rho[id] : 1.0, ux ? ux[id] : 0.0, uy ? uy[id] : 0.0, uz ? uz[id] : 0.0,
+                               T ? T[id] : 0.0};
+                if (kind0 < 0) {
+                    kind0 = t;
+                    memcpy(st, s, sizeof(st));
+                } else if (t != kind0 || memcmp(st, s, sizeof(st)) != 0) {
+                    return fail(LBM_ERR_UNSUPPORTED, "config_from_types: face " + std::to_string(f) + " is not uniform");
+                }
+            }
+        lbm_face &F = c.faces[f];
+        F.rho = st[0];
+        F.u[0] = st[1];
+        F.u[1] = st[2];
+        F.u[2] = st[3];
+        F.T = st[4];
+        switch (kind0) {
+        case 1: F.kind = LBM_FACE_WALL; break;       // TYPE_S
+        case 3: F.kind = LBM_FACE_INLET; break;      // TYPE_IN
+        case 2: F.kind = LBM_FACE_OUTLET_EQ; break;  // TYPE_OUT
+        case 0: F.kind = LBM_FACE_PERIODIC; periodic_axis[a]++; break;  // TYPE_F ghost: wraps
+        default: return fail(LBM_ERR_UNSUPPORTED, "config_from_types: unsupported ghost type " + std::to_string(kind0));
+        }
+    }
+    int dims[3] = {nx, ny, nz};
+    for (int a = 0; a < 3; a++) {
+        if (periodic_axis[a] == 1) return fail(LBM_ERR_UNSUPPORTED, "config_from_types: one-sided TYPE_F ghost face");
+        if (periodic_axis[a] == 2) dims[a] += 2;  // the reference wraps over N+2 cells
+    }
+    c.nx = dims[0];
+    c.ny = dims[1];
+    c.nz = dims[2];
+    *out = c;
+    return LBM_OK;
+}
+
+static void free_handle(lbm_handle *h) {
+    if (!h) return;
+    for (int i = 0; i < 2; i++) {
+        if (h->gexec[i]) cudaGraphExecDestroy(h->gexec[i]);
+        if (h->f[i]) cudaFree(h->f[i]);
+        if (h->g[i]) cudaFree(h->g[i]);
+    }
+    cudaFree(h->mom);
+    cudaFree(h->band);
+    cudaFree(h->ds);
+    cudaFree(h->hist);
+    cudaFree(h->mk.pos);
+    cudaFree(h->mk.ds);
+    cudaFree(h->mk.udes);
+    cudaFree(h->mk.rho);
+    cudaFree(h->mk.force);
+    cudaFree(h->mk.acc);
+    for (int i = 0; i < 4; i++)
+        if (h->ev[i]) cudaEventDestroy(h->ev[i]);
+    for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+    if (h->s) cudaStreamDestroy(h->s);
+    delete h;
+}
+
+template <class Tp>
+static cudaError_t dalloc(lbm_handle *h, Tp **p, size_t bytes) {
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e == cudaSuccess) h->dev_bytes += bytes;
+    return e;
+}
+
+extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
+    if (!cfg || !out) return fail(LBM_ERR_INVALID, "create: null argument");
+    *out = nullptr;
+    const lbm_config &c = *cfg;
+    if (c.nx < 1 || c.ny < 1 || c.nz < 1) return fail(LBM_ERR_INVALID, "create: grid extents must be >= 1");
+    if (!(c.tau > 0.5)) return fail(LBM_ERR_INVALID, "create: tau must be > 0.5 (nu = (tau - 0.5)/3 > 0)");
+    if (c.storage < 0 || c.storage > 2) return fail(LBM_ERR_INVALID, "create: unknown storage format");
+    if (c.thermal && !(c.tau_g > 0.5)) return fail(LBM_ERR_INVALID, "create: tau_g must be > 0.5");
+    for (int a = 0; a < 3; a++) {
+        bool p0 = c.faces[2 * a].kind == LBM_FACE_PERIODIC, p1 = c.faces[2 * a + 1].kind == LBM_FACE_PERIODIC;
+        if (p0 != p1) return fail(LBM_ERR_INVALID, "create: a periodic axis needs both faces periodic");
+    }
+    for (int f = 0; f < 6; f++)
+        if (c.faces[f].kind < 0 || c.faces[f].kind > 4) return fail(LBM_ERR_INVALID, "create: unknown face kind");
+    lbm_handle *h = new lbm_handle();
+    h->cfg = c;
+    memset(&h->P, 0, sizeof(h->P));
+    StepParams &P = h->P;
+    P.nx = c.nx;
+    P.ny = c.ny;
+    P.nz = c.nz;
+    P.N = (long long)c.nx * c.ny * c.nz;
+    for (int a = 0; a < 3; a++)
+        if (c.faces[2 * a].kind == LBM_FACE_PERIODIC) P.periodic |= 1 << a;
+    P.omega = (float)(1.0 / c.tau);
+    P.omega_t = c.thermal ? (float)(1.0 / c.tau_g) : 0.0f;
+    for (int a = 0; a < 3; a++) {
+        P.body[a] = (float)c.body_force[a];
+        P.gbeta[a] = c.thermal ? (float)c.gbeta[a] : 0.0f;
+    }
+    P.T0 = (float)c.T_ref;
+    P.forced = (c.body_force[0] != 0 || c.body_force[1] != 0 || c.body_force[2] != 0 ||
+                (c.thermal && (c.gbeta[0] != 0 || c.gbeta[1] != 0 || c.gbeta[2] != 0)))
+                   ? 1
+                   : 0;
+    build_classes(c, P);
+    h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
+    if (c.graph_steps > 0) h->gsteps = c.graph_steps + (c.graph_steps & 1);
+    if (c.graph_steps < 0) h->gsteps = 0;
+    choose_block(h);
+    lbm_status st = LBM_OK;
+    auto chk = [&](cudaError_t e, const char *what) {
+        if (e != cudaSuccess && st == LBM_OK) {
+            st = (e == cudaErrorMemoryAllocation) ? LBM_ERR_NOMEM : LBM_ERR_CUDA;
+            g_err = std::string("create: ") + what + ": " + cudaGetErrorString(e);
+        }
+    };
+    chk(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking), "stream");
+    const size_t fb = (size_t)Q * P.N * h->esize;
+    for (int i = 0; i < 2 && st == LBM_OK; i++) chk(dalloc(h, &h->f[i], fb), "populations");
+    if (c.thermal)
+        for (int i = 0; i < 2 && st == LBM_OK; i++) chk(dalloc(h, &h->g[i], (size_t)QT * P.N * h->esize), "thermal");
+    if (st == LBM_OK) chk(dalloc(h, &h->mom, (size_t)5 * P.N * sizeof(float)), "moments");
+    if (st == LBM_OK) chk(dalloc(h, &h->ds, sizeof(DevState)), "state");
+    if (st == LBM_OK) chk(dalloc(h, &h->hist, (size_t)h->hist_cap * 8 * sizeof(double)), "history");
+    if (st == LBM_OK) {
+        DevState d;
+        memset(&d, 0, sizeof(d));
+        d.hist_cap = h->hist_cap;
+        chk(cudaMemcpyAsync(h->ds, &d, sizeof(d), cudaMemcpyHostToDevice, h->s), "state init");
+        chk(cudaMemsetAsync(h->hist, 0, (size_t)h->hist_cap * 8 * sizeof(double), h->s), "history init");
+    }
+    for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
+    if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
+    if (st != LBM_OK) {
+        free_handle(h);
+        return st;
+    }
+    *out = h;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_destroy(lbm_handle *h) {
+    if (!h) return LBM_OK;
+    if (h->s) cudaStreamSynchronize(h->s);
+    free_handle(h);
+    return LBM_OK;
+}
+
+static lbm_status do_init(lbm_handle *h, const float *dfields) {
+    float init[5] = {(float)h->cfg.rho0, (float)h->cfg.u0[0], (float)h->cfg.u0[1], (float)h->cfg.u0[2],
+                     (float)h->cfg.T_init};
+    CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, dfields, init, h->cfg.thermal != 0, h->s));
+    h->cur = 0;
+    h->steps = 0;
+    h->inited = true;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_init(lbm_handle *h) {
+    if (!h) return fail(LBM_ERR_INVALID, "init: null handle");
+    lbm_status s = do_init(h, nullptr);
+    if (s != LBM_OK) return s;
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const double *ux, const double *uy,
+                                         const double *uz, const double *T) {
+    if (!h || !rho || !ux || !uy || !uz) return fail(LBM_ERR_INVALID, "init_fields: null argument");
+    const long long N = h->P.N;
+    std::vector<float> tmp((size_t)5 * N);
+    for (long long c = 0; c < N; c++) {
+        tmp[c] = (float)rho[c];
+        tmp[N + c] = (float)ux[c];
+        tmp[2 * N + c] = (float)uy[c];
+        tmp[3 * N + c] = (float)uz[c];
+        tmp[4 * N + c] = T ? (float)T[c] : (float)h->cfg.T_init;
+    }
+    // the moment buffer doubles as upload staging
+    CUDA_TRY(cudaMemcpyAsync(h->mom, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
+    lbm_status s = do_init(h, h->mom);
+    if (s != LBM_OK) return s;
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// IBM set-up
+// ---------------------------------------------------------------------------
+extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *ds,
+                                         const double *udes) {
+    if (!h || !ic || !xyz || !ds) return fail(LBM_ERR_INVALID, "set_markers: null argument");
+    if (ic->n_markers < 1 || ic->m_max < 1) return fail(LBM_ERR_INVALID, "set_markers: need markers and m_max >= 1");
+    if (!(ic->radius > 0)) return fail(LBM_ERR_INVALID, "set_markers: radius must be > 0");
+    if (ic->free_body && (!(ic->density_ratio > 0.0) || !(ic->volume > 0.0) || !(ic->inertia > 0.0)))
+        return fail(LBM_ERR_INVALID, "set_markers: free body needs density_ratio, volume and inertia > 0");
+    if (ic->thermal && !h->cfg.thermal) return fail(LBM_ERR_INVALID, "set_markers: thermal IBM needs a thermal lattice");
+    const int n = ic->n_markers;
+    const bool fresh = !h->ibm || h->mk.n != n;
+    if (fresh) {
+        cudaFree(h->mk.pos);
+        cudaFree(h->mk.ds);
+        cudaFree(h->mk.udes);
+        cudaFree(h->mk.rho);
+        cudaFree(h->mk.force);
+        cudaFree(h->mk.acc);
+        cudaFree(h->band);
+        memset(&h->mk, 0, sizeof(h->mk));
+        h->band = nullptr;
+        CUDA_TRY(dalloc(h, &h->mk.pos, (size_t)3 * n * sizeof(double)));
+        CUDA_TRY(dalloc(h, &h->mk.ds, (size_t)n * sizeof(double)));
+        CUDA_TRY(dalloc(h, &h->mk.udes, (size_t)3 * n * sizeof(float)));
+        CUDA_TRY(dalloc(h, &h->mk.rho, (size_t)n * sizeof(float)));
+        CUDA_TRY(dalloc(h, &h->mk.force, (size_t)4 * n * sizeof(float)));
+        CUDA_TRY(dalloc(h, &h->mk.acc, (size_t)4 * n * sizeof(double)));
+        h->mk.n = n;
+    }
+    h->icfg = *ic;
+    h->mk.tdes = (float)ic->T_body;
+    // band: every stencil node of a marker within `radius` of the centre
+    int bs[3], dims[3] = {h->P.nx, h->P.ny, h->P.nz}, org[3];
+    for (int a = 0; a < 3; a++) {
+        bs[a] = std::min(dims[a], (int)std::ceil(2.0 * ic->radius) + 6);
+        int o = (int)std::floor(ic->center[a] - ic->radius) - 2;
+        org[a] = std::max(0, std::min(o, dims[a] - bs[a]));
+    }
+    long long nb = (long long)bs[0] * bs[1] * bs[2];
+    if (fresh || nb != h->P.nb) {
+        cudaFree(h->band);
+        h->band = nullptr;
+        CUDA_TRY(dalloc(h, &h->band, (size_t)12 * nb * sizeof(float)));
+        CUDA_TRY(cudaMemsetAsync(h->band, 0, (size_t)12 * nb * sizeof(float), h->s));
+    }
+    h->P.band_on = 1;
+    h->P.bsx = bs[0];
+    h->P.bsy = bs[1];
+    h->P.bsz = bs[2];
+    h->P.nb = nb;
+    std::vector<float> ud((size_t)3 * n);
+    for (int a = 0; a < 3; a++)
+        for (int m = 0; m < n; m++) ud[(size_t)a * n + m] = (float)(udes ? udes[(size_t)a * n + m] : ic->velocity[a]);
+    CUDA_TRY(cudaMemcpyAsync(h->mk.pos, xyz, (size_t)3 * n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemcpyAsync(h->mk.ds, ds, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemcpyAsync(h->mk.udes, ud.data(), ud.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemsetAsync(h->mk.acc, 0, (size_t)4 * n * sizeof(double), h->s));
+    // device state: band origin and rigid body
+    DevState d;
+    CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    for (int a = 0; a < 3; a++) {
+        d.band_o[a] = org[a];
+        d.body_xc[a] = ic->center[a];
+        d.body_v[a] = ic->velocity[a];
+        d.body_om[a] = 0.0;
+        d.body_dxc[a] = 0.0;
+    }
+    d.have_prev = 0;
+    for (int k = 0; k < 6; k++) d.internal_prev[k] = 0.0;
+    CUDA_TRY(cudaMemcpyAsync(h->ds, &d, sizeof(d), cudaMemcpyHostToDevice, h->s));
+    h->bp.free_body = ic->free_body;
+    h->bp.radius = ic->radius;
+    h->bp.mass = ic->density_ratio * ic->volume;
+    h->bp.inertia = ic->inertia;
+    for (int a = 0; a < 3; a++)
+        h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
+    h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
+    h->ibm = true;
+    // graphs captured earlier do not contain the IBM launches
+    for (int i = 0; i < 2; i++)
+        if (h->gexec[i]) {
+            cudaGraphExecDestroy(h->gexec[i]);
+            h->gexec[i] = nullptr;
+        }
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Stepping
+// ---------------------------------------------------------------------------
+static LaunchArgs make_args(lbm_handle *h, int gather) {
+    LaunchArgs a;
+    a.P = &h->P;
+    a.A = h->f[h->cur];
+    a.B = h->f[1 - h->cur];
+    a.GA = h->g[h->cur];
+    a.GB = h->g[1 - h->cur];
+    a.ds = h->ds;
+    a.mom = nullptr;
+    a.band = h->band;
+    a.gather = gather;
+    a.export_only = 0;
+    a.thermal = h->cfg.thermal;
+    a.tx = h->tx;
+    a.ty = h->ty;
+    a.stream = h->s;
+    return a;
+}
+
+// Enqueue one reference iteration.  ev_pair (optional) brackets the fused kernel.
+static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaEvent_t e1) {
+    LaunchArgs a = make_args(h, gather);
+    cudaError_t e;
+    if (e0) cudaEventRecord(e0, h->s);
+    if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
+    if (e1) cudaEventRecord(e1, h->s);
+    if (h->ibm) {
+        IbmArgs ia;
+        ia.P = &h->P;
+        ia.mk = h->mk;
+        ia.ds = h->ds;
+        ia.band = h->band;
+        ia.thermal = h->icfg.thermal;
+        ia.stream = h->s;
+        for (int it = 1; it <= h->icfg.m_max; it++) {
+            if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
+            if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
+        }
+        if ((e = launch_band_collide(h->cfg.storage, a, h->icfg.literal_sign ? -1.0f : 1.0f)) != cudaSuccess) return e;
+        if ((e = launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap)) != cudaSuccess) return e;
+    }
+    h->cur = 1 - h->cur;
+    return cudaSuccess;
+}
+
+static lbm_status ensure_graph(lbm_handle *h) {
+    const int p = h->cur;
+    if (h->gexec[p]) return LBM_OK;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+    cudaError_t e = cudaSuccess;
+    for (int i = 0; i < h->gsteps && e == cudaSuccess; i++) e = enqueue_step(h, 1, nullptr, nullptr);
+    cudaError_t e2 = cudaStreamEndCapture(h->s, &g);
+    h->cur = p;  // gsteps is even: the capture ends where it started
+    if (e != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return fail(LBM_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    }
+    if (e2 != cudaSuccess) return fail(LBM_ERR_CUDA, std::string("graph capture end: ") + cudaGetErrorString(e2));
+    cudaError_t e3 = cudaGraphInstantiate(&h->gexec[p], g, 0);
+    cudaGraphDestroy(g);
+    if (e3 != cudaSuccess) {
+        h->gexec[p] = nullptr;
+        return fail(LBM_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e3));
+    }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
+    if (!h) return fail(LBM_ERR_INVALID, "step: null handle");
+    if (!h->inited) return fail(LBM_ERR_STATE, "step: call lbmgpu_init first");
+    if (nsteps < 0) return fail(LBM_ERR_INVALID, "step: negative step count");
+    while (nsteps > 0) {
+        if (h->steps == 0) {
+            CUDA_TRY(enqueue_step(h, 0, nullptr, nullptr));
+            h->steps++;
+            nsteps--;
+            continue;
+        }
+        if (h->gsteps > 0 && nsteps >= h->gsteps) {
+            lbm_status s = ensure_graph(h);
+            if (s != LBM_OK) return s;
+            CUDA_TRY(cudaGraphLaunch(h->gexec[h->cur], h->s));
+            h->steps += h->gsteps;
+            nsteps -= h->gsteps;
+            continue;
+        }
+        CUDA_TRY(enqueue_step(h, 1, nullptr, nullptr));
+        h->steps++;
+        nsteps--;
+    }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms) {
+    if (!h) return fail(LBM_ERR_INVALID, "step_profiled: null handle");
+    if (!h->inited) return fail(LBM_ERR_STATE, "step_profiled: call lbmgpu_init first");
+    if (nsteps < 0) return fail(LBM_ERR_INVALID, "step_profiled: negative step count");
+    // one event pair per fused launch, all read after the last step so the
+    // host never stalls the stream between steps
+    while ((int)h->evpool.size() < 2 * nsteps) {
+        cudaEvent_t e;
+        CUDA_TRY(cudaEventCreate(&e));
+        h->evpool.push_back(e);
+    }
+    CUDA_TRY(cudaEventRecord(h->ev[0], h->s));
+    for (int i = 0; i < nsteps; i++) {
+        CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, h->evpool[2 * i], h->evpool[2 * i + 1]));
+        h->steps++;
+    }
+    CUDA_TRY(cudaEventRecord(h->ev[1], h->s));
+    CUDA_TRY(cudaEventSynchronize(h->ev[1]));
+    float tot = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&tot, h->ev[0], h->ev[1]));
+    double fused = 0.0;
+    for (int i = 0; i < nsteps; i++) {
+        float ms = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->evpool[2 * i], h->evpool[2 * i + 1]));
+        fused += ms;
+    }
+    if (total_ms) *total_ms = tot;
+    if (fused_ms) *fused_ms = fused;
+    return LBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Read-back
+// ---------------------------------------------------------------------------
+static lbm_status export_moments(lbm_handle *h) {
+    if (!h->inited) return fail(LBM_ERR_STATE, "download: call lbmgpu_init first");
+    LaunchArgs a = make_args(h, h->steps == 0 ? 0 : 1);
+    a.mom = h->mom;
+    a.export_only = 1;
+    CUDA_TRY(launch_step(h->cfg.storage, a));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host) {
+    if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
+    if (field < 0 || field > 4 || (field == 4 && !h->cfg.thermal)) return fail(LBM_ERR_INVALID, "download: bad field");
+    lbm_status s = export_moments(h);
+    if (s != LBM_OK) return s;
+    CUDA_TRY(cudaMemcpyAsync(host, h->mom + (size_t)field * h->P.N, (size_t)h->P.N * sizeof(float),
+                             cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host) {
+    if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
+    lbm_status s = export_moments(h);
+    if (s != LBM_OK) return s;
+    const int nf = h->cfg.thermal ? 5 : 4;
+    CUDA_TRY(cudaMemcpyAsync(host, h->mom, (size_t)nf * h->P.N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_download(lbm_handle *h, int field, double *host) {
+    if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
+    std::vector<float> tmp((size_t)h->P.N);
+    lbm_status s = lbmgpu_download_f32(h, field, tmp.data());
+    if (s != LBM_OK) return s;
+    for (size_t i = 0; i < tmp.size(); i++) host[i] = tmp[i];
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
+    if (!h || !out || max_steps < 0) return fail(LBM_ERR_INVALID, "get_forces: bad argument");
+    if (!h->ibm) return fail(LBM_ERR_STATE, "get_forces: no markers set");
+    DevState d;
+    CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    long long avail = std::min<long long>(d.step, h->hist_cap);
+    long long n = std::min<long long>(avail, max_steps);
+    // the last n entries of the ring, in at most two contiguous pieces
+    long long first = (d.step - n) % h->hist_cap;
+    long long n1 = std::min(n, h->hist_cap - first);
+    if (n1 > 0)
+        CUDA_TRY(cudaMemcpyAsync(out, h->hist + first * 8, (size_t)n1 * 8 * sizeof(double), cudaMemcpyDeviceToHost,
+                                 h->s));
+    if (n > n1)
+        CUDA_TRY(cudaMemcpyAsync(out + n1 * 8, h->hist, (size_t)(n - n1) * 8 * sizeof(double),
+                                 cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    if (n_out) *n_out = (int)n;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]) {
+    if (!h || !out) return fail(LBM_ERR_INVALID, "get_body: null argument");
+    DevState d;
+    CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    for (int a = 0; a < 3; a++) {
+        out[a] = d.body_xc[a];
+        out[3 + a] = d.body_v[a];
+        out[6 + a] = d.body_om[a];
+    }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_get_markers(lbm_handle *h, double *xyz) {
+    if (!h || !xyz) return fail(LBM_ERR_INVALID, "get_markers: null argument");
+    if (!h->ibm) return fail(LBM_ERR_STATE, "get_markers: no markers set");
+    CUDA_TRY(cudaMemcpyAsync(xyz, h->mk.pos, (size_t)3 * h->mk.n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_status(lbm_handle *h, uint32_t *flags) {
+    if (!h || !flags) return fail(LBM_ERR_INVALID, "status: null argument");
+    uint32_t v = 0;
+    CUDA_TRY(cudaMemcpyAsync(&v, &h->ds->status, sizeof(v), cudaMemcpyDeviceToHost, h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    *flags = v;
+    if (v & ST_RHO_RANGE) return fail(LBM_ERR_DIVERGED, "status: density left (0, 100) or became NaN");
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_sync(lbm_handle *h) {
+    if (!h) return fail(LBM_ERR_INVALID, "sync: null handle");
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_steps_done(lbm_handle *h, long long *steps) {
+    if (!h || !steps) return fail(LBM_ERR_INVALID, "steps_done: null argument");
+    *steps = h->steps;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes) {
+    if (!h || !bytes) return fail(LBM_ERR_INVALID, "device_bytes: null argument");
+    *bytes = h->dev_bytes;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_host_alloc(size_t bytes, void **ptr) {
+    if (!ptr) return fail(LBM_ERR_INVALID, "host_alloc: null argument");
+    CUDA_TRY(cudaMallocHost(ptr, bytes));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_host_free(void *ptr) {
+    CUDA_TRY(cudaFreeHost(ptr));
+    return LBM_OK;
+}

@@ -1,0 +1,279 @@
+// lbm_ibm.cu -- immersed-boundary kernels (marker-parallel, one warp per
+// marker) and the FP64 force reduction / rigid-body update.
+//
+// The implicit multi-direct forcing of IBLBM (lbm.cpp:1259-1390) is run on
+// the band of cells around the body:
+//   k_ibm_interp(first=1): U_m = sum u delta, rho_m = sum rho delta (unforced
+//                          moments written by k_step), F_m = 2 rho_m (U_des - U_m)
+//   k_ibm_spread:          Ft(x) += F_m ds_m delta(x - X_m)
+//   k_ibm_interp(first=0): U_m from u = u_unf + Ft / (2 rho); next F_m
+//   ... m_max spreads in total ...
+//   k_ibm_finish:          FP64 sums of -F_m ds (drag/lift), torque and heat
+//                          in a fixed order; Newton-Euler update when free
+//                          (Kempe & Froehlich internal-fluid treatment).
+// Each marker's stencil is the 4x4x4 node block with |r| < 2, on which the
+// 4-point Peskin delta (lbm.cpp:1095-1102) is non-zero; node (a,b,c) of the
+// block is handled by lane a + 4b + 16c (mod 32), two nodes per lane, and the
+// warp reduces with shuffles in a fixed order.
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+namespace lbmk {
+
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__global__ void __launch_bounds__(128) k_ibm_interp(const __grid_constant__ StepParams P, MarkerDev mk,
+                                                    DevState *__restrict__ ds, const float *__restrict__ band,
+                                                    int first, int thermal) {
+    const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (m >= mk.n) return;  // whole warp leaves together
+    const int n = mk.n;
+    const double X = mk.pos[m], Y = mk.pos[n + m], Z = mk.pos[2 * n + m];
+    const double flx = floor(X), fly = floor(Y), flz = floor(Z);
+    const float fx = (float)(X - flx), fy = (float)(Y - fly), fz = (float)(Z - flz);
+    // stencil node a: reference node i = floor(X) - 1 + a, device cell i - 1
+    const int bx0 = (int)flx - 2 - ds->band_o[0];
+    const int by0 = (int)fly - 2 - ds->band_o[1];
+    const int bz0 = (int)flz - 2 - ds->band_o[2];
+    const long long nb = P.nb;
+    float su = 0.f, sv = 0.f, sw = 0.f, sr = 0.f, sT = 0.f;
+    bool edge = false;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int s = lane + 32 * h;
+        const int a = s & 3, b = (s >> 2) & 3, c = s >> 4;
+        const float wgt = peskin((float)(a - 1) - fx) * peskin((float)(b - 1) - fy) * peskin((float)(c - 1) - fz);
+        const int bx = bx0 + a, by = by0 + b, bz = bz0 + c;
+        if ((unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy && (unsigned)bz < (unsigned)P.bsz) {
+            const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
+            const float rho = 1.0f + band[q];
+            const float hr = 0.5f / rho;
+            su += wgt * (band[nb + q] + hr * band[7 * nb + q]);
+            sv += wgt * (band[2 * nb + q] + hr * band[8 * nb + q]);
+            sw += wgt * (band[3 * nb + q] + hr * band[9 * nb + q]);
+            if (first) sr += wgt * rho;
+            if (thermal) sT += wgt * (band[10 * nb + q] + 0.5f * band[11 * nb + q]);
+        } else if (wgt != 0.0f) {
+            edge = true;
+        }
+    }
+    su = warp_sum(su);
+    sv = warp_sum(sv);
+    sw = warp_sum(sw);
+    if (first) sr = warp_sum(sr);
+    if (thermal) sT = warp_sum(sT);
+    const bool any_edge = __any_sync(0xffffffffu, edge);
+    if (lane == 0) {
+        if (any_edge) atomicOr(&ds->status, ST_BAND_EDGE);
+        if (first) mk.rho[m] = sr;
+        const float rm = first ? sr : mk.rho[m];
+        const float Fx = 2.0f * rm * (mk.udes[m] - su);
+        const float Fy = 2.0f * rm * (mk.udes[n + m] - sv);
+        const float Fz = 2.0f * rm * (mk.udes[2 * n + m] - sw);
+        mk.force[m] = Fx;
+        mk.force[n + m] = Fy;
+        mk.force[2 * n + m] = Fz;
+        const double dsv = mk.ds[m];
+        mk.acc[m] += -(double)Fx * dsv;
+        mk.acc[n + m] += -(double)Fy * dsv;
+        mk.acc[2 * n + m] += -(double)Fz * dsv;
+        if (thermal) {
+            const float Qm = 2.0f * (mk.tdes - sT);
+            mk.force[3 * n + m] = Qm;
+            mk.acc[3 * n + m] += (double)Qm * dsv;
+        }
+        if (!isfinite(Fx) || !isfinite(Fy) || !isfinite(Fz)) atomicOr(&ds->status, ST_NONFINITE_FORCE);
+    }
+}
+
+__global__ void __launch_bounds__(128) k_ibm_spread(const __grid_constant__ StepParams P, MarkerDev mk,
+                                                    const DevState *__restrict__ ds, float *__restrict__ band,
+                                                    int thermal) {
+    const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31;
+    if (m >= mk.n) return;
+    const int n = mk.n;
+    const double X = mk.pos[m], Y = mk.pos[n + m], Z = mk.pos[2 * n + m];
+    const double flx = floor(X), fly = floor(Y), flz = floor(Z);
+    const float fx = (float)(X - flx), fy = (float)(Y - fly), fz = (float)(Z - flz);
+    const int bx0 = (int)flx - 2 - ds->band_o[0];
+    const int by0 = (int)fly - 2 - ds->band_o[1];
+    const int bz0 = (int)flz - 2 - ds->band_o[2];
+    const long long nb = P.nb;
+    const float dsv = (float)mk.ds[m];
+    const float Fx = mk.force[m] * dsv, Fy = mk.force[n + m] * dsv, Fz = mk.force[2 * n + m] * dsv;
+    const float Qm = thermal ? mk.force[3 * n + m] * dsv : 0.0f;
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+        const int s = lane + 32 * h;
+        const int a = s & 3, b = (s >> 2) & 3, c = s >> 4;
+        const float wgt = peskin((float)(a - 1) - fx) * peskin((float)(b - 1) - fy) * peskin((float)(c - 1) - fz);
+        const int bx = bx0 + a, by = by0 + b, bz = bz0 + c;
+        if (wgt != 0.0f && (unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy &&
+            (unsigned)bz < (unsigned)P.bsz) {
+            const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
+            atomicAdd(&band[7 * nb + q], Fx * wgt);
+            atomicAdd(&band[8 * nb + q], Fy * wgt);
+            atomicAdd(&band[9 * nb + q], Fz * wgt);
+            if (thermal) atomicAdd(&band[11 * nb + q], Qm * wgt);
+        }
+    }
+}
+
+// One block.  Deterministic FP64 reductions: each thread sums a strided set
+// in index order, then a fixed shared-memory tree.
+__device__ __forceinline__ void block_tree(double (*red)[256], int nq, int t) {
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int k = 0; k < nq; k++) red[k][t] += red[k][t + w];
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(256) k_ibm_finish(const __grid_constant__ StepParams P, MarkerDev mk,
+                                                    DevState *__restrict__ ds, BodyParams bp,
+                                                    const float *__restrict__ band, double *__restrict__ hist,
+                                                    long long hist_cap) {
+    __shared__ double red[7][256];
+    __shared__ double sh_dxc[3], sh_om[3], sh_v[3], sh_xc[3], sh_f[7];
+    const int t = threadIdx.x;
+    const int n = mk.n;
+    const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
+    double s[7] = {0, 0, 0, 0, 0, 0, 0};
+    for (int m = t; m < n; m += 256) {
+        const double fx = mk.acc[m], fy = mk.acc[n + m], fz = mk.acc[2 * n + m], hq = mk.acc[3 * n + m];
+        const double rx = mk.pos[m] - xc0, ry = mk.pos[n + m] - xc1, rz = mk.pos[2 * n + m] - xc2;
+        s[0] += fx;
+        s[1] += fy;
+        s[2] += fz;
+        s[3] += ry * fz - rz * fy;
+        s[4] += rz * fx - rx * fz;
+        s[5] += rx * fy - ry * fx;
+        s[6] += hq;
+        mk.acc[m] = 0.0;
+        mk.acc[n + m] = 0.0;
+        mk.acc[2 * n + m] = 0.0;
+        mk.acc[3 * n + m] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < 7; k++) red[k][t] = s[k];
+    block_tree(red, 7, t);
+    if (t == 0) {
+        const long long step = ds->step;
+        double *h = hist + (step % hist_cap) * 8;
+        for (int k = 0; k < 7; k++) {
+            h[k] = red[k][0];
+            sh_f[k] = red[k][0];
+        }
+        h[7] = (double)step;
+        ds->step = step + 1;
+    }
+    if (!bp.free_body) return;
+    // fluid momentum and angular momentum inside the body after the forced
+    // collision, u_unf + F_b / (2 rho) + Ft / rho, volume fraction
+    // clamp(R + 1/2 - |x - xc|, 0, 1) (Kempe & Froehlich 2012)
+    __syncthreads();
+    double q[6] = {0, 0, 0, 0, 0, 0};
+    const long long nb = P.nb;
+    for (long long b = t; b < nb; b += 256) {
+        const int bx = (int)(b % P.bsx), by = (int)((b / P.bsx) % P.bsy), bz = (int)(b / ((long long)P.bsx * P.bsy));
+        const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
+        if (x >= P.nx || y >= P.ny || z >= P.nz) continue;
+        const double rx = (x + 1) - xc0, ry = (y + 1) - xc1, rz = (z + 1) - xc2;
+        double a = bp.radius + 0.5 - sqrt(rx * rx + ry * ry + rz * rz);
+        if (a <= 0.0) continue;
+        if (a > 1.0) a = 1.0;
+        const double rho = 1.0 + (double)band[b];
+        const double ux = (double)band[nb + b] + 0.5 * band[4 * nb + b] / rho + band[7 * nb + b] / rho;
+        const double uy = (double)band[2 * nb + b] + 0.5 * band[5 * nb + b] / rho + band[8 * nb + b] / rho;
+        const double uz = (double)band[3 * nb + b] + 0.5 * band[6 * nb + b] / rho + band[9 * nb + b] / rho;
+        q[0] += a * ux;
+        q[1] += a * uy;
+        q[2] += a * uz;
+        q[3] += a * (ry * uz - rz * uy);
+        q[4] += a * (rz * ux - rx * uz);
+        q[5] += a * (rx * uy - ry * ux);
+    }
+#pragma unroll
+    for (int k = 0; k < 6; k++) red[k][t] = q[k];
+    block_tree(red, 6, t);
+    if (t == 0) {
+        if (!ds->have_prev) {
+            for (int k = 0; k < 6; k++) ds->internal_prev[k] = red[k][0];
+            ds->have_prev = 1;
+        }
+        // Newton-Euler, dt = 1: rho_s V dV/dt = F_h + dI/dt + (rho_s - rho_f) V g
+        for (int a = 0; a < 3; a++) {
+            const double dI = red[a][0] - ds->internal_prev[a];
+            const double dL = red[3 + a][0] - ds->internal_prev[3 + a];
+            const double vn =
+                ((bp.dof >> a) & 1) ? ds->body_v[a] + (sh_f[a] + dI) / bp.mass + bp.gacc[a] : ds->body_v[a];
+            const double om =
+                ((bp.dof >> (3 + a)) & 1) ? ds->body_om[a] + (sh_f[3 + a] + dL) / bp.inertia : ds->body_om[a];
+            const double d = 0.5 * (ds->body_v[a] + vn);
+            sh_dxc[a] = d;
+            sh_v[a] = vn;
+            sh_om[a] = om;
+            sh_xc[a] = ds->body_xc[a] + d;
+            ds->body_dxc[a] = d;
+            ds->body_v[a] = vn;
+            ds->body_om[a] = om;
+            ds->body_xc[a] = sh_xc[a];
+        }
+        for (int k = 0; k < 6; k++) ds->internal_prev[k] = red[k][0];
+        const int ns[3] = {P.nx, P.ny, P.nz};
+        const int bs[3] = {P.bsx, P.bsy, P.bsz};
+        for (int a = 0; a < 3; a++) {
+            int o = (int)floor(sh_xc[a] - bp.radius) - 2;
+            o = max(0, min(o, ns[a] - bs[a]));
+            ds->band_o[a] = o;
+        }
+    }
+    __syncthreads();
+    const double R = bp.radius;
+    for (int m = t; m < n; m += 256) {
+        const double r0 = mk.pos[m] - (sh_xc[0] - sh_dxc[0]);
+        const double r1 = mk.pos[n + m] - (sh_xc[1] - sh_dxc[1]);
+        const double r2 = mk.pos[2 * n + m] - (sh_xc[2] - sh_dxc[2]);
+        double q0 = r0 + (sh_om[1] * r2 - sh_om[2] * r1);
+        double q1 = r1 + (sh_om[2] * r0 - sh_om[0] * r2);
+        double q2 = r2 + (sh_om[0] * r1 - sh_om[1] * r0);
+        const double sc = R / sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+        q0 *= sc;
+        q1 *= sc;
+        q2 *= sc;
+        mk.pos[m] = sh_xc[0] + q0;
+        mk.pos[n + m] = sh_xc[1] + q1;
+        mk.pos[2 * n + m] = sh_xc[2] + q2;
+        mk.udes[m] = (float)(sh_v[0] + (sh_om[1] * q2 - sh_om[2] * q1));
+        mk.udes[n + m] = (float)(sh_v[1] + (sh_om[2] * q0 - sh_om[0] * q2));
+        mk.udes[2 * n + m] = (float)(sh_v[2] + (sh_om[0] * q1 - sh_om[1] * q0));
+    }
+}
+
+cudaError_t launch_ibm_interp(const IbmArgs &a, int first) {
+    const int threads = 128;
+    const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;
+    k_ibm_interp<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, first, a.thermal);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ibm_spread(const IbmArgs &a) {
+    const int threads = 128;
+    const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;
+    k_ibm_spread<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, a.thermal);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap) {
+    k_ibm_finish<<<1, 256, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
+    return cudaGetLastError();
+}
+
+}  // namespace lbmk

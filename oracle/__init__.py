@@ -93,7 +93,9 @@ def lib():
         L.orc_step_ibm.restype = l
         L.orc_step_ibm.argtypes = [vp, vp, vp, C.POINTER(d), C.POINTER(d)]
         L.orc_fibonacci_sphere.argtypes = [i, d, C.POINTER(d)] + [C.POINTER(d)] * 7
-        L.orc_body_step.argtypes = [vp, vp, d, C.POINTER(d)]
+        L.orc_body_step.argtypes = [vp, vp, d, C.POINTER(d), C.POINTER(d)]
+        L.orc_internal_momentum.argtypes = [vp, C.POINTER(d), d, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(d)]
         L.orc_nusselt_volume.restype = d
         L.orc_nusselt_volume.argtypes = [vp, d, d]
         _lib = L
@@ -140,7 +142,8 @@ class Body(C.Structure):
 
     _fields_ = [("xc", C.c_double * 3), ("v", C.c_double * 3), ("om", C.c_double * 3),
                 ("rho_ratio", C.c_double), ("vol", C.c_double), ("inertia", C.c_double),
-                ("grav", C.c_double * 3)]
+                ("grav", C.c_double * 3), ("dof", C.c_int), ("have_prev", C.c_int),
+                ("internal_prev", C.c_double * 6)]
 
 
 class Lattice:
@@ -337,3 +340,97 @@ def read_ref_dump(path: str, NX: int, NY: int, NZ: int, nfields: int, steps: int
 
 if __name__ == "__main__":  # pragma: no cover
     print(build(force="--force" in sys.argv))
+
+
+# --------------------------------------------------------------------------
+# Helpers mirroring the GPU path's read-back and IBM driver
+# --------------------------------------------------------------------------
+
+def moments(lat: Lattice, body=(0.0, 0.0, 0.0), gbeta=(0.0, 0.0, 0.0), T0: float = 0.0) -> dict:
+    """MacroProp moments of the post-streaming state, interior cells
+    (lbm.cpp:668-679): rho = sum f, u = (sum f c + F/2) / rho with
+    F = body + gbeta (T - T0); T = sum g."""
+    f = lat.f[:, 1:-1, 1:-1, 1:-1]
+    cx = (CX19 if lat.q == 19 else np.array([0, 1, 0, -1, 0, 1, -1, -1, 1]))
+    cy = (CY19 if lat.q == 19 else np.array([0, 0, 1, 0, -1, 1, 1, -1, -1]))
+    cz = (CZ19 if lat.q == 19 else np.zeros(9, int))
+    rho = f.sum(axis=0)
+    jx = np.tensordot(cx, f, axes=(0, 0))
+    jy = np.tensordot(cy, f, axes=(0, 0))
+    jz = np.tensordot(cz, f, axes=(0, 0))
+    out = {"rho": rho}
+    F = [np.full_like(rho, body[a]) for a in range(3)]
+    if lat.thermal:
+        T = lat.g[:, 1:-1, 1:-1, 1:-1].sum(axis=0)
+        out["T"] = T
+        for a in range(3):
+            F[a] = F[a] + gbeta[a] * (T - T0)
+    out["ux"] = (jx + 0.5 * F[0]) / rho
+    out["uy"] = (jy + 0.5 * F[1]) / rho
+    out["uz"] = (jz + 0.5 * F[2]) / rho
+    return out
+
+
+def internal_momentum(lat: Lattice, xc, radius: float, lo, hi) -> np.ndarray:
+    out = np.zeros(6)
+    c = np.ascontiguousarray(xc, dtype=np.float64)
+    lo_a = (C.c_int * 3)(*lo)
+    hi_a = (C.c_int * 3)(*hi)
+    lib().orc_internal_momentum(lat.h, _dp(c), radius, lo_a, hi_a, _dp(out))
+    return out
+
+
+def body_step(body: Body, mk: Markers, radius: float, force, internal) -> None:
+    f = np.ascontiguousarray(force[:6], dtype=np.float64)
+    im = np.ascontiguousarray(internal[:6], dtype=np.float64)
+    lib().orc_body_step(C.byref(body), C.byref(mk), radius, _dp(f), _dp(im))
+
+
+def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, steps=10, lit_sign=0,
+                thermal=None, free=None):
+    """Channel + immersed sphere with the GPU path's conventions: inlet
+    equilibrium at x = 0, zero-gradient outlet, bounce-back y/z walls,
+    Fibonacci markers, interpolated marker density.  thermal = dict(tau_g,
+    gbeta, T_in, T_body) adds the D3Q7 population and the thermal IBM;
+    free = dict(rho_ratio, gravity[, dof]) makes the body free (Newton-Euler;
+    dof bits 0-2 translation, 3-5 rotation, default all six).
+    Returns (lattice, markers, per-step force history [steps, 7], body)."""
+    lat = Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    t[:, :, 0] = TYPE_IN
+    t[:, :, -1] = TYPE_OUTZG
+    t[:, 0, :] = TYPE_S
+    t[:, -1, :] = TYPE_S
+    t[0, :, :] = TYPE_S
+    t[-1, :, :] = TYPE_S
+    lat.ux[t != TYPE_S] = u_in
+    if thermal:
+        lat.enable_thermal(thermal["tau_g"], thermal.get("T0", 0.0), thermal.get("gbeta", (0.0, 0.0, 0.0)))
+        lat.T[:] = thermal.get("T_in", 0.0)
+    lat.init()
+    mk = fibonacci_sphere(n_markers, diameter, center)
+    if thermal:
+        mk["Td"][:] = thermal["T_body"]
+    R = diameter / 2.0
+    body = Body()
+    for a in range(3):
+        body.xc[a] = center[a]
+    if free:
+        body.rho_ratio = free["rho_ratio"]
+        body.vol = np.pi * diameter ** 3 / 6.0 if "vol" not in free else free["vol"]
+        body.inertia = 0.4 * body.rho_ratio * body.vol * R * R if "inertia" not in free else free["inertia"]
+        for a in range(3):
+            body.grav[a] = free["gravity"][a]
+        body.dof = free.get("dof", 63)
+    hist = np.zeros((steps, 7))
+    for s in range(steps):
+        c = [body.xc[0], body.xc[1], body.xc[2]]
+        lo, hi = sphere_box(c, diameter, lat)
+        op = ibm_opts(lo, hi, m_max, lit_sign=lit_sign, rho_mode=0, thermal=1 if thermal else 0)
+        out = lat.step_ibm(mk, op, c)
+        hist[s] = out
+        if free:
+            im = internal_momentum(lat, c, R, lo, hi)
+            body_step(body, mk, R, out, im)
+    return lat, mk, hist, body

@@ -33,10 +33,10 @@
  *     factor (Seta 2013 style), T = sum g + Q/2.
  *   - Boussinesq body force F = g_beta * (T - T0) along the gravity axis,
  *     the form of lbm.cpp:804-805.
- *   - Rigid-body update with the rigid internal-fluid approximation of
- *     Uhlmann (J. Comput. Phys. 209, 2005):
- *       (rho_s - rho_f) V_s dV/dt = F_h + (rho_s - rho_f) V_s g
- *       (1 - rho_f/rho_s) I_p dOmega/dt = T_h.
+ *   - Rigid-body update with the internal-fluid treatment of Kempe &
+ *     Froehlich (J. Comput. Phys. 231, 2012):
+ *       rho_s V_s dV/dt = F_h + d/dt(int u dV) + (rho_s - rho_f) V_s g
+ *       I_p dOmega/dt   = T_h + d/dt(int r x u dV).
  *   - Fibonacci (golden-angle) sphere markers with area weight pi D^2 / N.
  *
  * Compile with -ffp-contract=off so that x86 and aarch64 give the same bits.
@@ -449,6 +449,10 @@ static inline int ibm_node_ok(uint8_t t) { return t == ORC_F || t == ORC_IN || t
 static void interp3(const orc *o, const orc_ibm_opts *op, double X, double Y, double Z,
                     const double *a, const double *b, const double *c3, double out[3]) {
     double s0 = 0, s1 = 0, s2 = 0;
+    if (!(X > -2 && X < o->NX + 2 && Y > -2 && Y < o->NY + 2 && Z > -2 && Z < o->NZ + 2)) {
+        out[0] = out[1] = out[2] = NAN; /* marker left the lattice */
+        return;
+    }
     int i0 = (int)floor(X) - 1, j0 = (int)floor(Y) - 1, k0 = (int)floor(Z) - 1;
     for (int i = i0; i <= i0 + 3; i++) {
         if (i < op->box_lo[0] || i > op->box_hi[0]) continue;
@@ -565,6 +569,7 @@ void orc_ibm_step(orc *o, orc_markers *mk, const orc_ibm_opts *op, const double 
     /* lattice scratch for the spread increments (Fm, lbm.cpp:1333-1344) */
     int bx = op->box_hi[0] - op->box_lo[0] + 1, by = op->box_hi[1] - op->box_lo[1] + 1,
         bz = op->box_hi[2] - op->box_lo[2] + 1;
+    if (bx < 1 || by < 1 || bz < 1) bx = by = bz = 1; /* body outside the lattice: nothing to spread */
     long nb = (long)bx * by * bz;
     double *Fm = (double *)calloc(4 * nb, sizeof(double));
     double sgn = op->lit_sign ? -1.0 : 1.0;
@@ -591,6 +596,7 @@ void orc_ibm_step(orc *o, orc_markers *mk, const orc_ibm_opts *op, const double 
         memset(Fm, 0, 4 * nb * sizeof(double));
         for (int m = 0; m < N; m++) {
             double X = mk->x[m], Y = mk->y[m], Z = mk->z[m];
+            if (!(X > -2 && X < o->NX + 2 && Y > -2 && Y < o->NY + 2 && Z > -2 && Z < o->NZ + 2)) continue;
             int i0 = (int)floor(X) - 1, j0 = (int)floor(Y) - 1, k0 = (int)floor(Z) - 1;
             for (int i = i0; i <= i0 + 3; i++) {
                 if (i < op->box_lo[0] || i > op->box_hi[0]) continue;
@@ -690,26 +696,67 @@ typedef struct orc_body {
     double xc[3], v[3], om[3];
     double rho_ratio;  /* rho_s / rho_f */
     double vol;        /* V_s */
-    double inertia;    /* I_p = 2/5 m R^2 with m = rho_s V_s */
+    double inertia;    /* I_p = 2/5 rho_s V_s R^2 */
     double grav[3];
+    int dof;           /* free degrees of freedom: bits 0-2 translation x,y,z, bits 3-5 rotation */
+    int have_prev;
+    double internal_prev[6];
 } orc_body;
 
-/* Newton-Euler step, dt = 1, rho_f = 1 (Uhlmann 2005 rigid internal fluid):
- * V' = V + (F_h / ((rho_s - 1) V_s) + g),  Om' = Om + T_h / ((1 - 1/rho_s) I_p),
- * x_c' = x_c + (V + V') / 2; markers follow x_c and rotate with Om' about it
- * (r' = r + Om' x r, rescaled to radius R); desired marker velocity
- * V' + Om' x r'. */
-void orc_body_step(orc_body *b, orc_markers *mk, double R, const double force[6]) {
-    double mrel = (b->rho_ratio - 1.0) * b->vol;
-    double irel = (1.0 - 1.0 / b->rho_ratio) * b->inertia;
+/* Fluid momentum and angular momentum inside the body (rho_f = 1), with the
+ * volume fraction of node x taken as clamp(R + 1/2 - |x - xc|, 0, 1) and the
+ * velocity after the forced collision, u + F/(2 rho) (the whole IBM impulse
+ * of this step): out = {sum a u, sum a (x - xc) x u}, over the box in k, j, i
+ * order. */
+void orc_internal_momentum(orc *o, const double xc[3], double R, const int lo[3], const int hi[3], double out[6]) {
+    double s[6] = {0, 0, 0, 0, 0, 0};
+    for (int k = lo[2]; k <= hi[2]; k++)
+        for (int j = lo[1]; j <= hi[1]; j++)
+            for (int i = lo[0]; i <= hi[0]; i++) {
+                double rx = i - xc[0], ry = j - xc[1], rz = k - xc[2];
+                double a = R + 0.5 - sqrt(rx * rx + ry * ry + rz * rz);
+                if (a <= 0) continue;
+                if (a > 1) a = 1;
+                long c = IDX(o, i, j, k);
+                /* momentum after the forced collision: u + F / (2 rho) */
+                double hr = 0.5 / o->rho[c];
+                double ux = o->ux[c] + hr * o->Fx[c], uy = o->uy[c] + hr * o->Fy[c], uz = o->uz[c] + hr * o->Fz[c];
+                s[0] += a * ux; s[1] += a * uy; s[2] += a * uz;
+                s[3] += a * (ry * uz - rz * uy);
+                s[4] += a * (rz * ux - rx * uz);
+                s[5] += a * (rx * uy - ry * ux);
+            }
+    for (int q = 0; q < 6; q++) out[q] = s[q];
+}
+
+/* Newton-Euler step (dt = 1, rho_f = 1) with the internal-fluid treatment of
+ * Kempe & Froehlich (J. Comput. Phys. 231, 2012):
+ *   rho_s V_s dV/dt   = F_h + d/dt(int u dV) + (rho_s - rho_f) V_s g
+ *   I_p dOmega/dt     = T_h + d/dt(int r x u dV)
+ * F_h, T_h: reaction of the IBM forces (sum of -F_m ds); the internal terms
+ * are differenced between consecutive steps.  Degrees of freedom not set in
+ * dof keep their velocity.  x_c' = x_c + (V + V')/2; markers follow x_c and
+ * rotate with Omega' (r' = r + Omega' x r, rescaled to radius R); desired
+ * marker velocity V' + Omega' x r'. */
+void orc_body_step(orc_body *b, orc_markers *mk, double R, const double force[6], const double internal[6]) {
+    if (!b->have_prev) {
+        for (int q = 0; q < 6; q++) b->internal_prev[q] = internal[q];
+        b->have_prev = 1;
+    }
+    double mass = b->rho_ratio * b->vol;
     double vn[3], dxc[3];
     for (int a = 0; a < 3; a++) {
-        vn[a] = b->v[a] + (force[a] / mrel + b->grav[a]);
-        b->om[a] = b->om[a] + force[3 + a] / irel;
+        double dI = internal[a] - b->internal_prev[a];
+        double dL = internal[3 + a] - b->internal_prev[3 + a];
+        vn[a] = ((b->dof >> a) & 1)
+                    ? b->v[a] + (force[a] + dI) / mass + (1.0 - 1.0 / b->rho_ratio) * b->grav[a]
+                    : b->v[a];
+        if ((b->dof >> (3 + a)) & 1) b->om[a] = b->om[a] + (force[3 + a] + dL) / b->inertia;
         dxc[a] = 0.5 * (b->v[a] + vn[a]);
         b->xc[a] += dxc[a];
         b->v[a] = vn[a];
     }
+    for (int q = 0; q < 6; q++) b->internal_prev[q] = internal[q];
     for (int m = 0; m < mk->n; m++) {
         double r0 = mk->x[m] - (b->xc[0] - dxc[0]);
         double r1 = mk->y[m] - (b->xc[1] - dxc[1]);

@@ -1,0 +1,80 @@
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+The reference's own lbm.cpp is compiled unmodified by oracle/build_ref.sh
+(with oracle/ref_config.h and oracle/ref_harness.cpp) and run here; its
+outputs are stored as small .npz fixtures:
+
+  cavity12_tau0.8_lid0.05_200.npz   D3Q19 lid-driven cavity 12^3, 200 steps:
+                                    full interior rho, ux, uy, uz
+  cavity64_tau0.8_lid0.05_5000.npz  the 64^3, tau = 0.8, 5000-step cavity:
+                                    mid planes k = 32 and i = 32 of rho, u,
+                                    plus interior sums and maxima
+  cylinder80x40_D10_n40_m5_100.npz  D2Q9 implicit-IBM cylinder (the shipped
+                                    default case shrunk): rho, ux, uy, Fx, Fy
+                                    on the k = 1 layer, Cl and Cd per step
+
+Run from the repository root:  python tests/golden/gen_golden.py
+(needs the reference tree; the 64^3 case takes a few minutes on 8 cores;
+--cav64-dump PATH reuses a dump the harness already wrote).
+"""
+from __future__ import annotations
+
+import argparse
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402
+
+OUT = os.path.dirname(os.path.abspath(__file__))
+REF = os.path.join(ROOT, "oracle", "_ref")
+
+
+def run(exe: str, args: list[str]) -> None:
+    subprocess.check_call([os.path.join(REF, exe)] + args)
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--cav64-dump", default=None)
+    ap.add_argument("--skip-cav64", action="store_true")
+    a = ap.parse_args()
+    oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5")
+    tmp = tempfile.mkdtemp()
+
+    # 12^3 cavity, 200 steps
+    p = os.path.join(tmp, "cav12.bin")
+    run("ref_cavity_12_0.8", ["200", p, "0.05"])
+    f = oracle.read_ref_dump(p, 14, 14, 14, 4)["fields"][:, 1:-1, 1:-1, 1:-1]
+    np.savez_compressed(os.path.join(OUT, "cavity12_tau0.8_lid0.05_200.npz"), rho=f[0], ux=f[1], uy=f[2], uz=f[3],
+                        n=12, tau=0.8, lid=0.05, steps=200)
+
+    # 64^3 cavity, 5000 steps
+    if not a.skip_cav64:
+        p = a.cav64_dump or os.path.join(tmp, "cav64.bin")
+        if not a.cav64_dump:
+            run("ref_cavity_64_0.8", ["5000", p, "0.05"])
+        f = oracle.read_ref_dump(p, 66, 66, 66, 4)["fields"][:, 1:-1, 1:-1, 1:-1]
+        np.savez_compressed(os.path.join(OUT, "cavity64_tau0.8_lid0.05_5000.npz"),
+                            zmid=f[:, 32, :, :], xmid=f[:, :, :, 32], sums=f.reshape(4, -1).sum(axis=1),
+                            absmax=np.abs(f.reshape(4, -1)).max(axis=1), n=64, tau=0.8, lid=0.05, steps=5000)
+
+    # 2D implicit IBM cylinder, 100 steps
+    p = os.path.join(tmp, "cyl.bin")
+    steps = 100
+    run("ref_cylinder_80_40_10_40_5", [str(steps), p])
+    r = oracle.read_ref_dump(p, 82, 42, 3, 7, steps, 40)
+    fl = r["fields"][:, 1]  # k = 1 layer
+    np.savez_compressed(os.path.join(OUT, "cylinder80x40_D10_n40_m5_100.npz"), rho=fl[0], ux=fl[1], uy=fl[2],
+                        Fx=fl[4], Fy=fl[5], cl=r["cl"], cd=r["cd"], markers=r["markers"], nx=80, ny=40, D=10.0,
+                        nodes=40, m_max=5, steps=steps)
+    print("golden fixtures written to", OUT)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,92 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, exports
+every entry point include/lbmgpu.h declares, maps the reference's per-cell
+geometry to face descriptors, and fails loudly (status codes, never a
+crash) when no device is usable."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+
+def _declared():
+    txt = open(os.path.join(ROOT, "include", "lbmgpu.h")).read()
+    return sorted(set(re.findall(r"\b(lbmgpu_\w+)\s*\(", txt)))
+
+
+def test_exports_every_declared_symbol(pkg):
+    L = pkg.load()
+    declared = _declared()
+    assert len(declared) >= 20
+    for name in declared:
+        assert hasattr(L, name), name
+    assert sorted(pkg.ABI_SYMBOLS) == declared
+    assert L.lbmgpu_abi_version() == 1
+
+
+def _ref_geometry(nx, ny, nz):
+    NX, NY, NZ = nx + 2, ny + 2, nz + 2
+    t = np.zeros((NZ, NY, NX), np.uint8)
+    z = np.zeros((NZ, NY, NX))
+    return t, z.copy(), z.copy(), z.copy(), z.copy()
+
+
+def test_config_from_types_cavity(pkg):
+    t, rho, ux, uy, uz = _ref_geometry(8, 6, 5)
+    rho[:] = 1.0
+    t[:] = 1
+    t[1:-1, 1:-1, 1:-1] = 0
+    ux[:, -1, :] = 0.05  # lid plane j = Ny+1
+    cfg = pkg.config_from_types(8, 6, 5, 0.8, t, rho, ux, uy, uz)
+    assert (cfg.nx, cfg.ny, cfg.nz) == (8, 6, 5)
+    assert [cfg.faces[f].kind for f in range(6)] == [pkg.FACE_WALL] * 6
+    assert cfg.faces[3].u[0] == 0.05 and cfg.faces[2].u[0] == 0.0
+
+
+def test_config_from_types_channel_and_periodic(pkg):
+    # Sphere_BB / IBM style: TYPE_IN at x=0, TYPE_OUT elsewhere on the ghosts
+    t, rho, ux, uy, uz = _ref_geometry(10, 6, 6)
+    rho[:] = 1.0
+    ux[:] = 0.1
+    t[:, :, 0] = 3
+    t[:, :, -1] = 2
+    t[:, 0, 1:-1] = 2
+    t[:, -1, 1:-1] = 2
+    t[0, 1:-1, 1:-1] = 2
+    t[-1, 1:-1, 1:-1] = 2
+    cfg = pkg.config_from_types(10, 6, 6, 0.6, t, rho, ux, uy, uz)
+    assert cfg.faces[0].kind == pkg.FACE_INLET and cfg.faces[1].kind == pkg.FACE_OUTLET_EQ
+    assert cfg.faces[0].u[0] == 0.1
+    # Couette style (lbm.cpp:1537-1555): TYPE_F ghosts in x and z wrap over N+2
+    t, rho, ux, uy, uz = _ref_geometry(2, 12, 2)
+    rho[:] = 1.0
+    t[:, 0, :] = 1
+    t[:, -1, :] = 1
+    ux[:, -1, :] = 0.02
+    cfg = pkg.config_from_types(2, 12, 2, 0.9, t, rho, ux, uy, uz)
+    assert (cfg.nx, cfg.ny, cfg.nz) == (4, 12, 4)
+    assert cfg.faces[0].kind == pkg.FACE_PERIODIC and cfg.faces[4].kind == pkg.FACE_PERIODIC
+    assert cfg.faces[3].kind == pkg.FACE_WALL and cfg.faces[3].u[0] == 0.02
+
+
+def test_config_from_types_rejects_interior_solid(pkg):
+    t, rho, ux, uy, uz = _ref_geometry(6, 6, 6)
+    t[:] = 1
+    t[1:-1, 1:-1, 1:-1] = 0
+    t[3, 3, 3] = 1
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.config_from_types(6, 6, 6, 0.8, t, rho, ux, uy, uz)
+    assert e.value.status == 7
+
+
+def test_create_rejects_bad_config_without_touching_device(pkg):
+    cfg = pkg.cavity_config(8, tau=0.5)
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(cfg)
+    assert e.value.status == 1
+    cfg = pkg.cavity_config(8)
+    cfg.faces[0].kind = pkg.FACE_PERIODIC
+    with pytest.raises(pkg.LbmError):
+        pkg.Solver(cfg)

@@ -1,0 +1,94 @@
+"""The FP64 oracle against golden vectors produced by the reference itself.
+
+The fixtures in tests/golden/ come from the reference's own lbm.cpp, built
+unmodified by oracle/build_ref.sh and run by tests/golden/gen_golden.py.
+These pin the restatement in oracle/lbm_oracle.c: the D3Q19 cavity path
+(Init, Collision, Streaming with moving-wall bounce-back, MacroProp) and the
+D2Q9 implicit IBM path (IBLBM with the reference's sign and rho_near
+conventions, added mass, Cl/Cd).
+"""
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+
+def test_cavity12_matches_reference(orc):
+    g = np.load(os.path.join(GOLDEN, "cavity12_tau0.8_lid0.05_200.npz"))
+    lat = orc.cavity(int(g["n"]), float(g["tau"]), float(g["lid"]))
+    assert lat.step_plain(int(g["steps"])) == 0
+    lid = float(g["lid"])
+    assert np.abs(lat.interior(lat.rho) - g["rho"]).max() < 1e-12
+    for c in ("ux", "uy", "uz"):
+        assert np.abs(lat.interior(getattr(lat, c)) - g[c]).max() / lid < 1e-12
+
+
+def _cylinder_literal(orc, g, steps):
+    nx, ny, D, nodes, mm = int(g["nx"]), int(g["ny"]), float(g["D"]), int(g["nodes"]), int(g["m_max"])
+    u_max = 0.1
+    nu = u_max * D / 40.0
+    tau = 0.5 + nu / (1.0 / 3.0)
+    lat = orc.Lattice(9, nx, ny, 1, tau)
+    t = lat.types
+    # main_setup_Cylinder_IBM (lbm.cpp:1828-1854)
+    t[:] = orc.TYPE_F
+    t[:, :, 0] = orc.TYPE_IN
+    t[:, :, -1] = orc.TYPE_OUT
+    t[:, 0, :] = orc.TYPE_OUT
+    t[:, -1, :] = orc.TYPE_OUT
+    lat.ux[:] = u_max
+    lat.init()
+    cx, cy = nx / 5.0, ny / 2.0
+    mk = orc.cylinder_markers_literal(nodes, D, cx, cy)
+    lo = [math.floor(cx - D), math.floor(cy - D), 1]
+    hi = [math.ceil(cx + D), math.ceil(cy + D), 1]
+    op = orc.ibm_opts(lo, hi, mm, lit_sign=1, rho_mode=1)
+    op.use_avg_density = 1
+    op.vsolid = orc.REF_PI * D * D * 0.25
+    cl, cd = [], []
+    for _ in range(steps):
+        out = lat.step_ibm(mk, op, [cx, cy, 1.0])
+        cl.append(out[1] / (0.5 * u_max ** 2 * D))
+        cd.append(out[0] / (0.5 * u_max ** 2 * D))
+    return lat, mk, np.array(cl), np.array(cd)
+
+
+def test_cylinder_ibm_matches_reference(orc):
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    lat, mk, cl, cd = _cylinder_literal(orc, g, int(g["steps"]))
+    assert np.abs(mk["x"] - g["markers"][:, 0]).max() == 0.0
+    assert np.abs(mk["nx"] - g["markers"][:, 3]).max() == 0.0
+    assert np.abs(mk["ds"] - g["markers"][:, 6]).max() == 0.0
+    for name, arr in (("rho", lat.rho), ("ux", lat.ux), ("uy", lat.uy), ("Fx", lat.Fx), ("Fy", lat.Fy)):
+        assert np.abs(arr[1] - g[name]).max() < 1e-12, name
+    assert np.abs(cd - g["cd"]).max() < 1e-10
+    assert np.abs(cl - g["cl"]).max() < 1e-10
+
+
+def test_kernel_is_peskin_4pt(orc):
+    L = orc.lib()
+    # partition of unity and first moment of the 4-point delta
+    for r0 in (0.0, 0.1, 0.37, 0.5, 0.93):
+        w = [L.orc_kernel(r0 - k) for k in range(-2, 3)]
+        assert abs(sum(w) - 1.0) < 1e-14
+        assert abs(sum(wi * (r0 - k) for wi, k in zip(w, range(-2, 3)))) < 1e-14
+    assert L.orc_kernel(2.0) == 0.0 and L.orc_kernel(-2.5) == 0.0
+
+
+def test_reference_literal_build_agrees_live(orc, tmp_path):
+    """When the reference tree is present, rebuild and rerun it for a fresh case."""
+    exe = os.path.join(orc.HERE, "_ref", "ref_cavity_12_0.8")
+    if not os.path.exists(exe):
+        pytest.skip("reference-literal oracle not built (no reference tree on this machine)")
+    import subprocess
+
+    out = str(tmp_path / "c.bin")
+    subprocess.check_call([exe, "37", out, "0.03"], stdout=subprocess.DEVNULL)
+    r = orc.read_ref_dump(out, 14, 14, 14, 4)["fields"]
+    lat = orc.cavity(12, 0.8, 0.03)
+    lat.step_plain(37)
+    for w, a in enumerate((lat.rho, lat.ux, lat.uy, lat.uz)):
+        assert np.abs(lat.interior(a) - r[w][1:-1, 1:-1, 1:-1]).max() < 1e-13
