@@ -48,7 +48,8 @@ class Config(C.Structure):
                 ("faces", Face * 6), ("rho0", C.c_double), ("u0", C.c_double * 3),
                 ("body_force", C.c_double * 3), ("thermal", C.c_int), ("tau_g", C.c_double),
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
-                ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int)]
+                ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
+                ("ibm_fused", C.c_int)]
 
 
 class IbmConfig(C.Structure):
@@ -120,7 +121,7 @@ def _dp(a: np.ndarray):
 
 def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0.0, 0.0), body=(0.0, 0.0, 0.0),
                 thermal=False, tau_g=0.0, T_init=0.0, T_ref=0.0, gbeta=(0.0, 0.0, 0.0), block=(0, 0),
-                graph_steps=0) -> Config:
+                graph_steps=0, staged=0, ibm_fused=0) -> Config:
     c = Config()
     c.nx, c.ny, c.nz, c.tau = nx, ny, nz, tau
     c.storage = STORAGE[storage] if isinstance(storage, str) else storage
@@ -141,6 +142,8 @@ def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0
     c.tau_g, c.T_init, c.T_ref = tau_g, T_init, T_ref
     c.block_x, c.block_y = block
     c.graph_steps = graph_steps
+    c.staged = staged
+    c.ibm_fused = ibm_fused
     return c
 
 

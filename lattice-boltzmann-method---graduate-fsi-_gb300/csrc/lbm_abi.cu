@@ -16,6 +16,7 @@
 using namespace lbmk;
 
 static thread_local std::string g_err;
+static constexpr size_t kGuard = 256;  // cells of slack before the first population array
 
 static lbm_status fail(lbm_status s, const std::string &msg) {
     g_err = msg;
@@ -33,8 +34,10 @@ struct lbm_handle {
     StepParams P;
     cudaStream_t s = nullptr;
     size_t esize = 4;
-    void *f[2] = {nullptr, nullptr};
+    void *f[2] = {nullptr, nullptr};   // population buffers A/B (past the guard)
     void *g[2] = {nullptr, nullptr};
+    void *fraw[2] = {nullptr, nullptr}; // allocations
+    void *graw[2] = {nullptr, nullptr};
     int cur = 0;
     float *mom = nullptr;
     float *band = nullptr;
@@ -52,6 +55,9 @@ struct lbm_handle {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;
     int tx = 128, ty = 2;
+    TmaPlan tma;
+    FusedPlan fused;
+    int use_fused = 1;
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
@@ -182,7 +188,7 @@ extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double ta
                                                const double *rho, const double *ux, const double *uy,
                                                const double *uz, const double *T, lbm_config *out) {
     if (!types || !out || nx < 1 || ny < 1 || nz < 1) return fail(LBM_ERR_INVALID, "config_from_types: bad arguments");
-    const int NX = nx + 2, NY = ny + 2, NZ = nz + 2;
+    const int NX = nx + 2, NY = ny + 2;
     auto at = [&](int i, int j, int k) { return (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k); };
     lbm_config c;
     memset(&c, 0, sizeof(c));
@@ -250,8 +256,8 @@ static void free_handle(lbm_handle *h) {
     if (!h) return;
     for (int i = 0; i < 2; i++) {
         if (h->gexec[i]) cudaGraphExecDestroy(h->gexec[i]);
-        if (h->f[i]) cudaFree(h->f[i]);
-        if (h->g[i]) cudaFree(h->g[i]);
+        if (h->fraw[i]) cudaFree(h->fraw[i]);
+        if (h->graw[i]) cudaFree(h->graw[i]);
     }
     cudaFree(h->mom);
     cudaFree(h->band);
@@ -325,10 +331,21 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         }
     };
     chk(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking), "stream");
-    const size_t fb = (size_t)Q * P.N * h->esize;
-    for (int i = 0; i < 2 && st == LBM_OK; i++) chk(dalloc(h, &h->f[i], fb), "populations");
+    // Population arrays: stride S = N rounded up to 256 cells plus 512 cells
+    // of slack (a tile-wide over-read past the last row stays inside the
+    // array, and the 19 streams do not sit at power-of-two distances), and a
+    // guard of kGuard cells before the first array.
+    P.S = ((P.N + 255) / 256) * 256 + 512;
+    const size_t fb = ((size_t)Q * P.S + 2 * kGuard) * h->esize;
+    for (int i = 0; i < 2 && st == LBM_OK; i++) {
+        chk(dalloc(h, &h->fraw[i], fb), "populations");
+        if (st == LBM_OK) h->f[i] = (char *)h->fraw[i] + kGuard * h->esize;
+    }
     if (c.thermal)
-        for (int i = 0; i < 2 && st == LBM_OK; i++) chk(dalloc(h, &h->g[i], (size_t)QT * P.N * h->esize), "thermal");
+        for (int i = 0; i < 2 && st == LBM_OK; i++) {
+            chk(dalloc(h, &h->graw[i], ((size_t)QT * P.S + 2 * kGuard) * h->esize), "thermal");
+            if (st == LBM_OK) h->g[i] = (char *)h->graw[i] + kGuard * h->esize;
+        }
     if (st == LBM_OK) chk(dalloc(h, &h->mom, (size_t)5 * P.N * sizeof(float)), "moments");
     if (st == LBM_OK) chk(dalloc(h, &h->ds, sizeof(DevState)), "state");
     if (st == LBM_OK) chk(dalloc(h, &h->hist, (size_t)h->hist_cap * 8 * sizeof(double)), "history");
@@ -340,6 +357,8 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaMemsetAsync(h->hist, 0, (size_t)h->hist_cap * 8 * sizeof(double), h->s), "history init");
     }
     for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
+    if (st == LBM_OK && c.staged >= 0) chk(plan_tma(c.storage, c.thermal != 0, P, c.staged, h->tma), "staged plan");
+    h->use_fused = c.ibm_fused >= 0 ? 1 : 0;
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);
@@ -359,7 +378,7 @@ extern "C" lbm_status lbmgpu_destroy(lbm_handle *h) {
 static lbm_status do_init(lbm_handle *h, const float *dfields) {
     float init[5] = {(float)h->cfg.rho0, (float)h->cfg.u0[0], (float)h->cfg.u0[1], (float)h->cfg.u0[2],
                      (float)h->cfg.T_init};
-    CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, dfields, init, h->cfg.thermal != 0, h->s));
+    CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, h->P.S, dfields, init, h->cfg.thermal != 0, h->s));
     h->cur = 0;
     h->steps = 0;
     h->inited = true;
@@ -475,6 +494,8 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
     h->ibm = true;
+    h->fused.enabled = 0;
+    if (h->use_fused) CUDA_TRY(plan_ibm_fused(h->cfg.storage, h->cfg.thermal != 0, h->P, n, h->fused));
     // graphs captured earlier do not contain the IBM launches
     for (int i = 0; i < 2; i++)
         if (h->gexec[i]) {
@@ -503,6 +524,7 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.thermal = h->cfg.thermal;
     a.tx = h->tx;
     a.ty = h->ty;
+    a.tma = h->tma;
     a.stream = h->s;
     return a;
 }
@@ -522,12 +544,19 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaE
         ia.band = h->band;
         ia.thermal = h->icfg.thermal;
         ia.stream = h->s;
-        for (int it = 1; it <= h->icfg.m_max; it++) {
-            if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
-            if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
+        const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
+        if (h->fused.enabled) {
+            if ((e = launch_ibm_fused(h->cfg.storage, h->cfg.thermal != 0, ia, h->fused, a.B, a.GB, h->bp, h->hist,
+                                      h->hist_cap, h->icfg.m_max, fsign)) != cudaSuccess)
+                return e;
+        } else {
+            for (int it = 1; it <= h->icfg.m_max; it++) {
+                if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
+                if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
+            }
+            if ((e = launch_band_collide(h->cfg.storage, a, fsign)) != cudaSuccess) return e;
+            if ((e = launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap)) != cudaSuccess) return e;
         }
-        if ((e = launch_band_collide(h->cfg.storage, a, h->icfg.literal_sign ? -1.0f : 1.0f)) != cudaSuccess) return e;
-        if ((e = launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap)) != cudaSuccess) return e;
     }
     h->cur = 1 - h->cur;
     return cudaSuccess;

@@ -5,9 +5,9 @@
 // links are D3Q19 links 0..6.
 //
 // Storage: populations are kept shifted, f~ = f - w (and g unshifted), in
-// float, __half or __nv_bfloat16, structure-of-arrays: pop[l * N + cell] with
-// cell = x + nx * (y + ny * z) over interior cells only.  All arithmetic is
-// FP32.
+// float, __half or __nv_bfloat16, structure-of-arrays: pop[l * S + cell] with
+// cell = x + nx * (y + ny * z) over interior cells only and a padded stride
+// S >= N.  All arithmetic is FP32.
 #pragma once
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
@@ -46,16 +46,19 @@ struct St;
 template <>
 struct St<float> {
     static __device__ __forceinline__ float ld(const float *p) { return __ldg(p); }
+    static __device__ __forceinline__ float lds(const float *p) { return *p; }
     static __device__ __forceinline__ void st(float *p, float v) { *p = v; }
 };
 template <>
 struct St<__half> {
     static __device__ __forceinline__ float ld(const __half *p) { return __half2float(__ldg(p)); }
+    static __device__ __forceinline__ float lds(const __half *p) { return __half2float(*p); }
     static __device__ __forceinline__ void st(__half *p, float v) { *p = __float2half_rn(v); }
 };
 template <>
 struct St<__nv_bfloat16> {
     static __device__ __forceinline__ float ld(const __nv_bfloat16 *p) { return __bfloat162float(__ldg(p)); }
+    static __device__ __forceinline__ float lds(const __nv_bfloat16 *p) { return __bfloat162float(*p); }
     static __device__ __forceinline__ void st(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
 };
 
@@ -75,6 +78,7 @@ struct StepParams {
     int nx, ny, nz;
     int periodic;          // bit a: axis a periodic
     long long N;           // nx * ny * nz
+    long long S;           // population stride (>= N + one tile of slack, see lbm_abi.cu)
     float omega;           // dt / tau
     float omega_t;         // dt / tau_g
     float body[3];         // uniform body force
@@ -106,6 +110,7 @@ enum : uint32_t {
     ST_BAND_EDGE = 2u,      // a marker stencil left the band / interior
     ST_NONFINITE_FORCE = 4u,
     ST_FEQ_NEG = 8u,
+    ST_TIMEOUT = 16u,       // a bounded mbarrier wait gave up
 };
 
 __device__ __forceinline__ int cell_class(int x, int y, int z, const StepParams &P) {

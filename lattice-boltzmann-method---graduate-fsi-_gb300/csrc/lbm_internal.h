@@ -7,6 +7,15 @@
 
 namespace lbmk {
 
+// Launch plan of the staged (bulk-copy) step kernel; enabled = 0 falls back
+// to the direct-load kernel.
+struct TmaPlan {
+    int enabled = 0;
+    int tx = 0, tiles_x = 0, grid = 0, per_sm = 0;
+    long long ntiles = 0;
+    size_t smem = 0;
+};
+
 struct LaunchArgs {
     const StepParams *P;
     const void *A;
@@ -20,13 +29,15 @@ struct LaunchArgs {
     int export_only;
     int thermal;
     int tx, ty;
+    TmaPlan tma;
     cudaStream_t stream;
 };
 
 cudaError_t launch_step(int storage, const LaunchArgs &a);
+cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int tx_pref, TmaPlan &tp);
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign);
-cudaError_t launch_init(int storage, void *A, void *GA, long long N, const float *fields, const float init[5],
-                        bool thermal, cudaStream_t s);
+cudaError_t launch_init(int storage, void *A, void *GA, long long N, long long S, const float *fields,
+                        const float init[5], bool thermal, cudaStream_t s);
 
 // Immersed-boundary marker set on the device.
 struct MarkerDev {
@@ -65,5 +76,16 @@ struct BodyParams {
     int dof;           // bits 0-2 translation, 3-5 rotation
 };
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap);
+
+// Single-launch IBM phase on one thread-block cluster (k_ibm_fused).
+struct FusedPlan {
+    int enabled = 0;
+    int cl = 0, slab = 0, nloc_max = 0;
+    size_t smem = 0;
+};
+cudaError_t plan_ibm_fused(int storage, bool thermal, const StepParams &P, int n_markers, FusedPlan &fp);
+cudaError_t launch_ibm_fused(int storage, bool lattice_thermal, const IbmArgs &a, const FusedPlan &fp, void *B,
+                             void *GB, const BodyParams &bp, double *hist, long long hist_cap, int m_max,
+                             float fsign);
 
 }  // namespace lbmk

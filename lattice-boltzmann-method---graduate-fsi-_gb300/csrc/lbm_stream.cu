@@ -12,6 +12,7 @@
 // through a per-boundary-class table (see ClassEntry).  Cells inside the IBM
 // band store their pre-collision populations and unforced moments instead;
 // k_band_collide finishes them once the IBM forcing is known.
+#include "lbm_collide.cuh"
 #include "lbm_device.cuh"
 #include "lbm_internal.h"
 
@@ -21,17 +22,16 @@ template <class T>
 __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q], int x, int y, int z,
                                             long long cell, int raw_cls, bool valid, bool bwarp, int gather,
                                             const StepParams &P) {
-    const long long N = P.N;
     if (!gather) {
 #pragma unroll
-        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(A + l * N + cell) : 0.0f;
+        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(A + l * P.S + cell) : 0.0f;
         return;
     }
     if (!bwarp) {
 #pragma unroll
         for (int l = 0; l < Q; l++) {
             const long long off = (long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l));
-            f[l] = valid ? St<T>::ld(A + l * N + cell - off) : 0.0f;
+            f[l] = valid ? St<T>::ld(A + l * P.S + cell - off) : 0.0f;
         }
         return;
     }
@@ -42,7 +42,7 @@ __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q],
         float v = 0.0f;
         if (valid) {
             if ((ce.bb >> l) & 1u) {
-                v = St<T>::ld(A + opp(l) * N + cell) + ce.val[l];
+                v = St<T>::ld(A + opp(l) * P.S + cell) + ce.val[l];
             } else if ((ce.eq >> l) & 1u) {
                 v = ce.val[l];
             } else {
@@ -57,7 +57,7 @@ __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q],
                     sy = min(max(sy, 0), P.ny - 1);
                     sz = min(max(sz, 0), P.nz - 1);
                 }
-                v = St<T>::ld(A + l * N + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+                v = St<T>::ld(A + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
             }
         }
         f[l] = v;
@@ -68,17 +68,16 @@ template <class T>
 __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT], int x, int y, int z,
                                             long long cell, int raw_cls, bool valid, bool bwarp, int gather,
                                             const StepParams &P) {
-    const long long N = P.N;
     if (!gather) {
 #pragma unroll
-        for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(G + l * N + cell) : 0.0f;
+        for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(G + l * P.S + cell) : 0.0f;
         return;
     }
     if (!bwarp) {
 #pragma unroll
         for (int l = 0; l < QT; l++) {
             const long long off = (long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l));
-            g[l] = valid ? St<T>::ld(G + l * N + cell - off) : 0.0f;
+            g[l] = valid ? St<T>::ld(G + l * P.S + cell - off) : 0.0f;
         }
         return;
     }
@@ -89,7 +88,7 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
         float v = 0.0f;
         if (valid) {
             if ((ce.bb >> l) & 1u) {
-                float own = St<T>::ld(G + opp(l) * N + cell);
+                float own = St<T>::ld(G + opp(l) * P.S + cell);
                 v = ((ce.tdir >> l) & 1u) ? (-own + ce.tval[l]) : own;
             } else if ((ce.eq >> l) & 1u) {
                 v = ce.tval[l];
@@ -105,71 +104,21 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
                     sy = min(max(sy, 0), P.ny - 1);
                     sz = min(max(sz, 0), P.nz - 1);
                 }
-                v = St<T>::ld(G + l * N + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+                v = St<T>::ld(G + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
             }
         }
         g[l] = v;
     }
 }
 
-// BGK + Guo collision on shifted populations (f~ = f - w), FP32:
-//   f~* = (1 - omega) f~ + omega (feq - w) + S,
-//   feq - w = w (drho + rho P3(u)) with the third-order P3 of Calc_feq
-//   (lbm.cpp:628-633), S = (1 - omega/2) w (3 c.F + 9 (c.F)(c.u) - 3 F.u)
-//   (lbm.cpp:101-102).
-__device__ __forceinline__ void collide_flow(float f[Q], float drho, float ux, float uy, float uz, float Fx,
-                                             float Fy, float Fz, bool forced, float omega) {
-    const float rho = 1.0f + drho;
-    const float usq = ux * ux + uy * uy + uz * uz;
-    const float c1 = 1.0f - omega;
-    const float gs = 1.0f - 0.5f * omega;
-    const float Fu = Fx * ux + Fy * uy + Fz * uz;
-#pragma unroll
-    for (int l = 0; l < Q; l++) {
-        const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
-        const float p3 = cu * (3.0f + 4.5f * cu + 4.5f * cu * cu - 4.5f * usq) - 1.5f * usq;
-        float out = c1 * f[l] + omega * wf(l) * (drho + rho * p3);
-        if (forced) {
-            const float cF = cx(l) * Fx + cy(l) * Fy + cz(l) * Fz;
-            out += gs * wf(l) * (3.0f * cF + 9.0f * cF * cu - 3.0f * Fu);
-        }
-        f[l] = out;
-    }
-}
-
-// D3Q7 BGK with source: g* = g - omega_t (g - w T (1 + 4 c.u)) + (1 - omega_t/2) w Qh.
-__device__ __forceinline__ void collide_heat(float g[QT], float T, float ux, float uy, float uz, float Qh,
-                                             float omega_t) {
-    const float gsrc = 1.0f - 0.5f * omega_t;
-#pragma unroll
-    for (int l = 0; l < QT; l++) {
-        const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
-        const float geq = wtf(l) * T * (1.0f + 4.0f * cu);
-        g[l] = g[l] - omega_t * (g[l] - geq) + gsrc * wtf(l) * Qh;
-    }
-}
-
-// Fused step.  gather = 0 on the first step (A then holds the initial
-// pre-collision populations in place); export_only = 1 computes and writes
-// the moments of the gathered state without colliding or storing.
+// Everything after the gather of one cell: moments, optional moment output,
+// band hand-off or collision, and the stores to B.
 template <class T, bool THERMAL>
-__global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
-                                              T *__restrict__ GB, const __grid_constant__ StepParams P,
-                                              DevState *__restrict__ ds, float *__restrict__ mom,
-                                              float *__restrict__ band, int gather, int export_only) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    const bool valid = (x < P.nx) && (y < P.ny);
+__device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
+                                            int gather, int export_only, T *__restrict__ B, T *__restrict__ GB,
+                                            const StepParams &P, DevState *__restrict__ ds, float *__restrict__ mom,
+                                            float *__restrict__ band) {
     const long long N = P.N;
-    const long long cell = valid ? (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z) : 0;
-    const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
-                             (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
-                          : 0;
-    const bool bwarp = __any_sync(0xffffffffu, raw != 0);
-
-    float f[Q];
-    gather_flow<T>(A, f, x, y, z, cell, raw, valid, bwarp, gather, P);
     float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
 #pragma unroll
     for (int l = 0; l < Q; l++) {
@@ -178,11 +127,9 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
         jy += cy(l) * f[l];
         jz += cz(l) * f[l];
     }
-    float g[QT];
     float Tc = 0.0f;
     float Fx = P.body[0], Fy = P.body[1], Fz = P.body[2];
     if (THERMAL) {
-        gather_heat<T>(GA, g, x, y, z, cell, raw, valid, bwarp, gather, P);
 #pragma unroll
         for (int l = 0; l < QT; l++) Tc += g[l];
         Fx += P.gbeta[0] * (Tc - P.T0);
@@ -190,7 +137,7 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
         Fz += P.gbeta[2] * (Tc - P.T0);
     }
     const float rho = 1.0f + drho;
-    const float inv = 1.0f / rho;
+    const float inv = inv_one_plus(drho);
     // Before the first streaming the reference collides with the velocity
     // stored at set-up (LBM::Init, lbm.cpp:31-57), i.e. without the F/2 shift
     // that MacroProp applies afterwards (lbm.cpp:677-679).
@@ -214,10 +161,10 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
             const long long nb = P.nb;
             const long long b = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
 #pragma unroll
-            for (int l = 0; l < Q; l++) St<T>::st(B + l * N + cell, f[l]);
+            for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
             if (THERMAL) {
 #pragma unroll
-                for (int l = 0; l < QT; l++) St<T>::st(GB + l * N + cell, g[l]);
+                for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
             }
             band[b] = drho;
             band[nb + b] = ux;
@@ -236,11 +183,201 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
     }
     collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, P.forced != 0, P.omega);
 #pragma unroll
-    for (int l = 0; l < Q; l++) St<T>::st(B + l * N + cell, f[l]);
+    for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
     if (THERMAL) {
         collide_heat(g, Tc, ux, uy, uz, 0.0f, P.omega_t);
 #pragma unroll
-        for (int l = 0; l < QT; l++) St<T>::st(GB + l * N + cell, g[l]);
+        for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
+    }
+}
+
+// Fused step, direct global loads (any row length).  gather = 0 on the first
+// step (A then holds the initial pre-collision populations in place);
+// export_only = 1 computes and writes the moments of the gathered state
+// without colliding or storing.
+template <class T, bool THERMAL>
+__global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
+                                              T *__restrict__ GB, const __grid_constant__ StepParams P,
+                                              DevState *__restrict__ ds, float *__restrict__ mom,
+                                              float *__restrict__ band, int gather, int export_only) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const bool valid = (x < P.nx) && (y < P.ny);
+    const long long cell = valid ? (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z) : 0;
+    const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
+                             (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
+                          : 0;
+    const bool bwarp = __any_sync(0xffffffffu, raw != 0);
+    float f[Q], g[QT];
+    gather_flow<T>(A, f, x, y, z, cell, raw, valid, bwarp, gather, P);
+    if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, bwarp, gather, P);
+    finish_cell<T, THERMAL>(f, g, x, y, z, cell, valid, gather, export_only, B, GB, P, ds, mom, band);
+}
+
+// ---------------------------------------------------------------------------
+// Staged variant: a persistent kernel whose CTAs walk row tiles of TX cells.
+// For every tile one thread issues, per population, a bulk asynchronous copy
+// (cp.async.bulk, the TMA engine) of the source row segment into shared
+// memory -- TX cells, widened by one 16-byte group on the side the link
+// comes from -- and arms an mbarrier with the byte count.  kStages tiles are
+// in flight per CTA, so the bytes in flight no longer depend on registers.
+// Interior cells read their 19 (+7) pulled populations from shared memory;
+// cells on a domain face take the boundary-class path from global memory.
+// Rows on a y/z face stage nothing.  Requires nx and TX to be multiples of
+// 16 bytes' worth of cells.
+// ---------------------------------------------------------------------------
+constexpr int kStages = 4;
+constexpr long long kWaitLimit = 1ll << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait: true when the phase with this parity completed.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity) {
+    for (long long i = 0; i < kWaitLimit; i++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+template <class T, bool THERMAL>
+__global__ void __launch_bounds__(256) k_step_tma(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
+                                                  T *__restrict__ GB, const __grid_constant__ StepParams P,
+                                                  DevState *__restrict__ ds, float *__restrict__ band, int TX,
+                                                  int tiles_x, long long ntiles) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    constexpr int AL = 16 / (int)sizeof(T);
+    constexpr int NQ = THERMAL ? Q + QT : Q;
+    const int W = TX + AL;
+    const long long stage_elems = (long long)NQ * W;
+    T *stage_base = reinterpret_cast<T *>(smem);
+    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + ((kStages * stage_elems * (long long)sizeof(T) + 15) / 16) * 16);
+    __shared__ int s_ok;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int st = 0; st < kStages; st++) mbar_init(&bars[st], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    const long long G = gridDim.x;
+    const long long t0 = blockIdx.x;
+    const long long nloc = t0 < ntiles ? (ntiles - t0 + G - 1) / G : 0;
+
+    auto coords = [&](long long t, int &x0, int &y, int &z) {
+        const long long row = t / tiles_x;
+        x0 = (int)(t - row * tiles_x) * TX;
+        y = (int)(row % P.ny);
+        z = (int)(row / P.ny);
+    };
+    // one thread: arm the stage's barrier and issue the row copies of tile t
+    auto issue = [&](long long t, int st) {
+        int x0, y, z;
+        coords(t, x0, y, z);
+        const bool edge_row = (y == 0 || y == P.ny - 1 || z == 0 || z == P.nz - 1);
+        if (edge_row) {
+            mbar_arrive_expect_tx(&bars[st], 0);
+            return;
+        }
+        const uint32_t full = (uint32_t)((TX + AL) * sizeof(T)), narrow = (uint32_t)(TX * sizeof(T));
+        uint32_t bytes = 0;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const int l = q < Q ? q : q - Q;
+            bytes += cx(l) != 0 ? full : narrow;
+        }
+        mbar_arrive_expect_tx(&bars[st], bytes);
+        T *dst0 = stage_base + st * stage_elems;
+#pragma unroll
+        for (int q = 0; q < NQ; q++) {
+            const int l = q < Q ? q : q - Q;
+            const T *base = q < Q ? A : GA;
+            const int xs = cx(l) > 0 ? x0 - AL : x0;
+            const T *src = base + l * P.S + xs + (long long)P.nx * ((y - cy(l)) + (long long)P.ny * (z - cz(l)));
+            bulk_g2s(dst0 + (long long)q * W, src, cx(l) != 0 ? full : narrow, &bars[st]);
+        }
+    };
+
+    if (tid == 0)
+        for (long long k = 0; k < nloc && k < kStages; k++) issue(t0 + k * G, (int)k);
+
+    for (long long k = 0; k < nloc; k++) {
+        const int st = (int)(k % kStages);
+        const uint32_t parity = (uint32_t)((k / kStages) & 1);
+        if (tid == 0) s_ok = mbar_wait_bounded(&bars[st], parity) ? 1 : 0;
+        __syncthreads();
+        if (!s_ok) {
+            // the copies of this stage never landed: report, wait (bounded)
+            // for the other stages still in flight, and leave
+            if (tid == 0) {
+                atomicOr(&ds->status, ST_TIMEOUT);
+                for (long long j = k + 1; j < nloc && j < k + kStages; j++)
+                    mbar_wait_bounded(&bars[j % kStages], (uint32_t)((j / kStages) & 1));
+            }
+            return;
+        }
+        mbar_try_wait(&bars[st], parity);  // per-thread acquire of the staged data
+        const long long t = t0 + k * G;
+        int x0, y, z;
+        coords(t, x0, y, z);
+        const int x = x0 + tid;
+        const bool valid = tid < TX && x < P.nx;
+        const long long cell = valid ? (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z) : 0;
+        const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) |
+                                 (y == P.ny - 1 ? 8 : 0) | (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
+                              : 0;
+        float f[Q], g[QT];
+        if (raw == 0 && valid) {
+            const T *sb = stage_base + st * stage_elems;
+#pragma unroll
+            for (int l = 0; l < Q; l++) {
+                const int off = cx(l) > 0 ? AL - 1 : (cx(l) < 0 ? 1 : 0);
+                f[l] = St<T>::lds(sb + l * W + tid + off);
+            }
+            if (THERMAL) {
+#pragma unroll
+                for (int l = 0; l < QT; l++) {
+                    const int off = cx(l) > 0 ? AL - 1 : (cx(l) < 0 ? 1 : 0);
+                    g[l] = St<T>::lds(sb + (Q + l) * W + tid + off);
+                }
+            }
+        } else {
+            gather_flow<T>(A, f, x, y, z, cell, raw, valid, true, 1, P);
+            if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, true, 1, P);
+        }
+        finish_cell<T, THERMAL>(f, g, x, y, z, cell, valid, 1, 0, B, GB, P, ds, nullptr, band);
+        __syncthreads();  // every read of this stage is done
+        if (tid == 0 && k + kStages < nloc) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(t0 + (k + kStages) * G, st);
+        }
     }
 }
 
@@ -260,11 +397,11 @@ __global__ void __launch_bounds__(256) k_band_collide(T *__restrict__ B, T *__re
     const int bz = (int)(b / ((long long)P.bsx * P.bsy));
     const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
     if (x < 0 || y < 0 || z < 0 || x >= P.nx || y >= P.ny || z >= P.nz) return;
-    const long long N = P.N, nb = P.nb;
+    const long long nb = P.nb;
     const long long cell = x + (long long)P.nx * (y + (long long)P.ny * z);
     float f[Q];
 #pragma unroll
-    for (int l = 0; l < Q; l++) f[l] = St<T>::ld(B + l * N + cell);
+    for (int l = 0; l < Q; l++) f[l] = St<T>::ld(B + l * P.S + cell);
     const float drho = band[b];
     const float rho = 1.0f + drho;
     const float ftx = band[7 * nb + b], fty = band[8 * nb + b], ftz = band[9 * nb + b];
@@ -276,24 +413,24 @@ __global__ void __launch_bounds__(256) k_band_collide(T *__restrict__ B, T *__re
     const float Fz = band[6 * nb + b] + fsign * ftz;
     collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, true, P.omega);
 #pragma unroll
-    for (int l = 0; l < Q; l++) St<T>::st(B + l * N + cell, f[l]);
+    for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
     if (THERMAL) {
         float g[QT];
 #pragma unroll
-        for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * N + cell);
+        for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * P.S + cell);
         const float Qt = band[11 * nb + b];
         const float Tc = band[10 * nb + b] + 0.5f * Qt;
         collide_heat(g, Tc, ux, uy, uz, Qt, P.omega_t);
 #pragma unroll
-        for (int l = 0; l < QT; l++) St<T>::st(GB + l * N + cell, g[l]);
+        for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
     }
 }
 
 // Initial populations (LBM::Init, lbm.cpp:31-57): f = feq3(rho, u) stored
 // shifted, g = geq(T, u); from uniform values or per-cell host fields.
 template <class T, bool THERMAL>
-__global__ void k_init(T *__restrict__ A, T *__restrict__ GA, long long N, const float *__restrict__ fields,
-                       float rho0, float ux0, float uy0, float uz0, float T0) {
+__global__ void k_init(T *__restrict__ A, T *__restrict__ GA, long long N, long long S,
+                       const float *__restrict__ fields, float rho0, float ux0, float uy0, float uz0, float T0) {
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (c >= N) return;
     float drho = rho0 - 1.0f, ux = ux0, uy = uy0, uz = uz0, Tc = T0;
@@ -310,13 +447,13 @@ __global__ void k_init(T *__restrict__ A, T *__restrict__ GA, long long N, const
     for (int l = 0; l < Q; l++) {
         const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
         const float p3 = cu * (3.0f + 4.5f * cu + 4.5f * cu * cu - 4.5f * usq) - 1.5f * usq;
-        St<T>::st(A + l * N + c, wf(l) * (drho + rho * p3));
+        St<T>::st(A + l * S + c, wf(l) * (drho + rho * p3));
     }
     if (THERMAL) {
 #pragma unroll
         for (int l = 0; l < QT; l++) {
             const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
-            St<T>::st(GA + l * N + c, wtf(l) * Tc * (1.0f + 4.0f * cu));
+            St<T>::st(GA + l * S + c, wtf(l) * Tc * (1.0f + 4.0f * cu));
         }
     }
 }
@@ -326,6 +463,18 @@ __global__ void k_init(T *__restrict__ A, T *__restrict__ GA, long long N, const
 // ---------------------------------------------------------------------------
 template <class T>
 static cudaError_t launch_step_t(const LaunchArgs &a) {
+    const TmaPlan &tp = a.tma;
+    if (tp.enabled && a.gather && !a.export_only && a.mom == nullptr) {
+        if (a.thermal)
+            k_step_tma<T, true><<<tp.grid, tp.tx, tp.smem, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA,
+                                                                       (T *)a.GB, *a.P, a.ds, a.band, tp.tx,
+                                                                       tp.tiles_x, tp.ntiles);
+        else
+            k_step_tma<T, false><<<tp.grid, tp.tx, tp.smem, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr,
+                                                                        *a.P, a.ds, a.band, tp.tx, tp.tiles_x,
+                                                                        tp.ntiles);
+        return cudaGetLastError();
+    }
     dim3 blk(a.tx, a.ty, 1);
     dim3 grd((a.P->nx + a.tx - 1) / a.tx, (a.P->ny + a.ty - 1) / a.ty, a.P->nz);
     if (a.thermal)
@@ -342,6 +491,46 @@ cudaError_t launch_step(int storage, const LaunchArgs &a) {
     case 0: return launch_step_t<float>(a);
     case 1: return launch_step_t<__half>(a);
     case 2: return launch_step_t<__nv_bfloat16>(a);
+    }
+    return cudaErrorInvalidValue;
+}
+
+template <class T, bool THERMAL>
+static cudaError_t plan_t(const StepParams &P, int tx_pref, TmaPlan &tp) {
+    constexpr int AL = 16 / (int)sizeof(T);
+    constexpr int NQ = THERMAL ? Q + QT : Q;
+    tp.enabled = 0;
+    int tx = tx_pref > 0 ? tx_pref : (sizeof(T) == 4 ? 128 : 256);
+    int nx_r = ((P.nx + 31) / 32) * 32;
+    if (tx > nx_r) tx = nx_r;
+    if (P.nx % AL != 0 || tx % 32 != 0 || tx % AL != 0 || tx > 256 || P.ny < 3 || P.nz < 3) return cudaSuccess;
+    const size_t stage_bytes = (size_t)NQ * (tx + AL) * sizeof(T);
+    const size_t smem = ((kStages * stage_bytes + 15) / 16) * 16 + kStages * sizeof(uint64_t);
+    cudaError_t e = cudaFuncSetAttribute(k_step_tma<T, THERMAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+    int per_sm = 0, dev = 0, sms = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_tma<T, THERMAL>, tx, smem)) != cudaSuccess)
+        return e;
+    if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+    if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+    if (per_sm < 1) return cudaSuccess;
+    tp.tx = tx;
+    tp.tiles_x = (P.nx + tx - 1) / tx;
+    tp.ntiles = (long long)tp.tiles_x * P.ny * P.nz;
+    tp.smem = smem;
+    long long g = (long long)per_sm * sms;
+    tp.grid = (int)(g < tp.ntiles ? g : tp.ntiles);
+    tp.per_sm = per_sm;
+    tp.enabled = 1;
+    return cudaSuccess;
+}
+
+cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int tx_pref, TmaPlan &tp) {
+    switch (storage) {
+    case 0: return thermal ? plan_t<float, true>(P, tx_pref, tp) : plan_t<float, false>(P, tx_pref, tp);
+    case 1: return thermal ? plan_t<__half, true>(P, tx_pref, tp) : plan_t<__half, false>(P, tx_pref, tp);
+    case 2:
+        return thermal ? plan_t<__nv_bfloat16, true>(P, tx_pref, tp) : plan_t<__nv_bfloat16, false>(P, tx_pref, tp);
     }
     return cudaErrorInvalidValue;
 }
@@ -369,25 +558,25 @@ cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign) {
 }
 
 template <class T>
-static cudaError_t launch_init_t(void *A, void *GA, long long N, const float *fields, const float init[5], bool thermal,
-                                 cudaStream_t s) {
+static cudaError_t launch_init_t(void *A, void *GA, long long N, long long S, const float *fields, const float init[5],
+                                 bool thermal, cudaStream_t s) {
     int threads = 256;
     long long blocks = (N + threads - 1) / threads;
     if (thermal)
-        k_init<T, true><<<(unsigned)blocks, threads, 0, s>>>((T *)A, (T *)GA, N, fields, init[0], init[1], init[2],
-                                                             init[3], init[4]);
+        k_init<T, true><<<(unsigned)blocks, threads, 0, s>>>((T *)A, (T *)GA, N, S, fields, init[0], init[1],
+                                                             init[2], init[3], init[4]);
     else
-        k_init<T, false><<<(unsigned)blocks, threads, 0, s>>>((T *)A, nullptr, N, fields, init[0], init[1], init[2],
-                                                              init[3], init[4]);
+        k_init<T, false><<<(unsigned)blocks, threads, 0, s>>>((T *)A, nullptr, N, S, fields, init[0], init[1],
+                                                              init[2], init[3], init[4]);
     return cudaGetLastError();
 }
 
-cudaError_t launch_init(int storage, void *A, void *GA, long long N, const float *fields, const float init[5],
-                        bool thermal, cudaStream_t s) {
+cudaError_t launch_init(int storage, void *A, void *GA, long long N, long long S, const float *fields,
+                        const float init[5], bool thermal, cudaStream_t s) {
     switch (storage) {
-    case 0: return launch_init_t<float>(A, GA, N, fields, init, thermal, s);
-    case 1: return launch_init_t<__half>(A, GA, N, fields, init, thermal, s);
-    case 2: return launch_init_t<__nv_bfloat16>(A, GA, N, fields, init, thermal, s);
+    case 0: return launch_init_t<float>(A, GA, N, S, fields, init, thermal, s);
+    case 1: return launch_init_t<__half>(A, GA, N, S, fields, init, thermal, s);
+    case 2: return launch_init_t<__nv_bfloat16>(A, GA, N, S, fields, init, thermal, s);
     }
     return cudaErrorInvalidValue;
 }

@@ -22,11 +22,15 @@ def _err(m, ref, lid):
     return eu, er
 
 
-@pytest.mark.parametrize("shape,tau", [((16, 16, 16), 0.8), ((12, 18, 10), 0.6), ((33, 20, 17), 0.55)])
-def test_cavity_fp32_vs_oracle(pkg, orc, shape, tau):
+@pytest.mark.parametrize("staged", [0, -1], ids=["staged", "direct"])
+@pytest.mark.parametrize("shape,tau", [((16, 16, 16), 0.8), ((12, 18, 10), 0.6), ((33, 20, 17), 0.55),
+                                       ((64, 9, 7), 0.7)])
+def test_cavity_fp32_vs_oracle(pkg, orc, shape, tau, staged):
+    """Both fused kernels: the bulk-copy staged one (row lengths that are a
+    multiple of 16 bytes) and the direct-load one (any row length)."""
     nx, ny, nz = shape
     lid, steps = 0.05, 300
-    s = pkg.Solver(pkg.cavity_config(nx, tau=tau, lid=lid, ny=ny, nz=nz))
+    s = pkg.Solver(pkg.cavity_config(nx, tau=tau, lid=lid, ny=ny, nz=nz, staged=staged))
     s.init()
     s.step(steps)
     m = s.moments()
@@ -68,6 +72,19 @@ def test_graph_replay_matches_eager_bitwise(pkg):
         s.step(1)
         s.step(37)
         s.step(20)
+    ma, mb = a.moments(), b.moments()
+    for c in ("rho", "ux", "uy", "uz"):
+        assert np.array_equal(ma[c], mb[c]), c
+
+
+@pytest.mark.parametrize("storage", ["f32", "f16", "bf16"])
+def test_staged_matches_direct_bitwise(pkg, storage):
+    """The staged (bulk-copy) and direct-load kernels compute the same update."""
+    a = pkg.Solver(pkg.cavity_config(32, tau=0.7, lid=0.05, ny=20, nz=12, storage=storage, staged=0))
+    b = pkg.Solver(pkg.cavity_config(32, tau=0.7, lid=0.05, ny=20, nz=12, storage=storage, staged=-1))
+    for s in (a, b):
+        s.init()
+        s.step(50)
     ma, mb = a.moments(), b.moments()
     for c in ("rho", "ux", "uy", "uz"):
         assert np.array_equal(ma[c], mb[c]), c

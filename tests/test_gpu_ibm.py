@@ -14,12 +14,13 @@ pytestmark = pytest.mark.gpu
 U = 0.05
 
 
-def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None):
-    cfgkw = {}
+def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None,
+                fused=0, u_in=U):
+    cfgkw = {"ibm_fused": fused}
     if thermal:
         cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0),
                      gbeta=thermal.get("gbeta", (0, 0, 0)), T_ref=thermal.get("T0", 0.0))
-    s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=U, storage=storage, **cfgkw))
+    s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=u_in, storage=storage, **cfgkw))
     s.init()
     mk = orc.fibonacci_sphere(nm, D, center)
     xyz = np.stack([mk["x"], mk["y"], mk["z"]])
@@ -35,11 +36,14 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
     return s
 
 
+@pytest.mark.parametrize("fused", [0, -1], ids=["cluster", "multikernel"])
 @pytest.mark.parametrize("lit_sign", [0, 1])
-def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign):
+def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, fused):
+    """Both IBM drivers: the single thread-block-cluster launch and the
+    multi-kernel chain."""
     nx, ny, nz, tau, D, nm, m_max, steps = 48, 30, 28, 0.56, 10.0, 314, 3, 120
     center = (16.0, 15.3, 14.6)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, fused=fused)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -70,33 +74,53 @@ def test_fixed_sphere_fp16_drag(pkg, orc):
     assert ed < 5e-3 and eu < 1e-3
 
 
-def test_thermal_free_sphere_vs_oracle(pkg, orc):
+@pytest.mark.parametrize("fused", [0, -1], ids=["cluster", "multikernel"])
+def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     """D3Q7 thermal population, Boussinesq force, thermal IBM (T_body = 1)
-    and the FP64 Newton-Euler body, against the oracle."""
+    and the FP64 Newton-Euler body (held in x and rotation, free in y and z)
+    settling in fluid at rest, against the oracle."""
     nx, ny, nz, tau, D, nm, m_max, steps = 40, 32, 28, 0.56, 8.0, 201, 3, 80
     center = (14.0, 16.2, 13.7)
     nu = (tau - 0.5) / 3.0
     alpha = nu / 0.71
-    th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-4, 0.0), T_body=1.0)
-    # held in x (streamwise) and in rotation, free in y and z
-    fr = dict(rho_ratio=1.5, gravity=(0.0, -1e-4, 0.0), dof=0b000110)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr)
+    th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
+    # rho_s/rho_f = 3: the explicit coupling of a D = 8 sphere is unstable at 1.5
+    fr = dict(rho_ratio=3.0, gravity=(0.0, -1e-5, 0.0), dof=0b000110)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, fused=fused, u_in=0.0)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
     body = s.body()
     xyz = s.markers()
     assert s.status() == 0
-    lat, mk, hist, ob = orc.sphere_case(nx, ny, nz, tau, D, center, nm, m_max, U, steps, thermal=th, free=fr)
+    lat, mk, hist, ob = orc.sphere_case(nx, ny, nz, tau, D, center, nm, m_max, 0.0, steps, thermal=th, free=fr)
     r = orc.moments(lat, gbeta=th["gbeta"], T0=0.0)
-    eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / U
+    vscale = max(np.abs(r[c]).max() for c in ("ux", "uy", "uz"))
+    eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / vscale
     eT = np.abs(m["T"] - r["T"]).max()
-    assert eu < 1e-5 and eT < 1e-5, (eu, eT)
-    drag = np.abs(hist[:, 0]).max()
-    assert np.abs(fg[:, :3] - hist[:, :3]).max() / drag < 1e-3
+    print("thermal free sphere: |u| err %.3e of max |u| %.3e, T err %.3e" % (eu, vscale, eT))
+    assert eu < 1e-4 and eT < 1e-5, (eu, eT)
+    fscale = np.abs(hist[:, :3]).max()
+    assert np.abs(fg[:, :3] - hist[:, :3]).max() / fscale < 1e-3
     heat = np.abs(hist[:, 6]).max()
     assert np.abs(fg[:, 6] - hist[:, 6]).max() / heat < 1e-3
     oxc = np.array([ob.xc[a] for a in range(3)])
     assert np.abs(body[:3] - oxc).max() < 1e-6
     oxyz = np.stack([mk["x"], mk["y"], mk["z"]])
     assert np.abs(xyz - oxyz).max() < 1e-6
+
+
+def test_cluster_and_multikernel_ibm_agree(pkg, orc):
+    """The two IBM drivers give the same forces and fields (up to the order of
+    float atomics)."""
+    nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
+    center = (24.0, 20.0, 20.0)
+    out = []
+    for fused in (0, -1):
+        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f16", fused=fused)
+        s.step(steps)
+        out.append((s.forces(), s.moments()))
+        assert s.status() == 0
+    fa, fb = out[0][0], out[1][0]
+    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
+    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-4
