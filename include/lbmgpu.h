@@ -92,8 +92,8 @@ typedef struct lbm_config {
     double gbeta[3];      /* Boussinesq: F += gbeta * (T - T0)  (lbm.cpp:804-805) */
     int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
     int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
-    int staged;           /* bulk-copy staged kernel: 0 = default tile width, >0 = tile width, <0 = off */
-    int ibm_fused;        /* IBM phase as one thread-block-cluster launch: 0 = on when it fits, <0 = off */
+    int staged;           /* bulk-copy staged kernel: 0 = default rows per tile, >0 = rows per tile, <0 = off */
+    int ibm_fused;        /* >0: IBM phase as one thread-block-cluster launch (when it fits); 0 = multi-kernel */
 } lbm_config;
 
 typedef struct lbm_ibm_config {

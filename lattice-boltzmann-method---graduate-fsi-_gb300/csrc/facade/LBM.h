@@ -1,0 +1,133 @@
+// LBM.h -- drop-in host facade with the reference's class surface
+// (DestinyFlow01/Lattice-Boltzmann-Method---Graduate-FSI-, LBM.h:528-761),
+// running the time step on the GPU through the C ABI (include/lbmgpu.h).
+//
+// What stays the same for a caller of the reference:
+//   - the cell types TYPE_F .. TYPE_Q (LBM.h:505-515), the D3Q19 tables
+//     cx/cy/cz/w/opposite in the reference order (LBM.h:542-552);
+//   - class LATTICE with type/density/ux/uy/uz/f/f_star/F/Fm (LBM.h:558-597)
+//     and the public LATTICE ***fluid array of (Nx+2)(Ny+2)(Nz+2) cells;
+//   - class MARKER (LBM.h:600-616) and the free functions kernel,
+//     NearestLatticeCoordinate, Calc_AverageDensity and IBLBM (LBM.h:674-688);
+//   - class LBM: LBM(Nx, Ny, Nz, tau), Init, Collision, Streaming, MacroProp,
+//     ConvLBM, Calc_feq, Determine_Wall_Velocity, getNx/getNy/getNz/getTAU.
+// What changes:
+//   - Init() reads fluid[..].type / density / ux.. (the set-up the reference's
+//     main_setup_* functions write), builds the device configuration and
+//     uploads the state; from then on the populations live on the GPU;
+//   - Collision() + Streaming() run one fused step on the device (Collision
+//     only records that a collision is pending); MacroProp() is fused into
+//     the step and here only marks the host mirror stale;
+//   - sync_to_host() fills fluid[..].density/ux/uy/uz (and T) with the
+//     MacroProp moments before output code reads them;
+//   - IBLBM registers the markers with the device on its first call; the
+//     forcing runs inside the next step and Cl/Cd are appended after it.
+// Compile-time choices of the reference (#define D3Q19, IBM scheme, m_max,
+// D, u_max ...) become fields of lbm_options.
+#pragma once
+#include <cmath>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../../include/lbmgpu.h"
+
+#ifndef TYPE_F
+#define TYPE_F 0    // fluid domain
+#define TYPE_S 1    // (stationary or moving) solid boundary
+#define TYPE_OUT 2  // outflow boundary
+#define TYPE_IN 3   // inflow boundary
+#define TYPE_P 4    // periodic boundary
+#define TYPE_L 5    // slip boundary
+#define TYPE_T 6    // Dirichlet temperature
+#define TYPE_Q 7    // Neumann heat flux
+#endif
+
+const int ndim = 3;
+const int npop = 19;
+const int cx[npop] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0};
+const int cy[npop] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1};
+const int cz[npop] = {0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1};
+const double w[npop] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18,
+                        1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
+                        1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
+const int opposite[npop] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+
+// Run-time replacement of the reference's compile-time configuration.
+struct lbm_options {
+    int storage = LBM_STORE_F32;  // LBM_STORE_F32 / F16 / BF16
+    int m_max = 5;                // implicit IBM iterations (LBM.h:357)
+    int literal_sign = 0;         // 1: the reference's force-sign convention (lbm.cpp:1347-1352)
+    double rho0 = 1.0;            // LBM.h:80
+    double u_max = 0.05;          // reference velocity for Cl/Cd
+    double ref_area = 1.0;        // Cl/Cd area: D for 2D (lbm.cpp:1402), pi D^2 / 4 for a sphere (lbm.cpp:3159)
+    double body_radius = 0.0;     // IBM body radius (0: from the marker cloud)
+    int thermal = 0;              // D3Q7 temperature population
+    double tau_g = 0.0, T_ref = 0.0, gbeta[3] = {0, 0, 0};
+};
+extern lbm_options g_lbm_options;
+
+class LATTICE {
+  public:
+    short type = TYPE_F;
+    double density = 1.0;
+    double ux = 0.0, uy = 0.0, uz = 0.0;
+    double f[npop], f_star[npop];
+    double F[3] = {0, 0, 0};
+    double Fm[3] = {0, 0, 0};
+    double T = 0.0;
+};
+
+class MARKER {
+  public:
+    double x, y, z = 1;
+    double u_boundary[3] = {0, 0, 0};
+    double u_boundary_des[3] = {0, 0, 0};
+    double F_boundary[3] = {0, 0, 0};
+    double normal[3] = {0, 0, 0};
+    double Fm_boundary[3] = {0, 0, 0};
+    // 2D normal t x z of the segment (x1,y1,z1)->(x2,y2,z2) (lbm.cpp:1048-1069)
+    void Normal_Marker(int n, double x1, double x2, double y1, double y2, double z1, double z2);
+};
+
+struct lbm_device_state;  // shared by shallow copies of an LBM (the reference returns LBM by value)
+
+class LBM {
+  private:
+    int Nx, Ny, Nz = 1;
+    double tau;
+    std::shared_ptr<lbm_device_state> dev;
+
+  public:
+    LATTICE ***fluid;
+
+    LBM(int Nx, int Ny, int Nz, double tau);
+
+    void Init();
+    void Collision();
+    void Streaming();
+    void MacroProp();
+    void ConvLBM(int i, int j, int k);          // host collision of one mirror cell (lbm.cpp:75-119)
+    double Calc_feq(int i, int j, int k, int l); // third-order equilibrium (lbm.cpp:628-633)
+    void Determine_Wall_Velocity(int i, int j, int k, std::vector<double> &uwall);  // lbm.cpp:941-962
+
+    int getNx() const;
+    int getNy() const;
+    int getNz() const;
+    double getTAU() const;
+
+    // GB300 additions
+    void sync_to_host();        // MacroProp moments into fluid[..]
+    lbm_handle *handle() const; // the device solve (nullptr before Init)
+    long long steps() const;
+    friend void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
+                      std::vector<double> &Cd, double V_CM[], double t);
+};
+
+void NearestLatticeCoordinate(int xmin, int xmax, int ymin, int ymax, int zmin, int zmax, int &i, int &j, int &k,
+                              std::vector<MARKER> &marker, int n);
+double kernel(double r);
+double Calc_AverageDensity(LBM &lb, std::vector<MARKER> &marker, int xmin, int xmax, int ymin, int ymax, int zmin,
+                           int zmax);
+void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
+           std::vector<double> &Cd, double V_CM[], double t);

@@ -1,0 +1,34 @@
+"""Build the C++ drop-in facade (LBM.h) and its two drivers against liblbmgpu.so.
+
+Outputs: csrc/facade/_build/liblbm_facade.a? -- no archive: the drivers
+dropin_cavity and dropin_sphere are linked directly with lbm_facade.cpp and
+-llbmgpu (rpath to the package directory).
+"""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(os.path.dirname(HERE))
+OUT = os.path.join(HERE, "_build")
+DRIVERS = ["dropin_cavity", "dropin_sphere"]
+
+
+def build(force: bool = False) -> list:
+    os.makedirs(OUT, exist_ok=True)
+    lib = os.path.join(PKG, "liblbmgpu.so")
+    srcs = [os.path.join(HERE, f) for f in ("lbm_facade.cpp", "LBM.h")]
+    outs = []
+    for d in DRIVERS:
+        exe = os.path.join(OUT, d)
+        deps = srcs + [os.path.join(HERE, d + ".cpp"), lib]
+        if force or not os.path.exists(exe) or any(os.path.getmtime(p) > os.path.getmtime(exe) for p in deps):
+            cmd = ["g++", "-O2", "-std=c++17", "-I" + HERE, os.path.join(HERE, d + ".cpp"),
+                   os.path.join(HERE, "lbm_facade.cpp"), "-L" + PKG, "-llbmgpu",
+                   "-Wl,-rpath," + PKG, "-o", exe]
+            subprocess.check_call(cmd)
+        outs.append(exe)
+    return outs
+
+
+if __name__ == "__main__":
+    print(build(force=True))

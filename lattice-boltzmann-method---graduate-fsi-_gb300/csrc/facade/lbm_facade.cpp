@@ -1,0 +1,288 @@
+// lbm_facade.cpp -- the reference's LBM class surface on top of liblbmgpu.
+#include <cstdio>
+#include <exception>
+#include <vector>
+
+#include "LBM.h"
+
+lbm_options g_lbm_options;
+
+struct lbm_device_state {
+    lbm_handle *h = nullptr;
+    bool collision_pending = false;
+    bool mirror_stale = false;
+    bool markers_set = false;
+    long long steps = 0;
+    std::vector<double> *cl = nullptr, *cd = nullptr;
+    int off[3] = {1, 1, 1};  // device cell = reference index - off (0 on periodic axes)
+    int dn[3] = {0, 0, 0};
+    ~lbm_device_state() {
+        if (h) lbmgpu_destroy(h);
+    }
+};
+
+// The reference terminates on invalid state (lbm.cpp:116, 774, 796); the
+// facade does the same when the device reports an error.
+static void check(const char *what, lbm_status s) {
+    if (s != LBM_OK) {
+        fprintf(stderr, "lbmgpu %s failed (status %d): %s\n", what, (int)s, lbmgpu_last_error());
+        std::terminate();
+    }
+}
+
+void MARKER::Normal_Marker(int n, double x1, double x2, double y1, double y2, double z1, double z2) {
+    (void)n;
+    double ddx = x2 - x1, ddy = y2 - y1, ddz = z2 - z1;
+    double norm = std::sqrt(ddx * ddx + ddy * ddy + ddz * ddz);
+    double t1[3] = {ddx / norm, ddy / norm, ddz / norm};
+    const double t2[3] = {0, 0, 1};
+    normal[0] = t1[1] * t2[2] - t1[2] * t2[1];
+    normal[1] = t1[2] * t2[0] - t1[0] * t2[2];
+    normal[2] = t1[0] * t2[1] - t1[1] * t2[0];
+}
+
+LBM::LBM(int Nx, int Ny, int Nz, double tau) : Nx(Nx), Ny(Ny), Nz(Nz), tau(tau) {
+    dev = std::make_shared<lbm_device_state>();
+    fluid = new LATTICE **[Nx + 2];
+    for (int i = 0; i < Nx + 2; i++) {
+        fluid[i] = new LATTICE *[Ny + 2];
+        for (int j = 0; j < Ny + 2; j++) fluid[i][j] = new LATTICE[Nz + 2];
+    }
+}
+
+int LBM::getNx() const { return Nx; }
+int LBM::getNy() const { return Ny; }
+int LBM::getNz() const { return Nz; }
+double LBM::getTAU() const { return tau; }
+lbm_handle *LBM::handle() const { return dev->h; }
+long long LBM::steps() const { return dev->steps; }
+
+double LBM::Calc_feq(int i, int j, int k, int l) {
+    const LATTICE &c = fluid[i][j][k];
+    const double cs2 = 1.0 / 3.0;
+    double u_dot_u = c.ux * c.ux + c.uy * c.uy + c.uz * c.uz;
+    double c_dot_u = c.ux * cx[l] + c.uy * cy[l] + c.uz * cz[l];
+    return c.density * w[l] *
+           (1 + c_dot_u / cs2 + c_dot_u * c_dot_u / (2 * cs2 * cs2) - u_dot_u / (2 * cs2) +
+            std::pow(c_dot_u, 3) / (6 * std::pow(cs2, 3)) - c_dot_u * u_dot_u / (2 * cs2 * cs2));
+}
+
+void LBM::ConvLBM(int i, int j, int k) {
+    LATTICE &c = fluid[i][j][k];
+    const double omega = 1.0 / tau, cs2 = 1.0 / 3.0;
+    double F_dot_u = c.F[0] * c.ux + c.F[1] * c.uy + c.F[2] * c.uz;
+    for (int l = 0; l < npop; l++) {
+        double c_dot_u = c.ux * cx[l] + c.uy * cy[l] + c.uz * cz[l];
+        double f_eq = Calc_feq(i, j, k, l);
+        double F_dot_c = c.F[0] * cx[l] + c.F[1] * cy[l] + c.F[2] * cz[l];
+        double S = (1 - omega * 0.5) * w[l] * (F_dot_c / cs2 + F_dot_c * c_dot_u / (cs2 * cs2) - F_dot_u / cs2);
+        c.f_star[l] = c.f[l] * (1 - omega) + omega * f_eq + S;
+    }
+}
+
+void LBM::Determine_Wall_Velocity(int i, int j, int k, std::vector<double> &uwall) {
+    int num = 0;
+    for (int l = 0; l < npop; l++) {
+        int in = (i + cx[l] + (Nx + 2)) % (Nx + 2), jn = (j + cy[l] + (Ny + 2)) % (Ny + 2),
+            kn = (k + cz[l] + (Nz + 2)) % (Nz + 2);
+        const LATTICE &nb = fluid[in][jn][kn];
+        if (nb.type == TYPE_S && (nb.ux != 0 || nb.uy != 0 || nb.uz != 0)) {
+            uwall[0] += nb.ux;
+            uwall[1] += nb.uy;
+            uwall[2] += nb.uz;
+            num++;
+        }
+    }
+    if (num) {
+        uwall[0] /= num;
+        uwall[1] /= num;
+        uwall[2] /= num;
+    }
+}
+
+void LBM::Init() {
+    const int NX = Nx + 2, NY = Ny + 2, NZ = Nz + 2;
+    const size_t n = (size_t)NX * NY * NZ;
+    std::vector<uint8_t> types(n);
+    std::vector<double> rho(n), ux(n), uy(n), uz(n), T(n);
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++) {
+                const LATTICE &c = fluid[i][j][k];
+                size_t id = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k);
+                types[id] = (uint8_t)c.type;
+                rho[id] = c.density;
+                ux[id] = c.ux;
+                uy[id] = c.uy;
+                uz[id] = c.uz;
+                T[id] = c.T;
+            }
+    lbm_config cfg;
+    check("config_from_types", lbmgpu_config_from_types(Nx, Ny, Nz, tau, types.data(), rho.data(), ux.data(),
+                                                        uy.data(), uz.data(), T.data(), &cfg));
+    const lbm_options &o = g_lbm_options;
+    cfg.storage = o.storage;
+    cfg.thermal = o.thermal;
+    cfg.tau_g = o.tau_g;
+    cfg.T_ref = o.T_ref;
+    for (int a = 0; a < 3; a++) cfg.gbeta[a] = o.gbeta[a];
+    const int dims[3] = {Nx, Ny, Nz};
+    const int ddims[3] = {cfg.nx, cfg.ny, cfg.nz};
+    for (int a = 0; a < 3; a++) {
+        dev->off[a] = ddims[a] == dims[a] + 2 ? 0 : 1;
+        dev->dn[a] = ddims[a];
+    }
+    if (dev->h) lbmgpu_destroy(dev->h);
+    dev->h = nullptr;
+    check("create", lbmgpu_create(&cfg, &dev->h));
+    const size_t nd = (size_t)cfg.nx * cfg.ny * cfg.nz;
+    std::vector<double> drho(nd), dux(nd), duy(nd), duz(nd), dT(nd);
+    for (int z = 0; z < cfg.nz; z++)
+        for (int y = 0; y < cfg.ny; y++)
+            for (int x = 0; x < cfg.nx; x++) {
+                const LATTICE &c = fluid[x + dev->off[0]][y + dev->off[1]][z + dev->off[2]];
+                size_t id = (size_t)x + (size_t)cfg.nx * ((size_t)y + (size_t)cfg.ny * z);
+                drho[id] = c.density;
+                dux[id] = c.ux;
+                duy[id] = c.uy;
+                duz[id] = c.uz;
+                dT[id] = c.T;
+            }
+    check("init_fields", lbmgpu_init_fields(dev->h, drho.data(), dux.data(), duy.data(), duz.data(),
+                                            cfg.thermal ? dT.data() : nullptr));
+    // host mirror as LBM::Init leaves it (lbm.cpp:31-57)
+    for (int i = 0; i < NX; i++)
+        for (int j = 0; j < NY; j++)
+            for (int k = 0; k < NZ; k++)
+                for (int l = 0; l < npop; l++) {
+                    double fe = Calc_feq(i, j, k, l);
+                    fluid[i][j][k].f[l] = fe;
+                    fluid[i][j][k].f_star[l] = fe;
+                }
+    dev->steps = 0;
+    dev->mirror_stale = false;
+}
+
+void LBM::Collision() { dev->collision_pending = true; }
+
+void LBM::Streaming() {
+    if (!dev->h) check("Streaming before Init", LBM_ERR_STATE);
+    check("step", lbmgpu_step(dev->h, 1));
+    dev->collision_pending = false;
+    dev->mirror_stale = true;
+    dev->steps++;
+    if (dev->markers_set && dev->cl && dev->cd) {
+        double f[8];
+        int got = 0;
+        check("get_forces", lbmgpu_get_forces(dev->h, f, 1, &got));
+        const lbm_options &o = g_lbm_options;
+        const double q = 0.5 * o.rho0 * o.u_max * o.u_max * o.ref_area;
+        dev->cd->push_back(f[0] / q);
+        dev->cl->push_back(f[1] / q);
+    }
+}
+
+void LBM::MacroProp() { dev->mirror_stale = true; }
+
+void LBM::sync_to_host() {
+    if (!dev->h) return;
+    const size_t nd = (size_t)dev->dn[0] * dev->dn[1] * dev->dn[2];
+    const int nf = g_lbm_options.thermal ? 5 : 4;
+    std::vector<float> buf(nf * nd);
+    check("download", lbmgpu_download_all_f32(dev->h, buf.data()));
+    for (int z = 0; z < dev->dn[2]; z++)
+        for (int y = 0; y < dev->dn[1]; y++)
+            for (int x = 0; x < dev->dn[0]; x++) {
+                size_t id = (size_t)x + (size_t)dev->dn[0] * ((size_t)y + (size_t)dev->dn[1] * z);
+                LATTICE &c = fluid[x + dev->off[0]][y + dev->off[1]][z + dev->off[2]];
+                c.density = buf[id];
+                c.ux = buf[nd + id];
+                c.uy = buf[2 * nd + id];
+                c.uz = buf[3 * nd + id];
+                if (nf == 5) c.T = buf[4 * nd + id];
+            }
+    dev->mirror_stale = false;
+}
+
+double kernel(double r) {
+    double a = std::fabs(r);
+    if (a <= 1) return (3 - 2 * a + std::sqrt(1 + 4 * a - 4 * r * r)) / 8;
+    if (a <= 2) return (5 - 2 * a - std::sqrt(-7 + 12 * a - 4 * r * r)) / 8;
+    return 0;
+}
+
+void NearestLatticeCoordinate(int xmin, int xmax, int ymin, int ymax, int zmin, int zmax, int &i, int &j, int &k,
+                              std::vector<MARKER> &marker, int n) {
+    double dot = 0;
+    for (int x = xmin; x <= xmax; x++)
+        for (int y = ymin; y <= ymax; y++)
+            for (int z = zmin; z <= zmax; z++) {
+                double d = (x - marker[n].x) * marker[n].normal[0] + (y - marker[n].y) * marker[n].normal[1] +
+                           (z - marker[n].z) * marker[n].normal[2];
+                if (d >= dot && d > 0) {
+                    i = x;
+                    j = y;
+                    k = z;
+                    dot = d;
+                }
+            }
+}
+
+double Calc_AverageDensity(LBM &lb, std::vector<MARKER> &marker, int xmin, int xmax, int ymin, int ymax, int zmin,
+                           int zmax) {
+    double rho = 0;
+    int number = 0;
+    for (int i = xmin; i <= xmax; i++)
+        for (int j = ymin; j <= ymax; j++)
+            for (int k = zmin; k <= zmax; k++) {
+                bool inside = true;
+                for (size_t n = 0; n < marker.size() && inside; n++) {
+                    double d = (i - marker[n].x) * marker[n].normal[0] + (j - marker[n].y) * marker[n].normal[1] +
+                               (k - marker[n].z) * marker[n].normal[2];
+                    if (d > 0) inside = false;
+                }
+                if (inside) {
+                    rho += lb.fluid[i][j][k].density;
+                    number++;
+                }
+            }
+    return number ? rho / number : 0.0;
+}
+
+void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
+           std::vector<double> &Cd, double V_CM[], double t) {
+    (void)t;
+    lbm_device_state &d = *lb.dev;
+    if (!d.h) check("IBLBM before Init", LBM_ERR_STATE);
+    d.cl = &Cl;
+    d.cd = &Cd;
+    if (d.markers_set) return;  // fixed body: the markers stay on the device
+    const int n = (int)marker.size();
+    std::vector<double> xyz(3 * (size_t)n), dsv(ds.begin(), ds.end());
+    double c[3] = {0, 0, 0};
+    for (int m = 0; m < n; m++) {
+        // device node coordinates: reference index minus the device offset
+        xyz[m] = marker[m].x - (d.off[0] - 1);
+        xyz[n + m] = marker[m].y - (d.off[1] - 1);
+        xyz[2 * (size_t)n + m] = marker[m].z - (d.off[2] - 1);
+        for (int a = 0; a < 3; a++) c[a] += xyz[(size_t)a * n + m] / n;
+    }
+    double R = g_lbm_options.body_radius;
+    if (R <= 0)
+        for (int m = 0; m < n; m++) {
+            double rr = 0;
+            for (int a = 0; a < 3; a++) rr += (xyz[(size_t)a * n + m] - c[a]) * (xyz[(size_t)a * n + m] - c[a]);
+            R = std::max(R, std::sqrt(rr));
+        }
+    lbm_ibm_config ic = {};
+    ic.n_markers = n;
+    ic.m_max = g_lbm_options.m_max;
+    ic.literal_sign = g_lbm_options.literal_sign;
+    ic.radius = R;
+    for (int a = 0; a < 3; a++) {
+        ic.center[a] = c[a];
+        ic.velocity[a] = V_CM[a];
+    }
+    check("set_markers", lbmgpu_set_markers(d.h, &ic, xyz.data(), dsv.data(), nullptr));
+    d.markers_set = true;
+}

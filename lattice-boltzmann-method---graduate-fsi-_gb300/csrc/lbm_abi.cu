@@ -331,11 +331,11 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         }
     };
     chk(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking), "stream");
-    // Population arrays: stride S = N rounded up to 256 cells plus 512 cells
-    // of slack (a tile-wide over-read past the last row stays inside the
-    // array, and the 19 streams do not sit at power-of-two distances), and a
-    // guard of kGuard cells before the first array.
-    P.S = ((P.N + 255) / 256) * 256 + 512;
+    // Population arrays: stride S = N plus at least two rows (and 512 cells)
+    // of slack, rounded up to 256 cells, so that a staged tile's over-read of
+    // one row and one 16-byte group past the last plane stays inside the
+    // array, and a guard of kGuard cells before the first array.
+    P.S = ((P.N + std::max<long long>(512, 2LL * P.nx + 64) + 255) / 256) * 256;
     const size_t fb = ((size_t)Q * P.S + 2 * kGuard) * h->esize;
     for (int i = 0; i < 2 && st == LBM_OK; i++) {
         chk(dalloc(h, &h->fraw[i], fb), "populations");
@@ -358,7 +358,7 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     }
     for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
     if (st == LBM_OK && c.staged >= 0) chk(plan_tma(c.storage, c.thermal != 0, P, c.staged, h->tma), "staged plan");
-    h->use_fused = c.ibm_fused >= 0 ? 1 : 0;
+    h->use_fused = c.ibm_fused > 0 ? 1 : 0;
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);

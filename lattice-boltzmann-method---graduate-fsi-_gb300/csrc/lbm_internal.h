@@ -11,7 +11,7 @@ namespace lbmk {
 // to the direct-load kernel.
 struct TmaPlan {
     int enabled = 0;
-    int tx = 0, tiles_x = 0, grid = 0, per_sm = 0;
+    int ty = 0, grid = 0, per_sm = 0;  // rows per tile, CTAs, CTAs per SM
     long long ntiles = 0;
     size_t smem = 0;
 };
@@ -34,7 +34,7 @@ struct LaunchArgs {
 };
 
 cudaError_t launch_step(int storage, const LaunchArgs &a);
-cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int tx_pref, TmaPlan &tp);
+cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int ty_pref, TmaPlan &tp);
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign);
 cudaError_t launch_init(int storage, void *A, void *GA, long long N, long long S, const float *fields,
                         const float init[5], bool thermal, cudaStream_t s);

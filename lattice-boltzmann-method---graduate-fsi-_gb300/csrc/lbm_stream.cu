@@ -216,19 +216,23 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
 }
 
 // ---------------------------------------------------------------------------
-// Staged variant: a persistent kernel whose CTAs walk row tiles of TX cells.
-// For every tile one thread issues, per population, a bulk asynchronous copy
-// (cp.async.bulk, the TMA engine) of the source row segment into shared
-// memory -- TX cells, widened by one 16-byte group on the side the link
-// comes from -- and arms an mbarrier with the byte count.  kStages tiles are
-// in flight per CTA, so the bytes in flight no longer depend on registers.
-// Interior cells read their 19 (+7) pulled populations from shared memory;
-// cells on a domain face take the boundary-class path from global memory.
-// Rows on a y/z face stage nothing.  Requires nx and TX to be multiples of
-// 16 bytes' worth of cells.
+// Staged variant (warp-specialised, persistent).  A tile is TY whole rows
+// (TY * nx cells) of one z plane.  Warp 0 is the producer: for every tile it
+// arms the stage's "full" mbarrier with the byte count and issues, lane per
+// population, one bulk asynchronous copy (cp.async.bulk, the TMA engine) of
+// the source rows of that population -- the TY rows shifted by (cy, cz),
+// widened by one 16-byte group on the side an x-link comes from -- into
+// shared memory.  The other warps consume: each waits on "full", reads the
+// pulled populations of its cells from shared memory, collides, stores to B
+// and arrives on the stage's "empty" mbarrier, which the producer waits on
+// before reusing the stage.  kStages tiles are in flight per CTA.  Cells on a
+// domain face (and every cell of the first and last z plane, whose tiles
+// stage nothing) take the boundary-class path from global memory.  All
+// mbarrier waits are bounded; a wait that gives up sets ST_TIMEOUT.
 // ---------------------------------------------------------------------------
 constexpr int kStages = 4;
-constexpr long long kWaitLimit = 1ll << 22;
+constexpr int kConsumers = 512;  // consumer threads per CTA (+ one producer warp)
+constexpr long long kWaitLimit = 1ll << 24;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -239,6 +243,10 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
 }
 
 __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
@@ -269,115 +277,124 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
 }
 
 template <class T, bool THERMAL>
-__global__ void __launch_bounds__(256) k_step_tma(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
-                                                  T *__restrict__ GB, const __grid_constant__ StepParams P,
-                                                  DevState *__restrict__ ds, float *__restrict__ band, int TX,
-                                                  int tiles_x, long long ntiles) {
+__global__ void __launch_bounds__(kConsumers + 32, 1)
+    k_step_tma(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA, T *__restrict__ GB,
+               const __grid_constant__ StepParams P, DevState *__restrict__ ds, float *__restrict__ band, int TY,
+               long long ntiles) {
     extern __shared__ __align__(128) unsigned char smem[];
     constexpr int AL = 16 / (int)sizeof(T);
     constexpr int NQ = THERMAL ? Q + QT : Q;
-    const int W = TX + AL;
+    const int nx = P.nx;
+    const int tcells = TY * nx;
+    const int W = tcells + AL;
     const long long stage_elems = (long long)NQ * W;
     T *stage_base = reinterpret_cast<T *>(smem);
-    uint64_t *bars = reinterpret_cast<uint64_t *>(smem + ((kStages * stage_elems * (long long)sizeof(T) + 15) / 16) * 16);
-    __shared__ int s_ok;
+    uint64_t *full = reinterpret_cast<uint64_t *>(smem + ((kStages * stage_elems * (long long)sizeof(T) + 15) / 16) * 16);
+    uint64_t *empty = full + kStages;
     const int tid = threadIdx.x;
+    const int warp = tid >> 5, lane = tid & 31;
+    const int ncw = kConsumers / 32;  // consumer warps
     if (tid == 0) {
-        for (int st = 0; st < kStages; st++) mbar_init(&bars[st], 1);
+        for (int st = 0; st < kStages; st++) {
+            mbar_init(&full[st], 1);
+            mbar_init(&empty[st], ncw);
+        }
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncthreads();
     const long long G = gridDim.x;
     const long long t0 = blockIdx.x;
     const long long nloc = t0 < ntiles ? (ntiles - t0 + G - 1) / G : 0;
+    const int tiles_y = P.ny / TY;
 
-    auto coords = [&](long long t, int &x0, int &y, int &z) {
-        const long long row = t / tiles_x;
-        x0 = (int)(t - row * tiles_x) * TX;
-        y = (int)(row % P.ny);
-        z = (int)(row / P.ny);
-    };
-    // one thread: arm the stage's barrier and issue the row copies of tile t
-    auto issue = [&](long long t, int st) {
-        int x0, y, z;
-        coords(t, x0, y, z);
-        const bool edge_row = (y == 0 || y == P.ny - 1 || z == 0 || z == P.nz - 1);
-        if (edge_row) {
-            mbar_arrive_expect_tx(&bars[st], 0);
-            return;
-        }
-        const uint32_t full = (uint32_t)((TX + AL) * sizeof(T)), narrow = (uint32_t)(TX * sizeof(T));
-        uint32_t bytes = 0;
+    if (warp == 0) {
+        // ---------------- producer ----------------
+        for (long long k = 0; k < nloc; k++) {
+            const int st = (int)(k % kStages);
+            if (k >= kStages) {
+                bool ok = true;
+                if (lane == 0) ok = mbar_wait_bounded(&empty[st], (uint32_t)(((k / kStages) - 1) & 1));
+                ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+                if (!ok) {
+                    if (lane == 0) atomicOr(&ds->status, ST_TIMEOUT);
+                    return;
+                }
+            }
+            const long long t = t0 + k * G;
+            const int y0 = (int)(t % tiles_y) * TY;
+            const int z = (int)(t / tiles_y);
+            const bool edge_plane = (z == 0 || z == P.nz - 1);
+            const uint32_t full_b = (uint32_t)((tcells + AL) * sizeof(T)), narrow_b = (uint32_t)(tcells * sizeof(T));
+            if (lane == 0) {
+                uint32_t bytes = 0;
+                if (!edge_plane) {
 #pragma unroll
-        for (int q = 0; q < NQ; q++) {
-            const int l = q < Q ? q : q - Q;
-            bytes += cx(l) != 0 ? full : narrow;
+                    for (int q = 0; q < NQ; q++) {
+                        const int l = q < Q ? q : q - Q;
+                        bytes += cx(l) != 0 ? full_b : narrow_b;
+                    }
+                }
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                mbar_arrive_expect_tx(&full[st], bytes);
+            }
+            __syncwarp();
+            if (!edge_plane && lane < NQ) {
+                const int q = lane;
+                const int l = q < Q ? q : q - Q;
+                const T *base = q < Q ? A : GA;
+                const int clx = cx(l), cly = cy(l), clz = cz(l);
+                const long long start = (clx > 0 ? -AL : 0) +
+                                        (long long)nx * ((long long)(y0 - cly) + (long long)P.ny * (z - clz));
+                bulk_g2s(stage_base + st * stage_elems + (long long)q * W, base + l * P.S + start,
+                         clx != 0 ? full_b : narrow_b, &full[st]);
+            }
         }
-        mbar_arrive_expect_tx(&bars[st], bytes);
-        T *dst0 = stage_base + st * stage_elems;
-#pragma unroll
-        for (int q = 0; q < NQ; q++) {
-            const int l = q < Q ? q : q - Q;
-            const T *base = q < Q ? A : GA;
-            const int xs = cx(l) > 0 ? x0 - AL : x0;
-            const T *src = base + l * P.S + xs + (long long)P.nx * ((y - cy(l)) + (long long)P.ny * (z - cz(l)));
-            bulk_g2s(dst0 + (long long)q * W, src, cx(l) != 0 ? full : narrow, &bars[st]);
-        }
-    };
-
-    if (tid == 0)
-        for (long long k = 0; k < nloc && k < kStages; k++) issue(t0 + k * G, (int)k);
-
+        return;
+    }
+    // ---------------- consumers ----------------
+    const int ct = tid - 32;
     for (long long k = 0; k < nloc; k++) {
         const int st = (int)(k % kStages);
         const uint32_t parity = (uint32_t)((k / kStages) & 1);
-        if (tid == 0) s_ok = mbar_wait_bounded(&bars[st], parity) ? 1 : 0;
-        __syncthreads();
-        if (!s_ok) {
-            // the copies of this stage never landed: report, wait (bounded)
-            // for the other stages still in flight, and leave
-            if (tid == 0) {
-                atomicOr(&ds->status, ST_TIMEOUT);
-                for (long long j = k + 1; j < nloc && j < k + kStages; j++)
-                    mbar_wait_bounded(&bars[j % kStages], (uint32_t)((j / kStages) & 1));
-            }
+        bool ok = true;
+        if (lane == 0) ok = mbar_wait_bounded(&full[st], parity);
+        ok = __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+        if (!ok) {
+            if (lane == 0) atomicOr(&ds->status, ST_TIMEOUT);
             return;
         }
-        mbar_try_wait(&bars[st], parity);  // per-thread acquire of the staged data
+        mbar_try_wait(&full[st], parity);  // per-thread acquire of the staged data
         const long long t = t0 + k * G;
-        int x0, y, z;
-        coords(t, x0, y, z);
-        const int x = x0 + tid;
-        const bool valid = tid < TX && x < P.nx;
-        const long long cell = valid ? (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z) : 0;
-        const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) |
-                                 (y == P.ny - 1 ? 8 : 0) | (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
-                              : 0;
-        float f[Q], g[QT];
-        if (raw == 0 && valid) {
-            const T *sb = stage_base + st * stage_elems;
+        const int y0 = (int)(t % tiles_y) * TY;
+        const int z = (int)(t / tiles_y);
+        const T *sb = stage_base + st * stage_elems;
+        for (int c = ct; c < tcells; c += kConsumers) {
+            const int y = y0 + c / nx, x = c - (c / nx) * nx;
+            const long long cell = (long long)x + (long long)nx * ((long long)y + (long long)P.ny * z);
+            const int raw = (x == 0 ? 1 : 0) | (x == nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
+                            (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0);
+            float f[Q], g[QT];
+            if (raw == 0) {
 #pragma unroll
-            for (int l = 0; l < Q; l++) {
-                const int off = cx(l) > 0 ? AL - 1 : (cx(l) < 0 ? 1 : 0);
-                f[l] = St<T>::lds(sb + l * W + tid + off);
-            }
-            if (THERMAL) {
-#pragma unroll
-                for (int l = 0; l < QT; l++) {
+                for (int l = 0; l < Q; l++) {
                     const int off = cx(l) > 0 ? AL - 1 : (cx(l) < 0 ? 1 : 0);
-                    g[l] = St<T>::lds(sb + (Q + l) * W + tid + off);
+                    f[l] = St<T>::lds(sb + l * W + c + off);
                 }
+                if (THERMAL) {
+#pragma unroll
+                    for (int l = 0; l < QT; l++) {
+                        const int off = cx(l) > 0 ? AL - 1 : (cx(l) < 0 ? 1 : 0);
+                        g[l] = St<T>::lds(sb + (Q + l) * W + c + off);
+                    }
+                }
+            } else {
+                gather_flow<T>(A, f, x, y, z, cell, raw, true, true, 1, P);
+                if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, true, true, 1, P);
             }
-        } else {
-            gather_flow<T>(A, f, x, y, z, cell, raw, valid, true, 1, P);
-            if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, true, 1, P);
+            finish_cell<T, THERMAL>(f, g, x, y, z, cell, true, 1, 0, B, GB, P, ds, nullptr, band);
         }
-        finish_cell<T, THERMAL>(f, g, x, y, z, cell, valid, 1, 0, B, GB, P, ds, nullptr, band);
-        __syncthreads();  // every read of this stage is done
-        if (tid == 0 && k + kStages < nloc) {
-            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue(t0 + (k + kStages) * G, st);
-        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
     }
 }
 
@@ -466,13 +483,11 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
     const TmaPlan &tp = a.tma;
     if (tp.enabled && a.gather && !a.export_only && a.mom == nullptr) {
         if (a.thermal)
-            k_step_tma<T, true><<<tp.grid, tp.tx, tp.smem, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA,
-                                                                       (T *)a.GB, *a.P, a.ds, a.band, tp.tx,
-                                                                       tp.tiles_x, tp.ntiles);
+            k_step_tma<T, true><<<tp.grid, kConsumers + 32, tp.smem, a.stream>>>(
+                (const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P, a.ds, a.band, tp.ty, tp.ntiles);
         else
-            k_step_tma<T, false><<<tp.grid, tp.tx, tp.smem, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr,
-                                                                        *a.P, a.ds, a.band, tp.tx, tp.tiles_x,
-                                                                        tp.ntiles);
+            k_step_tma<T, false><<<tp.grid, kConsumers + 32, tp.smem, a.stream>>>(
+                (const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds, a.band, tp.ty, tp.ntiles);
         return cudaGetLastError();
     }
     dim3 blk(a.tx, a.ty, 1);
@@ -496,27 +511,30 @@ cudaError_t launch_step(int storage, const LaunchArgs &a) {
 }
 
 template <class T, bool THERMAL>
-static cudaError_t plan_t(const StepParams &P, int tx_pref, TmaPlan &tp) {
+static cudaError_t plan_t(const StepParams &P, int ty_pref, TmaPlan &tp) {
     constexpr int AL = 16 / (int)sizeof(T);
     constexpr int NQ = THERMAL ? Q + QT : Q;
     tp.enabled = 0;
-    int tx = tx_pref > 0 ? tx_pref : (sizeof(T) == 4 ? 128 : 256);
-    int nx_r = ((P.nx + 31) / 32) * 32;
-    if (tx > nx_r) tx = nx_r;
-    if (P.nx % AL != 0 || tx % 32 != 0 || tx % AL != 0 || tx > 256 || P.ny < 3 || P.nz < 3) return cudaSuccess;
-    const size_t stage_bytes = (size_t)NQ * (tx + AL) * sizeof(T);
-    const size_t smem = ((kStages * stage_bytes + 15) / 16) * 16 + kStages * sizeof(uint64_t);
+    if (P.nx % AL != 0 || P.nx < 2 || P.ny < 3 || P.nz < 3) return cudaSuccess;
+    // rows per tile: about 40 KB of staged populations, dividing ny
+    int ty = ty_pref > 0 ? ty_pref : (int)(40960 / ((size_t)NQ * P.nx * sizeof(T)));
+    if (ty < 1) ty = 1;
+    if (ty > P.ny) ty = P.ny;
+    while (P.ny % ty != 0) ty--;
+    const size_t stage_bytes = (size_t)NQ * ((size_t)ty * P.nx + AL) * sizeof(T);
+    const size_t smem = ((kStages * stage_bytes + 15) / 16) * 16 + 2 * kStages * sizeof(uint64_t);
+    if (smem > 220 * 1024) return cudaSuccess;
     cudaError_t e = cudaFuncSetAttribute(k_step_tma<T, THERMAL>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     int per_sm = 0, dev = 0, sms = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_tma<T, THERMAL>, tx, smem)) != cudaSuccess)
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_step_tma<T, THERMAL>, kConsumers + 32, smem)) !=
+        cudaSuccess)
         return e;
     if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
     if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
     if (per_sm < 1) return cudaSuccess;
-    tp.tx = tx;
-    tp.tiles_x = (P.nx + tx - 1) / tx;
-    tp.ntiles = (long long)tp.tiles_x * P.ny * P.nz;
+    tp.ty = ty;
+    tp.ntiles = (long long)(P.ny / ty) * P.nz;
     tp.smem = smem;
     long long g = (long long)per_sm * sms;
     tp.grid = (int)(g < tp.ntiles ? g : tp.ntiles);
@@ -525,12 +543,12 @@ static cudaError_t plan_t(const StepParams &P, int tx_pref, TmaPlan &tp) {
     return cudaSuccess;
 }
 
-cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int tx_pref, TmaPlan &tp) {
+cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int ty_pref, TmaPlan &tp) {
     switch (storage) {
-    case 0: return thermal ? plan_t<float, true>(P, tx_pref, tp) : plan_t<float, false>(P, tx_pref, tp);
-    case 1: return thermal ? plan_t<__half, true>(P, tx_pref, tp) : plan_t<__half, false>(P, tx_pref, tp);
+    case 0: return thermal ? plan_t<float, true>(P, ty_pref, tp) : plan_t<float, false>(P, ty_pref, tp);
+    case 1: return thermal ? plan_t<__half, true>(P, ty_pref, tp) : plan_t<__half, false>(P, ty_pref, tp);
     case 2:
-        return thermal ? plan_t<__nv_bfloat16, true>(P, tx_pref, tp) : plan_t<__nv_bfloat16, false>(P, tx_pref, tp);
+        return thermal ? plan_t<__nv_bfloat16, true>(P, ty_pref, tp) : plan_t<__nv_bfloat16, false>(P, ty_pref, tp);
     }
     return cudaErrorInvalidValue;
 }

@@ -387,7 +387,7 @@ def body_step(body: Body, mk: Markers, radius: float, force, internal) -> None:
 
 
 def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, steps=10, lit_sign=0,
-                thermal=None, free=None):
+                thermal=None, free=None, outlet=TYPE_OUTZG):
     """Channel + immersed sphere with the GPU path's conventions: inlet
     equilibrium at x = 0, zero-gradient outlet, bounce-back y/z walls,
     Fibonacci markers, interpolated marker density.  thermal = dict(tau_g,
@@ -399,7 +399,7 @@ def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, 
     t = lat.types
     t[:] = TYPE_F
     t[:, :, 0] = TYPE_IN
-    t[:, :, -1] = TYPE_OUTZG
+    t[:, :, -1] = outlet
     t[:, 0, :] = TYPE_S
     t[:, -1, :] = TYPE_S
     t[0, :, :] = TYPE_S
@@ -434,3 +434,9 @@ def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, 
             im = internal_momentum(lat, c, R, lo, hi)
             body_step(body, mk, R, out, im)
     return lat, mk, hist, body
+
+
+def read_dropin_cavity(path: str, n: int) -> dict:
+    """Read the dump of the facade driver dropin_cavity (rho, ux, uy, uz, x fastest)."""
+    a = np.fromfile(path, dtype=np.float64).reshape(4, n, n, n)
+    return {"rho": a[0], "ux": a[1], "uy": a[2], "uz": a[3]}

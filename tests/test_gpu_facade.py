@@ -1,0 +1,47 @@
+"""The C++ drop-in facade (csrc/facade/LBM.h): the reference's own time loops
+(main.cpp:195-221) driving the GPU through the C ABI, against the oracle."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def drivers(pkg):
+    import importlib.util
+
+    p = os.path.join(os.path.dirname(pkg.__file__), "csrc", "facade", "build_facade.py")
+    spec = importlib.util.spec_from_file_location("build_facade", p)
+    m = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(m)
+    return dict(zip(m.DRIVERS, m.build()))
+
+
+def test_dropin_cavity_loop(drivers, orc, tmp_path):
+    n, steps = 16, 200
+    out = str(tmp_path / "cav.bin")
+    subprocess.check_call([drivers["dropin_cavity"], str(n), str(steps), out])
+    g = orc.read_dropin_cavity(out, n)
+    lat = orc.cavity(n, 0.8, 0.05)
+    lat.step_plain(steps)
+    r = orc.moments(lat)
+    for c in ("ux", "uy", "uz"):
+        assert np.abs(g[c] - r[c]).max() / 0.05 < 1e-5
+    assert np.abs(g["rho"] - r["rho"]).max() < 1e-5
+
+
+def test_dropin_sphere_ibm_loop(drivers, orc, tmp_path):
+    nx, ny, nz, tau, D, nm, steps = 48, 28, 28, 0.56, 8.0, 201, 60
+    out = str(tmp_path / "cd.csv")
+    subprocess.check_call([drivers["dropin_sphere"], str(nx), str(ny), str(nz), str(tau), str(D), str(nm),
+                           str(steps), out])
+    cd = np.loadtxt(out, delimiter=",", skiprows=1)
+    assert cd.shape == (steps, 3)
+    center = (nx / 4.0, ny / 2.0, nz / 2.0)
+    lat, mk, hist, _ = orc.sphere_case(nx, ny, nz, tau, D, center, nm, 5, 0.05, steps, outlet=orc.TYPE_OUT)
+    q = 0.5 * 0.05 ** 2 * orc.REF_PI * D * D / 4
+    ref_cd = hist[:, 0] / q
+    assert np.abs(cd[:, 1] - ref_cd).max() / np.abs(ref_cd).max() < 1e-3
