@@ -66,7 +66,8 @@ enum { LBM_FIELD_RHO = 0, LBM_FIELD_UX = 1, LBM_FIELD_UY = 2, LBM_FIELD_UZ = 3, 
 enum {
     LBM_STATUS_RHO_RANGE = 1,   /* rho outside (0, 100) or NaN: lbm.cpp:772-775 */
     LBM_STATUS_BAND_EDGE = 2,   /* an IBM stencil reached outside the band/interior */
-    LBM_STATUS_NONFINITE_FORCE = 4
+    LBM_STATUS_NONFINITE_FORCE = 4,
+    LBM_STATUS_TIMEOUT = 16     /* a bounded device wait (mbarrier, grid barrier) gave up */
 };
 
 typedef struct lbm_face {
@@ -92,8 +93,8 @@ typedef struct lbm_config {
     double gbeta[3];      /* Boussinesq: F += gbeta * (T - T0)  (lbm.cpp:804-805) */
     int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
     int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
-    int staged;           /* bulk-copy staged kernel: 0 = default rows per tile, >0 = rows per tile, <0 = off */
-    int ibm_fused;        /* >0: IBM phase as one thread-block-cluster launch (when it fits); 0 = multi-kernel */
+    int staged;           /* bulk-copy (TMA) staged kernel: 0 = off, 1 = on, >1 = on with that many rows per tile */
+    int ibm_fused;        /* 0: IBM phase as one cooperative launch when the device allows; <0: chain of kernels */
 } lbm_config;
 
 typedef struct lbm_ibm_config {
@@ -144,8 +145,13 @@ lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const dou
  * Collision -> Streaming -> MacroProp).  Asynchronous on the handle's stream. */
 lbm_status lbmgpu_step(lbm_handle *h, int nsteps);
 
-/* Same, with CUDA events on the handle's stream: total device time of the
- * n steps and the summed device time of the fused collide-stream kernel. */
+/* lbmgpu_step bracketed by CUDA events on the handle's stream (graph replay
+ * included): device time of the n steps. */
+lbm_status lbmgpu_step_timed(lbm_handle *h, int nsteps, double *ms);
+
+/* Steps launched one by one with CUDA events on the handle's stream: total
+ * device time of the n steps and the summed device time of the fused
+ * collide-stream kernel. */
 lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms);
 
 /* MacroProp moments of the current state (rho, u = (sum f c + F/2)/rho, T),

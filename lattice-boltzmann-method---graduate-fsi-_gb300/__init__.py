@@ -26,12 +26,12 @@ STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
 FACE_WALL, FACE_INLET, FACE_OUTLET_EQ, FACE_OUTLET_ZG, FACE_PERIODIC = 0, 1, 2, 3, 4
 TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
 FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
-STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE = 1, 2, 4
+STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE, STATUS_TIMEOUT = 1, 2, 4, 16
 
 # Every symbol include/lbmgpu.h declares.
 ABI_SYMBOLS = [
     "lbmgpu_config_from_types", "lbmgpu_create", "lbmgpu_destroy", "lbmgpu_init", "lbmgpu_init_fields",
-    "lbmgpu_set_markers", "lbmgpu_step", "lbmgpu_step_profiled", "lbmgpu_download", "lbmgpu_download_f32",
+    "lbmgpu_set_markers", "lbmgpu_step", "lbmgpu_step_timed", "lbmgpu_step_profiled", "lbmgpu_download", "lbmgpu_download_f32",
     "lbmgpu_download_all_f32", "lbmgpu_get_forces", "lbmgpu_get_body", "lbmgpu_get_markers", "lbmgpu_status",
     "lbmgpu_sync", "lbmgpu_steps_done", "lbmgpu_device_bytes", "lbmgpu_host_alloc", "lbmgpu_host_free",
     "lbmgpu_last_error", "lbmgpu_abi_version",
@@ -89,6 +89,7 @@ def load(path: str | None = None):
     L.lbmgpu_init_fields.argtypes = [vp, dp, dp, dp, dp, dp]
     L.lbmgpu_set_markers.argtypes = [vp, C.POINTER(IbmConfig), dp, dp, dp]
     L.lbmgpu_step.argtypes = [vp, i]
+    L.lbmgpu_step_timed.argtypes = [vp, i, dp]
     L.lbmgpu_step_profiled.argtypes = [vp, i, dp, dp]
     L.lbmgpu_download.argtypes = [vp, i, dp]
     L.lbmgpu_download_f32.argtypes = [vp, i, C.POINTER(C.c_float)]
@@ -220,6 +221,11 @@ class Solver:
 
     def step(self, n: int = 1):
         check(self.L.lbmgpu_step(self.h, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        ms = C.c_double()
+        check(self.L.lbmgpu_step_timed(self.h, int(n), C.byref(ms)))
+        return ms.value
 
     def step_profiled(self, n: int):
         tot, fused = C.c_double(), C.c_double()

@@ -56,8 +56,10 @@ struct lbm_handle {
     int gsteps = 16;
     int tx = 128, ty = 2;
     TmaPlan tma;
-    FusedPlan fused;
-    int use_fused = 1;
+    CoopPlan coop;
+    int use_coop = 1;
+    GridBarrier *gbar = nullptr;  // grid barrier of the one-launch IBM phase
+    double *gpart = nullptr;      // its per-CTA partial sums
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
@@ -263,6 +265,8 @@ static void free_handle(lbm_handle *h) {
     cudaFree(h->band);
     cudaFree(h->ds);
     cudaFree(h->hist);
+    cudaFree(h->gbar);
+    cudaFree(h->gpart);
     cudaFree(h->mk.pos);
     cudaFree(h->mk.ds);
     cudaFree(h->mk.udes);
@@ -336,6 +340,8 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     // one row and one 16-byte group past the last plane stays inside the
     // array, and a guard of kGuard cells before the first array.
     P.S = ((P.N + std::max<long long>(512, 2LL * P.nx + 64) + 255) / 256) * 256;
+    for (int l = 0; l < Q; l++)
+        P.pofs[l] = (long long)l * P.S - ((long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l)));
     const size_t fb = ((size_t)Q * P.S + 2 * kGuard) * h->esize;
     for (int i = 0; i < 2 && st == LBM_OK; i++) {
         chk(dalloc(h, &h->fraw[i], fb), "populations");
@@ -357,8 +363,9 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaMemsetAsync(h->hist, 0, (size_t)h->hist_cap * 8 * sizeof(double), h->s), "history init");
     }
     for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
-    if (st == LBM_OK && c.staged >= 0) chk(plan_tma(c.storage, c.thermal != 0, P, c.staged, h->tma), "staged plan");
-    h->use_fused = c.ibm_fused > 0 ? 1 : 0;
+    if (st == LBM_OK && c.staged > 0)
+        chk(plan_tma(c.storage, c.thermal != 0, P, c.staged > 1 ? c.staged : 0, h->tma), "staged plan");
+    h->use_coop = c.ibm_fused >= 0 ? 1 : 0;
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);
@@ -379,6 +386,7 @@ static lbm_status do_init(lbm_handle *h, const float *dfields) {
     float init[5] = {(float)h->cfg.rho0, (float)h->cfg.u0[0], (float)h->cfg.u0[1], (float)h->cfg.u0[2],
                      (float)h->cfg.T_init};
     CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, h->P.S, dfields, init, h->cfg.thermal != 0, h->s));
+    if (h->gbar) CUDA_TRY(cudaMemsetAsync(h->gbar, 0, sizeof(GridBarrier), h->s));
     h->cur = 0;
     h->steps = 0;
     h->inited = true;
@@ -494,8 +502,15 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
     h->ibm = true;
-    h->fused.enabled = 0;
-    if (h->use_fused) CUDA_TRY(plan_ibm_fused(h->cfg.storage, h->cfg.thermal != 0, h->P, n, h->fused));
+    h->coop.enabled = 0;
+    if (h->use_coop) {
+        CUDA_TRY(plan_ibm_coop(h->cfg.storage, h->cfg.thermal != 0, h->coop));
+        if (h->coop.enabled && !h->gbar) {
+            CUDA_TRY(dalloc(h, &h->gbar, sizeof(GridBarrier)));
+            CUDA_TRY(dalloc(h, &h->gpart, (size_t)h->coop.grid * 16 * sizeof(double)));
+        }
+        if (h->gbar) CUDA_TRY(cudaMemsetAsync(h->gbar, 0, sizeof(GridBarrier), h->s));
+    }
     // graphs captured earlier do not contain the IBM launches
     for (int i = 0; i < 2; i++)
         if (h->gexec[i]) {
@@ -545,9 +560,9 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaE
         ia.thermal = h->icfg.thermal;
         ia.stream = h->s;
         const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
-        if (h->fused.enabled) {
-            if ((e = launch_ibm_fused(h->cfg.storage, h->cfg.thermal != 0, ia, h->fused, a.B, a.GB, h->bp, h->hist,
-                                      h->hist_cap, h->icfg.m_max, fsign)) != cudaSuccess)
+        if (h->coop.enabled) {
+            if ((e = launch_ibm_coop(h->cfg.storage, h->cfg.thermal != 0, ia, h->coop, a.B, a.GB, h->bp, h->hist,
+                                     h->hist_cap, h->icfg.m_max, fsign, h->gbar, h->gpart)) != cudaSuccess)
                 return e;
         } else {
             for (int it = 1; it <= h->icfg.m_max; it++) {
@@ -597,8 +612,13 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
             continue;
         }
         if (h->gsteps > 0 && nsteps >= h->gsteps) {
-            lbm_status s = ensure_graph(h);
-            if (s != LBM_OK) return s;
+            if (ensure_graph(h) != LBM_OK) {
+                // a launch that cannot be captured on this device/driver:
+                // keep stepping eagerly from now on
+                cudaGetLastError();
+                h->gsteps = 0;
+                continue;
+            }
             CUDA_TRY(cudaGraphLaunch(h->gexec[h->cur], h->s));
             h->steps += h->gsteps;
             nsteps -= h->gsteps;
@@ -608,6 +628,19 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
         h->steps++;
         nsteps--;
     }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_step_timed(lbm_handle *h, int nsteps, double *ms) {
+    if (!h || !ms) return fail(LBM_ERR_INVALID, "step_timed: null argument");
+    CUDA_TRY(cudaEventRecord(h->ev[0], h->s));
+    lbm_status st = lbmgpu_step(h, nsteps);
+    if (st != LBM_OK) return st;
+    CUDA_TRY(cudaEventRecord(h->ev[1], h->s));
+    CUDA_TRY(cudaEventSynchronize(h->ev[1]));
+    float t = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&t, h->ev[0], h->ev[1]));
+    *ms = t;
     return LBM_OK;
 }
 

@@ -21,24 +21,62 @@ __device__ __forceinline__ float inv_one_plus(float drho) {
 //   feq - w = w (drho + (1 + drho) P3(u)) with the third-order P3 of Calc_feq
 //   (lbm.cpp:628-633), S = (1 - omega/2) w (3 c.F + 9 (c.F)(c.u) - 3 F.u)
 //   (lbm.cpp:101-102).
+// Links come in opposite pairs (l, l+1) for odd l (LBM.h:551), so
+// P3 = E(cu) +/- O(cu) with E = 4.5 cu^2 - 1.5 u^2 and
+// O = cu (3 + 4.5 (cu^2 - u^2)), and likewise for S: the pair shares one
+// evaluation of each part.
 __device__ __forceinline__ void collide_flow(float f[Q], float drho, float ux, float uy, float uz, float Fx,
                                              float Fy, float Fz, bool forced, float omega) {
     const float usq = ux * ux + uy * uy + uz * uz;
     const float c1 = 1.0f - omega;
     const float gs = 1.0f - 0.5f * omega;
     const float Fu = Fx * ux + Fy * uy + Fz * uz;
+    {
+        const float p = -1.5f * usq;
+        f[0] = c1 * f[0] + omega * wf(0) * (drho + p + drho * p);
+        if (forced) f[0] += gs * wf(0) * (-3.0f * Fu);
+    }
 #pragma unroll
-    for (int l = 0; l < Q; l++) {
+    for (int l = 1; l < Q; l += 2) {
         const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
-        const float p3 = cu * (3.0f + 4.5f * cu + 4.5f * cu * cu - 4.5f * usq) - 1.5f * usq;
-        // w (rho (1 + P3) - 1) = w (drho + P3 + drho P3), without forming 1 + drho
-        float out = c1 * f[l] + omega * wf(l) * (drho + p3 + drho * p3);
+        const float cu2 = cu * cu;
+        const float ev = 4.5f * cu2 - 1.5f * usq;
+        const float od = cu * (3.0f + 4.5f * (cu2 - usq));
+        // (1 + drho) x without forming 1 + drho
+        const float be = drho + ev + drho * ev;
+        const float bo = od + drho * od;
+        const float ow = omega * wf(l);
+        float a = c1 * f[l] + ow * (be + bo);
+        float b = c1 * f[l + 1] + ow * (be - bo);
         if (forced) {
             const float cF = cx(l) * Fx + cy(l) * Fy + cz(l) * Fz;
-            out += gs * wf(l) * (3.0f * cF + 9.0f * cF * cu - 3.0f * Fu);
+            const float e = 9.0f * cF * cu - 3.0f * Fu;
+            const float o = 3.0f * cF;
+            const float gw = gs * wf(l);
+            a += gw * (e + o);
+            b += gw * (e - o);
         }
-        f[l] = out;
+        f[l] = a;
+        f[l + 1] = b;
     }
+}
+
+// Moments of shifted populations, summed by opposite pairs:
+// drho = sum f~, j = sum c f~ (sum w = 1, sum w c = 0).
+__device__ __forceinline__ void moments_pairs(const float f[Q], float &drho, float &jx, float &jy, float &jz) {
+    float r = f[0], x = 0.0f, y = 0.0f, z = 0.0f;
+#pragma unroll
+    for (int l = 1; l < Q; l += 2) {
+        const float s = f[l] + f[l + 1], d = f[l] - f[l + 1];
+        r += s;
+        if (cx(l) != 0) x += cx(l) * d;
+        if (cy(l) != 0) y += cy(l) * d;
+        if (cz(l) != 0) z += cz(l) * d;
+    }
+    drho = r;
+    jx = x;
+    jy = y;
+    jz = z;
 }
 
 // D3Q7 BGK with source: g* = g - omega_t (g - w T (1 + 4 c.u)) + (1 - omega_t/2) w Qh.

@@ -79,6 +79,7 @@ struct StepParams {
     int periodic;          // bit a: axis a periodic
     long long N;           // nx * ny * nz
     long long S;           // population stride (>= N + one tile of slack, see lbm_abi.cu)
+    long long pofs[Q];     // l * S - (cx + nx (cy + ny cz)): pull offset of link l from the cell
     float omega;           // dt / tau
     float omega_t;         // dt / tau_g
     float body[3];         // uniform body force

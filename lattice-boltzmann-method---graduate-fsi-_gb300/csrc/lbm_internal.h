@@ -77,15 +77,18 @@ struct BodyParams {
 };
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap);
 
-// Single-launch IBM phase on one thread-block cluster (k_ibm_fused).
-struct FusedPlan {
-    int enabled = 0;
-    int cl = 0, slab = 0, nloc_max = 0;
-    size_t smem = 0;
+// Single-launch IBM phase on a cooperative grid (k_ibm_coop).
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
 };
-cudaError_t plan_ibm_fused(int storage, bool thermal, const StepParams &P, int n_markers, FusedPlan &fp);
-cudaError_t launch_ibm_fused(int storage, bool lattice_thermal, const IbmArgs &a, const FusedPlan &fp, void *B,
-                             void *GB, const BodyParams &bp, double *hist, long long hist_cap, int m_max,
-                             float fsign);
+struct CoopPlan {
+    int enabled = 0;
+    int grid = 0;
+};
+cudaError_t plan_ibm_coop(int storage, bool thermal, CoopPlan &cp);
+cudaError_t launch_ibm_coop(int storage, bool lattice_thermal, const IbmArgs &a, const CoopPlan &cp, void *B,
+                            void *GB, const BodyParams &bp, double *hist, long long hist_cap, int m_max, float fsign,
+                            GridBarrier *gb, double *part);
 
 }  // namespace lbmk

@@ -28,11 +28,9 @@ __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q],
         return;
     }
     if (!bwarp) {
+        const T *a = A + cell;
 #pragma unroll
-        for (int l = 0; l < Q; l++) {
-            const long long off = (long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l));
-            f[l] = valid ? St<T>::ld(A + l * P.S + cell - off) : 0.0f;
-        }
+        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
         return;
     }
     const int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
@@ -74,11 +72,9 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
         return;
     }
     if (!bwarp) {
+        const T *a = G + cell;
 #pragma unroll
-        for (int l = 0; l < QT; l++) {
-            const long long off = (long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l));
-            g[l] = valid ? St<T>::ld(G + l * P.S + cell - off) : 0.0f;
-        }
+        for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
         return;
     }
     const int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
@@ -113,20 +109,14 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
 
 // Everything after the gather of one cell: moments, optional moment output,
 // band hand-off or collision, and the stores to B.
-template <class T, bool THERMAL>
+template <class T, bool THERMAL, bool FORCED>
 __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
                                             int gather, int export_only, T *__restrict__ B, T *__restrict__ GB,
                                             const StepParams &P, DevState *__restrict__ ds, float *__restrict__ mom,
                                             float *__restrict__ band) {
     const long long N = P.N;
-    float drho = 0.0f, jx = 0.0f, jy = 0.0f, jz = 0.0f;
-#pragma unroll
-    for (int l = 0; l < Q; l++) {
-        drho += f[l];
-        jx += cx(l) * f[l];
-        jy += cy(l) * f[l];
-        jz += cz(l) * f[l];
-    }
+    float drho, jx, jy, jz;
+    moments_pairs(f, drho, jx, jy, jz);
     float Tc = 0.0f;
     float Fx = P.body[0], Fy = P.body[1], Fz = P.body[2];
     if (THERMAL) {
@@ -181,7 +171,7 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
             return;
         }
     }
-    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, P.forced != 0, P.omega);
+    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, FORCED, P.omega);
 #pragma unroll
     for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
     if (THERMAL) {
@@ -195,7 +185,7 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
 // step (A then holds the initial pre-collision populations in place);
 // export_only = 1 computes and writes the moments of the gathered state
 // without colliding or storing.
-template <class T, bool THERMAL>
+template <class T, bool THERMAL, bool FORCED>
 __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
                                               T *__restrict__ GB, const __grid_constant__ StepParams P,
                                               DevState *__restrict__ ds, float *__restrict__ mom,
@@ -212,7 +202,7 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
     float f[Q], g[QT];
     gather_flow<T>(A, f, x, y, z, cell, raw, valid, bwarp, gather, P);
     if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, bwarp, gather, P);
-    finish_cell<T, THERMAL>(f, g, x, y, z, cell, valid, gather, export_only, B, GB, P, ds, mom, band);
+    finish_cell<T, THERMAL, FORCED>(f, g, x, y, z, cell, valid, gather, export_only, B, GB, P, ds, mom, band);
 }
 
 // ---------------------------------------------------------------------------
@@ -391,7 +381,7 @@ __global__ void __launch_bounds__(kConsumers + 32, 1)
                 gather_flow<T>(A, f, x, y, z, cell, raw, true, true, 1, P);
                 if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, true, true, 1, P);
             }
-            finish_cell<T, THERMAL>(f, g, x, y, z, cell, true, 1, 0, B, GB, P, ds, nullptr, band);
+            finish_cell<T, THERMAL, true>(f, g, x, y, z, cell, true, 1, 0, B, GB, P, ds, nullptr, band);
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[st]);
@@ -492,12 +482,16 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
     }
     dim3 blk(a.tx, a.ty, 1);
     dim3 grd((a.P->nx + a.tx - 1) / a.tx, (a.P->ny + a.ty - 1) / a.ty, a.P->nz);
+    const bool forced = a.P->forced != 0;
     if (a.thermal)
-        k_step<T, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P, a.ds,
-                                                   a.mom, a.band, a.gather, a.export_only);
+        k_step<T, true, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P,
+                                                         a.ds, a.mom, a.band, a.gather, a.export_only);
+    else if (forced)
+        k_step<T, false, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds,
+                                                          a.mom, a.band, a.gather, a.export_only);
     else
-        k_step<T, false><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds, a.mom,
-                                                    a.band, a.gather, a.export_only);
+        k_step<T, false, false><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds,
+                                                           a.mom, a.band, a.gather, a.export_only);
     return cudaGetLastError();
 }
 

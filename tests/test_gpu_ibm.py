@@ -36,11 +36,11 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
     return s
 
 
-@pytest.mark.parametrize("fused", [1, 0], ids=["cluster", "multikernel"])
+@pytest.mark.parametrize("fused", [0, -1], ids=["onelaunch", "chain"])
 @pytest.mark.parametrize("lit_sign", [0, 1])
 def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, fused):
-    """Both IBM drivers: the single thread-block-cluster launch and the
-    multi-kernel chain."""
+    """Both IBM drivers: the one-launch cooperative kernel and the chain of
+    kernels."""
     nx, ny, nz, tau, D, nm, m_max, steps = 48, 30, 28, 0.56, 10.0, 314, 3, 120
     center = (16.0, 15.3, 14.6)
     s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, fused=fused)
@@ -74,7 +74,7 @@ def test_fixed_sphere_fp16_drag(pkg, orc):
     assert ed < 5e-3 and eu < 1e-3
 
 
-@pytest.mark.parametrize("fused", [1, 0], ids=["cluster", "multikernel"])
+@pytest.mark.parametrize("fused", [0, -1], ids=["onelaunch", "chain"])
 def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     """D3Q7 thermal population, Boussinesq force, thermal IBM (T_body = 1)
     and the FP64 Newton-Euler body (held in x and rotation, free in y and z)
@@ -110,17 +110,17 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     assert np.abs(xyz - oxyz).max() < 1e-6
 
 
-def test_cluster_and_multikernel_ibm_agree(pkg, orc):
+def test_onelaunch_and_chain_ibm_agree(pkg, orc):
     """The two IBM drivers give the same forces and fields (up to the order of
-    float atomics)."""
+    float atomics), on the benchmark's sphere at reduced domain size."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
     center = (24.0, 20.0, 20.0)
     out = []
-    for fused in (1, 0):
-        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f16", fused=fused)
+    for fused in (0, -1):
+        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", fused=fused)
         s.step(steps)
         out.append((s.forces(), s.moments()))
         assert s.status() == 0
     fa, fb = out[0][0], out[1][0]
     assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
-    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-4
+    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-5
