@@ -179,6 +179,31 @@ lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes);
 lbm_status lbmgpu_host_alloc(size_t bytes, void **ptr);
 lbm_status lbmgpu_host_free(void *ptr);
 
+/* ------------------------------------------------------------------------
+ * Batched cavities: many independent lid-driven cavities of uneven sizes
+ * (each the reference's box with TYPE_S ghost walls and the lid on the
+ * j = Ny+1 plane, lbm.cpp:1548-1551), advanced together by one persistent
+ * launch per time step over a flattened tile queue, replayed through CUDA
+ * graphs.  No counterpart in the reference (it runs one case per build);
+ * each cavity follows LBM::Collision/Streaming/MacroProp.
+ * ------------------------------------------------------------------------ */
+typedef struct lbm_batch lbm_batch;
+/* dims: [n][3] interior extents; tau: [n]; lid_u: lid velocity along x. */
+lbm_status lbmgpu_batch_create(int n, const int *dims, const double *tau, double lid_u, int storage,
+                               lbm_batch **out);
+lbm_status lbmgpu_batch_destroy(lbm_batch *b);
+lbm_status lbmgpu_batch_init(lbm_batch *b);
+lbm_status lbmgpu_batch_step(lbm_batch *b, int nsteps);
+lbm_status lbmgpu_batch_step_timed(lbm_batch *b, int nsteps, double *ms);
+/* Choose threads per tile and grid shape by timing; chosen = {threads, grid}.
+ * Advances the state: re-initialise afterwards. */
+lbm_status lbmgpu_batch_autotune(lbm_batch *b, int *chosen);
+/* rho, ux, uy, uz of one cavity ([4][cells], x fastest). */
+lbm_status lbmgpu_batch_download(lbm_batch *b, int problem, float *host);
+/* Per-cavity status words (LBM_STATUS_*). */
+lbm_status lbmgpu_batch_status(lbm_batch *b, uint32_t *flags);
+lbm_status lbmgpu_batch_info(lbm_batch *b, long long *total_cells, long long *steps);
+
 const char *lbmgpu_last_error(void);
 int lbmgpu_abi_version(void);
 

@@ -35,6 +35,9 @@ ABI_SYMBOLS = [
     "lbmgpu_download_all_f32", "lbmgpu_get_forces", "lbmgpu_get_body", "lbmgpu_get_markers", "lbmgpu_status",
     "lbmgpu_sync", "lbmgpu_steps_done", "lbmgpu_device_bytes", "lbmgpu_host_alloc", "lbmgpu_host_free",
     "lbmgpu_last_error", "lbmgpu_abi_version",
+    "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
+    "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
+    "lbmgpu_batch_info",
 ]
 
 
@@ -103,6 +106,15 @@ def load(path: str | None = None):
     L.lbmgpu_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
     L.lbmgpu_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
     L.lbmgpu_host_free.argtypes = [vp]
+    L.lbmgpu_batch_create.argtypes = [i, C.POINTER(C.c_int), dp, d, i, C.POINTER(vp)]
+    L.lbmgpu_batch_destroy.argtypes = [vp]
+    L.lbmgpu_batch_init.argtypes = [vp]
+    L.lbmgpu_batch_step.argtypes = [vp, i]
+    L.lbmgpu_batch_step_timed.argtypes = [vp, i, dp]
+    L.lbmgpu_batch_autotune.argtypes = [vp, C.POINTER(C.c_int)]
+    L.lbmgpu_batch_download.argtypes = [vp, i, C.POINTER(C.c_float)]
+    L.lbmgpu_batch_status.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     for nm in ABI_SYMBOLS:
         fn = getattr(L, nm)
         if fn.restype is None and nm not in ("lbmgpu_last_error", "lbmgpu_abi_version"):
@@ -299,3 +311,61 @@ def config_from_types(nx, ny, nz, tau, types, rho=None, ux=None, uy=None, uz=Non
     check(L.lbmgpu_config_from_types(nx, ny, nz, tau, t.ctypes.data_as(C.POINTER(C.c_uint8)), *ptrs,
                                      C.byref(cfg)))
     return cfg
+
+
+class Batch:
+    """Many lid-driven cavities advanced together (lbmgpu_batch_*)."""
+
+    def __init__(self, dims, taus, lid=0.05, storage="f16"):
+        self.L = load()
+        self.dims = np.ascontiguousarray(np.asarray(dims, dtype=np.int32).reshape(-1, 3))
+        self.taus = np.ascontiguousarray(np.asarray(taus, dtype=np.float64))
+        self.n = self.dims.shape[0]
+        self.h = C.c_void_p()
+        st = STORAGE[storage] if isinstance(storage, str) else storage
+        check(self.L.lbmgpu_batch_create(self.n, self.dims.ctypes.data_as(C.POINTER(C.c_int)), _dp(self.taus), lid, st,
+                                         C.byref(self.h)))
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            self.L.lbmgpu_batch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def init(self):
+        check(self.L.lbmgpu_batch_init(self.h))
+
+    def step(self, n):
+        check(self.L.lbmgpu_batch_step(self.h, int(n)))
+
+    def step_timed(self, n) -> float:
+        ms = C.c_double()
+        check(self.L.lbmgpu_batch_step_timed(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def autotune(self):
+        ch = (C.c_int * 2)()
+        check(self.L.lbmgpu_batch_autotune(self.h, ch))
+        return ch[0], ch[1]
+
+    def moments(self, p) -> dict:
+        nx, ny, nz = (int(v) for v in self.dims[p])
+        out = np.empty(4 * nx * ny * nz, dtype=np.float32)
+        check(self.L.lbmgpu_batch_download(self.h, p, out.ctypes.data_as(C.POINTER(C.c_float))))
+        out = out.reshape(4, nz, ny, nx)
+        return {"rho": out[0], "ux": out[1], "uy": out[2], "uz": out[3]}
+
+    def status(self) -> np.ndarray:
+        out = np.zeros(self.n, dtype=np.uint32)
+        check(self.L.lbmgpu_batch_status(self.h, out.ctypes.data_as(C.POINTER(C.c_uint32))))
+        return out
+
+    def total_cells(self) -> int:
+        v = C.c_longlong()
+        check(self.L.lbmgpu_batch_info(self.h, C.byref(v), None))
+        return v.value

@@ -23,6 +23,8 @@ static lbm_status fail(lbm_status s, const std::string &msg) {
     return s;
 }
 
+void lbm_set_last_error(const std::string &m) { g_err = m; }
+
 #define CUDA_TRY(expr)                                                                                    \
     do {                                                                                                  \
         cudaError_t e_ = (expr);                                                                          \
@@ -56,10 +58,8 @@ struct lbm_handle {
     int gsteps = 16;
     int tx = 128, ty = 2;
     TmaPlan tma;
-    CoopPlan coop;
-    int use_coop = 1;
-    GridBarrier *gbar = nullptr;  // grid barrier of the one-launch IBM phase
-    double *gpart = nullptr;      // its per-CTA partial sums
+    AsmPlan asmp;
+    int use_asm = 1;
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
@@ -254,6 +254,16 @@ extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double ta
     return LBM_OK;
 }
 
+static void free_asm(lbm_handle *h) {
+    cudaFree(h->asmp.pair_ptr);
+    cudaFree(h->asmp.pair_idx);
+    cudaFree(h->asmp.pairA);
+    cudaFree(h->asmp.pairB);
+    cudaFree(h->asmp.node_ptr);
+    cudaFree(h->asmp.node_mk);
+    h->asmp = AsmPlan();
+}
+
 static void free_handle(lbm_handle *h) {
     if (!h) return;
     for (int i = 0; i < 2; i++) {
@@ -265,8 +275,9 @@ static void free_handle(lbm_handle *h) {
     cudaFree(h->band);
     cudaFree(h->ds);
     cudaFree(h->hist);
-    cudaFree(h->gbar);
-    cudaFree(h->gpart);
+    free_asm(h);
+    cudaFree(h->mk.u0);
+    cudaFree(h->mk.t0);
     cudaFree(h->mk.pos);
     cudaFree(h->mk.ds);
     cudaFree(h->mk.udes);
@@ -365,7 +376,7 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
     if (st == LBM_OK && c.staged > 0)
         chk(plan_tma(c.storage, c.thermal != 0, P, c.staged > 1 ? c.staged : 0, h->tma), "staged plan");
-    h->use_coop = c.ibm_fused >= 0 ? 1 : 0;
+    h->use_asm = c.ibm_fused >= 0 ? 1 : 0;
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);
@@ -386,7 +397,6 @@ static lbm_status do_init(lbm_handle *h, const float *dfields) {
     float init[5] = {(float)h->cfg.rho0, (float)h->cfg.u0[0], (float)h->cfg.u0[1], (float)h->cfg.u0[2],
                      (float)h->cfg.T_init};
     CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, h->P.S, dfields, init, h->cfg.thermal != 0, h->s));
-    if (h->gbar) CUDA_TRY(cudaMemsetAsync(h->gbar, 0, sizeof(GridBarrier), h->s));
     h->cur = 0;
     h->steps = 0;
     h->inited = true;
@@ -442,6 +452,8 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         cudaFree(h->mk.force);
         cudaFree(h->mk.acc);
         cudaFree(h->band);
+        cudaFree(h->mk.u0);
+        cudaFree(h->mk.t0);
         memset(&h->mk, 0, sizeof(h->mk));
         h->band = nullptr;
         CUDA_TRY(dalloc(h, &h->mk.pos, (size_t)3 * n * sizeof(double)));
@@ -502,14 +514,62 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
     h->ibm = true;
-    h->coop.enabled = 0;
-    if (h->use_coop) {
-        CUDA_TRY(plan_ibm_coop(h->cfg.storage, h->cfg.thermal != 0, h->coop));
-        if (h->coop.enabled && !h->gbar) {
-            CUDA_TRY(dalloc(h, &h->gbar, sizeof(GridBarrier)));
-            CUDA_TRY(dalloc(h, &h->gpart, (size_t)h->coop.grid * 16 * sizeof(double)));
+    // assembled (marker-space) IBM: rigid pattern that only translates, and
+    // a marker count the one-CTA iteration holds in shared memory
+    free_asm(h);
+    const bool rotates = ic->free_body && ((h->bp.dof >> 3) & 7);
+    if (h->use_asm && n <= 4096 && !rotates) {
+        std::vector<int> pptr(n + 1, 0), pidx;
+        for (int m = 0; m < n; m++) {
+            for (int j = 0; j < n; j++) {
+                bool near = true;
+                for (int a = 0; a < 3 && near; a++)
+                    near = std::fabs(xyz[(size_t)a * n + m] - xyz[(size_t)a * n + j]) < 4.0;
+                if (near) pidx.push_back(j);
+            }
+            pptr[m + 1] = (int)pidx.size();
         }
-        if (h->gbar) CUDA_TRY(cudaMemsetAsync(h->gbar, 0, sizeof(GridBarrier), h->s));
+        CUDA_TRY(dalloc(h, &h->asmp.pair_ptr, pptr.size() * sizeof(int)));
+        CUDA_TRY(dalloc(h, &h->asmp.pair_idx, pidx.size() * sizeof(int)));
+        CUDA_TRY(dalloc(h, &h->asmp.pairA, pidx.size() * sizeof(float)));
+        CUDA_TRY(dalloc(h, &h->asmp.pairB, pidx.size() * sizeof(float)));
+        CUDA_TRY(cudaMemcpyAsync(h->asmp.pair_ptr, pptr.data(), pptr.size() * sizeof(int), cudaMemcpyHostToDevice, h->s));
+        CUDA_TRY(cudaMemcpyAsync(h->asmp.pair_idx, pidx.data(), pidx.size() * sizeof(int), cudaMemcpyHostToDevice, h->s));
+        CUDA_TRY(cudaMemsetAsync(h->asmp.pairB, 0, pidx.size() * sizeof(float), h->s));
+        if (!ic->free_body) {
+            // band node -> markers whose 4x4x4 stencil covers it
+            std::vector<std::vector<int>> lists((size_t)nb);
+            for (int m = 0; m < n; m++) {
+                int lo[3];
+                for (int a = 0; a < 3; a++) lo[a] = (int)std::floor(xyz[(size_t)a * n + m]) - 2 - org[a];
+                for (int c = 0; c < 4; c++)
+                    for (int b2 = 0; b2 < 4; b2++)
+                        for (int a2 = 0; a2 < 4; a2++) {
+                            int bx = lo[0] + a2, by = lo[1] + b2, bz = lo[2] + c;
+                            if (bx < 0 || by < 0 || bz < 0 || bx >= bs[0] || by >= bs[1] || bz >= bs[2]) continue;
+                            lists[(size_t)bx + (size_t)bs[0] * ((size_t)by + (size_t)bs[1] * bz)].push_back(m);
+                        }
+            }
+            std::vector<int> nptr(nb + 1, 0), nmk;
+            for (long long b2 = 0; b2 < nb; b2++) {
+                nmk.insert(nmk.end(), lists[b2].begin(), lists[b2].end());
+                nptr[b2 + 1] = (int)nmk.size();
+            }
+            CUDA_TRY(dalloc(h, &h->asmp.node_ptr, nptr.size() * sizeof(int)));
+            CUDA_TRY(dalloc(h, &h->asmp.node_mk, std::max<size_t>(1, nmk.size()) * sizeof(int)));
+            CUDA_TRY(cudaMemcpyAsync(h->asmp.node_ptr, nptr.data(), nptr.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                     h->s));
+            if (!nmk.empty())
+                CUDA_TRY(cudaMemcpyAsync(h->asmp.node_mk, nmk.data(), nmk.size() * sizeof(int),
+                                         cudaMemcpyHostToDevice, h->s));
+        }
+        if (!h->mk.u0) {
+            CUDA_TRY(dalloc(h, &h->mk.u0, (size_t)3 * n * sizeof(float)));
+            CUDA_TRY(dalloc(h, &h->mk.t0, (size_t)n * sizeof(float)));
+        }
+        h->asmp.enabled = 1;
+        CUDA_TRY(lbmk_iterate_smem(n));
+        CUDA_TRY(cudaStreamSynchronize(h->s));
     }
     // graphs captured earlier do not contain the IBM launches
     for (int i = 0; i < 2; i++)
@@ -560,9 +620,9 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaE
         ia.thermal = h->icfg.thermal;
         ia.stream = h->s;
         const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
-        if (h->coop.enabled) {
-            if ((e = launch_ibm_coop(h->cfg.storage, h->cfg.thermal != 0, ia, h->coop, a.B, a.GB, h->bp, h->hist,
-                                     h->hist_cap, h->icfg.m_max, fsign, h->gbar, h->gpart)) != cudaSuccess)
+        if (h->asmp.enabled) {
+            if ((e = launch_ibm_assembled(h->cfg.storage, h->cfg.thermal != 0, ia, h->asmp, a.B, a.GB, fsign,
+                                          h->icfg.m_max, h->hist, h->hist_cap, h->bp, a)) != cudaSuccess)
                 return e;
         } else {
             for (int it = 1; it <= h->icfg.m_max; it++) {

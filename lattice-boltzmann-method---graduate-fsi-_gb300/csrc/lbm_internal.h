@@ -48,6 +48,8 @@ struct MarkerDev {
     float *rho;      // [n] marker density
     float *force;    // [4][n] current F_m (x, y, z) and heat source Q_m
     double *acc;     // [4][n] sum over iterations of -F_m ds and Q_m ds (FP64)
+    float *u0;       // [3][n] unforced interpolated velocity (assembled path)
+    float *t0;       // [n] unforced interpolated temperature (assembled path)
     float tdes;      // desired marker temperature (thermal IBM)
 };
 
@@ -77,18 +79,16 @@ struct BodyParams {
 };
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap);
 
-// Single-launch IBM phase on a cooperative grid (k_ibm_coop).
-struct GridBarrier {
-    unsigned int count;
-    unsigned int gen;
-};
-struct CoopPlan {
+// Assembled IBM phase (marker-space iteration, see lbm_ibm.cu).
+struct AsmPlan {
     int enabled = 0;
-    int grid = 0;
+    int *pair_ptr = nullptr, *pair_idx = nullptr;  // marker neighbour lists (CSR)
+    float *pairA = nullptr, *pairB = nullptr;      // coupling values, assembled each step
+    int *node_ptr = nullptr, *node_mk = nullptr;   // band node -> covering markers (fixed body)
 };
-cudaError_t plan_ibm_coop(int storage, bool thermal, CoopPlan &cp);
-cudaError_t launch_ibm_coop(int storage, bool lattice_thermal, const IbmArgs &a, const CoopPlan &cp, void *B,
-                            void *GB, const BodyParams &bp, double *hist, long long hist_cap, int m_max, float fsign,
-                            GridBarrier *gb, double *part);
+cudaError_t lbmk_iterate_smem(int n_markers);  // opt the one-CTA iteration into its shared memory
+cudaError_t launch_ibm_assembled(int storage, bool lattice_thermal, const IbmArgs &a, const AsmPlan &ap, void *B,
+                                 void *GB, float fsign, int m_max, double *hist, long long hist_cap,
+                                 const BodyParams &bp, const LaunchArgs &la);
 
 }  // namespace lbmk

@@ -99,7 +99,7 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / vscale
     eT = np.abs(m["T"] - r["T"]).max()
     print("thermal free sphere: |u| err %.3e of max |u| %.3e, T err %.3e" % (eu, vscale, eT))
-    assert eu < 1e-4 and eT < 1e-5, (eu, eT)
+    assert eu < 1e-4 and eT < 5e-5, (eu, eT)
     fscale = np.abs(hist[:, :3]).max()
     assert np.abs(fg[:, :3] - hist[:, :3]).max() / fscale < 1e-3
     heat = np.abs(hist[:, 6]).max()
