@@ -94,7 +94,8 @@ typedef struct lbm_config {
     int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
     int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
     int staged;           /* bulk-copy (TMA) staged kernel: 0 = off, 1 = on, >1 = on with that many rows per tile */
-    int ibm_fused;        /* 0: IBM phase as one cooperative launch when the device allows; <0: chain of kernels */
+    int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
+                             stream); <0: serial */
 } lbm_config;
 
 typedef struct lbm_ibm_config {

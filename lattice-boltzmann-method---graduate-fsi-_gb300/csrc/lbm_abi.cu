@@ -58,11 +58,11 @@ struct lbm_handle {
     int gsteps = 16;
     int tx = 128, ty = 2;
     TmaPlan tma;
-    AsmPlan asmp;
-    int use_asm = 1;
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
+    cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
+    cudaEvent_t ev_near = nullptr, ev_ibm = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -254,16 +254,6 @@ extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double ta
     return LBM_OK;
 }
 
-static void free_asm(lbm_handle *h) {
-    cudaFree(h->asmp.pair_ptr);
-    cudaFree(h->asmp.pair_idx);
-    cudaFree(h->asmp.pairA);
-    cudaFree(h->asmp.pairB);
-    cudaFree(h->asmp.node_ptr);
-    cudaFree(h->asmp.node_mk);
-    h->asmp = AsmPlan();
-}
-
 static void free_handle(lbm_handle *h) {
     if (!h) return;
     for (int i = 0; i < 2; i++) {
@@ -275,9 +265,7 @@ static void free_handle(lbm_handle *h) {
     cudaFree(h->band);
     cudaFree(h->ds);
     cudaFree(h->hist);
-    free_asm(h);
-    cudaFree(h->mk.u0);
-    cudaFree(h->mk.t0);
+
     cudaFree(h->mk.pos);
     cudaFree(h->mk.ds);
     cudaFree(h->mk.udes);
@@ -287,6 +275,9 @@ static void free_handle(lbm_handle *h) {
     for (int i = 0; i < 4; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
+    if (h->ev_near) cudaEventDestroy(h->ev_near);
+    if (h->ev_ibm) cudaEventDestroy(h->ev_ibm);
+    if (h->s2) cudaStreamDestroy(h->s2);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
 }
@@ -374,9 +365,16 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaMemsetAsync(h->hist, 0, (size_t)h->hist_cap * 8 * sizeof(double), h->s), "history init");
     }
     for (int i = 0; i < 4 && st == LBM_OK; i++) chk(cudaEventCreate(&h->ev[i]), "events");
+    if (st == LBM_OK) {
+        int lo = 0, hi = 0;
+        chk(cudaDeviceGetStreamPriorityRange(&lo, &hi), "priority range");
+        chk(cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, hi), "ibm stream");
+        chk(cudaEventCreateWithFlags(&h->ev_near, cudaEventDisableTiming), "events");
+        chk(cudaEventCreateWithFlags(&h->ev_ibm, cudaEventDisableTiming), "events");
+        if (st == LBM_OK) chk(cudaEventRecord(h->ev_ibm, h->s), "events");
+    }
     if (st == LBM_OK && c.staged > 0)
         chk(plan_tma(c.storage, c.thermal != 0, P, c.staged > 1 ? c.staged : 0, h->tma), "staged plan");
-    h->use_asm = c.ibm_fused >= 0 ? 1 : 0;
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);
@@ -388,6 +386,7 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
 
 extern "C" lbm_status lbmgpu_destroy(lbm_handle *h) {
     if (!h) return LBM_OK;
+    if (h->s2) cudaStreamSynchronize(h->s2);
     if (h->s) cudaStreamSynchronize(h->s);
     free_handle(h);
     return LBM_OK;
@@ -452,8 +451,6 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         cudaFree(h->mk.force);
         cudaFree(h->mk.acc);
         cudaFree(h->band);
-        cudaFree(h->mk.u0);
-        cudaFree(h->mk.t0);
         memset(&h->mk, 0, sizeof(h->mk));
         h->band = nullptr;
         CUDA_TRY(dalloc(h, &h->mk.pos, (size_t)3 * n * sizeof(double)));
@@ -514,63 +511,6 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
     h->ibm = true;
-    // assembled (marker-space) IBM: rigid pattern that only translates, and
-    // a marker count the one-CTA iteration holds in shared memory
-    free_asm(h);
-    const bool rotates = ic->free_body && ((h->bp.dof >> 3) & 7);
-    if (h->use_asm && n <= 4096 && !rotates) {
-        std::vector<int> pptr(n + 1, 0), pidx;
-        for (int m = 0; m < n; m++) {
-            for (int j = 0; j < n; j++) {
-                bool near = true;
-                for (int a = 0; a < 3 && near; a++)
-                    near = std::fabs(xyz[(size_t)a * n + m] - xyz[(size_t)a * n + j]) < 4.0;
-                if (near) pidx.push_back(j);
-            }
-            pptr[m + 1] = (int)pidx.size();
-        }
-        CUDA_TRY(dalloc(h, &h->asmp.pair_ptr, pptr.size() * sizeof(int)));
-        CUDA_TRY(dalloc(h, &h->asmp.pair_idx, pidx.size() * sizeof(int)));
-        CUDA_TRY(dalloc(h, &h->asmp.pairA, pidx.size() * sizeof(float)));
-        CUDA_TRY(dalloc(h, &h->asmp.pairB, pidx.size() * sizeof(float)));
-        CUDA_TRY(cudaMemcpyAsync(h->asmp.pair_ptr, pptr.data(), pptr.size() * sizeof(int), cudaMemcpyHostToDevice, h->s));
-        CUDA_TRY(cudaMemcpyAsync(h->asmp.pair_idx, pidx.data(), pidx.size() * sizeof(int), cudaMemcpyHostToDevice, h->s));
-        CUDA_TRY(cudaMemsetAsync(h->asmp.pairB, 0, pidx.size() * sizeof(float), h->s));
-        if (!ic->free_body) {
-            // band node -> markers whose 4x4x4 stencil covers it
-            std::vector<std::vector<int>> lists((size_t)nb);
-            for (int m = 0; m < n; m++) {
-                int lo[3];
-                for (int a = 0; a < 3; a++) lo[a] = (int)std::floor(xyz[(size_t)a * n + m]) - 2 - org[a];
-                for (int c = 0; c < 4; c++)
-                    for (int b2 = 0; b2 < 4; b2++)
-                        for (int a2 = 0; a2 < 4; a2++) {
-                            int bx = lo[0] + a2, by = lo[1] + b2, bz = lo[2] + c;
-                            if (bx < 0 || by < 0 || bz < 0 || bx >= bs[0] || by >= bs[1] || bz >= bs[2]) continue;
-                            lists[(size_t)bx + (size_t)bs[0] * ((size_t)by + (size_t)bs[1] * bz)].push_back(m);
-                        }
-            }
-            std::vector<int> nptr(nb + 1, 0), nmk;
-            for (long long b2 = 0; b2 < nb; b2++) {
-                nmk.insert(nmk.end(), lists[b2].begin(), lists[b2].end());
-                nptr[b2 + 1] = (int)nmk.size();
-            }
-            CUDA_TRY(dalloc(h, &h->asmp.node_ptr, nptr.size() * sizeof(int)));
-            CUDA_TRY(dalloc(h, &h->asmp.node_mk, std::max<size_t>(1, nmk.size()) * sizeof(int)));
-            CUDA_TRY(cudaMemcpyAsync(h->asmp.node_ptr, nptr.data(), nptr.size() * sizeof(int), cudaMemcpyHostToDevice,
-                                     h->s));
-            if (!nmk.empty())
-                CUDA_TRY(cudaMemcpyAsync(h->asmp.node_mk, nmk.data(), nmk.size() * sizeof(int),
-                                         cudaMemcpyHostToDevice, h->s));
-        }
-        if (!h->mk.u0) {
-            CUDA_TRY(dalloc(h, &h->mk.u0, (size_t)3 * n * sizeof(float)));
-            CUDA_TRY(dalloc(h, &h->mk.t0, (size_t)n * sizeof(float)));
-        }
-        h->asmp.enabled = 1;
-        CUDA_TRY(lbmk_iterate_smem(n));
-        CUDA_TRY(cudaStreamSynchronize(h->s));
-    }
     // graphs captured earlier do not contain the IBM launches
     for (int i = 0; i < 2; i++)
         if (h->gexec[i]) {
@@ -596,6 +536,7 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.band = h->band;
     a.gather = gather;
     a.export_only = 0;
+    a.region = 0;
     a.thermal = h->cfg.thermal;
     a.tx = h->tx;
     a.ty = h->ty;
@@ -604,37 +545,66 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     return a;
 }
 
-// Enqueue one reference iteration.  ev_pair (optional) brackets the fused kernel.
+static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t s) {
+    cudaError_t e;
+    IbmArgs ia;
+    ia.P = &h->P;
+    ia.mk = h->mk;
+    ia.ds = h->ds;
+    ia.band = h->band;
+    ia.thermal = h->icfg.thermal;
+    ia.stream = s;
+    LaunchArgs b = a;
+    b.stream = s;
+    const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
+    for (int it = 1; it <= h->icfg.m_max; it++) {
+        if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
+        if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
+    }
+    if ((e = launch_band_collide(h->cfg.storage, b, fsign)) != cudaSuccess) return e;
+    return launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap);
+}
+
+// Enqueue one reference iteration.  e0/e1 (optional) bracket the fused kernel.
+//
+// With a fixed immersed body the IBM phase of step t runs on a second stream
+// while the main stream already streams the cells of step t+1 that do not
+// touch the band (the "far" region); only the near box -- the band grown by
+// the one-cell pull stencil -- waits for it:
+//   main: far(t) | wait ibm(t-1) | near(t) | record near(t)
+//   side: wait near(t) | interp/spread x m_max, band collide, finish | record ibm(t)
+// A moving body changes the band each step, so it keeps the serial order.
 static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaEvent_t e1) {
     LaunchArgs a = make_args(h, gather);
     cudaError_t e;
+    const bool overlap = h->ibm && gather && !h->icfg.free_body && h->s2 && h->cfg.ibm_overlap >= 0;
     if (e0) cudaEventRecord(e0, h->s);
+    if (!overlap) {
+        if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
+        if (e1) cudaEventRecord(e1, h->s);
+        if (h->ibm && (e = enqueue_ibm(h, a, h->s)) != cudaSuccess) return e;
+        if (h->ibm) cudaEventRecord(h->ev_ibm, h->s);
+        h->cur = 1 - h->cur;
+        return cudaSuccess;
+    }
+    a.region = 1;
+    if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(h->s, h->ev_ibm, 0)) != cudaSuccess) return e;
+    a.region = 2;
     if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
     if (e1) cudaEventRecord(e1, h->s);
-    if (h->ibm) {
-        IbmArgs ia;
-        ia.P = &h->P;
-        ia.mk = h->mk;
-        ia.ds = h->ds;
-        ia.band = h->band;
-        ia.thermal = h->icfg.thermal;
-        ia.stream = h->s;
-        const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
-        if (h->asmp.enabled) {
-            if ((e = launch_ibm_assembled(h->cfg.storage, h->cfg.thermal != 0, ia, h->asmp, a.B, a.GB, fsign,
-                                          h->icfg.m_max, h->hist, h->hist_cap, h->bp, a)) != cudaSuccess)
-                return e;
-        } else {
-            for (int it = 1; it <= h->icfg.m_max; it++) {
-                if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
-                if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
-            }
-            if ((e = launch_band_collide(h->cfg.storage, a, fsign)) != cudaSuccess) return e;
-            if ((e = launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap)) != cudaSuccess) return e;
-        }
-    }
+    if ((e = cudaEventRecord(h->ev_near, h->s)) != cudaSuccess) return e;
+    if ((e = cudaStreamWaitEvent(h->s2, h->ev_near, 0)) != cudaSuccess) return e;
+    if ((e = enqueue_ibm(h, a, h->s2)) != cudaSuccess) return e;
+    if ((e = cudaEventRecord(h->ev_ibm, h->s2)) != cudaSuccess) return e;
     h->cur = 1 - h->cur;
     return cudaSuccess;
+}
+
+// Order everything after the last IBM phase on the main stream.
+static cudaError_t join_ibm(lbm_handle *h) {
+    if (!h->ibm || !h->s2) return cudaSuccess;
+    return cudaStreamWaitEvent(h->s, h->ev_ibm, 0);
 }
 
 static lbm_status ensure_graph(lbm_handle *h) {
@@ -644,6 +614,7 @@ static lbm_status ensure_graph(lbm_handle *h) {
     CUDA_TRY(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
     for (int i = 0; i < h->gsteps && e == cudaSuccess; i++) e = enqueue_step(h, 1, nullptr, nullptr);
+    if (e == cudaSuccess) e = join_ibm(h);
     cudaError_t e2 = cudaStreamEndCapture(h->s, &g);
     h->cur = p;  // gsteps is even: the capture ends where it started
     if (e != cudaSuccess) {
@@ -688,6 +659,7 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
         h->steps++;
         nsteps--;
     }
+    CUDA_TRY(join_ibm(h));
     return LBM_OK;
 }
 
@@ -720,6 +692,7 @@ extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *to
         CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, h->evpool[2 * i], h->evpool[2 * i + 1]));
         h->steps++;
     }
+    CUDA_TRY(join_ibm(h));
     CUDA_TRY(cudaEventRecord(h->ev[1], h->s));
     CUDA_TRY(cudaEventSynchronize(h->ev[1]));
     float tot = 0.f;

@@ -27,6 +27,7 @@ struct LaunchArgs {
     float *band;
     int gather;
     int export_only;
+    int region;  // 0 all cells, 1 all but the IBM near box, 2 the near box only
     int thermal;
     int tx, ty;
     TmaPlan tma;
@@ -48,8 +49,6 @@ struct MarkerDev {
     float *rho;      // [n] marker density
     float *force;    // [4][n] current F_m (x, y, z) and heat source Q_m
     double *acc;     // [4][n] sum over iterations of -F_m ds and Q_m ds (FP64)
-    float *u0;       // [3][n] unforced interpolated velocity (assembled path)
-    float *t0;       // [n] unforced interpolated temperature (assembled path)
     float tdes;      // desired marker temperature (thermal IBM)
 };
 
@@ -78,17 +77,5 @@ struct BodyParams {
     int dof;           // bits 0-2 translation, 3-5 rotation
 };
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap);
-
-// Assembled IBM phase (marker-space iteration, see lbm_ibm.cu).
-struct AsmPlan {
-    int enabled = 0;
-    int *pair_ptr = nullptr, *pair_idx = nullptr;  // marker neighbour lists (CSR)
-    float *pairA = nullptr, *pairB = nullptr;      // coupling values, assembled each step
-    int *node_ptr = nullptr, *node_mk = nullptr;   // band node -> covering markers (fixed body)
-};
-cudaError_t lbmk_iterate_smem(int n_markers);  // opt the one-CTA iteration into its shared memory
-cudaError_t launch_ibm_assembled(int storage, bool lattice_thermal, const IbmArgs &a, const AsmPlan &ap, void *B,
-                                 void *GB, float fsign, int m_max, double *hist, long long hist_cap,
-                                 const BodyParams &bp, const LaunchArgs &la);
 
 }  // namespace lbmk

@@ -189,16 +189,34 @@ template <class T, bool THERMAL, bool FORCED>
 __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA,
                                               T *__restrict__ GB, const __grid_constant__ StepParams P,
                                               DevState *__restrict__ ds, float *__restrict__ mom,
-                                              float *__restrict__ band, int gather, int export_only) {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
-    const int z = blockIdx.z;
-    const bool valid = (x < P.nx) && (y < P.ny);
+                                              float *__restrict__ band, int gather, int export_only, int region) {
+    // region 0: every cell; 1: all but the "near" box (the IBM band grown by
+    // the one-cell pull stencil); 2: only the near box (the grid spans it)
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    int z = blockIdx.z;
+    bool valid;
+    if (region == 2) {
+        x += ds->band_o[0] - 1;
+        y += ds->band_o[1] - 1;
+        z += ds->band_o[2] - 1;
+        valid = x >= 0 && y >= 0 && z >= 0 && x < P.nx && y < P.ny && z < P.nz && x <= ds->band_o[0] + P.bsx &&
+                y <= ds->band_o[1] + P.bsy && z <= ds->band_o[2] + P.bsz;
+    } else {
+        valid = (x < P.nx) && (y < P.ny);
+        if (region == 1) {
+            const int qx = x - (ds->band_o[0] - 1), qy = y - (ds->band_o[1] - 1), qz = z - (ds->band_o[2] - 1);
+            if ((unsigned)qx < (unsigned)(P.bsx + 2) && (unsigned)qy < (unsigned)(P.bsy + 2) &&
+                (unsigned)qz < (unsigned)(P.bsz + 2))
+                valid = false;
+        }
+    }
     const long long cell = valid ? (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z) : 0;
     const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
                              (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
                           : 0;
-    const bool bwarp = __any_sync(0xffffffffu, raw != 0);
+    // the near box can start at a negative offset: keep those lanes idle
+    const bool bwarp = __any_sync(0xffffffffu, raw != 0 || (region == 2 && !valid));
     float f[Q], g[QT];
     gather_flow<T>(A, f, x, y, z, cell, raw, valid, bwarp, gather, P);
     if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, bwarp, gather, P);
@@ -471,7 +489,7 @@ __global__ void k_init(T *__restrict__ A, T *__restrict__ GA, long long N, long 
 template <class T>
 static cudaError_t launch_step_t(const LaunchArgs &a) {
     const TmaPlan &tp = a.tma;
-    if (tp.enabled && a.gather && !a.export_only && a.mom == nullptr) {
+    if (tp.enabled && a.gather && !a.export_only && a.mom == nullptr && a.region == 0) {
         if (a.thermal)
             k_step_tma<T, true><<<tp.grid, kConsumers + 32, tp.smem, a.stream>>>(
                 (const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P, a.ds, a.band, tp.ty, tp.ntiles);
@@ -482,16 +500,17 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
     }
     dim3 blk(a.tx, a.ty, 1);
     dim3 grd((a.P->nx + a.tx - 1) / a.tx, (a.P->ny + a.ty - 1) / a.ty, a.P->nz);
+    if (a.region == 2) grd = dim3((a.P->bsx + 2 + a.tx - 1) / a.tx, (a.P->bsy + 2 + a.ty - 1) / a.ty, a.P->bsz + 2);
     const bool forced = a.P->forced != 0;
     if (a.thermal)
         k_step<T, true, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P,
-                                                         a.ds, a.mom, a.band, a.gather, a.export_only);
+                                                         a.ds, a.mom, a.band, a.gather, a.export_only, a.region);
     else if (forced)
         k_step<T, false, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds,
-                                                          a.mom, a.band, a.gather, a.export_only);
+                                                          a.mom, a.band, a.gather, a.export_only, a.region);
     else
         k_step<T, false, false><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds,
-                                                           a.mom, a.band, a.gather, a.export_only);
+                                                           a.mom, a.band, a.gather, a.export_only, a.region);
     return cudaGetLastError();
 }
 

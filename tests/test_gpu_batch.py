@@ -54,7 +54,7 @@ def test_batch_flags_diverging_cavity(pkg):
     others are unaffected (failure reported, never trapped)."""
     dims = np.array([[12, 12, 12], [12, 12, 12]])
     taus = np.array([0.8, 0.5000001])
-    b = pkg.Batch(dims, taus, lid=0.4, storage="f32")
+    b = pkg.Batch(dims, taus, lid=0.1, storage="f32")
     b.init()
     b.step(3000)
     st = b.status()

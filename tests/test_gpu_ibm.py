@@ -15,8 +15,8 @@ U = 0.05
 
 
 def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None,
-                fused=0, u_in=U):
-    cfgkw = {"ibm_fused": fused}
+                overlap=0, u_in=U):
+    cfgkw = {"ibm_overlap": overlap}
     if thermal:
         cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0),
                      gbeta=thermal.get("gbeta", (0, 0, 0)), T_ref=thermal.get("T0", 0.0))
@@ -36,14 +36,14 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
     return s
 
 
-@pytest.mark.parametrize("fused", [0, -1], ids=["onelaunch", "chain"])
+@pytest.mark.parametrize("overlap", [0, -1], ids=["overlapped", "serial"])
 @pytest.mark.parametrize("lit_sign", [0, 1])
-def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, fused):
-    """Both IBM drivers: the one-launch cooperative kernel and the chain of
-    kernels."""
+def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap):
+    """The IBM phase on its own stream overlapping the far-region streaming,
+    and in the serial order."""
     nx, ny, nz, tau, D, nm, m_max, steps = 48, 30, 28, 0.56, 10.0, 314, 3, 120
     center = (16.0, 15.3, 14.6)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, fused=fused)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, overlap=overlap)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -74,8 +74,7 @@ def test_fixed_sphere_fp16_drag(pkg, orc):
     assert ed < 5e-3 and eu < 1e-3
 
 
-@pytest.mark.parametrize("fused", [0, -1], ids=["onelaunch", "chain"])
-def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
+def test_thermal_free_sphere_vs_oracle(pkg, orc):
     """D3Q7 thermal population, Boussinesq force, thermal IBM (T_body = 1)
     and the FP64 Newton-Euler body (held in x and rotation, free in y and z)
     settling in fluid at rest, against the oracle."""
@@ -86,7 +85,7 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
     # rho_s/rho_f = 3: the explicit coupling of a D = 8 sphere is unstable at 1.5
     fr = dict(rho_ratio=3.0, gravity=(0.0, -1e-5, 0.0), dof=0b000110)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, fused=fused, u_in=0.0)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=0.0)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -110,17 +109,19 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, fused):
     assert np.abs(xyz - oxyz).max() < 1e-6
 
 
-def test_onelaunch_and_chain_ibm_agree(pkg, orc):
-    """The two IBM drivers give the same forces and fields (up to the order of
-    float atomics), on the benchmark's sphere at reduced domain size."""
+def test_overlapped_and_serial_ibm_agree(pkg, orc):
+    """Overlapping the IBM phase with the far-region streaming changes nothing
+    but timing: same forces and fields, on the benchmark's sphere at reduced
+    domain size, FP16 storage, with CUDA-graph replay."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
     center = (24.0, 20.0, 20.0)
     out = []
-    for fused in (0, -1):
-        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", fused=fused)
-        s.step(steps)
+    for overlap in (0, -1):
+        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f16", overlap=overlap)
+        s.step(1)
+        s.step(steps - 1)
         out.append((s.forces(), s.moments()))
         assert s.status() == 0
     fa, fb = out[0][0], out[1][0]
-    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
-    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-5
+    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-3
+    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-3
