@@ -96,6 +96,7 @@ typedef struct lbm_config {
     int staged;           /* bulk-copy (TMA) staged kernel: 0 = off, 1 = on, >1 = on with that many rows per tile */
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
                              stream); <0: serial */
+    int vector;           /* 0: 8-byte group loads when the row length allows; <0: scalar loads */
 } lbm_config;
 
 typedef struct lbm_ibm_config {

@@ -57,6 +57,7 @@ struct lbm_handle {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;
     int tx = 128, ty = 2;
+    int vec = 0;  // 8-byte group kernel eligible
     TmaPlan tma;
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -326,6 +327,10 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
                    : 0;
     build_classes(c, P);
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
+    {
+        const int V = c.storage == LBM_STORE_F32 ? 2 : 4;
+        h->vec = (c.vector >= 0 && !c.thermal && !(P.periodic & 1) && c.nx % V == 0 && c.nx >= 2 * V) ? 1 : 0;
+    }
     if (c.graph_steps > 0) h->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) h->gsteps = 0;
     choose_block(h);
@@ -537,6 +542,7 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.gather = gather;
     a.export_only = 0;
     a.region = 0;
+    a.vec = h->vec;
     a.thermal = h->cfg.thermal;
     a.tx = h->tx;
     a.ty = h->ty;
@@ -565,7 +571,9 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
     return launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap);
 }
 
-// Enqueue one reference iteration.  e0/e1 (optional) bracket the fused kernel.
+// Enqueue one reference iteration.  ev (optional, 4 events) bracket the fused
+// collide-stream launches: ev[0..1] the whole grid or its far region, ev[2..3]
+// the near box (recorded as an empty interval when there is none).
 //
 // With a fixed immersed body the IBM phase of step t runs on a second stream
 // while the main stream already streams the cells of step t+1 that do not
@@ -574,14 +582,18 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
 //   main: far(t) | wait ibm(t-1) | near(t) | record near(t)
 //   side: wait near(t) | interp/spread x m_max, band collide, finish | record ibm(t)
 // A moving body changes the band each step, so it keeps the serial order.
-static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaEvent_t e1) {
+static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev) {
     LaunchArgs a = make_args(h, gather);
     cudaError_t e;
     const bool overlap = h->ibm && gather && !h->icfg.free_body && h->s2 && h->cfg.ibm_overlap >= 0;
-    if (e0) cudaEventRecord(e0, h->s);
+    if (ev) cudaEventRecord(ev[0], h->s);
     if (!overlap) {
         if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
-        if (e1) cudaEventRecord(e1, h->s);
+        if (ev) {
+            cudaEventRecord(ev[1], h->s);
+            cudaEventRecord(ev[2], h->s);
+            cudaEventRecord(ev[3], h->s);
+        }
         if (h->ibm && (e = enqueue_ibm(h, a, h->s)) != cudaSuccess) return e;
         if (h->ibm) cudaEventRecord(h->ev_ibm, h->s);
         h->cur = 1 - h->cur;
@@ -589,10 +601,12 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, cudaEvent_t e0, cudaE
     }
     a.region = 1;
     if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[1], h->s);
     if ((e = cudaStreamWaitEvent(h->s, h->ev_ibm, 0)) != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[2], h->s);
     a.region = 2;
     if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
-    if (e1) cudaEventRecord(e1, h->s);
+    if (ev) cudaEventRecord(ev[3], h->s);
     if ((e = cudaEventRecord(h->ev_near, h->s)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(h->s2, h->ev_near, 0)) != cudaSuccess) return e;
     if ((e = enqueue_ibm(h, a, h->s2)) != cudaSuccess) return e;
@@ -613,7 +627,7 @@ static lbm_status ensure_graph(lbm_handle *h) {
     cudaGraph_t g = nullptr;
     CUDA_TRY(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
     cudaError_t e = cudaSuccess;
-    for (int i = 0; i < h->gsteps && e == cudaSuccess; i++) e = enqueue_step(h, 1, nullptr, nullptr);
+    for (int i = 0; i < h->gsteps && e == cudaSuccess; i++) e = enqueue_step(h, 1, nullptr);
     if (e == cudaSuccess) e = join_ibm(h);
     cudaError_t e2 = cudaStreamEndCapture(h->s, &g);
     h->cur = p;  // gsteps is even: the capture ends where it started
@@ -637,7 +651,7 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
     if (nsteps < 0) return fail(LBM_ERR_INVALID, "step: negative step count");
     while (nsteps > 0) {
         if (h->steps == 0) {
-            CUDA_TRY(enqueue_step(h, 0, nullptr, nullptr));
+            CUDA_TRY(enqueue_step(h, 0, nullptr));
             h->steps++;
             nsteps--;
             continue;
@@ -655,7 +669,7 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
             nsteps -= h->gsteps;
             continue;
         }
-        CUDA_TRY(enqueue_step(h, 1, nullptr, nullptr));
+        CUDA_TRY(enqueue_step(h, 1, nullptr));
         h->steps++;
         nsteps--;
     }
@@ -682,14 +696,14 @@ extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *to
     if (nsteps < 0) return fail(LBM_ERR_INVALID, "step_profiled: negative step count");
     // one event pair per fused launch, all read after the last step so the
     // host never stalls the stream between steps
-    while ((int)h->evpool.size() < 2 * nsteps) {
+    while ((int)h->evpool.size() < 4 * nsteps) {
         cudaEvent_t e;
         CUDA_TRY(cudaEventCreate(&e));
         h->evpool.push_back(e);
     }
     CUDA_TRY(cudaEventRecord(h->ev[0], h->s));
     for (int i = 0; i < nsteps; i++) {
-        CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, h->evpool[2 * i], h->evpool[2 * i + 1]));
+        CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, &h->evpool[4 * i]));
         h->steps++;
     }
     CUDA_TRY(join_ibm(h));
@@ -699,9 +713,10 @@ extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *to
     CUDA_TRY(cudaEventElapsedTime(&tot, h->ev[0], h->ev[1]));
     double fused = 0.0;
     for (int i = 0; i < nsteps; i++) {
-        float ms = 0.f;
-        CUDA_TRY(cudaEventElapsedTime(&ms, h->evpool[2 * i], h->evpool[2 * i + 1]));
-        fused += ms;
+        float ms = 0.f, ms2 = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&ms, h->evpool[4 * i], h->evpool[4 * i + 1]));
+        CUDA_TRY(cudaEventElapsedTime(&ms2, h->evpool[4 * i + 2], h->evpool[4 * i + 3]));
+        fused += ms + ms2;
     }
     if (total_ms) *total_ms = tot;
     if (fused_ms) *fused_ms = fused;

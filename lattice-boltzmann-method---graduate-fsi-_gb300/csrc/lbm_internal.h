@@ -28,6 +28,7 @@ struct LaunchArgs {
     int gather;
     int export_only;
     int region;  // 0 all cells, 1 all but the IBM near box, 2 the near box only
+    int vec;     // vector (8-byte group) kernel eligible
     int thermal;
     int tx, ty;
     TmaPlan tma;

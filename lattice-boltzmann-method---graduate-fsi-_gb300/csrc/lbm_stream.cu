@@ -224,6 +224,124 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
 }
 
 // ---------------------------------------------------------------------------
+// Vector variant: each thread owns V = 8 / sizeof(T) consecutive cells of a
+// row (4 for 16-bit storage, 2 for FP32) and pulls every population of the
+// group with one aligned 8-byte load of the source row.  For links with
+// c_x = +1 (-1) the group needs one more element on its left (right): it
+// comes from the neighbouring lane's load through a warp shuffle, or for the
+// first (last) lane of the warp from one extra scalar load.  So a thread
+// keeps 19 x 8 bytes in flight.  Groups touching a domain face take the
+// boundary-class path cell by cell.  Rows must be a multiple of V cells and
+// x must not be periodic.
+// ---------------------------------------------------------------------------
+template <class T>
+struct Vec8;
+template <>
+struct Vec8<float> {
+    typedef float2 type;
+    static constexpr int V = 2;
+    static __device__ __forceinline__ type ld(const float *p) { return __ldg(reinterpret_cast<const float2 *>(p)); }
+    static __device__ __forceinline__ float el(const type &v, int k) { return k == 0 ? v.x : v.y; }
+    static __device__ __forceinline__ unsigned first_bits(const type &v) { return __float_as_uint(v.x); }
+    static __device__ __forceinline__ unsigned last_bits(const type &v) { return __float_as_uint(v.y); }
+    static __device__ __forceinline__ float from_bits(unsigned b) { return __uint_as_float(b); }
+};
+template <class H>
+struct Vec8Half {
+    typedef uint2 type;
+    static constexpr int V = 4;
+    static __device__ __forceinline__ type ld(const H *p) { return __ldg(reinterpret_cast<const uint2 *>(p)); }
+    static __device__ __forceinline__ float cvt(unsigned short b) {
+        H h;
+        memcpy(&h, &b, 2);
+        return St<H>::lds(&h);
+    }
+    static __device__ __forceinline__ float el(const type &v, int k) {
+        const unsigned w = k < 2 ? v.x : v.y;
+        return cvt((unsigned short)((k & 1) ? (w >> 16) : (w & 0xffffu)));
+    }
+    static __device__ __forceinline__ unsigned first_bits(const type &v) { return v.x & 0xffffu; }
+    static __device__ __forceinline__ unsigned last_bits(const type &v) { return v.y >> 16; }
+    static __device__ __forceinline__ float from_bits(unsigned b) { return cvt((unsigned short)b); }
+};
+template <>
+struct Vec8<__half> : Vec8Half<__half> {};
+template <>
+struct Vec8<__nv_bfloat16> : Vec8Half<__nv_bfloat16> {};
+
+template <class T, bool FORCED>
+__global__ void __launch_bounds__(256) k_step_vec(const T *__restrict__ A, T *__restrict__ B,
+                                                  const __grid_constant__ StepParams P, DevState *__restrict__ ds,
+                                                  float *__restrict__ band, int region) {
+    typedef Vec8<T> VT;
+    constexpr int V = VT::V;
+    const int lane = threadIdx.x & 31;
+    const int x0 = V * (blockIdx.x * blockDim.x + threadIdx.x);
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    const int z = blockIdx.z;
+    const bool gvalid = x0 < P.nx && y < P.ny;
+    const bool interior = gvalid && x0 >= 1 && x0 + V - 1 <= P.nx - 2 && y >= 1 && y <= P.ny - 2 && z >= 1 &&
+                          z <= P.nz - 2;
+    typename VT::type v[Q];
+    float prev[Q], next[Q];
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        int sy = y - cy(l), sz = z - cz(l);
+        if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+        if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+        const bool row_ok = gvalid && sy >= 0 && sy < P.ny && sz >= 0 && sz < P.nz;
+        const T *rowp = A + l * P.S + (long long)P.nx * ((long long)sy + (long long)P.ny * sz);
+        if (row_ok) {
+            v[l] = VT::ld(rowp + x0);
+        } else {
+            memset(&v[l], 0, sizeof(v[l]));
+        }
+        if (cx(l) > 0) {
+            const unsigned up = __shfl_up_sync(0xffffffffu, VT::last_bits(v[l]), 1);
+            float pv = VT::from_bits(up);
+            if (lane == 0) pv = (row_ok && x0 >= 1) ? St<T>::ld(rowp + x0 - 1) : 0.0f;
+            prev[l] = pv;
+        } else if (cx(l) < 0) {
+            const unsigned dn = __shfl_down_sync(0xffffffffu, VT::first_bits(v[l]), 1);
+            float nv = VT::from_bits(dn);
+            if (lane == 31) nv = (row_ok && x0 + V < P.nx) ? St<T>::ld(rowp + x0 + V) : 0.0f;
+            next[l] = nv;
+        }
+    }
+    if (!gvalid) return;
+#pragma unroll
+    for (int k = 0; k < V; k++) {
+        const int x = x0 + k;
+        bool valid = true;
+        if (region == 1) {
+            const int qx = x - (ds->band_o[0] - 1), qy = y - (ds->band_o[1] - 1), qz = z - (ds->band_o[2] - 1);
+            if ((unsigned)qx < (unsigned)(P.bsx + 2) && (unsigned)qy < (unsigned)(P.bsy + 2) &&
+                (unsigned)qz < (unsigned)(P.bsz + 2))
+                valid = false;
+        }
+        if (!valid) continue;
+        const long long cell = (long long)x + (long long)P.nx * ((long long)y + (long long)P.ny * z);
+        float f[Q], g[QT];
+        if (interior) {
+#pragma unroll
+            for (int l = 0; l < Q; l++) {
+                if (cx(l) == 0)
+                    f[l] = VT::el(v[l], k);
+                else if (cx(l) > 0)
+                    f[l] = k == 0 ? prev[l] : VT::el(v[l], k - 1);
+                else
+                    f[l] = k == V - 1 ? next[l] : VT::el(v[l], k + 1);
+            }
+        } else {
+            const int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
+                            (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0);
+            gather_flow<T>(A, f, x, y, z, cell, raw, true, true, 1, P);
+        }
+        finish_cell<T, false, FORCED>(f, g, x, y, z, cell, true, 1, 0, B, nullptr, P, ds, nullptr, band);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Staged variant (warp-specialised, persistent).  A tile is TY whole rows
 // (TY * nx cells) of one z plane.  Warp 0 is the producer: for every tile it
 // arms the stage's "full" mbarrier with the byte count and issues, lane per
@@ -496,6 +614,18 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
         else
             k_step_tma<T, false><<<tp.grid, kConsumers + 32, tp.smem, a.stream>>>(
                 (const T *)a.A, (T *)a.B, nullptr, nullptr, *a.P, a.ds, a.band, tp.ty, tp.ntiles);
+        return cudaGetLastError();
+    }
+    if (a.vec && a.gather && !a.export_only && a.mom == nullptr && !a.thermal && a.region != 2) {
+        constexpr int V = Vec8<T>::V;
+        const int groups = a.P->nx / V;
+        const int tx = groups >= 128 ? 128 : (groups >= 64 ? 64 : 32);
+        dim3 blk(tx, 256 / tx, 1);
+        dim3 grd((groups + tx - 1) / tx, (a.P->ny + blk.y - 1) / blk.y, a.P->nz);
+        if (a.P->forced)
+            k_step_vec<T, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, *a.P, a.ds, a.band, a.region);
+        else
+            k_step_vec<T, false><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, *a.P, a.ds, a.band, a.region);
         return cudaGetLastError();
     }
     dim3 blk(a.tx, a.ty, 1);

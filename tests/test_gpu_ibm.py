@@ -111,17 +111,18 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc):
 
 def test_overlapped_and_serial_ibm_agree(pkg, orc):
     """Overlapping the IBM phase with the far-region streaming changes nothing
-    but timing: same forces and fields, on the benchmark's sphere at reduced
-    domain size, FP16 storage, with CUDA-graph replay."""
+    but timing: same forces and fields up to the order of the float atomics of
+    the spreading, on the benchmark's sphere at reduced domain size, with
+    CUDA-graph replay."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
     center = (24.0, 20.0, 20.0)
     out = []
     for overlap in (0, -1):
-        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f16", overlap=overlap)
+        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", overlap=overlap)
         s.step(1)
         s.step(steps - 1)
         out.append((s.forces(), s.moments()))
         assert s.status() == 0
     fa, fb = out[0][0], out[1][0]
-    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-3
-    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-3
+    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
+    assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-5
