@@ -262,6 +262,51 @@ def run_batched(pkg, steps: int, seq_steps: int):
             "diverged_cavities": int((st != 0).sum())}
 
 
+def run_serving(pkg, orc, seconds: float, step_scale: float, rate: float = 200.0):
+    """Poisson arrivals at `rate` requests/s for `seconds` (seed 5); each a
+    lid-driven cavity or a channel with a fixed sphere (50/50), grid from
+    {64^3, 96^3, 128^3, 192x96x96}, Re from U[100, 1000], steps log-uniform in
+    [1000, 20000] times step_scale, FP32 or FP16 storage (50/50).  Admission
+    by an HBM budget, state device-resident, continuous batching."""
+    rng = np.random.default_rng(5)
+    t, reqs = 0.0, []
+    grids = [(64, 64, 64), (96, 96, 96), (128, 128, 128), (192, 96, 96)]
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t > seconds:
+            break
+        g = grids[rng.integers(0, 4)]
+        steps = int(round(np.exp(rng.uniform(np.log(1000), np.log(20000))) * step_scale))
+        reqs.append(dict(arrival_s=t, kind=int(rng.integers(0, 2)), nx=g[0], ny=g[1], nz=g[2],
+                         reynolds=float(rng.uniform(100, 1000)), steps=max(1, steps),
+                         storage="f32" if rng.random() < 0.5 else "f16"))
+    # keep the fields of two small cavities for the error check
+    cav = sorted([i for i, r in enumerate(reqs) if r["kind"] == 0 and r["nx"] == 64], key=lambda i: reqs[i]["steps"])
+    for i in cav[:2]:
+        reqs[i]["keep"] = True
+    t0 = time.perf_counter()
+    res, upd = pkg.serve_run(reqs, max_active=64, chunk_steps=100, hbm_budget_bytes=200e9)
+    wall = time.perf_counter() - t0
+    lat = np.array([r["latency_s"] for r in res if r["status"] == 0])
+    errs = []
+    for i in cav[:2]:
+        r = reqs[i]
+        tau = 0.5 + 3 * 0.05 * r["nx"] / r["reynolds"]
+        lattice = orc.cavity(r["nx"], tau, 0.05)
+        lattice.step_plain(r["steps"])
+        ref = orc.moments(lattice)
+        f = res[i]["fields"]
+        errs.append({"request": i, "storage": r["storage"], "steps": r["steps"],
+                     "max_u_err_over_U": float(max(np.abs(f[1 + k] - ref[c]).max()
+                                                   for k, c in enumerate(("ux", "uy", "uz"))) / 0.05)})
+    return {"workload": "Poisson %.0f req/s for %.1f s, steps x %.2f of log-U[1000, 20000]" % (rate, seconds,
+                                                                                               step_scale),
+            "requests": len(reqs), "completed": int(len(lat)), "wall_s": wall,
+            "aggregate_mlups": upd / wall / 1e6, "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
+            "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
+            "oracle_sample": errs}
+
+
 def cpu_baseline_sample(threads: int | None = None):
     """FP64 restatement (oracle) on the same workload, a bounded sample of
     lattice steps, all host threads."""
@@ -299,6 +344,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=2.0)
+    ap.add_argument("--serve-step-scale", type=float, default=0.05)
     args = ap.parse_args()
     rank, world, local = dist_env()
     if args.warmup < 3:
@@ -363,6 +411,11 @@ def main():
         import __graft_entry__ as ge
 
         line["batched"] = run_batched(ge.load_package(), steps=200, seq_steps=100)
+    if not args.no_serve:
+        import __graft_entry__ as ge
+        import oracle as orc
+
+        line["serving"] = run_serving(ge.load_package(), orc, args.serve_seconds, args.serve_step_scale)
     if not args.no_cpu_baseline:
         cb = cpu_baseline_sample()
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -96,7 +96,7 @@ typedef struct lbm_config {
     int staged;           /* bulk-copy (TMA) staged kernel: 0 = off, 1 = on, >1 = on with that many rows per tile */
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
                              stream); <0: serial */
-    int vector;           /* 0: 8-byte group loads when the row length allows; <0: scalar loads */
+    int vector;           /* >0: 8-byte group loads with warp shuffles when the row length allows; 0: scalar */
 } lbm_config;
 
 typedef struct lbm_ibm_config {
@@ -205,6 +205,45 @@ lbm_status lbmgpu_batch_download(lbm_batch *b, int problem, float *host);
 /* Per-cavity status words (LBM_STATUS_*). */
 lbm_status lbmgpu_batch_status(lbm_batch *b, uint32_t *flags);
 lbm_status lbmgpu_batch_info(lbm_batch *b, long long *total_cells, long long *steps);
+
+/* ------------------------------------------------------------------------
+ * Serving loop: requests (lid-driven cavities or channels with a fixed
+ * sphere) arrive on a wall-clock schedule; each is admitted as soon as it has
+ * arrived, a slot is free and its device memory fits the budget, keeps its
+ * state on the device and is advanced in chunks on its own stream while the
+ * others run (continuous batching).  No counterpart in the reference.
+ * ------------------------------------------------------------------------ */
+enum { LBM_SERVE_CAVITY = 0, LBM_SERVE_SPHERE = 1 };
+
+typedef struct lbm_serve_request {
+    double arrival_s;  /* arrival time, seconds after the start of the run; sorted */
+    int kind;          /* LBM_SERVE_CAVITY or LBM_SERVE_SPHERE */
+    int nx, ny, nz;
+    double reynolds;   /* cavity: lid 0.05 and nx; sphere: inflow 0.05 and D = floor(ny / 6.4) */
+    int steps;
+    int storage;       /* LBM_STORE_* */
+    float *fields;     /* optional: rho, ux, uy, uz of the result, [4][cells] */
+} lbm_serve_request;
+
+typedef struct lbm_serve_options {
+    double hbm_budget_bytes; /* admission budget (0: unlimited) */
+    int max_active;          /* solves in flight at once */
+    int chunk_steps;         /* steps issued per solve per pass */
+    double time_limit_s;     /* stop admitting and issuing after this (0: none) */
+    int sphere_markers;      /* markers per sphere (0: about pi D^2) */
+    int m_max;               /* IBM iterations for spheres (0: 3) */
+} lbm_serve_options;
+
+typedef struct lbm_serve_result {
+    double admit_s, finish_s; /* -1 when it never happened */
+    int status;               /* lbm_status of the request (LBM_ERR_STATE: cut by the time limit) */
+    uint32_t flags;           /* device status word at the end */
+    double drag;              /* sphere: x force of the last step (sum of -F_m ds) */
+} lbm_serve_result;
+
+/* Run the whole request trace; lattice_updates = cells x steps issued. */
+lbm_status lbmgpu_serve_run(const lbm_serve_request *reqs, int n, const lbm_serve_options *opt,
+                            lbm_serve_result *out, double *lattice_updates);
 
 const char *lbmgpu_last_error(void);
 int lbmgpu_abi_version(void);

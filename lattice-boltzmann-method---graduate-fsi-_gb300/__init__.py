@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "lbmgpu_last_error", "lbmgpu_abi_version",
     "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
-    "lbmgpu_batch_info",
+    "lbmgpu_batch_info", "lbmgpu_serve_run",
 ]
 
 
@@ -62,6 +62,25 @@ class IbmConfig(C.Structure):
                 ("density_ratio", C.c_double), ("volume", C.c_double), ("inertia", C.c_double),
                 ("gravity", C.c_double * 3), ("velocity", C.c_double * 3), ("T_body", C.c_double),
                 ("free_dofs", C.c_int)]
+
+
+class ServeRequest(C.Structure):
+    _fields_ = [("arrival_s", C.c_double), ("kind", C.c_int), ("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int),
+                ("reynolds", C.c_double), ("steps", C.c_int), ("storage", C.c_int),
+                ("fields", C.POINTER(C.c_float))]
+
+
+class ServeOptions(C.Structure):
+    _fields_ = [("hbm_budget_bytes", C.c_double), ("max_active", C.c_int), ("chunk_steps", C.c_int),
+                ("time_limit_s", C.c_double), ("sphere_markers", C.c_int), ("m_max", C.c_int)]
+
+
+class ServeResult(C.Structure):
+    _fields_ = [("admit_s", C.c_double), ("finish_s", C.c_double), ("status", C.c_int), ("flags", C.c_uint32),
+                ("drag", C.c_double)]
+
+
+SERVE_CAVITY, SERVE_SPHERE = 0, 1
 
 
 class LbmError(RuntimeError):
@@ -116,6 +135,7 @@ def load(path: str | None = None):
     L.lbmgpu_batch_download.argtypes = [vp, i, C.POINTER(C.c_float)]
     L.lbmgpu_batch_status.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
     for nm in ABI_SYMBOLS:
         fn = getattr(L, nm)
         if fn.restype is None and nm not in ("lbmgpu_last_error", "lbmgpu_abi_version"):
@@ -371,3 +391,41 @@ class Batch:
         v = C.c_longlong()
         check(self.L.lbmgpu_batch_info(self.h, C.byref(v), None))
         return v.value
+
+
+def serve_run(requests, max_active=32, chunk_steps=50, hbm_budget_bytes=0.0, time_limit_s=0.0, sphere_markers=0,
+              m_max=3, keep_fields=False):
+    """Run a request trace through lbmgpu_serve_run.  requests: list of dicts
+    with arrival_s, kind, nx, ny, nz, reynolds, steps, storage ("f32"/"f16").
+    Returns (results list of dicts, lattice updates issued)."""
+    L = load()
+    n = len(requests)
+    arr = (ServeRequest * max(1, n))()
+    bufs = []
+    for i, r in enumerate(requests):
+        a = arr[i]
+        a.arrival_s, a.kind = r["arrival_s"], r["kind"]
+        a.nx, a.ny, a.nz = r["nx"], r["ny"], r["nz"]
+        a.reynolds, a.steps = r["reynolds"], r["steps"]
+        st = r.get("storage", "f32")
+        a.storage = STORAGE[st] if isinstance(st, str) else st
+        if r.get("keep", keep_fields):
+            buf = np.zeros(4 * r["nx"] * r["ny"] * r["nz"], dtype=np.float32)
+            bufs.append(buf)
+            a.fields = buf.ctypes.data_as(C.POINTER(C.c_float))
+        else:
+            bufs.append(None)
+    o = ServeOptions()
+    o.hbm_budget_bytes, o.max_active, o.chunk_steps = hbm_budget_bytes, max_active, chunk_steps
+    o.time_limit_s, o.sphere_markers, o.m_max = time_limit_s, sphere_markers, m_max
+    res = (ServeResult * max(1, n))()
+    upd = C.c_double()
+    check(L.lbmgpu_serve_run(arr, n, C.byref(o), res, C.byref(upd)))
+    out = []
+    for i, r in enumerate(requests):
+        d = {"admit_s": res[i].admit_s, "finish_s": res[i].finish_s, "status": res[i].status,
+             "flags": res[i].flags, "drag": res[i].drag, "latency_s": res[i].finish_s - r["arrival_s"]}
+        if bufs[i] is not None:
+            d["fields"] = bufs[i].reshape(4, r["nz"], r["ny"], r["nx"])
+        out.append(d)
+    return out, upd.value

@@ -185,6 +185,8 @@ static void choose_block(lbm_handle *h) {
 // ---------------------------------------------------------------------------
 extern "C" int lbmgpu_abi_version(void) { return 1; }
 
+cudaStream_t lbm_handle_stream(lbm_handle *h) { return h->s; }
+
 extern "C" const char *lbmgpu_last_error(void) { return g_err.c_str(); }
 
 extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const uint8_t *types,
@@ -329,7 +331,7 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
     {
         const int V = c.storage == LBM_STORE_F32 ? 2 : 4;
-        h->vec = (c.vector >= 0 && !c.thermal && !(P.periodic & 1) && c.nx % V == 0 && c.nx >= 2 * V) ? 1 : 0;
+        h->vec = (c.vector > 0 && !c.thermal && !(P.periodic & 1) && c.nx % V == 0 && c.nx >= 2 * V) ? 1 : 0;
     }
     if (c.graph_steps > 0) h->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) h->gsteps = 0;
