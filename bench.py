@@ -139,7 +139,9 @@ def make_solver(pkg, orc, storage: str):
 
 
 def kernel_launches_per_lbm_step():
-    return 1 + 2 * M_MAX + 2  # fused collide-stream, m_max x (interp, spread), band collide, finish
+    # far-region and near-region fused steps, m_max x (interp, spread),
+    # band collide, finish
+    return 2 + 2 * M_MAX + 2
 
 
 def run_gpu(args):
@@ -301,7 +303,9 @@ def run_serving(pkg, orc, seconds: float, step_scale: float, rate: float = 200.0
                                                    for k, c in enumerate(("ux", "uy", "uz"))) / 0.05)})
     return {"workload": "Poisson %.0f req/s for %.1f s, steps x %.2f of log-U[1000, 20000]" % (rate, seconds,
                                                                                                step_scale),
-            "requests": len(reqs), "completed": int(len(lat)), "wall_s": wall,
+            "requests": len(reqs), "completed": int(len(lat)),
+            "diverged": int(sum(1 for r in res if r["status"] == 4)),
+            "cut_by_time_limit_or_rejected": int(sum(1 for r in res if r["status"] not in (0, 4))), "wall_s": wall,
             "aggregate_mlups": upd / wall / 1e6, "p50_latency_s": float(np.percentile(lat, 50)) if len(lat) else None,
             "p99_latency_s": float(np.percentile(lat, 99)) if len(lat) else None,
             "oracle_sample": errs}

@@ -97,6 +97,8 @@ typedef struct lbm_config {
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
                              stream); <0: serial */
     int vector;           /* >0: 8-byte group loads with warp shuffles when the row length allows; 0: scalar */
+    int xface;            /* 0: lanes on x = 0 / x = nx-1 keep the plain pull and redo their five
+                             x-crossing links; <0: their whole warp takes the boundary-class path */
 } lbm_config;
 
 typedef struct lbm_ibm_config {
@@ -155,6 +157,13 @@ lbm_status lbmgpu_step_timed(lbm_handle *h, int nsteps, double *ms);
  * device time of the n steps and the summed device time of the fused
  * collide-stream kernel. */
 lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms);
+
+/* As lbmgpu_step_profiled, split further: phases[0] total, [1] fused
+ * collide-stream launches (far + near), [2] the near-region launch alone,
+ * [3] the IBM phase (interpolation/spreading, band collision, reductions),
+ * each summed over the n steps, in milliseconds.  With the IBM phase
+ * overlapped, [3] runs concurrently with the next step's far launch. */
+lbm_status lbmgpu_step_phases(lbm_handle *h, int nsteps, double *phases);
 
 /* MacroProp moments of the current state (rho, u = (sum f c + F/2)/rho, T),
  * interior cells, x fastest. */

@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "lbmgpu_last_error", "lbmgpu_abi_version",
     "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
-    "lbmgpu_batch_info", "lbmgpu_serve_run",
+    "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_step_phases",
 ]
 
 
@@ -53,7 +53,7 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("vector", C.c_int)]
+                ("vector", C.c_int), ("xface", C.c_int)]
 
 
 class IbmConfig(C.Structure):
@@ -135,6 +135,7 @@ def load(path: str | None = None):
     L.lbmgpu_batch_download.argtypes = [vp, i, C.POINTER(C.c_float)]
     L.lbmgpu_batch_status.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
+    L.lbmgpu_step_phases.argtypes = [vp, i, dp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
     for nm in ABI_SYMBOLS:
         fn = getattr(L, nm)
@@ -155,7 +156,7 @@ def _dp(a: np.ndarray):
 
 def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0.0, 0.0), body=(0.0, 0.0, 0.0),
                 thermal=False, tau_g=0.0, T_init=0.0, T_ref=0.0, gbeta=(0.0, 0.0, 0.0), block=(0, 0),
-                graph_steps=0, staged=0, ibm_overlap=0, vector=0) -> Config:
+                graph_steps=0, staged=0, ibm_overlap=0, vector=0, xface=0) -> Config:
     c = Config()
     c.nx, c.ny, c.nz, c.tau = nx, ny, nz, tau
     c.storage = STORAGE[storage] if isinstance(storage, str) else storage
@@ -179,6 +180,7 @@ def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0
     c.staged = staged
     c.ibm_overlap = ibm_overlap
     c.vector = vector
+    c.xface = xface
     return c
 
 
@@ -265,6 +267,11 @@ class Solver:
         tot, fused = C.c_double(), C.c_double()
         check(self.L.lbmgpu_step_profiled(self.h, int(n), C.byref(tot), C.byref(fused)))
         return tot.value, fused.value
+
+    def step_phases(self, n: int) -> dict:
+        ph = np.zeros(4)
+        check(self.L.lbmgpu_step_phases(self.h, int(n), _dp(ph)))
+        return {"total": ph[0], "fused": ph[1], "near": ph[2], "ibm": ph[3]}
 
     def sync(self):
         check(self.L.lbmgpu_sync(self.h))

@@ -351,6 +351,14 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     P.S = ((P.N + std::max<long long>(512, 2LL * P.nx + 64) + 255) / 256) * 256;
     for (int l = 0; l < Q; l++)
         P.pofs[l] = (long long)l * P.S - ((long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l)));
+    P.idx32 = ((long long)Q * P.S + P.nx * (long long)P.ny < (1LL << 31)) ? 1 : 0;
+    for (int l = 0; l < Q; l++) {
+        P.pofs32[l] = P.idx32 ? (int)P.pofs[l] : 0;
+        P.sofs32[l] = P.idx32 ? (int)((long long)l * P.S) : 0;
+    }
+    // x-face lanes fix their own x-crossing links: warps stay on the plain
+    // pull in every row that is not on a y/z face
+    P.xface = (c.xface >= 0 && P.nx >= 2 && P.ny >= 3 && P.nz >= 3) ? 1 : 0;
     const size_t fb = ((size_t)Q * P.S + 2 * kGuard) * h->esize;
     for (int i = 0; i < 2 && st == LBM_OK; i++) {
         chk(dalloc(h, &h->fraw[i], fb), "populations");
@@ -596,7 +604,9 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev
             cudaEventRecord(ev[2], h->s);
             cudaEventRecord(ev[3], h->s);
         }
+        if (ev) cudaEventRecord(ev[4], h->s);
         if (h->ibm && (e = enqueue_ibm(h, a, h->s)) != cudaSuccess) return e;
+        if (ev) cudaEventRecord(ev[5], h->s);
         if (h->ibm) cudaEventRecord(h->ev_ibm, h->s);
         h->cur = 1 - h->cur;
         return cudaSuccess;
@@ -611,7 +621,9 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev
     if (ev) cudaEventRecord(ev[3], h->s);
     if ((e = cudaEventRecord(h->ev_near, h->s)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(h->s2, h->ev_near, 0)) != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[4], h->s2);
     if ((e = enqueue_ibm(h, a, h->s2)) != cudaSuccess) return e;
+    if (ev) cudaEventRecord(ev[5], h->s2);
     if ((e = cudaEventRecord(h->ev_ibm, h->s2)) != cudaSuccess) return e;
     h->cur = 1 - h->cur;
     return cudaSuccess;
@@ -667,6 +679,9 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
                 continue;
             }
             CUDA_TRY(cudaGraphLaunch(h->gexec[h->cur], h->s));
+            // the graph ends joined on the main stream; re-arm the IBM event
+            // outside the capture so later waits on it are ordinary ones
+            if (h->ibm && h->s2) CUDA_TRY(cudaEventRecord(h->ev_ibm, h->s));
             h->steps += h->gsteps;
             nsteps -= h->gsteps;
             continue;
@@ -692,20 +707,23 @@ extern "C" lbm_status lbmgpu_step_timed(lbm_handle *h, int nsteps, double *ms) {
     return LBM_OK;
 }
 
-extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms) {
+// Steps launched one by one with six events each: far/whole fused launch,
+// near launch, IBM phase (on whichever stream runs it).
+static lbm_status step_phases(lbm_handle *h, int nsteps, double *total, double *fused, double *near_ms,
+                              double *ibm_ms) {
     if (!h) return fail(LBM_ERR_INVALID, "step_profiled: null handle");
     if (!h->inited) return fail(LBM_ERR_STATE, "step_profiled: call lbmgpu_init first");
     if (nsteps < 0) return fail(LBM_ERR_INVALID, "step_profiled: negative step count");
-    // one event pair per fused launch, all read after the last step so the
-    // host never stalls the stream between steps
-    while ((int)h->evpool.size() < 4 * nsteps) {
+    // all events are read after the last step so the host never stalls the
+    // stream between steps
+    while ((int)h->evpool.size() < 6 * nsteps) {
         cudaEvent_t e;
         CUDA_TRY(cudaEventCreate(&e));
         h->evpool.push_back(e);
     }
     CUDA_TRY(cudaEventRecord(h->ev[0], h->s));
     for (int i = 0; i < nsteps; i++) {
-        CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, &h->evpool[4 * i]));
+        CUDA_TRY(enqueue_step(h, h->steps == 0 ? 0 : 1, &h->evpool[6 * i]));
         h->steps++;
     }
     CUDA_TRY(join_ibm(h));
@@ -713,16 +731,31 @@ extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *to
     CUDA_TRY(cudaEventSynchronize(h->ev[1]));
     float tot = 0.f;
     CUDA_TRY(cudaEventElapsedTime(&tot, h->ev[0], h->ev[1]));
-    double fused = 0.0;
+    double far = 0.0, nr = 0.0, ib = 0.0;
     for (int i = 0; i < nsteps; i++) {
-        float ms = 0.f, ms2 = 0.f;
-        CUDA_TRY(cudaEventElapsedTime(&ms, h->evpool[4 * i], h->evpool[4 * i + 1]));
-        CUDA_TRY(cudaEventElapsedTime(&ms2, h->evpool[4 * i + 2], h->evpool[4 * i + 3]));
-        fused += ms + ms2;
+        const cudaEvent_t *e = &h->evpool[6 * i];
+        float a = 0.f, b = 0.f, c = 0.f;
+        CUDA_TRY(cudaEventElapsedTime(&a, e[0], e[1]));
+        CUDA_TRY(cudaEventElapsedTime(&b, e[2], e[3]));
+        CUDA_TRY(cudaEventElapsedTime(&c, e[4], e[5]));
+        far += a;
+        nr += b;
+        ib += c;
     }
-    if (total_ms) *total_ms = tot;
-    if (fused_ms) *fused_ms = fused;
+    if (total) *total = tot;
+    if (fused) *fused = far + nr;
+    if (near_ms) *near_ms = nr;
+    if (ibm_ms) *ibm_ms = ib;
     return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_step_profiled(lbm_handle *h, int nsteps, double *total_ms, double *fused_ms) {
+    return step_phases(h, nsteps, total_ms, fused_ms, nullptr, nullptr);
+}
+
+extern "C" lbm_status lbmgpu_step_phases(lbm_handle *h, int nsteps, double *phases) {
+    if (!phases) return fail(LBM_ERR_INVALID, "step_phases: null argument");
+    return step_phases(h, nsteps, &phases[0], &phases[1], &phases[2], &phases[3]);
 }
 
 // ---------------------------------------------------------------------------

@@ -12,7 +12,7 @@ namespace lbmk {
 __device__ __forceinline__ float inv_one_plus(float drho) {
     const float s = 1.0f + drho;
     const float e = drho - (s - 1.0f);
-    const float inv = 1.0f / s;
+    const float inv = __frcp_rn(s);  // correctly rounded, as 1.0f / s
     return inv - inv * inv * e;
 }
 

@@ -80,6 +80,10 @@ struct StepParams {
     long long N;           // nx * ny * nz
     long long S;           // population stride (>= N + one tile of slack, see lbm_abi.cu)
     long long pofs[Q];     // l * S - (cx + nx (cy + ny cz)): pull offset of link l from the cell
+    int pofs32[Q];         // the same as 32-bit ints when idx32
+    int sofs32[Q];         // l * S as 32-bit ints when idx32
+    int idx32;             // 19 S < 2^31: 32-bit offsets from a per-cell base pointer
+    int xface;            // x-face lanes stay on the plain path and fix their x-crossing links
     float omega;           // dt / tau
     float omega_t;         // dt / tau_g
     float body[3];         // uniform body force

@@ -126,7 +126,12 @@ __device__ __forceinline__ void spread_marker(int m, int lane, const StepParams 
     }
 }
 
-__global__ void __launch_bounds__(128) k_ibm_interp(const __grid_constant__ StepParams P, MarkerDev mk,
+// The IBM kernels run beside the far-region collide-stream launch, which
+// leaves each SM 4096 registers: blocks of 64 threads with at most 64
+// registers a thread fit there without waiting for its blocks to retire.
+constexpr int kIbmThreads = 64;
+
+__global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_interp(const __grid_constant__ StepParams P, MarkerDev mk,
                                                     DevState *__restrict__ ds, const float *__restrict__ band,
                                                     int first, int thermal) {
     const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
@@ -134,7 +139,7 @@ __global__ void __launch_bounds__(128) k_ibm_interp(const __grid_constant__ Step
     interp_marker(m, threadIdx.x & 31, P, mk, ds, band, first, thermal);
 }
 
-__global__ void __launch_bounds__(128) k_ibm_spread(const __grid_constant__ StepParams P, MarkerDev mk,
+__global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_spread(const __grid_constant__ StepParams P, MarkerDev mk,
                                                     const DevState *__restrict__ ds, float *__restrict__ band,
                                                     int thermal) {
     const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
@@ -144,26 +149,26 @@ __global__ void __launch_bounds__(128) k_ibm_spread(const __grid_constant__ Step
 
 // One block.  Deterministic FP64 reductions: each thread sums a strided set
 // in index order, then a fixed shared-memory tree.
-__device__ __forceinline__ void block_tree(double (*red)[256], int nq, int t) {
+__device__ __forceinline__ void block_tree(double (*red)[kIbmThreads], int nq, int t) {
     __syncthreads();
-    for (int w = 128; w > 0; w >>= 1) {
+    for (int w = kIbmThreads / 2; w > 0; w >>= 1) {
         if (t < w)
             for (int k = 0; k < nq; k++) red[k][t] += red[k][t + w];
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(256) k_ibm_finish(const __grid_constant__ StepParams P, MarkerDev mk,
+__global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_finish(const __grid_constant__ StepParams P, MarkerDev mk,
                                                     DevState *__restrict__ ds, BodyParams bp,
                                                     const float *__restrict__ band, double *__restrict__ hist,
                                                     long long hist_cap) {
-    __shared__ double red[7][256];
+    __shared__ double red[7][kIbmThreads];
     __shared__ double sh_dxc[3], sh_om[3], sh_v[3], sh_xc[3], sh_f[7];
     const int t = threadIdx.x;
     const int n = mk.n;
     const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int m = t; m < n; m += 256) {
+    for (int m = t; m < n; m += kIbmThreads) {
         const double fx = mk.acc[m], fy = mk.acc[n + m], fz = mk.acc[2 * n + m], hq = mk.acc[3 * n + m];
         const double rx = mk.pos[m] - xc0, ry = mk.pos[n + m] - xc1, rz = mk.pos[2 * n + m] - xc2;
         s[0] += fx;
@@ -198,7 +203,7 @@ __global__ void __launch_bounds__(256) k_ibm_finish(const __grid_constant__ Step
     __syncthreads();
     double q[6] = {0, 0, 0, 0, 0, 0};
     const long long nb = P.nb;
-    for (long long b = t; b < nb; b += 256) {
+    for (long long b = t; b < nb; b += kIbmThreads) {
         const int bx = (int)(b % P.bsx), by = (int)((b / P.bsx) % P.bsy), bz = (int)(b / ((long long)P.bsx * P.bsy));
         const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
         if (x >= P.nx || y >= P.ny || z >= P.nz) continue;
@@ -254,7 +259,7 @@ __global__ void __launch_bounds__(256) k_ibm_finish(const __grid_constant__ Step
     }
     __syncthreads();
     const double R = bp.radius;
-    for (int m = t; m < n; m += 256) {
+    for (int m = t; m < n; m += kIbmThreads) {
         const double r0 = mk.pos[m] - (sh_xc[0] - sh_dxc[0]);
         const double r1 = mk.pos[n + m] - (sh_xc[1] - sh_dxc[1]);
         const double r2 = mk.pos[2 * n + m] - (sh_xc[2] - sh_dxc[2]);
@@ -275,21 +280,21 @@ __global__ void __launch_bounds__(256) k_ibm_finish(const __grid_constant__ Step
 }
 
 cudaError_t launch_ibm_interp(const IbmArgs &a, int first) {
-    const int threads = 128;
+    const int threads = kIbmThreads;
     const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;
     k_ibm_interp<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, first, a.thermal);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ibm_spread(const IbmArgs &a) {
-    const int threads = 128;
+    const int threads = kIbmThreads;
     const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;
     k_ibm_spread<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, a.thermal);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap) {
-    k_ibm_finish<<<1, 256, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
+    k_ibm_finish<<<1, kIbmThreads, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
     return cudaGetLastError();
 }
 

@@ -18,6 +18,35 @@
 
 namespace lbmk {
 
+// One link of the boundary-class path: bounce-back, face equilibrium, or a
+// pull from the (wrapped, or zero-gradient clamped) source cell.
+template <class T>
+__device__ __forceinline__ float pull_link(const T *__restrict__ A, int l, int x, int y, int z, long long cell,
+                                           const ClassEntry &ce, const StepParams &P) {
+    if ((ce.bb >> l) & 1u) return St<T>::ld(A + opp(l) * P.S + cell) + ce.val[l];
+    if ((ce.eq >> l) & 1u) return ce.val[l];
+    int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+    // periodic axes wrap; a zero-gradient link then clamps the remaining
+    // ghost coordinates onto the interior
+    if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+    if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+    if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+    if ((ce.zg >> l) & 1u) {
+        sx = min(max(sx, 0), P.nx - 1);
+        sy = min(max(sy, 0), P.ny - 1);
+        sz = min(max(sz, 0), P.nz - 1);
+    }
+    return St<T>::ld(A + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+}
+
+__device__ __forceinline__ int periodic_mask(const StepParams &P) {
+    return ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
+}
+
+// Pull the 19 populations of one cell.  A warp whose lanes all lie in rows
+// off the y/z faces takes the plain offsets; a lane on x = 0 or x = nx-1
+// then redoes the five links that cross its x face with the boundary-class
+// rule (xfix).  Any other warp takes the boundary-class path for every link.
 template <class T>
 __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q], int x, int y, int z,
                                             long long cell, int raw_cls, bool valid, bool bwarp, int gather,
@@ -29,39 +58,51 @@ __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q],
     }
     if (!bwarp) {
         const T *a = A + cell;
+        if (P.idx32) {
 #pragma unroll
-        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
-        return;
-    }
-    const int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
-    const ClassEntry &ce = P.cls[raw_cls & ~pm];
+            for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs32[l]) : 0.0f;
+        } else {
 #pragma unroll
-    for (int l = 0; l < Q; l++) {
-        float v = 0.0f;
-        if (valid) {
-            if ((ce.bb >> l) & 1u) {
-                v = St<T>::ld(A + opp(l) * P.S + cell) + ce.val[l];
-            } else if ((ce.eq >> l) & 1u) {
-                v = ce.val[l];
-            } else {
-                int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
-                // periodic axes wrap; a zero-gradient link then clamps the
-                // remaining ghost coordinates onto the interior
-                if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
-                if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
-                if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
-                if ((ce.zg >> l) & 1u) {
-                    sx = min(max(sx, 0), P.nx - 1);
-                    sy = min(max(sy, 0), P.ny - 1);
-                    sz = min(max(sz, 0), P.nz - 1);
-                }
-                v = St<T>::ld(A + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+            for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
+        }
+        if (raw_cls & 3) {
+            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+#pragma unroll
+            for (int l = 1; l < Q; l++) {
+                if (cx(l) > 0 && (raw_cls & 1)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+                if (cx(l) < 0 && (raw_cls & 2)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
             }
         }
-        f[l] = v;
+        return;
     }
+    const ClassEntry &ce = P.cls[raw_cls & ~periodic_mask(P)];
+#pragma unroll
+    for (int l = 0; l < Q; l++) f[l] = valid ? pull_link<T>(A, l, x, y, z, cell, ce, P) : 0.0f;
 }
 
+// One D3Q7 link of the boundary-class path: adiabatic or Dirichlet
+// (anti-)bounce-back, face equilibrium, or a pull from the source cell.
+template <class T>
+__device__ __forceinline__ float pull_heat_link(const T *__restrict__ G, int l, int x, int y, int z, long long cell,
+                                                const ClassEntry &ce, const StepParams &P) {
+    if ((ce.bb >> l) & 1u) {
+        const float own = St<T>::ld(G + opp(l) * P.S + cell);
+        return ((ce.tdir >> l) & 1u) ? (-own + ce.tval[l]) : own;
+    }
+    if ((ce.eq >> l) & 1u) return ce.tval[l];
+    int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+    if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+    if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+    if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+    if ((ce.zg >> l) & 1u) {
+        sx = min(max(sx, 0), P.nx - 1);
+        sy = min(max(sy, 0), P.ny - 1);
+        sz = min(max(sz, 0), P.nz - 1);
+    }
+    return St<T>::ld(G + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+}
+
+// The D3Q7 temperature populations, with the same split as gather_flow.
 template <class T>
 __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT], int x, int y, int z,
                                             long long cell, int raw_cls, bool valid, bool bwarp, int gather,
@@ -75,36 +116,19 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
         const T *a = G + cell;
 #pragma unroll
         for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
-        return;
-    }
-    const int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
-    const ClassEntry &ce = P.cls[raw_cls & ~pm];
+        if (raw_cls & 3) {
+            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
 #pragma unroll
-    for (int l = 0; l < QT; l++) {
-        float v = 0.0f;
-        if (valid) {
-            if ((ce.bb >> l) & 1u) {
-                float own = St<T>::ld(G + opp(l) * P.S + cell);
-                v = ((ce.tdir >> l) & 1u) ? (-own + ce.tval[l]) : own;
-            } else if ((ce.eq >> l) & 1u) {
-                v = ce.tval[l];
-            } else {
-                int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
-                // periodic axes wrap; a zero-gradient link then clamps the
-                // remaining ghost coordinates onto the interior
-                if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
-                if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
-                if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
-                if ((ce.zg >> l) & 1u) {
-                    sx = min(max(sx, 0), P.nx - 1);
-                    sy = min(max(sy, 0), P.ny - 1);
-                    sz = min(max(sz, 0), P.nz - 1);
-                }
-                v = St<T>::ld(G + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+            for (int l = 1; l < QT; l++) {
+                if (cx(l) > 0 && (raw_cls & 1)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+                if (cx(l) < 0 && (raw_cls & 2)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
             }
         }
-        g[l] = v;
+        return;
     }
+    const ClassEntry &ce = P.cls[raw_cls & ~periodic_mask(P)];
+#pragma unroll
+    for (int l = 0; l < QT; l++) g[l] = valid ? pull_heat_link<T>(G, l, x, y, z, cell, ce, P) : 0.0f;
 }
 
 // Everything after the gather of one cell: moments, optional moment output,
@@ -113,7 +137,7 @@ template <class T, bool THERMAL, bool FORCED>
 __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
                                             int gather, int export_only, T *__restrict__ B, T *__restrict__ GB,
                                             const StepParams &P, DevState *__restrict__ ds, float *__restrict__ mom,
-                                            float *__restrict__ band) {
+                                            float *__restrict__ band, bool check_band = true) {
     const long long N = P.N;
     float drho, jx, jy, jz;
     moments_pairs(f, drho, jx, jy, jz);
@@ -145,7 +169,7 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
     }
     if (export_only || !valid) return;
 
-    if (P.band_on) {
+    if (check_band && P.band_on) {
         const int bx = x - ds->band_o[0], by = y - ds->band_o[1], bz = z - ds->band_o[2];
         if ((unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy && (unsigned)bz < (unsigned)P.bsz) {
             const long long nb = P.nb;
@@ -172,8 +196,14 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
         }
     }
     collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, FORCED, P.omega);
+    if (P.idx32) {
+        T *b = B + cell;
 #pragma unroll
-    for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
+        for (int l = 0; l < Q; l++) St<T>::st(b + P.sofs32[l], f[l]);
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
+    }
     if (THERMAL) {
         collide_heat(g, Tc, ux, uy, uz, 0.0f, P.omega_t);
 #pragma unroll
@@ -215,12 +245,16 @@ __global__ void __launch_bounds__(256) k_step(const T *__restrict__ A, T *__rest
     const int raw = valid ? ((x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0) |
                              (z == 0 ? 16 : 0) | (z == P.nz - 1 ? 32 : 0))
                           : 0;
+    // With xface, x-face lanes of rows off the y/z faces stay on the plain
+    // path and fix their x-crossing links themselves (gather_flow).
+    const int rawrow = P.xface ? (raw & ~3) : raw;
     // the near box can start at a negative offset: keep those lanes idle
-    const bool bwarp = __any_sync(0xffffffffu, raw != 0 || (region == 2 && !valid));
+    const bool bwarp = __any_sync(0xffffffffu, rawrow != 0 || (region == 2 && !valid));
     float f[Q], g[QT];
     gather_flow<T>(A, f, x, y, z, cell, raw, valid, bwarp, gather, P);
     if (THERMAL) gather_heat<T>(GA, g, x, y, z, cell, raw, valid, bwarp, gather, P);
-    finish_cell<T, THERMAL, FORCED>(f, g, x, y, z, cell, valid, gather, export_only, B, GB, P, ds, mom, band);
+    finish_cell<T, THERMAL, FORCED>(f, g, x, y, z, cell, valid, gather, export_only, B, GB, P, ds, mom, band,
+                                    region != 1);
 }
 
 // ---------------------------------------------------------------------------
@@ -528,8 +562,10 @@ __global__ void __launch_bounds__(kConsumers + 32, 1)
 // unforced velocity from k_step, the accumulated IBM force Ft (band[7..9])
 // and heat source (band[11]).  u = u_unf + Ft / (2 rho) and F = Fb + sign Ft
 // (sign = -1 reproduces lbm.cpp:1347-1352); T = T_unf + Qt / 2.
+// 64-thread blocks of at most 64 registers: they fit beside the far-region
+// collide-stream blocks (which leave 4096 registers per SM) when overlapped.
 template <class T, bool THERMAL>
-__global__ void __launch_bounds__(256) k_band_collide(T *__restrict__ B, T *__restrict__ GB,
+__global__ void __launch_bounds__(64, 16) k_band_collide(T *__restrict__ B, T *__restrict__ GB,
                                                       const __grid_constant__ StepParams P,
                                                       const DevState *__restrict__ ds,
                                                       const float *__restrict__ band, float fsign) {
@@ -698,7 +734,7 @@ cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int ty_pref
 
 template <class T>
 static cudaError_t launch_band_t(const LaunchArgs &a, float fsign) {
-    int threads = 256;
+    const int threads = 64;
     long long blocks = (a.P->nb + threads - 1) / threads;
     if (a.thermal)
         k_band_collide<T, true><<<(unsigned)blocks, threads, 0, a.stream>>>((T *)a.B, (T *)a.GB, *a.P, a.ds, a.band,

@@ -152,3 +152,30 @@ def test_vector_matches_scalar_bitwise(pkg, storage):
         out.append(s.moments())
     for c in ("rho", "ux", "uy", "uz"):
         assert np.array_equal(out[0][c], out[1][c]), c
+
+
+@pytest.mark.parametrize("case", ["cavity_f32", "cavity_f16", "channel_thermal", "couette_periodic_x"])
+def test_xface_fix_matches_boundary_path_bitwise(pkg, case):
+    """Lanes on x = 0 and x = nx-1 either keep the plain pull and redo their
+    x-crossing links, or send their whole warp down the boundary-class path.
+    Both give the same bits."""
+    out = []
+    for xp in (0, -1):
+        if case.startswith("cavity"):
+            cfg = pkg.cavity_config(37, tau=0.6, lid=0.05, ny=21, nz=13, storage=case[-3:], xface=xp)
+        elif case == "channel_thermal":
+            cfg = pkg.channel_config(40, 18, 14, 0.6, u_in=0.05, thermal=True, T_in=1.0, tau_g=0.7,
+                                     gbeta=(0.0, 1e-4, 0.0), xface=xp)
+        else:
+            faces = {f: {"kind": pkg.FACE_PERIODIC} for f in (0, 1)}
+            faces.update({f: {"kind": pkg.FACE_WALL} for f in (2, 4, 5)})
+            faces[3] = {"kind": pkg.FACE_WALL, "u": (0.05, 0.0, 0.0)}
+            cfg = pkg.make_config(24, 16, 12, 0.7, "f32", faces, xface=xp)
+        s = pkg.Solver(cfg)
+        s.init()
+        s.step(1)
+        s.step(70)
+        assert s.status() == 0
+        out.append(s.moments())
+    for c in out[0]:
+        assert np.array_equal(out[0][c], out[1][c]), c

@@ -15,10 +15,10 @@ U = 0.05
 
 
 def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None,
-                overlap=0, u_in=U):
-    cfgkw = {"ibm_overlap": overlap}
+                overlap=0, u_in=U, graph_steps=0):
+    cfgkw = {"ibm_overlap": overlap, "graph_steps": graph_steps}
     if thermal:
-        cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0),
+        cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0), graph_steps=graph_steps,
                      gbeta=thermal.get("gbeta", (0, 0, 0)), T_ref=thermal.get("T0", 0.0))
     s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=u_in, storage=storage, **cfgkw))
     s.init()
@@ -126,3 +126,24 @@ def test_overlapped_and_serial_ibm_agree(pkg, orc):
     fa, fb = out[0][0], out[1][0]
     assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
     assert np.abs(out[0][1]["ux"] - out[1][1]["ux"]).max() / U < 1e-5
+
+
+@pytest.mark.parametrize("overlap", [0, -1], ids=["overlapped", "serial"])
+def test_graph_replay_and_eager_steps_interleave(pkg, orc, overlap):
+    """Graph replays of 10 steps mixed with single eager steps give what eager
+    stepping gives, with the IBM phase overlapped or serial."""
+    nx, ny, nz, tau, D, nm, m_max = 48, 32, 32, 0.6, 10.0, 315, 3
+    center = (16.0, 16.0, 16.0)
+    out = []
+    for gs in (10, 0):
+        s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, overlap=overlap, graph_steps=gs)
+        for n in (1, 10, 3, 20, 1, 10):
+            s.step(n)
+        assert s.status() == 0
+        assert s.steps_done() == 45
+        out.append((s.forces(), s.moments()))
+    fa, fb = out[0][0], out[1][0]
+    assert fa.shape == fb.shape
+    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fb[:, 0]).max() < 1e-4
+    for c in ("ux", "uy", "uz"):
+        assert np.abs(out[0][1][c] - out[1][1][c]).max() / U < 1e-5, c
