@@ -215,6 +215,31 @@ lbm_status lbmgpu_batch_download(lbm_batch *b, int problem, float *host);
 lbm_status lbmgpu_batch_status(lbm_batch *b, uint32_t *flags);
 lbm_status lbmgpu_batch_info(lbm_batch *b, long long *total_cells, long long *steps);
 
+/* Batched cavities without any device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc -- a host that gives
+ * the solver buffers from its own pre-sized device pool and must stay inside
+ * that pool's budget, or code that must not add the device-wide
+ * synchronisation an allocation can cause while other work is in flight.
+ * The caller owns the population buffers pop_a/pop_b (device memory, storage
+ * type of `storage`): cavity p's populations start at element
+ * base_p = 19 * sum_{q<p} S_q with S_q = 64 * ceil(Nx_q Ny_q Nz_q / 64), link l
+ * of cell c at base_p + l * S_p + c, values stored as f - w.  nsteps steps run
+ * A -> B -> A ...; the newest state ends in pop_a when nsteps is even, else in
+ * pop_b.  first_step = 1 takes pop_a as the initial (pre-collision) state.
+ * The library's working data (parameter table, tile table, status words) is
+ * a fixed 8.4 MB device array that every GPU loading the library holds until
+ * exit: at most 1024 cavities and 2^20 tiles of 256 cells; larger batches are
+ * rejected with LBM_ERR_INVALID.  Every call clears the status words itself
+ * and rewrites the tables, so nothing in that array has to start at zero.
+ * The first call on a device looks up that array's device address; make it
+ * before any stream capture.  All calls share
+ * the array: calls that overlap on the GPU race.  status_out (host, n words,
+ * may be NULL) receives the per-cavity status words; stream may be NULL (the
+ * default stream).  Allocates nothing. */
+lbm_status lbmgpu_batch_step_noalloc(int n, const int *dims, const double *tau, double lid_u, int storage,
+                                     void *pop_a, void *pop_b, int first_step, int nsteps, uint32_t *status_out,
+                                     void *stream);
+
 /* ------------------------------------------------------------------------
  * Serving loop: requests (lid-driven cavities or channels with a fixed
  * sphere) arrive on a wall-clock schedule; each is admitted as soon as it has

@@ -37,7 +37,7 @@ ABI_SYMBOLS = [
     "lbmgpu_last_error", "lbmgpu_abi_version",
     "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
-    "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_step_phases",
+    "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_batch_step_noalloc", "lbmgpu_step_phases",
 ]
 
 
@@ -136,6 +136,7 @@ def load(path: str | None = None):
     L.lbmgpu_batch_status.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.lbmgpu_step_phases.argtypes = [vp, i, dp]
+    L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
     for nm in ABI_SYMBOLS:
         fn = getattr(L, nm)
@@ -436,3 +437,28 @@ def serve_run(requests, max_active=32, chunk_steps=50, hbm_budget_bytes=0.0, tim
             d["fields"] = bufs[i].reshape(4, r["nz"], r["ny"], r["nx"])
         out.append(d)
     return out, upd.value
+
+
+def batch_layout(dims, storage="f16"):
+    """Element offsets and strides of the caller-owned population buffers of
+    lbmgpu_batch_step_noalloc: S_p = 64 * ceil(N_p / 64), base_p = 19 * sum S_q."""
+    dims = np.asarray(dims, dtype=np.int64).reshape(-1, 3)
+    N = dims.prod(axis=1)
+    S = ((N + 63) // 64) * 64
+    base = np.concatenate([[0], np.cumsum(19 * S)[:-1]])
+    total = int(19 * S.sum())
+    return base, S, total
+
+
+def batch_step_noalloc(dims, taus, lid, storage, pop_a_ptr, pop_b_ptr, first_step, nsteps, stream=0):
+    """Run lbmgpu_batch_step_noalloc on caller-owned device buffers; returns the status words."""
+    L = load()
+    dims = np.ascontiguousarray(np.asarray(dims, dtype=np.int32).reshape(-1, 3))
+    taus = np.ascontiguousarray(np.asarray(taus, dtype=np.float64))
+    n = dims.shape[0]
+    st = np.zeros(n, dtype=np.uint32)
+    check(L.lbmgpu_batch_step_noalloc(n, dims.ctypes.data_as(C.POINTER(C.c_int)), _dp(taus), lid,
+                                      STORAGE[storage] if isinstance(storage, str) else storage,
+                                      C.c_void_p(pop_a_ptr), C.c_void_p(pop_b_ptr), int(first_step), int(nsteps),
+                                      st.ctypes.data_as(C.POINTER(C.c_uint32)), C.c_void_p(stream or None)))
+    return st

@@ -412,3 +412,119 @@ extern "C" lbm_status lbmgpu_batch_info(lbm_batch *b, long long *total_cells, lo
     if (steps) *steps = b->steps;
     return LBM_OK;
 }
+
+// ---------------------------------------------------------------------------
+// Batched cavities without any device allocation.
+//
+// Some callers cannot call cudaMalloc: a host that hands the solver buffers
+// from its own pre-sized device pool and must stay inside that pool's fixed
+// budget, or code that must not introduce the device-wide synchronisation an
+// allocation can cause while other work is in flight.  For them this entry
+// point runs k_batch_step on the caller's population buffers and keeps its
+// own working data -- the per-cavity parameter table, the tile table and the
+// per-cavity status words -- in one file-scope device array of fixed size.
+// Every GPU that loads the library holds that array until the process exits.
+// Every call shares it, so calls that overlap on the GPU race with each other.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kNoAllocMaxCavities = 1024;
+constexpr long long kNoAllocMaxTiles = 1ll << 20;  // 256-cell tiles: up to 268M cells
+constexpr int kNoAllocTile = 256;
+struct NoAllocScratch {
+    BatchProb prob[kNoAllocMaxCavities];
+    uint32_t status[kNoAllocMaxCavities];
+    int2 tiles[kNoAllocMaxTiles];
+};
+constexpr int kMaxDevices = 64;
+}  // namespace
+
+// 8.4 MB of working space
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+static NoAllocScratch *g_noalloc_ptr[kMaxDevices];  // device address of the array, per device
+
+extern "C" lbm_status lbmgpu_batch_step_noalloc(int n, const int *dims, const double *tau, double lid_u, int storage,
+                                                void *pop_a, void *pop_b, int first_step, int nsteps,
+                                                uint32_t *status_out, void *stream) {
+    if (n < 1 || !dims || !tau || !pop_a || !pop_b || nsteps < 0 || storage < 0 || storage > 2)
+        return bfail(LBM_ERR_INVALID, "batch_step_noalloc: bad arguments");
+    if (n > kNoAllocMaxCavities)
+        return bfail(LBM_ERR_INVALID, "batch_step_noalloc: " + std::to_string(n) + " cavities exceed the maximum of " +
+                                          std::to_string(kNoAllocMaxCavities));
+    std::vector<BatchProb> hp(n);
+    std::vector<int2> tiles;
+    long long base = 0;
+    for (int p = 0; p < n; p++) {
+        BatchProb &pr = hp[p];
+        memset(&pr, 0, sizeof(pr));
+        pr.nx = dims[3 * p];
+        pr.ny = dims[3 * p + 1];
+        pr.nz = dims[3 * p + 2];
+        if (pr.nx < 2 || pr.ny < 2 || pr.nz < 2 || !(tau[p] > 0.5))
+            return bfail(LBM_ERR_INVALID,
+                         "batch_step_noalloc: cavity " + std::to_string(p) + " needs edges >= 2 and tau > 0.5");
+        pr.N = (long long)pr.nx * pr.ny * pr.nz;
+        pr.S = ((pr.N + 63) / 64) * 64;
+        pr.base = base;
+        pr.omega = (float)(1.0 / tau[p]);
+        pr.lid = (float)lid_u;
+        base += (long long)Q * pr.S;
+        const long long nt = (pr.N + kNoAllocTile - 1) / kNoAllocTile;
+        if ((long long)tiles.size() + nt > kNoAllocMaxTiles)
+            return bfail(LBM_ERR_INVALID, "batch_step_noalloc: more than " + std::to_string(kNoAllocMaxTiles) +
+                                              " tiles of 256 cells (" +
+                                              std::to_string(kNoAllocMaxTiles * kNoAllocTile) + " cells) in total");
+        for (long long k = 0; k < nt; k++) tiles.push_back(make_int2(p, (int)k));
+    }
+    int dev = 0;
+    BCUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kMaxDevices) return bfail(LBM_ERR_UNSUPPORTED, "batch_step_noalloc: device index too large");
+    if (!g_noalloc_ptr[dev]) {
+        // once per device, with the device current: the device address of the
+        // array (its host-side name is only a stand-in)
+        void *p = nullptr;
+        BCUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+        g_noalloc_ptr[dev] = reinterpret_cast<NoAllocScratch *>(p);
+    }
+    NoAllocScratch *sc = g_noalloc_ptr[dev];
+    cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    BCUDA(cudaMemcpyAsync(sc->prob, hp.data(), (size_t)n * sizeof(BatchProb), cudaMemcpyHostToDevice, s));
+    BCUDA(cudaMemcpyAsync(sc->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
+    BCUDA(cudaMemsetAsync(sc->status, 0, (size_t)n * sizeof(uint32_t), s));  // starts at zero on every call
+    int sms = 0, per = 0;
+    BCUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    switch (storage) {
+    case 0: BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<float, false>, kNoAllocTile, 0)); break;
+    case 1: BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<__half, false>, kNoAllocTile, 0)); break;
+    default:
+        BCUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_batch_step<__nv_bfloat16, false>, kNoAllocTile, 0));
+    }
+    const long long ntiles = (long long)tiles.size();
+    const int grid = (int)std::min<long long>(ntiles, (long long)std::max(1, per) * std::max(1, sms));
+    void *bufs[2] = {pop_a, pop_b};
+    for (int i = 0; i < nsteps; i++) {
+        const int gather = (i == 0 && first_step) ? 0 : 1;
+        const void *A = bufs[i & 1];
+        void *B = bufs[(i + 1) & 1];
+        switch (storage) {
+        case 0:
+            k_batch_step<float, false><<<grid, kNoAllocTile, 0, s>>>((const float *)A, (float *)B, sc->prob, sc->tiles,
+                                                                      ntiles, kNoAllocTile, gather, sc->status, nullptr);
+            break;
+        case 1:
+            k_batch_step<__half, false><<<grid, kNoAllocTile, 0, s>>>((const __half *)A, (__half *)B, sc->prob,
+                                                                       sc->tiles, ntiles, kNoAllocTile, gather,
+                                                                       sc->status, nullptr);
+            break;
+        default:
+            k_batch_step<__nv_bfloat16, false><<<grid, kNoAllocTile, 0, s>>>(
+                (const __nv_bfloat16 *)A, (__nv_bfloat16 *)B, sc->prob, sc->tiles, ntiles, kNoAllocTile, gather,
+                sc->status, nullptr);
+        }
+        BCUDA(cudaGetLastError());
+    }
+    if (status_out) {
+        BCUDA(cudaMemcpyAsync(status_out, sc->status, (size_t)n * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+        BCUDA(cudaStreamSynchronize(s));
+    }
+    return LBM_OK;
+}
