@@ -93,10 +93,11 @@ typedef struct lbm_config {
     double gbeta[3];      /* Boussinesq: F += gbeta * (T - T0)  (lbm.cpp:804-805) */
     int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
     int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
-    int staged;           /* bulk-copy (TMA) staged kernel: 0 = off, 1 = on, >1 = on with that many rows per tile */
+    int staged;           /* >0: the tensor-copy (TMA) staged kernel where rows allow it (row length a
+                             multiple of 32 cells and of 16 bytes); 0: direct loads everywhere (faster
+                             as measured) */
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
                              stream); <0: serial */
-    int vector;           /* >0: 8-byte group loads with warp shuffles when the row length allows; 0: scalar */
     int xface;            /* 0: lanes on x = 0 / x = nx-1 keep the plain pull and redo their five
                              x-crossing links; <0: their whole warp takes the boundary-class path */
 } lbm_config;

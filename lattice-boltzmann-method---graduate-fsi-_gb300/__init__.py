@@ -53,7 +53,7 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("vector", C.c_int), ("xface", C.c_int)]
+                ("xface", C.c_int)]
 
 
 class IbmConfig(C.Structure):
@@ -157,7 +157,7 @@ def _dp(a: np.ndarray):
 
 def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0.0, 0.0), body=(0.0, 0.0, 0.0),
                 thermal=False, tau_g=0.0, T_init=0.0, T_ref=0.0, gbeta=(0.0, 0.0, 0.0), block=(0, 0),
-                graph_steps=0, staged=0, ibm_overlap=0, vector=0, xface=0) -> Config:
+                graph_steps=0, staged=0, ibm_overlap=0, xface=0) -> Config:
     c = Config()
     c.nx, c.ny, c.nz, c.tau = nx, ny, nz, tau
     c.storage = STORAGE[storage] if isinstance(storage, str) else storage
@@ -180,7 +180,6 @@ def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0
     c.graph_steps = graph_steps
     c.staged = staged
     c.ibm_overlap = ibm_overlap
-    c.vector = vector
     c.xface = xface
     return c
 

@@ -57,8 +57,8 @@ struct lbm_handle {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;
     int tx = 128, ty = 2;
-    int vec = 0;  // 8-byte group kernel eligible
-    TmaPlan tma;
+    StagedPlan stp;                       // staged (bulk-copy) step kernel
+    int tile_x = 1, tile_y = 1;           // tile of the staged kernel (near-box rounding)
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
@@ -329,10 +329,6 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
                    : 0;
     build_classes(c, P);
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
-    {
-        const int V = c.storage == LBM_STORE_F32 ? 2 : 4;
-        h->vec = (c.vector > 0 && !c.thermal && !(P.periodic & 1) && c.nx % V == 0 && c.nx >= 2 * V) ? 1 : 0;
-    }
     if (c.graph_steps > 0) h->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) h->gsteps = 0;
     choose_block(h);
@@ -351,10 +347,17 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     P.S = ((P.N + std::max<long long>(512, 2LL * P.nx + 64) + 255) / 256) * 256;
     for (int l = 0; l < Q; l++)
         P.pofs[l] = (long long)l * P.S - ((long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l)));
-    P.idx32 = ((long long)Q * P.S + P.nx * (long long)P.ny < (1LL << 31)) ? 1 : 0;
+    // 32-bit element indices: every index (cell + l S - shift) stays below
+    // 19 S < 2^31 and is never negative (S exceeds any shift); idle lanes
+    // load the stencil of cell (1,1,1), which needs every edge >= 3
+    P.idx32 = ((long long)Q * P.S + P.nx * (long long)P.ny < (1LL << 31) && P.nx >= 3 && P.ny >= 3 && P.nz >= 3 &&
+               P.S > 1 + (long long)P.nx + (long long)P.nx * P.ny)
+                  ? 1
+                  : 0;
+    P.safe_cell = P.idx32 ? (unsigned)(1 + P.nx * (1 + (long long)P.ny)) : 0u;
     for (int l = 0; l < Q; l++) {
-        P.pofs32[l] = P.idx32 ? (int)P.pofs[l] : 0;
-        P.sofs32[l] = P.idx32 ? (int)((long long)l * P.S) : 0;
+        P.pofs32[l] = P.idx32 ? (unsigned)P.pofs[l] : 0u;
+        P.sofs32[l] = P.idx32 ? (unsigned)((long long)l * P.S) : 0u;
     }
     // x-face lanes fix their own x-crossing links: warps stay on the plain
     // pull in every row that is not on a y/z face
@@ -388,8 +391,14 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaEventCreateWithFlags(&h->ev_ibm, cudaEventDisableTiming), "events");
         if (st == LBM_OK) chk(cudaEventRecord(h->ev_ibm, h->s), "events");
     }
-    if (st == LBM_OK && c.staged > 0)
-        chk(plan_tma(c.storage, c.thermal != 0, P, c.staged > 1 ? c.staged : 0, h->tma), "staged plan");
+    if (st == LBM_OK && c.staged > 0) {
+        void *fb[2] = {h->f[0], h->f[1]}, *gb[2] = {h->g[0], h->g[1]};
+        chk(plan_staged(c.storage, c.thermal != 0, P, fb, gb, h->stp), "staged plan");
+        if (h->stp.enabled) {
+            h->tile_x = h->stp.tx;
+            h->tile_y = h->stp.ty;
+        }
+    }
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
         free_handle(h);
@@ -497,6 +506,18 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     h->P.bsy = bs[1];
     h->P.bsz = bs[2];
     h->P.nb = nb;
+    // near box: the band grown by the one-cell pull stencil, rounded out to
+    // whole tiles of the staged kernel in x and y
+    {
+        const int tile[3] = {h->tile_x, h->tile_y, 1};
+        for (int a = 0; a < 3; a++) {
+            int lo = std::max(0, org[a] - 1), hi = std::min(dims[a], org[a] + bs[a] + 1);
+            lo = (lo / tile[a]) * tile[a];
+            hi = std::min(dims[a], ((hi + tile[a] - 1) / tile[a]) * tile[a]);
+            h->P.nlo[a] = lo;
+            h->P.nhi[a] = hi;
+        }
+    }
     std::vector<float> ud((size_t)3 * n);
     for (int a = 0; a < 3; a++)
         for (int m = 0; m < n; m++) ud[(size_t)a * n + m] = (float)(udes ? udes[(size_t)a * n + m] : ic->velocity[a]);
@@ -552,11 +573,11 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.gather = gather;
     a.export_only = 0;
     a.region = 0;
-    a.vec = h->vec;
     a.thermal = h->cfg.thermal;
     a.tx = h->tx;
     a.ty = h->ty;
-    a.tma = h->tma;
+    a.st = &h->stp;
+    a.buf_a = h->cur;
     a.stream = h->s;
     return a;
 }

@@ -18,43 +18,53 @@ __device__ __forceinline__ float inv_one_plus(float drho) {
 
 // BGK + Guo collision on shifted populations (f~ = f - w), FP32:
 //   f~* = (1 - omega) f~ + omega (feq - w) + S,
-//   feq - w = w (drho + (1 + drho) P3(u)) with the third-order P3 of Calc_feq
+//   feq - w = w (drho + rho P3(u)) with the third-order P3 of Calc_feq
 //   (lbm.cpp:628-633), S = (1 - omega/2) w (3 c.F + 9 (c.F)(c.u) - 3 F.u)
 //   (lbm.cpp:101-102).
 // Links come in opposite pairs (l, l+1) for odd l (LBM.h:551), so
 // P3 = E(cu) +/- O(cu) with E = 4.5 cu^2 - 1.5 u^2 and
 // O = cu (3 + 4.5 (cu^2 - u^2)), and likewise for S: the pair shares one
-// evaluation of each part.
+// evaluation of each part.  Per weight class the factors omega w rho and
+// omega w (drho - 1.5 rho u^2) are formed once, so a pair costs a square, one
+// fused multiply-add for the even part, three operations for the odd part
+// and two fused multiply-adds per link.  drho enters additively, never
+// through fl(1 + drho).
 __device__ __forceinline__ void collide_flow(float f[Q], float drho, float ux, float uy, float uz, float Fx,
                                              float Fy, float Fz, bool forced, float omega) {
     const float usq = ux * ux + uy * uy + uz * uz;
     const float c1 = 1.0f - omega;
+    const float rho = 1.0f + drho;
+    const float orho = omega * rho;
+    const float odrho = omega * drho;
+    const float m15 = -1.5f * usq;
+    const float t3 = fmaf(-4.5f, usq, 3.0f);
+    // class 0 (rest), 1 (axis), 2 (diagonal)
+    const float k0 = orho * wf(0), k1 = orho * wf(1), k2 = orho * wf(7);
+    const float b0 = fmaf(k0, m15, odrho * wf(0));
+    const float b1 = fmaf(k1, m15, odrho * wf(1));
+    const float b2 = fmaf(k2, m15, odrho * wf(7));
+    const float h1 = 4.5f * k1, h2 = 4.5f * k2;
     const float gs = 1.0f - 0.5f * omega;
     const float Fu = Fx * ux + Fy * uy + Fz * uz;
-    {
-        const float p = -1.5f * usq;
-        f[0] = c1 * f[0] + omega * wf(0) * (drho + p + drho * p);
-        if (forced) f[0] += gs * wf(0) * (-3.0f * Fu);
-    }
+    f[0] = fmaf(c1, f[0], b0);
+    if (forced) f[0] += gs * wf(0) * (-3.0f * Fu);
 #pragma unroll
     for (int l = 1; l < Q; l += 2) {
+        const bool diag = (l >= 7);
+        const float k = diag ? k2 : k1, bb = diag ? b2 : b1, hh = diag ? h2 : h1;
         const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
         const float cu2 = cu * cu;
-        const float ev = 4.5f * cu2 - 1.5f * usq;
-        const float od = cu * (3.0f + 4.5f * (cu2 - usq));
-        // (1 + drho) x without forming 1 + drho
-        const float be = drho + ev + drho * ev;
-        const float bo = od + drho * od;
-        const float ow = omega * wf(l);
-        float a = c1 * f[l] + ow * (be + bo);
-        float b = c1 * f[l + 1] + ow * (be - bo);
+        const float ev = fmaf(hh, cu2, bb);              // omega w (drho + rho E)
+        const float od = (k * cu) * fmaf(4.5f, cu2, t3);  // omega w rho O
+        float a = fmaf(c1, f[l], ev + od);
+        float b = fmaf(c1, f[l + 1], ev - od);
         if (forced) {
             const float cF = cx(l) * Fx + cy(l) * Fy + cz(l) * Fz;
-            const float e = 9.0f * cF * cu - 3.0f * Fu;
-            const float o = 3.0f * cF;
             const float gw = gs * wf(l);
-            a += gw * (e + o);
-            b += gw * (e - o);
+            const float e = gw * fmaf(9.0f * cF, cu, -3.0f * Fu);
+            const float o = gw * (3.0f * cF);
+            a += e + o;
+            b += e - o;
         }
         f[l] = a;
         f[l + 1] = b;

@@ -80,9 +80,11 @@ struct StepParams {
     long long N;           // nx * ny * nz
     long long S;           // population stride (>= N + one tile of slack, see lbm_abi.cu)
     long long pofs[Q];     // l * S - (cx + nx (cy + ny cz)): pull offset of link l from the cell
-    int pofs32[Q];         // the same as 32-bit ints when idx32
-    int sofs32[Q];         // l * S as 32-bit ints when idx32
-    int idx32;             // 19 S < 2^31: 32-bit offsets from a per-cell base pointer
+    unsigned pofs32[Q];    // the same as 32-bit words when idx32 (never negative)
+    unsigned sofs32[Q];    // l * S as 32-bit words when idx32
+    int idx32;             // 19 S < 2^31 and a safe cell exists: 32-bit element indices
+    unsigned safe_cell;    // a cell whose whole pull stencil is inside the lattice: idle
+                           // lanes load from it instead of being predicated off
     int xface;            // x-face lanes stay on the plain path and fix their x-crossing links
     float omega;           // dt / tau
     float omega_t;         // dt / tau_g
@@ -94,6 +96,7 @@ struct StepParams {
     int band_on;
     int bsx, bsy, bsz;     // band extent
     long long nb;          // bsx * bsy * bsz
+    int nlo[3], nhi[3];    // near box of a fixed body: band grown by one cell, rounded out to tiles
     ClassEntry cls[64];
 };
 

@@ -1,19 +1,25 @@
 // lbm_internal.h -- launcher interface between the C-ABI layer (lbm_abi.cu)
 // and the kernel translation units.  Not part of the public ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "lbm_device.cuh"
 
 namespace lbmk {
 
-// Launch plan of the staged (bulk-copy) step kernel; enabled = 0 falls back
-// to the direct-load kernel.
-struct TmaPlan {
+// Launch plan of the staged (tensor-copy) step kernel k_step_st; enabled = 0
+// leaves every launch to the direct-load kernel k_step.
+struct StagedPlan {
     int enabled = 0;
-    int ty = 0, grid = 0, per_sm = 0;  // rows per tile, CTAs, CTAs per SM
+    int tx = 0, ty = 0;            // tile of one z plane
+    int tiles_x = 0, tiles_y = 0;  // tiles per row of tiles, rows of tiles per plane
     long long ntiles = 0;
+    int grid = 0;                  // blocks, all resident at once
     size_t smem = 0;
+    // per population buffer (A/B ping-pong): flow narrow box, flow wide box,
+    // heat narrow box, heat wide box; the narrow maps also serve the stores
+    CUtensorMap maps[2][4];
 };
 
 struct LaunchArgs {
@@ -28,15 +34,17 @@ struct LaunchArgs {
     int gather;
     int export_only;
     int region;  // 0 all cells, 1 all but the IBM near box, 2 the near box only
-    int vec;     // vector (8-byte group) kernel eligible
     int thermal;
     int tx, ty;
-    TmaPlan tma;
+    const StagedPlan *st;  // staged kernel plan (or null)
+    int buf_a;             // index of the population buffer read (A)
     cudaStream_t stream;
 };
 
 cudaError_t launch_step(int storage, const LaunchArgs &a);
-cudaError_t plan_tma(int storage, bool thermal, const StepParams &P, int ty_pref, TmaPlan &tp);
+cudaError_t plan_staged(int storage, bool thermal, const StepParams &P, void *const f[2], void *const g[2],
+                        StagedPlan &sp);
+cudaError_t launch_staged(int storage, const LaunchArgs &a);
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign);
 cudaError_t launch_init(int storage, void *A, void *GA, long long N, long long S, const float *fields,
                         const float init[5], bool thermal, cudaStream_t s);

@@ -1,0 +1,214 @@
+// lbm_step.cuh -- per-cell pieces of the fused collide-stream step shared
+// by the direct (k_step) and the staged (k_step_st) kernels: the pull of
+// the 19 (+7) populations with the boundary-class rules, and the update
+// (moments, IBM band hand-off or BGK + Guo collision).
+#pragma once
+#include "lbm_collide.cuh"
+#include "lbm_device.cuh"
+
+namespace lbmk {
+
+// One link of the boundary-class path: bounce-back, face equilibrium, or a
+// pull from the (wrapped, or zero-gradient clamped) source cell.
+template <class T>
+__device__ __forceinline__ float pull_link(const T *__restrict__ A, int l, int x, int y, int z, long long cell,
+                                           const ClassEntry &ce, const StepParams &P) {
+    if ((ce.bb >> l) & 1u) return St<T>::ld(A + opp(l) * P.S + cell) + ce.val[l];
+    if ((ce.eq >> l) & 1u) return ce.val[l];
+    int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+    // periodic axes wrap; a zero-gradient link then clamps the remaining
+    // ghost coordinates onto the interior
+    if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+    if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+    if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+    if ((ce.zg >> l) & 1u) {
+        sx = min(max(sx, 0), P.nx - 1);
+        sy = min(max(sy, 0), P.ny - 1);
+        sz = min(max(sz, 0), P.nz - 1);
+    }
+    return St<T>::ld(A + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+}
+
+__device__ __forceinline__ int periodic_mask(const StepParams &P) {
+    return ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
+}
+
+// Pull the 19 populations of one cell.  A warp whose lanes all lie in rows
+// off the y/z faces takes the plain offsets; a lane on x = 0 or x = nx-1
+// then redoes the five links that cross its x face with the boundary-class
+// rule (xfix).  Any other warp takes the boundary-class path for every link.
+template <class T>
+__device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q], int x, int y, int z,
+                                            long long cell, int raw_cls, bool valid, bool bwarp, int gather,
+                                            const StepParams &P) {
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(A + l * P.S + cell) : 0.0f;
+        return;
+    }
+    if (!bwarp) {
+        const T *a = A + cell;
+        if (P.idx32) {
+            // idle lanes read a safe stencil instead of being predicated off
+            const unsigned c = valid ? (unsigned)cell : P.safe_cell;
+#pragma unroll
+            for (int l = 0; l < Q; l++) f[l] = St<T>::ld(A + (c + P.pofs32[l]));
+        } else {
+#pragma unroll
+            for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
+        }
+        if (raw_cls & 3) {
+            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+#pragma unroll
+            for (int l = 1; l < Q; l++) {
+                if (cx(l) > 0 && (raw_cls & 1)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+                if (cx(l) < 0 && (raw_cls & 2)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+            }
+        }
+        return;
+    }
+    const ClassEntry &ce = P.cls[raw_cls & ~periodic_mask(P)];
+#pragma unroll
+    for (int l = 0; l < Q; l++) f[l] = valid ? pull_link<T>(A, l, x, y, z, cell, ce, P) : 0.0f;
+}
+
+// One D3Q7 link of the boundary-class path: adiabatic or Dirichlet
+// (anti-)bounce-back, face equilibrium, or a pull from the source cell.
+template <class T>
+__device__ __forceinline__ float pull_heat_link(const T *__restrict__ G, int l, int x, int y, int z, long long cell,
+                                                const ClassEntry &ce, const StepParams &P) {
+    if ((ce.bb >> l) & 1u) {
+        const float own = St<T>::ld(G + opp(l) * P.S + cell);
+        return ((ce.tdir >> l) & 1u) ? (-own + ce.tval[l]) : own;
+    }
+    if ((ce.eq >> l) & 1u) return ce.tval[l];
+    int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+    if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+    if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+    if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+    if ((ce.zg >> l) & 1u) {
+        sx = min(max(sx, 0), P.nx - 1);
+        sy = min(max(sy, 0), P.ny - 1);
+        sz = min(max(sz, 0), P.nz - 1);
+    }
+    return St<T>::ld(G + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
+}
+
+// The D3Q7 temperature populations, with the same split as gather_flow.
+template <class T>
+__device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT], int x, int y, int z,
+                                            long long cell, int raw_cls, bool valid, bool bwarp, int gather,
+                                            const StepParams &P) {
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(G + l * P.S + cell) : 0.0f;
+        return;
+    }
+    if (!bwarp) {
+        const T *a = G + cell;
+#pragma unroll
+        for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
+        if (raw_cls & 3) {
+            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+#pragma unroll
+            for (int l = 1; l < QT; l++) {
+                if (cx(l) > 0 && (raw_cls & 1)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+                if (cx(l) < 0 && (raw_cls & 2)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+            }
+        }
+        return;
+    }
+    const ClassEntry &ce = P.cls[raw_cls & ~periodic_mask(P)];
+#pragma unroll
+    for (int l = 0; l < QT; l++) g[l] = valid ? pull_heat_link<T>(G, l, x, y, z, cell, ce, P) : 0.0f;
+}
+
+// Everything after the gather of one cell except the stores: moments,
+// optional moment output, then either the band hand-off (f, g keep the
+// pre-collision populations; the unforced moments go to the band arrays) or
+// the collision.  Returns whether f (and g) are to be stored for this cell.
+template <class T, bool THERMAL, bool FORCED>
+__device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
+                                            int gather, int export_only, const StepParams &P,
+                                            DevState *__restrict__ ds, float *__restrict__ mom,
+                                            float *__restrict__ band, bool check_band) {
+    const long long N = P.N;
+    float drho, jx, jy, jz;
+    moments_pairs(f, drho, jx, jy, jz);
+    float Tc = 0.0f;
+    float Fx = P.body[0], Fy = P.body[1], Fz = P.body[2];
+    if (THERMAL) {
+#pragma unroll
+        for (int l = 0; l < QT; l++) Tc += g[l];
+        Fx += P.gbeta[0] * (Tc - P.T0);
+        Fy += P.gbeta[1] * (Tc - P.T0);
+        Fz += P.gbeta[2] * (Tc - P.T0);
+    }
+    const float rho = 1.0f + drho;
+    const float inv = inv_one_plus(drho);
+    // Before the first streaming the reference collides with the velocity
+    // stored at set-up (LBM::Init, lbm.cpp:31-57), i.e. without the F/2 shift
+    // that MacroProp applies afterwards (lbm.cpp:677-679).
+    const float hf = gather ? 0.5f : 0.0f;
+    const float ux = (jx + hf * Fx) * inv;
+    const float uy = (jy + hf * Fy) * inv;
+    const float uz = (jz + hf * Fz) * inv;
+    if (valid && !(rho > 0.0f && rho < 100.0f)) atomicOr(&ds->status, ST_RHO_RANGE);
+    if (mom != nullptr && valid) {
+        mom[cell] = rho;
+        mom[N + cell] = ux;
+        mom[2 * N + cell] = uy;
+        mom[3 * N + cell] = uz;
+        if (THERMAL) mom[4 * N + cell] = Tc;
+    }
+    if (export_only || !valid) return false;
+
+    if (check_band && P.band_on) {
+        const int bx = x - ds->band_o[0], by = y - ds->band_o[1], bz = z - ds->band_o[2];
+        if ((unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy && (unsigned)bz < (unsigned)P.bsz) {
+            const long long nb = P.nb;
+            const long long b = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
+            band[b] = drho;
+            band[nb + b] = ux;
+            band[2 * nb + b] = uy;
+            band[3 * nb + b] = uz;
+            band[4 * nb + b] = Fx;
+            band[5 * nb + b] = Fy;
+            band[6 * nb + b] = Fz;
+            band[7 * nb + b] = 0.0f;
+            band[8 * nb + b] = 0.0f;
+            band[9 * nb + b] = 0.0f;
+            band[10 * nb + b] = Tc;
+            band[11 * nb + b] = 0.0f;
+            return true;
+        }
+    }
+    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, FORCED, P.omega);
+    if (THERMAL) collide_heat(g, Tc, ux, uy, uz, 0.0f, P.omega_t);
+    return true;
+}
+
+// update_cell followed by the stores to B (and GB).
+template <class T, bool THERMAL, bool FORCED>
+__device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
+                                            int gather, int export_only, T *__restrict__ B, T *__restrict__ GB,
+                                            const StepParams &P, DevState *__restrict__ ds, float *__restrict__ mom,
+                                            float *__restrict__ band, bool check_band = true) {
+    if (!update_cell<T, THERMAL, FORCED>(f, g, x, y, z, cell, valid, gather, export_only, P, ds, mom, band,
+                                         check_band))
+        return;
+    if (P.idx32) {
+        const unsigned c = (unsigned)cell;
+#pragma unroll
+        for (int l = 0; l < Q; l++) St<T>::st(B + (c + P.sofs32[l]), f[l]);
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
+    }
+    if (THERMAL) {
+#pragma unroll
+        for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
+    }
+}
+
+}  // namespace lbmk

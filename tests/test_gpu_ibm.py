@@ -15,10 +15,11 @@ U = 0.05
 
 
 def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None,
-                overlap=0, u_in=U, graph_steps=0):
-    cfgkw = {"ibm_overlap": overlap, "graph_steps": graph_steps}
+                overlap=0, u_in=U, graph_steps=0, staged=0):
+    cfgkw = {"ibm_overlap": overlap, "graph_steps": graph_steps, "staged": staged}
     if thermal:
         cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0), graph_steps=graph_steps,
+                     staged=staged,
                      gbeta=thermal.get("gbeta", (0, 0, 0)), T_ref=thermal.get("T0", 0.0))
     s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=u_in, storage=storage, **cfgkw))
     s.init()
@@ -36,14 +37,16 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
     return s
 
 
+@pytest.mark.parametrize("staged", [0, 1], ids=["direct", "staged"])
 @pytest.mark.parametrize("overlap", [0, -1], ids=["overlapped", "serial"])
 @pytest.mark.parametrize("lit_sign", [0, 1])
-def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap):
+def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap, staged):
     """The IBM phase on its own stream overlapping the far-region streaming,
-    and in the serial order."""
-    nx, ny, nz, tau, D, nm, m_max, steps = 48, 30, 28, 0.56, 10.0, 314, 3, 120
+    and in the serial order; direct-load and staged (64 x 32 rows) kernels."""
+    nx, ny, nz, tau, D, nm, m_max, steps = 64, 32, 28, 0.56, 10.0, 314, 3, 120
     center = (16.0, 15.3, 14.6)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, overlap=overlap)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, overlap=overlap,
+                    staged=staged)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -60,7 +63,7 @@ def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap):
 
 
 def test_fixed_sphere_fp16_drag(pkg, orc):
-    nx, ny, nz, tau, D, nm, m_max, steps = 48, 30, 28, 0.56, 10.0, 314, 3, 150
+    nx, ny, nz, tau, D, nm, m_max, steps = 64, 32, 28, 0.56, 10.0, 314, 3, 150
     center = (16.0, 15.0, 14.0)
     s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f16")
     s.step(steps)
@@ -74,18 +77,19 @@ def test_fixed_sphere_fp16_drag(pkg, orc):
     assert ed < 5e-3 and eu < 1e-3
 
 
-def test_thermal_free_sphere_vs_oracle(pkg, orc):
+@pytest.mark.parametrize("staged", [0, 1], ids=["direct", "staged"])
+def test_thermal_free_sphere_vs_oracle(pkg, orc, staged):
     """D3Q7 thermal population, Boussinesq force, thermal IBM (T_body = 1)
     and the FP64 Newton-Euler body (held in x and rotation, free in y and z)
     settling in fluid at rest, against the oracle."""
-    nx, ny, nz, tau, D, nm, m_max, steps = 40, 32, 28, 0.56, 8.0, 201, 3, 80
+    nx, ny, nz, tau, D, nm, m_max, steps = 64, 32, 28, 0.56, 8.0, 201, 3, 80
     center = (14.0, 16.2, 13.7)
     nu = (tau - 0.5) / 3.0
     alpha = nu / 0.71
     th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
     # rho_s/rho_f = 3: the explicit coupling of a D = 8 sphere is unstable at 1.5
     fr = dict(rho_ratio=3.0, gravity=(0.0, -1e-5, 0.0), dof=0b000110)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=0.0)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=0.0, staged=staged)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -132,7 +136,7 @@ def test_overlapped_and_serial_ibm_agree(pkg, orc):
 def test_graph_replay_and_eager_steps_interleave(pkg, orc, overlap):
     """Graph replays of 10 steps mixed with single eager steps give what eager
     stepping gives, with the IBM phase overlapped or serial."""
-    nx, ny, nz, tau, D, nm, m_max = 48, 32, 32, 0.6, 10.0, 315, 3
+    nx, ny, nz, tau, D, nm, m_max = 64, 32, 32, 0.6, 10.0, 315, 3
     center = (16.0, 16.0, 16.0)
     out = []
     for gs in (10, 0):
