@@ -63,7 +63,8 @@ struct lbm_handle {
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;
     cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
-    cudaEvent_t ev_near = nullptr, ev_ibm = nullptr;
+    cudaStream_t s3 = nullptr;            // force reduction, beside the last spreading and band collision
+    cudaEvent_t ev_near = nullptr, ev_ibm = nullptr, ev_acc = nullptr, ev_fin = nullptr;
 };
 
 // ---------------------------------------------------------------------------
@@ -280,7 +281,10 @@ static void free_handle(lbm_handle *h) {
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
     if (h->ev_near) cudaEventDestroy(h->ev_near);
     if (h->ev_ibm) cudaEventDestroy(h->ev_ibm);
+    if (h->ev_acc) cudaEventDestroy(h->ev_acc);
+    if (h->ev_fin) cudaEventDestroy(h->ev_fin);
     if (h->s2) cudaStreamDestroy(h->s2);
+    if (h->s3) cudaStreamDestroy(h->s3);
     if (h->s) cudaStreamDestroy(h->s);
     delete h;
 }
@@ -388,8 +392,12 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaDeviceGetStreamPriorityRange(&lo, &hi), "priority range");
         chk(cudaStreamCreateWithPriority(&h->s2, cudaStreamNonBlocking, hi), "ibm stream");
         chk(cudaEventCreateWithFlags(&h->ev_near, cudaEventDisableTiming), "events");
+        chk(cudaStreamCreateWithPriority(&h->s3, cudaStreamNonBlocking, hi), "reduction stream");
         chk(cudaEventCreateWithFlags(&h->ev_ibm, cudaEventDisableTiming), "events");
+        chk(cudaEventCreateWithFlags(&h->ev_acc, cudaEventDisableTiming), "events");
+        chk(cudaEventCreateWithFlags(&h->ev_fin, cudaEventDisableTiming), "events");
         if (st == LBM_OK) chk(cudaEventRecord(h->ev_ibm, h->s), "events");
+        if (st == LBM_OK) chk(cudaEventRecord(h->ev_fin, h->s), "events");
     }
     if (st == LBM_OK && c.staged > 0) {
         void *fb[2] = {h->f[0], h->f[1]}, *gb[2] = {h->g[0], h->g[1]};
@@ -411,6 +419,7 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
 extern "C" lbm_status lbmgpu_destroy(lbm_handle *h) {
     if (!h) return LBM_OK;
     if (h->s2) cudaStreamSynchronize(h->s2);
+    if (h->s3) cudaStreamSynchronize(h->s3);
     if (h->s) cudaStreamSynchronize(h->s);
     free_handle(h);
     return LBM_OK;
@@ -582,7 +591,10 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     return a;
 }
 
-static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t s) {
+// The IBM phase on stream s.  split: the force reduction (which needs only the
+// last interpolation) runs on s3 beside the last spreading and the band
+// collision, and the next phase's first interpolation waits for it.
+static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t s, bool split) {
     cudaError_t e;
     IbmArgs ia;
     ia.P = &h->P;
@@ -594,11 +606,21 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
     LaunchArgs b = a;
     b.stream = s;
     const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
+    if (split && (e = cudaStreamWaitEvent(s, h->ev_fin, 0)) != cudaSuccess) return e;
     for (int it = 1; it <= h->icfg.m_max; it++) {
         if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
+        if (split && it == h->icfg.m_max) {
+            if ((e = cudaEventRecord(h->ev_acc, s)) != cudaSuccess) return e;
+            if ((e = cudaStreamWaitEvent(h->s3, h->ev_acc, 0)) != cudaSuccess) return e;
+            IbmArgs fa = ia;
+            fa.stream = h->s3;
+            if ((e = launch_ibm_finish(fa, h->bp, h->hist, h->hist_cap)) != cudaSuccess) return e;
+            if ((e = cudaEventRecord(h->ev_fin, h->s3)) != cudaSuccess) return e;
+        }
         if ((e = launch_ibm_spread(ia)) != cudaSuccess) return e;
     }
     if ((e = launch_band_collide(h->cfg.storage, b, fsign)) != cudaSuccess) return e;
+    if (split) return cudaSuccess;
     return launch_ibm_finish(ia, h->bp, h->hist, h->hist_cap);
 }
 
@@ -626,7 +648,7 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev
             cudaEventRecord(ev[3], h->s);
         }
         if (ev) cudaEventRecord(ev[4], h->s);
-        if (h->ibm && (e = enqueue_ibm(h, a, h->s)) != cudaSuccess) return e;
+        if (h->ibm && (e = enqueue_ibm(h, a, h->s, false)) != cudaSuccess) return e;
         if (ev) cudaEventRecord(ev[5], h->s);
         if (h->ibm) cudaEventRecord(h->ev_ibm, h->s);
         h->cur = 1 - h->cur;
@@ -643,7 +665,7 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev
     if ((e = cudaEventRecord(h->ev_near, h->s)) != cudaSuccess) return e;
     if ((e = cudaStreamWaitEvent(h->s2, h->ev_near, 0)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[4], h->s2);
-    if ((e = enqueue_ibm(h, a, h->s2)) != cudaSuccess) return e;
+    if ((e = enqueue_ibm(h, a, h->s2, true)) != cudaSuccess) return e;
     if (ev) cudaEventRecord(ev[5], h->s2);
     if ((e = cudaEventRecord(h->ev_ibm, h->s2)) != cudaSuccess) return e;
     h->cur = 1 - h->cur;
@@ -653,7 +675,9 @@ static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev
 // Order everything after the last IBM phase on the main stream.
 static cudaError_t join_ibm(lbm_handle *h) {
     if (!h->ibm || !h->s2) return cudaSuccess;
-    return cudaStreamWaitEvent(h->s, h->ev_ibm, 0);
+    cudaError_t e = cudaStreamWaitEvent(h->s, h->ev_ibm, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(h->s, h->ev_fin, 0);
+    return e;
 }
 
 static lbm_status ensure_graph(lbm_handle *h) {
@@ -702,7 +726,10 @@ extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
             CUDA_TRY(cudaGraphLaunch(h->gexec[h->cur], h->s));
             // the graph ends joined on the main stream; re-arm the IBM event
             // outside the capture so later waits on it are ordinary ones
-            if (h->ibm && h->s2) CUDA_TRY(cudaEventRecord(h->ev_ibm, h->s));
+            if (h->ibm && h->s2) {
+                CUDA_TRY(cudaEventRecord(h->ev_ibm, h->s));
+                CUDA_TRY(cudaEventRecord(h->ev_fin, h->s));
+            }
             h->steps += h->gsteps;
             nsteps -= h->gsteps;
             continue;

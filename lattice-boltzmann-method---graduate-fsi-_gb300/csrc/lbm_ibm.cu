@@ -149,26 +149,31 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_spread(const __grid_con
 
 // One block.  Deterministic FP64 reductions: each thread sums a strided set
 // in index order, then a fixed shared-memory tree.
-__device__ __forceinline__ void block_tree(double (*red)[kIbmThreads], int nq, int t) {
+// The one-block reduction kernel runs on its own, so it takes a full-size
+// block: its per-thread loops over the markers and the band are four times
+// shorter than with kIbmThreads.
+constexpr int kFinishThreads = 256;
+
+__device__ __forceinline__ void block_tree(double (*red)[kFinishThreads], int nq, int t) {
     __syncthreads();
-    for (int w = kIbmThreads / 2; w > 0; w >>= 1) {
+    for (int w = kFinishThreads / 2; w > 0; w >>= 1) {
         if (t < w)
             for (int k = 0; k < nq; k++) red[k][t] += red[k][t + w];
         __syncthreads();
     }
 }
 
-__global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_finish(const __grid_constant__ StepParams P, MarkerDev mk,
+__global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_constant__ StepParams P, MarkerDev mk,
                                                     DevState *__restrict__ ds, BodyParams bp,
                                                     const float *__restrict__ band, double *__restrict__ hist,
                                                     long long hist_cap) {
-    __shared__ double red[7][kIbmThreads];
+    __shared__ double red[7][kFinishThreads];
     __shared__ double sh_dxc[3], sh_om[3], sh_v[3], sh_xc[3], sh_f[7];
     const int t = threadIdx.x;
     const int n = mk.n;
     const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int m = t; m < n; m += kIbmThreads) {
+    for (int m = t; m < n; m += kFinishThreads) {
         const double fx = mk.acc[m], fy = mk.acc[n + m], fz = mk.acc[2 * n + m], hq = mk.acc[3 * n + m];
         const double rx = mk.pos[m] - xc0, ry = mk.pos[n + m] - xc1, rz = mk.pos[2 * n + m] - xc2;
         s[0] += fx;
@@ -203,7 +208,7 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_finish(const __grid_con
     __syncthreads();
     double q[6] = {0, 0, 0, 0, 0, 0};
     const long long nb = P.nb;
-    for (long long b = t; b < nb; b += kIbmThreads) {
+    for (long long b = t; b < nb; b += kFinishThreads) {
         const int bx = (int)(b % P.bsx), by = (int)((b / P.bsx) % P.bsy), bz = (int)(b / ((long long)P.bsx * P.bsy));
         const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
         if (x >= P.nx || y >= P.ny || z >= P.nz) continue;
@@ -259,7 +264,7 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_finish(const __grid_con
     }
     __syncthreads();
     const double R = bp.radius;
-    for (int m = t; m < n; m += kIbmThreads) {
+    for (int m = t; m < n; m += kFinishThreads) {
         const double r0 = mk.pos[m] - (sh_xc[0] - sh_dxc[0]);
         const double r1 = mk.pos[n + m] - (sh_xc[1] - sh_dxc[1]);
         const double r2 = mk.pos[2 * n + m] - (sh_xc[2] - sh_dxc[2]);
@@ -294,7 +299,7 @@ cudaError_t launch_ibm_spread(const IbmArgs &a) {
 }
 
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap) {
-    k_ibm_finish<<<1, kIbmThreads, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
+    k_ibm_finish<<<1, kFinishThreads, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
     return cudaGetLastError();
 }
 
