@@ -148,9 +148,12 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
     dim3 blk(a.tx, a.ty, 1);
     dim3 grd((a.P->nx + a.tx - 1) / a.tx, (a.P->ny + a.ty - 1) / a.ty, a.P->nz);
     const bool forced = a.P->forced != 0;
-    if (a.region == 2)
-        grd = dim3((a.P->nhi[0] - a.P->nlo[0] + a.tx - 1) / a.tx, (a.P->nhi[1] - a.P->nlo[1] + a.ty - 1) / a.ty,
+    if (a.region == 2) {
+        // the near box is a few tens of cells wide: 32 x 8 blocks keep few lanes idle
+        blk = dim3(32, 8, 1);
+        grd = dim3((a.P->nhi[0] - a.P->nlo[0] + 31) / 32, (a.P->nhi[1] - a.P->nlo[1] + 7) / 8,
                    a.P->nhi[2] - a.P->nlo[2]);
+    }
     if (a.thermal)
         k_step<T, true, true><<<grd, blk, 0, a.stream>>>((const T *)a.A, (T *)a.B, (const T *)a.GA, (T *)a.GB, *a.P,
                                                          a.ds, a.mom, a.band, a.gather, a.export_only, a.region);
