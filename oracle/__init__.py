@@ -80,6 +80,7 @@ def lib():
         L.orc_feq.restype = d
         L.orc_feq.argtypes = [vp, d, d, d, d, i]
         L.orc_init.argtypes = [vp]
+        L.orc_mea.argtypes = [vp, i, i, i, i, i, i, C.POINTER(C.c_double)]
         L.orc_collide.restype = l
         L.orc_collide.argtypes = [vp]
         L.orc_stream.argtypes = [vp]
@@ -215,6 +216,13 @@ class Lattice:
     def interior(self, a: np.ndarray) -> np.ndarray:
         return a[1:-1, 1:-1, 1:-1] if self.nz > 1 or a.shape[0] > 1 else a
 
+    def mea(self, box) -> np.ndarray:
+        """Momentum-exchange sums (x, y, z) over the fluid cells of box =
+        (xmin, xmax, ymin, ymax, zmin, zmax), ghost-inclusive indices."""
+        out = np.zeros(3)
+        self.L.orc_mea(self.h, *[int(b) for b in box], _dp(out))
+        return out
+
     def ibm_step(self, mk: Markers, op: IbmOpts, center) -> np.ndarray:
         c = np.ascontiguousarray(center, dtype=np.float64)
         out = np.zeros(7)
@@ -266,6 +274,34 @@ def channel(nx: int, ny: int, nz: int, tau: float, u_in: float = 0.05, outlet: i
     lat.ux[fluidlike] = u_in
     lat.init()
     return lat
+
+
+def sphere_bb(nx: int, ny: int, nz: int, tau: float, diameter: float, u_max: float = 0.1):
+    """The reference's staircase sphere (main_setup_Sphere / Generate_Sphere,
+    lbm.cpp:1759-1822): cells whose centre (i - 1/2, j - 1/2, k - 1/2) lies
+    within D/2 of (Nx/5, Ny/2, Nz/2) are TYPE_S at rest; ghost plane x = 0
+    TYPE_IN, every other ghost plane TYPE_OUT; fluid-like cells start at
+    rho = 1, u = (u_max, 0, 0).  Returns (lattice, MEA box)."""
+    lat = Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    c = (nx / 5.0, ny / 2.0, nz / 2.0)
+    k, j, i = np.meshgrid(np.arange(nz + 2), np.arange(ny + 2), np.arange(nx + 2), indexing="ij")
+    r = np.sqrt((c[0] - (i - 0.5)) ** 2 + (c[1] - (j - 0.5)) ** 2 + (c[2] - (k - 0.5)) ** 2)
+    inside = (r <= diameter / 2.0) & (i >= 1) & (i <= nx) & (j >= 1) & (j <= ny) & (k <= nz)
+    t[inside] = TYPE_S
+    t[:, :, 0] = TYPE_IN
+    t[:, :, -1] = TYPE_OUT
+    t[:, 0, :] = TYPE_OUT
+    t[:, -1, :] = TYPE_OUT
+    t[0, :, :] = TYPE_OUT
+    t[-1, :, :] = TYPE_OUT
+    lat.rho[:] = 1.0
+    lat.ux[t != TYPE_S] = u_max
+    lat.init()
+    box = (int(c[0] - diameter), int(c[0] + diameter), int(c[1] - diameter), int(c[1] + diameter),
+           int(c[2] - diameter), int(c[2] + diameter))
+    return lat, box
 
 
 def fibonacci_sphere(n: int, diameter: float, center) -> Markers:

@@ -9,6 +9,7 @@
 # usage: oracle/build_ref.sh [variant ...]
 #   cavity:N[:TAU]            D3Q19 cavity, N^3 interior
 #   cylinder:NX:NY:D:NODES:M  D2Q9 implicit IBM cylinder
+#   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${REF:-/root/reference}
@@ -18,7 +19,7 @@ if [ ! -f "$REF/lbm.cpp" ]; then
     exit 0
 fi
 mkdir -p "$OUT"
-[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5
+[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05
 CXX=${CXX:-g++}
 FLAGS="-O2 -fopenmp -ffp-contract=off -w -include $HERE/ref_config.h -I$HERE/shim -I$REF"
 pids=""
@@ -36,6 +37,13 @@ for v in "$@"; do
         nodes=$(echo "$v" | cut -d: -f5); mm=$(echo "$v" | cut -d: -f6)
         exe="$OUT/ref_cylinder_${nx}_${ny}_${d}_${nodes}_${mm}"
         $CXX $FLAGS -DREF_CYLINDER -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    sphere)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)
+        d=$(echo "$v" | cut -d: -f5); re=$(echo "$v" | cut -d: -f6); u=$(echo "$v" | cut -d: -f7)
+        exe="$OUT/ref_sphere_${nx}_${ny}_${nz}_${d}_${re}_${u}"
+        $CXX $FLAGS -DREF_SPHERE -DREF_NX=$nx -DREF_NY=$ny -DREF_NZ=$nz -DREF_D=$d -DREF_RE=$re -DREF_U=$u \
             -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     *) echo "unknown variant $v"; exit 2 ;;

@@ -400,6 +400,34 @@ long orc_step_plain(orc *o, int nsteps) {
     return bad;
 }
 
+/* MEA_CD / MEA_CL, lbm.cpp:3085-3163 (momentum exchange on staircase solid
+ * cells): over the fluid cells of the box [xmin,xmax] x [ymin,ymax] x
+ * [zmin,zmax] (ghost-inclusive reference indices), every link l whose cell
+ * i - c_l is TYPE_S adds (f*_l + f_opp(l)) c_l.  out = (sum x, sum y, sum z);
+ * the reference's drag is -out[0] and its lift +out[1] (times dx^3/dt, then
+ * divided by 1/2 rho0 u^2 times the area). */
+void orc_mea(const orc *o, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax, double out[3]) {
+    long n = o->ncell;
+    double sx = 0, sy = 0, sz = 0;
+    for (int i = xmin; i <= xmax; ++i)
+        for (int j = ymin; j <= ymax; ++j)
+            for (int k = zmin; k <= zmax; ++k) {
+                long c = IDX(o, i, j, k);
+                if (o->type[c] != ORC_F) continue;
+                for (int l = 0; l < o->q; ++l) {
+                    long nb = IDX(o, i - o->cx[l], j - o->cy[l], k - o->cz[l]);
+                    if (o->type[nb] != ORC_S) continue;
+                    const double t = o->fs[l * n + c] + o->f[o->opp[l] * n + c];
+                    sx += t * o->cx[l];
+                    sy += t * o->cy[l];
+                    sz += t * o->cz[l];
+                }
+            }
+    out[0] = sx;
+    out[1] = sy;
+    out[2] = sz;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Immersed boundary                                                         */
 /* ------------------------------------------------------------------------ */

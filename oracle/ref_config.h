@@ -11,6 +11,10 @@
  *                 3D code paths; the harness sets the geometry itself.
  *   REF_CYLINDER  D2Q9 implicit IBM cylinder (the shipped default case),
  *                 shrunk to test size.
+ *   REF_SPHERE    D3Q19 staircase sphere with momentum-exchange Cl/Cd (the
+ *                 reference's Sphere_BB case), shrunk to test size; REF_D,
+ *                 REF_RE and REF_U set the diameter, Reynolds number and
+ *                 inflow velocity.
  * Sizes come from REF_NX/REF_NY/REF_NZ/REF_TAU (and REF_D, REF_NODES,
  * REF_MMAX for the cylinder).
  */
@@ -80,6 +84,23 @@ static int m_max = REF_MMAX;
 static const double Vsolid = PI * D * D * 0.25;
 #define T_OUT 30000
 #define Nt 10
+#elif defined REF_SPHERE
+#define Sphere_BB
+#define MOMENTUM_EXCHANGE_ALGORITHM
+#define D3Q19
+#define Re REF_RE
+static const double D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = REF_NZ;
+static const double u_max = REF_U;
+static double center_x = dx * (Nx / 5.0);
+static double center_y = dy * (Ny / 2.0);
+static double center_z = dz * (Nz / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+#define T_OUT 30000
+#define Nt 10
 #else
-#error "define REF_CAVITY or REF_CYLINDER"
+#error "define REF_CAVITY, REF_CYLINDER or REF_SPHERE"
 #endif

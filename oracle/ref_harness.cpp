@@ -7,8 +7,9 @@
 //   - runs the reference's own Init / Collision / Streaming / MacroProp and
 //     IBLBM in the order of main.cpp:195-221,
 //   - times only the step loop (wall clock), and
-//   - dumps rho, u (and F, Cl, Cd for the IBM case) as raw doubles,
-//     x fastest, ghost layers included.
+//   - dumps rho, u (and F, Cl, Cd for the IBM case; Cl, Cd of the
+//     momentum exchange after every step for the staircase sphere) as raw
+//     doubles, x fastest, ghost layers included.
 #include "LBM.h"
 
 #include <omp.h>
@@ -107,6 +108,29 @@ int main(int argc, char **argv) {
     fclose(fp);
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cylinder\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
+           Nx, steps, t1 - t0, mlups, omp_get_max_threads());
+#elif defined REF_SPHERE
+    LBM lb = main_setup_Sphere();
+    std::vector<double> CL, CD;
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int step = 1; step <= steps; step++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+        // the calls of main.cpp:369-372, every step
+        CL.push_back(MEA_CL(lb, center_x - D, center_x + D, center_y - D, center_y + D, center_z - D, center_z + D));
+        CD.push_back(MEA_CD(lb, center_x - D, center_x + D, center_y - D, center_y + D, center_z - D, center_z + D));
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+    fwrite(CL.data(), sizeof(double), CL.size(), fp);
+    fwrite(CD.data(), sizeof(double), CD.size(), fp);
+    fclose(fp);
+    double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
+    printf("{\"case\": \"sphere_bb\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
 #endif
     return 0;

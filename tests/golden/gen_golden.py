@@ -12,6 +12,11 @@ outputs are stored as small .npz fixtures:
   cylinder80x40_D10_n40_m5_100.npz  D2Q9 implicit-IBM cylinder (the shipped
                                     default case shrunk): rho, ux, uy, Fx, Fy
                                     on the k = 1 layer, Cl and Cd per step
+  sphere_bb48x24x24_D8_Re20_100.npz  D3Q19 staircase sphere (the Sphere_BB
+                                    case shrunk, u = 0.05): mid planes
+                                    k = 12 and j = 12 of rho, u, interior
+                                    sums and maxima, momentum-exchange Cl
+                                    and Cd after every step
 
 Run from the repository root:  python tests/golden/gen_golden.py
 (needs the reference tree; the 64^3 case takes a few minutes on 8 cores;
@@ -44,7 +49,7 @@ def main() -> None:
     ap.add_argument("--cav64-dump", default=None)
     ap.add_argument("--skip-cav64", action="store_true")
     a = ap.parse_args()
-    oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5")
+    oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05")
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps
@@ -73,6 +78,16 @@ def main() -> None:
     np.savez_compressed(os.path.join(OUT, "cylinder80x40_D10_n40_m5_100.npz"), rho=fl[0], ux=fl[1], uy=fl[2],
                         Fx=fl[4], Fy=fl[5], cl=r["cl"], cd=r["cd"], markers=r["markers"], nx=80, ny=40, D=10.0,
                         nodes=40, m_max=5, steps=steps)
+    # staircase sphere with momentum exchange, 100 steps
+    p = os.path.join(tmp, "sph.bin")
+    steps = 100
+    run("ref_sphere_48_24_24_8_20_0.05", [str(steps), p])
+    r = oracle.read_ref_dump(p, 50, 26, 26, 4, steps, 0)
+    f = r["fields"][:, 1:-1, 1:-1, 1:-1]
+    np.savez_compressed(os.path.join(OUT, "sphere_bb48x24x24_D8_Re20_100.npz"), zmid=f[:, 12, :, :],
+                        ymid=f[:, :, 12, :], sums=f.reshape(4, -1).sum(axis=1),
+                        absmax=np.abs(f.reshape(4, -1)).max(axis=1), cl=r["cl"], cd=r["cd"], nx=48, ny=24, nz=24,
+                        D=8.0, Re=20.0, u=0.05, steps=steps)
     print("golden fixtures written to", OUT)
 
 

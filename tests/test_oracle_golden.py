@@ -92,3 +92,28 @@ def test_reference_literal_build_agrees_live(orc, tmp_path):
     lat.step_plain(37)
     for w, a in enumerate((lat.rho, lat.ux, lat.uy, lat.uz)):
         assert np.abs(lat.interior(a) - r[w][1:-1, 1:-1, 1:-1]).max() < 1e-13
+
+
+def test_staircase_sphere_mea_matches_reference(orc):
+    """The reference's Sphere_BB case (staircase sphere, bounce-back on
+    interior solid cells, TYPE_IN / TYPE_OUT ghosts) and its momentum-exchange
+    Cl / Cd (MEA_CL / MEA_CD, lbm.cpp:3085-3163) after every step."""
+    g = np.load(os.path.join(GOLDEN, "sphere_bb48x24x24_D8_Re20_100.npz"))
+    nx, ny, nz, D, Re, u = int(g["nx"]), int(g["ny"]), int(g["nz"]), float(g["D"]), float(g["Re"]), float(g["u"])
+    tau = 0.5 + (u * D / Re) / (1.0 / 3.0)
+    lat, box = orc.sphere_bb(nx, ny, nz, tau, D, u)
+    area = 0.5 * u * u * D * D * 3.14159265 / 4.0
+    cl, cd = [], []
+    for _ in range(int(g["steps"])):
+        lat.collide()
+        lat.stream()
+        lat.macro()
+        m = lat.mea(box)
+        cl.append(m[1] / area)
+        cd.append(-m[0] / area)
+    assert np.abs(np.array(cd) - g["cd"]).max() < 1e-12 * np.abs(g["cd"]).max()
+    assert np.abs(np.array(cl) - g["cl"]).max() < 1e-12 * np.abs(g["cd"]).max()
+    f = np.stack([lat.interior(getattr(lat, c)) for c in ("rho", "ux", "uy", "uz")])
+    assert np.abs(f[:, 12] - g["zmid"]).max() < 1e-12
+    assert np.abs(f[:, :, 12] - g["ymid"]).max() < 1e-12
+    assert np.allclose(f.reshape(4, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
