@@ -124,9 +124,11 @@ typedef struct lbm_handle lbm_handle;
 /* Derive a configuration from the reference's per-cell description
  * (fluid[i][j][k].type and the ghost velocities/densities/temperatures),
  * arrays of (nx+2)(ny+2)(nz+2) entries, x fastest; u/rho/T may be NULL.
- * Fails with LBM_ERR_UNSUPPORTED if solids lie inside the domain or a face
- * is not uniform.  Periodic axes (TYPE_F ghost layers) are mapped to an
- * interior of N+2 cells, as the reference wraps over N+2 (lbm.cpp:187-189). */
+ * Interior TYPE_S cells at rest are accepted: pass their mask to
+ * lbmgpu_set_solids.  Fails with LBM_ERR_UNSUPPORTED for other non-fluid
+ * interior cells, moving interior solids, or a face that is not uniform.
+ * Periodic axes (TYPE_F ghost layers) are mapped to an interior of N+2
+ * cells, as the reference wraps over N+2 (lbm.cpp:187-189). */
 lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const uint8_t *types, const double *rho,
                                     const double *ux, const double *uy, const double *uz, const double *T,
                                     lbm_config *out);
@@ -176,6 +178,21 @@ lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host);
 /* IBM force history, oldest first: per step {Fx, Fy, Fz, Tx, Ty, Tz, heat,
  * step}, where F = sum over forcing iterations of -F_m ds_m (the reference's
  * Drag/Lift accumulators, lbm.cpp:1322-1323).  *n_out = entries written. */
+/* Interior solid cells at rest -- staircase bodies such as the reference's
+ * Generate_Sphere (lbm.cpp:1759-1787) or its cylinders: mask has nx*ny*nz
+ * entries (x fastest), non-zero = TYPE_S.  Their links bounce back (halfway,
+ * lbm.cpp:252-274) inside the fused step and the momentum exchange on them is
+ * recorded every step.  Call after lbmgpu_create and before lbmgpu_init; a
+ * fixed IBM body on the same handle then keeps the serial order. */
+lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask);
+
+/* Momentum exchange on the solid cells, MEA_CD / MEA_CL (lbm.cpp:3085-3163)
+ * summed over every fluid cell next to a solid: rows of 4 doubles
+ * (Fx, Fy, Fz, step) for reference steps 1 .. n (the last max_steps of
+ * them), F = -sum (f*_l + f_opp(l)) c_l in lattice units.  The reference's
+ * coefficients are Cd = Fx / (0.5 rho0 U^2 A), Cl = -Fy / (0.5 rho0 U^2 A). */
+lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 /* Rigid body: {xc[3], v[3], omega[3]}. */
 lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]);

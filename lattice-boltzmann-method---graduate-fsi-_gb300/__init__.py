@@ -38,6 +38,7 @@ ABI_SYMBOLS = [
     "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
     "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_batch_step_noalloc", "lbmgpu_step_phases",
+    "lbmgpu_set_solids", "lbmgpu_get_solid_forces",
 ]
 
 
@@ -136,6 +137,8 @@ def load(path: str | None = None):
     L.lbmgpu_batch_status.argtypes = [vp, C.POINTER(C.c_uint32)]
     L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.lbmgpu_step_phases.argtypes = [vp, i, dp]
+    L.lbmgpu_set_solids.argtypes = [vp, C.POINTER(C.c_uint8)]
+    L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
     L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
     for nm in ABI_SYMBOLS:
@@ -267,6 +270,20 @@ class Solver:
         tot, fused = C.c_double(), C.c_double()
         check(self.L.lbmgpu_step_profiled(self.h, int(n), C.byref(tot), C.byref(fused)))
         return tot.value, fused.value
+
+    def set_solids(self, mask: np.ndarray):
+        """Interior solid cells at rest: mask of shape (nz, ny, nx), non-zero = solid."""
+        m = np.ascontiguousarray(np.asarray(mask) != 0, dtype=np.uint8).reshape(-1)
+        if m.size != self.ncell:
+            raise ValueError("mask must have nx*ny*nz entries")
+        check(self.L.lbmgpu_set_solids(self.h, m.ctypes.data_as(C.POINTER(C.c_uint8))))
+
+    def solid_forces(self, max_steps: int = 1 << 16) -> np.ndarray:
+        """Rows (Fx, Fy, Fz, step) of the momentum exchange on the solid cells."""
+        out = np.zeros((max_steps, 4))
+        n = C.c_int()
+        check(self.L.lbmgpu_get_solid_forces(self.h, _dp(out), max_steps, C.byref(n)))
+        return out[: n.value]
 
     def step_phases(self, n: int) -> dict:
         ph = np.zeros(4)

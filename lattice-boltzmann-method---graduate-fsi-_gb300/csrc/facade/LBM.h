@@ -44,6 +44,9 @@
 #endif
 
 const int ndim = 3;
+// truncated PI of the reference (LBM.h:74)
+static const double PI = 3.14159265;
+
 const int npop = 19;
 const int cx[npop] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0};
 const int cy[npop] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1};
@@ -131,3 +134,7 @@ double Calc_AverageDensity(LBM &lb, std::vector<MARKER> &marker, int xmin, int x
                            int zmax);
 void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
            std::vector<double> &Cd, double V_CM[], double t);
+// Momentum-exchange lift / drag of the interior solid cells after the latest
+// step (LBM.h:790-792); normalised with g_lbm_options u_max and ref_area.
+double MEA_CL(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax);
+double MEA_CD(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax);

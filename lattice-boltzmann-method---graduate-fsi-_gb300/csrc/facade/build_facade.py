@@ -10,7 +10,7 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
-DRIVERS = ["dropin_cavity", "dropin_sphere"]
+DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb"]
 
 
 def build(force: bool = False) -> list:

@@ -12,6 +12,7 @@ struct lbm_device_state {
     bool collision_pending = false;
     bool mirror_stale = false;
     bool markers_set = false;
+    bool solids = false;      // interior TYPE_S cells on the device
     long long steps = 0;
     std::vector<double> *cl = nullptr, *cd = nullptr;
     int off[3] = {1, 1, 1};  // device cell = reference index - off (0 on periodic axes)
@@ -136,6 +137,25 @@ void LBM::Init() {
     dev->h = nullptr;
     check("create", lbmgpu_create(&cfg, &dev->h));
     const size_t nd = (size_t)cfg.nx * cfg.ny * cfg.nz;
+    // interior TYPE_S cells (Generate_Sphere and the like): solid mask
+    {
+        std::vector<uint8_t> mask(nd, 0);
+        bool any = false;
+        for (int z = 0; z < cfg.nz; z++)
+            for (int y = 0; y < cfg.ny; y++)
+                for (int x = 0; x < cfg.nx; x++) {
+                    const int i = x + dev->off[0], j = y + dev->off[1], k = z + dev->off[2];
+                    const bool ghost = (dev->off[0] && (i == 0 || i == Nx + 1)) ||
+                                       (dev->off[1] && (j == 0 || j == Ny + 1)) ||
+                                       (dev->off[2] && (k == 0 || k == Nz + 1));
+                    if (!ghost && fluid[i][j][k].type == TYPE_S) {
+                        mask[(size_t)x + (size_t)cfg.nx * ((size_t)y + (size_t)cfg.ny * z)] = 1;
+                        any = true;
+                    }
+                }
+        if (any) check("set_solids", lbmgpu_set_solids(dev->h, mask.data()));
+        dev->solids = any;
+    }
     std::vector<double> drho(nd), dux(nd), duy(nd), duz(nd), dT(nd);
     for (int z = 0; z < cfg.nz; z++)
         for (int y = 0; y < cfg.ny; y++)
@@ -286,3 +306,20 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
     check("set_markers", lbmgpu_set_markers(d.h, &ic, xyz.data(), dsv.data(), nullptr));
     d.markers_set = true;
 }
+
+// Momentum-exchange coefficients of the solid cells after the latest step
+// (MEA_CL / MEA_CD, lbm.cpp:3085-3163).  The device sums over every fluid
+// cell next to an interior solid; the box arguments of the reference, which
+// only keep the domain walls out of the sum, are not needed.
+static double mea_component(LBM &lb, int comp) {
+    lbm_handle *h = lb.handle();
+    if (!h) return 0.0;
+    std::vector<double> rows(4);
+    int n = 0;
+    if (lbmgpu_get_solid_forces(h, rows.data(), 1, &n) != LBM_OK || n < 1) return 0.0;
+    const lbm_options &o = g_lbm_options;
+    return rows[comp] / (0.5 * o.rho0 * o.u_max * o.u_max * o.ref_area);
+}
+
+double MEA_CL(LBM &lb, int, int, int, int, int, int) { return -mea_component(lb, 1); }
+double MEA_CD(LBM &lb, int, int, int, int, int, int) { return mea_component(lb, 0); }

@@ -7,6 +7,7 @@
 #include <cstdio>
 #include <cstring>
 #include <string>
+#include <cstddef>
 #include <vector>
 
 #include "../../include/lbmgpu.h"
@@ -58,6 +59,14 @@ struct lbm_handle {
     int gsteps = 16;
     int tx = 128, ty = 2;
     StagedPlan stp;                       // staged (bulk-copy) step kernel
+    // interior solid cells and their momentum exchange
+    bool solids = false;
+    uint32_t *solid_d = nullptr, *near_d = nullptr;
+    float *mea_part = nullptr;
+    int *mea_blocks = nullptr;
+    int n_mea_blocks = 0;
+    double *mea_ring = nullptr;
+    long long mea_cap = 1 << 16;
     int tile_x = 1, tile_y = 1;           // tile of the staged kernel (near-box rounding)
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -200,12 +209,17 @@ extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double ta
     memset(&c, 0, sizeof(c));
     c.tau = tau;
     c.rho0 = 1.0;
-    // interior must be fluid
+    // interior: fluid, or solid at rest (lbmgpu_set_solids)
     for (int k = 1; k <= nz; k++)
         for (int j = 1; j <= ny; j++)
-            for (int i = 1; i <= nx; i++)
-                if (types[at(i, j, k)] != 0)
+            for (int i = 1; i <= nx; i++) {
+                const size_t c = at(i, j, k);
+                if (types[c] == 0) continue;
+                if (types[c] != 1)
                     return fail(LBM_ERR_UNSUPPORTED, "config_from_types: non-fluid cell inside the domain");
+                if ((ux && ux[c] != 0) || (uy && uy[c] != 0) || (uz && uz[c] != 0))
+                    return fail(LBM_ERR_UNSUPPORTED, "config_from_types: moving solid cell inside the domain");
+            }
     // face planes (without edges): uniform type and state
     const int lim[3] = {nx, ny, nz};
     int periodic_axis[3] = {0, 0, 0};
@@ -280,6 +294,9 @@ static void free_handle(lbm_handle *h) {
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
     if (h->ev_near) cudaEventDestroy(h->ev_near);
+    for (void *p : {(void *)h->solid_d, (void *)h->near_d, (void *)h->mea_part, (void *)h->mea_blocks,
+                    (void *)h->mea_ring})
+        if (p) cudaFree(p);
     if (h->ev_ibm) cudaEventDestroy(h->ev_ibm);
     if (h->ev_acc) cudaEventDestroy(h->ev_acc);
     if (h->ev_fin) cudaEventDestroy(h->ev_fin);
@@ -428,7 +445,16 @@ extern "C" lbm_status lbmgpu_destroy(lbm_handle *h) {
 static lbm_status do_init(lbm_handle *h, const float *dfields) {
     float init[5] = {(float)h->cfg.rho0, (float)h->cfg.u0[0], (float)h->cfg.u0[1], (float)h->cfg.u0[2],
                      (float)h->cfg.T_init};
-    CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->P.N, h->P.S, dfields, init, h->cfg.thermal != 0, h->s));
+    // with solid cells both buffers start alike: a solid cell is never
+    // rewritten and keeps its initial populations in A and B
+    CUDA_TRY(launch_init(h->cfg.storage, h->f[0], h->g[0], h->solids ? h->f[1] : nullptr,
+                         h->solids ? h->g[1] : nullptr, h->P.N, h->P.S, dfields, init, h->cfg.thermal != 0, h->s));
+    if (h->solids) {
+        // the first momentum-exchange record is that of reference step 1
+        const long long one = 1;
+        CUDA_TRY(cudaMemcpyAsync((char *)h->ds + offsetof(DevState, mea_step), &one, sizeof(one),
+                                 cudaMemcpyHostToDevice, h->s));
+    }
     h->cur = 0;
     h->steps = 0;
     h->inited = true;
@@ -638,10 +664,14 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
 static cudaError_t enqueue_step(lbm_handle *h, int gather, const cudaEvent_t *ev) {
     LaunchArgs a = make_args(h, gather);
     cudaError_t e;
-    const bool overlap = h->ibm && gather && !h->icfg.free_body && h->s2 && h->cfg.ibm_overlap >= 0;
+    const bool overlap = h->ibm && gather && !h->icfg.free_body && h->s2 && h->cfg.ibm_overlap >= 0 && !h->solids;
     if (ev) cudaEventRecord(ev[0], h->s);
     if (!overlap) {
         if ((e = launch_step(h->cfg.storage, a)) != cudaSuccess) return e;
+        if (h->solids && gather &&
+            (e = launch_mea_finish(h->mea_part, h->mea_blocks, h->n_mea_blocks, h->mea_ring, h->mea_cap, h->ds, 1,
+                                   h->s)) != cudaSuccess)
+            return e;
         if (ev) {
             cudaEventRecord(ev[1], h->s);
             cudaEventRecord(ev[2], h->s);
@@ -845,6 +875,104 @@ extern "C" lbm_status lbmgpu_download(lbm_handle *h, int field, double *host) {
     lbm_status s = lbmgpu_download_f32(h, field, tmp.data());
     if (s != LBM_OK) return s;
     for (size_t i = 0; i < tmp.size(); i++) host[i] = tmp[i];
+    return LBM_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Interior solid cells (staircase bodies) and their momentum exchange
+// ---------------------------------------------------------------------------
+extern "C" lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask) {
+    if (!h || !mask) return fail(LBM_ERR_INVALID, "set_solids: null argument");
+    if (h->inited) return fail(LBM_ERR_STATE, "set_solids: call before lbmgpu_init");
+    if (h->solids) return fail(LBM_ERR_STATE, "set_solids: solids already set");
+    const int nx = h->P.nx, ny = h->P.ny, nz = h->P.nz;
+    const long long N = h->P.N, words = (N + 31) / 32;
+    std::vector<uint32_t> sol((size_t)words, 0u), nea((size_t)words, 0u);
+    long long nsolid = 0;
+    for (long long c = 0; c < N; c++)
+        if (mask[c]) {
+            sol[(size_t)(c >> 5)] |= 1u << (c & 31);
+            nsolid++;
+        }
+    if (nsolid == 0) return fail(LBM_ERR_INVALID, "set_solids: no solid cell");
+    // near: a solid, or a cell one of whose 18 neighbours is one
+    const int per = h->P.periodic;
+    const int gx = (nx + h->tx - 1) / h->tx, gy = (ny + h->ty - 1) / h->ty;
+    std::vector<char> blk((size_t)gx * gy * nz, 0);
+    for (int z = 0; z < nz; z++)
+        for (int y = 0; y < ny; y++)
+            for (int x = 0; x < nx; x++) {
+                const long long c = x + (long long)nx * (y + (long long)ny * z);
+                bool nr = mask[c] != 0;
+                for (int l = 1; l < Q && !nr; l++) {
+                    int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+                    if (per & 1) sx = (sx + nx) % nx;
+                    if (per & 2) sy = (sy + ny) % ny;
+                    if (per & 4) sz = (sz + nz) % nz;
+                    if (sx < 0 || sy < 0 || sz < 0 || sx >= nx || sy >= ny || sz >= nz) continue;
+                    nr = mask[sx + (long long)nx * (sy + (long long)ny * sz)] != 0;
+                }
+                if (nr) {
+                    nea[(size_t)(c >> 5)] |= 1u << (c & 31);
+                    blk[(size_t)(x / h->tx) + (size_t)gx * ((size_t)(y / h->ty) + (size_t)gy * z)] = 1;
+                }
+            }
+    std::vector<int> list;
+    for (size_t b = 0; b < blk.size(); b++)
+        if (blk[b]) list.push_back((int)b);
+    CUDA_TRY(dalloc(h, &h->solid_d, (size_t)words * 4));
+    CUDA_TRY(dalloc(h, &h->near_d, (size_t)words * 4));
+    CUDA_TRY(dalloc(h, &h->mea_part, blk.size() * 3 * sizeof(float)));
+    CUDA_TRY(dalloc(h, &h->mea_blocks, list.size() * sizeof(int)));
+    CUDA_TRY(dalloc(h, &h->mea_ring, (size_t)h->mea_cap * 4 * sizeof(double)));
+    CUDA_TRY(cudaMemcpyAsync(h->solid_d, sol.data(), (size_t)words * 4, cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemcpyAsync(h->near_d, nea.data(), (size_t)words * 4, cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemcpyAsync(h->mea_blocks, list.data(), list.size() * sizeof(int), cudaMemcpyHostToDevice, h->s));
+    CUDA_TRY(cudaMemsetAsync(h->mea_part, 0, blk.size() * 3 * sizeof(float), h->s));
+    CUDA_TRY(cudaMemsetAsync(h->mea_ring, 0, (size_t)h->mea_cap * 4 * sizeof(double), h->s));
+    CUDA_TRY(cudaStreamSynchronize(h->s));
+    h->n_mea_blocks = (int)list.size();
+    h->P.solid = h->solid_d;
+    h->P.nearw = h->near_d;
+    h->P.mea = h->mea_part;
+    h->solids = true;
+    h->stp.enabled = 0;  // the staged kernel has no solid cells
+    for (int i = 0; i < 2; i++)
+        if (h->gexec[i]) {
+            cudaGraphExecDestroy(h->gexec[i]);
+            h->gexec[i] = nullptr;
+        }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
+    if (!h || !out || max_steps < 0) return fail(LBM_ERR_INVALID, "get_solid_forces: bad argument");
+    if (!h->solids) return fail(LBM_ERR_STATE, "get_solid_forces: no solid cells set");
+    if (!h->inited) return fail(LBM_ERR_STATE, "get_solid_forces: call lbmgpu_init first");
+    long long n = 0;
+    if (h->steps >= 1) {
+        // the latest step's exchange needs its streamed populations: one
+        // gather-only pass, recorded without advancing (the next step
+        // recomputes the same record)
+        LaunchArgs a = make_args(h, 1);
+        a.export_only = 1;
+        CUDA_TRY(launch_step(h->cfg.storage, a));
+        CUDA_TRY(launch_mea_finish(h->mea_part, h->mea_blocks, h->n_mea_blocks, h->mea_ring, h->mea_cap, h->ds, 0,
+                                   h->s));
+        // records of reference steps 1 .. steps
+        n = std::min<long long>(std::min<long long>(h->steps, h->mea_cap), max_steps);
+        const long long last = h->steps;
+        long long first = (last - n + 1) % h->mea_cap;
+        long long n1 = std::min(n, h->mea_cap - first);
+        if (n1 > 0)
+            CUDA_TRY(cudaMemcpyAsync(out, h->mea_ring + first * 4, (size_t)n1 * 4 * sizeof(double),
+                                     cudaMemcpyDeviceToHost, h->s));
+        if (n > n1)
+            CUDA_TRY(cudaMemcpyAsync(out + n1 * 4, h->mea_ring, (size_t)(n - n1) * 4 * sizeof(double),
+                                     cudaMemcpyDeviceToHost, h->s));
+        CUDA_TRY(cudaStreamSynchronize(h->s));
+    }
+    if (n_out) *n_out = (int)n;
     return LBM_OK;
 }
 

@@ -62,6 +62,11 @@ struct St<__nv_bfloat16> {
     static __device__ __forceinline__ void st(__nv_bfloat16 *p, float v) { *p = __float2bfloat16_rn(v); }
 };
 
+// Bit of a packed per-cell mask (32 cells per word, cell index order).
+__device__ __forceinline__ bool mask_bit(const uint32_t *__restrict__ m, long long cell) {
+    return (__ldg(m + (cell >> 5)) >> (cell & 31)) & 1u;
+}
+
 // Boundary class of a cell: which ghost faces it touches.  Bit 2a is the low
 // face of axis a, bit 2a+1 the high face; periodic axes never set bits.
 struct ClassEntry {
@@ -97,6 +102,10 @@ struct StepParams {
     int bsx, bsy, bsz;     // band extent
     long long nb;          // bsx * bsy * bsz
     int nlo[3], nhi[3];    // near box of a fixed body: band grown by one cell, rounded out to tiles
+    // interior solid cells (staircase bodies), or null
+    const uint32_t *solid;  // bit per interior cell: stationary solid (bounce-back on its links)
+    const uint32_t *nearw;  // bit per interior cell: a solid, or a neighbour of one
+    float *mea;             // per-block momentum-exchange partial sums [blocks][3], or null
     ClassEntry cls[64];
 };
 
@@ -104,6 +113,7 @@ struct StepParams {
 // origin and the FP64 rigid body.
 struct DevState {
     uint32_t status;
+    long long mea_step;     // reference step of the next momentum-exchange record
     int band_o[3];          // band origin (interior cell coordinates)
     long long step;         // steps completed on the device
     long long hist_cap;

@@ -284,6 +284,41 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
     }
 }
 
+// One block: fixed-order FP64 sum of the per-block momentum-exchange
+// partials of the listed blocks; record (Fx, Fy, Fz, step) with F the force
+// on the solid cells (minus the exchange sums), then advance the step.
+__global__ void __launch_bounds__(256) k_mea_finish(const float *__restrict__ part, const int *__restrict__ blocks,
+                                                    int nblocks, double *__restrict__ ring, long long ring_cap,
+                                                    DevState *__restrict__ ds, int advance) {
+    __shared__ double red[3][256];
+    const int t = threadIdx.x;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = t; i < nblocks; i += 256) {
+        const long long b = blocks[i];
+        for (int k = 0; k < 3; k++) s[k] += (double)part[3 * b + k];
+    }
+    for (int k = 0; k < 3; k++) red[k][t] = s[k];
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+        if (t < w)
+            for (int k = 0; k < 3; k++) red[k][t] += red[k][t + w];
+        __syncthreads();
+    }
+    if (t == 0) {
+        const long long step = ds->mea_step;
+        double *r = ring + (step % ring_cap) * 4;
+        for (int k = 0; k < 3; k++) r[k] = -red[k][0];
+        r[3] = (double)step;
+        if (advance) ds->mea_step = step + 1;
+    }
+}
+
+cudaError_t launch_mea_finish(const float *part, const int *blocks, int nblocks, double *ring, long long ring_cap,
+                              DevState *ds, int advance, cudaStream_t s) {
+    k_mea_finish<<<1, 256, 0, s>>>(part, blocks, nblocks, ring, ring_cap, ds, advance);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_ibm_interp(const IbmArgs &a, int first) {
     const int threads = kIbmThreads;
     const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;

@@ -46,8 +46,15 @@ cudaError_t plan_staged(int storage, bool thermal, const StepParams &P, void *co
                         StagedPlan &sp);
 cudaError_t launch_staged(int storage, const LaunchArgs &a);
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign);
-cudaError_t launch_init(int storage, void *A, void *GA, long long N, long long S, const float *fields,
-                        const float init[5], bool thermal, cudaStream_t s);
+// Initial populations (equilibrium of the given or uniform fields) into A,
+// GA and, when non-null, also into A2 / GA2.
+cudaError_t launch_init(int storage, void *A, void *GA, void *A2, void *GA2, long long N, long long S,
+                        const float *fields, const float init[5], bool thermal, cudaStream_t s);
+// Momentum-exchange record of one step: fixed-order FP64 sum of the listed
+// per-block partials into the ring (Fx, Fy, Fz, step) -- the force on the
+// solid cells, minus the sums.
+cudaError_t launch_mea_finish(const float *part, const int *blocks, int nblocks, double *ring, long long ring_cap,
+                              DevState *ds, int advance, cudaStream_t s);
 
 // Immersed-boundary marker set on the device.
 struct MarkerDev {

@@ -123,6 +123,63 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
     for (int l = 0; l < QT; l++) g[l] = valid ? pull_heat_link<T>(G, l, x, y, z, cell, ce, P) : 0.0f;
 }
 
+// Pull of a cell near interior solid cells (staircase bodies).  A link whose
+// source cell is a solid bounces back the cell's own post-collision
+// population of the opposite link (stationary wall: no velocity term); every
+// other link follows the boundary-class rules.  A solid cell itself keeps its
+// populations (read in place: its moments for the read-back).  mea gets the
+// momentum exchange of the cell, sum over its solid links of
+// (f*_l + f_opp(l)) c_l with f* the cell's post-collision and f the pulled
+// populations (MEA_CD / MEA_CL, lbm.cpp:3085-3163; shifted storage adds
+// 2 w_l).
+template <class T, bool THERMAL>
+__device__ __forceinline__ void gather_solid(const T *__restrict__ A, const T *__restrict__ G, float f[Q],
+                                             float g[QT], int x, int y, int z, long long cell, int raw_cls,
+                                             bool valid, bool solid_cell, int gather, const StepParams &P,
+                                             float mea[3]) {
+    mea[0] = mea[1] = mea[2] = 0.0f;
+    if (!valid || !gather || solid_cell) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(A + l * P.S + cell) : 0.0f;
+        if (THERMAL) {
+#pragma unroll
+            for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(G + l * P.S + cell) : 0.0f;
+        }
+        return;
+    }
+    const ClassEntry &ce = P.cls[raw_cls & ~periodic_mask(P)];
+    uint32_t sl = 0;
+#pragma unroll
+    for (int l = 1; l < Q; l++) {
+        int sx = x - cx(l), sy = y - cy(l), sz = z - cz(l);
+        if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+        if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+        if (P.periodic & 4) sz = sz < 0 ? sz + P.nz : (sz >= P.nz ? sz - P.nz : sz);
+        const bool inside = (unsigned)sx < (unsigned)P.nx && (unsigned)sy < (unsigned)P.ny && (unsigned)sz < (unsigned)P.nz;
+        if (inside && mask_bit(P.solid, sx + (long long)P.nx * (sy + (long long)P.ny * sz))) sl |= 1u << l;
+    }
+    f[0] = St<T>::ld(A + cell);
+#pragma unroll
+    for (int l = 1; l < Q; l++)
+        f[l] = ((sl >> l) & 1u) ? St<T>::ld(A + opp(l) * P.S + cell) : pull_link<T>(A, l, x, y, z, cell, ce, P);
+    if (THERMAL) {
+        g[0] = St<T>::ld(G + cell);
+#pragma unroll
+        for (int l = 1; l < QT; l++)  // adiabatic bounce-back of the D3Q7 population on solid links
+            g[l] = ((sl >> l) & 1u) ? St<T>::ld(G + opp(l) * P.S + cell) : pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+    }
+    if (P.mea != nullptr && sl) {
+#pragma unroll
+        for (int l = 1; l < Q; l++) {
+            if (!((sl >> l) & 1u)) continue;
+            const float t = St<T>::ld(A + l * P.S + cell) + f[opp(l)] + 2.0f * wf(l);
+            mea[0] += t * cx(l);
+            mea[1] += t * cy(l);
+            mea[2] += t * cz(l);
+        }
+    }
+}
+
 // Everything after the gather of one cell except the stores: moments,
 // optional moment output, then either the band hand-off (f, g keep the
 // pre-collision populations; the unforced moments go to the band arrays) or
@@ -131,7 +188,7 @@ template <class T, bool THERMAL, bool FORCED>
 __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
                                             int gather, int export_only, const StepParams &P,
                                             DevState *__restrict__ ds, float *__restrict__ mom,
-                                            float *__restrict__ band, bool check_band) {
+                                            float *__restrict__ band, bool check_band, bool frozen = false) {
     const long long N = P.N;
     float drho, jx, jy, jz;
     moments_pairs(f, drho, jx, jy, jz);
@@ -161,7 +218,7 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
         mom[3 * N + cell] = uz;
         if (THERMAL) mom[4 * N + cell] = Tc;
     }
-    if (export_only || !valid) return false;
+    if (export_only || !valid || frozen) return false;
 
     if (check_band && P.band_on) {
         const int bx = x - ds->band_o[0], by = y - ds->band_o[1], bz = z - ds->band_o[2];
@@ -193,9 +250,9 @@ template <class T, bool THERMAL, bool FORCED>
 __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int y, int z, long long cell, bool valid,
                                             int gather, int export_only, T *__restrict__ B, T *__restrict__ GB,
                                             const StepParams &P, DevState *__restrict__ ds, float *__restrict__ mom,
-                                            float *__restrict__ band, bool check_band = true) {
+                                            float *__restrict__ band, bool check_band = true, bool frozen = false) {
     if (!update_cell<T, THERMAL, FORCED>(f, g, x, y, z, cell, valid, gather, export_only, P, ds, mom, band,
-                                         check_band))
+                                         check_band, frozen))
         return;
     if (P.idx32) {
         const unsigned c = (unsigned)cell;

@@ -71,11 +71,21 @@ def test_config_from_types_channel_and_periodic(pkg):
     assert cfg.faces[3].kind == pkg.FACE_WALL and cfg.faces[3].u[0] == 0.02
 
 
-def test_config_from_types_rejects_interior_solid(pkg):
+def test_config_from_types_interior_solids(pkg):
+    """Interior solid cells at rest are accepted (their mask goes to
+    lbmgpu_set_solids); a moving one or another interior type is refused."""
     t, rho, ux, uy, uz = _ref_geometry(6, 6, 6)
     t[:] = 1
     t[1:-1, 1:-1, 1:-1] = 0
     t[3, 3, 3] = 1
+    cfg = pkg.config_from_types(6, 6, 6, 0.8, t, rho, ux, uy, uz)
+    assert (cfg.nx, cfg.ny, cfg.nz) == (6, 6, 6)
+    ux2 = ux.copy()
+    ux2[3, 3, 3] = 0.01
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.config_from_types(6, 6, 6, 0.8, t, rho, ux2, uy, uz)
+    assert e.value.status == 7
+    t[3, 3, 3] = 3
     with pytest.raises(pkg.LbmError) as e:
         pkg.config_from_types(6, 6, 6, 0.8, t, rho, ux, uy, uz)
     assert e.value.status == 7

@@ -45,3 +45,19 @@ def test_dropin_sphere_ibm_loop(drivers, orc, tmp_path):
     q = 0.5 * 0.05 ** 2 * orc.REF_PI * D * D / 4
     ref_cd = hist[:, 0] / q
     assert np.abs(cd[:, 1] - ref_cd).max() / np.abs(ref_cd).max() < 1e-3
+
+
+def test_dropin_staircase_sphere_loop(drivers, tmp_path):
+    """The reference's Sphere_BB set-up and loop with MEA_CL / MEA_CD after
+    every step, through the facade, against the reference's own run."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "sphere_bb48x24x24_D8_Re20_100.npz"))
+    out = str(tmp_path / "mea.csv")
+    subprocess.check_call([drivers["dropin_sphere_bb"], str(int(g["nx"])), str(int(g["ny"])), str(int(g["nz"])),
+                           str(float(g["D"])), str(float(g["Re"])), str(float(g["u"])), str(int(g["steps"])), out])
+    r = np.loadtxt(out, delimiter=",", skiprows=1)
+    assert r.shape == (int(g["steps"]), 3)
+    scale = np.abs(g["cd"]).max()
+    assert np.abs(r[:, 2] - g["cd"]).max() / scale < 1e-4
+    assert np.abs(r[:, 1] - g["cl"]).max() / scale < 1e-4
