@@ -60,7 +60,9 @@ enum { LBM_FACE_WALL = 0, LBM_FACE_INLET = 1, LBM_FACE_OUTLET_EQ = 2, LBM_FACE_O
 enum { LBM_TWALL_ADIABATIC = 0, LBM_TWALL_DIRICHLET = 1 };
 
 /* Fields for lbmgpu_download*. */
-enum { LBM_FIELD_RHO = 0, LBM_FIELD_UX = 1, LBM_FIELD_UY = 2, LBM_FIELD_UZ = 3, LBM_FIELD_T = 4 };
+enum { LBM_FIELD_RHO = 0, LBM_FIELD_UX = 1, LBM_FIELD_UY = 2, LBM_FIELD_UZ = 3, LBM_FIELD_T = 4,
+       /* heat flux sum g c (lbm.cpp:778-792), thermal solves */
+       LBM_FIELD_QX = 5, LBM_FIELD_QY = 6, LBM_FIELD_QZ = 7 };
 
 /* Device status bits (lbmgpu_status). */
 enum {
@@ -194,6 +196,30 @@ lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask);
 lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+
+/* ------------------------------------------------------------------------
+ * Output in the reference's file formats.
+ * ---------------------------------------------------------------------- */
+
+/* OutputVTK (lbm.cpp:2290-2642): a RectilinearGrid .vtr of the current state
+ * -- Density, Velocity / u_ref, Force density (IBM), Temperature and Heat flux
+ * (thermal), CellType -- over the reference's cells i = 0..Nx+1,
+ * j = 0..Ny+1, k = 1..Nz, appended raw Float32 data.  Ghost cells carry their
+ * face's boundary state (a moving wall at edges).  types: the ghost-inclusive
+ * fluid[..].type array given to lbmgpu_config_from_types, for the CellType
+ * array (NULL: derived from the faces and the solid mask).  Returns once the
+ * snapshot is enqueued; a host thread writes the file while the device goes
+ * on stepping.  One file is in flight at a time: the next call (or
+ * lbmgpu_output_wait) finishes the previous one and returns its status. */
+lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types);
+lbm_status lbmgpu_output_wait(lbm_handle *h);
+
+/* OutputVTK_Marker (lbm.cpp:3033-3077): legacy ASCII POLYDATA of the markers
+ * (points, closed polyline, vertices). */
+lbm_status lbmgpu_output_markers_vtk(lbm_handle *h, const char *path);
+
+/* OutputCSV (lbm.cpp:3169-3186): "time,error" rows, time = (i+1) time_step. */
+lbm_status lbmgpu_output_csv(const char *path, const double *values, int n, double time_step);
 /* Rigid body: {xc[3], v[3], omega[3]}. */
 lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]);
 /* Marker positions [3][n]. */

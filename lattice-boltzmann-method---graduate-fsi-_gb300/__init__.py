@@ -38,7 +38,8 @@ ABI_SYMBOLS = [
     "lbmgpu_batch_create", "lbmgpu_batch_destroy", "lbmgpu_batch_init", "lbmgpu_batch_step",
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
     "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_batch_step_noalloc", "lbmgpu_step_phases",
-    "lbmgpu_set_solids", "lbmgpu_get_solid_forces",
+    "lbmgpu_set_solids", "lbmgpu_get_solid_forces", "lbmgpu_output_vtk_async", "lbmgpu_output_wait",
+    "lbmgpu_output_markers_vtk", "lbmgpu_output_csv",
 ]
 
 
@@ -138,6 +139,10 @@ def load(path: str | None = None):
     L.lbmgpu_batch_info.argtypes = [vp, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)]
     L.lbmgpu_step_phases.argtypes = [vp, i, dp]
     L.lbmgpu_set_solids.argtypes = [vp, C.POINTER(C.c_uint8)]
+    L.lbmgpu_output_vtk_async.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
+    L.lbmgpu_output_wait.argtypes = [vp]
+    L.lbmgpu_output_markers_vtk.argtypes = [vp, C.c_char_p]
+    L.lbmgpu_output_csv.argtypes = [C.c_char_p, dp, i, d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
     L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
@@ -285,6 +290,21 @@ class Solver:
         check(self.L.lbmgpu_get_solid_forces(self.h, _dp(out), max_steps, C.byref(n)))
         return out[: n.value]
 
+    def output_vtk_async(self, path: str, u_ref: float = 1.0, types=None):
+        """Write a .vtr of the current state in the reference's layout; returns
+        while a host thread writes (see output_wait)."""
+        t = None
+        if types is not None:
+            self._vtk_types = np.ascontiguousarray(types, dtype=np.uint8).ravel()
+            t = self._vtk_types.ctypes.data_as(C.POINTER(C.c_uint8))
+        check(self.L.lbmgpu_output_vtk_async(self.h, path.encode(), float(u_ref), t))
+
+    def output_wait(self):
+        check(self.L.lbmgpu_output_wait(self.h))
+
+    def output_markers_vtk(self, path: str):
+        check(self.L.lbmgpu_output_markers_vtk(self.h, path.encode()))
+
     def step_phases(self, n: int) -> dict:
         ph = np.zeros(4)
         check(self.L.lbmgpu_step_phases(self.h, int(n), _dp(ph)))
@@ -345,6 +365,30 @@ class Solver:
         v = C.c_size_t()
         check(self.L.lbmgpu_device_bytes(self.h, C.byref(v)))
         return v.value
+
+
+def output_csv(path: str, values, time_step: float):
+    """OutputCSV: "time,error" rows with time = (i+1) * time_step."""
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    check(load().lbmgpu_output_csv(path.encode(), _dp(v), int(v.size), float(time_step)))
+
+
+def read_vtr(path: str) -> dict:
+    """Parse a RectilinearGrid .vtr with appended raw data (as OutputVTK
+    writes it): header text and every DataArray by name."""
+    import re
+
+    raw = open(path, "rb").read()
+    cut = raw.index(b'<AppendedData encoding="raw">') + len(b'<AppendedData encoding="raw">')
+    head = raw[:cut].decode()
+    assert raw[cut:cut + 1] == b"_"
+    data = raw[cut + 1:]
+    out = {"header": head}
+    for m in re.finditer(r'Name="([^"]+)"(?: NumberOfComponents="(\d+)")? format="appended" offset="(\d+)"', head):
+        off = int(m.group(3))
+        n = int(np.frombuffer(data[off:off + 4], dtype=np.uint32)[0])
+        out[m.group(1)] = np.frombuffer(data[off + 4:off + 4 + n], dtype=np.float32).copy()
+    return out
 
 
 def config_from_types(nx, ny, nz, tau, types, rho=None, ux=None, uy=None, uz=None, T=None) -> Config:

@@ -138,3 +138,6 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
 // step (LBM.h:790-792); normalised with g_lbm_options u_max and ref_area.
 double MEA_CL(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax);
 double MEA_CD(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax);
+// OutputVTK (LBM.h:776-846) from the device, written while the loop goes on;
+// lbmgpu_output_wait(lb.handle()) finishes the file in flight.
+void OutputVTK_async(int &nout, LBM &lb);

@@ -323,3 +323,21 @@ static double mea_component(LBM &lb, int comp) {
 
 double MEA_CL(LBM &lb, int, int, int, int, int, int) { return -mea_component(lb, 1); }
 double MEA_CD(LBM &lb, int, int, int, int, int, int) { return mea_component(lb, 0); }
+
+// OutputVTK (lbm.cpp:2290-2642) without the host mirror: the device writes
+// ./field%06d.vtr of the current state from a host thread while the time
+// loop goes on.  Velocity is divided by g_lbm_options.u_max as the reference
+// does; the cell types come from fluid[..].type.
+void OutputVTK_async(int &nout, LBM &lb) {
+    lbm_handle *h = lb.handle();
+    if (!h) check("OutputVTK_async before Init", LBM_ERR_STATE);
+    const int NX = lb.getNx() + 2, NY = lb.getNy() + 2, NZ = lb.getNz() + 2;
+    std::vector<uint8_t> types((size_t)NX * NY * NZ);
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++)
+                types[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = (uint8_t)lb.fluid[i][j][k].type;
+    char name[64];
+    snprintf(name, sizeof(name), "./field%06d.vtr", nout);
+    check("output_vtk_async", lbmgpu_output_vtk_async(h, name, g_lbm_options.u_max, types.data()));
+}

@@ -12,6 +12,7 @@
 
 #include "../../include/lbmgpu.h"
 #include "lbm_device.cuh"
+#include "lbm_handle.h"
 #include "lbm_internal.h"
 
 using namespace lbmk;
@@ -32,49 +33,6 @@ void lbm_set_last_error(const std::string &m) { g_err = m; }
         if (e_ != cudaSuccess) return fail(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
-struct lbm_handle {
-    lbm_config cfg;
-    StepParams P;
-    cudaStream_t s = nullptr;
-    size_t esize = 4;
-    void *f[2] = {nullptr, nullptr};   // population buffers A/B (past the guard)
-    void *g[2] = {nullptr, nullptr};
-    void *fraw[2] = {nullptr, nullptr}; // allocations
-    void *graw[2] = {nullptr, nullptr};
-    int cur = 0;
-    float *mom = nullptr;
-    float *band = nullptr;
-    DevState *ds = nullptr;
-    bool inited = false;
-    long long steps = 0;
-    // IBM
-    bool ibm = false;
-    lbm_ibm_config icfg;
-    MarkerDev mk;
-    BodyParams bp;
-    double *hist = nullptr;
-    long long hist_cap = 1 << 16;
-    // graphs
-    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
-    int gsteps = 16;
-    int tx = 128, ty = 2;
-    StagedPlan stp;                       // staged (bulk-copy) step kernel
-    // interior solid cells and their momentum exchange
-    bool solids = false;
-    uint32_t *solid_d = nullptr, *near_d = nullptr;
-    float *mea_part = nullptr;
-    int *mea_blocks = nullptr;
-    int n_mea_blocks = 0;
-    double *mea_ring = nullptr;
-    long long mea_cap = 1 << 16;
-    int tile_x = 1, tile_y = 1;           // tile of the staged kernel (near-box rounding)
-    size_t dev_bytes = 0;
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    std::vector<cudaEvent_t> evpool;
-    cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
-    cudaStream_t s3 = nullptr;            // force reduction, beside the last spreading and band collision
-    cudaEvent_t ev_near = nullptr, ev_ibm = nullptr, ev_acc = nullptr, ev_fin = nullptr;
-};
 
 // ---------------------------------------------------------------------------
 // Boundary classes
@@ -294,6 +252,7 @@ static void free_handle(lbm_handle *h) {
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
     if (h->ev_near) cudaEventDestroy(h->ev_near);
+    lbm_output_free(h);
     for (void *p : {(void *)h->solid_d, (void *)h->near_d, (void *)h->mea_part, (void *)h->mea_blocks,
                     (void *)h->mea_ring})
         if (p) cudaFree(p);
@@ -393,7 +352,8 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
             chk(dalloc(h, &h->graw[i], ((size_t)QT * P.S + 2 * kGuard) * h->esize), "thermal");
             if (st == LBM_OK) h->g[i] = (char *)h->graw[i] + kGuard * h->esize;
         }
-    if (st == LBM_OK) chk(dalloc(h, &h->mom, (size_t)5 * P.N * sizeof(float)), "moments");
+    // moments: rho, u (3) [, T, heat flux (3)]
+    if (st == LBM_OK) chk(dalloc(h, &h->mom, (size_t)(c.thermal ? 8 : 5) * P.N * sizeof(float)), "moments");
     if (st == LBM_OK) chk(dalloc(h, &h->ds, sizeof(DevState)), "state");
     if (st == LBM_OK) chk(dalloc(h, &h->hist, (size_t)h->hist_cap * 8 * sizeof(double)), "history");
     if (st == LBM_OK) {
@@ -482,6 +442,7 @@ extern "C" lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const
         tmp[4 * N + c] = T ? (float)T[c] : (float)h->cfg.T_init;
     }
     // the moment buffer doubles as upload staging
+    CUDA_TRY(lbm_mom_acquire(h));
     CUDA_TRY(cudaMemcpyAsync(h->mom, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
     lbm_status s = do_init(h, h->mom);
     if (s != LBM_OK) return s;
@@ -839,18 +800,26 @@ extern "C" lbm_status lbmgpu_step_phases(lbm_handle *h, int nsteps, double *phas
 // ---------------------------------------------------------------------------
 // Read-back
 // ---------------------------------------------------------------------------
-static lbm_status export_moments(lbm_handle *h) {
-    if (!h->inited) return fail(LBM_ERR_STATE, "download: call lbmgpu_init first");
+// Gather-only pass writing the moments of the current state into h->mom,
+// after any asynchronous output copy of the previous contents.
+cudaError_t lbm_export_moments_async(lbm_handle *h) {
+    cudaError_t e = lbm_mom_acquire(h);
+    if (e != cudaSuccess) return e;
     LaunchArgs a = make_args(h, h->steps == 0 ? 0 : 1);
     a.mom = h->mom;
     a.export_only = 1;
-    CUDA_TRY(launch_step(h->cfg.storage, a));
+    return launch_step(h->cfg.storage, a);
+}
+
+static lbm_status export_moments(lbm_handle *h) {
+    if (!h->inited) return fail(LBM_ERR_STATE, "download: call lbmgpu_init first");
+    CUDA_TRY(lbm_export_moments_async(h));
     return LBM_OK;
 }
 
 extern "C" lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host) {
     if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
-    if (field < 0 || field > 4 || (field == 4 && !h->cfg.thermal)) return fail(LBM_ERR_INVALID, "download: bad field");
+    if (field < 0 || field > 7 || (field >= 4 && !h->cfg.thermal)) return fail(LBM_ERR_INVALID, "download: bad field");
     lbm_status s = export_moments(h);
     if (s != LBM_OK) return s;
     CUDA_TRY(cudaMemcpyAsync(host, h->mom + (size_t)field * h->P.N, (size_t)h->P.N * sizeof(float),

@@ -1,0 +1,74 @@
+// lbm_handle.h -- the state behind an lbm_handle (C ABI in lbm_abi.cu; the
+// asynchronous output in lbm_output.cu reads it too).  Not part of the
+// public ABI.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/lbmgpu.h"
+#include "lbm_device.cuh"
+#include "lbm_internal.h"
+
+struct lbm_output;  // asynchronous writer (lbm_output.cu)
+
+using lbmk::BodyParams;
+using lbmk::MarkerDev;
+using lbmk::StagedPlan;
+using lbmk::StepParams;
+using lbmk::DevState;
+
+struct lbm_handle {
+    lbm_output *out = nullptr;            // asynchronous VTK writer, created on first use
+    lbm_config cfg;
+    StepParams P;
+    cudaStream_t s = nullptr;
+    size_t esize = 4;
+    void *f[2] = {nullptr, nullptr};   // population buffers A/B (past the guard)
+    void *g[2] = {nullptr, nullptr};
+    void *fraw[2] = {nullptr, nullptr}; // allocations
+    void *graw[2] = {nullptr, nullptr};
+    int cur = 0;
+    float *mom = nullptr;
+    float *band = nullptr;
+    DevState *ds = nullptr;
+    bool inited = false;
+    long long steps = 0;
+    // IBM
+    bool ibm = false;
+    lbm_ibm_config icfg;
+    MarkerDev mk;
+    BodyParams bp;
+    double *hist = nullptr;
+    long long hist_cap = 1 << 16;
+    // graphs
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
+    int gsteps = 16;
+    int tx = 128, ty = 2;
+    StagedPlan stp;                       // staged (bulk-copy) step kernel
+    // interior solid cells and their momentum exchange
+    bool solids = false;
+    uint32_t *solid_d = nullptr, *near_d = nullptr;
+    float *mea_part = nullptr;
+    int *mea_blocks = nullptr;
+    int n_mea_blocks = 0;
+    double *mea_ring = nullptr;
+    long long mea_cap = 1 << 16;
+    int tile_x = 1, tile_y = 1;           // tile of the staged kernel (near-box rounding)
+    size_t dev_bytes = 0;
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::vector<cudaEvent_t> evpool;
+    cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
+    cudaStream_t s3 = nullptr;            // force reduction, beside the last spreading and band collision
+    cudaEvent_t ev_near = nullptr, ev_ibm = nullptr, ev_acc = nullptr, ev_fin = nullptr;
+};
+
+// Launch the gather-only export of the current state's moments into h->mom
+// (rho, ux, uy, uz [, T]) on h->s.
+cudaError_t lbm_export_moments_async(lbm_handle *h);
+void lbm_set_last_error(const std::string &m);
+// Order h->s after the asynchronous output's read of h->mom (no-op without one).
+cudaError_t lbm_mom_acquire(lbm_handle *h);
+void lbm_output_free(lbm_handle *h);

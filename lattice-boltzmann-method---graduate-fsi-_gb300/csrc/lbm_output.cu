@@ -1,0 +1,408 @@
+// lbm_output.cu -- output of the solver state in the reference's file formats,
+// written by a host thread while the device keeps stepping.
+//
+//   lbmgpu_output_vtk_async   OutputVTK (lbm.cpp:2290-2642): RectilinearGrid,
+//                             appended raw Float32 cell data
+//   lbmgpu_output_markers_vtk OutputVTK_Marker (lbm.cpp:3033-3077): legacy
+//                             ASCII POLYDATA of the markers
+//   lbmgpu_output_csv         OutputCSV (lbm.cpp:3169-3186): "time,error"
+//
+// The VTK path: a gather-only export pass writes the moments into the
+// handle's moment buffer on the main stream; a copy stream moves them to
+// pinned host memory once that pass is done; a writer thread waits for the
+// copy and formats the file.  The main stream goes on with the next steps
+// meanwhile -- only the next writer of the moment buffer (download, init
+// from fields, the next output) waits for the copy.  One file is in flight at
+// a time: a new call first finishes the previous one.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "lbm_handle.h"
+
+struct lbm_output {
+    float *host = nullptr;  // pinned: moments, then the band snapshot
+    size_t host_floats = 0;
+    cudaStream_t copy = nullptr;
+    cudaEvent_t exported = nullptr, copied = nullptr;
+    bool copy_issued = false;
+    std::thread writer;
+    lbm_status result = LBM_OK;  // of the last finished write
+    std::string error;
+};
+
+namespace {
+
+lbm_status out_fail(lbm_status s, const std::string &m) {
+    lbm_set_last_error(m);
+    return s;
+}
+
+// Wait for the writer in flight; its status becomes the call's.
+lbm_status join_writer(lbm_output *o) {
+    if (o->writer.joinable()) o->writer.join();
+    lbm_status r = o->result;
+    if (r != LBM_OK) lbm_set_last_error(o->error);
+    o->result = LBM_OK;
+    return r;
+}
+
+// Reference cell-type code of a face kind (LBM.h:505-515).
+float face_type(int kind) {
+    switch (kind) {
+    case LBM_FACE_WALL: return 1.0f;                                  // TYPE_S
+    case LBM_FACE_INLET: return 3.0f;                                 // TYPE_IN
+    case LBM_FACE_OUTLET_EQ: case LBM_FACE_OUTLET_ZG: return 2.0f;    // TYPE_OUT
+    default: return 0.0f;                                             // TYPE_F
+    }
+}
+
+struct VtkJob {
+    std::string path;
+    lbm_config cfg;
+    int dn[3];      // device extent
+    int nref[3];    // reference interior extent (N, or device - 2 on a periodic axis)
+    int off[3];     // device cell = reference index - off
+    double u_ref;
+    int thermal, force, solids;
+    long long N;
+    const float *mom;     // pinned moments
+    const float *band;    // pinned band snapshot (force density) or null
+    int band_o[3], bs[3];
+    float fsign;
+    float body[3];
+    std::vector<uint8_t> types;  // ghost-inclusive cell types given by the caller, or empty
+    std::vector<uint32_t> solid; // packed interior solid mask (device extent), or empty
+    cudaEvent_t copied;
+};
+
+// Boundary state of a ghost cell: among the faces that contain it, a moving
+// wall first (as the class tables do at edges), else the lowest axis.
+const lbm_face *ghost_face(const lbm_config &c, const int side[3]) {
+    const lbm_face *pick = nullptr;
+    for (int a = 0; a < 3; a++) {
+        if (side[a] < 0) continue;
+        const lbm_face *f = &c.faces[2 * a + side[a]];
+        const bool moving = f->kind == LBM_FACE_WALL && (f->u[0] != 0 || f->u[1] != 0 || f->u[2] != 0);
+        if (!pick || moving) pick = f;
+        if (moving) break;
+    }
+    return pick;
+}
+
+void write_vtk(VtkJob j, lbm_output *o) {
+    if (cudaEventSynchronize(j.copied) != cudaSuccess) {
+        o->result = LBM_ERR_CUDA;
+        o->error = "output_vtk: copy failed";
+        return;
+    }
+    const int Nx = j.nref[0], Ny = j.nref[1], Nz = j.nref[2];
+    const int zc = Nz;  // planes k = 1 .. Nz, as the reference writes (zcomp)
+    const size_t ncell = (size_t)(Nx + 2) * (Ny + 2) * zc;
+    FILE *fp = fopen(j.path.c_str(), "wb");
+    if (!fp) {
+        o->result = LBM_ERR_INVALID;
+        o->error = "output_vtk: cannot open " + j.path;
+        return;
+    }
+    unsigned long offset = 0;
+    fprintf(fp, "<?xml version=\"1.0\"?>\n");
+    fprintf(fp, "<VTKFile type=\"RectilinearGrid\" version=\"1.0\" byte_order=\"LittleEndian\" header_type=\"UInt32\">\n");
+    fprintf(fp, "  <RectilinearGrid WholeExtent=\"0 %d 0 %d 0 %d\">\n", Nx + 2, Ny + 2, zc);
+    fprintf(fp, "  <Piece Extent=\"0 %d 0 %d 0 %d\">\n", Nx + 2, Ny + 2, zc);
+    fprintf(fp, "    <PointData>\n");
+    fprintf(fp, "    </PointData>\n");
+    fprintf(fp, "    <CellData>\n");
+    auto arr = [&](const char *name, int comps) {
+        if (comps == 1)
+            fprintf(fp, "      <DataArray type=\"Float32\" Name=\"%s\" format=\"appended\" offset=\"%ld\" />\n", name,
+                    (long)offset);
+        else
+            fprintf(fp,
+                    "      <DataArray type=\"Float32\" Name=\"%s\" NumberOfComponents=\"%d\" format=\"appended\" "
+                    "offset=\"%ld\" />\n",
+                    name, comps, (long)offset);
+        offset += 4 + (unsigned long)comps * 4 * ncell;
+    };
+    arr("Density", 1);
+    arr("Velocity", 3);
+    if (j.force) arr("Force density", 3);
+    if (j.thermal) {
+        arr("Temperature", 1);
+        arr("Heat flux", 3);
+    }
+    arr("CellType", 1);
+    fprintf(fp, "    </CellData>\n");
+    fprintf(fp, "    <Coordinates>\n");
+    fprintf(fp, "      <DataArray type=\"Float32\" Name=\"CoordinateX\" format=\"appended\" offset=\"%ld\" />\n",
+            (long)offset);
+    offset += 4 + 4 * (unsigned long)(Nx + 3);
+    fprintf(fp, "      <DataArray type=\"Float32\" Name=\"CoordinateY\" format=\"appended\" offset=\"%ld\" />\n",
+            (long)offset);
+    offset += 4 + 4 * (unsigned long)(Ny + 3);
+    fprintf(fp, "      <DataArray type=\"Float32\" Name=\"CoordinateZ\" format=\"appended\" offset=\"%ld\" />\n",
+            (long)offset);
+    fprintf(fp, "    </Coordinates>\n");
+    fprintf(fp, "  </Piece>\n");
+    fprintf(fp, "  </RectilinearGrid>\n");
+    fprintf(fp, "  <AppendedData encoding=\"raw\">");
+    fprintf(fp, "_");
+
+    const long long N = j.N;
+    const int NXr = Nx + 2, NYr = Ny + 2;
+    // device cell of reference cell (i, j, k), or -1 for a ghost (side[] set)
+    auto locate = [&](int i, int jj, int k, int side[3]) -> long long {
+        const int r[3] = {i, jj, k};
+        long long d[3];
+        bool ghost = false;
+        for (int a = 0; a < 3; a++) {
+            side[a] = -1;
+            const int v = r[a] - j.off[a];
+            if (v < 0) {
+                side[a] = 0;
+                ghost = true;
+            } else if (v >= j.dn[a]) {
+                side[a] = 1;
+                ghost = true;
+            }
+            d[a] = v;
+        }
+        if (ghost) return -1;
+        return d[0] + (long long)j.dn[0] * (d[1] + (long long)j.dn[1] * d[2]);
+    };
+    std::vector<float> buf;
+    auto flush = [&](int comps) {
+        const uint32_t bytes = (uint32_t)(comps * 4 * ncell);
+        fwrite(&bytes, sizeof(uint32_t), 1, fp);
+        fwrite(buf.data(), sizeof(float), buf.size(), fp);
+        buf.clear();
+    };
+    buf.reserve(3 * ncell);
+    // Density, Velocity (/ u_ref), Force density, Temperature, Heat flux
+    for (int field = 0; field < 5; field++) {
+        if (field == 2 && !j.force) continue;
+        if (field >= 3 && !j.thermal) continue;
+        const int comps = (field == 0 || field == 3) ? 1 : 3;
+        for (int k = 1; k <= zc; k++)
+            for (int jj = 0; jj < NYr; jj++)
+                for (int i = 0; i < NXr; i++) {
+                    int side[3];
+                    const long long c = locate(i, jj, k, side);
+                    float v[3] = {0.0f, 0.0f, 0.0f};
+                    if (c >= 0) {
+                        if (field == 0) v[0] = j.mom[c];
+                        if (field == 1)
+                            for (int a = 0; a < 3; a++) v[a] = (float)(j.mom[(1 + a) * N + c] / j.u_ref);
+                        if (field == 2) {
+                            for (int a = 0; a < 3; a++) v[a] = j.body[a];
+                            const int bx = (int)(c % j.dn[0]) - j.band_o[0];
+                            const int by = (int)((c / j.dn[0]) % j.dn[1]) - j.band_o[1];
+                            const int bz = (int)(c / ((long long)j.dn[0] * j.dn[1])) - j.band_o[2];
+                            if (j.band && (unsigned)bx < (unsigned)j.bs[0] && (unsigned)by < (unsigned)j.bs[1] &&
+                                (unsigned)bz < (unsigned)j.bs[2]) {
+                                const long long nb = (long long)j.bs[0] * j.bs[1] * j.bs[2];
+                                const long long b = bx + (long long)j.bs[0] * (by + (long long)j.bs[1] * bz);
+                                for (int a = 0; a < 3; a++) v[a] = j.band[(4 + a) * nb + b] + j.fsign * j.band[(7 + a) * nb + b];
+                            }
+                        }
+                        if (field == 3) v[0] = j.mom[4 * N + c];
+                        if (field == 4)
+                            for (int a = 0; a < 3; a++) v[a] = j.mom[(5 + a) * N + c];
+                    } else {
+                        const lbm_face *f = ghost_face(j.cfg, side);
+                        if (field == 0) v[0] = (float)f->rho;
+                        if (field == 1)
+                            for (int a = 0; a < 3; a++) v[a] = (float)(f->u[a] / j.u_ref);
+                        if (field == 3) v[0] = (float)f->T;
+                    }
+                    for (int a = 0; a < comps; a++) buf.push_back(v[a]);
+                }
+        flush(comps);
+    }
+    // CellType: the float value of the reference's type code
+    for (int k = 1; k <= zc; k++)
+        for (int jj = 0; jj < NYr; jj++)
+            for (int i = 0; i < NXr; i++) {
+                float t;
+                if (!j.types.empty()) {
+                    t = (float)j.types[(size_t)i + (size_t)NXr * ((size_t)jj + (size_t)NYr * k)];
+                } else {
+                    int side[3];
+                    const long long c = locate(i, jj, k, side);
+                    if (c >= 0)
+                        t = (!j.solid.empty() && ((j.solid[(size_t)(c >> 5)] >> (c & 31)) & 1u)) ? 1.0f : 0.0f;
+                    else
+                        t = face_type(ghost_face(j.cfg, side)->kind);
+                }
+                buf.push_back(t);
+            }
+    flush(1);
+    // coordinates of the cell vertices
+    for (int a = 0; a < 3; a++) {
+        const int n = a == 0 ? Nx + 3 : (a == 1 ? Ny + 3 : zc + 1);
+        const uint32_t bytes = (uint32_t)(4 * n);
+        fwrite(&bytes, sizeof(uint32_t), 1, fp);
+        for (int i = 0; i < n; i++) {
+            const float v = (float)i;
+            fwrite(&v, sizeof(float), 1, fp);
+        }
+    }
+    fprintf(fp, "  </AppendedData>\n");
+    fprintf(fp, "</VTKFile>\n");
+    if (fclose(fp) != 0) {
+        o->result = LBM_ERR_INVALID;
+        o->error = "output_vtk: write failed: " + j.path;
+    }
+}
+
+}  // namespace
+
+cudaError_t lbm_mom_acquire(lbm_handle *h) {
+    if (!h->out || !h->out->copy_issued) return cudaSuccess;
+    return cudaStreamWaitEvent(h->s, h->out->copied, 0);
+}
+
+void lbm_output_free(lbm_handle *h) {
+    lbm_output *o = h->out;
+    if (!o) return;
+    if (o->writer.joinable()) o->writer.join();
+    if (o->copy) cudaStreamSynchronize(o->copy);
+    if (o->host) cudaFreeHost(o->host);
+    if (o->exported) cudaEventDestroy(o->exported);
+    if (o->copied) cudaEventDestroy(o->copied);
+    if (o->copy) cudaStreamDestroy(o->copy);
+    delete o;
+    h->out = nullptr;
+}
+
+extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
+    if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_vtk: bad argument");
+    if (!h->inited) return out_fail(LBM_ERR_STATE, "output_vtk: call lbmgpu_init first");
+    if (!h->out) {
+        h->out = new lbm_output();
+        lbm_output *o = h->out;
+        if (cudaStreamCreateWithFlags(&o->copy, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaEventCreateWithFlags(&o->exported, cudaEventDisableTiming) != cudaSuccess ||
+            cudaEventCreateWithFlags(&o->copied, cudaEventDisableTiming) != cudaSuccess) {
+            lbm_output_free(h);
+            return out_fail(LBM_ERR_CUDA, "output_vtk: stream/event creation failed");
+        }
+    }
+    lbm_output *o = h->out;
+    lbm_status prev = join_writer(o);
+    if (prev != LBM_OK) return prev;
+    const long long N = h->P.N;
+    const int nmom = h->cfg.thermal ? 8 : 5;
+    const bool force = h->ibm;
+    const size_t nb = force ? (size_t)h->P.nb : 0;
+    const size_t need = (size_t)nmom * N + 12 * nb;
+    if (o->host_floats < need) {
+        if (o->host) cudaFreeHost(o->host);
+        o->host = nullptr;
+        o->host_floats = 0;
+        if (cudaMallocHost((void **)&o->host, need * sizeof(float)) != cudaSuccess)
+            return out_fail(LBM_ERR_NOMEM, "output_vtk: pinned staging allocation failed");
+        o->host_floats = need;
+    }
+    // snapshot on the main stream: the export pass, and the band (small,
+    // and rewritten by the next step)
+    if (lbm_export_moments_async(h) != cudaSuccess) return out_fail(LBM_ERR_CUDA, "output_vtk: export failed");
+    if (force && cudaMemcpyAsync(o->host + (size_t)nmom * N, h->band, 12 * nb * sizeof(float),
+                                 cudaMemcpyDeviceToHost, h->s) != cudaSuccess)
+        return out_fail(LBM_ERR_CUDA, "output_vtk: band copy failed");
+    if (cudaEventRecord(o->exported, h->s) != cudaSuccess ||
+        cudaStreamWaitEvent(o->copy, o->exported, 0) != cudaSuccess ||
+        cudaMemcpyAsync(o->host, h->mom, (size_t)nmom * N * sizeof(float), cudaMemcpyDeviceToHost, o->copy) !=
+            cudaSuccess ||
+        cudaEventRecord(o->copied, o->copy) != cudaSuccess)
+        return out_fail(LBM_ERR_CUDA, "output_vtk: copy failed");
+    o->copy_issued = true;
+    VtkJob j;
+    j.path = path;
+    j.cfg = h->cfg;
+    j.N = N;
+    for (int a = 0; a < 3; a++) {
+        j.dn[a] = a == 0 ? h->P.nx : (a == 1 ? h->P.ny : h->P.nz);
+        const bool per = h->cfg.faces[2 * a].kind == LBM_FACE_PERIODIC;
+        j.off[a] = per ? 0 : 1;
+        j.nref[a] = per ? j.dn[a] - 2 : j.dn[a];
+        j.body[a] = (float)h->cfg.body_force[a];
+    }
+    j.u_ref = u_ref;
+    j.thermal = h->cfg.thermal;
+    j.force = force;
+    j.solids = h->solids;
+    j.mom = o->host;
+    j.band = force ? o->host + (size_t)nmom * N : nullptr;
+    j.fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
+    j.bs[0] = h->P.bsx;
+    j.bs[1] = h->P.bsy;
+    j.bs[2] = h->P.bsz;
+    if (force) {
+        DevState d;
+        if (cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s) != cudaSuccess ||
+            cudaStreamSynchronize(h->s) != cudaSuccess)
+            return out_fail(LBM_ERR_CUDA, "output_vtk: state read failed");
+        for (int a = 0; a < 3; a++) j.band_o[a] = d.band_o[a];
+    }
+    if (types) {
+        const size_t nt = (size_t)(j.nref[0] + 2) * (j.nref[1] + 2) * (j.nref[2] + 2);
+        j.types.assign(types, types + nt);
+    } else if (h->solids) {
+        const size_t words = (size_t)((N + 31) / 32);
+        j.solid.resize(words);
+        if (cudaMemcpyAsync(j.solid.data(), h->solid_d, words * 4, cudaMemcpyDeviceToHost, h->s) != cudaSuccess ||
+            cudaStreamSynchronize(h->s) != cudaSuccess)
+            return out_fail(LBM_ERR_CUDA, "output_vtk: solid mask read failed");
+    }
+    j.copied = o->copied;
+    o->writer = std::thread(write_vtk, std::move(j), o);
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_output_wait(lbm_handle *h) {
+    if (!h) return out_fail(LBM_ERR_INVALID, "output_wait: null handle");
+    if (!h->out) return LBM_OK;
+    return join_writer(h->out);
+}
+
+extern "C" lbm_status lbmgpu_output_markers_vtk(lbm_handle *h, const char *path) {
+    if (!h || !path) return out_fail(LBM_ERR_INVALID, "output_markers: bad argument");
+    if (!h->ibm) return out_fail(LBM_ERR_STATE, "output_markers: no markers set");
+    const int n = h->mk.n;
+    std::vector<double> pos(3 * (size_t)n);
+    if (cudaMemcpyAsync(pos.data(), h->mk.pos, pos.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s) !=
+            cudaSuccess ||
+        cudaStreamSynchronize(h->s) != cudaSuccess)
+        return out_fail(LBM_ERR_CUDA, "output_markers: copy failed");
+    FILE *fp = fopen(path, "w");
+    if (!fp) return out_fail(LBM_ERR_INVALID, std::string("output_markers: cannot open ") + path);
+    // legacy ASCII POLYDATA; numbers as the reference's stream prints them
+    // (6 significant digits); device positions are the reference's node
+    // coordinates
+    fprintf(fp, "# vtk DataFile Version 3.0\nwall_state\nASCII\nDATASET POLYDATA\n");
+    fprintf(fp, "POINTS %d float\n", n);
+    for (int m = 0; m < n; m++) fprintf(fp, "%g %g %g \n", pos[m], pos[(size_t)n + m], pos[2 * (size_t)n + m]);
+    fprintf(fp, "LINES %d %d\n", n, 3 * n);
+    for (int m = 0; m < n; m++) fprintf(fp, "2 %d %d\n", m % n, (m + 1) % n);
+    fprintf(fp, "VERTICES 1 %d\n", n + 1);
+    fprintf(fp, "%d ", n);
+    for (int m = 0; m < n; m++) fprintf(fp, "%d ", m);
+    if (fclose(fp) != 0) return out_fail(LBM_ERR_INVALID, std::string("output_markers: write failed: ") + path);
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_output_csv(const char *path, const double *values, int n, double time_step) {
+    if (!path || (!values && n > 0) || n < 0) return out_fail(LBM_ERR_INVALID, "output_csv: bad argument");
+    FILE *fp = fopen(path, "w");
+    if (!fp) return out_fail(LBM_ERR_INVALID, std::string("output_csv: cannot open ") + path);
+    fprintf(fp, "time,error\n");
+    for (int i = 0; i < n; i++) fprintf(fp, "%g,%g\n", (i + 1) * time_step, values[i]);
+    if (fclose(fp) != 0) return out_fail(LBM_ERR_INVALID, std::string("output_csv: write failed: ") + path);
+    return LBM_OK;
+}

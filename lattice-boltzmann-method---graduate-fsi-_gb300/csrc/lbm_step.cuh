@@ -216,7 +216,20 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
         mom[N + cell] = ux;
         mom[2 * N + cell] = uy;
         mom[3 * N + cell] = uz;
-        if (THERMAL) mom[4 * N + cell] = Tc;
+        if (THERMAL) {
+            // temperature and heat flux sum g c (lbm.cpp:778-792)
+            mom[4 * N + cell] = Tc;
+            float qx = 0.0f, qy = 0.0f, qz = 0.0f;
+#pragma unroll
+            for (int l = 1; l < QT; l++) {
+                qx += cx(l) * g[l];
+                qy += cy(l) * g[l];
+                qz += cz(l) * g[l];
+            }
+            mom[5 * N + cell] = qx;
+            mom[6 * N + cell] = qy;
+            mom[7 * N + cell] = qz;
+        }
     }
     if (export_only || !valid || frozen) return false;
 

@@ -42,7 +42,7 @@ static void dump_field(LBM &lb, FILE *fp, int which) {
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s steps out.bin [lid_velocity]\n", argv[0]);
+        fprintf(stderr, "usage: %s steps out.bin [lid_velocity [vtk]]\n", argv[0]);
         return 2;
     }
     int steps = atoi(argv[1]);
@@ -71,6 +71,11 @@ int main(int argc, char **argv) {
     if (!fp) return 3;
     for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
     fclose(fp);
+    if (argc > 4) {
+        // the reference's own VTK writer (lbm.cpp:2290-2642): ./field000000.vtr
+        int nout = 0;
+        OutputVTK(nout, lb);
+    }
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cavity\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());

@@ -6,6 +6,9 @@ outputs are stored as small .npz fixtures:
 
   cavity12_tau0.8_lid0.05_200.npz   D3Q19 lid-driven cavity 12^3, 200 steps:
                                     full interior rho, ux, uy, uz
+  cavity12_vtk_200.npz              the same run's OutputVTK file
+                                    (lbm.cpp:2290-2642): header text and
+                                    every appended array
   cavity64_tau0.8_lid0.05_5000.npz  the 64^3, tau = 0.8, 5000-step cavity:
                                     mid planes k = 32 and i = 32 of rho, u,
                                     plus interior sums and maxima
@@ -40,6 +43,22 @@ OUT = os.path.dirname(os.path.abspath(__file__))
 REF = os.path.join(ROOT, "oracle", "_ref")
 
 
+def read_vtr(path: str) -> dict:
+    """Header text and every appended DataArray of a RectilinearGrid file."""
+    import re
+
+    raw = open(path, "rb").read()
+    cut = raw.index(b'<AppendedData encoding="raw">') + len(b'<AppendedData encoding="raw">')
+    head = raw[:cut].decode()
+    data = raw[cut + 1:]
+    out = {"header": np.array(head)}
+    for m in re.finditer(r'Name="([^"]+)"(?: NumberOfComponents="(\d+)")? format="appended" offset="(\d+)"', head):
+        off = int(m.group(3))
+        n = int(np.frombuffer(data[off:off + 4], dtype=np.uint32)[0])
+        out[m.group(1)] = np.frombuffer(data[off + 4:off + 4 + n], dtype=np.float32).copy()
+    return out
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -52,9 +71,11 @@ def main() -> None:
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05")
     tmp = tempfile.mkdtemp()
 
-    # 12^3 cavity, 200 steps
+    # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
     p = os.path.join(tmp, "cav12.bin")
-    run("ref_cavity_12_0.8", ["200", p, "0.05"])
+    subprocess.check_call([os.path.join(REF, "ref_cavity_12_0.8"), "200", p, "0.05", "vtk"], cwd=tmp)
+    v = read_vtr(os.path.join(tmp, "field000000.vtr"))
+    np.savez_compressed(os.path.join(OUT, "cavity12_vtk_200.npz"), **v)
     f = oracle.read_ref_dump(p, 14, 14, 14, 4)["fields"][:, 1:-1, 1:-1, 1:-1]
     np.savez_compressed(os.path.join(OUT, "cavity12_tau0.8_lid0.05_200.npz"), rho=f[0], ux=f[1], uy=f[2], uz=f[3],
                         n=12, tau=0.8, lid=0.05, steps=200)

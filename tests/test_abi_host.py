@@ -100,3 +100,10 @@ def test_create_rejects_bad_config_without_touching_device(pkg):
     cfg.faces[0].kind = pkg.FACE_PERIODIC
     with pytest.raises(pkg.LbmError):
         pkg.Solver(cfg)
+
+
+def test_output_csv_reference_format(pkg, tmp_path):
+    """OutputCSV (lbm.cpp:3169-3186): header "time,error", time (i+1) dt."""
+    p = str(tmp_path / "cd.csv")
+    pkg.output_csv(p, [1.5, 0.25, 3e-7], 0.5)
+    assert open(p).read() == "time,error\n0.5,1.5\n1,0.25\n1.5,3e-07\n"
