@@ -197,6 +197,15 @@ lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, in
 
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 
+/* Checkpoint and restart (no counterpart in the reference, which restarts
+ * from its set-up): the current populations, the device state (step counters,
+ * band origin, rigid body), the markers and the force histories.  Load onto a
+ * handle created with the same configuration and the same lbmgpu_set_markers /
+ * lbmgpu_set_solids calls, instead of lbmgpu_init; the run then continues as
+ * if never interrupted. */
+lbm_status lbmgpu_save_state(lbm_handle *h, const char *path);
+lbm_status lbmgpu_load_state(lbm_handle *h, const char *path);
+
 /* ------------------------------------------------------------------------
  * Output in the reference's file formats.
  * ---------------------------------------------------------------------- */

@@ -39,7 +39,7 @@ ABI_SYMBOLS = [
     "lbmgpu_batch_step_timed", "lbmgpu_batch_autotune", "lbmgpu_batch_download", "lbmgpu_batch_status",
     "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_batch_step_noalloc", "lbmgpu_step_phases",
     "lbmgpu_set_solids", "lbmgpu_get_solid_forces", "lbmgpu_output_vtk_async", "lbmgpu_output_wait",
-    "lbmgpu_output_markers_vtk", "lbmgpu_output_csv",
+    "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
 ]
 
 
@@ -141,6 +141,8 @@ def load(path: str | None = None):
     L.lbmgpu_set_solids.argtypes = [vp, C.POINTER(C.c_uint8)]
     L.lbmgpu_output_vtk_async.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
     L.lbmgpu_output_wait.argtypes = [vp]
+    L.lbmgpu_save_state.argtypes = [vp, C.c_char_p]
+    L.lbmgpu_load_state.argtypes = [vp, C.c_char_p]
     L.lbmgpu_output_markers_vtk.argtypes = [vp, C.c_char_p]
     L.lbmgpu_output_csv.argtypes = [C.c_char_p, dp, i, d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
@@ -298,6 +300,12 @@ class Solver:
             self._vtk_types = np.ascontiguousarray(types, dtype=np.uint8).ravel()
             t = self._vtk_types.ctypes.data_as(C.POINTER(C.c_uint8))
         check(self.L.lbmgpu_output_vtk_async(self.h, path.encode(), float(u_ref), t))
+
+    def save_state(self, path: str):
+        check(self.L.lbmgpu_save_state(self.h, path.encode()))
+
+    def load_state(self, path: str):
+        check(self.L.lbmgpu_load_state(self.h, path.encode()))
 
     def output_wait(self):
         check(self.L.lbmgpu_output_wait(self.h))
