@@ -207,6 +207,44 @@ lbm_status lbmgpu_save_state(lbm_handle *h, const char *path);
 lbm_status lbmgpu_load_state(lbm_handle *h, const char *path);
 
 /* ------------------------------------------------------------------------
+ * MORE_DETAILS mode (LBM.h:55): pressure, viscous stress and the running
+ * statistics of Sup_MacroProp.  A run-time switch per handle here.
+ * ---------------------------------------------------------------------- */
+
+/* Components of lbmgpu_download_details ([7][cells], FP32): MacroProp's
+ * pressure = rho / 3 and viscous stress
+ * sigma_ab = -(tau - 1/2) / tau * sum_l f_l (c_la - u_a)(c_lb - u_b)
+ * (lbm.cpp:681-705) of the current state; sigma is symmetric, its six
+ * distinct components are given. */
+enum { LBM_DETAIL_P = 0, LBM_DETAIL_SXX = 1, LBM_DETAIL_SXY = 2, LBM_DETAIL_SXZ = 3, LBM_DETAIL_SYY = 4,
+       LBM_DETAIL_SYZ = 5, LBM_DETAIL_SZZ = 6, LBM_DETAIL_COUNT = 7 };
+
+/* Components of lbmgpu_download_stats ([20][cells], FP64): the
+ * Sup_MacroProp averages and rms values (lbm.cpp:865-939) of velocity (3),
+ * pressure (1) and Reynolds stress (6 distinct: xx xy xz yy yz zz).  The
+ * reference never computes the vorticity (lbm.cpp:712-770 is commented out):
+ * its averages and rms values are zero and not held. */
+enum { LBM_STAT_AVG_U = 0, LBM_STAT_AVG_P = 3, LBM_STAT_AVG_RS = 4, LBM_STAT_RMS_U = 10, LBM_STAT_RMS_P = 13,
+       LBM_STAT_RMS_RS = 14, LBM_STAT_COUNT = 20 };
+
+/* on = 1: allocate the detail and statistics arrays (7 floats + 20 doubles
+ * per cell), clear the statistics, and add the Pressure / Viscous Stress /
+ * Vorticity arrays of the reference's MORE_DETAILS OutputVTK to
+ * lbmgpu_output_vtk_async.  on = 0 frees them. */
+lbm_status lbmgpu_set_more_details(lbm_handle *h, int on);
+/* Pressure and viscous stress of the current state, [LBM_DETAIL_COUNT][cells]. */
+lbm_status lbmgpu_download_details(lbm_handle *h, float *host);
+/* LBM::Sup_MacroProp(n) (lbm.cpp:865-939; main.cpp:389 calls it every Nt
+ * steps): fold the current state into the statistics with
+ * told = (n - nt) * dt, the reference's weights included (the velocity
+ * sample weighted dt, the others 1; the pressure rms squares the current
+ * pressure, lbm.cpp:913).  Synchronous. */
+lbm_status lbmgpu_sup_macroprop(lbm_handle *h, int n, int nt, double dt);
+/* The statistics, [LBM_STAT_COUNT][cells]; samples / told (may be NULL): how
+ * many samples were folded in and the told of the latest one. */
+lbm_status lbmgpu_download_stats(lbm_handle *h, double *host, int *samples, double *told);
+
+/* ------------------------------------------------------------------------
  * Output in the reference's file formats.
  * ---------------------------------------------------------------------- */
 
@@ -222,6 +260,13 @@ lbm_status lbmgpu_load_state(lbm_handle *h, const char *path);
  * lbmgpu_output_wait) finishes the previous one and returns its status. */
 lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types);
 lbm_status lbmgpu_output_wait(lbm_handle *h);
+
+/* OutputAVGVTK (lbm.cpp:2644-3031), MORE_DETAILS mode: Density, Velocity,
+ * Avg / Rms velocity (/ u_ref), Pressure, Avg / Rms pressure, Viscous Stress,
+ * Vorticity, Avg / Rms vorticity (zero, as in the reference), Avg / Rms
+ * Reynolds stress (/ u_ref^2), CellType; ghost cells carry the statistics a
+ * cell held at its face's state since the first sample.  Synchronous. */
+lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, double u_ref, const uint8_t *types);
 
 /* OutputVTK_Marker (lbm.cpp:3033-3077): legacy ASCII POLYDATA of the markers
  * (points, closed polyline, vertices). */

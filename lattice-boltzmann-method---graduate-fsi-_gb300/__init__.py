@@ -26,6 +26,9 @@ STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
 FACE_WALL, FACE_INLET, FACE_OUTLET_EQ, FACE_OUTLET_ZG, FACE_PERIODIC = 0, 1, 2, 3, 4
 TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
 FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
+# MORE_DETAILS: the six distinct stress components, and the statistics rows
+SYM6 = ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))
+STAT_AVG_U, STAT_AVG_P, STAT_AVG_RS, STAT_RMS_U, STAT_RMS_P, STAT_RMS_RS, STAT_COUNT = 0, 3, 4, 10, 13, 14, 20
 STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE, STATUS_TIMEOUT = 1, 2, 4, 16
 
 # Every symbol include/lbmgpu.h declares.
@@ -40,6 +43,8 @@ ABI_SYMBOLS = [
     "lbmgpu_batch_info", "lbmgpu_serve_run", "lbmgpu_batch_step_noalloc", "lbmgpu_step_phases",
     "lbmgpu_set_solids", "lbmgpu_get_solid_forces", "lbmgpu_output_vtk_async", "lbmgpu_output_wait",
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
+    "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
+    "lbmgpu_output_avg_vtk",
 ]
 
 
@@ -145,6 +150,11 @@ def load(path: str | None = None):
     L.lbmgpu_load_state.argtypes = [vp, C.c_char_p]
     L.lbmgpu_output_markers_vtk.argtypes = [vp, C.c_char_p]
     L.lbmgpu_output_csv.argtypes = [C.c_char_p, dp, i, d]
+    L.lbmgpu_set_more_details.argtypes = [vp, i]
+    L.lbmgpu_download_details.argtypes = [vp, C.POINTER(C.c_float)]
+    L.lbmgpu_sup_macroprop.argtypes = [vp, i, i, d]
+    L.lbmgpu_download_stats.argtypes = [vp, dp, C.POINTER(i), dp]
+    L.lbmgpu_output_avg_vtk.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
     L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
@@ -300,6 +310,39 @@ class Solver:
             self._vtk_types = np.ascontiguousarray(types, dtype=np.uint8).ravel()
             t = self._vtk_types.ctypes.data_as(C.POINTER(C.c_uint8))
         check(self.L.lbmgpu_output_vtk_async(self.h, path.encode(), float(u_ref), t))
+
+    # MORE_DETAILS mode (LBM.h:55) ---------------------------------------
+    def set_more_details(self, on: bool = True):
+        check(self.L.lbmgpu_set_more_details(self.h, 1 if on else 0))
+
+    def details(self) -> dict:
+        """Pressure rho/3 and viscous stress (lbm.cpp:681-705) of the current
+        state: {"p": [cells], "sigma": [6][cells] in SYM6 order}."""
+        out = np.empty((7, self.ncell), dtype=np.float32)
+        check(self.L.lbmgpu_download_details(self.h, out.ctypes.data_as(C.POINTER(C.c_float))))
+        return {"p": out[0].reshape(self.shape), "sigma": out[1:].reshape((6,) + self.shape)}
+
+    def sup_macroprop(self, n: int, nt: int = 10, dt: float = 1.0):
+        """LBM::Sup_MacroProp(n) (lbm.cpp:865-939), told = (n - nt) dt."""
+        check(self.L.lbmgpu_sup_macroprop(self.h, int(n), int(nt), float(dt)))
+
+    def stats(self) -> dict:
+        out = np.empty((STAT_COUNT, self.ncell), dtype=np.float64)
+        n = C.c_int(0)
+        told = np.zeros(1)
+        check(self.L.lbmgpu_download_stats(self.h, _dp(out), C.byref(n), _dp(told)))
+        sh = self.shape
+        return {"avg_u": out[0:3].reshape((3,) + sh), "avg_p": out[3].reshape(sh),
+                "avg_rs": out[4:10].reshape((6,) + sh), "rms_u": out[10:13].reshape((3,) + sh),
+                "rms_p": out[13].reshape(sh), "rms_rs": out[14:20].reshape((6,) + sh), "samples": n.value,
+                "told": float(told[0])}
+
+    def output_avg_vtk(self, path: str, u_ref: float = 1.0, types=None):
+        t = None
+        if types is not None:
+            types = np.ascontiguousarray(types, dtype=np.uint8)
+            t = types.ctypes.data_as(C.POINTER(C.c_uint8))
+        check(self.L.lbmgpu_output_avg_vtk(self.h, path.encode(), float(u_ref), t))
 
     def save_state(self, path: str):
         check(self.L.lbmgpu_save_state(self.h, path.encode()))

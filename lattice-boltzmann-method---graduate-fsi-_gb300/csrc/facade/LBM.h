@@ -67,6 +67,7 @@ struct lbm_options {
     double body_radius = 0.0;     // IBM body radius (0: from the marker cloud)
     int thermal = 0;              // D3Q7 temperature population
     double tau_g = 0.0, T_ref = 0.0, gbeta[3] = {0, 0, 0};
+    int Nt = 10;                  // output cadence (LBM.h:493-496): Sup_MacroProp's told = (n - Nt) dt
 };
 extern lbm_options g_lbm_options;
 
@@ -79,6 +80,21 @@ class LATTICE {
     double F[3] = {0, 0, 0};
     double Fm[3] = {0, 0, 0};
     double T = 0.0;
+#if defined MORE_DETAILS
+    // LBM.h:572-588; vorticity and its statistics stay zero, as in the
+    // reference (whose vorticity code is commented out)
+    double pressure = 0.0;
+    double sigma[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double vorticity[3] = {0, 0, 0};
+    double avg_velocity[3] = {0, 0, 0};
+    double avg_pressure = 0;
+    double avg_vorticity[3] = {0, 0, 0};
+    double avg_ReynoldStress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    double rms_velocity[3] = {0, 0, 0};
+    double rms_pressure = 0;
+    double rms_vorticity[3] = {0, 0, 0};
+    double rms_ReynoldStress[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+#endif
 };
 
 class MARKER {
@@ -119,8 +135,14 @@ class LBM {
     int getNz() const;
     double getTAU() const;
 
+#if defined MORE_DETAILS
+    // LBM::Sup_MacroProp (lbm.cpp:865-939) on the device; the statistics
+    // reach fluid[..] with sync_to_host
+    void Sup_MacroProp(int n);
+#endif
+
     // GB300 additions
-    void sync_to_host();        // MacroProp moments into fluid[..]
+    void sync_to_host();        // MacroProp moments (MORE_DETAILS: and details, statistics) into fluid[..]
     lbm_handle *handle() const; // the device solve (nullptr before Init)
     long long steps() const;
     friend void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
@@ -141,3 +163,7 @@ double MEA_CD(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zma
 // OutputVTK (LBM.h:776-846) from the device, written while the loop goes on;
 // lbmgpu_output_wait(lb.handle()) finishes the file in flight.
 void OutputVTK_async(int &nout, LBM &lb);
+#if defined MORE_DETAILS
+// OutputAVGVTK (LBM.h:780-782) from the device: ./avgfield.vtr
+void OutputAVGVTK(int &nout, LBM &lb);
+#endif

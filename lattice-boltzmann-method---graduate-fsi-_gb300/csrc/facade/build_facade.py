@@ -1,8 +1,8 @@
-"""Build the C++ drop-in facade (LBM.h) and its two drivers against liblbmgpu.so.
+"""Build the C++ drop-in facade (LBM.h) drivers against liblbmgpu.so.
 
-Outputs: csrc/facade/_build/liblbm_facade.a? -- no archive: the drivers
-dropin_cavity and dropin_sphere are linked directly with lbm_facade.cpp and
--llbmgpu (rpath to the package directory).
+Each driver in DRIVERS is compiled together with lbm_facade.cpp (with the
+reference compile-time switches of DRIVER_FLAGS) and linked with -llbmgpu
+(rpath to the package directory) into csrc/facade/_build/.
 """
 import os
 import subprocess
@@ -10,7 +10,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
-DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb"]
+DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details"]
+# compile-time switches of the reference a driver is built with
+DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"]}
 
 
 def build(force: bool = False) -> list:
@@ -22,7 +24,7 @@ def build(force: bool = False) -> list:
         exe = os.path.join(OUT, d)
         deps = srcs + [os.path.join(HERE, d + ".cpp"), lib]
         if force or not os.path.exists(exe) or any(os.path.getmtime(p) > os.path.getmtime(exe) for p in deps):
-            cmd = ["g++", "-O2", "-std=c++17", "-I" + HERE, os.path.join(HERE, d + ".cpp"),
+            cmd = ["g++", "-O2", "-std=c++17", "-I" + HERE] + DRIVER_FLAGS.get(d, []) + [os.path.join(HERE, d + ".cpp"),
                    os.path.join(HERE, "lbm_facade.cpp"), "-L" + PKG, "-llbmgpu",
                    "-Wl,-rpath," + PKG, "-o", exe]
             subprocess.check_call(cmd)

@@ -156,6 +156,9 @@ void LBM::Init() {
         if (any) check("set_solids", lbmgpu_set_solids(dev->h, mask.data()));
         dev->solids = any;
     }
+#if defined MORE_DETAILS
+    check("set_more_details", lbmgpu_set_more_details(dev->h, 1));
+#endif
     std::vector<double> drho(nd), dux(nd), duy(nd), duz(nd), dT(nd);
     for (int z = 0; z < cfg.nz; z++)
         for (int y = 0; y < cfg.ny; y++)
@@ -221,8 +224,42 @@ void LBM::sync_to_host() {
                 c.uz = buf[3 * nd + id];
                 if (nf == 5) c.T = buf[4 * nd + id];
             }
+#if defined MORE_DETAILS
+    std::vector<float> det(LBM_DETAIL_COUNT * nd);
+    std::vector<double> st(LBM_STAT_COUNT * nd);
+    check("download_details", lbmgpu_download_details(dev->h, det.data()));
+    check("download_stats", lbmgpu_download_stats(dev->h, st.data(), nullptr, nullptr));
+    static const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+    for (int z = 0; z < dev->dn[2]; z++)
+        for (int y = 0; y < dev->dn[1]; y++)
+            for (int x = 0; x < dev->dn[0]; x++) {
+                size_t id = (size_t)x + (size_t)dev->dn[0] * ((size_t)y + (size_t)dev->dn[1] * z);
+                LATTICE &c = fluid[x + dev->off[0]][y + dev->off[1]][z + dev->off[2]];
+                c.pressure = det[id];
+                c.avg_pressure = st[LBM_STAT_AVG_P * nd + id];
+                c.rms_pressure = st[LBM_STAT_RMS_P * nd + id];
+                for (int a = 0; a < 3; a++) {
+                    c.avg_velocity[a] = st[(LBM_STAT_AVG_U + a) * nd + id];
+                    c.rms_velocity[a] = st[(LBM_STAT_RMS_U + a) * nd + id];
+                }
+                for (int q = 0; q < 6; q++) {
+                    const int a = ia[q], b = ib[q];
+                    c.sigma[a][b] = c.sigma[b][a] = det[(LBM_DETAIL_SXX + q) * nd + id];
+                    c.avg_ReynoldStress[a][b] = c.avg_ReynoldStress[b][a] = st[(LBM_STAT_AVG_RS + q) * nd + id];
+                    c.rms_ReynoldStress[a][b] = c.rms_ReynoldStress[b][a] = st[(LBM_STAT_RMS_RS + q) * nd + id];
+                }
+            }
+#endif
     dev->mirror_stale = false;
 }
+
+#if defined MORE_DETAILS
+void LBM::Sup_MacroProp(int n) {
+    if (!dev->h) check("Sup_MacroProp before Init", LBM_ERR_STATE);
+    check("sup_macroprop", lbmgpu_sup_macroprop(dev->h, n, g_lbm_options.Nt, 1.0));
+    dev->mirror_stale = true;
+}
+#endif
 
 double kernel(double r) {
     double a = std::fabs(r);
@@ -341,3 +378,19 @@ void OutputVTK_async(int &nout, LBM &lb) {
     snprintf(name, sizeof(name), "./field%06d.vtr", nout);
     check("output_vtk_async", lbmgpu_output_vtk_async(h, name, g_lbm_options.u_max, types.data()));
 }
+
+#if defined MORE_DETAILS
+// OutputAVGVTK: the reference names its file only for its tandem-triangle
+// case (lbm.cpp:2654-2658); here it is always ./avgfield.vtr.
+void OutputAVGVTK(int &, LBM &lb) {
+    lbm_handle *h = lb.handle();
+    if (!h) check("OutputAVGVTK before Init", LBM_ERR_STATE);
+    const int NX = lb.getNx() + 2, NY = lb.getNy() + 2, NZ = lb.getNz() + 2;
+    std::vector<uint8_t> types((size_t)NX * NY * NZ);
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++)
+                types[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = (uint8_t)lb.fluid[i][j][k].type;
+    check("output_avg_vtk", lbmgpu_output_avg_vtk(h, "./avgfield.vtr", g_lbm_options.u_max, types.data()));
+}
+#endif

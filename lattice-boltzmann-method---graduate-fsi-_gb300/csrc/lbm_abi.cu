@@ -254,7 +254,7 @@ static void free_handle(lbm_handle *h) {
     if (h->ev_near) cudaEventDestroy(h->ev_near);
     lbm_output_free(h);
     for (void *p : {(void *)h->solid_d, (void *)h->near_d, (void *)h->mea_part, (void *)h->mea_blocks,
-                    (void *)h->mea_ring})
+                    (void *)h->mea_ring, (void *)h->det, (void *)h->stats})
         if (p) cudaFree(p);
     if (h->ev_ibm) cudaEventDestroy(h->ev_ibm);
     if (h->ev_acc) cudaEventDestroy(h->ev_acc);

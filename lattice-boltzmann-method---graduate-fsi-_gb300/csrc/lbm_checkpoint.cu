@@ -7,7 +7,9 @@
 // marker density, force accumulators) and the force / momentum-exchange
 // histories.  Restoring onto a handle created with the same configuration
 // (and the same lbmgpu_set_markers / lbmgpu_set_solids calls) continues the
-// run exactly where it was saved.
+// run exactly where it was saved.  In MORE_DETAILS mode the Sup_MacroProp
+// statistics (and their sample count and latest told) travel too; the
+// restoring handle must be in that mode as well.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -19,12 +21,14 @@
 
 namespace {
 
-const char kMagic[8] = {'L', 'B', 'M', 'G', 'P', 'U', 'C', '1'};
+const char kMagic[8] = {'L', 'B', 'M', 'G', 'P', 'U', 'C', '2'};
 
 struct CkptHeader {
     char magic[8];
-    int nx, ny, nz, storage, thermal, ibm_markers, solids, pad;
+    int nx, ny, nz, storage, thermal, ibm_markers, solids, details;
     long long S, steps, hist_cap, mea_cap;
+    long long stat_samples;
+    double stat_told;
 };
 
 lbm_status ck_fail(lbm_status s, const std::string &m) {
@@ -53,6 +57,7 @@ std::vector<Region> regions(lbm_handle *h, int src_buffer) {
         r.push_back({h->mk.acc, 4 * n * sizeof(double)});
     }
     if (h->solids) r.push_back({h->mea_ring, (size_t)h->mea_cap * 4 * sizeof(double)});
+    if (h->details) r.push_back({h->stats, (size_t)LBM_STAT_COUNT * h->P.N * sizeof(double)});
     return r;
 }
 
@@ -67,6 +72,9 @@ CkptHeader header_of(lbm_handle *h) {
     c.thermal = h->cfg.thermal;
     c.ibm_markers = h->ibm ? h->mk.n : 0;
     c.solids = h->solids ? 1 : 0;
+    c.details = h->details ? 1 : 0;
+    c.stat_samples = h->stat_samples;
+    c.stat_told = h->stat_told;
     c.S = h->P.S;
     c.steps = h->steps;
     c.hist_cap = h->hist_cap;
@@ -109,6 +117,7 @@ extern "C" lbm_status lbmgpu_load_state(lbm_handle *h, const char *path) {
     }
     if (c.nx != mine.nx || c.ny != mine.ny || c.nz != mine.nz || c.storage != mine.storage ||
         c.thermal != mine.thermal || c.ibm_markers != mine.ibm_markers || c.solids != mine.solids ||
+        c.details != mine.details ||
         c.S != mine.S || c.hist_cap != mine.hist_cap || c.mea_cap != mine.mea_cap) {
         fclose(fp);
         return ck_fail(LBM_ERR_INVALID, "load_state: the file was saved from a different configuration");
@@ -130,6 +139,8 @@ extern "C" lbm_status lbmgpu_load_state(lbm_handle *h, const char *path) {
     if (!ok) return ck_fail(LBM_ERR_INVALID, std::string("load_state: read failed: ") + path);
     h->cur = 0;
     h->steps = c.steps;
+    h->stat_samples = (int)c.stat_samples;
+    h->stat_told = c.stat_told;
     h->inited = true;
     for (int i = 0; i < 2; i++)
         if (h->gexec[i]) {

@@ -63,6 +63,12 @@ struct lbm_handle {
     cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
     cudaStream_t s3 = nullptr;            // force reduction, beside the last spreading and band collision
     cudaEvent_t ev_near = nullptr, ev_ibm = nullptr, ev_acc = nullptr, ev_fin = nullptr;
+    // MORE_DETAILS mode (lbm_details.cu)
+    bool details = false;
+    float *det = nullptr;                 // [7][N]: p, sigma xx xy xz yy yz zz
+    double *stats = nullptr;              // [20][N]: Sup_MacroProp averages and rms values
+    int stat_samples = 0;                 // samples folded in
+    double stat_told = 0.0;               // told of the latest sample
 };
 
 // Launch the gather-only export of the current state's moments into h->mom
@@ -72,3 +78,6 @@ void lbm_set_last_error(const std::string &m);
 // Order h->s after the asynchronous output's read of h->mom (no-op without one).
 cudaError_t lbm_mom_acquire(lbm_handle *h);
 void lbm_output_free(lbm_handle *h);
+// The moment export followed by the MORE_DETAILS pass into h->det on h->s;
+// fold = 1 also folds the state into h->stats with Sup_MacroProp's told, dt.
+cudaError_t lbm_details_async(lbm_handle *h, int fold, double told, double dt);

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <string>
 #include <thread>
 #include <vector>
@@ -62,23 +63,37 @@ float face_type(int kind) {
     }
 }
 
-struct VtkJob {
-    std::string path;
+// Cells of a reference-layout file: i = 0..Nx+1, j = 0..Ny+1, k = 1..Nz of
+// the reference's fluid array, ghosts included.
+struct VtkGrid {
     lbm_config cfg;
     int dn[3];      // device extent
     int nref[3];    // reference interior extent (N, or device - 2 on a periodic axis)
     int off[3];     // device cell = reference index - off
-    double u_ref;
-    int thermal, force, solids;
     long long N;
-    const float *mom;     // pinned moments
-    const float *band;    // pinned band snapshot (force density) or null
-    int band_o[3], bs[3];
-    float fsign;
-    float body[3];
     std::vector<uint8_t> types;  // ghost-inclusive cell types given by the caller, or empty
     std::vector<uint32_t> solid; // packed interior solid mask (device extent), or empty
-    cudaEvent_t copied;
+
+    // device cell of reference cell (i, j, k), or -1 for a ghost (side[] set)
+    long long locate(int i, int jj, int k, int side[3]) const {
+        const int r[3] = {i, jj, k};
+        long long d[3];
+        bool ghost = false;
+        for (int a = 0; a < 3; a++) {
+            side[a] = -1;
+            const int v = r[a] - off[a];
+            if (v < 0) {
+                side[a] = 0;
+                ghost = true;
+            } else if (v >= dn[a]) {
+                side[a] = 1;
+                ghost = true;
+            }
+            d[a] = v;
+        }
+        if (ghost) return -1;
+        return d[0] + (long long)dn[0] * (d[1] + (long long)dn[1] * d[2]);
+    }
 };
 
 // Boundary state of a ghost cell: among the faces that contain it, a moving
@@ -95,20 +110,54 @@ const lbm_face *ghost_face(const lbm_config &c, const int side[3]) {
     return pick;
 }
 
-void write_vtk(VtkJob j, lbm_output *o) {
-    if (cudaEventSynchronize(j.copied) != cudaSuccess) {
-        o->result = LBM_ERR_CUDA;
-        o->error = "output_vtk: copy failed";
-        return;
+// One cell-data array: its name, components, and the values of a cell --
+// an interior cell c >= 0, or a ghost (c < 0) in the state of face gf.
+struct VtkArray {
+    const char *name;
+    int comps;
+    std::function<void(long long c, const lbm_face *gf, float *v)> value;
+};
+
+VtkGrid grid_of(lbm_handle *h) {
+    VtkGrid g;
+    g.cfg = h->cfg;
+    g.N = h->P.N;
+    for (int a = 0; a < 3; a++) {
+        g.dn[a] = a == 0 ? h->P.nx : (a == 1 ? h->P.ny : h->P.nz);
+        const bool per = h->cfg.faces[2 * a].kind == LBM_FACE_PERIODIC;
+        g.off[a] = per ? 0 : 1;
+        g.nref[a] = per ? g.dn[a] - 2 : g.dn[a];
     }
-    const int Nx = j.nref[0], Ny = j.nref[1], Nz = j.nref[2];
+    return g;
+}
+
+// The caller's types array, else the device solid mask (read on h->s).
+bool grid_types(lbm_handle *h, VtkGrid &g, const uint8_t *types) {
+    if (types) {
+        const size_t nt = (size_t)(g.nref[0] + 2) * (g.nref[1] + 2) * (g.nref[2] + 2);
+        g.types.assign(types, types + nt);
+    } else if (h->solids) {
+        const size_t words = (size_t)((g.N + 31) / 32);
+        g.solid.resize(words);
+        if (cudaMemcpyAsync(g.solid.data(), h->solid_d, words * 4, cudaMemcpyDeviceToHost, h->s) != cudaSuccess ||
+            cudaStreamSynchronize(h->s) != cudaSuccess)
+            return false;
+    }
+    return true;
+}
+
+// A RectilinearGrid .vtr in the layout of the reference's writers
+// (lbm.cpp:2290-2642, 2644-3031): the arrays, then CellType, cell-vertex
+// coordinates, appended raw Float32 data with UInt32 byte counts.
+bool write_rectilinear(const std::string &path, const VtkGrid &g, const std::vector<VtkArray> &arrays,
+                       std::string &err) {
+    const int Nx = g.nref[0], Ny = g.nref[1], Nz = g.nref[2];
     const int zc = Nz;  // planes k = 1 .. Nz, as the reference writes (zcomp)
     const size_t ncell = (size_t)(Nx + 2) * (Ny + 2) * zc;
-    FILE *fp = fopen(j.path.c_str(), "wb");
+    FILE *fp = fopen(path.c_str(), "wb");
     if (!fp) {
-        o->result = LBM_ERR_INVALID;
-        o->error = "output_vtk: cannot open " + j.path;
-        return;
+        err = "cannot open " + path;
+        return false;
     }
     unsigned long offset = 0;
     fprintf(fp, "<?xml version=\"1.0\"?>\n");
@@ -118,7 +167,7 @@ void write_vtk(VtkJob j, lbm_output *o) {
     fprintf(fp, "    <PointData>\n");
     fprintf(fp, "    </PointData>\n");
     fprintf(fp, "    <CellData>\n");
-    auto arr = [&](const char *name, int comps) {
+    auto decl = [&](const char *name, int comps) {
         if (comps == 1)
             fprintf(fp, "      <DataArray type=\"Float32\" Name=\"%s\" format=\"appended\" offset=\"%ld\" />\n", name,
                     (long)offset);
@@ -129,14 +178,8 @@ void write_vtk(VtkJob j, lbm_output *o) {
                     name, comps, (long)offset);
         offset += 4 + (unsigned long)comps * 4 * ncell;
     };
-    arr("Density", 1);
-    arr("Velocity", 3);
-    if (j.force) arr("Force density", 3);
-    if (j.thermal) {
-        arr("Temperature", 1);
-        arr("Heat flux", 3);
-    }
-    arr("CellType", 1);
+    for (const VtkArray &a : arrays) decl(a.name, a.comps);
+    decl("CellType", 1);
     fprintf(fp, "    </CellData>\n");
     fprintf(fp, "    <Coordinates>\n");
     fprintf(fp, "      <DataArray type=\"Float32\" Name=\"CoordinateX\" format=\"appended\" offset=\"%ld\" />\n",
@@ -153,91 +196,41 @@ void write_vtk(VtkJob j, lbm_output *o) {
     fprintf(fp, "  <AppendedData encoding=\"raw\">");
     fprintf(fp, "_");
 
-    const long long N = j.N;
     const int NXr = Nx + 2, NYr = Ny + 2;
-    // device cell of reference cell (i, j, k), or -1 for a ghost (side[] set)
-    auto locate = [&](int i, int jj, int k, int side[3]) -> long long {
-        const int r[3] = {i, jj, k};
-        long long d[3];
-        bool ghost = false;
-        for (int a = 0; a < 3; a++) {
-            side[a] = -1;
-            const int v = r[a] - j.off[a];
-            if (v < 0) {
-                side[a] = 0;
-                ghost = true;
-            } else if (v >= j.dn[a]) {
-                side[a] = 1;
-                ghost = true;
-            }
-            d[a] = v;
-        }
-        if (ghost) return -1;
-        return d[0] + (long long)j.dn[0] * (d[1] + (long long)j.dn[1] * d[2]);
-    };
     std::vector<float> buf;
+    buf.reserve(9 * ncell);
     auto flush = [&](int comps) {
         const uint32_t bytes = (uint32_t)(comps * 4 * ncell);
         fwrite(&bytes, sizeof(uint32_t), 1, fp);
         fwrite(buf.data(), sizeof(float), buf.size(), fp);
         buf.clear();
     };
-    buf.reserve(3 * ncell);
-    // Density, Velocity (/ u_ref), Force density, Temperature, Heat flux
-    for (int field = 0; field < 5; field++) {
-        if (field == 2 && !j.force) continue;
-        if (field >= 3 && !j.thermal) continue;
-        const int comps = (field == 0 || field == 3) ? 1 : 3;
+    for (const VtkArray &a : arrays) {
         for (int k = 1; k <= zc; k++)
             for (int jj = 0; jj < NYr; jj++)
                 for (int i = 0; i < NXr; i++) {
                     int side[3];
-                    const long long c = locate(i, jj, k, side);
-                    float v[3] = {0.0f, 0.0f, 0.0f};
-                    if (c >= 0) {
-                        if (field == 0) v[0] = j.mom[c];
-                        if (field == 1)
-                            for (int a = 0; a < 3; a++) v[a] = (float)(j.mom[(1 + a) * N + c] / j.u_ref);
-                        if (field == 2) {
-                            for (int a = 0; a < 3; a++) v[a] = j.body[a];
-                            const int bx = (int)(c % j.dn[0]) - j.band_o[0];
-                            const int by = (int)((c / j.dn[0]) % j.dn[1]) - j.band_o[1];
-                            const int bz = (int)(c / ((long long)j.dn[0] * j.dn[1])) - j.band_o[2];
-                            if (j.band && (unsigned)bx < (unsigned)j.bs[0] && (unsigned)by < (unsigned)j.bs[1] &&
-                                (unsigned)bz < (unsigned)j.bs[2]) {
-                                const long long nb = (long long)j.bs[0] * j.bs[1] * j.bs[2];
-                                const long long b = bx + (long long)j.bs[0] * (by + (long long)j.bs[1] * bz);
-                                for (int a = 0; a < 3; a++) v[a] = j.band[(4 + a) * nb + b] + j.fsign * j.band[(7 + a) * nb + b];
-                            }
-                        }
-                        if (field == 3) v[0] = j.mom[4 * N + c];
-                        if (field == 4)
-                            for (int a = 0; a < 3; a++) v[a] = j.mom[(5 + a) * N + c];
-                    } else {
-                        const lbm_face *f = ghost_face(j.cfg, side);
-                        if (field == 0) v[0] = (float)f->rho;
-                        if (field == 1)
-                            for (int a = 0; a < 3; a++) v[a] = (float)(f->u[a] / j.u_ref);
-                        if (field == 3) v[0] = (float)f->T;
-                    }
-                    for (int a = 0; a < comps; a++) buf.push_back(v[a]);
+                    const long long c = g.locate(i, jj, k, side);
+                    float v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+                    a.value(c, c >= 0 ? nullptr : ghost_face(g.cfg, side), v);
+                    for (int q = 0; q < a.comps; q++) buf.push_back(v[q]);
                 }
-        flush(comps);
+        flush(a.comps);
     }
     // CellType: the float value of the reference's type code
     for (int k = 1; k <= zc; k++)
         for (int jj = 0; jj < NYr; jj++)
             for (int i = 0; i < NXr; i++) {
                 float t;
-                if (!j.types.empty()) {
-                    t = (float)j.types[(size_t)i + (size_t)NXr * ((size_t)jj + (size_t)NYr * k)];
+                if (!g.types.empty()) {
+                    t = (float)g.types[(size_t)i + (size_t)NXr * ((size_t)jj + (size_t)NYr * k)];
                 } else {
                     int side[3];
-                    const long long c = locate(i, jj, k, side);
+                    const long long c = g.locate(i, jj, k, side);
                     if (c >= 0)
-                        t = (!j.solid.empty() && ((j.solid[(size_t)(c >> 5)] >> (c & 31)) & 1u)) ? 1.0f : 0.0f;
+                        t = (!g.solid.empty() && ((g.solid[(size_t)(c >> 5)] >> (c & 31)) & 1u)) ? 1.0f : 0.0f;
                     else
-                        t = face_type(ghost_face(j.cfg, side)->kind);
+                        t = face_type(ghost_face(g.cfg, side)->kind);
                 }
                 buf.push_back(t);
             }
@@ -255,11 +248,92 @@ void write_vtk(VtkJob j, lbm_output *o) {
     fprintf(fp, "  </AppendedData>\n");
     fprintf(fp, "</VTKFile>\n");
     if (fclose(fp) != 0) {
-        o->result = LBM_ERR_INVALID;
-        o->error = "output_vtk: write failed: " + j.path;
+        err = "write failed: " + path;
+        return false;
     }
+    return true;
 }
 
+// sigma (6 distinct components, xx xy xz yy yz zz) as the 9 of a 3x3 tensor
+const int kSym9[9] = {0, 1, 2, 1, 3, 4, 2, 4, 5};
+
+// MORE_DETAILS arrays of a ghost cell: the face's equilibrium, whose central
+// second moment is rho cs^2 delta.
+float ghost_pressure(const lbm_face *gf) { return (float)(gf->rho / 3.0); }
+float ghost_stress_diag(const lbm_face *gf, double tau) { return (float)(-(tau - 0.5) * (gf->rho / 3.0) / tau); }
+
+struct VtkJob {
+    std::string path;
+    VtkGrid grid;
+    double u_ref, tau;
+    int thermal, force, details;
+    const float *mom;     // pinned moments
+    const float *band;    // pinned band snapshot (force density) or null
+    const float *det;     // pinned pressure and stress, or null
+    int band_o[3], bs[3];
+    float fsign;
+    float body[3];
+    cudaEvent_t copied;
+};
+
+void write_vtk(VtkJob j, lbm_output *o) {
+    if (cudaEventSynchronize(j.copied) != cudaSuccess) {
+        o->result = LBM_ERR_CUDA;
+        o->error = "output_vtk: copy failed";
+        return;
+    }
+    const long long N = j.grid.N;
+    const int *dn = j.grid.dn;
+    std::vector<VtkArray> arrays;
+    arrays.push_back({"Density", 1, [&](long long c, const lbm_face *gf, float *v) {
+                          v[0] = c >= 0 ? j.mom[c] : (float)gf->rho;
+                      }});
+    arrays.push_back({"Velocity", 3, [&](long long c, const lbm_face *gf, float *v) {
+                          for (int a = 0; a < 3; a++)
+                              v[a] = c >= 0 ? (float)(j.mom[(1 + a) * N + c] / j.u_ref) : (float)(gf->u[a] / j.u_ref);
+                      }});
+    if (j.force)
+        arrays.push_back({"Force density", 3, [&](long long c, const lbm_face *, float *v) {
+                              if (c < 0) return;
+                              for (int a = 0; a < 3; a++) v[a] = j.body[a];
+                              const int bx = (int)(c % dn[0]) - j.band_o[0];
+                              const int by = (int)((c / dn[0]) % dn[1]) - j.band_o[1];
+                              const int bz = (int)(c / ((long long)dn[0] * dn[1])) - j.band_o[2];
+                              if (j.band && (unsigned)bx < (unsigned)j.bs[0] && (unsigned)by < (unsigned)j.bs[1] &&
+                                  (unsigned)bz < (unsigned)j.bs[2]) {
+                                  const long long nb = (long long)j.bs[0] * j.bs[1] * j.bs[2];
+                                  const long long b = bx + (long long)j.bs[0] * (by + (long long)j.bs[1] * bz);
+                                  for (int a = 0; a < 3; a++)
+                                      v[a] = j.band[(4 + a) * nb + b] + j.fsign * j.band[(7 + a) * nb + b];
+                              }
+                          }});
+    if (j.details) {
+        // MORE_DETAILS arrays of OutputVTK (lbm.cpp:2342-2347, 2471-2527)
+        arrays.push_back({"Pressure", 1, [&](long long c, const lbm_face *gf, float *v) {
+                              v[0] = c >= 0 ? j.det[c] : ghost_pressure(gf);
+                          }});
+        arrays.push_back({"Viscous Stress", 9, [&](long long c, const lbm_face *gf, float *v) {
+                              for (int q = 0; q < 9; q++)
+                                  v[q] = c >= 0 ? j.det[(1 + kSym9[q]) * N + c]
+                                                : ((q % 4 == 0) ? ghost_stress_diag(gf, j.tau) : 0.0f);
+                          }});
+        arrays.push_back({"Vorticity", 3, [&](long long, const lbm_face *, float *) {}});
+    }
+    if (j.thermal) {
+        arrays.push_back({"Temperature", 1, [&](long long c, const lbm_face *gf, float *v) {
+                              v[0] = c >= 0 ? j.mom[4 * N + c] : (float)gf->T;
+                          }});
+        arrays.push_back({"Heat flux", 3, [&](long long c, const lbm_face *, float *v) {
+                              if (c >= 0)
+                                  for (int a = 0; a < 3; a++) v[a] = j.mom[(5 + a) * N + c];
+                          }});
+    }
+    std::string err;
+    if (!write_rectilinear(j.path, j.grid, arrays, err)) {
+        o->result = LBM_ERR_INVALID;
+        o->error = "output_vtk: " + err;
+    }
+}
 }  // namespace
 
 cudaError_t lbm_mom_acquire(lbm_handle *h) {
@@ -300,7 +374,8 @@ extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, d
     const int nmom = h->cfg.thermal ? 8 : 5;
     const bool force = h->ibm;
     const size_t nb = force ? (size_t)h->P.nb : 0;
-    const size_t need = (size_t)nmom * N + 12 * nb;
+    const size_t ndet = h->details ? (size_t)LBM_DETAIL_COUNT * N : 0;
+    const size_t need = (size_t)nmom * N + 12 * nb + ndet;
     if (o->host_floats < need) {
         if (o->host) cudaFreeHost(o->host);
         o->host = nullptr;
@@ -309,36 +384,36 @@ extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, d
             return out_fail(LBM_ERR_NOMEM, "output_vtk: pinned staging allocation failed");
         o->host_floats = need;
     }
-    // snapshot on the main stream: the export pass, and the band (small,
-    // and rewritten by the next step)
-    if (lbm_export_moments_async(h) != cudaSuccess) return out_fail(LBM_ERR_CUDA, "output_vtk: export failed");
-    if (force && cudaMemcpyAsync(o->host + (size_t)nmom * N, h->band, 12 * nb * sizeof(float),
-                                 cudaMemcpyDeviceToHost, h->s) != cudaSuccess)
+    float *host_band = o->host + (size_t)nmom * N;
+    float *host_det = host_band + 12 * nb;
+    // snapshot on the main stream: the export pass (and the MORE_DETAILS
+    // pass), and the band (small, and rewritten by the next step)
+    const cudaError_t ex = h->details ? lbm_details_async(h, 0, 0.0, 1.0) : lbm_export_moments_async(h);
+    if (ex != cudaSuccess) return out_fail(LBM_ERR_CUDA, "output_vtk: export failed");
+    if (force && cudaMemcpyAsync(host_band, h->band, 12 * nb * sizeof(float), cudaMemcpyDeviceToHost, h->s) !=
+                     cudaSuccess)
         return out_fail(LBM_ERR_CUDA, "output_vtk: band copy failed");
     if (cudaEventRecord(o->exported, h->s) != cudaSuccess ||
         cudaStreamWaitEvent(o->copy, o->exported, 0) != cudaSuccess ||
         cudaMemcpyAsync(o->host, h->mom, (size_t)nmom * N * sizeof(float), cudaMemcpyDeviceToHost, o->copy) !=
             cudaSuccess ||
+        (ndet && cudaMemcpyAsync(host_det, h->det, ndet * sizeof(float), cudaMemcpyDeviceToHost, o->copy) !=
+                     cudaSuccess) ||
         cudaEventRecord(o->copied, o->copy) != cudaSuccess)
         return out_fail(LBM_ERR_CUDA, "output_vtk: copy failed");
     o->copy_issued = true;
     VtkJob j;
     j.path = path;
-    j.cfg = h->cfg;
-    j.N = N;
-    for (int a = 0; a < 3; a++) {
-        j.dn[a] = a == 0 ? h->P.nx : (a == 1 ? h->P.ny : h->P.nz);
-        const bool per = h->cfg.faces[2 * a].kind == LBM_FACE_PERIODIC;
-        j.off[a] = per ? 0 : 1;
-        j.nref[a] = per ? j.dn[a] - 2 : j.dn[a];
-        j.body[a] = (float)h->cfg.body_force[a];
-    }
+    j.grid = grid_of(h);
+    for (int a = 0; a < 3; a++) j.body[a] = (float)h->cfg.body_force[a];
     j.u_ref = u_ref;
+    j.tau = h->cfg.tau;
     j.thermal = h->cfg.thermal;
     j.force = force;
-    j.solids = h->solids;
+    j.details = h->details;
     j.mom = o->host;
-    j.band = force ? o->host + (size_t)nmom * N : nullptr;
+    j.band = force ? host_band : nullptr;
+    j.det = h->details ? host_det : nullptr;
     j.fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
     j.bs[0] = h->P.bsx;
     j.bs[1] = h->P.bsy;
@@ -350,18 +425,89 @@ extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, d
             return out_fail(LBM_ERR_CUDA, "output_vtk: state read failed");
         for (int a = 0; a < 3; a++) j.band_o[a] = d.band_o[a];
     }
-    if (types) {
-        const size_t nt = (size_t)(j.nref[0] + 2) * (j.nref[1] + 2) * (j.nref[2] + 2);
-        j.types.assign(types, types + nt);
-    } else if (h->solids) {
-        const size_t words = (size_t)((N + 31) / 32);
-        j.solid.resize(words);
-        if (cudaMemcpyAsync(j.solid.data(), h->solid_d, words * 4, cudaMemcpyDeviceToHost, h->s) != cudaSuccess ||
-            cudaStreamSynchronize(h->s) != cudaSuccess)
-            return out_fail(LBM_ERR_CUDA, "output_vtk: solid mask read failed");
-    }
+    if (!grid_types(h, j.grid, types)) return out_fail(LBM_ERR_CUDA, "output_vtk: solid mask read failed");
     j.copied = o->copied;
     o->writer = std::thread(write_vtk, std::move(j), o);
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
+    if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_avg_vtk: bad argument");
+    if (!h->details) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_set_more_details first");
+    if (!h->inited) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_init first");
+    if (h->out) {
+        lbm_status prev = join_writer(h->out);
+        if (prev != LBM_OK) return prev;
+    }
+    const long long N = h->P.N;
+    std::vector<float> mom((size_t)4 * N), det((size_t)LBM_DETAIL_COUNT * N);
+    std::vector<double> st((size_t)LBM_STAT_COUNT * N);
+    cudaError_t e = lbm_details_async(h, 0, 0.0, 1.0);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(mom.data(), h->mom, mom.size() * sizeof(float), cudaMemcpyDeviceToHost, h->s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(det.data(), h->det, det.size() * sizeof(float), cudaMemcpyDeviceToHost, h->s);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(st.data(), h->stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+    if (e != cudaSuccess) return out_fail(LBM_ERR_CUDA, std::string("output_avg_vtk: ") + cudaGetErrorString(e));
+    VtkGrid g = grid_of(h);
+    if (!grid_types(h, g, types)) return out_fail(LBM_ERR_CUDA, "output_avg_vtk: solid mask read failed");
+    const double tau = h->cfg.tau, u2 = u_ref * u_ref;
+    const bool sampled = h->stat_samples > 0;
+    const double told = h->stat_told;
+    // a ghost keeps its face state from the first sample on: the averages
+    // are that state, the velocity rms and averaged fluctuations zero, the
+    // Reynolds-stress rms |u_a u_b| and the pressure rms p sqrt(told / (told + 1))
+    auto stat = [&](long long c, int k) { return c >= 0 ? st[(size_t)k * N + c] : 0.0; };
+    auto vel = [&](double x) { return (float)((double)(float)x / u_ref); };
+    auto rs = [&](double x) { return (float)((double)(float)x / u2); };
+    std::vector<VtkArray> arrays;
+    arrays.push_back({"Density", 1, [&](long long c, const lbm_face *gf, float *v) {
+                          v[0] = c >= 0 ? mom[c] : (float)gf->rho;
+                      }});
+    arrays.push_back({"Velocity", 3, [&](long long c, const lbm_face *gf, float *v) {
+                          for (int a = 0; a < 3; a++) v[a] = c >= 0 ? vel(mom[(1 + a) * N + c]) : vel(gf->u[a]);
+                      }});
+    arrays.push_back({"Avg velocity", 3, [&](long long c, const lbm_face *gf, float *v) {
+                          for (int a = 0; a < 3; a++)
+                              v[a] = c >= 0 ? vel(stat(c, LBM_STAT_AVG_U + a)) : (sampled ? vel(gf->u[a]) : 0.0f);
+                      }});
+    arrays.push_back({"Rms velocity", 3, [&](long long c, const lbm_face *, float *v) {
+                          for (int a = 0; a < 3; a++) v[a] = vel(stat(c, LBM_STAT_RMS_U + a));
+                      }});
+    arrays.push_back({"Pressure", 1, [&](long long c, const lbm_face *gf, float *v) {
+                          v[0] = c >= 0 ? det[c] : ghost_pressure(gf);
+                      }});
+    arrays.push_back({"Avg pressure", 1, [&](long long c, const lbm_face *gf, float *v) {
+                          v[0] = c >= 0 ? (float)stat(c, LBM_STAT_AVG_P) : (sampled ? (float)(gf->rho / 3.0) : 0.0f);
+                      }});
+    arrays.push_back({"Rms pressure", 1, [&](long long c, const lbm_face *gf, float *v) {
+                          if (c >= 0) {
+                              v[0] = (float)stat(c, LBM_STAT_RMS_P);
+                          } else if (sampled) {
+                              const double p = gf->rho / 3.0;
+                              v[0] = (float)sqrt(p * p * told / (told + 1.0));
+                          }
+                      }});
+    arrays.push_back({"Viscous Stress", 9, [&](long long c, const lbm_face *gf, float *v) {
+                          for (int q = 0; q < 9; q++)
+                              v[q] = c >= 0 ? det[(1 + kSym9[q]) * N + c]
+                                            : ((q % 4 == 0) ? ghost_stress_diag(gf, tau) : 0.0f);
+                      }});
+    for (const char *name : {"Vorticity", "Avg vorticity", "Rms vorticity"})
+        arrays.push_back({name, 3, [&](long long, const lbm_face *, float *) {}});
+    arrays.push_back({"Avg reynolds Stress", 9, [&](long long c, const lbm_face *, float *v) {
+                          for (int q = 0; q < 9; q++) v[q] = rs(stat(c, LBM_STAT_AVG_RS + kSym9[q]));
+                      }});
+    arrays.push_back({"Rms reynolds Stress", 9, [&](long long c, const lbm_face *gf, float *v) {
+                          static const int ia[9] = {0, 0, 0, 1, 1, 1, 2, 2, 2}, ib[9] = {0, 1, 2, 0, 1, 2, 0, 1, 2};
+                          for (int q = 0; q < 9; q++)
+                              v[q] = c >= 0 ? rs(stat(c, LBM_STAT_RMS_RS + kSym9[q]))
+                                            : (sampled ? rs(fabs(gf->u[ia[q]] * gf->u[ib[q]])) : 0.0f);
+                      }});
+    std::string err;
+    if (!write_rectilinear(path, g, arrays, err)) return out_fail(LBM_ERR_INVALID, "output_avg_vtk: " + err);
     return LBM_OK;
 }
 

@@ -476,3 +476,83 @@ def read_dropin_cavity(path: str, n: int) -> dict:
     """Read the dump of the facade driver dropin_cavity (rho, ux, uy, uz, x fastest)."""
     a = np.fromfile(path, dtype=np.float64).reshape(4, n, n, n)
     return {"rho": a[0], "ux": a[1], "uy": a[2], "uz": a[3]}
+
+
+# --------------------------------------------------------------------------
+# MORE_DETAILS (LBM.h:55): pressure, viscous stress, running statistics
+# --------------------------------------------------------------------------
+
+# the six distinct components of a symmetric 3x3 tensor, in this order
+SYM6 = ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))
+
+
+def details(lat: Lattice) -> dict:
+    """The MORE_DETAILS part of LBM::MacroProp (lbm.cpp:681-705) over every
+    cell, ghosts included, after lat.macro(): pressure = density / 3 and
+    sigma[a][b] = -(tau - 0.5) * sum_l f_l (c_la - u_a)(c_lb - u_b) / tau,
+    summed over l in the reference order.  sigma is returned as the six
+    distinct components (SYM6 order), shape (6, NZ, NY, NX)."""
+    c = (CX19, CY19, CZ19)
+    u = (lat.ux, lat.uy, lat.uz)
+    f = lat.f
+    sig = np.empty((6,) + lat.shape)
+    for s, (a, b) in enumerate(SYM6):
+        acc = np.zeros(lat.shape)
+        for l in range(19):
+            acc = acc + f[l] * (c[a][l] - u[a]) * (c[b][l] - u[b])
+        sig[s] = -(lat.tau - 0.5) * acc / lat.tau
+    return {"p": lat.rho / 3.0, "sigma": sig}
+
+
+class SupStats:
+    """The running statistics of LBM::Sup_MacroProp (lbm.cpp:865-939), FP64,
+    on arrays of any shape.  update(n, ...) is the call made at reference
+    step n (main.cpp:389, every nt steps) with told = (n - nt) dt.  The
+    reference's own weights are kept: the velocity average weights the new
+    sample by dt, every other average by 1; the pressure rms squares the
+    current pressure where the other rms values square their previous rms
+    (lbm.cpp:913); the Reynolds-stress rms takes u_a u_b minus the averaged
+    fluctuation product.  Vorticity is never computed by the reference (its
+    code is commented out, lbm.cpp:712-770), so its averages and rms stay 0
+    and are not carried.  avg_rs / rms_rs hold the six distinct components
+    (SYM6 order): the reference's [b][a] entries are bitwise equal to them."""
+
+    def __init__(self, shape):
+        z = lambda k: np.zeros((k,) + tuple(shape))  # noqa: E731
+        self.avg_u, self.avg_p, self.avg_rs = z(3), np.zeros(shape), z(6)
+        self.rms_u, self.rms_p, self.rms_rs = z(3), np.zeros(shape), z(6)
+
+    def update(self, n: int, nt: int, dt: float, u, p) -> None:
+        told = (n - nt) * dt
+        for a in range(3):
+            self.avg_u[a] = (self.avg_u[a] * told + u[a] * dt) / (told + dt)
+        self.avg_p = (self.avg_p * told + p * 1) / (told + 1)
+        d = [u[a] - self.avg_u[a] for a in range(3)]
+        for s, (a, b) in enumerate(SYM6):
+            self.avg_rs[s] = (self.avg_rs[s] * told + d[a] * d[b] * 1) / (told + 1)
+        for a in range(3):
+            self.rms_u[a] = np.sqrt((self.rms_u[a] * self.rms_u[a] * told + d[a] * d[a] * 1) / (told + 1))
+        dp = p - self.avg_p
+        self.rms_p = np.sqrt((p * p * told + dp * dp * 1) / (told + 1))
+        for s, (a, b) in enumerate(SYM6):
+            e = u[a] * u[b] - self.avg_rs[s]
+            self.rms_rs[s] = np.sqrt((self.rms_rs[s] * self.rms_rs[s] * told + e * e * 1) / (told + 1))
+
+
+def cavity_details_run(n: int, tau: float, lid: float, steps: int, nt: int = 10):
+    """The MORE_DETAILS cavity run: Collision, Streaming, MacroProp every
+    step and Sup_MacroProp every nt steps (main.cpp:214-223, 389).  Returns
+    the lattice, the last details() and the statistics, ghosts included."""
+    lat = cavity(n, tau, lid)
+    stats = SupStats(lat.shape)
+    det = None
+    for s in range(1, steps + 1):
+        lat.collide()
+        lat.stream()
+        lat.macro()
+        if s % nt == 0:
+            det = details(lat)
+            stats.update(s, nt, 1.0, (lat.ux, lat.uy, lat.uz), det["p"])
+    if det is None:
+        det = details(lat)
+    return lat, det, stats

@@ -8,6 +8,7 @@
 #
 # usage: oracle/build_ref.sh [variant ...]
 #   cavity:N[:TAU]            D3Q19 cavity, N^3 interior
+#   details:N[:TAU]           the same cavity in MORE_DETAILS mode
 #   cylinder:NX:NY:D:NODES:M  D2Q9 implicit IBM cylinder
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
 set -e
@@ -19,7 +20,7 @@ if [ ! -f "$REF/lbm.cpp" ]; then
     exit 0
 fi
 mkdir -p "$OUT"
-[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05
+[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05 details:8:0.8
 CXX=${CXX:-g++}
 FLAGS="-O2 -fopenmp -ffp-contract=off -w -include $HERE/ref_config.h -I$HERE/shim -I$REF"
 pids=""
@@ -30,6 +31,12 @@ for v in "$@"; do
         n=$(echo "$v" | cut -d: -f2); tau=$(echo "$v" | cut -d: -f3); [ -z "$tau" ] && tau=0.8
         exe="$OUT/ref_cavity_${n}_${tau}"
         $CXX $FLAGS -DREF_CAVITY -DREF_NX=$n -DREF_NY=$n -DREF_NZ=$n -DREF_TAU=$tau \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    details)
+        n=$(echo "$v" | cut -d: -f2); tau=$(echo "$v" | cut -d: -f3); [ -z "$tau" ] && tau=0.8
+        exe="$OUT/ref_details_${n}_${tau}"
+        $CXX $FLAGS -DREF_CAVITY -DREF_DETAILS -DREF_NX=$n -DREF_NY=$n -DREF_NZ=$n -DREF_TAU=$tau \
             -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     cylinder)

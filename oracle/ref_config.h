@@ -16,7 +16,9 @@
  *                 REF_RE and REF_U set the diameter, Reynolds number and
  *                 inflow velocity.
  * Sizes come from REF_NX/REF_NY/REF_NZ/REF_TAU (and REF_D, REF_NODES,
- * REF_MMAX for the cylinder).
+ * REF_MMAX for the cylinder).  REF_DETAILS (with REF_CAVITY) also switches on
+ * the reference's MORE_DETAILS mode (LBM.h:55): pressure, viscous stress and
+ * the Sup_MacroProp running averages.
  */
 #include <cmath>
 #include <iostream>
@@ -35,6 +37,10 @@ static const double PI = 3.14159265;  // LBM.h:74
 static const double cs2 = pow(dx, 2) / (3 * pow(dt, 2));
 #define p0 rho0 *cs2
 #define Conventional_LBM
+
+#if defined REF_DETAILS
+#define MORE_DETAILS
+#endif
 
 #define TYPE_F 0
 #define TYPE_S 1

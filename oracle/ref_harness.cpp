@@ -8,8 +8,10 @@
 //     IBLBM in the order of main.cpp:195-221,
 //   - times only the step loop (wall clock), and
 //   - dumps rho, u (and F, Cl, Cd for the IBM case; Cl, Cd of the
-//     momentum exchange after every step for the staircase sphere) as raw
-//     doubles, x fastest, ghost layers included.
+//     momentum exchange after every step for the staircase sphere; in
+//     MORE_DETAILS mode the pressure, the viscous stress and the
+//     Sup_MacroProp averages and rms values) as raw doubles, x fastest, ghost
+//     layers included.
 #include "LBM.h"
 
 #include <omp.h>
@@ -34,6 +36,21 @@ static void dump_field(LBM &lb, FILE *fp, int which) {
                 case 4: v = c.F[0]; break;
                 case 5: v = c.F[1]; break;
                 case 6: v = c.F[2]; break;
+#if defined MORE_DETAILS
+                // 7: pressure; 8..16: sigma[a][b]; 17..19: avg_velocity;
+                // 20: avg_pressure; 21..29: avg_ReynoldStress; 30..32:
+                // rms_velocity; 33: rms_pressure; 34..42: rms_ReynoldStress
+                case 7: v = c.pressure; break;
+                case 20: v = c.avg_pressure; break;
+                case 33: v = c.rms_pressure; break;
+                default:
+                    if (which >= 8 && which <= 16) v = c.sigma[(which - 8) / 3][(which - 8) % 3];
+                    if (which >= 17 && which <= 19) v = c.avg_velocity[which - 17];
+                    if (which >= 21 && which <= 29) v = c.avg_ReynoldStress[(which - 21) / 3][(which - 21) % 3];
+                    if (which >= 30 && which <= 32) v = c.rms_velocity[which - 30];
+                    if (which >= 34 && which <= 42) v = c.rms_ReynoldStress[(which - 34) / 3][(which - 34) % 3];
+                    break;
+#endif
                 }
                 buf[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = v;
             }
@@ -65,11 +82,18 @@ int main(int argc, char **argv) {
         lb.Collision();
         lb.Streaming();
         lb.MacroProp();
+#if defined MORE_DETAILS
+        // the call of main.cpp:389, made at the output cadence (main.cpp:223)
+        if (s % Nt == 0) lb.Sup_MacroProp(s);
+#endif
     }
     double t1 = omp_get_wtime();
     FILE *fp = fopen(out, "wb");
     if (!fp) return 3;
     for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+#if defined MORE_DETAILS
+    for (int w = 7; w <= 42; w++) dump_field(lb, fp, w);
+#endif
     fclose(fp);
     if (argc > 4) {
         // the reference's own VTK writer (lbm.cpp:2290-2642): ./field000000.vtr

@@ -20,6 +20,14 @@ outputs are stored as small .npz fixtures:
                                     k = 12 and j = 12 of rho, u, interior
                                     sums and maxima, momentum-exchange Cl
                                     and Cd after every step
+  cavity8_details_200.npz           the 8^3 cavity (tau = 0.8, lid 0.05)
+                                    built in MORE_DETAILS mode, 200 steps,
+                                    Sup_MacroProp every 10 steps: every
+                                    cell (ghosts included) of rho, u,
+                                    pressure, the 6 distinct viscous
+                                    stresses, the running averages and rms
+                                    values; and that run's OutputVTK file
+                                    (vtk_* keys)
 
 Run from the repository root:  python tests/golden/gen_golden.py
 (needs the reference tree; the 64^3 case takes a few minutes on 8 cores;
@@ -68,7 +76,8 @@ def main() -> None:
     ap.add_argument("--cav64-dump", default=None)
     ap.add_argument("--skip-cav64", action="store_true")
     a = ap.parse_args()
-    oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05")
+    oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
+                     "details:8:0.8")
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -109,6 +118,27 @@ def main() -> None:
                         ymid=f[:, :, 12, :], sums=f.reshape(4, -1).sum(axis=1),
                         absmax=np.abs(f.reshape(4, -1)).max(axis=1), cl=r["cl"], cd=r["cd"], nx=48, ny=24, nz=24,
                         D=8.0, Re=20.0, u=0.05, steps=steps)
+    # MORE_DETAILS cavity, 200 steps (averages sampled every Nt = 10 steps)
+    d = os.path.join(tmp, "det")
+    os.makedirs(d)
+    p = os.path.join(d, "det.bin")
+    subprocess.check_call([os.path.join(REF, "ref_details_8_0.8"), "200", p, "0.05", "vtk"], cwd=d)
+    # dump order: rho, u, then pressure, sigma[3][3], avg_velocity,
+    # avg_pressure, avg_ReynoldStress, rms_velocity, rms_pressure,
+    # rms_ReynoldStress
+    f = oracle.read_ref_dump(p, 10, 10, 10, 40)["fields"]
+    sym = {}
+    for base, name in ((5, "sigma"), (18, "avg_rs"), (31, "rms_rs")):
+        t = f[base:base + 9].reshape(3, 3, 10, 10, 10)
+        for a in range(3):
+            for b in range(a):
+                assert np.array_equal(t[a, b], t[b, a]), (name, a, b)
+        sym[name] = np.stack([t[0, 0], t[0, 1], t[0, 2], t[1, 1], t[1, 2], t[2, 2]])
+    v = read_vtr(os.path.join(d, "field000000.vtr"))
+    np.savez_compressed(os.path.join(OUT, "cavity8_details_200.npz"), rho=f[0], u=f[1:4], p=f[4],
+                        sigma=sym["sigma"], avg_u=f[14:17], avg_p=f[17], avg_rs=sym["avg_rs"], rms_u=f[27:30],
+                        rms_p=f[30], rms_rs=sym["rms_rs"], n=8, tau=0.8, lid=0.05, steps=200, nt=10,
+                        **{"vtk_" + k: a for k, a in v.items()})
     print("golden fixtures written to", OUT)
 
 

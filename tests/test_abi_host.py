@@ -107,3 +107,14 @@ def test_output_csv_reference_format(pkg, tmp_path):
     p = str(tmp_path / "cd.csv")
     pkg.output_csv(p, [1.5, 0.25, 3e-7], 0.5)
     assert open(p).read() == "time,error\n0.5,1.5\n1,0.25\n1.5,3e-07\n"
+
+
+def test_more_details_entry_points_reject_null_handles(pkg):
+    """The MORE_DETAILS calls check their arguments before any device work."""
+    L = pkg.load()
+    assert L.lbmgpu_set_more_details(None, 1) == 1
+    assert L.lbmgpu_sup_macroprop(None, 10, 10, 1.0) == 1
+    assert L.lbmgpu_download_details(None, None) == 1
+    assert L.lbmgpu_download_stats(None, None, None, None) == 1
+    assert L.lbmgpu_output_avg_vtk(None, b"x.vtr", 0.1, None) == 1
+    assert "null" in L.lbmgpu_last_error().decode() or "bad argument" in L.lbmgpu_last_error().decode()

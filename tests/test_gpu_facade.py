@@ -61,3 +61,30 @@ def test_dropin_staircase_sphere_loop(drivers, tmp_path):
     scale = np.abs(g["cd"]).max()
     assert np.abs(r[:, 2] - g["cd"]).max() / scale < 1e-4
     assert np.abs(r[:, 1] - g["cl"]).max() / scale < 1e-4
+
+
+def test_dropin_more_details_loop(drivers, pkg, tmp_path):
+    """The loop of a MORE_DETAILS build (Sup_MacroProp every Nt steps,
+    main.cpp:389), through the facade compiled with -DMORE_DETAILS: the
+    LATTICE fields pressure, sigma, avg_* and rms_* against the reference's
+    own MORE_DETAILS run, and its OutputAVGVTK file."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "cavity8_details_200.npz"))
+    n, steps = int(g["n"]), int(g["steps"])
+    out = str(tmp_path / "det.bin")
+    subprocess.check_call([drivers["dropin_details"], str(n), str(steps), out], cwd=str(tmp_path))
+    a = np.fromfile(out, dtype=np.float64).reshape(36, n, n, n)
+    inner = (Ellipsis, slice(1, -1), slice(1, -1), slice(1, -1))
+    sym9 = [0, 1, 2, 1, 3, 4, 2, 4, 5]
+    lid = float(g["lid"])
+    assert np.abs(a[0] - g["p"][inner]).max() < 1e-7
+    assert np.abs(a[1:10] - g["sigma"][sym9][inner]).max() < 1e-7
+    assert np.abs(a[10:13] - g["avg_u"][inner]).max() < 2e-6 * lid
+    assert np.abs(a[13] - g["avg_p"][inner]).max() < 1e-7
+    assert np.abs(a[14:23] - g["avg_rs"][sym9][inner]).max() < 2e-6 * lid * lid
+    assert np.abs(a[23:26] - g["rms_u"][inner]).max() < 2e-6 * lid
+    assert np.abs(a[26] - g["rms_p"][inner]).max() < 1e-7
+    assert np.abs(a[27:36] - g["rms_rs"][sym9][inner]).max() < 2e-6 * lid * lid
+    v = pkg.read_vtr(str(tmp_path / "avgfield.vtr"))
+    assert "Avg reynolds Stress" in v and v["CellType"].shape == ((n + 2) * (n + 2) * n,)

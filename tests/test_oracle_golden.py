@@ -117,3 +117,24 @@ def test_staircase_sphere_mea_matches_reference(orc):
     assert np.abs(f[:, 12] - g["zmid"]).max() < 1e-12
     assert np.abs(f[:, :, 12] - g["ymid"]).max() < 1e-12
     assert np.allclose(f.reshape(4, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
+
+
+def test_more_details_match_reference(orc):
+    """MORE_DETAILS mode of the reference (LBM.h:55) on the 8^3 cavity: the
+    pressure and viscous stress of MacroProp (lbm.cpp:681-705) and the
+    Sup_MacroProp running averages / rms values (lbm.cpp:865-939, called every
+    Nt = 10 steps) at every cell, ghosts included.  The restatement sums in
+    the reference's order: bit-exact."""
+    g = np.load(os.path.join(GOLDEN, "cavity8_details_200.npz"))
+    lat, det, st = orc.cavity_details_run(int(g["n"]), float(g["tau"]), float(g["lid"]), int(g["steps"]),
+                                          int(g["nt"]))
+    assert np.array_equal(lat.rho, g["rho"])
+    assert np.array_equal(np.stack([lat.ux, lat.uy, lat.uz]), g["u"])
+    assert np.array_equal(det["p"], g["p"])
+    assert np.array_equal(det["sigma"], g["sigma"])
+    for k in ("avg_u", "avg_p", "avg_rs", "rms_u", "rms_p", "rms_rs"):
+        assert np.array_equal(getattr(st, k), g[k]), k
+    # the reference's pressure-rms weighting (the current pressure squared
+    # where the other rms values square their previous rms): on a ghost cell
+    # at rest p = 1/3 and rms_p = p sqrt(told / (told + 1)), told = 190
+    assert abs(g["rms_p"][0, 0, 0] - np.sqrt(190.0 / 191.0) / 3.0) < 1e-15
