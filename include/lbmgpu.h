@@ -102,7 +102,18 @@ typedef struct lbm_config {
                              stream); <0: serial */
     int xface;            /* 0: lanes on x = 0 / x = nx-1 keep the plain pull and redo their five
                              x-crossing links; <0: their whole warp takes the boundary-class path */
+    int lattice;          /* LBM_LATTICE_*: 0 or 19 = D3Q19; 9 = D2Q9 (the reference's #define D2Q9
+                             build; nz = 1, faces 4/5 unused) */
 } lbm_config;
+
+enum { LBM_LATTICE_D3Q19 = 19, LBM_LATTICE_D2Q9 = 9 };
+
+/* Prescribed body velocity V_CM(t) of a two-dimensional IBM body (IBLBM,
+ * lbm.cpp:1140-1151), t = step * dt: FIXED 0 (Cylinder_IBM); CONSTANT the
+ * lbm_ibm_config velocity (Cylinder_IBM_Moving_Arbie); INLINE_OSC
+ * V_x = -amp cos(2 pi f t) (Cylinder_Inline_Oscillating); TRANSVERSE_OSC
+ * V_y = -2 pi f amp sin(2 pi f t) (Cylinder_Transverse_Oscillation). */
+enum { LBM_MOTION_FIXED = 0, LBM_MOTION_CONSTANT = 1, LBM_MOTION_INLINE_OSC = 2, LBM_MOTION_TRANSVERSE_OSC = 3 };
 
 typedef struct lbm_ibm_config {
     int n_markers;
@@ -119,6 +130,15 @@ typedef struct lbm_ibm_config {
     double velocity[3];   /* initial body velocity */
     double T_body;        /* marker temperature for the thermal IBM */
     int free_dofs;        /* free body: bits 0-2 translation x,y,z, bits 3-5 rotation; 0 = all six */
+    /* D2Q9 handles: the options of the reference's two-dimensional IBLBM */
+    int rho_nearest;      /* 1: marker density at NearestLatticeCoordinate over the whole box
+                             (lbm.cpp:1315-1317; needs normals); 0: delta-interpolated */
+    int added_mass;       /* 1: Drag/Lift += rho_avg V_s (V - V_before) / dt with rho_avg of
+                             Calc_AverageDensity (lbm.cpp:1105-1132, 1392-1398; needs normals) */
+    int motion;           /* LBM_MOTION_* */
+    double motion_amp, motion_freq;
+    int scheme;           /* 0: implicit multi-direct forcing (lbm.cpp:1259-1390);
+                             1: explicit direct forcing (lbm.cpp:1171-1258) */
 } lbm_ibm_config;
 
 typedef struct lbm_handle lbm_handle;
@@ -135,6 +155,12 @@ lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const ui
                                     const double *ux, const double *uy, const double *uz, const double *T,
                                     lbm_config *out);
 
+/* The same for the reference's D2Q9 build (Nz = 1): arrays of (nx+2)(ny+2)
+ * entries, x fastest, the computational layer fluid[i][j][1].  The result
+ * has lattice = LBM_LATTICE_D2Q9 and nz = 1. */
+lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, const uint8_t *types, const double *rho,
+                                       const double *ux, const double *uy, lbm_config *out);
+
 lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out);
 lbm_status lbmgpu_destroy(lbm_handle *h);
 
@@ -149,6 +175,10 @@ lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const double *ux
  * the body velocity). */
 lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *ds,
                               const double *udes);
+/* Outward marker normals ([3][n], MARKER::normal, lbm.cpp:1048-1069) for
+ * the nearest-node density and the added-mass average of a D2Q9 handle;
+ * call after lbmgpu_set_markers. */
+lbm_status lbmgpu_set_marker_normals(lbm_handle *h, const double *nxyz);
 
 /* Advance n reference iterations (IBLBM -> Collision -> Streaming, or
  * Collision -> Streaming -> MacroProp).  Asynchronous on the handle's stream. */

@@ -24,6 +24,9 @@ LIB_PATH = os.path.join(HERE, "liblbmgpu.so")
 STORE_F32, STORE_F16, STORE_BF16 = 0, 1, 2
 STORAGE = {"f32": STORE_F32, "f16": STORE_F16, "bf16": STORE_BF16}
 FACE_WALL, FACE_INLET, FACE_OUTLET_EQ, FACE_OUTLET_ZG, FACE_PERIODIC = 0, 1, 2, 3, 4
+LATTICE_D3Q19, LATTICE_D2Q9 = 19, 9
+# prescribed motion of a D2Q9 IBM body (IBLBM, lbm.cpp:1140-1151)
+MOTION_FIXED, MOTION_CONSTANT, MOTION_INLINE_OSC, MOTION_TRANSVERSE_OSC = 0, 1, 2, 3
 TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
 FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
 # MORE_DETAILS: the six distinct stress components, and the statistics rows
@@ -44,7 +47,7 @@ ABI_SYMBOLS = [
     "lbmgpu_set_solids", "lbmgpu_get_solid_forces", "lbmgpu_output_vtk_async", "lbmgpu_output_wait",
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
-    "lbmgpu_output_avg_vtk",
+    "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
 ]
 
 
@@ -60,7 +63,7 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("xface", C.c_int)]
+                ("xface", C.c_int), ("lattice", C.c_int)]
 
 
 class IbmConfig(C.Structure):
@@ -68,7 +71,8 @@ class IbmConfig(C.Structure):
                 ("thermal", C.c_int), ("radius", C.c_double), ("center", C.c_double * 3),
                 ("density_ratio", C.c_double), ("volume", C.c_double), ("inertia", C.c_double),
                 ("gravity", C.c_double * 3), ("velocity", C.c_double * 3), ("T_body", C.c_double),
-                ("free_dofs", C.c_int)]
+                ("free_dofs", C.c_int), ("rho_nearest", C.c_int), ("added_mass", C.c_int), ("motion", C.c_int),
+                ("motion_amp", C.c_double), ("motion_freq", C.c_double), ("scheme", C.c_int)]
 
 
 class ServeRequest(C.Structure):
@@ -155,6 +159,8 @@ def load(path: str | None = None):
     L.lbmgpu_sup_macroprop.argtypes = [vp, i, i, d]
     L.lbmgpu_download_stats.argtypes = [vp, dp, C.POINTER(i), dp]
     L.lbmgpu_output_avg_vtk.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
+    L.lbmgpu_config_from_types_2d.argtypes = [i, i, d, C.POINTER(C.c_uint8), dp, dp, dp, C.POINTER(Config)]
+    L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
     L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
@@ -254,7 +260,12 @@ class Solver:
 
     def set_markers(self, xyz, ds, radius, center, m_max=5, literal_sign=False, free_body=False, udes=None,
                     density_ratio=0.0, volume=0.0, inertia=0.0, gravity=(0, 0, 0), velocity=(0, 0, 0),
-                    thermal=False, T_body=0.0, free_dofs=0):
+                    thermal=False, T_body=0.0, free_dofs=0, normals=None, rho_nearest=False, added_mass=False,
+                    motion=0, motion_amp=0.0, motion_freq=0.0, scheme=0):
+        """Markers of an immersed body.  The last group of options applies to
+        D2Q9 handles (the reference's two-dimensional IBLBM): normals [3][n]
+        for the nearest-node density and the added mass, the motion
+        (MOTION_*) and the forcing scheme (0 implicit, 1 explicit)."""
         xyz = np.ascontiguousarray(xyz, dtype=np.float64)
         ds = np.ascontiguousarray(ds, dtype=np.float64)
         n = ds.shape[0]
@@ -268,12 +279,17 @@ class Solver:
             ic.velocity[a] = velocity[a]
         ic.density_ratio, ic.volume, ic.inertia, ic.T_body = density_ratio, volume, inertia, T_body
         ic.free_dofs = free_dofs
+        ic.rho_nearest, ic.added_mass, ic.motion = int(rho_nearest), int(added_mass), int(motion)
+        ic.motion_amp, ic.motion_freq, ic.scheme = motion_amp, motion_freq, int(scheme)
         ud = None
         if udes is not None:
             udes = np.ascontiguousarray(udes, dtype=np.float64)
             ud = _dp(udes)
         check(self.L.lbmgpu_set_markers(self.h, C.byref(ic), _dp(xyz), _dp(ds), ud))
         self.n_markers = n
+        if normals is not None:
+            nrm = np.ascontiguousarray(normals, dtype=np.float64)
+            check(self.L.lbmgpu_set_marker_normals(self.h, _dp(nrm)))
 
     def step(self, n: int = 1):
         check(self.L.lbmgpu_step(self.h, int(n)))
@@ -451,6 +467,18 @@ def config_from_types(nx, ny, nz, tau, types, rho=None, ux=None, uy=None, uz=Non
     cfg = Config()
     check(L.lbmgpu_config_from_types(nx, ny, nz, tau, t.ctypes.data_as(C.POINTER(C.c_uint8)), *ptrs,
                                      C.byref(cfg)))
+    return cfg
+
+
+def config_from_types_2d(nx, ny, tau, types, rho=None, ux=None, uy=None) -> Config:
+    """The reference's D2Q9 build (Nz = 1): the computational layer
+    fluid[i][j][1] (arrays of (ny+2, nx+2), x fastest) -> a D2Q9 Config."""
+    L = load()
+    t = np.ascontiguousarray(types, dtype=np.uint8).ravel()
+    arrs = [None if a is None else np.ascontiguousarray(a, dtype=np.float64).ravel() for a in (rho, ux, uy)]
+    ptrs = [None if a is None else _dp(a) for a in arrs]
+    cfg = Config()
+    check(L.lbmgpu_config_from_types_2d(nx, ny, tau, t.ctypes.data_as(C.POINTER(C.c_uint8)), *ptrs, C.byref(cfg)))
     return cfg
 
 

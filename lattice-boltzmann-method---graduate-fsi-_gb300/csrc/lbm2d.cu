@@ -1,0 +1,1177 @@
+// lbm2d.cu -- the reference's two-dimensional build (#define D2Q9) on the
+// device: D2Q9 BGK with Guo forcing and pull streaming, and the 2D immersed
+// boundary of IBLBM (lbm.cpp:1135-1416) with the reference's own options.
+//
+// One reference iteration (IBLBM -> Collision -> Streaming) is two launches:
+//   k_step2d  gather (= Streaming of the previous step, lbm.cpp:182-296),
+//             moments, BGK + Guo collision (lbm.cpp:60-119); cells inside the
+//             IBM box store their pre-collision populations and unforced
+//             moments instead.
+//   k_ibm2d   one thread block: the whole IBM pass on the box -- marker
+//             stencils, the implicit multi-direct forcing (lbm.cpp:1259-1390)
+//             or the explicit direct forcing (lbm.cpp:1171-1258), the added
+//             mass (lbm.cpp:1392-1398), the collision of the box cells, and
+//             the body kinematics of the next step (lbm.cpp:1140-1167).
+// A box of (2D+2)^2 nodes and a few hundred markers is far too little work
+// for more than one block; one block runs the m_max iterations with block
+// barriers only, its working fields staying in L2.
+//
+// Spreading is node-centred: each box node sums the forces of the markers
+// whose stencil covers it, in ascending marker order, through lists built
+// from the stencils (once for a fixed body, every step for a moving one) --
+// the reference's order of summation (lbm.cpp:1336-1344), with no atomics.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "lbm2d.cuh"
+#include "lbm_device.cuh"
+#include "lbm_handle.h"
+
+namespace l2d {
+
+using lbmk::St;
+
+constexpr int kIbmBlock = 1024;
+constexpr double kRefPi = 3.14159265;  // the reference's truncated PI (LBM.h:74)
+
+// ---------------------------------------------------------------------------
+// Collide-stream
+// ---------------------------------------------------------------------------
+template <class T>
+__device__ __forceinline__ float pull_link2(const T *__restrict__ A, int l, int x, int y, long long cell,
+                                            const Class2 &ce, const Params2 &P) {
+    if ((ce.bb >> l) & 1u) return St<T>::ld(A + opp9(l) * P.S + cell) + ce.val[l];
+    if ((ce.eq >> l) & 1u) return ce.val[l];
+    int sx = x - cx9(l), sy = y - cy9(l);
+    if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+    if (P.periodic & 2) sy = sy < 0 ? sy + P.ny : (sy >= P.ny ? sy - P.ny : sy);
+    if ((ce.zg >> l) & 1u) {
+        sx = min(max(sx, 0), P.nx - 1);
+        sy = min(max(sy, 0), P.ny - 1);
+    }
+    return St<T>::ld(A + l * P.S + sx + (long long)P.nx * sy);
+}
+
+// BGK + Guo on shifted populations (ConvLBM, lbm.cpp:91-118, with the D2Q9
+// tables; cs^2 = 1/3): f~* = f~ (1 - w) + w (feq - w_l) + S.
+__device__ __forceinline__ void collide9(float f[Q9], float drho, float ux, float uy, float Fx, float Fy,
+                                         float omega, bool forced) {
+    const float rho = 1.0f + drho;
+    const float usq = ux * ux + uy * uy;
+    const float c1 = 1.0f - 0.5f * omega;
+    const float Fu = Fx * ux + Fy * uy;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
+        const float poly = 3.0f * cu + 4.5f * cu * cu - 1.5f * usq + 4.5f * cu * cu * cu - 4.5f * cu * usq;
+        const float feq_s = w9f(l) * (drho + rho * poly);
+        float v = f[l] * (1.0f - omega) + omega * feq_s;
+        if (forced) {
+            const float Fc = (float)cx9(l) * Fx + (float)cy9(l) * Fy;
+            v += c1 * w9f(l) * (3.0f * Fc + 9.0f * Fc * cu - 3.0f * Fu);
+        }
+        f[l] = v;
+    }
+}
+
+template <class T, bool FORCED>
+__global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__restrict__ B,
+                                                const __grid_constant__ Params2 P, State2 *__restrict__ ds,
+                                                float *__restrict__ mom, float *__restrict__ band, int gather,
+                                                int export_only) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.nx || y >= P.ny) return;
+    const long long cell = x + (long long)P.nx * y;
+    float f[Q9];
+    const bool face = x == 0 || x == P.nx - 1 || y == 0 || y == P.ny - 1;
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(A + l * P.S + cell);
+    } else if (!face) {
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(A + l * P.S + cell + P.pofs[l]);
+    } else {
+        int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
+        raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
+        const Class2 &ce = P.cls[raw];
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = pull_link2<T>(A, l, x, y, cell, ce, P);
+    }
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        drho += f[l];
+        jx += (float)cx9(l) * f[l];
+        jy += (float)cy9(l) * f[l];
+    }
+    const float Fx = FORCED ? P.body[0] : 0.0f, Fy = FORCED ? P.body[1] : 0.0f;
+    const float rho = 1.0f + drho;
+    const float inv = 1.0f / rho;
+    // before the first streaming the stored set-up velocity is used as is
+    // (LBM::Init, lbm.cpp:31-57); MacroProp adds F/2 afterwards (lbm.cpp:677-679)
+    const float hf = gather ? 0.5f : 0.0f;
+    const float ux = (jx + hf * Fx) * inv, uy = (jy + hf * Fy) * inv;
+    if (!(rho > 0.0f && rho < 100.0f)) atomicOr(&ds->status, lbmk::ST_RHO_RANGE);
+    if (mom != nullptr) {
+        mom[cell] = rho;
+        mom[P.N + cell] = ux;
+        mom[2 * P.N + cell] = uy;
+    }
+    if (export_only) return;
+    if (P.band_on) {
+        const int bx = x - ds->box_lo[0], by = y - ds->box_lo[1];
+        if ((unsigned)bx < (unsigned)ds->box_w && (unsigned)by < (unsigned)ds->box_h) {
+            // the IBM pass collides this cell: hand over the unforced moments
+            // (lbm.cpp:1262-1285) and keep the populations
+            const long long b = bx + (long long)P.bsx * by, nb = P.nb;
+            band[b] = drho;
+            band[nb + b] = ux;
+            band[2 * nb + b] = uy;
+            band[3 * nb + b] = Fx;
+            band[4 * nb + b] = Fy;
+#pragma unroll
+            for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+            return;
+        }
+    }
+    collide9(f, drho, ux, uy, Fx, Fy, P.omega, FORCED);
+#pragma unroll
+    for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+}
+
+// f = feq(rho, u) (LBM::Init, lbm.cpp:31-57), shifted; fields [3][N] or null
+// (uniform init[3]).
+template <class T>
+__global__ void k_init2d(T *__restrict__ A, long long N, long long S, const float *__restrict__ fields,
+                         float rho0, float ux0, float uy0) {
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const float rho = fields ? fields[c] : rho0;
+    const float ux = fields ? fields[N + c] : ux0, uy = fields ? fields[2 * N + c] : uy0;
+    const float usq = ux * ux + uy * uy;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
+        const float poly = 3.0f * cu + 4.5f * cu * cu - 1.5f * usq + 4.5f * cu * cu * cu - 4.5f * cu * usq;
+        St<T>::st(A + l * S + c, w9f(l) * ((rho - 1.0f) + rho * poly));
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Immersed boundary
+// ---------------------------------------------------------------------------
+struct Ibm2 {
+    int n, m_max, lit_sign, rho_nearest, added_mass, motion, scheme;
+    double Dbox;     // the box reaches centre -/+ Dbox (the body diameter, lbm.cpp:1165-1166)
+    double vsolid, amp, freq;
+    double vconst[3];
+    double *pos;      // [3][n] reference node coordinates
+    const double *nrm;  // [3][n]
+    const double *dsw;  // [n]
+    double *acc;      // [2][n] FP64 force sums of the pass
+    float *fs;        // [2][n] F_m ds_m of the current iteration
+    float *rhom;      // [n]
+    int *s0;          // [2][n] stencil origin, box coordinates
+    float *swt;       // [16][n] stencil weights (0 outside the box)
+    int *cnt, *off;   // [nb], [nb]
+    int *lm;          // [16 n] spreading lists: marker
+    float *lw;        //                         weight
+    double *hist;     // [cap][4]: drag, lift, 0, step
+};
+
+// 4-point Peskin delta (lbm.cpp:1095-1102).
+__device__ __forceinline__ double peskin_d(double r) {
+    const double a = fabs(r);
+    if (a <= 1.0) return (3.0 - 2.0 * a + sqrt(1.0 + 4.0 * a - 4.0 * r * r)) / 8.0;
+    if (a <= 2.0) return (5.0 - 2.0 * a - sqrt(-7.0 + 12.0 * a - 4.0 * r * r)) / 8.0;
+    return 0.0;
+}
+
+// V_CM(t) of the prescribed motions (lbm.cpp:1140-1151).
+__device__ __forceinline__ void motion_velocity(const Ibm2 &ib, double t, double V[3]) {
+    V[0] = V[1] = V[2] = 0.0;
+    if (ib.motion == LBM_MOTION_CONSTANT) {
+        V[0] = ib.vconst[0];
+        V[1] = ib.vconst[1];
+        V[2] = ib.vconst[2];
+    } else if (ib.motion == LBM_MOTION_INLINE_OSC) {
+        V[0] = -ib.amp * cos(2.0 * kRefPi * ib.freq * t);
+    } else if (ib.motion == LBM_MOTION_TRANSVERSE_OSC) {
+        V[1] = -2.0 * kRefPi * ib.freq * ib.amp * sin(2.0 * kRefPi * ib.freq * t);
+    }
+}
+
+// The kinematics of IBLBM for reference step s (lbm.cpp:1137-1167): V_CM
+// of step s and of the step before, the centre moved by the trapezoid, and
+// the box [floor(c - D), ceil(c + D)] (z = 1).  box_of only computes the box
+// of step s (for the collide-stream launch that precedes the IBM pass);
+// advance_body commits the step (V, centre, markers, desired velocity) at
+// the start of the pass.  Both evaluate V(s) and the centre with the same
+// operations, so the box matches the committed centre.
+__device__ void box_of(State2 *st, const Ibm2 &ib, const Params2 &P, long long s) {
+    double V[3], c[2];
+    motion_velocity(ib, (double)s, V);
+    for (int a = 0; a < 2; a++) c[a] = st->center[a] + (V[a] + st->V[a]) * 1.0 / 2;
+    const int xmin = (int)floor(c[0] - ib.Dbox), xmax = (int)ceil(c[0] + ib.Dbox);
+    const int ymin = (int)floor(c[1] - ib.Dbox), ymax = (int)ceil(c[1] + ib.Dbox);
+    // reference node i is device cell i - 1; the box must lie in the interior
+    int lo0 = xmin - 1, lo1 = ymin - 1, w = xmax - xmin + 1, hgt = ymax - ymin + 1;
+    if (lo0 < 0 || lo1 < 0 || lo0 + w > P.nx || lo1 + hgt > P.ny || w > P.bsx || hgt > P.bsy) {
+        atomicOr(&st->status, lbmk::ST_BAND_EDGE);
+        lo0 = max(lo0, 0);
+        lo1 = max(lo1, 0);
+        w = min(min(w, P.bsx), P.nx - lo0);
+        hgt = min(min(hgt, P.bsy), P.ny - lo1);
+    }
+    st->box_lo[0] = lo0;
+    st->box_lo[1] = lo1;
+    st->box_w = w;
+    st->box_h = hgt;
+}
+
+// Block-wide; callers synchronise before and after.
+__device__ void advance_body(State2 *st, const Ibm2 &ib, long long s) {
+    __shared__ double sV[3], sVo[3];
+    if (threadIdx.x == 0) {
+        double V[3];
+        motion_velocity(ib, (double)s, V);
+        for (int a = 0; a < 3; a++) {
+            sVo[a] = st->V[a];
+            sV[a] = V[a];
+            st->Vold[a] = st->V[a];
+            st->V[a] = V[a];
+            st->center[a] += (V[a] + sVo[a]) * 1.0 / 2;
+        }
+        st->ibm_step = s;
+        if (ib.motion != LBM_MOTION_FIXED) st->lists_ok = 0;
+    }
+    __syncthreads();
+    if (ib.motion != LBM_MOTION_FIXED)
+        for (int m = threadIdx.x; m < ib.n; m += blockDim.x)
+            for (int a = 0; a < 3; a++) ib.pos[a * ib.n + m] += (sV[a] + sVo[a]) * 1.0 / 2;
+}
+
+// The box of reference step 1, before its collide-stream launch.
+__global__ void k_kin2d(State2 *st, Ibm2 ib, const __grid_constant__ Params2 P) { box_of(st, ib, P, 1); }
+
+// Block-wide exclusive scan of one int per thread (blockDim 1024).
+__device__ int block_scan(int v, int *total) {
+    __shared__ int wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+    }
+    if (lane == 31) wsum[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = lane < (int)(blockDim.x >> 5) ? wsum[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        wsum[lane] = s;
+    }
+    __syncthreads();
+    const int before = (w > 0 ? wsum[w - 1] : 0) + x - v;
+    *total = wsum[31];
+    __syncthreads();
+    return before;
+}
+
+// FP64 block sum in a fixed order.
+__device__ double block_sum_d(double v) {
+    __shared__ double part[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    if (lane == 0) part[w] = v;
+    __syncthreads();
+    double s = 0.0;
+    if (threadIdx.x == 0)
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += part[i];
+    __syncthreads();
+    return s;  // valid in thread 0
+}
+
+// Marker m's stencil: origin (box coordinates) and the 16 weights
+// kernel(rx) kernel(ry) kernel(rz) of the box nodes i = floor(X)-1 .. +2
+// (x outer), j likewise, k = 1 (lbm.cpp:1288-1309); 0 outside the box.
+__device__ __forceinline__ void marker_stencil(const Ibm2 &ib, const State2 *st, int m) {
+    const int n = ib.n;
+    const double X = ib.pos[m], Y = ib.pos[n + m], Z = ib.pos[2 * n + m];
+    const int i0 = (int)floor(X) - 1, j0 = (int)floor(Y) - 1;
+    // box node (bx, by) is reference node (box_lo + 1 + bx, ...)
+    const int bx0 = i0 - (st->box_lo[0] + 1), by0 = j0 - (st->box_lo[1] + 1);
+    ib.s0[m] = bx0;
+    ib.s0[n + m] = by0;
+    const double kz = peskin_d(1.0 - Z);
+    for (int a = 0; a < 4; a++) {
+        const double kx = peskin_d((double)(i0 + a) - X);
+        for (int b = 0; b < 4; b++) {
+            const double ky = peskin_d((double)(j0 + b) - Y);
+            const bool in = (unsigned)(bx0 + a) < (unsigned)st->box_w && (unsigned)(by0 + b) < (unsigned)st->box_h;
+            ib.swt[(4 * a + b) * n + m] = in ? (float)(kx * ky * kz) : 0.0f;
+        }
+    }
+}
+
+// Interpolation of the box field (a, b) at marker m over its stencil, in the
+// reference's node order.
+__device__ __forceinline__ void interp2(const Ibm2 &ib, const Params2 &P, const float *__restrict__ fa,
+                                        const float *__restrict__ fb, int m, float &sa, float &sb) {
+    const int n = ib.n;
+    const int bx0 = ib.s0[m], by0 = ib.s0[n + m];
+    float a0 = 0.0f, b0 = 0.0f;
+#pragma unroll
+    for (int a = 0; a < 4; a++)
+#pragma unroll
+        for (int b = 0; b < 4; b++) {
+            const float w = ib.swt[(4 * a + b) * n + m];
+            if (w != 0.0f) {
+                const long long q = (bx0 + a) + (long long)P.bsx * (by0 + b);
+                a0 += fa[q] * w;
+                if (fb) b0 += fb[q] * w;
+            }
+        }
+    sa = a0;
+    sb = b0;
+}
+
+// NearestLatticeCoordinate (lbm.cpp:1074-1092) over box nodes
+// [xa, xb] x [ya, yb] (box coordinates), one warp: the last node in
+// x-outer / y-inner order with the largest (x - X) . n > 0.  Returns the box
+// node, or -1 when none lies on the outer side.
+__device__ __forceinline__ long long nearest_node(const Ibm2 &ib, const State2 *st, const Params2 &P, int m,
+                                                  int xa, int xb, int ya, int yb) {
+    const int n = ib.n, lane = threadIdx.x & 31;
+    const double X = ib.pos[m], Y = ib.pos[n + m], Z = ib.pos[2 * n + m];
+    const double nx = ib.nrm[m], ny = ib.nrm[n + m], nz = ib.nrm[2 * n + m];
+    const int w = xb - xa + 1, h = yb - ya + 1;
+    double best = 0.0;
+    int bo = -1;
+    for (int o = lane; o < w * h; o += 32) {
+        const int bx = xa + o / h, by = ya + o % h;
+        const double d = ((double)(st->box_lo[0] + 1 + bx) - X) * nx + ((double)(st->box_lo[1] + 1 + by) - Y) * ny +
+                         (1.0 - Z) * nz;
+        if (d >= best && d > 0.0) {
+            best = d;
+            bo = o;
+        }
+    }
+#pragma unroll
+    for (int s = 16; s > 0; s >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, s);
+        const int oo = __shfl_xor_sync(0xffffffffu, bo, s);
+        if (oo >= 0 && (bo < 0 || ob > best || (ob == best && oo > bo))) {
+            best = ob;
+            bo = oo;
+        }
+    }
+    if (bo < 0) return -1;
+    return (long long)(xa + bo / h) + (long long)P.bsx * (ya + bo % h);
+}
+
+template <class T>
+__global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __grid_constant__ Params2 P,
+                                                     State2 *__restrict__ st, Ibm2 ib, float *__restrict__ band) {
+    const int tid = threadIdx.x, nt = blockDim.x;
+    const int n = ib.n;
+    const long long nb = P.nb;
+    // IBLBM's prelude for this step: V_CM, markers, centre (the box of the
+    // step was set before its collide-stream launch)
+    const long long step = st->ibm_step + 1;
+    __syncthreads();
+    advance_body(st, ib, step);
+    __syncthreads();
+    const int bw = st->box_w, bh = st->box_h, nbox = bw * bh;
+    const int lists_ok = st->lists_ok;
+    float *drho = band, *ux = band + nb, *uy = band + 2 * nb, *Fx = band + 3 * nb, *Fy = band + 4 * nb;
+    auto bq = [&](int o) { return (long long)(o % bw) + (long long)P.bsx * (o / bw); };
+    __syncthreads();
+
+    // stencils and spreading lists (fixed body: once)
+    if (!lists_ok) {
+        for (int m = tid; m < n; m += nt) marker_stencil(ib, st, m);
+        for (int o = tid; o < nbox; o += nt) ib.cnt[bq(o)] = 0;
+        __syncthreads();
+        for (int m = tid; m < n; m += nt)
+            for (int k = 0; k < 16; k++)
+                if (ib.swt[k * n + m] != 0.0f)
+                    atomicAdd(&ib.cnt[(ib.s0[m] + k / 4) + (long long)P.bsx * (ib.s0[n + m] + k % 4)], 1);
+        __syncthreads();
+        // offsets: contiguous chunks of box nodes per thread, then a block scan
+        const int chunk = (nbox + nt - 1) / nt, o0 = tid * chunk, o1 = min(nbox, o0 + chunk);
+        int mine = 0;
+        for (int o = o0; o < o1; o++) mine += ib.cnt[bq(o)];
+        int total;
+        int run = block_scan(mine, &total);
+        for (int o = o0; o < o1; o++) {
+            const long long q = bq(o);
+            ib.off[q] = run;
+            run += ib.cnt[q];
+            ib.cnt[q] = 0;
+        }
+        __syncthreads();
+        for (int m = tid; m < n; m += nt)
+            for (int k = 0; k < 16; k++) {
+                const float w = ib.swt[k * n + m];
+                if (w == 0.0f) continue;
+                const long long q = (ib.s0[m] + k / 4) + (long long)P.bsx * (ib.s0[n + m] + k % 4);
+                const int slot = ib.off[q] + atomicAdd(&ib.cnt[q], 1);
+                ib.lm[slot] = m;
+                ib.lw[slot] = w;
+            }
+        __syncthreads();
+        // ascending marker order in every list (the reference's summation order)
+        for (int o = tid; o < nbox; o += nt) {
+            const long long q = bq(o);
+            const int a = ib.off[q], c = ib.cnt[q];
+            for (int i = 1; i < c; i++) {
+                const int km = ib.lm[a + i];
+                const float kw = ib.lw[a + i];
+                int j = i - 1;
+                while (j >= 0 && ib.lm[a + j] > km) {
+                    ib.lm[a + j + 1] = ib.lm[a + j];
+                    ib.lw[a + j + 1] = ib.lw[a + j];
+                    j--;
+                }
+                ib.lm[a + j + 1] = km;
+                ib.lw[a + j + 1] = kw;
+            }
+        }
+        if (tid == 0 && ib.motion == LBM_MOTION_FIXED) st->lists_ok = 1;
+    }
+    for (int m = tid; m < 2 * n; m += nt) ib.acc[m] = 0.0;
+    __syncthreads();
+
+    // marker density: nearest node over the box (lbm.cpp:1315-1317), over
+    // the 2x2 cell around the marker in the explicit scheme (lbm.cpp:1216-1219),
+    // or delta-interpolated
+    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
+    if (ib.rho_nearest) {
+        for (int m = warp; m < n; m += nwarp) {
+            int xa = 0, xb = bw - 1, ya = 0, yb = bh - 1;
+            if (ib.scheme == 1) {
+                const double X = ib.pos[m], Y = ib.pos[n + m];
+                xa = (int)floor(X) - (st->box_lo[0] + 1);
+                xb = (int)ceil(X) - (st->box_lo[0] + 1);
+                ya = (int)floor(Y) - (st->box_lo[1] + 1);
+                yb = (int)ceil(Y) - (st->box_lo[1] + 1);
+                if (xa < 0 || ya < 0 || xb >= bw || yb >= bh) {
+                    if (lane == 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
+                    xa = max(xa, 0);
+                    ya = max(ya, 0);
+                    xb = min(xb, bw - 1);
+                    yb = min(yb, bh - 1);
+                }
+            }
+            const long long q = nearest_node(ib, st, P, m, xa, xb, ya, yb);
+            if (lane == 0) {
+                if (q < 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
+                ib.rhom[m] = q < 0 ? 1.0f : 1.0f + drho[q];
+            }
+        }
+    } else {
+        for (int m = tid; m < n; m += nt) {
+            float sr, dummy;
+            interp2(ib, P, drho, nullptr, m, sr, dummy);
+            // sum (1 + drho) delta = sum delta + sum drho delta
+            float wsum = 0.0f;
+            for (int k = 0; k < 16; k++) wsum += ib.swt[k * n + m];
+            ib.rhom[m] = wsum + sr;
+        }
+    }
+    __syncthreads();
+
+    const float sgn = ib.lit_sign ? -1.0f : 1.0f;
+    double node_drag = 0.0, node_lift = 0.0;
+    const int iters = ib.scheme == 1 ? 1 : ib.m_max;
+    for (int it = 0; it < iters; it++) {
+        // interpolate the current velocity; marker forces (lbm.cpp:1314-1324)
+        for (int m = tid; m < n; m += nt) {
+            float ub, vb;
+            interp2(ib, P, ux, uy, m, ub, vb);
+            const float rho = ib.rhom[m];
+            const float V0 = (float)st->V[0], V1 = (float)st->V[1];
+            const float Fbx = 2.0f * rho * (V0 - ub), Fby = 2.0f * rho * (V1 - vb);
+            const double dsv = ib.dsw[m];
+            ib.fs[m] = (float)(Fbx * dsv);
+            ib.fs[n + m] = (float)(Fby * dsv);
+            if (ib.scheme == 0) {
+                ib.acc[m] += -(double)Fbx * 1.0 * dsv;
+                ib.acc[n + m] += -(double)Fby * 1.0 * dsv;
+            }
+            if (!isfinite(Fbx) || !isfinite(Fby)) atomicOr(&st->status, lbmk::ST_NONFINITE_FORCE);
+        }
+        __syncthreads();
+        // spreading, node-centred, ascending marker order (lbm.cpp:1331-1352)
+        for (int o = tid; o < nbox; o += nt) {
+            const long long q = bq(o);
+            const int a = ib.off[q], c = ib.cnt[q];
+            float sx = 0.0f, sy = 0.0f;
+            for (int i = 0; i < c; i++) {
+                const int m = ib.lm[a + i];
+                const float w = ib.lw[a + i];
+                sx += ib.fs[m] * w;
+                sy += ib.fs[n + m] * w;
+            }
+            const float rho = 1.0f + drho[q];
+            if (ib.scheme == 0) {
+                Fx[q] += sgn * sx;
+                Fy[q] += sgn * sy;
+            } else {
+                // explicit: F = sum F_m ds delta, u += F / 2 rho, Drag -= F dx^2
+                Fx[q] += sx;
+                Fy[q] += sy;
+                node_drag += -(double)sx;
+                node_lift += -(double)sy;
+            }
+            ux[q] += sx / (2.0f * rho);
+            uy[q] += sy / (2.0f * rho);
+        }
+        __syncthreads();
+    }
+
+    // the pass's force: sum over markers (implicit) or box nodes (explicit)
+    double dl = 0.0, ll = 0.0;
+    if (ib.scheme == 0) {
+        for (int m = tid; m < n; m += nt) {
+            dl += ib.acc[m];
+            ll += ib.acc[n + m];
+        }
+    } else {
+        dl = node_drag;
+        ll = node_lift;
+    }
+    const double drag = block_sum_d(dl), lift = block_sum_d(ll);
+
+    // added mass (lbm.cpp:1392-1398): mean density of the box nodes inside
+    // every marker (Calc_AverageDensity, lbm.cpp:1105-1132); skipped when
+    // V_CM did not change, where it adds rho_avg * 0
+    __shared__ double sam[2];
+    const double dV0 = st->V[0] - st->Vold[0], dV1 = st->V[1] - st->Vold[1];
+    if (ib.added_mass && (dV0 != 0.0 || dV1 != 0.0)) {
+        double rs = 0.0, cnt = 0.0;
+        for (int o = tid; o < nbox; o += nt) {
+            const int bx = o % bw, by = o / bw;
+            const double X = (double)(st->box_lo[0] + 1 + bx), Y = (double)(st->box_lo[1] + 1 + by);
+            bool inside = true;
+            for (int m = 0; m < n && inside; m++) {
+                const double d = (X - ib.pos[m]) * ib.nrm[m] + (Y - ib.pos[n + m]) * ib.nrm[n + m] +
+                                 (1.0 - ib.pos[2 * n + m]) * ib.nrm[2 * n + m];
+                if (d > 0.0) inside = false;
+            }
+            if (inside) {
+                rs += 1.0 + (double)drho[bq(o)];
+                cnt += 1.0;
+            }
+        }
+        const double tr = block_sum_d(rs), tc = block_sum_d(cnt);
+        if (tid == 0) {
+            const double ravg = tr / tc;
+            sam[0] = ravg * ib.vsolid * dV0 / 1.0;
+            sam[1] = ravg * ib.vsolid * dV1 / 1.0;
+        }
+    } else if (tid == 0) {
+        sam[0] = sam[1] = 0.0;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        const long long s = step;
+        double *row = ib.hist + 4 * ((s - 1) % st->hist_cap);
+        row[0] = drag + sam[0];
+        row[1] = lift + sam[1];
+        row[2] = 0.0;
+        row[3] = (double)s;
+    }
+
+    // collision of the box cells with the forced velocity and the force
+    for (int o = tid; o < nbox; o += nt) {
+        const long long q = bq(o);
+        const long long cell = (st->box_lo[0] + o % bw) + (long long)P.nx * (st->box_lo[1] + o / bw);
+        float f[Q9];
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
+        collide9(f, drho[q], ux[q], uy[q], Fx[q], Fy[q], P.omega, true);
+#pragma unroll
+        for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+    }
+    __syncthreads();
+    // the box of the next step, for its collide-stream launch
+    if (tid == 0) box_of(st, ib, P, step + 1);
+}
+
+}  // namespace l2d
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+using namespace l2d;
+
+struct lbm2d {
+    Params2 P;
+    State2 *st = nullptr;
+    void *f[2] = {nullptr, nullptr};
+    int cur = 0;
+    float *mom = nullptr;
+    float *band = nullptr;
+    bool ibm = false, normals = false, kin_ready = false;
+    lbm_ibm_config ic;
+    Ibm2 ib;
+    double *hist = nullptr;
+    long long hist_cap = 1 << 16;
+    cudaGraphExec_t gexec = nullptr;
+    int gsteps = 16;
+    int tx = 128, ty = 2;
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+lbm_status f2(lbm_status s, const std::string &m) {
+    lbm_set_last_error(m);
+    return s;
+}
+
+#define CK2(expr)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) return f2(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+template <class Tp>
+cudaError_t alloc2(lbm_handle *h, Tp **p, size_t bytes) {
+    cudaError_t e = cudaMalloc((void **)p, bytes);
+    if (e == cudaSuccess) {
+        h->d2->allocs.push_back((void *)*p);
+        h->dev_bytes += bytes;
+    } else {
+        *p = nullptr;
+    }
+    return e;
+}
+
+double feq9_host(double rho, double ux, double uy, int l) {
+    const double cu = cx9(l) * ux + cy9(l) * uy, usq = ux * ux + uy * uy, cs2 = 1.0 / 3.0;
+    return rho * w9d(l) *
+           (1 + cu / cs2 + cu * cu / (2 * cs2 * cs2) - usq / (2 * cs2) + cu * cu * cu / (6 * cs2 * cs2 * cs2) -
+            cu * usq / (2 * cs2 * cs2));
+}
+
+int face_priority2(int kind) {
+    switch (kind) {
+    case LBM_FACE_WALL: return 4;
+    case LBM_FACE_INLET: return 3;
+    case LBM_FACE_OUTLET_EQ: return 2;
+    case LBM_FACE_OUTLET_ZG: return 1;
+    }
+    return 0;
+}
+
+// Boundary classes of the four faces: as for D3Q19 (a link crossing several
+// ghost faces takes the highest-priority kind; a cell's wall velocity is the
+// mean over its moving wall neighbours, Determine_Wall_Velocity,
+// lbm.cpp:941-962).
+void build_classes2(const lbm_config &c, Params2 &P) {
+    for (int cls = 0; cls < 16; cls++) {
+        Class2 e;
+        memset(&e, 0, sizeof(e));
+        auto crossed = [&](int dx, int dy, int fs[2]) {
+            int k = 0;
+            if (!(P.periodic & 1)) {
+                if (dx < 0 && (cls & 1)) fs[k++] = 0;
+                if (dx > 0 && (cls & 2)) fs[k++] = 1;
+            }
+            if (!(P.periodic & 2)) {
+                if (dy < 0 && (cls & 4)) fs[k++] = 2;
+                if (dy > 0 && (cls & 8)) fs[k++] = 3;
+            }
+            return k;
+        };
+        auto resolve = [&](const int *fs, int k, double uw[2]) {
+            int best = -1, bp = -1;
+            for (int i = 0; i < k; i++) {
+                const int p = face_priority2(c.faces[fs[i]].kind);
+                if (p > bp) {
+                    bp = p;
+                    best = fs[i];
+                }
+            }
+            uw[0] = uw[1] = 0.0;
+            if (best >= 0 && c.faces[best].kind == LBM_FACE_WALL)
+                for (int i = 0; i < k; i++) {
+                    const lbm_face &F = c.faces[fs[i]];
+                    if (F.kind == LBM_FACE_WALL && (F.u[0] != 0 || F.u[1] != 0)) {
+                        uw[0] = F.u[0];
+                        uw[1] = F.u[1];
+                    }
+                }
+            return best;
+        };
+        double uwall[2] = {0, 0};
+        int num = 0;
+        for (int l = 0; l < Q9; l++) {
+            int fs[2];
+            const int k = crossed(cx9(l), cy9(l), fs);
+            if (!k) continue;
+            double uw[2];
+            const int fi = resolve(fs, k, uw);
+            if (c.faces[fi].kind == LBM_FACE_WALL && (uw[0] != 0 || uw[1] != 0)) {
+                uwall[0] += uw[0];
+                uwall[1] += uw[1];
+                num++;
+            }
+        }
+        if (num) {
+            uwall[0] /= num;
+            uwall[1] /= num;
+        }
+        for (int l = 0; l < Q9; l++) {
+            int fs[2];
+            const int k = crossed(-cx9(l), -cy9(l), fs);
+            if (!k) continue;
+            double uw[2];
+            const int fi = resolve(fs, k, uw);
+            const lbm_face &F = c.faces[fi];
+            if (F.kind == LBM_FACE_WALL) {
+                e.bb |= 1u << l;
+                // f_l = f*_opp(l) - 2 w (u_w . c_opp) / cs^2 (lbm.cpp:274)
+                e.val[l] = (float)(6.0 * w9d(l) * (uwall[0] * cx9(l) + uwall[1] * cy9(l)));
+            } else if (F.kind == LBM_FACE_INLET || F.kind == LBM_FACE_OUTLET_EQ) {
+                e.eq |= 1u << l;
+                e.val[l] = (float)(feq9_host(F.rho, F.u[0], F.u[1], l) - w9d(l));
+            } else if (F.kind == LBM_FACE_OUTLET_ZG) {
+                e.zg |= 1u << l;
+            }
+        }
+        P.cls[cls] = e;
+    }
+}
+
+cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only) {
+    lbm2d *d = h->d2;
+    const dim3 block(d->tx, d->ty);
+    const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
+    const void *A = d->f[d->cur];
+    void *B = d->f[1 - d->cur];
+    const bool forced = d->P.forced != 0;
+#define L2D_STEP(T)                                                                                             \
+    if (forced)                                                                                               \
+        k_step2d<T, true><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather,  \
+                                                   export_only);                                              \
+    else                                                                                                      \
+        k_step2d<T, false><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather, \
+                                                    export_only);
+    switch (h->cfg.storage) {
+    case LBM_STORE_F16: L2D_STEP(__half) break;
+    case LBM_STORE_BF16: L2D_STEP(__nv_bfloat16) break;
+    default: L2D_STEP(float) break;
+    }
+#undef L2D_STEP
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ibm2d(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    void *B = d->f[1 - d->cur];
+    switch (h->cfg.storage) {
+    case LBM_STORE_F16: k_ibm2d<__half><<<1, kIbmBlock, 0, h->s>>>((__half *)B, d->P, d->st, d->ib, d->band); break;
+    case LBM_STORE_BF16:
+        k_ibm2d<__nv_bfloat16><<<1, kIbmBlock, 0, h->s>>>((__nv_bfloat16 *)B, d->P, d->st, d->ib, d->band);
+        break;
+    default: k_ibm2d<float><<<1, kIbmBlock, 0, h->s>>>((float *)B, d->P, d->st, d->ib, d->band); break;
+    }
+    return cudaGetLastError();
+}
+
+// One reference iteration.
+cudaError_t enqueue_step2d(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    const int gather = h->steps == 0 ? 0 : 1;
+    cudaError_t e = launch_step2d(h, gather, nullptr, 0);
+    if (e == cudaSuccess && d->ibm) e = launch_ibm2d(h);
+    d->cur = 1 - d->cur;
+    h->steps++;
+    return e;
+}
+
+}  // namespace
+
+lbm_status l2d_create(lbm_handle *h) {
+    const lbm_config &c = h->cfg;
+    if (c.nz != 1) return f2(LBM_ERR_INVALID, "create: a D2Q9 configuration has nz = 1");
+    if (c.thermal) return f2(LBM_ERR_UNSUPPORTED, "create: no thermal population on D2Q9 handles");
+    for (int a = 0; a < 2; a++) {
+        const bool p0 = c.faces[2 * a].kind == LBM_FACE_PERIODIC, p1 = c.faces[2 * a + 1].kind == LBM_FACE_PERIODIC;
+        if (p0 != p1) return f2(LBM_ERR_INVALID, "create: a periodic axis needs both faces periodic");
+    }
+    h->d2 = new lbm2d();
+    lbm2d *d = h->d2;
+    Params2 &P = d->P;
+    memset(&P, 0, sizeof(P));
+    P.nx = c.nx;
+    P.ny = c.ny;
+    P.N = (long long)c.nx * c.ny;
+    P.S = ((P.N + 2LL * c.nx + 64 + 255) / 256) * 256;
+    P.omega = (float)(1.0 / c.tau);
+    P.body[0] = (float)c.body_force[0];
+    P.body[1] = (float)c.body_force[1];
+    P.forced = (c.body_force[0] != 0 || c.body_force[1] != 0) ? 1 : 0;
+    for (int a = 0; a < 2; a++)
+        if (c.faces[2 * a].kind == LBM_FACE_PERIODIC) P.periodic |= 1 << a;
+    for (int l = 0; l < Q9; l++) P.pofs[l] = -(cx9(l) + c.nx * cy9(l));
+    build_classes2(c, P);
+    h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
+    if (c.graph_steps > 0) d->gsteps = c.graph_steps + (c.graph_steps & 1);
+    if (c.graph_steps < 0) d->gsteps = 0;
+    d->tx = c.block_x > 0 ? ((c.block_x + 31) / 32) * 32 : (c.nx >= 128 ? 128 : (c.nx >= 64 ? 64 : 32));
+    d->ty = c.block_y > 0 ? c.block_y : std::max(1, 256 / d->tx);
+    CK2(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->f[i], (size_t)Q9 * P.S * h->esize));
+    CK2(alloc2(h, &d->mom, (size_t)3 * P.N * sizeof(float)));
+    CK2(alloc2(h, &d->st, sizeof(State2)));
+    CK2(alloc2(h, &d->hist, (size_t)d->hist_cap * 4 * sizeof(double)));
+    State2 s0;
+    memset(&s0, 0, sizeof(s0));
+    s0.hist_cap = d->hist_cap;
+    CK2(cudaMemcpyAsync(d->st, &s0, sizeof(s0), cudaMemcpyHostToDevice, h->s));
+    CK2(cudaMemsetAsync(d->hist, 0, (size_t)d->hist_cap * 4 * sizeof(double), h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+void l2d_free(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    if (!d) return;
+    if (d->gexec) cudaGraphExecDestroy(d->gexec);
+    for (void *p : d->allocs) cudaFree(p);
+    delete d;
+    h->d2 = nullptr;
+}
+
+lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const double *uy) {
+    lbm2d *d = h->d2;
+    const long long N = d->P.N;
+    float *dfields = nullptr;
+    if (rho) {
+        std::vector<float> tmp((size_t)3 * N);
+        for (long long c = 0; c < N; c++) {
+            tmp[c] = (float)rho[c];
+            tmp[N + c] = (float)ux[c];
+            tmp[2 * N + c] = (float)uy[c];
+        }
+        // staged through the moment buffer (3N floats)
+        CK2(cudaMemcpyAsync(d->mom, tmp.data(), tmp.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
+        dfields = d->mom;
+        CK2(cudaStreamSynchronize(h->s));
+    }
+    const int thr = 256;
+    const unsigned blocks = (unsigned)((N + thr - 1) / thr);
+    const float r0 = (float)h->cfg.rho0, u0 = (float)h->cfg.u0[0], v0 = (float)h->cfg.u0[1];
+    switch (h->cfg.storage) {
+    case LBM_STORE_F16: k_init2d<__half><<<blocks, thr, 0, h->s>>>((__half *)d->f[0], N, d->P.S, dfields, r0, u0, v0); break;
+    case LBM_STORE_BF16:
+        k_init2d<__nv_bfloat16><<<blocks, thr, 0, h->s>>>((__nv_bfloat16 *)d->f[0], N, d->P.S, dfields, r0, u0, v0);
+        break;
+    default: k_init2d<float><<<blocks, thr, 0, h->s>>>((float *)d->f[0], N, d->P.S, dfields, r0, u0, v0); break;
+    }
+    CK2(cudaGetLastError());
+    CK2(cudaStreamSynchronize(h->s));
+    d->cur = 0;
+    h->steps = 0;
+    h->inited = true;
+    if (d->gexec) {
+        cudaGraphExecDestroy(d->gexec);
+        d->gexec = nullptr;
+    }
+    return LBM_OK;
+}
+
+lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *dsw) {
+    lbm2d *d = h->d2;
+    if (d->ibm) return f2(LBM_ERR_STATE, "set_markers: markers already set");
+    if (h->steps > 0) return f2(LBM_ERR_STATE, "set_markers: call before the first step");
+    const int n = ic->n_markers;
+    if (n < 1 || !xyz || !dsw) return f2(LBM_ERR_INVALID, "set_markers: bad markers");
+    if (ic->free_body || ic->thermal) return f2(LBM_ERR_UNSUPPORTED, "set_markers: D2Q9 bodies are fixed or prescribed");
+    if (ic->scheme == 0 && ic->m_max < 1) return f2(LBM_ERR_INVALID, "set_markers: m_max must be >= 1");
+    if (ic->motion < LBM_MOTION_FIXED || ic->motion > LBM_MOTION_TRANSVERSE_OSC)
+        return f2(LBM_ERR_INVALID, "set_markers: unknown motion");
+    if (!(ic->radius > 0)) return f2(LBM_ERR_INVALID, "set_markers: radius must be positive");
+    d->ic = *ic;
+    Params2 &P = d->P;
+    // the box [floor(c - D), ceil(c + D)] spans at most 2D + 2 nodes per axis
+    const double D = 2.0 * ic->radius;
+    P.bsx = std::min(P.nx, (int)std::ceil(2.0 * D) + 3);
+    P.bsy = std::min(P.ny, (int)std::ceil(2.0 * D) + 3);
+    P.nb = (long long)P.bsx * P.bsy;
+    P.band_on = 1;
+    Ibm2 &ib = d->ib;
+    memset(&ib, 0, sizeof(ib));
+    ib.n = n;
+    ib.m_max = ic->m_max;
+    ib.lit_sign = ic->literal_sign;
+    ib.rho_nearest = ic->rho_nearest;
+    ib.added_mass = ic->added_mass;
+    ib.motion = ic->motion;
+    ib.scheme = ic->scheme;
+    ib.Dbox = D;
+    ib.vsolid = ic->volume;
+    ib.amp = ic->motion_amp;
+    ib.freq = ic->motion_freq;
+    for (int a = 0; a < 3; a++) ib.vconst[a] = ic->velocity[a];
+    CK2(alloc2(h, &d->band, (size_t)5 * P.nb * sizeof(float)));
+    CK2(alloc2(h, &ib.pos, (size_t)3 * n * sizeof(double)));
+    double *nrm = nullptr, *dsd = nullptr;
+    CK2(alloc2(h, &nrm, (size_t)3 * n * sizeof(double)));
+    CK2(alloc2(h, &dsd, (size_t)n * sizeof(double)));
+    ib.nrm = nrm;
+    ib.dsw = dsd;
+    CK2(alloc2(h, &ib.acc, (size_t)2 * n * sizeof(double)));
+    CK2(alloc2(h, &ib.fs, (size_t)2 * n * sizeof(float)));
+    CK2(alloc2(h, &ib.rhom, (size_t)n * sizeof(float)));
+    CK2(alloc2(h, &ib.s0, (size_t)2 * n * sizeof(int)));
+    CK2(alloc2(h, &ib.swt, (size_t)16 * n * sizeof(float)));
+    CK2(alloc2(h, &ib.cnt, (size_t)P.nb * sizeof(int)));
+    CK2(alloc2(h, &ib.off, (size_t)P.nb * sizeof(int)));
+    CK2(alloc2(h, &ib.lm, (size_t)16 * n * sizeof(int)));
+    CK2(alloc2(h, &ib.lw, (size_t)16 * n * sizeof(float)));
+    ib.hist = d->hist;
+    CK2(cudaMemcpyAsync(ib.pos, xyz, (size_t)3 * n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    CK2(cudaMemcpyAsync(dsd, dsw, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->s));
+    CK2(cudaMemsetAsync(nrm, 0, (size_t)3 * n * sizeof(double), h->s));
+    CK2(cudaMemsetAsync(d->band, 0, (size_t)5 * P.nb * sizeof(float), h->s));
+    // V_CM starts at zero (main.cpp: double V_CM[3] = {0,0,0}); the centre
+    // is the given one
+    State2 s0;
+    CK2(cudaMemcpyAsync(&s0, d->st, sizeof(s0), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    for (int a = 0; a < 3; a++) {
+        s0.center[a] = ic->center[a];
+        s0.V[a] = s0.Vold[a] = 0.0;
+    }
+    s0.lists_ok = 0;
+    s0.ibm_step = 0;
+    CK2(cudaMemcpyAsync(d->st, &s0, sizeof(s0), cudaMemcpyHostToDevice, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    d->ibm = true;
+    d->kin_ready = false;
+    if (d->gexec) {
+        cudaGraphExecDestroy(d->gexec);
+        d->gexec = nullptr;
+    }
+    return LBM_OK;
+}
+
+lbm_status l2d_set_normals(lbm_handle *h, const double *nxyz) {
+    lbm2d *d = h->d2;
+    if (!d->ibm) return f2(LBM_ERR_STATE, "set_marker_normals: call lbmgpu_set_markers first");
+    CK2(cudaMemcpyAsync((void *)d->ib.nrm, nxyz, (size_t)3 * d->ib.n * sizeof(double), cudaMemcpyHostToDevice,
+                        h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    d->normals = true;
+    return LBM_OK;
+}
+
+lbm_status l2d_step(lbm_handle *h, int nsteps) {
+    lbm2d *d = h->d2;
+    if (!h->inited) return f2(LBM_ERR_STATE, "step: call lbmgpu_init first");
+    if (nsteps < 0) return f2(LBM_ERR_INVALID, "step: negative count");
+    if (d->ibm && (d->ic.rho_nearest || d->ic.added_mass) && !d->normals)
+        return f2(LBM_ERR_STATE, "step: the nearest-node density and the added mass need lbmgpu_set_marker_normals");
+    if (d->ibm && !d->kin_ready) {
+        // kinematics of reference step 1 (IBLBM's prelude)
+        k_kin2d<<<1, 1, 0, h->s>>>(d->st, d->ib, d->P);
+        CK2(cudaGetLastError());
+        d->kin_ready = true;
+    }
+    int left = nsteps;
+    // the first step (no gather) and odd remainders run eagerly; whole
+    // graphs of gsteps (even: the buffers return to the same parity) replay
+    while (left > 0 && h->steps == 0) {
+        CK2(enqueue_step2d(h));
+        left--;
+    }
+    if (d->gsteps > 0 && left >= d->gsteps) {
+        if (!d->gexec) {
+            cudaGraph_t g;
+            const long long s0 = h->steps;
+            const int c0 = d->cur;
+            CK2(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+            for (int i = 0; i < d->gsteps; i++) enqueue_step2d(h);
+            cudaError_t e = cudaStreamEndCapture(h->s, &g);
+            h->steps = s0;
+            d->cur = c0;
+            CK2(e);
+            e = cudaGraphInstantiate(&d->gexec, g, 0);
+            cudaGraphDestroy(g);
+            CK2(e);
+        }
+        while (left >= d->gsteps) {
+            CK2(cudaGraphLaunch(d->gexec, h->s));
+            h->steps += d->gsteps;
+            left -= d->gsteps;
+        }
+    }
+    while (left > 0) {
+        CK2(enqueue_step2d(h));
+        left--;
+    }
+    return LBM_OK;
+}
+
+lbm_status l2d_export(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    if (!h->inited) return f2(LBM_ERR_STATE, "download: call lbmgpu_init first");
+    // gather-only pass over the current state (no collision, no store)
+    const int gather = h->steps == 0 ? 0 : 1;
+    CK2(launch_step2d(h, gather, d->mom, 1));
+    return LBM_OK;
+}
+
+lbm_status l2d_download_f32(lbm_handle *h, int field, float *host) {
+    lbm2d *d = h->d2;
+    if (field < 0 || field > 3) return f2(LBM_ERR_INVALID, "download: bad field for a D2Q9 handle");
+    const size_t N = (size_t)d->P.N;
+    if (field == 3) {
+        memset(host, 0, N * sizeof(float));
+        return LBM_OK;
+    }
+    lbm_status s = l2d_export(h);
+    if (s != LBM_OK) return s;
+    CK2(cudaMemcpyAsync(host, d->mom + (size_t)field * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+lbm_status l2d_download_all_f32(lbm_handle *h, float *host) {
+    lbm2d *d = h->d2;
+    const size_t N = (size_t)d->P.N;
+    lbm_status s = l2d_export(h);
+    if (s != LBM_OK) return s;
+    CK2(cudaMemcpyAsync(host, d->mom, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    memset(host + 3 * N, 0, N * sizeof(float));
+    return LBM_OK;
+}
+
+lbm_status l2d_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
+    lbm2d *d = h->d2;
+    if (!d->ibm) return f2(LBM_ERR_STATE, "get_forces: no markers set");
+    CK2(cudaStreamSynchronize(h->s));
+    const long long have = std::min<long long>(h->steps, d->hist_cap);
+    const long long take = std::min<long long>(have, max_steps);
+    std::vector<double> ring((size_t)d->hist_cap * 4);
+    CK2(cudaMemcpy(ring.data(), d->hist, ring.size() * sizeof(double), cudaMemcpyDeviceToHost));
+    for (long long i = 0; i < take; i++) {
+        const long long s = h->steps - take + 1 + i;  // reference step, 1-based
+        const double *r = &ring[(size_t)(4 * ((s - 1) % d->hist_cap))];
+        double *o = out + 8 * i;
+        o[0] = r[0];
+        o[1] = r[1];
+        o[2] = 0.0;
+        o[3] = o[4] = o[5] = 0.0;
+        o[6] = 0.0;
+        o[7] = r[3];
+    }
+    if (n_out) *n_out = (int)take;
+    return LBM_OK;
+}
+
+lbm_status l2d_get_markers(lbm_handle *h, double *xyz) {
+    lbm2d *d = h->d2;
+    if (!d->ibm) return f2(LBM_ERR_STATE, "get_markers: no markers set");
+    CK2(cudaMemcpyAsync(xyz, d->ib.pos, (size_t)3 * d->ib.n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
+lbm_status l2d_get_body(lbm_handle *h, double out[9]) {
+    lbm2d *d = h->d2;
+    State2 s;
+    CK2(cudaMemcpyAsync(&s, d->st, sizeof(s), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    for (int a = 0; a < 3; a++) {
+        out[a] = s.center[a];
+        out[3 + a] = s.V[a];
+        out[6 + a] = 0.0;
+    }
+    return LBM_OK;
+}
+
+lbm_status l2d_status(lbm_handle *h, uint32_t *flags) {
+    lbm2d *d = h->d2;
+    uint32_t v = 0;
+    CK2(cudaMemcpyAsync(&v, &d->st->status, sizeof(v), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    *flags = v;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, const uint8_t *types,
+                                                  const double *rho, const double *ux, const double *uy,
+                                                  lbm_config *out) {
+    if (!types || !out || nx < 1 || ny < 1) return f2(LBM_ERR_INVALID, "config_from_types_2d: bad arguments");
+    const int NX = nx + 2;
+    auto at = [&](int i, int j) { return (size_t)i + (size_t)NX * j; };
+    lbm_config c;
+    memset(&c, 0, sizeof(c));
+    c.tau = tau;
+    c.rho0 = 1.0;
+    c.lattice = LBM_LATTICE_D2Q9;
+    for (int j = 1; j <= ny; j++)
+        for (int i = 1; i <= nx; i++)
+            if (types[at(i, j)] != 0)
+                return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: non-fluid cell inside the domain");
+    int periodic_axis[2] = {0, 0};
+    for (int f = 0; f < 4; f++) {
+        const int a = f / 2, side = f % 2;
+        const int lim = a == 0 ? ny : nx;
+        int kind0 = -1;
+        double st[3] = {0, 0, 0};
+        for (int p = 1; p <= lim; p++) {
+            const size_t id = a == 0 ? at(side ? nx + 1 : 0, p) : at(p, side ? ny + 1 : 0);
+            const int t = types[id];
+            const double s[3] = {rho ? rho[id] : 1.0, ux ? ux[id] : 0.0, uy ? uy[id] : 0.0};
+            if (kind0 < 0) {
+                kind0 = t;
+                memcpy(st, s, sizeof(st));
+            } else if (t != kind0 || memcmp(st, s, sizeof(st)) != 0) {
+                return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: face " + std::to_string(f) + " is not uniform");
+            }
+        }
+        lbm_face &F = c.faces[f];
+        F.rho = st[0];
+        F.u[0] = st[1];
+        F.u[1] = st[2];
+        switch (kind0) {
+        case 1: F.kind = LBM_FACE_WALL; break;
+        case 3: F.kind = LBM_FACE_INLET; break;
+        case 2: F.kind = LBM_FACE_OUTLET_EQ; break;
+        case 0: F.kind = LBM_FACE_PERIODIC; periodic_axis[a]++; break;
+        default:
+            return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: unsupported ghost type " + std::to_string(kind0));
+        }
+    }
+    int dims[2] = {nx, ny};
+    for (int a = 0; a < 2; a++) {
+        if (periodic_axis[a] == 1) return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: one-sided TYPE_F ghost face");
+        if (periodic_axis[a] == 2) dims[a] += 2;  // the reference wraps over N+2 cells
+    }
+    c.faces[4].kind = c.faces[5].kind = LBM_FACE_PERIODIC;
+    c.nx = dims[0];
+    c.ny = dims[1];
+    c.nz = 1;
+    *out = c;
+    return LBM_OK;
+}

@@ -1,0 +1,69 @@
+// lbm2d.cuh -- device-side definitions of the D2Q9 solver (lbm2d.cu).
+//
+// Lattice: D2Q9 in the reference order (LBM.h, the D2Q9 tables:
+// c = (0,0) (1,0) (0,1) (-1,0) (0,-1) (1,1) (-1,1) (-1,-1) (1,-1)), so that
+// population l on the device is population l of the reference's
+// LATTICE::f[] in a D2Q9 build.  Populations are kept shifted (f - w), SoA
+// pop[l * S + cell], cell = x + nx * y over the interior of the reference's
+// single computational layer k = 1.
+#pragma once
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+namespace l2d {
+
+constexpr int Q9 = 9;
+
+__host__ __device__ constexpr int cx9(int l) {
+    constexpr int v[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+    return v[l];
+}
+__host__ __device__ constexpr int cy9(int l) {
+    constexpr int v[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+    return v[l];
+}
+__host__ __device__ constexpr int opp9(int l) {
+    constexpr int v[9] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+    return v[l];
+}
+__host__ __device__ constexpr float w9f(int l) { return l == 0 ? (4.0f / 9.0f) : (l < 5 ? (1.0f / 9.0f) : (1.0f / 36.0f)); }
+__host__ __device__ constexpr double w9d(int l) { return l == 0 ? (4.0 / 9.0) : (l < 5 ? (1.0 / 9.0) : (1.0 / 36.0)); }
+
+// Boundary class of a face cell (bit 0: x = 0, 1: x = nx-1, 2: y = 0,
+// 3: y = ny-1; periodic axes set none): per link, bounce-back from a wall,
+// the face equilibrium, or a zero-gradient pull.
+struct Class2 {
+    uint32_t bb, eq, zg;
+    float val[Q9];  // bb: +6 w (c . u_wall);  eq: feq(face) - w
+};
+
+struct Params2 {
+    int nx, ny;
+    long long N, S;
+    float omega;
+    float body[2];
+    int forced;
+    int periodic;   // bit 0: x, bit 1: y
+    int pofs[Q9];   // plain pull offset of link l: -(cx + nx cy)
+    Class2 cls[16];
+    int bsx, bsy;   // allocated box (band) extent; band arrays are [5][bsx * bsy]
+    long long nb;
+    int band_on;
+};
+
+// Device state of a D2Q9 solve.  The body kinematics are those of IBLBM
+// (lbm.cpp:1136-1167): V_CM of the current step and of the step before, the
+// centre, and the box [floor(c - D), ceil(c + D)] of the current step.
+struct State2 {
+    uint32_t status;
+    int box_lo[2];      // device cell of the box's lower corner (reference node - 1)
+    int box_w, box_h;   // box extent of the current step
+    long long ibm_step; // reference step of the current IBM pass (1-based)
+    double center[3];
+    double V[3], Vold[3];
+    int lists_ok;       // spreading lists valid (fixed body)
+    long long hist_cap;
+};
+
+}  // namespace l2d

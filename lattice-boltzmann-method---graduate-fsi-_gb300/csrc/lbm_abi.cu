@@ -232,6 +232,7 @@ extern "C" lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double ta
 
 static void free_handle(lbm_handle *h) {
     if (!h) return;
+    if (h->d2) l2d_free(h);
     for (int i = 0; i < 2; i++) {
         if (h->gexec[i]) cudaGraphExecDestroy(h->gexec[i]);
         if (h->fraw[i]) cudaFree(h->fraw[i]);
@@ -286,6 +287,21 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     }
     for (int f = 0; f < 6; f++)
         if (c.faces[f].kind < 0 || c.faces[f].kind > 4) return fail(LBM_ERR_INVALID, "create: unknown face kind");
+    if (c.lattice != 0 && c.lattice != LBM_LATTICE_D3Q19 && c.lattice != LBM_LATTICE_D2Q9)
+        return fail(LBM_ERR_INVALID, "create: unknown lattice");
+    if (c.lattice == LBM_LATTICE_D2Q9) {
+        lbm_handle *h = new lbm_handle();
+        h->cfg = c;
+        lbm_status st = l2d_create(h);
+        for (int i = 0; i < 4 && st == LBM_OK; i++)
+            if (cudaEventCreate(&h->ev[i]) != cudaSuccess) st = fail(LBM_ERR_CUDA, "create: events");
+        if (st != LBM_OK) {
+            free_handle(h);
+            return st;
+        }
+        *out = h;
+        return LBM_OK;
+    }
     lbm_handle *h = new lbm_handle();
     h->cfg = c;
     memset(&h->P, 0, sizeof(h->P));
@@ -423,6 +439,7 @@ static lbm_status do_init(lbm_handle *h, const float *dfields) {
 
 extern "C" lbm_status lbmgpu_init(lbm_handle *h) {
     if (!h) return fail(LBM_ERR_INVALID, "init: null handle");
+    if (h->d2) return l2d_init(h, nullptr, nullptr, nullptr);
     lbm_status s = do_init(h, nullptr);
     if (s != LBM_OK) return s;
     CUDA_TRY(cudaStreamSynchronize(h->s));
@@ -432,6 +449,7 @@ extern "C" lbm_status lbmgpu_init(lbm_handle *h) {
 extern "C" lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const double *ux, const double *uy,
                                          const double *uz, const double *T) {
     if (!h || !rho || !ux || !uy || !uz) return fail(LBM_ERR_INVALID, "init_fields: null argument");
+    if (h->d2) return l2d_init(h, rho, ux, uy);
     const long long N = h->P.N;
     std::vector<float> tmp((size_t)5 * N);
     for (long long c = 0; c < N; c++) {
@@ -456,6 +474,7 @@ extern "C" lbm_status lbmgpu_init_fields(lbm_handle *h, const double *rho, const
 extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *ds,
                                          const double *udes) {
     if (!h || !ic || !xyz || !ds) return fail(LBM_ERR_INVALID, "set_markers: null argument");
+    if (h->d2) return l2d_set_markers(h, ic, xyz, ds);
     if (ic->n_markers < 1 || ic->m_max < 1) return fail(LBM_ERR_INVALID, "set_markers: need markers and m_max >= 1");
     if (!(ic->radius > 0)) return fail(LBM_ERR_INVALID, "set_markers: radius must be > 0");
     if (ic->free_body && (!(ic->density_ratio > 0.0) || !(ic->volume > 0.0) || !(ic->inertia > 0.0)))
@@ -697,6 +716,7 @@ static lbm_status ensure_graph(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_step(lbm_handle *h, int nsteps) {
     if (!h) return fail(LBM_ERR_INVALID, "step: null handle");
+    if (h->d2) return l2d_step(h, nsteps);
     if (!h->inited) return fail(LBM_ERR_STATE, "step: call lbmgpu_init first");
     if (nsteps < 0) return fail(LBM_ERR_INVALID, "step: negative step count");
     while (nsteps > 0) {
@@ -751,6 +771,7 @@ extern "C" lbm_status lbmgpu_step_timed(lbm_handle *h, int nsteps, double *ms) {
 static lbm_status step_phases(lbm_handle *h, int nsteps, double *total, double *fused, double *near_ms,
                               double *ibm_ms) {
     if (!h) return fail(LBM_ERR_INVALID, "step_profiled: null handle");
+    if (h->d2) return fail(LBM_ERR_UNSUPPORTED, "step_profiled: not for D2Q9 handles (use lbmgpu_step_timed)");
     if (!h->inited) return fail(LBM_ERR_STATE, "step_profiled: call lbmgpu_init first");
     if (nsteps < 0) return fail(LBM_ERR_INVALID, "step_profiled: negative step count");
     // all events are read after the last step so the host never stalls the
@@ -819,6 +840,7 @@ static lbm_status export_moments(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host) {
     if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
+    if (h->d2) return l2d_download_f32(h, field, host);
     if (field < 0 || field > 7 || (field >= 4 && !h->cfg.thermal)) return fail(LBM_ERR_INVALID, "download: bad field");
     lbm_status s = export_moments(h);
     if (s != LBM_OK) return s;
@@ -830,6 +852,7 @@ extern "C" lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host)
 
 extern "C" lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host) {
     if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
+    if (h->d2) return l2d_download_all_f32(h, host);
     lbm_status s = export_moments(h);
     if (s != LBM_OK) return s;
     const int nf = h->cfg.thermal ? 5 : 4;
@@ -840,7 +863,7 @@ extern "C" lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host) {
 
 extern "C" lbm_status lbmgpu_download(lbm_handle *h, int field, double *host) {
     if (!h || !host) return fail(LBM_ERR_INVALID, "download: null argument");
-    std::vector<float> tmp((size_t)h->P.N);
+    std::vector<float> tmp((size_t)h->cfg.nx * h->cfg.ny * h->cfg.nz);
     lbm_status s = lbmgpu_download_f32(h, field, tmp.data());
     if (s != LBM_OK) return s;
     for (size_t i = 0; i < tmp.size(); i++) host[i] = tmp[i];
@@ -852,6 +875,7 @@ extern "C" lbm_status lbmgpu_download(lbm_handle *h, int field, double *host) {
 // ---------------------------------------------------------------------------
 extern "C" lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask) {
     if (!h || !mask) return fail(LBM_ERR_INVALID, "set_solids: null argument");
+    if (h->d2) return fail(LBM_ERR_UNSUPPORTED, "set_solids: not for D2Q9 handles");
     if (h->inited) return fail(LBM_ERR_STATE, "set_solids: call before lbmgpu_init");
     if (h->solids) return fail(LBM_ERR_STATE, "set_solids: solids already set");
     const int nx = h->P.nx, ny = h->P.ny, nz = h->P.nz;
@@ -947,6 +971,7 @@ extern "C" lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int ma
 
 extern "C" lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
     if (!h || !out || max_steps < 0) return fail(LBM_ERR_INVALID, "get_forces: bad argument");
+    if (h->d2) return l2d_get_forces(h, out, max_steps, n_out);
     if (!h->ibm) return fail(LBM_ERR_STATE, "get_forces: no markers set");
     DevState d;
     CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
@@ -967,8 +992,15 @@ extern "C" lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_step
     return LBM_OK;
 }
 
+extern "C" lbm_status lbmgpu_set_marker_normals(lbm_handle *h, const double *nxyz) {
+    if (!h || !nxyz) return fail(LBM_ERR_INVALID, "set_marker_normals: null argument");
+    if (!h->d2) return fail(LBM_ERR_UNSUPPORTED, "set_marker_normals: D2Q9 handles only");
+    return l2d_set_normals(h, nxyz);
+}
+
 extern "C" lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]) {
     if (!h || !out) return fail(LBM_ERR_INVALID, "get_body: null argument");
+    if (h->d2) return l2d_get_body(h, out);
     DevState d;
     CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
     CUDA_TRY(cudaStreamSynchronize(h->s));
@@ -982,6 +1014,7 @@ extern "C" lbm_status lbmgpu_get_body(lbm_handle *h, double out[9]) {
 
 extern "C" lbm_status lbmgpu_get_markers(lbm_handle *h, double *xyz) {
     if (!h || !xyz) return fail(LBM_ERR_INVALID, "get_markers: null argument");
+    if (h->d2) return l2d_get_markers(h, xyz);
     if (!h->ibm) return fail(LBM_ERR_STATE, "get_markers: no markers set");
     CUDA_TRY(cudaMemcpyAsync(xyz, h->mk.pos, (size_t)3 * h->mk.n * sizeof(double), cudaMemcpyDeviceToHost, h->s));
     CUDA_TRY(cudaStreamSynchronize(h->s));
@@ -991,8 +1024,13 @@ extern "C" lbm_status lbmgpu_get_markers(lbm_handle *h, double *xyz) {
 extern "C" lbm_status lbmgpu_status(lbm_handle *h, uint32_t *flags) {
     if (!h || !flags) return fail(LBM_ERR_INVALID, "status: null argument");
     uint32_t v = 0;
-    CUDA_TRY(cudaMemcpyAsync(&v, &h->ds->status, sizeof(v), cudaMemcpyDeviceToHost, h->s));
-    CUDA_TRY(cudaStreamSynchronize(h->s));
+    if (h->d2) {
+        lbm_status st = l2d_status(h, &v);
+        if (st != LBM_OK) return st;
+    } else {
+        CUDA_TRY(cudaMemcpyAsync(&v, &h->ds->status, sizeof(v), cudaMemcpyDeviceToHost, h->s));
+        CUDA_TRY(cudaStreamSynchronize(h->s));
+    }
     *flags = v;
     if (v & ST_RHO_RANGE) return fail(LBM_ERR_DIVERGED, "status: density left (0, 100) or became NaN");
     return LBM_OK;

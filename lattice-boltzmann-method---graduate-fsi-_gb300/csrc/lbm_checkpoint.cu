@@ -86,6 +86,7 @@ CkptHeader header_of(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_save_state(lbm_handle *h, const char *path) {
     if (!h || !path) return ck_fail(LBM_ERR_INVALID, "save_state: null argument");
+    if (h->d2) return ck_fail(LBM_ERR_UNSUPPORTED, "save_state: not for D2Q9 handles");
     if (!h->inited) return ck_fail(LBM_ERR_STATE, "save_state: call lbmgpu_init first");
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     FILE *fp = fopen(path, "wb");
@@ -106,6 +107,7 @@ extern "C" lbm_status lbmgpu_save_state(lbm_handle *h, const char *path) {
 
 extern "C" lbm_status lbmgpu_load_state(lbm_handle *h, const char *path) {
     if (!h || !path) return ck_fail(LBM_ERR_INVALID, "load_state: null argument");
+    if (h->d2) return ck_fail(LBM_ERR_UNSUPPORTED, "load_state: not for D2Q9 handles");
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     FILE *fp = fopen(path, "rb");
     if (!fp) return ck_fail(LBM_ERR_INVALID, std::string("load_state: cannot open ") + path);

@@ -184,6 +184,7 @@ cudaError_t lbm_details_async(lbm_handle *h, int smp_fold, double told, double d
 
 extern "C" lbm_status lbmgpu_set_more_details(lbm_handle *h, int on) {
     if (!h) return det_fail(LBM_ERR_INVALID, "set_more_details: null handle");
+    if (h->d2) return det_fail(LBM_ERR_UNSUPPORTED, "set_more_details: not for D2Q9 handles");
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     if (!on) {
         if (h->det) cudaFree(h->det);

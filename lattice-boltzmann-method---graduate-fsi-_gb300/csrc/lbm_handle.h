@@ -13,6 +13,7 @@
 #include "lbm_internal.h"
 
 struct lbm_output;  // asynchronous writer (lbm_output.cu)
+struct lbm2d;       // D2Q9 solve (lbm2d.cu)
 
 using lbmk::BodyParams;
 using lbmk::MarkerDev;
@@ -69,7 +70,24 @@ struct lbm_handle {
     double *stats = nullptr;              // [20][N]: Sup_MacroProp averages and rms values
     int stat_samples = 0;                 // samples folded in
     double stat_told = 0.0;               // told of the latest sample
+    // D2Q9 handles (lattice = 9): everything lives in d2; the fields above
+    // other than cfg, s, ev, esize, steps, inited and dev_bytes stay unused
+    lbm2d *d2 = nullptr;
 };
+
+// D2Q9 solves (lbm2d.cu), reached through the same entry points.
+lbm_status l2d_create(lbm_handle *h);
+void l2d_free(lbm_handle *h);
+lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const double *uy);
+lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *ds);
+lbm_status l2d_set_normals(lbm_handle *h, const double *nxyz);
+lbm_status l2d_step(lbm_handle *h, int nsteps);
+lbm_status l2d_download_f32(lbm_handle *h, int field, float *host);
+lbm_status l2d_download_all_f32(lbm_handle *h, float *host);
+lbm_status l2d_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+lbm_status l2d_get_markers(lbm_handle *h, double *xyz);
+lbm_status l2d_get_body(lbm_handle *h, double out[9]);
+lbm_status l2d_status(lbm_handle *h, uint32_t *flags);
 
 // Launch the gather-only export of the current state's moments into h->mom
 // (rho, ux, uy, uz [, T]) on h->s.

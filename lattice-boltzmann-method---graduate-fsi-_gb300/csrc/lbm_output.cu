@@ -356,6 +356,7 @@ void lbm_output_free(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
     if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_vtk: bad argument");
+    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_vtk: not for D2Q9 handles");
     if (!h->inited) return out_fail(LBM_ERR_STATE, "output_vtk: call lbmgpu_init first");
     if (!h->out) {
         h->out = new lbm_output();
@@ -433,6 +434,7 @@ extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, d
 
 extern "C" lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
     if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_avg_vtk: bad argument");
+    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_avg_vtk: not for D2Q9 handles");
     if (!h->details) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_set_more_details first");
     if (!h->inited) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_init first");
     if (h->out) {
@@ -519,6 +521,7 @@ extern "C" lbm_status lbmgpu_output_wait(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_output_markers_vtk(lbm_handle *h, const char *path) {
     if (!h || !path) return out_fail(LBM_ERR_INVALID, "output_markers: bad argument");
+    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_markers: not for D2Q9 handles");
     if (!h->ibm) return out_fail(LBM_ERR_STATE, "output_markers: no markers set");
     const int n = h->mk.n;
     std::vector<double> pos(3 * (size_t)n);

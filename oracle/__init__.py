@@ -135,7 +135,7 @@ class IbmOpts(C.Structure):
     _fields_ = [("box_lo", C.c_int * 3), ("box_hi", C.c_int * 3), ("m_max", C.c_int),
                 ("lit_sign", C.c_int), ("rho_mode", C.c_int), ("thermal", C.c_int),
                 ("use_avg_density", C.c_int), ("vsolid", C.c_double),
-                ("vcm_new", C.c_double * 3), ("vcm_old", C.c_double * 3)]
+                ("vcm_new", C.c_double * 3), ("vcm_old", C.c_double * 3), ("scheme", C.c_int)]
 
 
 class Body(C.Structure):
@@ -556,3 +556,74 @@ def cavity_details_run(n: int, tau: float, lid: float, steps: int, nt: int = 10)
     if det is None:
         det = details(lat)
     return lat, det, stats
+
+
+# --------------------------------------------------------------------------
+# The reference's two-dimensional IBM cylinders (D2Q9)
+# --------------------------------------------------------------------------
+
+def cylinder2d_literal(nx: int, ny: int, D: float, nodes: int, m_max: int, steps: int, u_max: float = 0.1,
+                       Re: float = 40.0, scheme: int = 0, motion=None, vsolid: float | None = None,
+                       marker_dy: float = 0.0):
+    """The reference's D2Q9 IBM cylinder loop (main.cpp:195-205) in its
+    literal options: main_setup_Cylinder_IBM (TYPE_IN at x = 0, TYPE_OUT
+    elsewhere, u = u_max), Generate_Cylinder_Marker at (Nx/5, Ny/2), and every
+    step IBLBM's kinematics (lbm.cpp:1137-1167: V_CM from motion(t), markers
+    and centre moved by the trapezoid, the box [floor(c - D), ceil(c + D)])
+    followed by the forcing (implicit, or explicit with scheme = 1; force
+    sign, nearest-node density and added mass as the reference), Collision
+    and Streaming.  motion(t) -> (Vx, Vy, Vz) or None for a fixed body.
+    marker_dy shifts the markers (not the centre, so not the box): the
+    transverse-oscillation case generates them at center_y + amplitude
+    (lbm.cpp:1966).  Returns the lattice, the markers, Cl and Cd per step
+    (C = F / (1/2 u^2 D))."""
+    import math
+
+    tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
+    lat = Lattice(9, nx, ny, 1, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    t[:, :, 0] = TYPE_IN
+    t[:, :, -1] = TYPE_OUT
+    t[:, 0, :] = TYPE_OUT
+    t[:, -1, :] = TYPE_OUT
+    lat.ux[:] = u_max
+    lat.init()
+    cx, cy = nx / 5.0, ny / 2.0
+    mk = cylinder_markers_literal(nodes, D, cx, cy + marker_dy)
+    if vsolid is None:
+        vsolid = REF_PI * D * D * 0.25
+    V = [0.0, 0.0, 0.0]
+    cl, cd = [], []
+    for s in range(1, steps + 1):
+        Vold = V
+        V = list(motion(s * 1.0)) if motion else [0.0, 0.0, 0.0]
+        for a, nm in enumerate(("x", "y", "z")):
+            mk[nm][:] += (V[a] + Vold[a]) * 1.0 / 2
+        for a, nm in enumerate(("udx", "udy", "udz")):
+            mk[nm][:] = V[a]
+        cx += (V[0] + Vold[0]) * 1.0 / 2
+        cy += (V[1] + Vold[1]) * 1.0 / 2
+        lo = [math.floor(cx - D), math.floor(cy - D), 1]
+        hi = [math.ceil(cx + D), math.ceil(cy + D), 1]
+        op = ibm_opts(lo, hi, m_max, lit_sign=1, rho_mode=1)
+        op.use_avg_density = 1
+        op.vsolid = vsolid
+        op.scheme = scheme
+        for a in range(3):
+            op.vcm_new[a] = V[a]
+            op.vcm_old[a] = Vold[a]
+        out = lat.step_ibm(mk, op, [cx, cy, 1.0])
+        cl.append(out[1] / (0.5 * 1.0 * u_max ** 2 * D))
+        cd.append(out[0] / (0.5 * 1.0 * u_max ** 2 * D))
+    return lat, mk, np.array(cl), np.array(cd)
+
+
+def transverse_motion(amplitude: float, frequency: float):
+    """V_CM(t) of Cylinder_Transverse_Oscillation (lbm.cpp:1146-1148)."""
+    import math
+
+    def v(t):
+        return (0.0, -2 * REF_PI * frequency * amplitude * math.sin(2 * REF_PI * frequency * t), 0.0)
+
+    return v

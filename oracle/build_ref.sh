@@ -10,6 +10,8 @@
 #   cavity:N[:TAU]            D3Q19 cavity, N^3 interior
 #   details:N[:TAU]           the same cavity in MORE_DETAILS mode
 #   cylinder:NX:NY:D:NODES:M  D2Q9 implicit IBM cylinder
+#   explicit:NX:NY:D:NODES    the same cylinder, explicit direct forcing
+#   transverse:NX:NY:D:NODES:M:AMP:FREQ  D2Q9 cylinder oscillating across the stream
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -20,7 +22,8 @@ if [ ! -f "$REF/lbm.cpp" ]; then
     exit 0
 fi
 mkdir -p "$OUT"
-[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05 details:8:0.8
+[ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05 details:8:0.8 \
+    explicit:80:40:10:40 transverse:80:40:10:40:5:2.0:0.005
 CXX=${CXX:-g++}
 FLAGS="-O2 -fopenmp -ffp-contract=off -w -include $HERE/ref_config.h -I$HERE/shim -I$REF"
 pids=""
@@ -45,6 +48,21 @@ for v in "$@"; do
         exe="$OUT/ref_cylinder_${nx}_${ny}_${d}_${nodes}_${mm}"
         $CXX $FLAGS -DREF_CYLINDER -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
             -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    explicit)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        nodes=$(echo "$v" | cut -d: -f5)
+        exe="$OUT/ref_explicit_${nx}_${ny}_${d}_${nodes}"
+        $CXX $FLAGS -DREF_CYLINDER -DREF_EXPLICIT -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=1 \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    transverse)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        nodes=$(echo "$v" | cut -d: -f5); mm=$(echo "$v" | cut -d: -f6); amp=$(echo "$v" | cut -d: -f7)
+        fr=$(echo "$v" | cut -d: -f8)
+        exe="$OUT/ref_transverse_${nx}_${ny}_${d}_${nodes}_${mm}_${amp}_${fr}"
+        $CXX $FLAGS -DREF_TRANSVERSE -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
+            -DREF_AMP=$amp -DREF_FREQ=$fr -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     sphere)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)

@@ -467,6 +467,7 @@ typedef struct orc_ibm_opts {
     int use_avg_density; /* 1: Calc_AverageDensity for the added-mass term */
     double vsolid;     /* V_solid for the added-mass term */
     double vcm_new[3], vcm_old[3];
+    int scheme;        /* 0: implicit multi-direct forcing; 1: explicit direct forcing */
 } orc_ibm_opts;
 
 static inline int ibm_node_ok(uint8_t t) { return t == ORC_F || t == ORC_IN || t == ORC_OUT || t == ORC_OUTZG; }
@@ -690,10 +691,77 @@ void orc_ibm_step(orc *o, orc_markers *mk, const orc_ibm_opts *op, const double 
     force_out[6] = heat;
 }
 
+/* IBLBM explicit direct forcing (lbm.cpp:1171-1258, Cylinder_IBM branch):
+ * unforced rho, u on every F/IN/OUT cell (F kept); the unforced velocity
+ * interpolated at the markers; F_m = 2 rho (U_des - U_m) with rho at
+ * NearestLatticeCoordinate over [floor x, ceil x] x [floor y, ceil y] x [1, 1];
+ * on the box nodes F = sum_m F_m ds_m delta (reset first), u += F / 2 rho and
+ * Drag/Lift += -F dx^2 (summed in node order; the reference's OpenMP loop
+ * adds them without a reduction).  Then the added mass, as in the implicit
+ * scheme.  force_out as orc_ibm_step (torque and heat 0). */
+void orc_ibm_step_explicit(orc *o, orc_markers *mk, const orc_ibm_opts *op, double force_out[7]) {
+    long n = o->ncell;
+    double drag[3] = {0, 0, 0};
+#pragma omp parallel for
+    for (long c = 0; c < n; c++) {
+        if (!ibm_node_ok(o->type[c])) continue;
+        double rho = 0, r0 = 0, r1 = 0, r2 = 0;
+        for (int l = 0; l < o->q; l++) {
+            double fl = o->f[l * n + c];
+            rho += fl; r0 += fl * o->cx[l]; r1 += fl * o->cy[l]; r2 += fl * o->cz[l];
+        }
+        o->rho[c] = rho;
+        o->ux[c] = r0 / rho; o->uy[c] = r1 / rho; o->uz[c] = r2 / rho;
+    }
+    int N = mk->n;
+    for (int m = 0; m < N; m++) {
+        double u3[3];
+        interp3(o, op, mk->x[m], mk->y[m], mk->z[m], o->ux, o->uy, o->uz, u3);
+        mk->ubx[m] = u3[0]; mk->uby[m] = u3[1]; mk->ubz[m] = u3[2];
+        orc_ibm_opts near = *op;
+        near.box_lo[0] = (int)floor(mk->x[m]); near.box_hi[0] = (int)ceil(mk->x[m]);
+        near.box_lo[1] = (int)floor(mk->y[m]); near.box_hi[1] = (int)ceil(mk->y[m]);
+        near.box_lo[2] = 1; near.box_hi[2] = 1;
+        double rho = o->rho[nearest_node(o, &near, mk, m)];
+        mk->Fbx[m] = 2 * rho * (mk->udx[m] - mk->ubx[m]) / 1.0;
+        mk->Fby[m] = 2 * rho * (mk->udy[m] - mk->uby[m]) / 1.0;
+        mk->Fbz[m] = 2 * rho * (mk->udz[m] - mk->ubz[m]) / 1.0;
+    }
+    for (int i = op->box_lo[0]; i <= op->box_hi[0]; i++)
+        for (int j = op->box_lo[1]; j <= op->box_hi[1]; j++)
+            for (int k = op->box_lo[2]; k <= op->box_hi[2]; k++) {
+                long c = IDX(o, i, j, k);
+                if (!ibm_node_ok(o->type[c])) continue;
+                double F[3] = {0, 0, 0};
+                for (int m = 0; m < N; m++) {
+                    double dl = orc_kernel(i - mk->x[m]) * orc_kernel(j - mk->y[m]) * orc_kernel(k - mk->z[m]);
+                    F[0] += mk->Fbx[m] * mk->ds[m] * dl;
+                    F[1] += mk->Fby[m] * mk->ds[m] * dl;
+                    F[2] += mk->Fbz[m] * mk->ds[m] * dl;
+                }
+                o->Fx[c] = F[0]; o->Fy[c] = F[1]; o->Fz[c] = F[2];
+                o->ux[c] += 1.0 * F[0] / (2 * o->rho[c]);
+                o->uy[c] += 1.0 * F[1] / (2 * o->rho[c]);
+                o->uz[c] += 1.0 * F[2] / (2 * o->rho[c]);
+                drag[0] += -F[0] * 1.0;
+                drag[1] += -F[1] * 1.0;
+            }
+    if (op->use_avg_density) {
+        double rho = average_density(o, op, mk);
+        drag[0] += rho * op->vsolid * (op->vcm_new[0] - op->vcm_old[0]) / 1.0;
+        drag[1] += rho * op->vsolid * (op->vcm_new[1] - op->vcm_old[1]) / 1.0;
+    }
+    force_out[0] = drag[0]; force_out[1] = drag[1]; force_out[2] = drag[2];
+    force_out[3] = force_out[4] = force_out[5] = force_out[6] = 0.0;
+}
+
 /* One IBM time step in the reference order (main.cpp:197-205):
  * IBLBM -> Collision -> Streaming.  Returns feq<0 count. */
 long orc_step_ibm(orc *o, orc_markers *mk, const orc_ibm_opts *op, const double center[3], double force_out[7]) {
-    orc_ibm_step(o, mk, op, center, force_out);
+    if (op->scheme == 1)
+        orc_ibm_step_explicit(o, mk, op, force_out);
+    else
+        orc_ibm_step(o, mk, op, center, force_out);
     long bad = orc_collide(o);
     orc_stream(o);
     return bad;

@@ -10,7 +10,12 @@
  *                 Sphere_BB case flag is used only to select the reference's
  *                 3D code paths; the harness sets the geometry itself.
  *   REF_CYLINDER  D2Q9 implicit IBM cylinder (the shipped default case),
- *                 shrunk to test size.
+ *                 shrunk to test size; with REF_EXPLICIT the explicit
+ *                 direct-forcing scheme instead.
+ *   REF_TRANSVERSE  D2Q9 implicit IBM cylinder oscillating across the
+ *                 stream (the reference's Cylinder_Transverse_Oscillation),
+ *                 shrunk; REF_AMP and REF_FREQ set its amplitude and
+ *                 frequency.
  *   REF_SPHERE    D3Q19 staircase sphere with momentum-exchange Cl/Cd (the
  *                 reference's Sphere_BB case), shrunk to test size; REF_D,
  *                 REF_RE and REF_U set the diameter, Reynolds number and
@@ -70,7 +75,11 @@ static const double nu = cs2 * (tau - 0.5);
 #define Nt 10
 #elif defined REF_CYLINDER
 #define IBM
+#if defined REF_EXPLICIT
+#define Explicit_Diffuse_Interface_Scheme
+#else
 #define Implicit_Diffuse_Interface_Scheme
+#endif
 #define Cylinder_IBM
 #define Volume_Force
 #define D2Q9
@@ -88,6 +97,36 @@ static const int number_nodes = REF_NODES;
 static const int level_marker = 1;
 static int m_max = REF_MMAX;
 static const double Vsolid = PI * D * D * 0.25;
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_TRANSVERSE
+#define IBM
+#define Implicit_Diffuse_Interface_Scheme
+#define Cylinder_Transverse_Oscillation
+#define Volume_Force
+#define D2Q9
+#define Re 100.0
+static const double D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static const double u_max = 0.05;
+static const double amplitude = REF_AMP;
+static const double frequency_e = REF_FREQ;
+// the quantities the reference derives frequency_e from (LBM.h:407-414),
+// printed by print_Info only
+static const double ratio_Amd = amplitude / D;
+static const double frequency_ratio = 1.2;
+static const double frequency_0 = frequency_e / frequency_ratio;
+static const double Strouhal_number = frequency_0 * D / u_max;
+static double center_x = dx * (Nx / 5.0);
+static double center_y = dy * (Ny / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+static const double Vsolid = PI * D * D * 0.25 * (Nz + 2);
+static const int number_nodes = REF_NODES;
+static const int level_marker = 1;
+static int m_max = REF_MMAX;
 #define T_OUT 30000
 #define Nt 10
 #elif defined REF_SPHERE
@@ -108,5 +147,5 @@ static const double tau = 0.5 * dt + nu / cs2;
 #define T_OUT 30000
 #define Nt 10
 #else
-#error "define REF_CAVITY, REF_CYLINDER or REF_SPHERE"
+#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE or REF_SPHERE"
 #endif

@@ -103,8 +103,12 @@ int main(int argc, char **argv) {
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cavity\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
-#elif defined REF_CYLINDER
+#elif defined REF_CYLINDER || defined REF_TRANSVERSE
+#if defined REF_TRANSVERSE
+    LBM lb = main_setup_Cylinder_TransverseOscillating();
+#else
     LBM lb = main_setup_Cylinder_IBM();
+#endif
     std::vector<MARKER> marker(number_nodes);
     Generate_Cylinder_Marker(marker);
     // arc-length weights as main.cpp:123-131 computes them
@@ -136,7 +140,7 @@ int main(int argc, char **argv) {
     }
     fclose(fp);
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
-    printf("{\"case\": \"cylinder\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
+    printf("{\"case\": \"cylinder2d\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
 #elif defined REF_SPHERE
     LBM lb = main_setup_Sphere();

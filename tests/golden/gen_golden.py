@@ -20,6 +20,18 @@ outputs are stored as small .npz fixtures:
                                     k = 12 and j = 12 of rho, u, interior
                                     sums and maxima, momentum-exchange Cl
                                     and Cd after every step
+  cylinder80x40_D10_n40_explicit_100.npz  the same cylinder with the
+                                    explicit direct-forcing scheme (run on
+                                    one thread: the reference's drag sum is
+                                    an unsynchronised OpenMP update)
+  cylinder80x40_D10_n40_m5_transverse_100.npz  the cylinder oscillating
+                                    across the stream
+                                    (Cylinder_Transverse_Oscillation, A = 2,
+                                    f = 0.005, u = 0.05, Re = 100)
+                                    These two keep Cl, Cd, the markers, and
+                                    rho, u, F in the IBM box window
+                                    i = 4..28, j = 8..32 of the k = 1 layer
+                                    plus sums over the whole layer
   cavity8_details_200.npz           the 8^3 cavity (tau = 0.8, lid 0.05)
                                     built in MORE_DETAILS mode, 200 steps,
                                     Sup_MacroProp every 10 steps: every
@@ -77,7 +89,7 @@ def main() -> None:
     ap.add_argument("--skip-cav64", action="store_true")
     a = ap.parse_args()
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
-                     "details:8:0.8")
+                     "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005")
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -118,6 +130,17 @@ def main() -> None:
                         ymid=f[:, :, 12, :], sums=f.reshape(4, -1).sum(axis=1),
                         absmax=np.abs(f.reshape(4, -1)).max(axis=1), cl=r["cl"], cd=r["cd"], nx=48, ny=24, nz=24,
                         D=8.0, Re=20.0, u=0.05, steps=steps)
+    # 2D cylinders: explicit scheme, transverse oscillation (100 steps)
+    for exe, name, env in (("ref_explicit_80_40_10_40", "cylinder80x40_D10_n40_explicit_100.npz", {"OMP_NUM_THREADS": "1"}),
+                           ("ref_transverse_80_40_10_40_5_2.0_0.005", "cylinder80x40_D10_n40_m5_transverse_100.npz", {})):
+        p = os.path.join(tmp, name + ".bin")
+        subprocess.check_call([os.path.join(REF, exe), "100", p], env=dict(os.environ, **env))
+        r = oracle.read_ref_dump(p, 82, 42, 3, 7, 100, 40)
+        fl = r["fields"][:, 1]  # k = 1 layer, [field][j][i]
+        np.savez_compressed(os.path.join(OUT, name), window=fl[[0, 1, 2, 4, 5], 8:33, 4:29],
+                            sums=fl[[0, 1, 2, 4, 5]].reshape(5, -1).sum(axis=1), cl=r["cl"], cd=r["cd"],
+                            markers=r["markers"], nx=80, ny=40, D=10.0, nodes=40, steps=100)
+
     # MORE_DETAILS cavity, 200 steps (averages sampled every Nt = 10 steps)
     d = os.path.join(tmp, "det")
     os.makedirs(d)

@@ -1,0 +1,198 @@
+"""GPU parity for the D2Q9 build (the reference's #define D2Q9, Nz = 1):
+D2Q9 collide-stream with its boundary classes against the FP64 oracle, and
+the two-dimensional IBM cylinders -- the shipped default (implicit
+multi-direct forcing), the explicit scheme and the transversely oscillating
+body -- against the reference's own runs (tests/golden).
+
+Tolerances: FP32 fields within 1e-5 of the reference velocity; Cl and Cd of
+the IBM cylinders within 2e-6 of the largest |Cd| of the run (measured: 7.0e-8
+implicit, 1.1e-7 explicit, 3.9e-7 oscillating; the force sums run over FP32
+velocities); FP16 storage within 1e-3 (measured 2.4e-4)."""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+pytestmark = pytest.mark.gpu
+
+CX9 = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+CY9 = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+
+
+def _layer_moments(lat, xs=slice(1, -1), body=(0.0, 0.0)):
+    """rho, u = (sum f c + F/2) / rho of the oracle's computational layer
+    k = 1, interior rows, columns xs."""
+    f = lat.f[:, 1, 1:-1, xs]
+    rho = f.sum(axis=0)
+    ux = (np.tensordot(CX9, f, axes=(0, 0)) + 0.5 * body[0]) / rho
+    uy = (np.tensordot(CY9, f, axes=(0, 0)) + 0.5 * body[1]) / rho
+    return rho, ux, uy
+
+
+def _check_fields(m, rho, ux, uy, uref, tol=1e-5):
+    e = max(np.abs(m["ux"][0] - ux).max(), np.abs(m["uy"][0] - uy).max()) / uref
+    er = np.abs(m["rho"][0] - rho).max()
+    assert e < tol and er < tol, (e, er)
+    assert not np.any(m["uz"])
+    return e
+
+
+def test_d2q9_cavity_vs_oracle(pkg, orc):
+    nx, ny, tau, lid, steps = 48, 32, 0.7, 0.05, 400
+    lat = orc.Lattice(9, nx, ny, 1, tau)
+    t = lat.types
+    t[:] = orc.TYPE_S
+    t[:, 1:-1, 1:-1] = orc.TYPE_F
+    lat.ux[:, -1, :] = lid
+    lat.init()
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t[1], lat.rho[1], lat.ux[1], lat.uy[1])
+    assert cfg.lattice == pkg.LATTICE_D2Q9 and cfg.nz == 1
+    s = pkg.Solver(cfg)
+    s.init()
+    s.step(steps)
+    assert s.status() == 0
+    lat.step_plain(steps)
+    _check_fields(s.moments(), *_layer_moments(lat), lid)
+
+
+def test_d2q9_poiseuille_periodic_forced_vs_oracle(pkg, orc):
+    """Periodic in x over the Nx + 2 columns (TYPE_F ghosts), walls in y,
+    a uniform body force (MacroProp's F/2 shift, Guo source)."""
+    nx, ny, tau, steps, fx = 6, 24, 0.9, 600, 2e-6
+    lat = orc.Lattice(9, nx, ny, 1, tau)
+    t = lat.types
+    t[:] = orc.TYPE_F
+    t[:, 0, :] = orc.TYPE_S
+    t[:, -1, :] = orc.TYPE_S
+    lat.init()
+    lat.set_body_force(fx, 0.0, 0.0)
+    # main_setup_Poiseuille sets F = -dp/dx at set-up (lbm.cpp:1518), so the
+    # first collision is forced too
+    lat.Fx[t == orc.TYPE_F] = fx
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t[1], lat.rho[1], lat.ux[1], lat.uy[1])
+    assert (cfg.nx, cfg.ny) == (nx + 2, ny)
+    cfg.body_force[0] = fx
+    s = pkg.Solver(cfg)
+    s.init()
+    s.step(steps)
+    lat.step_plain(steps)
+    rho, ux, uy = _layer_moments(lat, xs=slice(None), body=(fx, 0.0))
+    umax = np.abs(ux).max()
+    assert umax > 1e-4
+    _check_fields(s.moments(), rho, ux, uy, umax)
+
+
+def _cylinder_gpu(pkg, orc, g, steps, storage="f32", graph_steps=0, **kw):
+    nx, ny, D, nodes = int(g["nx"]), int(g["ny"]), float(g["D"]), int(g["nodes"])
+    u_max, Re = kw.pop("u_max", 0.1), kw.pop("Re", 40.0)
+    marker_dy = kw.pop("marker_dy", 0.0)
+    tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
+    t = np.zeros((ny + 2, nx + 2), np.uint8)
+    t[:, 0] = orc.TYPE_IN
+    t[:, -1] = orc.TYPE_OUT
+    t[0, :] = orc.TYPE_OUT
+    t[-1, :] = orc.TYPE_OUT
+    ones = np.ones((ny + 2, nx + 2))
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t, ones, u_max * ones, 0.0 * ones)
+    cfg.storage = pkg.STORAGE[storage]
+    cfg.graph_steps = graph_steps
+    cfg.u0[0] = u_max
+    s = pkg.Solver(cfg)
+    s.init()
+    cx, cy = nx / 5.0, ny / 2.0
+    mk = orc.cylinder_markers_literal(nodes, D, cx, cy + marker_dy)
+    xyz = np.stack([mk["x"], mk["y"], mk["z"]])
+    nrm = np.stack([mk["nx"], mk["ny"], mk["nz"]])
+    vsolid = kw.pop("vsolid", orc.REF_PI * D * D * 0.25)
+    s.set_markers(xyz, mk["ds"], D / 2.0, (cx, cy, 1.0), literal_sign=True, normals=nrm, rho_nearest=True,
+                  added_mass=True, volume=vsolid, **kw)
+    s.step(steps)
+    assert s.status() == 0
+    rows = s.forces()
+    assert rows.shape[0] == steps and np.array_equal(rows[:, 7], np.arange(1, steps + 1))
+    q = 0.5 * u_max ** 2 * D
+    return s, rows[:, 1] / q, rows[:, 0] / q
+
+
+def _coeff_err(cl, cd, g):
+    scale = np.abs(g["cd"]).max()
+    return max(np.abs(cd - g["cd"]).max(), np.abs(cl - g["cl"]).max()) / scale
+
+
+def test_d2q9_ibm_cylinder_vs_reference(pkg, orc):
+    """The shipped default case (Cylinder_IBM, implicit forcing, literal force
+    sign, nearest-node density, added mass), shrunk: Cl / Cd after every step
+    against the reference's run, the fields against the oracle (pinned to the
+    same run)."""
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    steps = int(g["steps"])
+    s, cl, cd = _cylinder_gpu(pkg, orc, g, steps, m_max=int(g["m_max"]))
+    e = _coeff_err(cl, cd, g)
+    print("cylinder Cl/Cd error / max|Cd|: %.3g" % e)
+    assert e < 2e-6
+    lat, mk, _, _ = orc.cylinder2d_literal(80, 40, 10.0, 40, int(g["m_max"]), steps)
+    _check_fields(s.moments(), *_layer_moments(lat), 0.1)
+
+
+def test_d2q9_ibm_explicit_vs_reference(pkg, orc):
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_explicit_100.npz"))
+    s, cl, cd = _cylinder_gpu(pkg, orc, g, int(g["steps"]), m_max=1, scheme=1)
+    e = _coeff_err(cl, cd, g)
+    print("explicit Cl/Cd error / max|Cd|: %.3g" % e)
+    assert e < 2e-6
+    lat, _, _, _ = orc.cylinder2d_literal(80, 40, 10.0, 40, 1, int(g["steps"]), scheme=1)
+    _check_fields(s.moments(), *_layer_moments(lat), 0.1)
+
+
+def test_d2q9_ibm_transverse_oscillation_vs_reference(pkg, orc):
+    """Moving markers and box (V_CM(t) of Cylinder_Transverse_Oscillation),
+    the added mass of a changing V_CM, markers at center_y + amplitude."""
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_transverse_100.npz"))
+    D = float(g["D"])
+    s, cl, cd = _cylinder_gpu(pkg, orc, g, int(g["steps"]), m_max=5, u_max=0.05, Re=100.0, marker_dy=2.0,
+                              vsolid=orc.REF_PI * D * D * 0.25 * 3, motion=pkg.MOTION_TRANSVERSE_OSC,
+                              motion_amp=2.0, motion_freq=0.005)
+    e = _coeff_err(cl, cd, g)
+    print("transverse Cl/Cd error / max|Cd|: %.3g" % e)
+    assert e < 2e-6
+    assert np.abs(s.markers().reshape(3, -1)[1] - g["markers"][:, 1]).max() < 1e-12
+    body = s.body()
+    lat, mk, _, _ = orc.cylinder2d_literal(80, 40, D, 40, 5, int(g["steps"]), u_max=0.05, Re=100.0,
+                                           motion=orc.transverse_motion(2.0, 0.005),
+                                           vsolid=orc.REF_PI * D * D * 0.25 * 3, marker_dy=2.0)
+    _check_fields(s.moments(), *_layer_moments(lat), 0.05)
+    # the body's V_CM of the last step
+    assert abs(body[4] - orc.transverse_motion(2.0, 0.005)(float(g["steps"]))[1]) < 1e-15
+
+
+def test_d2q9_ibm_fp16_storage(pkg, orc):
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    _, cl, cd = _cylinder_gpu(pkg, orc, g, int(g["steps"]), storage="f16", m_max=int(g["m_max"]))
+    e = _coeff_err(cl, cd, g)
+    print("cylinder FP16 Cl/Cd error / max|Cd|: %.3g" % e)
+    assert e < 1e-3
+
+
+def test_d2q9_graph_replay_matches_eager(pkg, orc):
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    out = []
+    for gs in (8, -1):
+        s, cl, cd = _cylinder_gpu(pkg, orc, g, 41, graph_steps=gs, m_max=3)
+        out.append((s.moments(), cl, cd))
+    for c in ("rho", "ux", "uy"):
+        assert np.array_equal(out[0][0][c], out[1][0][c]), c
+    assert np.array_equal(out[0][1], out[1][1]) and np.array_equal(out[0][2], out[1][2])
+
+
+def test_d2q9_unsupported_calls_fail_loudly(pkg, tmp_path):
+    t = np.ones((10, 12), np.uint8)
+    t[1:-1, 1:-1] = 0
+    s = pkg.Solver(pkg.config_from_types_2d(10, 8, 0.8, t))
+    s.init()
+    for call in (lambda: s.save_state(str(tmp_path / "x")), lambda: s.output_vtk_async(str(tmp_path / "x.vtr")),
+                 lambda: s.set_more_details(True), lambda: s.set_solids(np.zeros((1, 8, 10)))):
+        with pytest.raises(pkg.LbmError) as e:
+            call()
+        assert e.value.status == 7

@@ -138,3 +138,28 @@ def test_more_details_match_reference(orc):
     # where the other rms values square their previous rms): on a ghost cell
     # at rest p = 1/3 and rms_p = p sqrt(told / (told + 1)), told = 190
     assert abs(g["rms_p"][0, 0, 0] - np.sqrt(190.0 / 191.0) / 3.0) < 1e-15
+
+
+@pytest.mark.parametrize("case", ["explicit", "transverse"])
+def test_cylinder2d_variants_match_reference(orc, case):
+    """The explicit direct-forcing scheme (lbm.cpp:1171-1258) and the
+    transversely oscillating cylinder (moving markers and box, added mass,
+    markers generated at center_y + amplitude, lbm.cpp:1966) against the
+    reference's own runs."""
+    if case == "explicit":
+        g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_explicit_100.npz"))
+        kw = dict(m_max=1, scheme=1)
+    else:
+        g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_transverse_100.npz"))
+        D = float(g["D"])
+        kw = dict(m_max=5, u_max=0.05, Re=100.0, motion=orc.transverse_motion(2.0, 0.005),
+                  vsolid=orc.REF_PI * D * D * 0.25 * 3, marker_dy=2.0)
+    lat, mk, cl, cd = orc.cylinder2d_literal(int(g["nx"]), int(g["ny"]), float(g["D"]), int(g["nodes"]),
+                                             steps=int(g["steps"]), **kw)
+    scale = np.abs(g["cd"]).max()
+    assert np.abs(cd - g["cd"]).max() < 1e-12 * scale
+    assert np.abs(cl - g["cl"]).max() < 1e-12 * scale
+    assert np.abs(mk["y"] - g["markers"][:, 1]).max() == 0.0
+    f = np.stack([lat.rho[1], lat.ux[1], lat.uy[1], lat.Fx[1], lat.Fy[1]])
+    assert np.abs(f[:, 8:33, 4:29] - g["window"]).max() < 1e-12
+    assert np.allclose(f.reshape(5, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
