@@ -311,6 +311,50 @@ def run_serving(pkg, orc, seconds: float, step_scale: float, rate: float = 200.0
             "oracle_sample": errs}
 
 
+def run_cylinder2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 10.0):
+    """The reference's shipped default build at its own size: the D2Q9
+    implicit-IBM cylinder (Cylinder_IBM, LBM.h:320-356: 800 x 400 cells,
+    D = 20, 200 markers, m_max = 20, Re = 40, u = 0.1) with the reference's
+    literal IBLBM options, through lbmgpu_step (CUDA graphs); beside it the
+    FP64 oracle's restatement of the same loop on the host cores."""
+    nx, ny, D, nodes, mm, u, Re = 800, 400, 20.0, 200, 20, 0.1, 40.0
+    tau = 0.5 + (u * D / Re) / (1.0 / 3.0)
+    t = np.zeros((ny + 2, nx + 2), np.uint8)
+    t[:, 0] = orc.TYPE_IN
+    t[:, -1] = orc.TYPE_OUT
+    t[0, :] = orc.TYPE_OUT
+    t[-1, :] = orc.TYPE_OUT
+    ones = np.ones((ny + 2, nx + 2))
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t, ones, u * ones, 0.0 * ones)
+    cfg.u0[0] = u
+    cfg.graph_steps = 50
+    s = pkg.Solver(cfg)
+    s.init()
+    mk = orc.cylinder_markers_literal(nodes, D, nx / 5.0, ny / 2.0)
+    s.set_markers(np.stack([mk["x"], mk["y"], mk["z"]]), mk["ds"], D / 2.0, (nx / 5.0, ny / 2.0, 1.0), m_max=mm,
+                  literal_sign=True, normals=np.stack([mk["nx"], mk["ny"], mk["nz"]]), rho_nearest=True,
+                  added_mass=True, volume=orc.REF_PI * D * D * 0.25)
+    s.step(100)
+    ms = s.step_timed(steps)
+    cd = s.forces(1)[0, 0] / (0.5 * u * u * D)
+    st = s.status()
+    s.close()
+    gpu = nx * ny * steps / (ms * 1e-3) / 1e6
+    c = orc.Cylinder2D(nx, ny, D, nodes, mm, u, Re)
+    c.step()
+    n, t0 = 0, time.perf_counter()
+    while n < 2 or (time.perf_counter() - t0 < cpu_seconds and n < 200):
+        c.step()
+        n += 1
+    cpu = nx * ny * n / (time.perf_counter() - t0) / 1e6
+    return {"workload": "D2Q9 implicit-IBM cylinder 800x400, D=20, 200 markers, m_max=20 (the reference's "
+                        "default build)", "value": gpu, "unit": "MLUPS", "ms_per_lbm_step": ms / steps,
+            "steps_timed": steps, "cd_last": float(cd), "status": int(st),
+            "cpu_port": {"value": cpu, "unit": "MLUPS", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": "%d steps of the same case, FP64 oracle (OpenMP)" % n},
+            "speedup_vs_cpu_port": gpu / cpu}
+
+
 def cpu_baseline_sample(threads: int | None = None):
     """FP64 restatement (oracle) on the same workload, a bounded sample of
     lattice steps, all host threads."""
@@ -349,6 +393,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batched", action="store_true")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-2d", action="store_true", help="skip the D2Q9 cylinder (the reference's default build)")
     ap.add_argument("--storages", default="f32,f16",
                     help="storage forms to time (the headline needs f16; f32 is the plain-form comparison)")
     ap.add_argument("--serve-seconds", type=float, default=2.0)
@@ -422,6 +467,12 @@ def main():
         import oracle as orc
 
         line["serving"] = run_serving(ge.load_package(), orc, args.serve_seconds, args.serve_step_scale)
+    if not args.no_2d:
+        import __graft_entry__ as ge
+        import oracle as orc
+
+        orc.build()
+        line["d2q9_cylinder"] = run_cylinder2d(ge.load_package(), orc)
     if not args.no_cpu_baseline:
         cb = cpu_baseline_sample()
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

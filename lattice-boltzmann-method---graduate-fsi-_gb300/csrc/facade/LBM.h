@@ -4,7 +4,8 @@
 //
 // What stays the same for a caller of the reference:
 //   - the cell types TYPE_F .. TYPE_Q (LBM.h:505-515), the D3Q19 tables
-//     cx/cy/cz/w/opposite in the reference order (LBM.h:542-552);
+//     cx/cy/cz/w/opposite in the reference order (LBM.h:542-552), or the D2Q9
+//     ones when built with -DD2Q9 (LBM.h:529-539);
 //   - class LATTICE with type/density/ux/uy/uz/f/f_star/F/Fm (LBM.h:558-597)
 //     and the public LATTICE ***fluid array of (Nx+2)(Ny+2)(Nz+2) cells;
 //   - class MARKER (LBM.h:600-616) and the free functions kernel,
@@ -43,10 +44,21 @@
 #define TYPE_Q 7    // Neumann heat flux
 #endif
 
-const int ndim = 3;
 // truncated PI of the reference (LBM.h:74)
 static const double PI = 3.14159265;
 
+#if defined D2Q9
+// D2Q9 in the reference order (LBM.h:529-539); the computational layer is
+// k = 1 of fluid[Nx+2][Ny+2][3]
+const int ndim = 2;
+const int npop = 9;
+const int cx[npop] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+const int cy[npop] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+const int cz[npop] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+const double w[npop] = {4.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 9, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
+const int opposite[npop] = {0, 3, 4, 1, 2, 7, 8, 5, 6};
+#else
+const int ndim = 3;
 const int npop = 19;
 const int cx[npop] = {0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0};
 const int cy[npop] = {0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1};
@@ -55,6 +67,7 @@ const double w[npop] = {1.0 / 3,  1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 18, 1.0 / 
                         1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36,
                         1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36, 1.0 / 36};
 const int opposite[npop] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
+#endif
 
 // Run-time replacement of the reference's compile-time configuration.
 struct lbm_options {
@@ -68,6 +81,19 @@ struct lbm_options {
     int thermal = 0;              // D3Q7 temperature population
     double tau_g = 0.0, T_ref = 0.0, gbeta[3] = {0, 0, 0};
     int Nt = 10;                  // output cadence (LBM.h:493-496): Sup_MacroProp's told = (n - Nt) dt
+    // the reference's global centre (center_x, center_y, 1): IBLBM's box is
+    // [centre - D, centre + D] (lbm.cpp:1165-1166); unset, the marker centroid
+    int body_center_set = 0;
+    double body_center[3] = {0, 0, 0};
+    // D2Q9 IBLBM options (#define D2Q9 builds): the reference's nearest-node
+    // density (lbm.cpp:1315-1317) and added mass (lbm.cpp:1392-1398, V_solid
+    // = vsolid), the prescribed V_CM(t) (LBM_MOTION_*, lbm.cpp:1140-1151) and
+    // the forcing scheme (0 implicit, 1 explicit)
+    int rho_nearest = 0, added_mass = 0;
+    double vsolid = 0.0;
+    int motion = LBM_MOTION_FIXED;
+    double motion_amp = 0.0, motion_freq = 0.0, motion_velocity[3] = {0, 0, 0};
+    int ibm_scheme = 0;
 };
 extern lbm_options g_lbm_options;
 

@@ -10,9 +10,9 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
-DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details"]
+DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details", "dropin_cylinder2d"]
 # compile-time switches of the reference a driver is built with
-DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"]}
+DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"], "dropin_cylinder2d": ["-DD2Q9"]}
 
 
 def build(force: bool = False) -> list:

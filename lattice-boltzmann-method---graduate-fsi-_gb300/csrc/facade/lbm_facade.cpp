@@ -119,8 +119,19 @@ void LBM::Init() {
                 T[id] = c.T;
             }
     lbm_config cfg;
+#if defined D2Q9
+    // the computational layer k = 1 (the k = 0, 2 layers of a D2Q9 build
+    // evolve on their own and are never read)
+    {
+        const size_t layer = (size_t)NX * NY;
+        check("config_from_types_2d",
+              lbmgpu_config_from_types_2d(Nx, Ny, tau, types.data() + layer, rho.data() + layer, ux.data() + layer,
+                                          uy.data() + layer, &cfg));
+    }
+#else
     check("config_from_types", lbmgpu_config_from_types(Nx, Ny, Nz, tau, types.data(), rho.data(), ux.data(),
                                                         uy.data(), uz.data(), T.data(), &cfg));
+#endif
     const lbm_options &o = g_lbm_options;
     cfg.storage = o.storage;
     cfg.thermal = o.thermal;
@@ -133,6 +144,10 @@ void LBM::Init() {
         dev->off[a] = ddims[a] == dims[a] + 2 ? 0 : 1;
         dev->dn[a] = ddims[a];
     }
+#if defined D2Q9
+    dev->off[2] = 1;  // device layer 0 is the reference's k = 1
+    dev->dn[2] = 1;
+#endif
     if (dev->h) lbmgpu_destroy(dev->h);
     dev->h = nullptr;
     check("create", lbmgpu_create(&cfg, &dev->h));
@@ -153,7 +168,9 @@ void LBM::Init() {
                         any = true;
                     }
                 }
+#if !defined D2Q9
         if (any) check("set_solids", lbmgpu_set_solids(dev->h, mask.data()));
+#endif
         dev->solids = any;
     }
 #if defined MORE_DETAILS
@@ -313,7 +330,9 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
     if (!d.h) check("IBLBM before Init", LBM_ERR_STATE);
     d.cl = &Cl;
     d.cd = &Cd;
-    if (d.markers_set) return;  // fixed body: the markers stay on the device
+    // the markers stay on the device (a prescribed D2Q9 motion moves them
+    // there: lbmgpu_get_markers reads them back)
+    if (d.markers_set) return;
     const int n = (int)marker.size();
     std::vector<double> xyz(3 * (size_t)n), dsv(ds.begin(), ds.end());
     double c[3] = {0, 0, 0};
@@ -324,7 +343,10 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
         xyz[2 * (size_t)n + m] = marker[m].z - (d.off[2] - 1);
         for (int a = 0; a < 3; a++) c[a] += xyz[(size_t)a * n + m] / n;
     }
-    double R = g_lbm_options.body_radius;
+    const lbm_options &o = g_lbm_options;
+    if (o.body_center_set)
+        for (int a = 0; a < 3; a++) c[a] = o.body_center[a] - (d.off[a] - 1);
+    double R = o.body_radius;
     if (R <= 0)
         for (int m = 0; m < n; m++) {
             double rr = 0;
@@ -333,14 +355,31 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
         }
     lbm_ibm_config ic = {};
     ic.n_markers = n;
-    ic.m_max = g_lbm_options.m_max;
-    ic.literal_sign = g_lbm_options.literal_sign;
+    ic.m_max = o.m_max;
+    ic.literal_sign = o.literal_sign;
     ic.radius = R;
     for (int a = 0; a < 3; a++) {
         ic.center[a] = c[a];
         ic.velocity[a] = V_CM[a];
     }
+#if defined D2Q9
+    // V_CM(t) is prescribed on the device; V_CM[] is the reference's initial zero
+    for (int a = 0; a < 3; a++) ic.velocity[a] = o.motion_velocity[a];
+    ic.rho_nearest = o.rho_nearest;
+    ic.added_mass = o.added_mass;
+    ic.volume = o.vsolid;
+    ic.motion = o.motion;
+    ic.motion_amp = o.motion_amp;
+    ic.motion_freq = o.motion_freq;
+    ic.scheme = o.ibm_scheme;
+#endif
     check("set_markers", lbmgpu_set_markers(d.h, &ic, xyz.data(), dsv.data(), nullptr));
+#if defined D2Q9
+    std::vector<double> nrm(3 * (size_t)n);
+    for (int m = 0; m < n; m++)
+        for (int a = 0; a < 3; a++) nrm[(size_t)a * n + m] = marker[m].normal[a];
+    check("set_marker_normals", lbmgpu_set_marker_normals(d.h, nrm.data()));
+#endif
     d.markers_set = true;
 }
 

@@ -174,7 +174,6 @@ struct Ibm2 {
     double *pos;      // [3][n] reference node coordinates
     const double *nrm;  // [3][n]
     const double *dsw;  // [n]
-    double *acc;      // [2][n] FP64 force sums of the pass
     float *fs;        // [2][n] F_m ds_m of the current iteration
     float *rhom;      // [n]
     int *s0;          // [2][n] stencil origin, box coordinates
@@ -182,7 +181,10 @@ struct Ibm2 {
     int *cnt, *off;   // [nb], [nb]
     int *lm;          // [16 n] spreading lists: marker
     float *lw;        //                         weight
+    int *qnear;       // [n] nearest box node of each marker (band index), -1 for none
+    uint8_t *inside;  // [nb] box node inside every marker (Calc_AverageDensity)
     double *hist;     // [cap][4]: drag, lift, 0, step
+    int smem;         // 1: the working fields of the pass live in shared memory
 };
 
 // 4-point Peskin delta (lbm.cpp:1095-1102).
@@ -235,26 +237,19 @@ __device__ void box_of(State2 *st, const Ibm2 &ib, const Params2 &P, long long s
     st->box_h = hgt;
 }
 
-// Block-wide; callers synchronise before and after.
+// One thread: V_CM of step s and the centre (the markers were moved by
+// k_move2d).
 __device__ void advance_body(State2 *st, const Ibm2 &ib, long long s) {
-    __shared__ double sV[3], sVo[3];
-    if (threadIdx.x == 0) {
-        double V[3];
-        motion_velocity(ib, (double)s, V);
-        for (int a = 0; a < 3; a++) {
-            sVo[a] = st->V[a];
-            sV[a] = V[a];
-            st->Vold[a] = st->V[a];
-            st->V[a] = V[a];
-            st->center[a] += (V[a] + sVo[a]) * 1.0 / 2;
-        }
-        st->ibm_step = s;
-        if (ib.motion != LBM_MOTION_FIXED) st->lists_ok = 0;
+    double V[3];
+    motion_velocity(ib, (double)s, V);
+    for (int a = 0; a < 3; a++) {
+        const double vo = st->V[a];
+        st->Vold[a] = vo;
+        st->V[a] = V[a];
+        st->center[a] += (V[a] + vo) * 1.0 / 2;
     }
-    __syncthreads();
-    if (ib.motion != LBM_MOTION_FIXED)
-        for (int m = threadIdx.x; m < ib.n; m += blockDim.x)
-            for (int a = 0; a < 3; a++) ib.pos[a * ib.n + m] += (sV[a] + sVo[a]) * 1.0 / 2;
+    st->ibm_step = s;
+    if (ib.motion != LBM_MOTION_FIXED) st->lists_ok = 0;
 }
 
 // The box of reference step 1, before its collide-stream launch.
@@ -325,28 +320,6 @@ __device__ __forceinline__ void marker_stencil(const Ibm2 &ib, const State2 *st,
     }
 }
 
-// Interpolation of the box field (a, b) at marker m over its stencil, in the
-// reference's node order.
-__device__ __forceinline__ void interp2(const Ibm2 &ib, const Params2 &P, const float *__restrict__ fa,
-                                        const float *__restrict__ fb, int m, float &sa, float &sb) {
-    const int n = ib.n;
-    const int bx0 = ib.s0[m], by0 = ib.s0[n + m];
-    float a0 = 0.0f, b0 = 0.0f;
-#pragma unroll
-    for (int a = 0; a < 4; a++)
-#pragma unroll
-        for (int b = 0; b < 4; b++) {
-            const float w = ib.swt[(4 * a + b) * n + m];
-            if (w != 0.0f) {
-                const long long q = (bx0 + a) + (long long)P.bsx * (by0 + b);
-                a0 += fa[q] * w;
-                if (fb) b0 += fb[q] * w;
-            }
-        }
-    sa = a0;
-    sb = b0;
-}
-
 // NearestLatticeCoordinate (lbm.cpp:1074-1092) over box nodes
 // [xa, xb] x [ya, yb] (box coordinates), one warp: the last node in
 // x-outer / y-inner order with the largest (x - X) . n > 0.  Returns the box
@@ -381,25 +354,93 @@ __device__ __forceinline__ long long nearest_node(const Ibm2 &ib, const State2 *
     return (long long)(xa + bo / h) + (long long)P.bsx * (ya + bo % h);
 }
 
+// Markers of step s (one warp each, many blocks): moved by the trapezoid of
+// V_CM (lbm.cpp:1153-1160), and their nearest box node (the whole box, or
+// the 2x2 cell around the marker in the explicit scheme, lbm.cpp:1216-1219).
+// Runs before the step's collide-stream launch; the box of step s is set.
+constexpr int kMoveBlock = 256;
+__global__ void __launch_bounds__(kMoveBlock) k_move2d(State2 *__restrict__ st, Ibm2 ib,
+                                                       const __grid_constant__ Params2 P) {
+    const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    const int lane = threadIdx.x & 31, n = ib.n;
+    if (m >= n) return;  // whole warp leaves together
+    if (ib.motion != LBM_MOTION_FIXED) {
+        double V[3];
+        motion_velocity(ib, (double)(st->ibm_step + 1), V);
+        if (lane == 0)
+            for (int a = 0; a < 3; a++) ib.pos[a * n + m] += (V[a] + st->V[a]) * 1.0 / 2;
+        __syncwarp();
+    }
+    if (!ib.rho_nearest) return;
+    const int bw = st->box_w, bh = st->box_h;
+    int xa = 0, xb = bw - 1, ya = 0, yb = bh - 1;
+    if (ib.scheme == 1) {
+        const double X = ib.pos[m], Y = ib.pos[n + m];
+        xa = (int)floor(X) - (st->box_lo[0] + 1);
+        xb = (int)ceil(X) - (st->box_lo[0] + 1);
+        ya = (int)floor(Y) - (st->box_lo[1] + 1);
+        yb = (int)ceil(Y) - (st->box_lo[1] + 1);
+        if (xa < 0 || ya < 0 || xb >= bw || yb >= bh) {
+            if (lane == 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
+            xa = max(xa, 0);
+            ya = max(ya, 0);
+            xb = min(xb, bw - 1);
+            yb = min(yb, bh - 1);
+        }
+    }
+    const long long q = nearest_node(ib, st, P, m, xa, xb, ya, yb);
+    if (lane == 0) {
+        if (q < 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
+        ib.qnear[m] = (int)q;
+    }
+}
+
+// Box nodes inside every marker, (x - X_m) . n_m <= 0 for all m
+// (Calc_AverageDensity, lbm.cpp:1105-1132), for the added mass of a moving
+// body; after k_move2d.
+__global__ void __launch_bounds__(kMoveBlock) k_inside2d(const State2 *__restrict__ st, Ibm2 ib,
+                                                         const __grid_constant__ Params2 P) {
+    const int bw = st->box_w, bh = st->box_h, n = ib.n;
+    const int o = blockIdx.x * blockDim.x + threadIdx.x;
+    if (o >= bw * bh) return;
+    const int bx = o % bw, by = o / bw;
+    const double X = (double)(st->box_lo[0] + 1 + bx), Y = (double)(st->box_lo[1] + 1 + by);
+    bool inside = true;
+    for (int m = 0; m < n && inside; m++) {
+        const double d = (X - ib.pos[m]) * ib.nrm[m] + (Y - ib.pos[n + m]) * ib.nrm[n + m] +
+                         (1.0 - ib.pos[2 * n + m]) * ib.nrm[2 * n + m];
+        if (d > 0.0) inside = false;
+    }
+    ib.inside[bx + (long long)P.bsx * by] = inside ? 1 : 0;
+}
+
+// Shared-memory bytes of the working fields of one pass: the box fields
+// (rho, u, F: 5 nb floats), list offsets and counts (2 nb), lists (2 x 16 n),
+// marker forces, densities, stencil origins and weights (21 n).
+__host__ __device__ inline size_t ibm2d_smem_bytes(long long nb, int n) {
+    return (size_t)4 * (7 * (size_t)nb + 53 * (size_t)n);
+}
+
 template <class T>
 __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __grid_constant__ Params2 P,
                                                      State2 *__restrict__ st, Ibm2 ib, float *__restrict__ band) {
+    extern __shared__ float smem[];
     const int tid = threadIdx.x, nt = blockDim.x;
     const int n = ib.n;
     const long long nb = P.nb;
-    // IBLBM's prelude for this step: V_CM, markers, centre (the box of the
-    // step was set before its collide-stream launch)
+    // IBLBM's prelude for this step: V_CM and the centre (the markers were
+    // moved and the box set before the collide-stream launch)
     const long long step = st->ibm_step + 1;
     __syncthreads();
-    advance_body(st, ib, step);
+    if (tid == 0) advance_body(st, ib, step);
     __syncthreads();
     const int bw = st->box_w, bh = st->box_h, nbox = bw * bh;
     const int lists_ok = st->lists_ok;
-    float *drho = band, *ux = band + nb, *uy = band + 2 * nb, *Fx = band + 3 * nb, *Fy = band + 4 * nb;
+    const float V0 = (float)st->V[0], V1 = (float)st->V[1];
     auto bq = [&](int o) { return (long long)(o % bw) + (long long)P.bsx * (o / bw); };
     __syncthreads();
 
-    // stencils and spreading lists (fixed body: once)
+    // stencils and spreading lists, in global scratch (fixed body: once)
     if (!lists_ok) {
         for (int m = tid; m < n; m += nt) marker_stencil(ib, st, m);
         for (int o = tid; o < nbox; o += nt) ib.cnt[bq(o)] = 0;
@@ -450,80 +491,101 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
             }
         }
         if (tid == 0 && ib.motion == LBM_MOTION_FIXED) st->lists_ok = 1;
+        __syncthreads();
     }
-    for (int m = tid; m < 2 * n; m += nt) ib.acc[m] = 0.0;
-    __syncthreads();
 
-    // marker density: nearest node over the box (lbm.cpp:1315-1317), over
-    // the 2x2 cell around the marker in the explicit scheme (lbm.cpp:1216-1219),
-    // or delta-interpolated
-    const int lane = tid & 31, warp = tid >> 5, nwarp = nt >> 5;
-    if (ib.rho_nearest) {
-        for (int m = warp; m < n; m += nwarp) {
-            int xa = 0, xb = bw - 1, ya = 0, yb = bh - 1;
-            if (ib.scheme == 1) {
-                const double X = ib.pos[m], Y = ib.pos[n + m];
-                xa = (int)floor(X) - (st->box_lo[0] + 1);
-                xb = (int)ceil(X) - (st->box_lo[0] + 1);
-                ya = (int)floor(Y) - (st->box_lo[1] + 1);
-                yb = (int)ceil(Y) - (st->box_lo[1] + 1);
-                if (xa < 0 || ya < 0 || xb >= bw || yb >= bh) {
-                    if (lane == 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
-                    xa = max(xa, 0);
-                    ya = max(ya, 0);
-                    xb = min(xb, bw - 1);
-                    yb = min(yb, bh - 1);
+    // working copies: shared memory when they fit, else the global arrays
+    float *drho = band, *ux = band + nb, *uy = band + 2 * nb, *Fx = band + 3 * nb, *Fy = band + 4 * nb;
+    int *cnt = ib.cnt, *off = ib.off, *lm = ib.lm, *s0 = ib.s0;
+    float *lw = ib.lw, *swt = ib.swt, *fs = ib.fs, *rhom = ib.rhom;
+    if (ib.smem) {
+        float *p = smem;
+        drho = p; ux = p + nb; uy = p + 2 * nb; Fx = p + 3 * nb; Fy = p + 4 * nb;
+        p += 5 * nb;
+        cnt = (int *)p; off = (int *)p + nb;
+        p += 2 * nb;
+        lm = (int *)p; lw = p + 16 * n; fs = p + 32 * n; rhom = p + 34 * n; s0 = (int *)p + 35 * n;
+        swt = p + 37 * n;
+        for (int o = tid; o < nbox; o += nt) {
+            const long long q = bq(o);
+            drho[q] = band[q];
+            ux[q] = band[nb + q];
+            uy[q] = band[2 * nb + q];
+            Fx[q] = band[3 * nb + q];
+            Fy[q] = band[4 * nb + q];
+            cnt[q] = ib.cnt[q];
+            off[q] = ib.off[q];
+        }
+        for (int i = tid; i < 16 * n; i += nt) {
+            lm[i] = ib.lm[i];
+            lw[i] = ib.lw[i];
+            swt[i] = ib.swt[i];
+        }
+        for (int i = tid; i < 2 * n; i += nt) s0[i] = ib.s0[i];
+        __syncthreads();
+    }
+    auto interp = [&](const float *fa, const float *fb, int m, float &sa, float &sb) {
+        const int bx0 = s0[m], by0 = s0[n + m];
+        float a0 = 0.0f, b0 = 0.0f;
+#pragma unroll
+        for (int a = 0; a < 4; a++)
+#pragma unroll
+            for (int b = 0; b < 4; b++) {
+                const float w = swt[(4 * a + b) * n + m];
+                if (w != 0.0f) {
+                    const long long q = (bx0 + a) + (long long)P.bsx * (by0 + b);
+                    a0 += fa[q] * w;
+                    if (fb) b0 += fb[q] * w;
                 }
             }
-            const long long q = nearest_node(ib, st, P, m, xa, xb, ya, yb);
-            if (lane == 0) {
-                if (q < 0) atomicOr(&st->status, lbmk::ST_BAND_EDGE);
-                ib.rhom[m] = q < 0 ? 1.0f : 1.0f + drho[q];
-            }
-        }
-    } else {
-        for (int m = tid; m < n; m += nt) {
+        sa = a0;
+        sb = b0;
+    };
+
+    // marker density: nearest node (k_move2d), or delta-interpolated
+    for (int m = tid; m < n; m += nt) {
+        if (ib.rho_nearest) {
+            const int q = ib.qnear[m];
+            rhom[m] = q < 0 ? 1.0f : 1.0f + drho[q];
+        } else {
             float sr, dummy;
-            interp2(ib, P, drho, nullptr, m, sr, dummy);
-            // sum (1 + drho) delta = sum delta + sum drho delta
+            interp(drho, nullptr, m, sr, dummy);
             float wsum = 0.0f;
-            for (int k = 0; k < 16; k++) wsum += ib.swt[k * n + m];
-            ib.rhom[m] = wsum + sr;
+            for (int k = 0; k < 16; k++) wsum += swt[k * n + m];
+            rhom[m] = wsum + sr;  // sum (1 + drho) delta
         }
     }
     __syncthreads();
 
     const float sgn = ib.lit_sign ? -1.0f : 1.0f;
-    double node_drag = 0.0, node_lift = 0.0;
+    double node_drag = 0.0, node_lift = 0.0, mk_drag = 0.0, mk_lift = 0.0;
     const int iters = ib.scheme == 1 ? 1 : ib.m_max;
     for (int it = 0; it < iters; it++) {
         // interpolate the current velocity; marker forces (lbm.cpp:1314-1324)
         for (int m = tid; m < n; m += nt) {
             float ub, vb;
-            interp2(ib, P, ux, uy, m, ub, vb);
-            const float rho = ib.rhom[m];
-            const float V0 = (float)st->V[0], V1 = (float)st->V[1];
+            interp(ux, uy, m, ub, vb);
+            const float rho = rhom[m];
             const float Fbx = 2.0f * rho * (V0 - ub), Fby = 2.0f * rho * (V1 - vb);
             const double dsv = ib.dsw[m];
-            ib.fs[m] = (float)(Fbx * dsv);
-            ib.fs[n + m] = (float)(Fby * dsv);
-            if (ib.scheme == 0) {
-                ib.acc[m] += -(double)Fbx * 1.0 * dsv;
-                ib.acc[n + m] += -(double)Fby * 1.0 * dsv;
-            }
+            fs[m] = (float)(Fbx * dsv);
+            fs[n + m] = (float)(Fby * dsv);
+            // a thread keeps its markers' FP64 sums over the iterations
+            mk_drag += -(double)Fbx * 1.0 * dsv;
+            mk_lift += -(double)Fby * 1.0 * dsv;
             if (!isfinite(Fbx) || !isfinite(Fby)) atomicOr(&st->status, lbmk::ST_NONFINITE_FORCE);
         }
         __syncthreads();
         // spreading, node-centred, ascending marker order (lbm.cpp:1331-1352)
         for (int o = tid; o < nbox; o += nt) {
             const long long q = bq(o);
-            const int a = ib.off[q], c = ib.cnt[q];
+            const int a = off[q], c = cnt[q];
             float sx = 0.0f, sy = 0.0f;
             for (int i = 0; i < c; i++) {
-                const int m = ib.lm[a + i];
-                const float w = ib.lw[a + i];
-                sx += ib.fs[m] * w;
-                sy += ib.fs[n + m] * w;
+                const int m = lm[a + i];
+                const float w = lw[a + i];
+                sx += fs[m] * w;
+                sy += fs[n + m] * w;
             }
             const float rho = 1.0f + drho[q];
             if (ib.scheme == 0) {
@@ -543,40 +605,24 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     }
 
     // the pass's force: sum over markers (implicit) or box nodes (explicit)
-    double dl = 0.0, ll = 0.0;
-    if (ib.scheme == 0) {
-        for (int m = tid; m < n; m += nt) {
-            dl += ib.acc[m];
-            ll += ib.acc[n + m];
-        }
-    } else {
-        dl = node_drag;
-        ll = node_lift;
-    }
-    const double drag = block_sum_d(dl), lift = block_sum_d(ll);
+    const double drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
+    const double lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
 
     // added mass (lbm.cpp:1392-1398): mean density of the box nodes inside
-    // every marker (Calc_AverageDensity, lbm.cpp:1105-1132); skipped when
-    // V_CM did not change, where it adds rho_avg * 0
+    // every marker (k_inside2d); skipped when V_CM did not change, where it
+    // adds rho_avg * 0
     __shared__ double sam[2];
     const double dV0 = st->V[0] - st->Vold[0], dV1 = st->V[1] - st->Vold[1];
     if (ib.added_mass && (dV0 != 0.0 || dV1 != 0.0)) {
-        double rs = 0.0, cnt = 0.0;
+        double rs = 0.0, cn = 0.0;
         for (int o = tid; o < nbox; o += nt) {
-            const int bx = o % bw, by = o / bw;
-            const double X = (double)(st->box_lo[0] + 1 + bx), Y = (double)(st->box_lo[1] + 1 + by);
-            bool inside = true;
-            for (int m = 0; m < n && inside; m++) {
-                const double d = (X - ib.pos[m]) * ib.nrm[m] + (Y - ib.pos[n + m]) * ib.nrm[n + m] +
-                                 (1.0 - ib.pos[2 * n + m]) * ib.nrm[2 * n + m];
-                if (d > 0.0) inside = false;
-            }
-            if (inside) {
-                rs += 1.0 + (double)drho[bq(o)];
-                cnt += 1.0;
+            const long long q = bq(o);
+            if (ib.inside[q]) {
+                rs += 1.0 + (double)drho[q];
+                cn += 1.0;
             }
         }
-        const double tr = block_sum_d(rs), tc = block_sum_d(cnt);
+        const double tr = block_sum_d(rs), tc = block_sum_d(cn);
         if (tid == 0) {
             const double ravg = tr / tc;
             sam[0] = ravg * ib.vsolid * dV0 / 1.0;
@@ -587,12 +633,11 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     }
     __syncthreads();
     if (tid == 0) {
-        const long long s = step;
-        double *row = ib.hist + 4 * ((s - 1) % st->hist_cap);
+        double *row = ib.hist + 4 * ((step - 1) % st->hist_cap);
         row[0] = drag + sam[0];
         row[1] = lift + sam[1];
         row[2] = 0.0;
-        row[3] = (double)s;
+        row[3] = (double)step;
     }
 
     // collision of the box cells with the forced velocity and the force
@@ -784,21 +829,49 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
 cudaError_t launch_ibm2d(lbm_handle *h) {
     lbm2d *d = h->d2;
     void *B = d->f[1 - d->cur];
+    const size_t sm = d->ib.smem ? ibm2d_smem_bytes(d->P.nb, d->ib.n) : 0;
     switch (h->cfg.storage) {
-    case LBM_STORE_F16: k_ibm2d<__half><<<1, kIbmBlock, 0, h->s>>>((__half *)B, d->P, d->st, d->ib, d->band); break;
+    case LBM_STORE_F16: k_ibm2d<__half><<<1, kIbmBlock, sm, h->s>>>((__half *)B, d->P, d->st, d->ib, d->band); break;
     case LBM_STORE_BF16:
-        k_ibm2d<__nv_bfloat16><<<1, kIbmBlock, 0, h->s>>>((__nv_bfloat16 *)B, d->P, d->st, d->ib, d->band);
+        k_ibm2d<__nv_bfloat16><<<1, kIbmBlock, sm, h->s>>>((__nv_bfloat16 *)B, d->P, d->st, d->ib, d->band);
         break;
-    default: k_ibm2d<float><<<1, kIbmBlock, 0, h->s>>>((float *)B, d->P, d->st, d->ib, d->band); break;
+    default: k_ibm2d<float><<<1, kIbmBlock, sm, h->s>>>((float *)B, d->P, d->st, d->ib, d->band); break;
     }
     return cudaGetLastError();
+}
+
+// Opt the IBM kernel of this storage into the shared memory it needs.
+cudaError_t ibm2d_smem_setup(int storage, size_t bytes) {
+    switch (storage) {
+    case LBM_STORE_F16:
+        return cudaFuncSetAttribute(k_ibm2d<__half>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    case LBM_STORE_BF16:
+        return cudaFuncSetAttribute(k_ibm2d<__nv_bfloat16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    default: return cudaFuncSetAttribute(k_ibm2d<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    }
 }
 
 // One reference iteration.
 cudaError_t enqueue_step2d(lbm_handle *h) {
     lbm2d *d = h->d2;
     const int gather = h->steps == 0 ? 0 : 1;
-    cudaError_t e = launch_step2d(h, gather, nullptr, 0);
+    cudaError_t e = cudaSuccess;
+    if (d->ibm) {
+        // markers of the step (a moving body; a fixed one needs its nearest
+        // nodes once) and, for the added mass of a moving body, the inside mask
+        const bool moving = d->ib.motion != LBM_MOTION_FIXED;
+        if (moving || (h->steps == 0 && d->ib.rho_nearest)) {
+            const unsigned blocks = (unsigned)((d->ib.n * 32 + kMoveBlock - 1) / kMoveBlock);
+            k_move2d<<<blocks, kMoveBlock, 0, h->s>>>(d->st, d->ib, d->P);
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && moving && d->ib.added_mass) {
+            const unsigned blocks = (unsigned)((d->P.nb + kMoveBlock - 1) / kMoveBlock);
+            k_inside2d<<<blocks, kMoveBlock, 0, h->s>>>(d->st, d->ib, d->P);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = launch_step2d(h, gather, nullptr, 0);
     if (e == cudaSuccess && d->ibm) e = launch_ibm2d(h);
     d->cur = 1 - d->cur;
     h->steps++;
@@ -937,7 +1010,8 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     CK2(alloc2(h, &dsd, (size_t)n * sizeof(double)));
     ib.nrm = nrm;
     ib.dsw = dsd;
-    CK2(alloc2(h, &ib.acc, (size_t)2 * n * sizeof(double)));
+    CK2(alloc2(h, &ib.qnear, (size_t)n * sizeof(int)));
+    CK2(alloc2(h, &ib.inside, (size_t)P.nb));
     CK2(alloc2(h, &ib.fs, (size_t)2 * n * sizeof(float)));
     CK2(alloc2(h, &ib.rhom, (size_t)n * sizeof(float)));
     CK2(alloc2(h, &ib.s0, (size_t)2 * n * sizeof(int)));
@@ -947,6 +1021,13 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     CK2(alloc2(h, &ib.lm, (size_t)16 * n * sizeof(int)));
     CK2(alloc2(h, &ib.lw, (size_t)16 * n * sizeof(float)));
     ib.hist = d->hist;
+    // the pass's working set in shared memory when it fits
+    const size_t sm = ibm2d_smem_bytes(P.nb, n);
+    int dev = 0, optin = 0;
+    CK2(cudaGetDevice(&dev));
+    CK2(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    ib.smem = sm + 1024 <= (size_t)optin ? 1 : 0;
+    if (ib.smem) CK2(ibm2d_smem_setup(h->cfg.storage, sm));
     CK2(cudaMemcpyAsync(ib.pos, xyz, (size_t)3 * n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CK2(cudaMemcpyAsync(dsd, dsw, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CK2(cudaMemsetAsync(nrm, 0, (size_t)3 * n * sizeof(double), h->s));

@@ -562,9 +562,7 @@ def cavity_details_run(n: int, tau: float, lid: float, steps: int, nt: int = 10)
 # The reference's two-dimensional IBM cylinders (D2Q9)
 # --------------------------------------------------------------------------
 
-def cylinder2d_literal(nx: int, ny: int, D: float, nodes: int, m_max: int, steps: int, u_max: float = 0.1,
-                       Re: float = 40.0, scheme: int = 0, motion=None, vsolid: float | None = None,
-                       marker_dy: float = 0.0):
+class Cylinder2D:
     """The reference's D2Q9 IBM cylinder loop (main.cpp:195-205) in its
     literal options: main_setup_Cylinder_IBM (TYPE_IN at x = 0, TYPE_OUT
     elsewhere, u = u_max), Generate_Cylinder_Marker at (Nx/5, Ny/2), and every
@@ -575,48 +573,66 @@ def cylinder2d_literal(nx: int, ny: int, D: float, nodes: int, m_max: int, steps
     and Streaming.  motion(t) -> (Vx, Vy, Vz) or None for a fixed body.
     marker_dy shifts the markers (not the centre, so not the box): the
     transverse-oscillation case generates them at center_y + amplitude
-    (lbm.cpp:1966).  Returns the lattice, the markers, Cl and Cd per step
-    (C = F / (1/2 u^2 D))."""
-    import math
+    (lbm.cpp:1966)."""
 
-    tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
-    lat = Lattice(9, nx, ny, 1, tau)
-    t = lat.types
-    t[:] = TYPE_F
-    t[:, :, 0] = TYPE_IN
-    t[:, :, -1] = TYPE_OUT
-    t[:, 0, :] = TYPE_OUT
-    t[:, -1, :] = TYPE_OUT
-    lat.ux[:] = u_max
-    lat.init()
-    cx, cy = nx / 5.0, ny / 2.0
-    mk = cylinder_markers_literal(nodes, D, cx, cy + marker_dy)
-    if vsolid is None:
-        vsolid = REF_PI * D * D * 0.25
-    V = [0.0, 0.0, 0.0]
-    cl, cd = [], []
-    for s in range(1, steps + 1):
-        Vold = V
-        V = list(motion(s * 1.0)) if motion else [0.0, 0.0, 0.0]
+    def __init__(self, nx: int, ny: int, D: float, nodes: int, m_max: int, u_max: float = 0.1, Re: float = 40.0,
+                 scheme: int = 0, motion=None, vsolid: float | None = None, marker_dy: float = 0.0):
+        tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
+        lat = Lattice(9, nx, ny, 1, tau)
+        t = lat.types
+        t[:] = TYPE_F
+        t[:, :, 0] = TYPE_IN
+        t[:, :, -1] = TYPE_OUT
+        t[:, 0, :] = TYPE_OUT
+        t[:, -1, :] = TYPE_OUT
+        lat.ux[:] = u_max
+        lat.init()
+        self.lat, self.D, self.m_max, self.u_max, self.scheme, self.motion = lat, D, m_max, u_max, scheme, motion
+        self.cx, self.cy = nx / 5.0, ny / 2.0
+        self.mk = cylinder_markers_literal(nodes, D, self.cx, self.cy + marker_dy)
+        self.vsolid = REF_PI * D * D * 0.25 if vsolid is None else vsolid
+        self.V = [0.0, 0.0, 0.0]
+        self.s = 0
+        self.cl, self.cd = [], []
+
+    def step(self):
+        import math
+
+        self.s += 1
+        Vold = self.V
+        V = list(self.motion(self.s * 1.0)) if self.motion else [0.0, 0.0, 0.0]
+        self.V = V
+        mk, D = self.mk, self.D
         for a, nm in enumerate(("x", "y", "z")):
             mk[nm][:] += (V[a] + Vold[a]) * 1.0 / 2
         for a, nm in enumerate(("udx", "udy", "udz")):
             mk[nm][:] = V[a]
-        cx += (V[0] + Vold[0]) * 1.0 / 2
-        cy += (V[1] + Vold[1]) * 1.0 / 2
-        lo = [math.floor(cx - D), math.floor(cy - D), 1]
-        hi = [math.ceil(cx + D), math.ceil(cy + D), 1]
-        op = ibm_opts(lo, hi, m_max, lit_sign=1, rho_mode=1)
+        self.cx += (V[0] + Vold[0]) * 1.0 / 2
+        self.cy += (V[1] + Vold[1]) * 1.0 / 2
+        lo = [math.floor(self.cx - D), math.floor(self.cy - D), 1]
+        hi = [math.ceil(self.cx + D), math.ceil(self.cy + D), 1]
+        op = ibm_opts(lo, hi, self.m_max, lit_sign=1, rho_mode=1)
         op.use_avg_density = 1
-        op.vsolid = vsolid
-        op.scheme = scheme
+        op.vsolid = self.vsolid
+        op.scheme = self.scheme
         for a in range(3):
             op.vcm_new[a] = V[a]
             op.vcm_old[a] = Vold[a]
-        out = lat.step_ibm(mk, op, [cx, cy, 1.0])
-        cl.append(out[1] / (0.5 * 1.0 * u_max ** 2 * D))
-        cd.append(out[0] / (0.5 * 1.0 * u_max ** 2 * D))
-    return lat, mk, np.array(cl), np.array(cd)
+        out = self.lat.step_ibm(mk, op, [self.cx, self.cy, 1.0])
+        q = 0.5 * 1.0 * self.u_max ** 2 * D
+        self.cl.append(out[1] / q)
+        self.cd.append(out[0] / q)
+
+
+def cylinder2d_literal(nx: int, ny: int, D: float, nodes: int, m_max: int, steps: int, u_max: float = 0.1,
+                       Re: float = 40.0, scheme: int = 0, motion=None, vsolid: float | None = None,
+                       marker_dy: float = 0.0):
+    """Cylinder2D run for `steps` steps: the lattice, the markers, Cl and Cd
+    per step (C = F / (1/2 u^2 D))."""
+    c = Cylinder2D(nx, ny, D, nodes, m_max, u_max, Re, scheme, motion, vsolid, marker_dy)
+    for _ in range(steps):
+        c.step()
+    return c.lat, c.mk, np.array(c.cl), np.array(c.cd)
 
 
 def transverse_motion(amplitude: float, frequency: float):

@@ -88,3 +88,27 @@ def test_dropin_more_details_loop(drivers, pkg, tmp_path):
     assert np.abs(a[27:36] - g["rms_rs"][sym9][inner]).max() < 2e-6 * lid * lid
     v = pkg.read_vtr(str(tmp_path / "avgfield.vtr"))
     assert "Avg reynolds Stress" in v and v["CellType"].shape == ((n + 2) * (n + 2) * n,)
+
+
+@pytest.mark.parametrize("case", ["fixed", "transverse"])
+def test_dropin_cylinder2d_loop(drivers, tmp_path, case):
+    """The reference's shipped default build (#define D2Q9, Cylinder_IBM,
+    implicit forcing) and its transverse-oscillation variant, set up and run
+    by the reference's own loop through the facade built with -DD2Q9: Cd / Cl
+    after every step against the reference's runs."""
+    from conftest import GOLDEN
+
+    if case == "fixed":
+        g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+        extra = []
+    else:
+        g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_transverse_100.npz"))
+        extra = ["0", "transverse", "2.0", "0.005"]
+    out = str(tmp_path / "cd.csv")
+    subprocess.check_call([drivers["dropin_cylinder2d"], "80", "40", "10", "40", "5", str(int(g["steps"])), out] +
+                          extra)
+    r = np.loadtxt(out, delimiter=",", skiprows=1)
+    assert r.shape == (int(g["steps"]), 3)
+    scale = np.abs(g["cd"]).max()
+    assert np.abs(r[:, 1] - g["cd"]).max() / scale < 2e-6
+    assert np.abs(r[:, 2] - g["cl"]).max() / scale < 2e-6
