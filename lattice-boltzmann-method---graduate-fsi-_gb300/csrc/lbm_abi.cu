@@ -249,6 +249,8 @@ static void free_handle(lbm_handle *h) {
     cudaFree(h->mk.rho);
     cudaFree(h->mk.force);
     cudaFree(h->mk.acc);
+    cudaFree(h->mk.sb);
+    cudaFree(h->mk.sw);
     for (int i = 0; i < 4; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
@@ -489,6 +491,8 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         cudaFree(h->mk.rho);
         cudaFree(h->mk.force);
         cudaFree(h->mk.acc);
+        cudaFree(h->mk.sb);
+        cudaFree(h->mk.sw);
         cudaFree(h->band);
         memset(&h->mk, 0, sizeof(h->mk));
         h->band = nullptr;
@@ -497,7 +501,9 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         CUDA_TRY(dalloc(h, &h->mk.udes, (size_t)3 * n * sizeof(float)));
         CUDA_TRY(dalloc(h, &h->mk.rho, (size_t)n * sizeof(float)));
         CUDA_TRY(dalloc(h, &h->mk.force, (size_t)4 * n * sizeof(float)));
-        CUDA_TRY(dalloc(h, &h->mk.acc, (size_t)4 * n * sizeof(double)));
+        CUDA_TRY(dalloc(h, &h->mk.acc, (size_t)11 * n * sizeof(double)));
+        CUDA_TRY(dalloc(h, &h->mk.sb, (size_t)3 * n * sizeof(int)));
+        CUDA_TRY(dalloc(h, &h->mk.sw, (size_t)12 * n * sizeof(float)));
         h->mk.n = n;
     }
     h->icfg = *ic;
@@ -539,7 +545,7 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     CUDA_TRY(cudaMemcpyAsync(h->mk.pos, xyz, (size_t)3 * n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CUDA_TRY(cudaMemcpyAsync(h->mk.ds, ds, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CUDA_TRY(cudaMemcpyAsync(h->mk.udes, ud.data(), ud.size() * sizeof(float), cudaMemcpyHostToDevice, h->s));
-    CUDA_TRY(cudaMemsetAsync(h->mk.acc, 0, (size_t)4 * n * sizeof(double), h->s));
+    CUDA_TRY(cudaMemsetAsync(h->mk.acc, 0, (size_t)11 * n * sizeof(double), h->s));
     // device state: band origin and rigid body
     DevState d;
     CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
@@ -561,6 +567,31 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     for (int a = 0; a < 3; a++)
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
+    // Keep the band in L2 while the far-region streaming (hundreds of MB)
+    // passes through it: a persisting access-policy window on the streams
+    // that run the IBM phase.  A per-context limit; best effort.
+    {
+        int dev = 0, max_persist = 0, max_win = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev) == cudaSuccess &&
+            max_persist > 0 && max_win > 0) {
+            const size_t bytes = std::min<size_t>((size_t)12 * nb * sizeof(float), (size_t)max_win);
+            size_t cur = 0;
+            cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
+            if (cur < bytes) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min<size_t>(bytes, max_persist));
+            cudaStreamAttrValue v;
+            memset(&v, 0, sizeof(v));
+            v.accessPolicyWindow.base_ptr = h->band;
+            v.accessPolicyWindow.num_bytes = bytes;
+            v.accessPolicyWindow.hitRatio = 1.0f;
+            v.accessPolicyWindow.hitProp = cudaAccessPropertyPersisting;
+            v.accessPolicyWindow.missProp = cudaAccessPropertyStreaming;
+            for (cudaStream_t st : {h->s, h->s2, h->s3})
+                if (st) cudaStreamSetAttribute(st, cudaStreamAttributeAccessPolicyWindow, &v);
+        }
+        cudaGetLastError();
+    }
     h->ibm = true;
     // graphs captured earlier do not contain the IBM launches
     for (int i = 0; i < 2; i++)
@@ -614,7 +645,7 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
     const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
     if (split && (e = cudaStreamWaitEvent(s, h->ev_fin, 0)) != cudaSuccess) return e;
     for (int it = 1; it <= h->icfg.m_max; it++) {
-        if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0)) != cudaSuccess) return e;
+        if ((e = launch_ibm_interp(ia, it == 1 ? 1 : 0, it == h->icfg.m_max ? 1 : 0)) != cudaSuccess) return e;
         if (split && it == h->icfg.m_max) {
             if ((e = cudaEventRecord(h->ev_acc, s)) != cudaSuccess) return e;
             if ((e = cudaStreamWaitEvent(h->s3, h->ev_acc, 0)) != cudaSuccess) return e;

@@ -54,7 +54,7 @@ std::vector<Region> regions(lbm_handle *h, int src_buffer) {
         r.push_back({h->mk.pos, 3 * n * sizeof(double)});
         r.push_back({h->mk.udes, 3 * n * sizeof(float)});
         r.push_back({h->mk.rho, n * sizeof(float)});
-        r.push_back({h->mk.acc, 4 * n * sizeof(double)});
+        r.push_back({h->mk.acc, 11 * n * sizeof(double)});
     }
     if (h->solids) r.push_back({h->mea_ring, (size_t)h->mea_cap * 4 * sizeof(double)});
     if (h->details) r.push_back({h->stats, (size_t)LBM_STAT_COUNT * h->P.N * sizeof(double)});

@@ -27,21 +27,74 @@ __device__ __forceinline__ float warp_sum(float v) {
     return v;
 }
 
-// Interpolation at marker m (one warp) and the marker force of the next
-// spreading: U_m = sum u delta with u = u_unf + Ft / (2 rho), rho_m on the
-// first pass, F_m = 2 rho_m (U_des - U_m); the FP64 accumulators collect
-// -F_m ds (the reference's Drag/Lift sums, lbm.cpp:1322-1323) and Q_m ds.
-__device__ __forceinline__ void interp_marker(int m, int lane, const StepParams &P, const MarkerDev &mk,
-                                              DevState *__restrict__ ds, const float *__restrict__ band, int first,
-                                              int thermal) {
+// Stencil of marker m: origin in band coordinates and the 4-point Peskin
+// weights per axis (lbm.cpp:1095-1102).  The first interpolation of a step
+// computes them from the marker position and stores them; the later passes
+// and the spreadings of the step read them back.  Node s of the 4x4x4 block
+// is (a, b, c) = (s & 3, (s >> 2) & 3, s >> 4); lane l holds s = l and l + 32,
+// which share a and b.
+struct Stencil {
+    int bx0, by0, bz0;
+    float kx, ky, kz0, kz1;  // this lane's weights: x of a, y of b, z of c and c + 2
+};
+
+__device__ __forceinline__ Stencil make_stencil(int m, int lane, const MarkerDev &mk, const DevState *ds,
+                                                bool store) {
     const int n = mk.n;
     const double X = mk.pos[m], Y = mk.pos[n + m], Z = mk.pos[2 * n + m];
     const double flx = floor(X), fly = floor(Y), flz = floor(Z);
     const float fx = (float)(X - flx), fy = (float)(Y - fly), fz = (float)(Z - flz);
+    Stencil st;
     // stencil node a: reference node i = floor(X) - 1 + a, device cell i - 1
-    const int bx0 = (int)flx - 2 - ds->band_o[0];
-    const int by0 = (int)fly - 2 - ds->band_o[1];
-    const int bz0 = (int)flz - 2 - ds->band_o[2];
+    st.bx0 = (int)flx - 2 - ds->band_o[0];
+    st.by0 = (int)fly - 2 - ds->band_o[1];
+    st.bz0 = (int)flz - 2 - ds->band_o[2];
+    const int a = lane & 3, b = (lane >> 2) & 3, c = lane >> 4;
+    st.kx = peskin((float)(a - 1) - fx);
+    st.ky = peskin((float)(b - 1) - fy);
+    st.kz0 = peskin((float)(c - 1) - fz);
+    st.kz1 = peskin((float)(c + 1) - fz);
+    if (store) {
+        if (lane == 0) {
+            mk.sb[m] = st.bx0;
+            mk.sb[n + m] = st.by0;
+            mk.sb[2 * n + m] = st.bz0;
+        }
+        if (b == 0 && c == 0) mk.sw[a * n + m] = st.kx;
+        if (a == 0 && c == 0) mk.sw[(4 + b) * n + m] = st.ky;
+        if (a == 0 && b == 0) {
+            mk.sw[(8 + c) * n + m] = st.kz0;
+            mk.sw[(10 + c) * n + m] = st.kz1;
+        }
+    }
+    return st;
+}
+
+__device__ __forceinline__ Stencil load_stencil(int m, int lane, const MarkerDev &mk) {
+    const int n = mk.n;
+    const int a = lane & 3, b = (lane >> 2) & 3, c = lane >> 4;
+    Stencil st;
+    st.bx0 = mk.sb[m];
+    st.by0 = mk.sb[n + m];
+    st.bz0 = mk.sb[2 * n + m];
+    st.kx = mk.sw[a * n + m];
+    st.ky = mk.sw[(4 + b) * n + m];
+    st.kz0 = mk.sw[(8 + c) * n + m];
+    st.kz1 = mk.sw[(10 + c) * n + m];
+    return st;
+}
+
+// Interpolation at marker m (one warp) and the marker force of the next
+// spreading: U_m = sum u delta with u = u_unf + Ft / (2 rho), rho_m on the
+// first pass, F_m = 2 rho_m (U_des - U_m); the FP64 accumulators collect
+// -F_m ds (the reference's Drag/Lift sums, lbm.cpp:1322-1323) and Q_m ds.
+// After the warp sums, lanes 0-2 finish the x, y, z components and lane 3
+// the heat source in parallel.
+__device__ __forceinline__ void interp_marker(int m, int lane, const StepParams &P, const MarkerDev &mk,
+                                              DevState *__restrict__ ds, const float *__restrict__ band, int first,
+                                              int last, int thermal) {
+    const int n = mk.n;
+    const Stencil st = first ? make_stencil(m, lane, mk, ds, true) : load_stencil(m, lane, mk);
     const long long nb = P.nb;
     float su = 0.f, sv = 0.f, sw = 0.f, sr = 0.f, sT = 0.f;
     bool edge = false;
@@ -49,8 +102,8 @@ __device__ __forceinline__ void interp_marker(int m, int lane, const StepParams 
     for (int h = 0; h < 2; h++) {
         const int s = lane + 32 * h;
         const int a = s & 3, b = (s >> 2) & 3, c = s >> 4;
-        const float wgt = peskin((float)(a - 1) - fx) * peskin((float)(b - 1) - fy) * peskin((float)(c - 1) - fz);
-        const int bx = bx0 + a, by = by0 + b, bz = bz0 + c;
+        const float wgt = st.kx * st.ky * (h == 0 ? st.kz0 : st.kz1);
+        const int bx = st.bx0 + a, by = st.by0 + b, bz = st.bz0 + c;
         if ((unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy && (unsigned)bz < (unsigned)P.bsz) {
             const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
             const float rho = 1.0f + band[q];
@@ -70,41 +123,51 @@ __device__ __forceinline__ void interp_marker(int m, int lane, const StepParams 
     if (first) sr = warp_sum(sr);
     if (thermal) sT = warp_sum(sT);
     const bool any_edge = __any_sync(0xffffffffu, edge);
-    if (lane == 0) {
-        if (any_edge) atomicOr(&ds->status, ST_BAND_EDGE);
-        if (first) mk.rho[m] = sr;
+    if (lane == 0 && any_edge) atomicOr(&ds->status, ST_BAND_EDGE);
+    if (first && lane == 0) mk.rho[m] = sr;
+    const double dsv = mk.ds[m];
+    double acc = 0.0;
+    if (lane < 3) {
+        const float sc = lane == 0 ? su : (lane == 1 ? sv : sw);
         const float rm = first ? sr : mk.rho[m];
-        const float Fx = 2.0f * rm * (mk.udes[m] - su);
-        const float Fy = 2.0f * rm * (mk.udes[n + m] - sv);
-        const float Fz = 2.0f * rm * (mk.udes[2 * n + m] - sw);
-        mk.force[m] = Fx;
-        mk.force[n + m] = Fy;
-        mk.force[2 * n + m] = Fz;
-        const double dsv = mk.ds[m];
-        mk.acc[m] += -(double)Fx * dsv;
-        mk.acc[n + m] += -(double)Fy * dsv;
-        mk.acc[2 * n + m] += -(double)Fz * dsv;
-        if (thermal) {
-            const float Qm = 2.0f * (mk.tdes - sT);
-            mk.force[3 * n + m] = Qm;
-            mk.acc[3 * n + m] += (double)Qm * dsv;
-        }
-        if (!isfinite(Fx) || !isfinite(Fy) || !isfinite(Fz)) atomicOr(&ds->status, ST_NONFINITE_FORCE);
+        const float F = 2.0f * rm * (mk.udes[lane * n + m] - sc);
+        mk.force[lane * n + m] = F;
+        acc = mk.acc[lane * n + m] + -(double)F * dsv;
+        if (!isfinite(F)) atomicOr(&ds->status, ST_NONFINITE_FORCE);
+    } else if (lane == 3 && thermal) {
+        const float Qm = 2.0f * (mk.tdes - sT);
+        mk.force[3 * n + m] = Qm;
+        acc = mk.acc[3 * n + m] + (double)Qm * dsv;
+    }
+    if (!last) {
+        if (lane < 3 || (lane == 3 && thermal)) mk.acc[lane * n + m] = acc;
+        return;
+    }
+    // the step's contribution of this marker, its torque about the body
+    // centre included: the FP64 work is spread over every SM and the
+    // one-block reduction only adds
+    const double a0 = __shfl_sync(0xffffffffu, acc, 0);
+    const double a1 = __shfl_sync(0xffffffffu, acc, 1);
+    const double a2 = __shfl_sync(0xffffffffu, acc, 2);
+    if (lane < 4) {
+        mk.acc[(lane < 3 ? 4 + lane : 10) * n + m] = acc;
+        mk.acc[lane * n + m] = 0.0;
+    } else if (lane < 7) {
+        const double rx = mk.pos[m] - ds->body_xc[0], ry = mk.pos[n + m] - ds->body_xc[1],
+                     rz = mk.pos[2 * n + m] - ds->body_xc[2];
+        const double t = lane == 4 ? ry * a2 - rz * a1 : (lane == 5 ? rz * a0 - rx * a2 : rx * a1 - ry * a0);
+        mk.acc[(3 + lane) * n + m] = t;
     }
 }
 
 // Spreading of marker m (one warp): Ft(x) += F_m ds_m delta(x - X_m)
-// (lbm.cpp:1331-1360), float atomics into the band.
+// (lbm.cpp:1331-1360), float atomics into the band, with the stencil the
+// step's first interpolation stored.
 __device__ __forceinline__ void spread_marker(int m, int lane, const StepParams &P, const MarkerDev &mk,
                                               const DevState *__restrict__ ds, float *__restrict__ band,
                                               int thermal) {
     const int n = mk.n;
-    const double X = mk.pos[m], Y = mk.pos[n + m], Z = mk.pos[2 * n + m];
-    const double flx = floor(X), fly = floor(Y), flz = floor(Z);
-    const float fx = (float)(X - flx), fy = (float)(Y - fly), fz = (float)(Z - flz);
-    const int bx0 = (int)flx - 2 - ds->band_o[0];
-    const int by0 = (int)fly - 2 - ds->band_o[1];
-    const int bz0 = (int)flz - 2 - ds->band_o[2];
+    const Stencil st = load_stencil(m, lane, mk);
     const long long nb = P.nb;
     const float dsv = (float)mk.ds[m];
     const float Fx = mk.force[m] * dsv, Fy = mk.force[n + m] * dsv, Fz = mk.force[2 * n + m] * dsv;
@@ -113,8 +176,8 @@ __device__ __forceinline__ void spread_marker(int m, int lane, const StepParams 
     for (int h = 0; h < 2; h++) {
         const int s = lane + 32 * h;
         const int a = s & 3, b = (s >> 2) & 3, c = s >> 4;
-        const float wgt = peskin((float)(a - 1) - fx) * peskin((float)(b - 1) - fy) * peskin((float)(c - 1) - fz);
-        const int bx = bx0 + a, by = by0 + b, bz = bz0 + c;
+        const float wgt = st.kx * st.ky * (h == 0 ? st.kz0 : st.kz1);
+        const int bx = st.bx0 + a, by = st.by0 + b, bz = st.bz0 + c;
         if (wgt != 0.0f && (unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy &&
             (unsigned)bz < (unsigned)P.bsz) {
             const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
@@ -133,10 +196,10 @@ constexpr int kIbmThreads = 64;
 
 __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_interp(const __grid_constant__ StepParams P, MarkerDev mk,
                                                     DevState *__restrict__ ds, const float *__restrict__ band,
-                                                    int first, int thermal) {
+                                                    int first, int last, int thermal) {
     const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
     if (m >= mk.n) return;  // whole warp leaves together
-    interp_marker(m, threadIdx.x & 31, P, mk, ds, band, first, thermal);
+    interp_marker(m, threadIdx.x & 31, P, mk, ds, band, first, last, thermal);
 }
 
 __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_spread(const __grid_constant__ StepParams P, MarkerDev mk,
@@ -173,21 +236,10 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
     const int n = mk.n;
     const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
-    for (int m = t; m < n; m += kFinishThreads) {
-        const double fx = mk.acc[m], fy = mk.acc[n + m], fz = mk.acc[2 * n + m], hq = mk.acc[3 * n + m];
-        const double rx = mk.pos[m] - xc0, ry = mk.pos[n + m] - xc1, rz = mk.pos[2 * n + m] - xc2;
-        s[0] += fx;
-        s[1] += fy;
-        s[2] += fz;
-        s[3] += ry * fz - rz * fy;
-        s[4] += rz * fx - rx * fz;
-        s[5] += rx * fy - ry * fx;
-        s[6] += hq;
-        mk.acc[m] = 0.0;
-        mk.acc[n + m] = 0.0;
-        mk.acc[2 * n + m] = 0.0;
-        mk.acc[3 * n + m] = 0.0;
-    }
+    // per-marker force, torque and heat of the step (the last interpolation)
+    for (int m = t; m < n; m += kFinishThreads)
+#pragma unroll
+        for (int k = 0; k < 7; k++) s[k] += mk.acc[(4 + k) * (long long)n + m];
 #pragma unroll
     for (int k = 0; k < 7; k++) red[k][t] = s[k];
     block_tree(red, 7, t);
@@ -319,10 +371,10 @@ cudaError_t launch_mea_finish(const float *part, const int *blocks, int nblocks,
     return cudaGetLastError();
 }
 
-cudaError_t launch_ibm_interp(const IbmArgs &a, int first) {
+cudaError_t launch_ibm_interp(const IbmArgs &a, int first, int last) {
     const int threads = kIbmThreads;
     const long long blocks = ((long long)a.mk.n * 32 + threads - 1) / threads;
-    k_ibm_interp<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, first, a.thermal);
+    k_ibm_interp<<<(unsigned)blocks, threads, 0, a.stream>>>(*a.P, a.mk, a.ds, a.band, first, last, a.thermal);
     return cudaGetLastError();
 }
 

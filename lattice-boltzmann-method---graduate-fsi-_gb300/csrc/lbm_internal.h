@@ -64,7 +64,11 @@ struct MarkerDev {
     float *udes;     // [3][n] desired velocity
     float *rho;      // [n] marker density
     float *force;    // [4][n] current F_m (x, y, z) and heat source Q_m
-    double *acc;     // [4][n] sum over iterations of -F_m ds and Q_m ds (FP64)
+    double *acc;     // [11][n] FP64: rows 0-3 the running sums over the iterations of -F_m ds and
+                     // Q_m ds; rows 4-10 the step's force, torque about the body centre and heat
+                     // of each marker, written by the last interpolation
+    int *sb;         // [3][n] stencil origin of the step, band coordinates
+    float *sw;       // [12][n] the step's Peskin weights per axis: x (4), y (4), z (4)
     float tdes;      // desired marker temperature (thermal IBM)
 };
 
@@ -79,7 +83,7 @@ struct IbmArgs {
 
 // first = 1: unforced interpolation and marker density; each call computes
 // the interpolated velocity (and temperature) and the next marker force.
-cudaError_t launch_ibm_interp(const IbmArgs &a, int first);
+cudaError_t launch_ibm_interp(const IbmArgs &a, int first, int last);
 cudaError_t launch_ibm_spread(const IbmArgs &a);
 
 // FP64 force/torque/heat reduction, history append and (optionally) the

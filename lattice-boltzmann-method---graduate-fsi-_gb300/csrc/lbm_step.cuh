@@ -281,4 +281,47 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
     }
 }
 
+// Collision of band cell b after the IBM forcing iterations: rho and the
+// unforced velocity from the step kernel, the accumulated IBM force Ft
+// (band[7..9]) and heat source (band[11]).  u = u_unf + Ft / (2 rho) and
+// F = Fb + sign Ft (sign = -1 reproduces lbm.cpp:1347-1352);
+// T = T_unf + Qt / 2.
+template <class T, bool THERMAL>
+__device__ __forceinline__ void band_collide_cell(T *__restrict__ B, T *__restrict__ GB, const StepParams &P,
+                                                  const DevState *__restrict__ ds, const float *__restrict__ band,
+                                                  float fsign, long long b) {
+    const int bx = (int)(b % P.bsx);
+    const int by = (int)((b / P.bsx) % P.bsy);
+    const int bz = (int)(b / ((long long)P.bsx * P.bsy));
+    const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
+    if (x < 0 || y < 0 || z < 0 || x >= P.nx || y >= P.ny || z >= P.nz) return;
+    const long long nb = P.nb;
+    const long long cell = x + (long long)P.nx * (y + (long long)P.ny * z);
+    float f[Q];
+#pragma unroll
+    for (int l = 0; l < Q; l++) f[l] = St<T>::ld(B + l * P.S + cell);
+    const float drho = band[b];
+    const float rho = 1.0f + drho;
+    const float ftx = band[7 * nb + b], fty = band[8 * nb + b], ftz = band[9 * nb + b];
+    const float ux = band[nb + b] + 0.5f * ftx / rho;
+    const float uy = band[2 * nb + b] + 0.5f * fty / rho;
+    const float uz = band[3 * nb + b] + 0.5f * ftz / rho;
+    const float Fx = band[4 * nb + b] + fsign * ftx;
+    const float Fy = band[5 * nb + b] + fsign * fty;
+    const float Fz = band[6 * nb + b] + fsign * ftz;
+    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, true, P.omega);
+#pragma unroll
+    for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
+    if (THERMAL) {
+        float g[QT];
+#pragma unroll
+        for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * P.S + cell);
+        const float Qt = band[11 * nb + b];
+        const float Tc = band[10 * nb + b] + 0.5f * Qt;
+        collide_heat(g, Tc, ux, uy, uz, Qt, P.omega_t);
+#pragma unroll
+        for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
+    }
+}
+
 }  // namespace lbmk

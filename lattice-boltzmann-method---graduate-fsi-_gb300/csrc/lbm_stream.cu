@@ -100,12 +100,10 @@ __global__ void __launch_bounds__(256, (THERMAL || SOLID) ? 4 : (FORCED ? 5 : 6)
                                     region != 1);
 }
 
-// Collision of the IBM band cells, after the forcing iterations: rho and the
-// unforced velocity from k_step, the accumulated IBM force Ft (band[7..9])
-// and heat source (band[11]).  u = u_unf + Ft / (2 rho) and F = Fb + sign Ft
-// (sign = -1 reproduces lbm.cpp:1347-1352); T = T_unf + Qt / 2.
-// 64-thread blocks of at most 64 registers: they fit beside the far-region
-// collide-stream blocks (which leave 4096 registers per SM) when overlapped.
+// Collision of the IBM band cells after the forcing iterations
+// (band_collide_cell).  64-thread blocks of at most 64 registers: they fit
+// beside the far-region collide-stream blocks (which leave 4096 registers
+// per SM) when overlapped.
 template <class T, bool THERMAL>
 __global__ void __launch_bounds__(64, 16) k_band_collide(T *__restrict__ B, T *__restrict__ GB,
                                                       const __grid_constant__ StepParams P,
@@ -113,38 +111,7 @@ __global__ void __launch_bounds__(64, 16) k_band_collide(T *__restrict__ B, T *_
                                                       const float *__restrict__ band, float fsign) {
     const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (b >= P.nb) return;
-    const int bx = (int)(b % P.bsx);
-    const int by = (int)((b / P.bsx) % P.bsy);
-    const int bz = (int)(b / ((long long)P.bsx * P.bsy));
-    const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
-    if (x < 0 || y < 0 || z < 0 || x >= P.nx || y >= P.ny || z >= P.nz) return;
-    const long long nb = P.nb;
-    const long long cell = x + (long long)P.nx * (y + (long long)P.ny * z);
-    float f[Q];
-#pragma unroll
-    for (int l = 0; l < Q; l++) f[l] = St<T>::ld(B + l * P.S + cell);
-    const float drho = band[b];
-    const float rho = 1.0f + drho;
-    const float ftx = band[7 * nb + b], fty = band[8 * nb + b], ftz = band[9 * nb + b];
-    const float ux = band[nb + b] + 0.5f * ftx / rho;
-    const float uy = band[2 * nb + b] + 0.5f * fty / rho;
-    const float uz = band[3 * nb + b] + 0.5f * ftz / rho;
-    const float Fx = band[4 * nb + b] + fsign * ftx;
-    const float Fy = band[5 * nb + b] + fsign * fty;
-    const float Fz = band[6 * nb + b] + fsign * ftz;
-    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, true, P.omega);
-#pragma unroll
-    for (int l = 0; l < Q; l++) St<T>::st(B + l * P.S + cell, f[l]);
-    if (THERMAL) {
-        float g[QT];
-#pragma unroll
-        for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * P.S + cell);
-        const float Qt = band[11 * nb + b];
-        const float Tc = band[10 * nb + b] + 0.5f * Qt;
-        collide_heat(g, Tc, ux, uy, uz, Qt, P.omega_t);
-#pragma unroll
-        for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
-    }
+    band_collide_cell<T, THERMAL>(B, GB, P, ds, band, fsign, b);
 }
 
 // Initial populations (LBM::Init, lbm.cpp:31-57): f = feq3(rho, u) stored
