@@ -185,7 +185,19 @@ struct Ibm2 {
     uint8_t *inside;  // [nb] box node inside every marker (Calc_AverageDensity)
     double *hist;     // [cap][4]: drag, lift, 0, step
     int smem;         // 1: the working fields of the pass live in shared memory
+    int fast;         // 1: box nodes in registers (at most kFastNodes per thread, n <= block size)
 };
+
+// Box nodes a thread of the register-resident pass owns.
+constexpr int kFastNodes = 4;
+
+// Shared-memory words of the register-resident pass: u at the box nodes
+// (2 nb), the marker forces (2 n), the stencils as (node, weight) pairs
+// (32 n), the spreading lists as (marker, weight) pairs (32 n), the marker
+// densities (n).
+__host__ __device__ inline size_t ibm2d_fast_smem_bytes(long long nb, int n) {
+    return (size_t)4 * (2 * (size_t)nb + 67 * (size_t)n);
+}
 
 // 4-point Peskin delta (lbm.cpp:1095-1102).
 __device__ __forceinline__ double peskin_d(double r) {
@@ -494,6 +506,135 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
         __syncthreads();
     }
 
+    const float sgn = ib.lit_sign ? -1.0f : 1.0f;
+    double drag, lift;
+    if (ib.fast) {
+        // Register-resident pass: every thread keeps its box nodes' index,
+        // 1 / (2 rho), u, F and list span in registers for the m_max
+        // iterations; shared memory holds u (read by the interpolation), the
+        // marker forces, the stencils and the lists as packed pairs.
+        float2 *uxy = reinterpret_cast<float2 *>(smem);
+        float2 *fsp = uxy + nb;
+        float2 *mst = fsp + n;                               // [16][n] (node as int bits, weight)
+        int2 *lst = reinterpret_cast<int2 *>(mst + 16 * n);  // (marker, weight as int bits)
+        float *rhm = reinterpret_cast<float *>(lst + 16 * n);
+        int nq[kFastNodes], la[kFastNodes], lc[kFastNodes];
+        float hr[kFastNodes], fx[kFastNodes], fy[kFastNodes], vx[kFastNodes], vy[kFastNodes];
+#pragma unroll
+        for (int k = 0; k < kFastNodes; k++) {
+            const int o = tid + k * nt;
+            nq[k] = -1;
+            la[k] = lc[k] = 0;
+            hr[k] = fx[k] = fy[k] = vx[k] = vy[k] = 0.0f;
+            if (o < nbox) {
+                const int q = (int)bq(o);
+                nq[k] = q;
+                hr[k] = 0.5f / (1.0f + band[q]);
+                vx[k] = band[nb + q];
+                vy[k] = band[2 * nb + q];
+                fx[k] = band[3 * nb + q];
+                fy[k] = band[4 * nb + q];
+                la[k] = ib.off[q];
+                lc[k] = ib.cnt[q];
+                uxy[q] = make_float2(vx[k], vy[k]);
+            }
+        }
+        for (int i = tid; i < 16 * n; i += nt) {
+            const int k = i / n, m = i - k * n;
+            const float w = ib.swt[i];
+            const int q = w != 0.0f ? (ib.s0[m] + k / 4) + P.bsx * (ib.s0[n + m] + k % 4) : -1;
+            mst[i] = make_float2(__int_as_float(q), w);
+            lst[i] = make_int2(ib.lm[i], __float_as_int(ib.lw[i]));
+        }
+        // marker density: nearest node (k_move2d), or delta-interpolated
+        float rmine = 0.0f, dsmine = 0.0f;
+        double dsd = 0.0;
+        if (tid < n) {
+            const int m = tid;
+            if (ib.rho_nearest) {
+                const int q = ib.qnear[m];
+                rmine = q < 0 ? 1.0f : 1.0f + band[q];
+            } else {
+                float sr = 0.0f;
+                for (int k = 0; k < 16; k++) {
+                    const float w = ib.swt[k * n + m];
+                    if (w != 0.0f) sr += (1.0f + band[(ib.s0[m] + k / 4) + P.bsx * (ib.s0[n + m] + k % 4)]) * w;
+                }
+                rmine = sr;
+            }
+            rhm[m] = rmine;
+            dsd = ib.dsw[m];
+            dsmine = (float)dsd;
+        }
+        __syncthreads();
+        double mk_drag = 0.0, mk_lift = 0.0, node_drag = 0.0, node_lift = 0.0;
+        const int iters = ib.scheme == 1 ? 1 : ib.m_max;
+        for (int it = 0; it < iters; it++) {
+            // interpolation and marker force (lbm.cpp:1314-1324), one
+            // thread per marker, nodes in the reference's order
+            if (tid < n) {
+                const int m = tid;
+                float ub = 0.0f, vb = 0.0f;
+#pragma unroll
+                for (int k = 0; k < 16; k++) {
+                    const float2 e = mst[k * n + m];
+                    const int q = __float_as_int(e.x);
+                    if (q >= 0) {
+                        const float2 u = uxy[q];
+                        ub += u.x * e.y;
+                        vb += u.y * e.y;
+                    }
+                }
+                const float Fbx = 2.0f * rmine * (V0 - ub), Fby = 2.0f * rmine * (V1 - vb);
+                fsp[m] = make_float2(Fbx * dsmine, Fby * dsmine);
+                mk_drag += -(double)Fbx * 1.0 * dsd;
+                mk_lift += -(double)Fby * 1.0 * dsd;
+                if (!isfinite(Fbx) || !isfinite(Fby)) atomicOr(&st->status, lbmk::ST_NONFINITE_FORCE);
+            }
+            __syncthreads();
+            // spreading onto this thread's nodes, ascending marker order
+#pragma unroll
+            for (int k = 0; k < kFastNodes; k++) {
+                if (nq[k] < 0) continue;
+                float sx = 0.0f, sy = 0.0f;
+                for (int i = la[k]; i < la[k] + lc[k]; i++) {
+                    const int2 e = lst[i];
+                    const float2 f = fsp[e.x];
+                    const float w = __int_as_float(e.y);
+                    sx += f.x * w;
+                    sy += f.y * w;
+                }
+                if (ib.scheme == 0) {
+                    fx[k] += sgn * sx;
+                    fy[k] += sgn * sy;
+                } else {
+                    fx[k] += sx;
+                    fy[k] += sy;
+                    node_drag += -(double)sx;
+                    node_lift += -(double)sy;
+                }
+                vx[k] += sx * hr[k];
+                vy[k] += sy * hr[k];
+                uxy[nq[k]] = make_float2(vx[k], vy[k]);
+            }
+            __syncthreads();
+        }
+        drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
+        lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
+        // collision of this thread's box cells
+#pragma unroll
+        for (int k = 0; k < kFastNodes; k++) {
+            if (nq[k] < 0) continue;
+            const int o = tid + k * nt;
+            const long long cell = (st->box_lo[0] + o % bw) + (long long)P.nx * (st->box_lo[1] + o / bw);
+            float f[Q9];
+#pragma unroll
+            for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
+            collide9(f, band[nq[k]], vx[k], vy[k], fx[k], fy[k], P.omega, true);
+#pragma unroll
+            for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+        }
+    } else {
     // working copies: shared memory when they fit, else the global arrays
     float *drho = band, *ux = band + nb, *uy = band + 2 * nb, *Fx = band + 3 * nb, *Fy = band + 4 * nb;
     int *cnt = ib.cnt, *off = ib.off, *lm = ib.lm, *s0 = ib.s0;
@@ -557,7 +698,6 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     }
     __syncthreads();
 
-    const float sgn = ib.lit_sign ? -1.0f : 1.0f;
     double node_drag = 0.0, node_lift = 0.0, mk_drag = 0.0, mk_lift = 0.0;
     const int iters = ib.scheme == 1 ? 1 : ib.m_max;
     for (int it = 0; it < iters; it++) {
@@ -605,8 +745,21 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     }
 
     // the pass's force: sum over markers (implicit) or box nodes (explicit)
-    const double drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
-    const double lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
+    drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
+    lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
+
+    // collision of the box cells with the forced velocity and the force
+    for (int o = tid; o < nbox; o += nt) {
+        const long long q = bq(o);
+        const long long cell = (st->box_lo[0] + o % bw) + (long long)P.nx * (st->box_lo[1] + o / bw);
+        float f[Q9];
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
+        collide9(f, drho[q], ux[q], uy[q], Fx[q], Fy[q], P.omega, true);
+#pragma unroll
+        for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+    }
+    }  // general pass
 
     // added mass (lbm.cpp:1392-1398): mean density of the box nodes inside
     // every marker (k_inside2d); skipped when V_CM did not change, where it
@@ -618,7 +771,7 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
         for (int o = tid; o < nbox; o += nt) {
             const long long q = bq(o);
             if (ib.inside[q]) {
-                rs += 1.0 + (double)drho[q];
+                rs += 1.0 + (double)band[q];
                 cn += 1.0;
             }
         }
@@ -640,17 +793,6 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
         row[3] = (double)step;
     }
 
-    // collision of the box cells with the forced velocity and the force
-    for (int o = tid; o < nbox; o += nt) {
-        const long long q = bq(o);
-        const long long cell = (st->box_lo[0] + o % bw) + (long long)P.nx * (st->box_lo[1] + o / bw);
-        float f[Q9];
-#pragma unroll
-        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
-        collide9(f, drho[q], ux[q], uy[q], Fx[q], Fy[q], P.omega, true);
-#pragma unroll
-        for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
-    }
     __syncthreads();
     // the box of the next step, for its collide-stream launch
     if (tid == 0) box_of(st, ib, P, step + 1);
@@ -829,7 +971,8 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
 cudaError_t launch_ibm2d(lbm_handle *h) {
     lbm2d *d = h->d2;
     void *B = d->f[1 - d->cur];
-    const size_t sm = d->ib.smem ? ibm2d_smem_bytes(d->P.nb, d->ib.n) : 0;
+    const size_t sm = d->ib.fast ? ibm2d_fast_smem_bytes(d->P.nb, d->ib.n)
+                                 : (d->ib.smem ? ibm2d_smem_bytes(d->P.nb, d->ib.n) : 0);
     switch (h->cfg.storage) {
     case LBM_STORE_F16: k_ibm2d<__half><<<1, kIbmBlock, sm, h->s>>>((__half *)B, d->P, d->st, d->ib, d->band); break;
     case LBM_STORE_BF16:
@@ -1027,7 +1170,10 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     CK2(cudaGetDevice(&dev));
     CK2(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     ib.smem = sm + 1024 <= (size_t)optin ? 1 : 0;
-    if (ib.smem) CK2(ibm2d_smem_setup(h->cfg.storage, sm));
+    const size_t smf = ibm2d_fast_smem_bytes(P.nb, n);
+    ib.fast = (n <= kIbmBlock && P.nb <= (long long)kFastNodes * kIbmBlock && smf + 1024 <= (size_t)optin) ? 1 : 0;
+    const size_t smax = std::max(ib.smem ? sm : (size_t)0, ib.fast ? smf : (size_t)0);
+    if (smax > 0) CK2(ibm2d_smem_setup(h->cfg.storage, smax));
     CK2(cudaMemcpyAsync(ib.pos, xyz, (size_t)3 * n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CK2(cudaMemcpyAsync(dsd, dsw, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, h->s));
     CK2(cudaMemsetAsync(nrm, 0, (size_t)3 * n * sizeof(double), h->s));

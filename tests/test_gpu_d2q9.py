@@ -196,3 +196,21 @@ def test_d2q9_unsupported_calls_fail_loudly(pkg, tmp_path):
         with pytest.raises(pkg.LbmError) as e:
             call()
         assert e.value.status == 7
+
+
+def test_d2q9_ibm_large_box_vs_oracle(pkg, orc):
+    """A body large enough that its IBM box (67 x 67 nodes) leaves the
+    register-resident pass for the shared-memory one."""
+    nx, ny, D, nodes, mm, steps = 200, 120, 32.0, 100, 3, 12
+
+    class G(dict):
+        pass
+
+    g = G(nx=nx, ny=ny, D=D, nodes=nodes)
+    s, cl, cd = _cylinder_gpu(pkg, orc, g, steps, m_max=mm)
+    lat, mk, rcl, rcd = orc.cylinder2d_literal(nx, ny, D, nodes, mm, steps)
+    scale = np.abs(rcd).max()
+    e = max(np.abs(cd - rcd).max(), np.abs(cl - rcl).max()) / scale
+    print("large-box Cl/Cd error / max|Cd|: %.3g" % e)
+    assert e < 2e-6
+    _check_fields(s.moments(), *_layer_moments(lat), 0.1)
