@@ -29,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liblbm_oracle.so")
 
-TYPE_F, TYPE_S, TYPE_OUT, TYPE_IN, TYPE_P, TYPE_L, TYPE_OUTZG = 0, 1, 2, 3, 4, 5, 8
+TYPE_F, TYPE_S, TYPE_OUT, TYPE_IN, TYPE_P, TYPE_L, TYPE_T, TYPE_OUTZG = 0, 1, 2, 3, 4, 5, 6, 8
 
 # D3Q19 in the reference order (LBM.h:542-552)
 CX19 = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
@@ -70,6 +70,10 @@ def lib():
         L.orc_create.argtypes = [i, i, i, i, d]
         L.orc_free.argtypes = [vp]
         L.orc_enable_thermal.argtypes = [vp, d, d, d, d, d]
+        L.orc_enable_energy.argtypes = [vp, d, d, d]
+        L.orc_energy_buoyancy.argtypes = [vp, d, d]
+        L.orc_types_energy.restype = C.POINTER(C.c_uint8)
+        L.orc_types_energy.argtypes = [vp]
         L.orc_ncell.restype = l
         L.orc_ncell.argtypes = [vp]
         L.orc_types.restype = C.POINTER(C.c_uint8)
@@ -157,6 +161,7 @@ class Lattice:
         self.shape = (nz + 2, ny + 2, nx + 2)
         self.n = int(self.L.orc_ncell(self.h))
         self.thermal = False
+        self.energy = False
 
     def __del__(self):
         try:
@@ -169,6 +174,22 @@ class Lattice:
     def enable_thermal(self, tau_g: float, T0: float = 0.0, gbeta=(0.0, 0.0, 0.0)):
         self.L.orc_enable_thermal(self.h, tau_g, T0, *gbeta)
         self.thermal = True
+
+    def enable_energy(self, tau_g: float, cp: float, nu: float):
+        """The reference's ENERGY model: g on the flow lattice (q
+        populations), viscous heating with cp and nu, Dirichlet walls where
+        ``types_energy`` is TYPE_T.  Set T (walls included) before init()."""
+        self.L.orc_enable_energy(self.h, tau_g, cp, nu)
+        self.energy = True
+
+    def energy_buoyancy(self, g_beta: float, T_star: float):
+        """Rayleigh_Benard: F_y = g_beta (T - T_star) on every cell."""
+        self.L.orc_energy_buoyancy(self.h, g_beta, T_star)
+
+    @property
+    def types_energy(self) -> np.ndarray:
+        p = self.L.orc_types_energy(self.h)
+        return np.ctypeslib.as_array(p, shape=(self.n,)).reshape(self.shape)
 
     def _view(self, which: int, comps: int = 1) -> np.ndarray:
         p = self.L.orc_field(self.h, which)
@@ -194,6 +215,10 @@ class Lattice:
     T = property(lambda s: s._view(9))
     g = property(lambda s: s._view(10, 7))
     gs = property(lambda s: s._view(11, 7))
+    eg = property(lambda s: s._view(13, s.q))
+    hq = property(lambda s: s._view(14, 3))
+    egs = property(lambda s: s._view(15, s.q))
+    fvis = property(lambda s: s._view(16, s.q))
 
     def set_body_force(self, fx, fy, fz):
         self.L.orc_set_body_force(self.h, fx, fy, fz)
@@ -358,6 +383,38 @@ def cylinder_markers_literal(nodes: int, D: float, cx: float, cy: float) -> Mark
     a["nz"][:] = tx * 0 - ty * 0
     a["ds"][:] = np.sqrt((a["x"] - x2) ** 2 + (a["y"] - y2) ** 2 + 0.0)
     return mk
+
+
+def couette_energy(ny: int, Re: float, tau: float = 0.9, nx: int = 2, nz: int = 2, Pr: float = 0.7,
+                   Br: float = 10.0, Tb: float = 0.5):
+    """main_setup_Couette (lbm.cpp:1537-1580) with ENERGY and D2Q9: walls
+    (TYPE_S, Dirichlet TYPE_T) on rows j = 0 and Ny + 1, the top one moving
+    at u_wall = Re nu / (Ny + 1), periodic in x and z; T = Tb on the fluid
+    and the bottom wall, Tt = Tb + u_wall^2 / (cp Ec) on the top wall.  The
+    thermal constants follow LBM.h:206-219: alpha = nu / Pr, tau_g = 0.5 +
+    alpha / cs2, k = cs2 tau_g, cp = k / alpha, Ec = Br / Pr.  Returns the
+    initialised lattice and the constants."""
+    cs2 = 1.0 / 3.0
+    nu = cs2 * (tau - 0.5)
+    uw = Re * nu / (ny + 1)
+    alpha = nu / Pr
+    tau_g = 0.5 + alpha / cs2
+    cp = cs2 * tau_g / alpha
+    Tt = Tb + uw ** 2 / (cp * (Br / Pr))
+    lat = Lattice(9, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    t[:, 0, :] = TYPE_S
+    t[:, -1, :] = TYPE_S
+    lat.enable_energy(tau_g, cp, nu)
+    te = lat.types_energy
+    te[:, 0, :] = TYPE_T
+    te[:, -1, :] = TYPE_T
+    lat.ux[:, -1, :] = uw
+    lat.T[:] = Tb
+    lat.T[:, -1, :] = Tt
+    lat.init()
+    return lat, dict(tau=tau, tau_g=tau_g, cp=cp, nu=nu, u_wall=uw, Tb=Tb, Tt=Tt)
 
 
 def read_ref_dump(path: str, NX: int, NY: int, NZ: int, nfields: int, steps: int = 0, nodes: int = 0):

@@ -13,6 +13,7 @@
 #   explicit:NX:NY:D:NODES    the same cylinder, explicit direct forcing
 #   transverse:NX:NY:D:NODES:M:AMP:FREQ  D2Q9 cylinder oscillating across the stream
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
+#   couette:NY:RE             D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${REF:-/root/reference}
@@ -23,7 +24,7 @@ if [ ! -f "$REF/lbm.cpp" ]; then
 fi
 mkdir -p "$OUT"
 [ $# -eq 0 ] && set -- cavity:12:0.8 cavity:64:0.8 cylinder:80:40:10:40:5 sphere:48:24:24:8:20:0.05 details:8:0.8 \
-    explicit:80:40:10:40 transverse:80:40:10:40:5:2.0:0.005
+    explicit:80:40:10:40 transverse:80:40:10:40:5:2.0:0.005 couette:30:20
 CXX=${CXX:-g++}
 FLAGS="-O2 -fopenmp -ffp-contract=off -w -include $HERE/ref_config.h -I$HERE/shim -I$REF"
 pids=""
@@ -63,6 +64,11 @@ for v in "$@"; do
         exe="$OUT/ref_transverse_${nx}_${ny}_${d}_${nodes}_${mm}_${amp}_${fr}"
         $CXX $FLAGS -DREF_TRANSVERSE -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
             -DREF_AMP=$amp -DREF_FREQ=$fr -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    couette)
+        ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3)
+        exe="$OUT/ref_couette_${ny}_${re}"
+        $CXX $FLAGS -DREF_COUETTE -DREF_NY=$ny -DREF_RE=$re -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     sphere)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)

@@ -52,7 +52,7 @@
 /* Cell types: LBM.h:505-515 (TYPE_F .. TYPE_Q).  ORC_OUTZG is new: a ghost
  * cell that repeats the post-collision populations of the interior cell next
  * to it (zero-gradient outlet). */
-enum { ORC_F = 0, ORC_S = 1, ORC_OUT = 2, ORC_IN = 3, ORC_P = 4, ORC_L = 5, ORC_OUTZG = 8 };
+enum { ORC_F = 0, ORC_S = 1, ORC_OUT = 2, ORC_IN = 3, ORC_P = 4, ORC_L = 5, ORC_T = 6, ORC_OUTZG = 8 };
 
 /* D2Q9 and D3Q19 tables in the reference order: LBM.h:528-555. */
 static const int CX9[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
@@ -99,6 +99,14 @@ typedef struct orc {
     int thermal;
     double tau_g, T0, gbeta[3];
     double *T, *Qh, *g, *gs;
+    /* the reference's own thermal model (ENERGY): temperature populations on
+     * the flow lattice, viscous heating, Dirichlet walls */
+    int energy, ebuoy;
+    double etau_g, ecp, enu;
+    double eg_beta, eT_star;   /* Rayleigh_Benard buoyancy F_y = g beta (T - T*) */
+    double *eg, *egs, *fvis;   /* [q][ncell] */
+    double *hq;                /* [3][ncell] heat flux sum g c */
+    uint8_t *type_e;           /* type_Energy: ORC_T (Dirichlet) on walls */
 } orc;
 
 static inline long IDX(const orc *o, int i, int j, int k) {
@@ -147,17 +155,39 @@ void orc_enable_thermal(orc *o, double tau_g, double T0, double gbx, double gby,
     o->gs = (double *)calloc(7 * (size_t)n, sizeof(double));
 }
 
+/* The reference's ENERGY thermal model (LBM.h:58): g on the flow lattice.
+ * T (fluid[..].T) must be set per cell by the caller, walls included. */
+void orc_enable_energy(orc *o, double tau_g, double cp, double nu) {
+    long n = o->ncell;
+    o->energy = 1;
+    o->etau_g = tau_g; o->ecp = cp; o->enu = nu;
+    if (!o->T) o->T = (double *)calloc(n, sizeof(double));
+    o->eg = (double *)calloc((size_t)o->q * n, sizeof(double));
+    o->egs = (double *)calloc((size_t)o->q * n, sizeof(double));
+    o->fvis = (double *)calloc((size_t)o->q * n, sizeof(double));
+    o->hq = (double *)calloc(3 * (size_t)n, sizeof(double));
+    o->type_e = (uint8_t *)calloc(n, 1);
+}
+
 void orc_free(orc *o) {
     if (!o) return;
     free(o->type); free(o->rho); free(o->ux); free(o->uy); free(o->uz);
     free(o->Fx); free(o->Fy); free(o->Fz); free(o->f); free(o->fs);
     free(o->T); free(o->Qh); free(o->g); free(o->gs);
+    free(o->eg); free(o->egs); free(o->fvis); free(o->hq); free(o->type_e);
     free(o);
+}
+
+/* Rayleigh_Benard's force update (lbm.cpp:803-805). */
+void orc_energy_buoyancy(orc *o, double g_beta, double T_star) {
+    o->ebuoy = 1;
+    o->eg_beta = g_beta; o->eT_star = T_star;
 }
 
 /* Accessors for the ctypes wrapper. */
 long orc_ncell(orc *o) { return o->ncell; }
 uint8_t *orc_types(orc *o) { return o->type; }
+uint8_t *orc_types_energy(orc *o) { return o->type_e; }
 double *orc_field(orc *o, int which) {
     switch (which) {
     case 0: return o->rho;
@@ -173,6 +203,10 @@ double *orc_field(orc *o, int which) {
     case 10: return o->g;
     case 11: return o->gs;
     case 12: return o->Qh;
+    case 13: return o->eg;
+    case 14: return o->hq;
+    case 15: return o->egs;
+    case 16: return o->fvis;
     default: return NULL;
     }
 }
@@ -199,6 +233,46 @@ static inline double geq7(double T, double ux, double uy, double uz, int l) {
     return W7[l] * T * (1.0 + (CX7[l] * ux + CY7[l] * uy + CZ7[l] * uz) / CS2T);
 }
 
+/* LBM::Determine_Wall_Temperature, lbm.cpp:965-981: mean T of the solid
+ * neighbours of a cell (periodic modulo over N+2). */
+static double wall_temperature(const orc *o, int i, int j, int k) {
+    int num = 0;
+    double Tw = 0;
+    for (int l = 0; l < o->q; l++) {
+        int in = (i + o->cx[l] + o->NX) % o->NX;
+        int jn = (j + o->cy[l] + o->NY) % o->NY;
+        int kn = (k + o->cz[l] + o->NZ) % o->NZ;
+        long nb = IDX(o, in, jn, kn);
+        if (o->type[nb] == ORC_S) {
+            Tw += o->T[nb];
+            num++;
+        }
+    }
+    Tw /= num;
+    return Tw;
+}
+
+/* LBM::Calc_geq, lbm.cpp:636-653: rho w T (cubic equilibrium shape), with
+ * the cell's T and u, or for a solid type the wall temperature of the cell
+ * and the given wall velocity. */
+static double energy_geq(const orc *o, int i, int j, int k, int l, int wall, const double uw[3]) {
+    long c = IDX(o, i, j, k);
+    double T, ux, uy, uz;
+    if (wall) {
+        T = wall_temperature(o, i, j, k);
+        ux = uw[0]; uy = uw[1]; uz = uw[2];
+    } else {
+        T = o->T[c];
+        ux = o->ux[c]; uy = o->uy[c]; uz = o->uz[c];
+    }
+    double cs2 = o->cs2;
+    double u_dot_u = pow(ux, 2) + pow(uy, 2) + pow(uz, 2);
+    double c_dot_u = ux * o->cx[l] + uy * o->cy[l] + uz * o->cz[l];
+    return o->rho[c] * o->w[l] * T *
+           (1 + c_dot_u / cs2 + pow(c_dot_u, 2) / (2 * cs2 * cs2) - u_dot_u / (2 * cs2) +
+            pow(c_dot_u, 3) / (6 * o->cs2_3) - c_dot_u * u_dot_u / (2 * cs2 * cs2));
+}
+
 /* LBM::Init, lbm.cpp:31-57: f = f* = feq(rho,u) on every cell, ghosts included. */
 void orc_init(orc *o) {
     long n = o->ncell;
@@ -216,6 +290,21 @@ void orc_init(orc *o) {
                 o->gs[l * n + c] = ge;
             }
         }
+    }
+    if (o->energy) {
+        /* g = g* = Calc_geq(cell type), the wall velocity zero (lbm.cpp:44-49) */
+        const double zero[3] = {0, 0, 0};
+#pragma omp parallel for collapse(2)
+        for (int k = 0; k < o->NZ; k++)
+            for (int j = 0; j < o->NY; j++)
+                for (int i = 0; i < o->NX; i++) {
+                    long c = IDX(o, i, j, k);
+                    for (int l = 0; l < o->q; l++) {
+                        double ge = energy_geq(o, i, j, k, l, o->type[c] == ORC_S, zero);
+                        o->eg[l * n + c] = ge;
+                        o->egs[l * n + c] = ge;
+                    }
+                }
     }
 }
 
@@ -240,6 +329,43 @@ long orc_collide(orc *o) {
                             (F_dot_c / cs2 + (F_dot_c) * (c_dot_u) / (cs2 * cs2) - F_dot_u / cs2);
             o->fs[l * n + c] = o->f[l * n + c] * (1 - omega) + omega * f_eq + Source * 1.0;
             if (f_eq < 0) bad++;
+        }
+        if (o->energy) {
+            /* ENERGY part of ConvLBM (lbm.cpp:121-177): viscous dissipation
+             * Phi = 2 nu rho S:S with S from the non-equilibrium part of f,
+             * the source F_vis and its time derivative against the previous
+             * step's F_vis */
+            double S[3][3];
+            const int *cc[3] = {o->cx, o->cy, o->cz};
+            for (int row = 0; row < 3; row++)
+                for (int col = 0; col < 3; col++) {
+                    S[row][col] = 0;
+                    if (col < row) continue;
+                    for (int l = 0; l < o->q; l++) {
+                        double f_eq = feq3(o, rho, ux, uy, uz, l);
+                        S[row][col] += cc[row][l] * cc[col][l] * (o->f[l * n + c] - f_eq);
+                    }
+                }
+            S[1][0] = S[0][1]; S[2][0] = S[0][2]; S[2][1] = S[1][2];
+            for (int row = 0; row < 3; row++)
+                for (int col = 0; col < 3; col++) S[row][col] = -S[row][col] / (2 * rho * o->tau * cs2);
+            double Phi = 0;
+            for (int row = 0; row < 3; row++)
+                for (int col = 0; col < 3; col++) Phi += S[row][col] * S[row][col];
+            Phi = 2 * o->enu * rho * Phi;
+            const double tg = o->etau_g;
+            const int ci = (int)(c % o->NX), cj = (int)((c / o->NX) % o->NY), ck = (int)(c / ((long)o->NX * o->NY));
+            const double zero[3] = {0, 0, 0};
+            for (int l = 0; l < o->q; l++) {
+                double c_dot_u = ux * o->cx[l] + uy * o->cy[l] + uz * o->cz[l];
+                double F_before = o->fvis[l * n + c];
+                double F = o->w[l] * Phi / o->ecp * (1 + c_dot_u * (tg - 0.5) / (cs2 * tg));
+                o->fvis[l * n + c] = F;
+                double dF_dt = (F - F_before) / 1.0;
+                double g_eq = energy_geq(o, ci, cj, ck, l, 0, zero);
+                double gl = o->eg[l * n + c];
+                o->egs[l * n + c] = gl - (gl - g_eq) / tg + 1.0 * F + 0.5 * pow(1.0, 2) * dF_dt;
+            }
         }
         if (o->thermal) {
             /* D3Q7 BGK with heat source Qh (new physics). */
@@ -310,10 +436,17 @@ void orc_stream(orc *o) {
                     uint8_t t = o->type[nb];
                     if (t == ORC_F) {
                         o->f[l * n + nb] = o->fs[l * n + c];
+                        if (o->energy) o->eg[l * n + nb] = o->egs[l * n + c];
                     } else if (t == ORC_S) {
                         if (!have_uw) { wall_velocity(o, i, j, k, uw); have_uw = 1; }
                         double uwall_dot_c = uw[0] * o->cx[l] + uw[1] * o->cy[l] + uw[2] * o->cz[l];
                         o->f[o->opp[l] * n + c] = o->fs[l * n + c] - 2 * o->w[l] * uwall_dot_c / cs2;
+                        /* Dirichlet wall (type_Energy TYPE_T): anti-bounce-back
+                         * against the wall equilibrium (lbm.cpp:277-280) */
+                        if (o->energy && o->type_e[nb] == ORC_T) {
+                            double g_eq = energy_geq(o, i, j, k, l, 1, uw);
+                            o->eg[o->opp[l] * n + c] = -o->egs[l * n + c] + 2 * g_eq;
+                        }
                     }
                     /* Pull-side view of the zero-gradient ghost: the
                      * population of this cell arriving from direction l's
@@ -379,11 +512,25 @@ long orc_macro(orc *o) {
         } else if (o->type[c] == ORC_F && (o->body[0] != 0 || o->body[1] != 0 || o->body[2] != 0)) {
             o->Fx[c] = o->body[0]; o->Fy[c] = o->body[1]; o->Fz[c] = o->body[2];
         }
+        if (o->energy) {
+            /* T = sum g, q = sum g c on every cell (lbm.cpp:776-792) */
+            double T = 0, gx = 0, gy = 0, gz = 0;
+            for (int l = 0; l < o->q; l++) {
+                double gl = o->eg[l * n + c];
+                T += gl; gx += gl * o->cx[l]; gy += gl * o->cy[l]; gz += gl * o->cz[l];
+            }
+            o->T[c] = T;
+            o->hq[c] = gx; o->hq[n + c] = gy; o->hq[2 * n + c] = gz;
+        }
         o->rho[c] = rho;
         o->ux[c] = (rho_ux + 0.5 * 1.0 * o->Fx[c]) / rho;
         o->uy[c] = (rho_uy + 0.5 * 1.0 * o->Fy[c]) / rho;
         o->uz[c] = (rho_uz + 0.5 * 1.0 * o->Fz[c]) / rho;
+        /* Rayleigh_Benard: F_y = g beta (T - T*) on every cell, after u took
+         * the previous force (lbm.cpp:803-805) */
+        if (o->energy && o->ebuoy) o->Fy[c] = o->eg_beta * (o->T[c] - o->eT_star);
         if (rho < 0 || rho > 100) bad++;
+        if (o->energy && (o->T[c] < 0 || o->T[c] > 100)) bad++;
     }
     return bad;
 }

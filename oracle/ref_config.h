@@ -16,6 +16,9 @@
  *                 stream (the reference's Cylinder_Transverse_Oscillation),
  *                 shrunk; REF_AMP and REF_FREQ set its amplitude and
  *                 frequency.
+ *   REF_COUETTE   D2Q9 Couette flow with the reference's own thermal model
+ *                 (ENERGY: temperature populations on the flow lattice,
+ *                 viscous heating, Dirichlet walls), Ny = REF_NY, Re = REF_RE.
  *   REF_SPHERE    D3Q19 staircase sphere with momentum-exchange Cl/Cd (the
  *                 reference's Sphere_BB case), shrunk to test size; REF_D,
  *                 REF_RE and REF_U set the diameter, Reynolds number and
@@ -129,6 +132,36 @@ static const int level_marker = 1;
 static int m_max = REF_MMAX;
 #define T_OUT 30000
 #define Nt 10
+#elif defined REF_COUETTE
+#define Couette_Flow
+#define ENERGY
+#define D2Q9
+#define Re REF_RE
+static const int Nx = 2;
+static const int Ny = REF_NY;
+static const int Nz = 2;
+static const double tau = 0.9;
+static const double nu = cs2 * (tau - 0.5);
+static const double u_wall = Re * nu / (Ny + 1);
+static const double u_max = u_wall;
+static double uwall_topx = u_wall;
+static double uwall_botx = 0;
+#define Velocity_Ratio
+#define Temperature_Ratio
+static const double Pr = 0.7;
+static const double Br = 10;
+static const double Ec = Br / Pr;
+static const double alpha = nu / Pr;
+static const double tau_g = 0.5 + alpha / (cs2 * dx);
+static const double k = cs2 * tau_g * dx;
+static const double cp = k / (rho0 * alpha);
+static const double Tb = 0.5;
+static const double dT = pow(u_wall, 2) / (cp * Ec);
+static const double Tt = Tb + dT;
+static const double j_dot_n = 0;
+static const double D = 1;
+#define T_OUT 30000
+#define Nt 10
 #elif defined REF_SPHERE
 #define Sphere_BB
 #define MOMENTUM_EXCHANGE_ALGORITHM
@@ -147,5 +180,5 @@ static const double tau = 0.5 * dt + nu / cs2;
 #define T_OUT 30000
 #define Nt 10
 #else
-#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE or REF_SPHERE"
+#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE, REF_COUETTE or REF_SPHERE"
 #endif

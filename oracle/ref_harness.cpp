@@ -36,6 +36,13 @@ static void dump_field(LBM &lb, FILE *fp, int which) {
                 case 4: v = c.F[0]; break;
                 case 5: v = c.F[1]; break;
                 case 6: v = c.F[2]; break;
+#if defined ENERGY
+                // 50: T; 51..53: heat flux q
+                case 50: v = c.T; break;
+                case 51: v = c.q[0]; break;
+                case 52: v = c.q[1]; break;
+                case 53: v = c.q[2]; break;
+#endif
 #if defined MORE_DETAILS
                 // 7: pressure; 8..16: sigma[a][b]; 17..19: avg_velocity;
                 // 20: avg_pressure; 21..29: avg_ReynoldStress; 30..32:
@@ -142,6 +149,22 @@ int main(int argc, char **argv) {
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cylinder2d\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
+#elif defined REF_COUETTE
+    LBM lb = main_setup_Couette();
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int s = 1; s <= steps; s++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+    for (int w = 50; w <= 53; w++) dump_field(lb, fp, w);
+    fclose(fp);
+    printf("{\"case\": \"couette_energy\", \"ny\": %d, \"steps\": %d, \"seconds\": %.6f}\n", Ny, steps, t1 - t0);
 #elif defined REF_SPHERE
     LBM lb = main_setup_Sphere();
     std::vector<double> CL, CD;

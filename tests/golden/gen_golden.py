@@ -28,6 +28,11 @@ outputs are stored as small .npz fixtures:
                                     across the stream
                                     (Cylinder_Transverse_Oscillation, A = 2,
                                     f = 0.005, u = 0.05, Re = 100)
+  couette_energy_ny30_re20_2000.npz  D2Q9 Couette flow with the reference's
+                                    own thermal model (ENERGY), Ny = 30,
+                                    Re = 20, 2000 steps: rho, u, T and the
+                                    heat flux q on every row of the k = 1
+                                    layer, ghosts included
                                     These two keep Cl, Cd, the markers, and
                                     rho, u, F in the IBM box window
                                     i = 4..28, j = 8..32 of the k = 1 layer
@@ -89,7 +94,8 @@ def main() -> None:
     ap.add_argument("--skip-cav64", action="store_true")
     a = ap.parse_args()
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
-                     "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005")
+                     "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
+                     "couette:30:20")
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -162,6 +168,14 @@ def main() -> None:
                         sigma=sym["sigma"], avg_u=f[14:17], avg_p=f[17], avg_rs=sym["avg_rs"], rms_u=f[27:30],
                         rms_p=f[30], rms_rs=sym["rms_rs"], n=8, tau=0.8, lid=0.05, steps=200, nt=10,
                         **{"vtk_" + k: a for k, a in v.items()})
+    # ENERGY Couette flow, 2000 steps: every k layer evolves alike (cz = 0)
+    p = os.path.join(tmp, "couette.bin")
+    run("ref_couette_30_20", ["2000", p])
+    f = oracle.read_ref_dump(p, 4, 32, 4, 8)["fields"]
+    for k in range(4):
+        assert np.array_equal(f[:, k], f[:, 1])
+    np.savez_compressed(os.path.join(OUT, "couette_energy_ny30_re20_2000.npz"), rho=f[0, 1], u=f[1:4, 1],
+                        T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=2000)
     print("golden fixtures written to", OUT)
 
 

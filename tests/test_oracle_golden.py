@@ -163,3 +163,27 @@ def test_cylinder2d_variants_match_reference(orc, case):
     f = np.stack([lat.rho[1], lat.ux[1], lat.uy[1], lat.Fx[1], lat.Fy[1]])
     assert np.abs(f[:, 8:33, 4:29] - g["window"]).max() < 1e-12
     assert np.allclose(f.reshape(5, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
+
+
+def test_energy_couette_matches_reference(orc):
+    """The reference's ENERGY model (LBM.h:58) on its Couette case, D2Q9:
+    temperature populations on the flow lattice with the cubic equilibrium
+    (lbm.cpp:636-653), viscous heating with the F_vis history term
+    (lbm.cpp:121-177), anti-bounce-back Dirichlet walls (lbm.cpp:277-280),
+    T and q summed on every cell (lbm.cpp:776-792).  Summed in the
+    reference's order: bit-exact after 2000 steps, ghosts included."""
+    g = np.load(os.path.join(GOLDEN, "couette_energy_ny30_re20_2000.npz"))
+    lat, c = orc.couette_energy(int(g["ny"]), float(g["Re"]))
+    assert lat.step_plain(int(g["steps"])) == 0
+    assert np.array_equal(lat.rho[1], g["rho"])
+    assert np.array_equal(np.stack([lat.ux[1], lat.uy[1], lat.uz[1]]), g["u"])
+    assert np.array_equal(lat.T[1], g["T"])
+    assert np.array_equal(lat.hq[:, 1], g["q"])
+    # the walls' temperature: Determine_Wall_Temperature's periodic neighbour
+    # search (lbm.cpp:965-981) wraps each wall row onto the other, so both
+    # ghost rows hold the mean of Tb and Tt from Init on (their g are never
+    # streamed)
+    mid = 0.5 * (c["Tb"] + c["Tt"])
+    assert abs(g["T"][0, 1] - mid) < 1e-12 and abs(g["T"][-1, 1] - mid) < 1e-12
+    # viscous heating lifts the centre above both walls
+    assert g["T"][16, 1] > mid + 1e-4
