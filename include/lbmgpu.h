@@ -69,7 +69,8 @@ enum {
     LBM_STATUS_RHO_RANGE = 1,   /* rho outside (0, 100) or NaN: lbm.cpp:772-775 */
     LBM_STATUS_BAND_EDGE = 2,   /* an IBM stencil reached outside the band/interior */
     LBM_STATUS_NONFINITE_FORCE = 4,
-    LBM_STATUS_TIMEOUT = 16     /* a bounded device wait (mbarrier, grid barrier) gave up */
+    LBM_STATUS_TIMEOUT = 16,    /* a bounded device wait (mbarrier, grid barrier) gave up */
+    LBM_STATUS_T_RANGE = 32     /* ENERGY: T outside (0, 100) or NaN: lbm.cpp:794-797 */
 };
 
 typedef struct lbm_face {
@@ -104,7 +105,16 @@ typedef struct lbm_config {
                              x-crossing links; <0: their whole warp takes the boundary-class path */
     int lattice;          /* LBM_LATTICE_*: 0 or 19 = D3Q19; 9 = D2Q9 (the reference's #define D2Q9
                              build; nz = 1, faces 4/5 unused) */
+    double cp;            /* thermal == LBM_THERMAL_ENERGY: specific heat capacity of the viscous-heating
+                             source Phi / cp (LBM.h:213) */
 } lbm_config;
+
+/* lbm_config.thermal: 0 none; 1 a D3Q7 temperature population with a heat
+ * source and Boussinesq buoyancy (D3Q19 handles); 2 the reference's own
+ * ENERGY model (LBM.h:58): temperature populations on the flow lattice with
+ * the cubic equilibrium, viscous heating and anti-bounce-back Dirichlet walls
+ * (D2Q9 handles; faces periodic or Dirichlet walls). */
+enum { LBM_THERMAL_NONE = 0, LBM_THERMAL_D3Q7 = 1, LBM_THERMAL_ENERGY = 2 };
 
 enum { LBM_LATTICE_D3Q19 = 19, LBM_LATTICE_D2Q9 = 9 };
 
@@ -160,6 +170,18 @@ lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const ui
  * has lattice = LBM_LATTICE_D2Q9 and nz = 1. */
 lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, const uint8_t *types, const double *rho,
                                        const double *ux, const double *uy, lbm_config *out);
+
+/* Adds the reference's ENERGY model to a D2Q9 configuration made by
+ * lbmgpu_config_from_types_2d from the same (nx+2)(ny+2) arrays: the
+ * type_Energy of the ghost cells (TYPE_T = 6 on every wall cell: Dirichlet,
+ * lbm.cpp:277-280) and the set-up temperature T, ghosts included (uniform on
+ * each wall face and over the fluid).  tau_g and cp are LBM.h's
+ * tau_g = 0.5 + alpha / cs2 and cp = k / (rho0 alpha).  Replaces the
+ * LATTICE::type_Energy / T set-up of main_setup_Couette (lbm.cpp:1552-1572).
+ * Fails with LBM_ERR_UNSUPPORTED for Neumann (TYPE_Q) or adiabatic walls,
+ * inlet/outlet faces, or a non-uniform set-up. */
+lbm_status lbmgpu_config_energy_2d(lbm_config *cfg, int nx, int ny, const uint8_t *types, const uint8_t *types_energy,
+                                   const double *T, double tau_g, double cp);
 
 lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out);
 lbm_status lbmgpu_destroy(lbm_handle *h);

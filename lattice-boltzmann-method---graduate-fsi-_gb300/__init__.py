@@ -29,10 +29,13 @@ LATTICE_D3Q19, LATTICE_D2Q9 = 19, 9
 MOTION_FIXED, MOTION_CONSTANT, MOTION_INLINE_OSC, MOTION_TRANSVERSE_OSC = 0, 1, 2, 3
 TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
 FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
+FIELD_QX, FIELD_QY, FIELD_QZ = 5, 6, 7
+# lbm_config.thermal: none, D3Q7 (D3Q19 handles), the reference's ENERGY model (D2Q9 handles)
+THERMAL_NONE, THERMAL_D3Q7, THERMAL_ENERGY = 0, 1, 2
 # MORE_DETAILS: the six distinct stress components, and the statistics rows
 SYM6 = ((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))
 STAT_AVG_U, STAT_AVG_P, STAT_AVG_RS, STAT_RMS_U, STAT_RMS_P, STAT_RMS_RS, STAT_COUNT = 0, 3, 4, 10, 13, 14, 20
-STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE, STATUS_TIMEOUT = 1, 2, 4, 16
+STATUS_RHO_RANGE, STATUS_BAND_EDGE, STATUS_NONFINITE_FORCE, STATUS_TIMEOUT, STATUS_T_RANGE = 1, 2, 4, 16, 32
 
 # Every symbol include/lbmgpu.h declares.
 ABI_SYMBOLS = [
@@ -48,6 +51,7 @@ ABI_SYMBOLS = [
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
+    "lbmgpu_config_energy_2d",
 ]
 
 
@@ -63,7 +67,7 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("xface", C.c_int), ("lattice", C.c_int)]
+                ("xface", C.c_int), ("lattice", C.c_int), ("cp", C.c_double)]
 
 
 class IbmConfig(C.Structure):
@@ -161,6 +165,8 @@ def load(path: str | None = None):
     L.lbmgpu_output_avg_vtk.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
     L.lbmgpu_config_from_types_2d.argtypes = [i, i, d, C.POINTER(C.c_uint8), dp, dp, dp, C.POINTER(Config)]
     L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
+    L.lbmgpu_config_energy_2d.argtypes = [C.POINTER(Config), i, i, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), dp, d,
+                                          d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
     L.lbmgpu_batch_step_noalloc.argtypes = [i, C.POINTER(C.c_int), dp, d, i, vp, vp, i, i, C.POINTER(C.c_uint32), vp]
     L.lbmgpu_serve_run.argtypes = [C.POINTER(ServeRequest), i, C.POINTER(ServeOptions), C.POINTER(ServeResult), dp]
@@ -479,6 +485,19 @@ def config_from_types_2d(nx, ny, tau, types, rho=None, ux=None, uy=None) -> Conf
     ptrs = [None if a is None else _dp(a) for a in arrs]
     cfg = Config()
     check(L.lbmgpu_config_from_types_2d(nx, ny, tau, t.ctypes.data_as(C.POINTER(C.c_uint8)), *ptrs, C.byref(cfg)))
+    return cfg
+
+
+def config_energy_2d(cfg: Config, nx, ny, types, types_energy, T, tau_g, cp) -> Config:
+    """Add the reference's ENERGY model to a D2Q9 Config made from the same
+    (ny+2, nx+2) arrays: type_Energy (TYPE_T = 6 on the walls), the set-up T
+    (ghosts included), tau_g and cp (LBM.h:206-214)."""
+    L = load()
+    t = np.ascontiguousarray(types, dtype=np.uint8).ravel()
+    te = np.ascontiguousarray(types_energy, dtype=np.uint8).ravel()
+    Ta = np.ascontiguousarray(T, dtype=np.float64).ravel()
+    check(L.lbmgpu_config_energy_2d(C.byref(cfg), nx, ny, t.ctypes.data_as(C.POINTER(C.c_uint8)),
+                                    te.ctypes.data_as(C.POINTER(C.c_uint8)), _dp(Ta), tau_g, cp))
     return cfg
 
 

@@ -19,8 +19,8 @@
 //   - Collision() + Streaming() run one fused step on the device (Collision
 //     only records that a collision is pending); MacroProp() is fused into
 //     the step and here only marks the host mirror stale;
-//   - sync_to_host() fills fluid[..].density/ux/uy/uz (and T) with the
-//     MacroProp moments before output code reads them;
+//   - sync_to_host() fills fluid[..].density/ux/uy/uz (and T; with ENERGY
+//     also q) with the MacroProp moments before output code reads them;
 //   - IBLBM registers the markers with the device on its first call; the
 //     forcing runs inside the next step and Cl/Cd are appended after it.
 // Compile-time choices of the reference (#define D3Q19, IBM scheme, m_max,
@@ -80,6 +80,9 @@ struct lbm_options {
     double body_radius = 0.0;     // IBM body radius (0: from the marker cloud)
     int thermal = 0;              // D3Q7 temperature population
     double tau_g = 0.0, T_ref = 0.0, gbeta[3] = {0, 0, 0};
+    // ENERGY builds (-DENERGY, D2Q9): LBM.h's cp = k / (rho0 alpha) of the
+    // viscous-heating source; tau_g above is its tau_g = 0.5 + alpha / cs2
+    double cp = 0.0;
     int Nt = 10;                  // output cadence (LBM.h:493-496): Sup_MacroProp's told = (n - Nt) dt
     // the reference's global centre (center_x, center_y, 1): IBLBM's box is
     // [centre - D, centre + D] (lbm.cpp:1165-1166); unset, the marker centroid
@@ -106,6 +109,14 @@ class LATTICE {
     double F[3] = {0, 0, 0};
     double Fm[3] = {0, 0, 0};
     double T = 0.0;
+#if defined ENERGY
+    // LBM.h:590-596: the energy equation's populations stay on the device;
+    // q (the heat flux sum g c) reaches the mirror with sync_to_host
+    double g[npop], g_star[npop];
+    double q[3] = {0, 0, 0};
+    short type_Energy = TYPE_F;
+    double F_vis[npop];
+#endif
 #if defined MORE_DETAILS
     // LBM.h:572-588; vorticity and its statistics stay zero, as in the
     // reference (whose vorticity code is commented out)

@@ -10,9 +10,11 @@ import subprocess
 HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
-DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details", "dropin_cylinder2d"]
+DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details", "dropin_cylinder2d",
+           "dropin_couette"]
 # compile-time switches of the reference a driver is built with
-DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"], "dropin_cylinder2d": ["-DD2Q9"]}
+DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"], "dropin_cylinder2d": ["-DD2Q9"],
+                "dropin_couette": ["-DD2Q9", "-DENERGY"]}
 
 
 def build(force: bool = False) -> list:

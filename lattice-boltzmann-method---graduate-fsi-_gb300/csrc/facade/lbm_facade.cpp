@@ -138,6 +138,20 @@ void LBM::Init() {
     cfg.tau_g = o.tau_g;
     cfg.T_ref = o.T_ref;
     for (int a = 0; a < 3; a++) cfg.gbeta[a] = o.gbeta[a];
+#if defined ENERGY && defined D2Q9
+    // the energy set-up of main_setup_Couette (lbm.cpp:1552-1572):
+    // type_Energy and T of the computational layer
+    {
+        const size_t layer = (size_t)NX * NY;
+        std::vector<uint8_t> te((size_t)NX * NY);
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++) te[(size_t)i + (size_t)NX * j] = (uint8_t)fluid[i][j][1].type_Energy;
+        check("config_energy_2d", lbmgpu_config_energy_2d(&cfg, Nx, Ny, types.data() + layer, te.data(),
+                                                          T.data() + layer, o.tau_g, o.cp));
+    }
+#elif defined ENERGY
+#error "the ENERGY model runs on D2Q9 builds (-DD2Q9)"
+#endif
     const int dims[3] = {Nx, Ny, Nz};
     const int ddims[3] = {cfg.nx, cfg.ny, cfg.nz};
     for (int a = 0; a < 3; a++) {
@@ -227,7 +241,14 @@ void LBM::MacroProp() { dev->mirror_stale = true; }
 void LBM::sync_to_host() {
     if (!dev->h) return;
     const size_t nd = (size_t)dev->dn[0] * dev->dn[1] * dev->dn[2];
+#if defined ENERGY
+    const int nf = 5;
+    std::vector<float> qx(nd), qy(nd);
+    check("download", lbmgpu_download_f32(dev->h, LBM_FIELD_QX, qx.data()));
+    check("download", lbmgpu_download_f32(dev->h, LBM_FIELD_QY, qy.data()));
+#else
     const int nf = g_lbm_options.thermal ? 5 : 4;
+#endif
     std::vector<float> buf(nf * nd);
     check("download", lbmgpu_download_all_f32(dev->h, buf.data()));
     for (int z = 0; z < dev->dn[2]; z++)
@@ -240,6 +261,11 @@ void LBM::sync_to_host() {
                 c.uy = buf[2 * nd + id];
                 c.uz = buf[3 * nd + id];
                 if (nf == 5) c.T = buf[4 * nd + id];
+#if defined ENERGY
+                c.q[0] = qx[id];
+                c.q[1] = qy[id];
+                c.q[2] = 0.0;
+#endif
             }
 #if defined MORE_DETAILS
     std::vector<float> det(LBM_DETAIL_COUNT * nd);

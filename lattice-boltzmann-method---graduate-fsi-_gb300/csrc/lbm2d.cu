@@ -164,6 +164,163 @@ __global__ void k_init2d(T *__restrict__ A, long long N, long long S, const floa
 }
 
 // ---------------------------------------------------------------------------
+// ENERGY: temperature populations on the flow lattice (LBM.h:58)
+// ---------------------------------------------------------------------------
+// The cubic equilibrium polynomial of Calc_feq / Calc_geq (lbm.cpp:636-653)
+// minus one, cs^2 = 1/3.
+__device__ __forceinline__ float poly9(float cu, float usq) {
+    return 3.0f * cu + 4.5f * cu * cu - 1.5f * usq + 4.5f * cu * cu * cu - 4.5f * cu * usq;
+}
+
+// One fused step of f and g.  Streaming (lbm.cpp:263-280): g follows f
+// into fluid cells; a link from a Dirichlet wall takes
+// -g*_opp(l) + 2 geq_opp(l)(rho, T_w, u_w) of the cell itself, rho of the
+// previous MacroProp.  MacroProp (lbm.cpp:668-792): rho, u, T = sum g and
+// q = sum g c.  ConvLBM (lbm.cpp:91-177): f by BGK + Guo; g by BGK with the
+// viscous-heating source F_l = w_l Phi / cp (1 + c_l.u (tau_g - 1/2) /
+// (cs2 tau_g)) plus half its change since the previous collision, where
+// Phi = 2 nu rho S:S and S = -sum c c (f - feq) / (2 rho tau cs2).
+// aux [4][N] keeps what the previous collision used, per cell: rho - 1, u
+// and Phi (the reference's F_vis history, F_vis = 0 before the first one).
+// ENERGY handles keep f and g in FP32: with geq = rho w T (lbm.cpp:646-650)
+// and T = sum g, each collision scales T by 1 + (rho - 1) / tau_g, so T
+// integrates any error of rho -- with FP16 f the Couette run's T drifted by
+// several times its viscous-heating signal in 2000 steps.
+template <class T, bool FORCED>
+__global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__restrict__ B,
+                                                  const float *__restrict__ GA, float *__restrict__ GB,
+                                                  const __grid_constant__ Params2 P,
+                                                  const __grid_constant__ Energy2 E, State2 *__restrict__ ds,
+                                                  float *__restrict__ aux, float *__restrict__ mom, int gather,
+                                                  int first, int export_only) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.nx || y >= P.ny) return;
+    const long long cell = x + (long long)P.nx * y;
+    float f[Q9], g[Q9];
+    const bool face = x == 0 || x == P.nx - 1 || y == 0 || y == P.ny - 1;
+    const float drho_p = aux[cell];
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q9; l++) {
+            f[l] = St<T>::ld(A + l * P.S + cell);
+            g[l] = GA[l * P.S + cell];
+        }
+    } else if (!face) {
+#pragma unroll
+        for (int l = 0; l < Q9; l++) {
+            f[l] = St<T>::ld(A + l * P.S + cell + P.pofs[l]);
+            g[l] = GA[l * P.S + cell + P.pofs[l]];
+        }
+    } else {
+        int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
+        raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
+        const Class2 &ce = P.cls[raw];
+        const int k = first ? 0 : 1;
+        const float tw = E.tw[raw][k], dtw = E.dtw[raw][k];
+#pragma unroll
+        for (int l = 0; l < Q9; l++) {
+            f[l] = pull_link2<T>(A, l, x, y, cell, ce, P);
+            if ((E.dir[raw] >> l) & 1u) {
+                // 2 geq - 2 w T_ref = 2 w (rho T_w (1 + pm1) - T_ref)
+                const float wall = 2.0f * w9f(l) * (dtw + drho_p * tw + (1.0f + drho_p) * tw * E.pm1[raw][l]);
+                g[l] = wall - GA[opp9(l) * P.S + cell];
+            } else {
+                // a periodic or interior source (the only other links of an
+                // ENERGY handle)
+                g[l] = pull_link2<float>(GA, l, x, y, cell, ce, P);
+            }
+        }
+    }
+    float drho = 0.0f, jx = 0.0f, jy = 0.0f, dT = 0.0f, qx = 0.0f, qy = 0.0f;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        drho += f[l];
+        jx += (float)cx9(l) * f[l];
+        jy += (float)cy9(l) * f[l];
+        dT += g[l];
+        qx += (float)cx9(l) * g[l];
+        qy += (float)cy9(l) * g[l];
+    }
+    // before the first MacroProp the collision takes the set-up T (uniform,
+    // the shift T_ref)
+    if (!gather) dT = 0.0f;
+    const float Fx = FORCED ? P.body[0] : 0.0f, Fy = FORCED ? P.body[1] : 0.0f;
+    const float rho = 1.0f + drho;
+    const float inv = 1.0f / rho;
+    const float hf = gather ? 0.5f : 0.0f;
+    const float ux = (jx + hf * Fx) * inv, uy = (jy + hf * Fy) * inv;
+    const float Tc = E.T_ref + dT;
+    if (!(rho > 0.0f && rho < 100.0f)) atomicOr(&ds->status, lbmk::ST_RHO_RANGE);
+    if (!(Tc > 0.0f && Tc < 100.0f)) atomicOr(&ds->status, lbmk::ST_T_RANGE);
+    if (mom != nullptr) {
+        mom[cell] = rho;
+        mom[P.N + cell] = ux;
+        mom[2 * P.N + cell] = uy;
+        mom[3 * P.N + cell] = Tc;
+        mom[4 * P.N + cell] = qx;  // sum g c: the shift w T_ref carries no momentum
+        mom[5 * P.N + cell] = qy;
+    }
+    if (export_only) return;
+    const float usq = ux * ux + uy * uy;
+    float sxx = 0.0f, sxy = 0.0f, syy = 0.0f;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
+        const float fne = f[l] - w9f(l) * (drho + rho * poly9(cu, usq));
+        sxx += (float)(cx9(l) * cx9(l)) * fne;
+        sxy += (float)(cx9(l) * cy9(l)) * fne;
+        syy += (float)(cy9(l) * cy9(l)) * fne;
+    }
+    const float sk = E.s_fac * inv;
+    sxx *= sk;
+    sxy *= sk;
+    syy *= sk;
+    const float phi = E.two_nu * rho * (sxx * sxx + 2.0f * sxy * sxy + syy * syy);
+    const float uxp = aux[P.N + cell], uyp = aux[2 * P.N + cell], phip = aux[3 * P.N + cell];
+    collide9(f, drho, ux, uy, Fx, Fy, P.omega, FORCED);
+    const float a = phi * E.inv_cp, ap = phip * E.inv_cp;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
+        const float cup = (float)cx9(l) * uxp + (float)cy9(l) * uyp;
+        const float Fl = w9f(l) * a * (1.0f + cu * E.tg_fac);
+        const float Fb = w9f(l) * ap * (1.0f + cup * E.tg_fac);
+        const float geq_s = w9f(l) * (dT + drho * Tc + rho * Tc * poly9(cu, usq));
+        g[l] = g[l] - (g[l] - geq_s) * E.inv_tau_g + Fl + 0.5f * (Fl - Fb);
+    }
+    aux[cell] = drho;
+    aux[P.N + cell] = ux;
+    aux[2 * P.N + cell] = uy;
+    aux[3 * P.N + cell] = phi;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        St<T>::st(B + l * P.S + cell, f[l]);
+        GB[l * P.S + cell] = g[l];
+    }
+}
+
+// g = geq(rho, u, T0) (LBM::Init, lbm.cpp:44-49), shifted by w T0 with T0
+// the uniform set-up T; aux = (rho - 1, u, Phi = 0).
+__global__ void k_init_energy2d(float *__restrict__ G, float *__restrict__ aux, long long N, long long S,
+                                const float *__restrict__ fields, float rho0, float ux0, float uy0, float T0) {
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= N) return;
+    const float rho = fields ? fields[c] : rho0;
+    const float ux = fields ? fields[N + c] : ux0, uy = fields ? fields[2 * N + c] : uy0;
+    const float usq = ux * ux + uy * uy;
+#pragma unroll
+    for (int l = 0; l < Q9; l++) {
+        const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
+        G[l * S + c] = w9f(l) * ((rho - 1.0f) * T0 + rho * T0 * poly9(cu, usq));
+    }
+    aux[c] = rho - 1.0f;
+    aux[N + c] = ux;
+    aux[2 * N + c] = uy;
+    aux[3 * N + c] = 0.0f;
+}
+
+// ---------------------------------------------------------------------------
 // Immersed boundary
 // ---------------------------------------------------------------------------
 struct Ibm2 {
@@ -820,6 +977,11 @@ struct lbm2d {
     cudaGraphExec_t gexec = nullptr;
     int gsteps = 16;
     int tx = 128, ty = 2;
+    // ENERGY: g ping-pong, per-cell history of the last collision
+    bool energy = false;
+    Energy2 E;
+    float *g[2] = {nullptr, nullptr};
+    float *aux = nullptr;
     std::vector<void *> allocs;
 };
 
@@ -869,7 +1031,7 @@ int face_priority2(int kind) {
 // ghost faces takes the highest-priority kind; a cell's wall velocity is the
 // mean over its moving wall neighbours, Determine_Wall_Velocity,
 // lbm.cpp:941-962).
-void build_classes2(const lbm_config &c, Params2 &P) {
+void build_classes2(const lbm_config &c, Params2 &P, double uwall_out[16][2] = nullptr) {
     for (int cls = 0; cls < 16; cls++) {
         Class2 e;
         memset(&e, 0, sizeof(e));
@@ -923,6 +1085,10 @@ void build_classes2(const lbm_config &c, Params2 &P) {
             uwall[0] /= num;
             uwall[1] /= num;
         }
+        if (uwall_out) {
+            uwall_out[cls][0] = uwall[0];
+            uwall_out[cls][1] = uwall[1];
+        }
         for (int l = 0; l < Q9; l++) {
             int fs[2];
             const int k = crossed(-cx9(l), -cy9(l), fs);
@@ -945,8 +1111,99 @@ void build_classes2(const lbm_config &c, Params2 &P) {
     }
 }
 
+// The ENERGY tables.  The wall temperature of Determine_Wall_Temperature
+// (lbm.cpp:965-981) is the mean T of a cell's solid neighbours, taken with
+// the periodic modulo over the whole ghost-inclusive grid; it is evaluated on
+// that grid for one cell of each boundary class.  Before the first MacroProp
+// the walls hold their set-up T; after it, the sum of their initial g (never
+// streamed): the mean set-up T of their own solid neighbours, which for a
+// wall row wraps onto the opposite wall row.  Corner ghost cells take the T
+// of their y face.
+void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16][2], Energy2 &E) {
+    const double cs2 = 1.0 / 3.0, tg = c.tau_g;
+    memset(&E, 0, sizeof(E));
+    E.inv_tau_g = (float)(1.0 / tg);
+    E.tg_fac = (float)((tg - 0.5) / (cs2 * tg));
+    E.inv_cp = (float)(1.0 / c.cp);
+    E.two_nu = (float)(2.0 * cs2 * (c.tau - 0.5));
+    E.s_fac = (float)(-1.0 / (2.0 * c.tau * cs2));
+    E.T_ref = (float)c.T_init;
+    const int gx = (P.periodic & 1) ? 0 : 1, gy = (P.periodic & 2) ? 0 : 1;
+    const int RX = P.nx + 2 * gx, RY = P.ny + 2 * gy;
+    std::vector<uint8_t> solid((size_t)RX * RY, 0);
+    std::vector<double> T0((size_t)RX * RY, c.T_init), T1((size_t)RX * RY, c.T_init);
+    auto at = [&](int i, int j) { return (size_t)i + (size_t)RX * j; };
+    for (int j = 0; j < RY; j++)
+        for (int i = 0; i < RX; i++) {
+            int f = -1;
+            if (gy && j == 0) f = 2;
+            else if (gy && j == RY - 1) f = 3;
+            else if (gx && i == 0) f = 0;
+            else if (gx && i == RX - 1) f = 1;
+            if (f >= 0) {
+                solid[at(i, j)] = 1;
+                T0[at(i, j)] = c.faces[f].T;
+            }
+        }
+    auto mean_solid = [&](const std::vector<double> &Tf, int i, int j) {
+        int num = 0;
+        double sum = 0.0;
+        for (int l = 0; l < Q9; l++) {
+            const int in = (i + cx9(l) + RX) % RX, jn = (j + cy9(l) + RY) % RY;
+            if (solid[at(in, jn)]) {
+                sum += Tf[at(in, jn)];
+                num++;
+            }
+        }
+        return num ? sum / num : 0.0;
+    };
+    for (int j = 0; j < RY; j++)
+        for (int i = 0; i < RX; i++)
+            if (solid[at(i, j)]) T1[at(i, j)] = mean_solid(T0, i, j);
+    for (int cls = 0; cls < 16; cls++) {
+        const int x = (cls & 1) ? 0 : ((cls & 2) ? P.nx - 1 : P.nx / 2);
+        const int y = (cls & 4) ? 0 : ((cls & 8) ? P.ny - 1 : P.ny / 2);
+        const double t0 = mean_solid(T0, x + gx, y + gy), t1 = mean_solid(T1, x + gx, y + gy);
+        E.tw[cls][0] = (float)t0;
+        E.tw[cls][1] = (float)t1;
+        E.dtw[cls][0] = (float)(t0 - c.T_init);
+        E.dtw[cls][1] = (float)(t1 - c.T_init);
+        E.dir[cls] = P.cls[cls].bb;
+        const double uwx = uwall[cls][0], uwy = uwall[cls][1], usq = uwx * uwx + uwy * uwy;
+        for (int l = 0; l < Q9; l++) {
+            // geq of the outgoing direction opp(l) (lbm.cpp:277-279)
+            const double cu = -(cx9(l) * uwx + cy9(l) * uwy);
+            E.pm1[cls][l] = (float)(cu / cs2 + cu * cu / (2 * cs2 * cs2) - usq / (2 * cs2) +
+                                    cu * cu * cu / (6 * cs2 * cs2 * cs2) - cu * usq / (2 * cs2 * cs2));
+        }
+    }
+}
+
+cudaError_t launch_energy2d(lbm_handle *h, int gather, float *mom, int export_only) {
+    lbm2d *d = h->d2;
+    const dim3 block(d->tx, d->ty);
+    const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
+    const void *A = d->f[d->cur];
+    void *B = d->f[1 - d->cur];
+    const float *GA = d->g[d->cur];
+    float *GB = d->g[1 - d->cur];
+    const int first = gather && h->steps == 1 ? 1 : 0;
+    const bool forced = d->P.forced != 0;
+#define L2D_ENERGY(T)                                                                                           \
+    if (forced)                                                                                               \
+        k_energy2d<T, true><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, GA, GB, d->P, d->E,                 \
+                                                     d->st, d->aux, mom, gather, first, export_only);          \
+    else                                                                                                      \
+        k_energy2d<T, false><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, GA, GB, d->P,                      \
+                                                      d->E, d->st, d->aux, mom, gather, first, export_only);
+    L2D_ENERGY(float)
+#undef L2D_ENERGY
+    return cudaGetLastError();
+}
+
 cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only) {
     lbm2d *d = h->d2;
+    if (d->energy) return launch_energy2d(h, gather, mom, export_only);
     const dim3 block(d->tx, d->ty);
     const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
     const void *A = d->f[d->cur];
@@ -1026,7 +1283,23 @@ cudaError_t enqueue_step2d(lbm_handle *h) {
 lbm_status l2d_create(lbm_handle *h) {
     const lbm_config &c = h->cfg;
     if (c.nz != 1) return f2(LBM_ERR_INVALID, "create: a D2Q9 configuration has nz = 1");
-    if (c.thermal) return f2(LBM_ERR_UNSUPPORTED, "create: no thermal population on D2Q9 handles");
+    if (c.thermal != LBM_THERMAL_NONE && c.thermal != LBM_THERMAL_ENERGY)
+        return f2(LBM_ERR_UNSUPPORTED, "create: D2Q9 handles take the ENERGY model (thermal = 2), not D3Q7");
+    if (c.thermal == LBM_THERMAL_ENERGY) {
+        if (!(c.cp > 0)) return f2(LBM_ERR_INVALID, "create: ENERGY needs cp > 0");
+        if (c.storage != LBM_STORE_F32)
+            return f2(LBM_ERR_UNSUPPORTED, "create: ENERGY handles store f in FP32 (T = sum g integrates every "
+                                           "error of rho through geq = rho w T)");
+        if (c.gbeta[0] != 0 || c.gbeta[1] != 0 || c.gbeta[2] != 0)
+            return f2(LBM_ERR_UNSUPPORTED, "create: no buoyancy on ENERGY handles");
+        for (int f = 0; f < 4; f++) {
+            const lbm_face &F = c.faces[f];
+            if (F.kind == LBM_FACE_PERIODIC) continue;
+            if (F.kind != LBM_FACE_WALL || F.thermal_kind != LBM_TWALL_DIRICHLET)
+                return f2(LBM_ERR_UNSUPPORTED, "create: ENERGY faces are periodic or Dirichlet walls (face " +
+                                                   std::to_string(f) + ")");
+        }
+    }
     for (int a = 0; a < 2; a++) {
         const bool p0 = c.faces[2 * a].kind == LBM_FACE_PERIODIC, p1 = c.faces[2 * a + 1].kind == LBM_FACE_PERIODIC;
         if (p0 != p1) return f2(LBM_ERR_INVALID, "create: a periodic axis needs both faces periodic");
@@ -1046,7 +1319,10 @@ lbm_status l2d_create(lbm_handle *h) {
     for (int a = 0; a < 2; a++)
         if (c.faces[2 * a].kind == LBM_FACE_PERIODIC) P.periodic |= 1 << a;
     for (int l = 0; l < Q9; l++) P.pofs[l] = -(cx9(l) + c.nx * cy9(l));
-    build_classes2(c, P);
+    double uwall[16][2];
+    build_classes2(c, P, uwall);
+    d->energy = c.thermal == LBM_THERMAL_ENERGY;
+    if (d->energy) build_energy2(c, P, uwall, d->E);
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
     if (c.graph_steps > 0) d->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) d->gsteps = 0;
@@ -1054,7 +1330,12 @@ lbm_status l2d_create(lbm_handle *h) {
     d->ty = c.block_y > 0 ? c.block_y : std::max(1, 256 / d->tx);
     CK2(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking));
     for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->f[i], (size_t)Q9 * P.S * h->esize));
-    CK2(alloc2(h, &d->mom, (size_t)3 * P.N * sizeof(float)));
+    if (d->energy) {
+        for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->g[i], (size_t)Q9 * P.S * sizeof(float)));
+        CK2(alloc2(h, &d->aux, (size_t)4 * P.N * sizeof(float)));
+    }
+    // moments: rho, ux, uy (ENERGY: and T, qx, qy)
+    CK2(alloc2(h, &d->mom, (size_t)(d->energy ? 6 : 3) * P.N * sizeof(float)));
     CK2(alloc2(h, &d->st, sizeof(State2)));
     CK2(alloc2(h, &d->hist, (size_t)d->hist_cap * 4 * sizeof(double)));
     State2 s0;
@@ -1102,6 +1383,10 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
     default: k_init2d<float><<<blocks, thr, 0, h->s>>>((float *)d->f[0], N, d->P.S, dfields, r0, u0, v0); break;
     }
     CK2(cudaGetLastError());
+    if (d->energy) {
+        k_init_energy2d<<<blocks, thr, 0, h->s>>>(d->g[0], d->aux, N, d->P.S, dfields, r0, u0, v0, d->E.T_ref);
+        CK2(cudaGetLastError());
+    }
     CK2(cudaStreamSynchronize(h->s));
     d->cur = 0;
     h->steps = 0;
@@ -1116,6 +1401,7 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
 lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *dsw) {
     lbm2d *d = h->d2;
     if (d->ibm) return f2(LBM_ERR_STATE, "set_markers: markers already set");
+    if (d->energy) return f2(LBM_ERR_UNSUPPORTED, "set_markers: no immersed body on ENERGY handles");
     if (h->steps > 0) return f2(LBM_ERR_STATE, "set_markers: call before the first step");
     const int n = ic->n_markers;
     if (n < 1 || !xyz || !dsw) return f2(LBM_ERR_INVALID, "set_markers: bad markers");
@@ -1225,7 +1511,9 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
     int left = nsteps;
     // the first step (no gather) and odd remainders run eagerly; whole
     // graphs of gsteps (even: the buffers return to the same parity) replay
-    while (left > 0 && h->steps == 0) {
+    // (ENERGY: also the second, whose streaming takes the set-up wall T)
+    const long long eager = d->energy ? 2 : 1;
+    while (left > 0 && h->steps < eager) {
         CK2(enqueue_step2d(h));
         left--;
     }
@@ -1268,15 +1556,17 @@ lbm_status l2d_export(lbm_handle *h) {
 
 lbm_status l2d_download_f32(lbm_handle *h, int field, float *host) {
     lbm2d *d = h->d2;
-    if (field < 0 || field > 3) return f2(LBM_ERR_INVALID, "download: bad field for a D2Q9 handle");
+    if (field < 0 || field > (d->energy ? 7 : 3)) return f2(LBM_ERR_INVALID, "download: bad field for a D2Q9 handle");
     const size_t N = (size_t)d->P.N;
-    if (field == 3) {
+    if (field == 3 || field == 7) {
         memset(host, 0, N * sizeof(float));
         return LBM_OK;
     }
     lbm_status s = l2d_export(h);
     if (s != LBM_OK) return s;
-    CK2(cudaMemcpyAsync(host, d->mom + (size_t)field * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    // moment rows: rho, ux, uy (, T, qx, qy)
+    const size_t row = field < 3 ? (size_t)field : (size_t)field - 1;
+    CK2(cudaMemcpyAsync(host, d->mom + row * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
     CK2(cudaStreamSynchronize(h->s));
     return LBM_OK;
 }
@@ -1287,6 +1577,7 @@ lbm_status l2d_download_all_f32(lbm_handle *h, float *host) {
     lbm_status s = l2d_export(h);
     if (s != LBM_OK) return s;
     CK2(cudaMemcpyAsync(host, d->mom, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    if (d->energy) CK2(cudaMemcpyAsync(host + 4 * N, d->mom + 3 * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
     CK2(cudaStreamSynchronize(h->s));
     memset(host + 3 * N, 0, N * sizeof(float));
     return LBM_OK;
@@ -1400,5 +1691,54 @@ extern "C" lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, co
     c.ny = dims[1];
     c.nz = 1;
     *out = c;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_config_energy_2d(lbm_config *cfg, int nx, int ny, const uint8_t *types,
+                                              const uint8_t *types_energy, const double *T, double tau_g, double cp) {
+    if (!cfg || !types || !types_energy || !T || nx < 1 || ny < 1)
+        return f2(LBM_ERR_INVALID, "config_energy_2d: bad arguments");
+    if (cfg->lattice != LBM_LATTICE_D2Q9) return f2(LBM_ERR_INVALID, "config_energy_2d: not a D2Q9 configuration");
+    const int NX = nx + 2, NY = ny + 2;
+    auto at = [&](int i, int j) { return (size_t)i + (size_t)NX * j; };
+    // the fluid's set-up T (the periodic ghost layers included): uniform
+    bool have = false;
+    double Tf = 0.0;
+    for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++) {
+            if (types[at(i, j)] != 0) continue;
+            if (!have) {
+                Tf = T[at(i, j)];
+                have = true;
+            } else if (T[at(i, j)] != Tf) {
+                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: the fluid's set-up T is not uniform");
+            }
+        }
+    if (!have) return f2(LBM_ERR_INVALID, "config_energy_2d: no fluid cell");
+    for (int f = 0; f < 4; f++) {
+        lbm_face &F = cfg->faces[f];
+        if (F.kind == LBM_FACE_PERIODIC) continue;
+        if (F.kind != LBM_FACE_WALL)
+            return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: inlet/outlet faces are not supported with ENERGY");
+        const int a = f / 2, side = f % 2;
+        const int lim = a == 0 ? ny : nx;
+        for (int p = 1; p <= lim; p++) {
+            const size_t id = a == 0 ? at(side ? nx + 1 : 0, p) : at(p, side ? ny + 1 : 0);
+            const int te = types_energy[id];
+            if (te == 7)
+                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: Neumann walls (TYPE_Q) are not supported: the "
+                                               "reference's update depends on its loop order");
+            if (te != 6)
+                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: every wall cell needs type_Energy = TYPE_T (6)");
+            if (p == 1) F.T = T[id];
+            else if (T[id] != F.T)
+                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: face " + std::to_string(f) + " T is not uniform");
+        }
+        F.thermal_kind = LBM_TWALL_DIRICHLET;
+    }
+    cfg->thermal = LBM_THERMAL_ENERGY;
+    cfg->tau_g = tau_g;
+    cfg->cp = cp;
+    cfg->T_init = Tf;
     return LBM_OK;
 }

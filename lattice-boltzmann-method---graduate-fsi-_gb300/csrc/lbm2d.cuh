@@ -52,6 +52,26 @@ struct Params2 {
     int band_on;
 };
 
+// The reference's ENERGY model (LBM.h:58) on a D2Q9 handle: temperature
+// populations g on the flow lattice, stored shifted (g - w T_ref) in the
+// storage type of f.  Per boundary class: the links whose source is a
+// Dirichlet wall, P(c_opp . u_w) - 1 of their wall equilibrium, and the wall
+// temperature (Determine_Wall_Temperature, lbm.cpp:965-981) at the first
+// streaming (the set-up wall T) and at later ones (the wall's own sum g
+// after the first MacroProp).
+struct Energy2 {
+    float inv_tau_g;     // 1 / tau_g
+    float tg_fac;        // (tau_g - 1/2) / (cs2 tau_g)
+    float inv_cp;        // 1 / cp
+    float two_nu;        // 2 nu, nu = cs2 (tau - 1/2)
+    float s_fac;         // -1 / (2 tau cs2): S = s_fac / rho * sum c c (f - feq)
+    float T_ref;         // shift of the stored g; the uniform set-up T
+    uint32_t dir[16];    // links l of a class whose source is a Dirichlet wall
+    float pm1[16][Q9];   // P(c_opp(l) . u_w) - 1 of the wall equilibrium
+    float tw[16][2];     // wall T (first streaming, later)
+    float dtw[16][2];    // wall T - T_ref
+};
+
 // Device state of a D2Q9 solve.  The body kinematics are those of IBLBM
 // (lbm.cpp:1136-1167): V_CM of the current step and of the step before, the
 // centre, and the box [floor(c - D), ceil(c + D)] of the current step.

@@ -129,6 +129,7 @@ enum : uint32_t {
     ST_NONFINITE_FORCE = 4u,
     ST_FEQ_NEG = 8u,
     ST_TIMEOUT = 16u,       // a bounded mbarrier wait gave up
+    ST_T_RANGE = 32u,       // ENERGY: T outside (0, 100) or NaN (lbm.cpp:794-797)
 };
 
 __device__ __forceinline__ int cell_class(int x, int y, int z, const StepParams &P) {

@@ -118,3 +118,51 @@ def test_more_details_entry_points_reject_null_handles(pkg):
     assert L.lbmgpu_download_stats(None, None, None, None) == 1
     assert L.lbmgpu_output_avg_vtk(None, b"x.vtr", 0.1, None) == 1
     assert "null" in L.lbmgpu_last_error().decode() or "bad argument" in L.lbmgpu_last_error().decode()
+
+
+def test_config_energy_2d_maps_couette_and_refuses_the_rest(pkg):
+    """lbmgpu_config_energy_2d: main_setup_Couette's type_Energy / T set-up
+    (lbm.cpp:1552-1572) -> Dirichlet wall faces; the unsupported energy
+    set-ups fail with LBM_ERR_UNSUPPORTED before any device work."""
+    nx, ny = 2, 10
+    t = np.zeros((ny + 2, nx + 2), np.uint8)
+    t[0] = t[-1] = 1
+    te = np.zeros_like(t)
+    te[0] = te[-1] = 6
+    T = np.full(t.shape, 0.5)
+    T[-1] = 0.625
+    cfg = pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t), nx, ny, t, te, T, 0.8, 2.0)
+    assert cfg.thermal == pkg.THERMAL_ENERGY and cfg.cp == 2.0 and cfg.tau_g == 0.8 and cfg.T_init == 0.5
+    assert [cfg.faces[f].thermal_kind for f in (2, 3)] == [pkg.TWALL_DIRICHLET] * 2
+    assert (cfg.faces[2].T, cfg.faces[3].T) == (0.5, 0.625)
+    for bad_te, bad_T, word in ((7, None, "Neumann"), (0, None, "TYPE_T"), (6, "fluid", "uniform")):
+        te2 = te.copy()
+        te2[0] = bad_te
+        T2 = T.copy()
+        if bad_T:
+            T2[3, 1] = 0.51
+        with pytest.raises(pkg.LbmError) as e:
+            pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t), nx, ny, t, te2, T2, 0.8, 2.0)
+        assert e.value.status == 7 and word in str(e.value), (word, str(e.value))
+    # an inlet face
+    t3 = t.copy()
+    t3[1:-1, 0] = 3
+    t3[1:-1, -1] = 2
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t3), nx, ny, t3, te, T, 0.8, 2.0)
+    assert e.value.status == 7
+    # create: the D3Q7 model is not a D2Q9 option; ENERGY needs cp > 0
+    c2 = pkg.config_from_types_2d(nx, ny, 0.9, t)
+    c2.thermal, c2.tau_g = pkg.THERMAL_D3Q7, 0.8
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(c2)
+    assert e.value.status == 7
+    cfg.storage = pkg.STORAGE["f16"]
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(cfg)
+    assert e.value.status == 7 and "FP32" in str(e.value)
+    cfg.storage = pkg.STORAGE["f32"]
+    cfg.cp = 0.0
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(cfg)
+    assert e.value.status == 1

@@ -112,3 +112,25 @@ def test_dropin_cylinder2d_loop(drivers, tmp_path, case):
     scale = np.abs(g["cd"]).max()
     assert np.abs(r[:, 1] - g["cd"]).max() / scale < 2e-6
     assert np.abs(r[:, 2] - g["cl"]).max() / scale < 2e-6
+
+
+def test_dropin_couette_energy_loop(drivers, tmp_path):
+    """The reference's Couette_Flow build with its ENERGY model (-DD2Q9
+    -DENERGY): main_setup_Couette's type_Energy / T set-up and the main loop
+    through the facade; rho, u, T and q of every fluid row against the
+    reference's own run (T within 1e-3 of the temperature spread: FP32)."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "couette_energy_ny30_re20_2000.npz"))
+    ny = int(g["ny"])
+    out = str(tmp_path / "couette.bin")
+    subprocess.check_call([drivers["dropin_couette"], str(ny), str(float(g["Re"])), str(int(g["steps"])), out],
+                          cwd=str(tmp_path))
+    a = np.fromfile(out, dtype=np.float64).reshape(8, ny, 4)
+    T = g["T"][1:-1]
+    assert np.abs(a[4] - T).max() < 1e-3 * (T.max() - T.min())
+    uw = np.abs(g["u"][0]).max()
+    assert np.abs(a[0] - g["rho"][1:-1]).max() < 1e-5
+    assert np.abs(a[1:4] - g["u"][:, 1:-1]).max() < 1e-5 * uw
+    q = g["q"][:, 1:-1]
+    assert np.abs(a[5:8] - q).max() < 1e-5 * np.abs(q).max()
