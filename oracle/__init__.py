@@ -329,6 +329,114 @@ def sphere_bb(nx: int, ny: int, nz: int, tau: float, diameter: float, u_max: flo
     return lat, box
 
 
+def _ctrunc(v: float) -> int:
+    """C's double -> int conversion (truncation toward zero)."""
+    return int(v)
+
+
+def staircase2d(kind: str, nx: int, ny: int, D: float, Re: float, u_max: float, lpd: float = 1.5, nb: int = 1):
+    """The reference's staircase 2D bodies with momentum-exchange Cl/Cd, set
+    up as its own code does (D2Q9, Nz = 1, ghost-inclusive grid):
+      "cylbasic"  Cylinder_Basic (Generate_Cylinder / main_setup_Cylinder,
+                  lbm.cpp:1429-1494): cells whose centre (i - 1/2, j - 1/2)
+                  lies within D/2 of (Nx/5, Ny/2), i, j in 1..N;
+      "tandem"    Cylinder_Tandem_Circle (lbm.cpp:1645-1704): nb circles of
+                  the integer diameter D (radius D/2 in integer division) at
+                  (Nx/5, Ny/2 + L/2 - n L), L = lpd D, the centres taken as
+                  int;
+      "triangle"  Cylinder_Tandem_Triangle (lbm.cpp:1706-1757): nb
+                  equilateral triangles, tip (Nx/5 + n L, Ny/2), columns
+                  i = 0..D with rows floor(-i/sqrt 3)..ceil(i/sqrt 3).
+    Ghost faces and initial state follow each set-up, including the order
+    in which the faces are assigned (it decides the corner ghosts).
+    tau = 0.5 + u_max D / Re / cs2.  Returns (lattice, MEA boxes in the
+    reference's indices, reference area A of C = F / (0.5 rho0 U^2 A))."""
+    cs2 = 1.0 / 3.0
+    tau = 0.5 + (u_max * D / Re) / cs2
+    lat = Lattice(9, nx, ny, 1, tau)
+    t = lat.types  # [k][j][i]
+    t[:] = TYPE_F
+    NX, NY = nx + 2, ny + 2
+    boxes = []
+    if kind == "cylbasic":
+        cx, cy = nx / 5.0, ny / 2.0
+        for k in (0, 1):
+            for j in range(1, ny + 1):
+                for i in range(1, nx + 1):
+                    if np.sqrt((cx - (i - 0.5)) ** 2 + (cy - (j - 0.5)) ** 2) <= D / 2.0:
+                        t[k, j, i] = TYPE_S
+        t[:, :, 0] = TYPE_IN
+        t[:, :, -1] = TYPE_OUT
+        t[:, 0, :] = TYPE_OUT
+        t[:, -1, :] = TYPE_OUT
+        fluid = t != TYPE_S
+        boxes.append((_ctrunc(cx - D), _ctrunc(cx + D), _ctrunc(cy - D), _ctrunc(cy + D)))
+        area = D
+    elif kind == "tandem":
+        Di = int(D)
+        L = Di * lpd
+        cx = nx // 5
+        cy0 = _ctrunc(ny // 2 + L / 2)
+        rad = float(Di // 2)
+        for n in range(nb):
+            cy = _ctrunc(cy0 - n * L)
+            for i in range(cx - Di, cx + Di + 1):
+                for j in range(cy - Di, cy + Di + 1):
+                    if np.sqrt((cx - (i - 0.5)) ** 2 + (cy - (j - 0.5)) ** 2) <= rad:
+                        t[0:2, j, i] = TYPE_S
+            boxes.append((_ctrunc(cx - L / 2), _ctrunc(cx + L / 2), _ctrunc(cy0 - n * L - L / 2),
+                          _ctrunc(cy0 - n * L + L / 2)))
+        t[:, 0, :] = TYPE_OUT
+        t[:, -1, :] = TYPE_OUT
+        t[:, :, 0] = TYPE_IN
+        t[:, :, -1] = TYPE_OUT
+        fluid = t != TYPE_S
+        area = float(Di)
+    elif kind == "triangle":
+        Di = int(D)
+        L = Di * lpd
+        tx, ty = nx // 5, ny // 2
+        for n in range(nb):
+            tip = _ctrunc(tx + n * L)
+            for i in range(Di + 1):
+                for j in range(int(np.floor(-i / np.sqrt(3))), int(np.ceil(i / np.sqrt(3))) + 1):
+                    t[:, ty + j, tip + i] = TYPE_S
+            boxes.append((_ctrunc(tx + n * L - Di // 4), _ctrunc(tx + n * L + (Di + L) / 2), ty - Di, ty + Di))
+        t[:, 0, :] = TYPE_OUT
+        t[:, -1, :] = TYPE_OUT
+        t[:, :, 0] = TYPE_IN
+        t[:, :, -1] = TYPE_OUT
+        t[0, :, :] = TYPE_F
+        t[-1, :, :] = TYPE_F
+        fluid = t != TYPE_S
+        area = 2.0 * Di / np.sqrt(3.0)
+    else:
+        raise ValueError(kind)
+    lat.rho[:] = 1.0
+    lat.ux[fluid] = u_max
+    lat.init()
+    return lat, boxes, area
+
+
+def staircase2d_run(kind: str, nx: int, ny: int, D: float, Re: float, u_max: float, steps: int, lpd: float = 1.5,
+                    nb: int = 1):
+    """Run a staircase case for `steps` steps in the reference order
+    (Collision, Streaming, MacroProp; main.cpp:214-220), taking MEA_CL /
+    MEA_CD (lbm.cpp:3085-3163) in every box after every step.  Returns
+    (lattice, cl[nb][steps], cd[nb][steps])."""
+    lat, boxes, area = staircase2d(kind, nx, ny, D, Re, u_max, lpd, nb)
+    q = 0.5 * 1.0 * u_max * u_max * area
+    cl = np.zeros((len(boxes), steps))
+    cd = np.zeros((len(boxes), steps))
+    for s_ in range(steps):
+        assert lat.step_plain(1) == 0
+        for b, (x0, x1, y0, y1) in enumerate(boxes):
+            m = lat.mea((x0, x1, y0, y1, 1, 1))
+            cl[b, s_] = m[1] / q
+            cd[b, s_] = -m[0] / q
+    return lat, cl, cd
+
+
 def fibonacci_sphere(n: int, diameter: float, center) -> Markers:
     mk = Markers(n)
     c = np.ascontiguousarray(center, dtype=np.float64)

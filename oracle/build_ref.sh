@@ -14,6 +14,9 @@
 #   transverse:NX:NY:D:NODES:M:AMP:FREQ  D2Q9 cylinder oscillating across the stream
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
 #   couette:NY:RE             D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls)
+#   cylbasic:NX:NY:D:RE:U     D2Q9 staircase cylinder, momentum-exchange Cl/Cd (Cylinder_Basic)
+#   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
+#   triangle:NX:NY:D:RE:U:LPD:NB  D2Q9 staircase triangles in tandem (Cylinder_Tandem_Triangle)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${REF:-/root/reference}
@@ -69,6 +72,23 @@ for v in "$@"; do
         ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3)
         exe="$OUT/ref_couette_${ny}_${re}"
         $CXX $FLAGS -DREF_COUETTE -DREF_NY=$ny -DREF_RE=$re -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    cylbasic)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        re=$(echo "$v" | cut -d: -f5); u=$(echo "$v" | cut -d: -f6)
+        exe="$OUT/ref_cylbasic_${nx}_${ny}_${d}_${re}_${u}"
+        $CXX $FLAGS -DREF_CYLBASIC -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_RE=$re -DREF_U=$u -o "$exe" \
+            "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    tandem|triangle)
+        kind=$(echo "$v" | cut -d: -f1)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        re=$(echo "$v" | cut -d: -f5); u=$(echo "$v" | cut -d: -f6); lpd=$(echo "$v" | cut -d: -f7)
+        nb=$(echo "$v" | cut -d: -f8)
+        flag=-DREF_TANDEM; [ "$kind" = triangle ] && flag=-DREF_TRIANGLE
+        exe="$OUT/ref_${kind}_${nx}_${ny}_${d}_${re}_${u}_${lpd}_${nb}"
+        $CXX $FLAGS $flag -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_RE=$re -DREF_U=$u -DREF_LPD=$lpd \
+            -DREF_NB=$nb -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     sphere)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)

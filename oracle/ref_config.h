@@ -19,6 +19,12 @@
  *   REF_COUETTE   D2Q9 Couette flow with the reference's own thermal model
  *                 (ENERGY: temperature populations on the flow lattice,
  *                 viscous heating, Dirichlet walls), Ny = REF_NY, Re = REF_RE.
+ *   REF_CYLBASIC  D2Q9 staircase cylinder with momentum-exchange Cl/Cd (the
+ *                 reference's Cylinder_Basic case), REF_NX x REF_NY, REF_D,
+ *                 REF_RE, REF_U.
+ *   REF_TANDEM    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle),
+ *                 REF_NB circles REF_LPD diameters apart; REF_TRIANGLE the
+ *                 equilateral triangles of Cylinder_Tandem_Triangle.
  *   REF_SPHERE    D3Q19 staircase sphere with momentum-exchange Cl/Cd (the
  *                 reference's Sphere_BB case), shrunk to test size; REF_D,
  *                 REF_RE and REF_U set the diameter, Reynolds number and
@@ -179,6 +185,60 @@ static const double nu = u_max * D / Re;
 static const double tau = 0.5 * dt + nu / cs2;
 #define T_OUT 30000
 #define Nt 10
+#elif defined REF_CYLBASIC
+#define Cylinder_Basic
+#define MOMENTUM_EXCHANGE_ALGORITHM
+#define D2Q9
+#define Re REF_RE
+static const double D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static const double u_max = REF_U;
+static double center_x = dx * (Nx / 5.0);
+static double center_y = dy * (Ny / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_TANDEM
+#define Cylinder_Tandem_Circle
+#define MOMENTUM_EXCHANGE_ALGORITHM
+#define D2Q9
+#define Re REF_RE
+static int D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static double LpD = REF_LPD;
+static double L = D * LpD;
+static int N = REF_NB;
+static int center_x = Nx / 5;
+static int center_y = Ny / 2 + L / 2;
+static double u_max = REF_U;
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_TRIANGLE
+#define Cylinder_Tandem_Triangle
+#define MOMENTUM_EXCHANGE_ALGORITHM
+#define D2Q9
+#define Re REF_RE
+static int D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static double LpD = REF_LPD;
+static int N = REF_NB;
+static int tip_x = Nx / 5;
+static int tip_y = Ny / 2;
+static double L = D * LpD;
+static double u_max = REF_U;
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+#define T_OUT 30000
+#define Nt 10
 #else
-#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE, REF_COUETTE or REF_SPHERE"
+#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE, REF_COUETTE, REF_CYLBASIC, REF_TANDEM, REF_TRIANGLE or REF_SPHERE"
 #endif

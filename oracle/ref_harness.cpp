@@ -165,6 +165,64 @@ int main(int argc, char **argv) {
     for (int w = 50; w <= 53; w++) dump_field(lb, fp, w);
     fclose(fp);
     printf("{\"case\": \"couette_energy\", \"ny\": %d, \"steps\": %d, \"seconds\": %.6f}\n", Ny, steps, t1 - t0);
+#elif defined REF_CYLBASIC || defined REF_TANDEM || defined REF_TRIANGLE
+    // the staircase 2D bodies with the momentum exchange of main.cpp:242-356,
+    // taken after every step (the reference takes it every Nt steps)
+#if defined REF_CYLBASIC
+    LBM lb = main_setup_Cylinder();
+    const int nb = 1;
+#elif defined REF_TANDEM
+    LBM lb = main_setup_Tandem_Circle();
+    const int nb = N;
+#else
+    LBM lb = main_setup_Tandem_Triangle();
+    const int nb = N;
+#endif
+    std::vector<std::vector<double>> CL(nb), CD(nb);
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int step = 1; step <= steps; step++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+        for (int n = 0; n < nb; n++) {
+#if defined REF_CYLBASIC
+            CL[n].push_back(MEA_CL(lb, center_x - D, center_x + D, center_y - D, center_y + D, 1, 1));
+            CD[n].push_back(MEA_CD(lb, center_x - D, center_x + D, center_y - D, center_y + D, 1, 1));
+#elif defined REF_TANDEM
+            CL[n].push_back(MEA_CL(lb, center_x - L / 2, center_x + L / 2, center_y - n * L - L / 2,
+                                   center_y - n * L + L / 2, 1, 1));
+            CD[n].push_back(MEA_CD(lb, center_x - L / 2, center_x + L / 2, center_y - n * L - L / 2,
+                                   center_y - n * L + L / 2, 1, 1));
+#else
+            CL[n].push_back(MEA_CL(lb, tip_x + n * L - D / 4, tip_x + n * L + (D + L) / 2, tip_y - D, tip_y + D, 1, 1));
+            CD[n].push_back(MEA_CD(lb, tip_x + n * L - D / 4, tip_x + n * L + (D + L) / 2, tip_y - D, tip_y + D, 1, 1));
+#endif
+        }
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+    for (int n = 0; n < nb; n++) {
+        fwrite(CL[n].data(), sizeof(double), CL[n].size(), fp);
+        fwrite(CD[n].data(), sizeof(double), CD[n].size(), fp);
+    }
+    fclose(fp);
+    // the solid cells of the set-up, layer k = 1 (x fastest)
+    if (argc > 3) {
+        FILE *fs = fopen(argv[3], "wb");
+        if (!fs) return 3;
+        for (int j = 0; j <= Ny + 1; j++)
+            for (int i = 0; i <= Nx + 1; i++) {
+                unsigned char t = (unsigned char)lb.fluid[i][j][1].type;
+                fwrite(&t, 1, 1, fs);
+            }
+        fclose(fs);
+    }
+    double mlups = (double)Nx * Ny * steps / (t1 - t0) / 1e6;
+    printf("{\"case\": \"staircase2d\", \"nx\": %d, \"bodies\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f}\n",
+           Nx, nb, steps, t1 - t0, mlups);
 #elif defined REF_SPHERE
     LBM lb = main_setup_Sphere();
     std::vector<double> CL, CD;

@@ -33,6 +33,13 @@ outputs are stored as small .npz fixtures:
                                     Re = 20, 2000 steps: rho, u, T and the
                                     heat flux q on every row of the k = 1
                                     layer, ghosts included
+  staircase2d_{cylbasic,tandem,triangle}_300.npz  the D2Q9 staircase bodies
+                                    with momentum-exchange Cl/Cd
+                                    (Cylinder_Basic, Cylinder_Tandem_Circle,
+                                    Cylinder_Tandem_Triangle, shrunk): Cl and
+                                    Cd of every body after every step, the
+                                    set-up's cell types, a window of rho, u
+                                    round the bodies and the layer sums
                                     These two keep Cl, Cd, the markers, and
                                     rho, u, F in the IBM box window
                                     i = 4..28, j = 8..32 of the k = 1 layer
@@ -84,6 +91,16 @@ def read_vtr(path: str) -> dict:
     return out
 
 
+# (name, build_ref variant, executable, nx, ny, bodies, window rows, window columns)
+STAIRCASE = (("cylbasic", "cylbasic:100:60:20:200:0.1", "ref_cylbasic_100_60_20_200_0.1", 100, 60, 1,
+              slice(14, 48), slice(4, 50)),
+             ("tandem", "tandem:160:100:10:100:0.05:1.5:2", "ref_tandem_160_100_10_100_0.05_1.5_2", 160, 100, 2,
+              slice(24, 72), slice(16, 60)),
+             ("triangle", "triangle:100:80:10:100:0.05:1.5:3", "ref_triangle_100_80_10_100_0.05_1.5_3", 100, 80, 3,
+              slice(26, 56), slice(14, 92)))
+STAIRCASE_VARIANTS = tuple(v for _, v, *_ in STAIRCASE)
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -95,7 +112,7 @@ def main() -> None:
     a = ap.parse_args()
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
-                     "couette:30:20")
+                     "couette:30:20", *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -176,6 +193,18 @@ def main() -> None:
         assert np.array_equal(f[:, k], f[:, 1])
     np.savez_compressed(os.path.join(OUT, "couette_energy_ny30_re20_2000.npz"), rho=f[0, 1], u=f[1:4, 1],
                         T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=2000)
+    # staircase 2D bodies, 300 steps
+    for name, _, exe, nx, ny, nb, wr, wc in STAIRCASE:
+        p = os.path.join(tmp, name + ".bin")
+        pt = os.path.join(tmp, name + ".types")
+        run(exe, ["300", p, pt])
+        r = oracle.read_ref_dump(p, nx + 2, ny + 2, 3, 4)
+        fl = r["fields"][:3, 1]
+        rest = np.fromfile(p)[4 * (nx + 2) * (ny + 2) * 3:].reshape(nb, 2, 300)
+        types = np.fromfile(pt, dtype=np.uint8).reshape(ny + 2, nx + 2)
+        np.savez_compressed(os.path.join(OUT, "staircase2d_%s_300.npz" % name), cl=rest[:, 0], cd=rest[:, 1],
+                            types=types, window=fl[:, wr, wc], wrows=np.array([wr.start, wr.stop]),
+                            wcols=np.array([wc.start, wc.stop]), sums=fl.reshape(3, -1).sum(axis=1), steps=300)
     print("golden fixtures written to", OUT)
 
 

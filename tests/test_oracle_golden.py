@@ -187,3 +187,22 @@ def test_energy_couette_matches_reference(orc):
     assert abs(g["T"][0, 1] - mid) < 1e-12 and abs(g["T"][-1, 1] - mid) < 1e-12
     # viscous heating lifts the centre above both walls
     assert g["T"][16, 1] > mid + 1e-4
+
+
+@pytest.mark.parametrize("case", [("cylbasic", 100, 60, 20.0, 200.0, 0.1, 1), ("tandem", 160, 100, 10, 100.0, 0.05, 2),
+                                  ("triangle", 100, 80, 10, 100.0, 0.05, 3)], ids=lambda c: c[0])
+def test_staircase2d_matches_reference(orc, case):
+    """The D2Q9 staircase bodies with momentum-exchange Cl/Cd: Cylinder_Basic,
+    Cylinder_Tandem_Circle and Cylinder_Tandem_Triangle (lbm.cpp:1429-1757),
+    their set-ups restated from the reference (cell types equal), MEA_CL /
+    MEA_CD in each body's box (main.cpp:242-356) after every step."""
+    kind, nx, ny, D, Re, u, nb = case
+    g = np.load(os.path.join(GOLDEN, "staircase2d_%s_300.npz" % kind))
+    lat, cl, cd = orc.staircase2d_run(kind, nx, ny, D, Re, u, int(g["steps"]), 1.5, nb)
+    assert np.array_equal(lat.types[1], g["types"])
+    scale = np.abs(g["cd"]).max()
+    assert np.abs(cl - g["cl"]).max() < 1e-12 * scale and np.abs(cd - g["cd"]).max() < 1e-12 * scale
+    f = np.stack([lat.rho[1], lat.ux[1], lat.uy[1]])
+    wr, wc = g["wrows"], g["wcols"]
+    assert np.abs(f[:, wr[0]:wr[1], wc[0]:wc[1]] - g["window"]).max() < 1e-13
+    assert np.allclose(f.reshape(3, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-10)
