@@ -167,7 +167,8 @@ lbm_status lbmgpu_config_from_types(int nx, int ny, int nz, double tau, const ui
 
 /* The same for the reference's D2Q9 build (Nz = 1): arrays of (nx+2)(ny+2)
  * entries, x fastest, the computational layer fluid[i][j][1].  The result
- * has lattice = LBM_LATTICE_D2Q9 and nz = 1. */
+ * has lattice = LBM_LATTICE_D2Q9 and nz = 1.  Interior TYPE_S cells at rest
+ * are accepted: pass their mask to lbmgpu_set_solids. */
 lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, const uint8_t *types, const double *rho,
                                        const double *ux, const double *uy, lbm_config *out);
 
@@ -246,6 +247,16 @@ lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask);
  * them), F = -sum (f*_l + f_opp(l)) c_l in lattice units.  The reference's
  * coefficients are Cd = Fx / (0.5 rho0 U^2 A), Cl = -Fy / (0.5 rho0 U^2 A). */
 lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+
+/* Momentum exchange over one box of the current state, MEA_CL / MEA_CD
+ * (lbm.cpp:3085-3163) called after a step: box = (xmin, xmax, ymin, ymax,
+ * zmin, zmax) in the reference's ghost-inclusive indices, inclusive, as its
+ * callers pass them (main.cpp:246-353).  out = F = -sum (f*_l + f_opp(l)) c_l
+ * over the fluid cells of the box and their solid links; Cd = Fx / q,
+ * Cl = -Fy / q.  D2Q9 handles (several bodies, one box each: the tandem
+ * cases); a D3Q19 handle returns LBM_ERR_UNSUPPORTED (its
+ * lbmgpu_get_solid_forces sums every solid after every step). */
+lbm_status lbmgpu_mea_box(lbm_handle *h, const int box[6], double out[3]);
 
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 

@@ -51,7 +51,7 @@ ABI_SYMBOLS = [
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
-    "lbmgpu_config_energy_2d",
+    "lbmgpu_config_energy_2d", "lbmgpu_mea_box",
 ]
 
 
@@ -165,6 +165,7 @@ def load(path: str | None = None):
     L.lbmgpu_output_avg_vtk.argtypes = [vp, C.c_char_p, d, C.POINTER(C.c_uint8)]
     L.lbmgpu_config_from_types_2d.argtypes = [i, i, d, C.POINTER(C.c_uint8), dp, dp, dp, C.POINTER(Config)]
     L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
+    L.lbmgpu_mea_box.argtypes = [vp, C.POINTER(C.c_int), dp]
     L.lbmgpu_config_energy_2d.argtypes = [C.POINTER(Config), i, i, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), dp, d,
                                           d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
@@ -323,6 +324,15 @@ class Solver:
         n = C.c_int()
         check(self.L.lbmgpu_get_solid_forces(self.h, _dp(out), max_steps, C.byref(n)))
         return out[: n.value]
+
+    def mea_box(self, box) -> np.ndarray:
+        """MEA_CL / MEA_CD over one box (xmin, xmax, ymin, ymax, zmin, zmax) of
+        the reference's ghost-inclusive indices, for the current state (D2Q9
+        handles): F = -sum (f*_l + f_opp(l)) c_l; Cd = F[0] / q, Cl = -F[1] / q."""
+        b = (C.c_int * 6)(*[int(v) for v in box])
+        out = np.zeros(3)
+        check(self.L.lbmgpu_mea_box(self.h, b, _dp(out)))
+        return out
 
     def output_vtk_async(self, path: str, u_ref: float = 1.0, types=None):
         """Write a .vtr of the current state in the reference's layout; returns

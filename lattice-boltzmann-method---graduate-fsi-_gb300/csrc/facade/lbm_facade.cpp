@@ -182,9 +182,7 @@ void LBM::Init() {
                         any = true;
                     }
                 }
-#if !defined D2Q9
         if (any) check("set_solids", lbmgpu_set_solids(dev->h, mask.data()));
-#endif
         dev->solids = any;
     }
 #if defined MORE_DETAILS
@@ -410,21 +408,37 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
 }
 
 // Momentum-exchange coefficients of the solid cells after the latest step
-// (MEA_CL / MEA_CD, lbm.cpp:3085-3163).  The device sums over every fluid
-// cell next to an interior solid; the box arguments of the reference, which
-// only keep the domain walls out of the sum, are not needed.
-static double mea_component(LBM &lb, int comp) {
+// (MEA_CL / MEA_CD, lbm.cpp:3085-3163).  A D3Q19 build sums over every
+// fluid cell next to an interior solid after every step (one body; the
+// reference's box only keeps the domain walls out of the sum).  A D2Q9 build
+// sums over the given box of the current state, so each body of the tandem
+// cases keeps its own coefficients.
+static double mea_component(LBM &lb, int comp, const int box[6]) {
     lbm_handle *h = lb.handle();
     if (!h) return 0.0;
+    const lbm_options &o = g_lbm_options;
+    const double q = 0.5 * o.rho0 * o.u_max * o.u_max * o.ref_area;
+#if defined D2Q9
+    double F[3];
+    check("mea_box", lbmgpu_mea_box(h, box, F));
+    return F[comp] / q;
+#else
+    (void)box;
     std::vector<double> rows(4);
     int n = 0;
     if (lbmgpu_get_solid_forces(h, rows.data(), 1, &n) != LBM_OK || n < 1) return 0.0;
-    const lbm_options &o = g_lbm_options;
-    return rows[comp] / (0.5 * o.rho0 * o.u_max * o.u_max * o.ref_area);
+    return rows[comp] / q;
+#endif
 }
 
-double MEA_CL(LBM &lb, int, int, int, int, int, int) { return -mea_component(lb, 1); }
-double MEA_CD(LBM &lb, int, int, int, int, int, int) { return mea_component(lb, 0); }
+double MEA_CL(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax) {
+    const int box[6] = {xmin, xmax, ymin, ymax, zmin, zmax};
+    return -mea_component(lb, 1, box);
+}
+double MEA_CD(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zmax) {
+    const int box[6] = {xmin, xmax, ymin, ymax, zmin, zmax};
+    return mea_component(lb, 0, box);
+}
 
 // OutputVTK (lbm.cpp:2290-2642) without the host mirror: the device writes
 // ./field%06d.vtr of the current state from a host thread while the time

@@ -79,7 +79,13 @@ __device__ __forceinline__ void collide9(float f[Q9], float drho, float ux, floa
     }
 }
 
-template <class T, bool FORCED>
+// With SOLID, interior solid cells (staircase bodies at rest) keep their
+// populations (the reference never collides or streams them, so they hold
+// their set-up equilibrium) and only report their moments; a link of a
+// fluid cell whose source is a solid takes the cell's own post-collision
+// population of the opposite link (halfway bounce-back, lbm.cpp:267-274,
+// wall at rest).
+template <class T, bool FORCED, bool SOLID>
 __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__restrict__ B,
                                                 const __grid_constant__ Params2 P, State2 *__restrict__ ds,
                                                 float *__restrict__ mom, float *__restrict__ band, int gather,
@@ -90,7 +96,32 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     const long long cell = x + (long long)P.nx * y;
     float f[Q9];
     const bool face = x == 0 || x == P.nx - 1 || y == 0 || y == P.ny - 1;
-    if (!gather) {
+    const uint32_t lk = SOLID ? (uint32_t)P.links[cell] : 0u;
+    if (SOLID && (lk & kSolidCell)) {
+        if (mom != nullptr) {
+            float drho = 0.0f, jx = 0.0f, jy = 0.0f;
+#pragma unroll
+            for (int l = 0; l < Q9; l++) {
+                const float v = St<T>::ld(A + l * P.S + cell);
+                drho += v;
+                jx += (float)cx9(l) * v;
+                jy += (float)cy9(l) * v;
+            }
+            const float rho = 1.0f + drho;
+            mom[cell] = rho;
+            mom[P.N + cell] = jx / rho;
+            mom[2 * P.N + cell] = jy / rho;
+        }
+        return;
+    }
+    if (SOLID && gather && (lk & kSolidLinks)) {
+        int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
+        raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
+        const Class2 &ce = P.cls[raw];
+#pragma unroll
+        for (int l = 0; l < Q9; l++)
+            f[l] = ((lk >> l) & 1u) ? St<T>::ld(A + opp9(l) * P.S + cell) : pull_link2<T>(A, l, x, y, cell, ce, P);
+    } else if (!gather) {
 #pragma unroll
         for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(A + l * P.S + cell);
     } else if (!face) {
@@ -143,6 +174,60 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     collide9(f, drho, ux, uy, Fx, Fy, P.omega, FORCED);
 #pragma unroll
     for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
+}
+
+// Momentum exchange over a box of the current state (MEA_CL / MEA_CD,
+// lbm.cpp:3085-3163): over the fluid cells of the box, every link l whose
+// source x - c_l is a solid adds (f*_l + f_opp(l)) c_l, with f* the cell's
+// post-collision populations of the last step (the buffer the next step
+// pulls from) and f_opp(l) that step's streamed population, pulled here from
+// the same buffer (its source x + c_l bounces back f*_l when it is a solid).
+// Shifted storage adds 2 w_l.  One block: each thread sums its cells in
+// order, then a fixed tree, so the result does not depend on scheduling.
+// out = -sum (the force on the body).
+template <class T>
+__global__ void __launch_bounds__(256) k_mea2d(const T *__restrict__ A, const __grid_constant__ Params2 P, int x0,
+                                               int x1, int y0, int y1, double *__restrict__ out) {
+    __shared__ double sp[2][256];
+    double px = 0.0, py = 0.0;
+    const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
+    const long long n = (bw > 0 && bh > 0) ? (long long)bw * bh : 0;
+    for (long long i = threadIdx.x; i < n; i += blockDim.x) {
+        const int x = x0 + (int)(i % bw), y = y0 + (int)(i / bw);
+        const long long cell = x + (long long)P.nx * y;
+        const uint32_t lk = P.links[cell];
+        if ((lk & kSolidCell) || !(lk & kSolidLinks)) continue;
+        int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
+        raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
+        const Class2 &ce = P.cls[raw];
+        float cpx = 0.0f, cpy = 0.0f;
+#pragma unroll
+        for (int l = 1; l < Q9; l++) {
+            if (!((lk >> l) & 1u)) continue;
+            const int o = opp9(l);
+            const float fo = ((lk >> o) & 1u) ? St<T>::ld(A + l * P.S + cell) : pull_link2<T>(A, o, x, y, cell, ce, P);
+            const float t = St<T>::ld(A + l * P.S + cell) + fo + 2.0f * w9f(l);
+            cpx += t * (float)cx9(l);
+            cpy += t * (float)cy9(l);
+        }
+        px += (double)cpx;
+        py += (double)cpy;
+    }
+    sp[0][threadIdx.x] = px;
+    sp[1][threadIdx.x] = py;
+    __syncthreads();
+    for (int h = blockDim.x / 2; h > 0; h >>= 1) {
+        if ((int)threadIdx.x < h) {
+            sp[0][threadIdx.x] += sp[0][threadIdx.x + h];
+            sp[1][threadIdx.x] += sp[1][threadIdx.x + h];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        out[0] = -sp[0][0];
+        out[1] = -sp[1][0];
+        out[2] = 0.0;
+    }
 }
 
 // f = feq(rho, u) (LBM::Init, lbm.cpp:31-57), shifted; fields [3][N] or null
@@ -982,6 +1067,9 @@ struct lbm2d {
     Energy2 E;
     float *g[2] = {nullptr, nullptr};
     float *aux = nullptr;
+    // interior solid cells: the per-cell link masks, a momentum-exchange result
+    uint16_t *links = nullptr;
+    double *mea_out = nullptr;
     std::vector<void *> allocs;
 };
 
@@ -1208,20 +1296,25 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
     const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
     const void *A = d->f[d->cur];
     void *B = d->f[1 - d->cur];
-    const bool forced = d->P.forced != 0;
+    const bool forced = d->P.forced != 0, solid = d->P.links != nullptr;
+#define L2D_LAUNCH(T, FO, SO)                                                                                  \
+    k_step2d<T, FO, SO><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather,    \
+                                                 export_only)
 #define L2D_STEP(T)                                                                                             \
-    if (forced)                                                                                               \
-        k_step2d<T, true><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather,  \
-                                                   export_only);                                              \
-    else                                                                                                      \
-        k_step2d<T, false><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather, \
-                                                    export_only);
+    if (solid) {                                                                                              \
+        if (forced) L2D_LAUNCH(T, true, true);                                                                \
+        else L2D_LAUNCH(T, false, true);                                                                      \
+    } else {                                                                                                  \
+        if (forced) L2D_LAUNCH(T, true, false);                                                               \
+        else L2D_LAUNCH(T, false, false);                                                                     \
+    }
     switch (h->cfg.storage) {
     case LBM_STORE_F16: L2D_STEP(__half) break;
     case LBM_STORE_BF16: L2D_STEP(__nv_bfloat16) break;
     default: L2D_STEP(float) break;
     }
 #undef L2D_STEP
+#undef L2D_LAUNCH
     return cudaGetLastError();
 }
 
@@ -1383,6 +1476,8 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
     default: k_init2d<float><<<blocks, thr, 0, h->s>>>((float *)d->f[0], N, d->P.S, dfields, r0, u0, v0); break;
     }
     CK2(cudaGetLastError());
+    // solid cells are never written by a step: both buffers hold their state
+    if (d->links) CK2(cudaMemcpyAsync(d->f[1], d->f[0], (size_t)Q9 * d->P.S * h->esize, cudaMemcpyDeviceToDevice, h->s));
     if (d->energy) {
         k_init_energy2d<<<blocks, thr, 0, h->s>>>(d->g[0], d->aux, N, d->P.S, dfields, r0, u0, v0, d->E.T_ref);
         CK2(cudaGetLastError());
@@ -1402,6 +1497,7 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     lbm2d *d = h->d2;
     if (d->ibm) return f2(LBM_ERR_STATE, "set_markers: markers already set");
     if (d->energy) return f2(LBM_ERR_UNSUPPORTED, "set_markers: no immersed body on ENERGY handles");
+    if (d->links) return f2(LBM_ERR_UNSUPPORTED, "set_markers: a D2Q9 handle takes solid cells or markers, not both");
     if (h->steps > 0) return f2(LBM_ERR_STATE, "set_markers: call before the first step");
     const int n = ic->n_markers;
     if (n < 1 || !xyz || !dsw) return f2(LBM_ERR_INVALID, "set_markers: bad markers");
@@ -1627,6 +1723,68 @@ lbm_status l2d_get_body(lbm_handle *h, double out[9]) {
     return LBM_OK;
 }
 
+lbm_status l2d_set_solids(lbm_handle *h, const uint8_t *mask) {
+    lbm2d *d = h->d2;
+    if (h->inited) return f2(LBM_ERR_STATE, "set_solids: call before lbmgpu_init");
+    if (d->links) return f2(LBM_ERR_STATE, "set_solids: solids already set");
+    if (d->ibm) return f2(LBM_ERR_UNSUPPORTED, "set_solids: a D2Q9 handle takes solid cells or markers, not both");
+    if (d->energy) return f2(LBM_ERR_UNSUPPORTED, "set_solids: no interior solids on ENERGY handles");
+    const Params2 &P = d->P;
+    std::vector<uint16_t> lk((size_t)P.N, 0);
+    long long nsolid = 0;
+    for (int y = 0; y < P.ny; y++)
+        for (int x = 0; x < P.nx; x++) {
+            const size_t c = (size_t)x + (size_t)P.nx * y;
+            if (mask[c]) {
+                lk[c] = (uint16_t)kSolidCell;
+                nsolid++;
+                continue;
+            }
+            for (int l = 1; l < Q9; l++) {
+                int sx = x - cx9(l), sy = y - cy9(l);
+                if (P.periodic & 1) sx = (sx + P.nx) % P.nx;
+                if (P.periodic & 2) sy = (sy + P.ny) % P.ny;
+                if (sx < 0 || sx >= P.nx || sy < 0 || sy >= P.ny) continue;
+                if (mask[(size_t)sx + (size_t)P.nx * sy]) lk[c] |= (uint16_t)(1u << l);
+            }
+        }
+    if (nsolid == 0) return LBM_OK;
+    CK2(alloc2(h, &d->links, (size_t)P.N * sizeof(uint16_t)));
+    CK2(alloc2(h, &d->mea_out, 4 * sizeof(double)));
+    CK2(cudaMemcpyAsync(d->links, lk.data(), lk.size() * sizeof(uint16_t), cudaMemcpyHostToDevice, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    d->P.links = d->links;
+    h->solids = true;
+    return LBM_OK;
+}
+
+lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]) {
+    lbm2d *d = h->d2;
+    if (!d->links) return f2(LBM_ERR_STATE, "mea_box: no solid cells set");
+    if (!h->inited) return f2(LBM_ERR_STATE, "mea_box: call lbmgpu_init first");
+    const Params2 &P = d->P;
+    // the reference's ghost-inclusive indices -> device cells (a periodic
+    // axis has no ghost layer on the device); the computational layer k = 1
+    out[0] = out[1] = out[2] = 0.0;
+    if (box[4] > 1 || box[5] < 1) return LBM_OK;
+    const int ox = (P.periodic & 1) ? 0 : 1, oy = (P.periodic & 2) ? 0 : 1;
+    const int x0 = std::max(box[0] - ox, 0), x1 = std::min(box[1] - ox, P.nx - 1);
+    const int y0 = std::max(box[2] - oy, 0), y1 = std::min(box[3] - oy, P.ny - 1);
+    if (x0 > x1 || y0 > y1) return LBM_OK;
+    const void *A = d->f[d->cur];
+    switch (h->cfg.storage) {
+    case LBM_STORE_F16: k_mea2d<__half><<<1, 256, 0, h->s>>>((const __half *)A, P, x0, x1, y0, y1, d->mea_out); break;
+    case LBM_STORE_BF16:
+        k_mea2d<__nv_bfloat16><<<1, 256, 0, h->s>>>((const __nv_bfloat16 *)A, P, x0, x1, y0, y1, d->mea_out);
+        break;
+    default: k_mea2d<float><<<1, 256, 0, h->s>>>((const float *)A, P, x0, x1, y0, y1, d->mea_out); break;
+    }
+    CK2(cudaGetLastError());
+    CK2(cudaMemcpyAsync(out, d->mea_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->s));
+    CK2(cudaStreamSynchronize(h->s));
+    return LBM_OK;
+}
+
 lbm_status l2d_status(lbm_handle *h, uint32_t *flags) {
     lbm2d *d = h->d2;
     uint32_t v = 0;
@@ -1647,10 +1805,15 @@ extern "C" lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, co
     c.tau = tau;
     c.rho0 = 1.0;
     c.lattice = LBM_LATTICE_D2Q9;
+    // interior TYPE_S cells at rest are staircase bodies (lbmgpu_set_solids)
     for (int j = 1; j <= ny; j++)
-        for (int i = 1; i <= nx; i++)
-            if (types[at(i, j)] != 0)
+        for (int i = 1; i <= nx; i++) {
+            const int t = types[at(i, j)];
+            if (t == 1 && ux && uy && (ux[at(i, j)] != 0 || uy[at(i, j)] != 0))
+                return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: moving interior solid cell");
+            if (t != 0 && t != 1)
                 return f2(LBM_ERR_UNSUPPORTED, "config_from_types_2d: non-fluid cell inside the domain");
+        }
     int periodic_axis[2] = {0, 0};
     for (int f = 0; f < 4; f++) {
         const int a = f / 2, side = f % 2;

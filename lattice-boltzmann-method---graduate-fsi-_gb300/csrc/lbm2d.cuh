@@ -50,7 +50,13 @@ struct Params2 {
     int bsx, bsy;   // allocated box (band) extent; band arrays are [5][bsx * bsy]
     long long nb;
     int band_on;
+    // interior solid cells (staircase bodies): per cell, bit l set when the
+    // source x - c_l of link l is a solid, bit 15 when the cell is one
+    const uint16_t *links;
 };
+
+constexpr uint32_t kSolidCell = 0x8000u;
+constexpr uint32_t kSolidLinks = 0x1FFu;
 
 // The reference's ENERGY model (LBM.h:58) on a D2Q9 handle: temperature
 // populations g on the flow lattice, stored shifted (g - w T_ref) in the

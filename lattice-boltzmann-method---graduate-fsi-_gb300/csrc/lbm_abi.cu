@@ -906,7 +906,7 @@ extern "C" lbm_status lbmgpu_download(lbm_handle *h, int field, double *host) {
 // ---------------------------------------------------------------------------
 extern "C" lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask) {
     if (!h || !mask) return fail(LBM_ERR_INVALID, "set_solids: null argument");
-    if (h->d2) return fail(LBM_ERR_UNSUPPORTED, "set_solids: not for D2Q9 handles");
+    if (h->d2) return l2d_set_solids(h, mask);
     if (h->inited) return fail(LBM_ERR_STATE, "set_solids: call before lbmgpu_init");
     if (h->solids) return fail(LBM_ERR_STATE, "set_solids: solids already set");
     const int nx = h->P.nx, ny = h->P.ny, nz = h->P.nz;
@@ -969,8 +969,16 @@ extern "C" lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask) {
     return LBM_OK;
 }
 
+extern "C" lbm_status lbmgpu_mea_box(lbm_handle *h, const int box[6], double out[3]) {
+    if (!h || !box || !out) return fail(LBM_ERR_INVALID, "mea_box: null argument");
+    if (!h->d2)
+        return fail(LBM_ERR_UNSUPPORTED, "mea_box: D2Q9 handles; a D3Q19 handle sums every solid (get_solid_forces)");
+    return l2d_mea_box(h, box, out);
+}
+
 extern "C" lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
     if (!h || !out || max_steps < 0) return fail(LBM_ERR_INVALID, "get_solid_forces: bad argument");
+    if (h->d2) return fail(LBM_ERR_UNSUPPORTED, "get_solid_forces: D2Q9 handles take lbmgpu_mea_box");
     if (!h->solids) return fail(LBM_ERR_STATE, "get_solid_forces: no solid cells set");
     if (!h->inited) return fail(LBM_ERR_STATE, "get_solid_forces: call lbmgpu_init first");
     long long n = 0;

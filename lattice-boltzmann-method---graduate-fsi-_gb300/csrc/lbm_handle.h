@@ -88,6 +88,8 @@ lbm_status l2d_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out)
 lbm_status l2d_get_markers(lbm_handle *h, double *xyz);
 lbm_status l2d_get_body(lbm_handle *h, double out[9]);
 lbm_status l2d_status(lbm_handle *h, uint32_t *flags);
+lbm_status l2d_set_solids(lbm_handle *h, const uint8_t *mask);
+lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]);
 
 // Launch the gather-only export of the current state's moments into h->mom
 // (rho, ux, uy, uz [, T]) on h->s.

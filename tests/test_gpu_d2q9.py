@@ -4,7 +4,8 @@ the two-dimensional IBM cylinders -- the shipped default (implicit
 multi-direct forcing), the explicit scheme and the transversely oscillating
 body -- against the reference's own runs (tests/golden).
 
-Tolerances: FP32 fields within 1e-5 of the reference velocity; Cl and Cd of
+Tolerances: FP32 fields within 1e-5 of the reference velocity (3e-5 for the
+staircase bodies at tau = 0.53); MEA Cl and Cd within 2e-5 of max |Cd|; Cl and Cd of
 the IBM cylinders within 2e-6 of the largest |Cd| of the run (measured: 7.0e-8
 implicit, 1.1e-7 explicit, 3.9e-7 oscillating; the force sums run over FP32
 velocities); FP16 storage within 1e-3 (measured 2.4e-4)."""
@@ -192,10 +193,106 @@ def test_d2q9_unsupported_calls_fail_loudly(pkg, tmp_path):
     s = pkg.Solver(pkg.config_from_types_2d(10, 8, 0.8, t))
     s.init()
     for call in (lambda: s.save_state(str(tmp_path / "x")), lambda: s.output_vtk_async(str(tmp_path / "x.vtr")),
-                 lambda: s.set_more_details(True), lambda: s.set_solids(np.zeros((1, 8, 10)))):
+                 lambda: s.set_more_details(True), lambda: s.solid_forces()):
         with pytest.raises(pkg.LbmError) as e:
             call()
         assert e.value.status == 7
+    # solid cells go in before init; markers and solids do not mix
+    with pytest.raises(pkg.LbmError) as e:
+        s.set_solids(np.zeros((1, 8, 10)))
+    assert e.value.status == 6
+    s2 = pkg.Solver(pkg.config_from_types_2d(10, 8, 0.8, t))
+    m = np.zeros((1, 8, 10))
+    m[0, 3:5, 3:5] = 1
+    s2.set_solids(m)
+    with pytest.raises(pkg.LbmError) as e:
+        s2.set_markers(np.zeros((3, 4)), np.ones(4), 1.0, (5.0, 4.0, 1.0))
+    assert e.value.status == 7
+
+
+STAIRCASE = [("cylbasic", 100, 60, 20.0, 200.0, 0.1, 1), ("tandem", 160, 100, 10, 100.0, 0.05, 2),
+             ("triangle", 100, 80, 10, 100.0, 0.05, 3)]
+
+
+def _staircase_gpu(pkg, orc, case, storage="f32"):
+    kind, nx, ny, D, Re, u, nb = case
+    lat, boxes, area = orc.staircase2d(kind, nx, ny, D, Re, u, 1.5, nb)
+    t = lat.types[1].copy()
+    solid = t[1:-1, 1:-1] == orc.TYPE_S
+    t[1:-1, 1:-1][solid] = orc.TYPE_F
+    rho, ux, uy = lat.rho[1], lat.ux[1], lat.uy[1]
+    cfg = pkg.config_from_types_2d(nx, ny, lat.tau, t, rho, ux, uy)
+    assert (cfg.nx, cfg.ny) == (nx, ny)
+    cfg.storage = pkg.STORAGE[storage]
+    s = pkg.Solver(cfg)
+    s.set_solids(solid[None].astype(np.uint8))
+    z = np.zeros((1, ny, nx))
+    s.init((rho[None, 1:-1, 1:-1], ux[None, 1:-1, 1:-1], uy[None, 1:-1, 1:-1], z))
+    return s, lat, boxes, 0.5 * u * u * area
+
+
+@pytest.mark.parametrize("case", STAIRCASE, ids=lambda c: c[0])
+def test_d2q9_staircase_mea_vs_reference(pkg, orc, case):
+    """Staircase bodies on a D2Q9 handle (Cylinder_Basic and the tandem
+    circles / triangles): MEA_CL / MEA_CD of every body in its own box after
+    every step against the reference's runs; the fields against the oracle
+    (pinned to the same runs)."""
+    g = np.load(os.path.join(GOLDEN, "staircase2d_%s_300.npz" % case[0]))
+    steps = int(g["steps"])
+    s, lat, boxes, q = _staircase_gpu(pkg, orc, case)
+    nb = len(boxes)
+    cl, cd = np.zeros((nb, steps)), np.zeros((nb, steps))
+    for k in range(steps):
+        s.step(1)
+        for b, box in enumerate(boxes):
+            F = s.mea_box(tuple(box) + (1, 1))
+            cd[b, k] = F[0] / q
+            cl[b, k] = -F[1] / q
+    assert s.status() == 0
+    scale = np.abs(g["cd"]).max()
+    e = max(np.abs(cd - g["cd"]).max(), np.abs(cl - g["cl"]).max()) / scale
+    print("%s MEA Cl/Cd error / max|Cd|: %.3g" % (case[0], e))
+    assert e < 2e-5
+    lat.step_plain(steps)
+    m = s.moments()
+    fluid = lat.types[1, 1:-1, 1:-1] != orc.TYPE_S
+    u = case[5]
+    # tau = 0.53 for Cylinder_Basic: FP32 fields within 3e-5 u (measured 1.1e-5)
+    for c, r in (("ux", lat.ux), ("uy", lat.uy)):
+        err = np.abs(m[c][0] - r[1, 1:-1, 1:-1])[fluid].max() / u
+        print("%s %s error / u: %.3g" % (case[0], c, err))
+        assert err < 3e-5, c
+    assert np.abs(m["rho"][0] - lat.rho[1, 1:-1, 1:-1]).max() < 1e-5
+    # solid cells keep their set-up equilibrium: rho = 1, u = 0
+    assert np.all(m["ux"][0][~fluid] == 0) and np.allclose(m["rho"][0][~fluid], 1.0, atol=1e-6)
+
+
+def test_d2q9_staircase_graph_replay_and_fp16(pkg, orc):
+    """Graph replay equals eager stepping bit for bit with solid cells; FP16
+    storage keeps the tandem circles' Cd within 1e-2 of the FP32 run
+    (measured 3.4e-3: the exchange sums stored populations near the walls,
+    each with FP16's 1e-5 rounding)."""
+    case = STAIRCASE[1]
+    out = []
+    for storage in ("f32", "f16"):
+        s, lat, boxes, q = _staircase_gpu(pkg, orc, case, storage)
+        s.step(200)
+        out.append(np.array([s.mea_box(tuple(b) + (1, 1))[0] / q for b in boxes]))
+    assert np.abs(out[1] - out[0]).max() < 1e-2 * np.abs(out[0]).max()
+    fields = []
+    for gs in (8, -1):
+        lat, boxes, area = orc.staircase2d(*case[:6], 1.5, case[6])
+        t = lat.types[1].copy()
+        solid = t[1:-1, 1:-1] == orc.TYPE_S
+        t[1:-1, 1:-1][solid] = orc.TYPE_F
+        cfg = pkg.config_from_types_2d(case[1], case[2], lat.tau, t, lat.rho[1], lat.ux[1], lat.uy[1])
+        cfg.graph_steps = gs
+        s = pkg.Solver(cfg)
+        s.set_solids(solid[None].astype(np.uint8))
+        s.init()
+        s.step(37)
+        fields.append((s.moments()["ux"], s.mea_box(tuple(boxes[0]) + (1, 1))))
+    assert np.array_equal(fields[0][0], fields[1][0]) and np.array_equal(fields[0][1], fields[1][1])
 
 
 def test_d2q9_ibm_large_box_vs_oracle(pkg, orc):

@@ -134,3 +134,25 @@ def test_dropin_couette_energy_loop(drivers, tmp_path):
     assert np.abs(a[1:4] - g["u"][:, 1:-1]).max() < 1e-5 * uw
     q = g["q"][:, 1:-1]
     assert np.abs(a[5:8] - q).max() < 1e-5 * np.abs(q).max()
+
+
+@pytest.mark.parametrize("case", [("cylbasic", 100, 60, 20, 200.0, 0.1, 1), ("tandem", 160, 100, 10, 100.0, 0.05, 2),
+                                  ("triangle", 100, 80, 10, 100.0, 0.05, 3)], ids=lambda c: c[0])
+def test_dropin_staircase2d_loop(drivers, tmp_path, case):
+    """The reference's staircase 2D cases with the momentum-exchange
+    algorithm, set up by its own code pattern (Generate_Cylinder /
+    Generate_Circle / Generate_Triangle and the face loops) and run by its
+    loop through the facade built with -DD2Q9: MEA_CL / MEA_CD of every body
+    in its box after every step against the reference's runs."""
+    from conftest import GOLDEN
+
+    kind, nx, ny, D, Re, u, nb = case
+    g = np.load(os.path.join(GOLDEN, "staircase2d_%s_300.npz" % kind))
+    steps = int(g["steps"])
+    out = str(tmp_path / "mea.bin")
+    subprocess.check_call([drivers["dropin_staircase2d"], kind, str(nx), str(ny), str(D), str(Re), str(u), "1.5",
+                           str(nb), str(steps), out])
+    a = np.fromfile(out).reshape(2, nb, steps)
+    scale = np.abs(g["cd"]).max()
+    assert np.abs(a[0] - g["cl"]).max() < 2e-5 * scale
+    assert np.abs(a[1] - g["cd"]).max() < 2e-5 * scale
