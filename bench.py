@@ -355,6 +355,87 @@ def run_cylinder2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 10.0):
             "speedup_vs_cpu_port": gpu / cpu}
 
 
+def run_tandem2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 6.0):
+    """The reference's tandem-circle case at its own size
+    (Cylinder_Tandem_Circle, LBM.h:243-259: 800 x 400 cells, two staircase
+    circles D = 20 at L/D = 1.5, Re = 200, u = 0.05): the D2Q9 step with
+    solid cells through lbmgpu_step (CUDA graphs), the momentum exchange of
+    both bodies (lbmgpu_mea_box) after the timed steps; beside it the FP64
+    oracle's restatement on the host cores."""
+    nx, ny, D, Re, u, lpd, nb = 800, 400, 20, 200.0, 0.05, 1.5, 2
+    lat, boxes, area = orc.staircase2d("tandem", nx, ny, D, Re, u, lpd, nb)
+    t = lat.types[1].copy()
+    solid = t[1:-1, 1:-1] == orc.TYPE_S
+    t[1:-1, 1:-1][solid] = orc.TYPE_F
+    cfg = pkg.config_from_types_2d(nx, ny, lat.tau, t, lat.rho[1], lat.ux[1], lat.uy[1])
+    cfg.graph_steps = 50
+    s = pkg.Solver(cfg)
+    s.set_solids(solid[None].astype(np.uint8))
+    z = np.zeros((1, ny, nx))
+    s.init((lat.rho[None, 1, 1:-1, 1:-1], lat.ux[None, 1, 1:-1, 1:-1], lat.uy[None, 1, 1:-1, 1:-1], z))
+    s.step(100)
+    ms = s.step_timed(steps)
+    q = 0.5 * u * u * area
+    cd = [float(s.mea_box(tuple(b) + (1, 1))[0] / q) for b in boxes]
+    st = s.status()
+    s.close()
+    gpu = nx * ny * steps / (ms * 1e-3) / 1e6
+    n, t0 = 0, time.perf_counter()
+    while n < 3 or (time.perf_counter() - t0 < cpu_seconds and n < 400):
+        lat.step_plain(1)
+        n += 1
+    cpu = nx * ny * n / (time.perf_counter() - t0) / 1e6
+    return {"workload": "D2Q9 staircase tandem circles 800x400, D=20, L/D=1.5, Re=200 (the reference's "
+                        "Cylinder_Tandem_Circle)", "value": gpu, "unit": "MLUPS", "ms_per_lbm_step": ms / steps,
+            "steps_timed": steps, "cd_bodies": cd, "status": int(st),
+            "cpu_port": {"value": cpu, "unit": "MLUPS", "cores": os.cpu_count() or 1, "kind": "port",
+                         "sample": "%d steps of the same case, FP64 oracle (OpenMP)" % n},
+            "speedup_vs_cpu_port": gpu / cpu}
+
+
+def run_energy2d(pkg, steps: int = 2000, nx: int = 2046, ny: int = 1024):
+    """The reference's ENERGY model on a wide Couette channel (its
+    main_setup_Couette geometry, periodic x, Dirichlet walls, the top one
+    moving at 0.05): k_energy2d streams f and g (FP32) and the per-cell
+    history, 176 B per cell update; achieved bandwidth against the measured
+    copy peak."""
+    cs2, tau = 1.0 / 3.0, 0.9
+    nu = cs2 * (tau - 0.5)
+    uw = 0.05
+    Pr, Br, Tb = 0.7, 10.0, 0.5
+    alpha = nu / Pr
+    tau_g = 0.5 + alpha / cs2
+    cp = cs2 * tau_g / alpha
+    Tt = Tb + uw ** 2 / (cp * Br / Pr)
+    t = np.zeros((ny + 2, nx + 2), np.uint8)
+    t[0, :] = t[-1, :] = 1
+    te = np.zeros_like(t)
+    te[0, :] = te[-1, :] = 6
+    ux = np.zeros(t.shape)
+    ux[-1, :] = uw
+    T = np.full(t.shape, Tb)
+    T[-1, :] = Tt
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t, np.ones(t.shape), ux, np.zeros(t.shape))
+    cfg = pkg.config_energy_2d(cfg, nx, ny, t, te, T, tau_g, cp)
+    cfg.graph_steps = 50
+    s = pkg.Solver(cfg)
+    s.init()
+    s.step(100)
+    ms = s.step_timed(steps)
+    st = s.status()
+    Tm = s.moments()["T"][0]
+    s.close()
+    cells = cfg.nx * cfg.ny
+    achieved = 176.0 * cells * steps / (ms * 1e-3) / 1e9
+    peak, peak_kind = measured_peak()
+    return {"workload": "ENERGY Couette channel %dx%d (periodic x, Dirichlet walls), FP32 f and g" % (cfg.nx, cfg.ny),
+            "value": cells * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS", "ms_per_lbm_step": ms / steps,
+            "steps_timed": steps, "status": int(st), "T_mid_minus_wall": float(Tm[ny // 2].mean() - Tm[0].mean()),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "bytes_per_cell": 176, "note": "graph-replayed steps, one k_energy2d launch each"}}
+
+
 def cpu_baseline_sample(threads: int | None = None):
     """FP64 restatement (oracle) on the same workload, a bounded sample of
     lattice steps, all host threads."""
@@ -473,6 +554,8 @@ def main():
 
         orc.build()
         line["d2q9_cylinder"] = run_cylinder2d(ge.load_package(), orc)
+        line["d2q9_tandem"] = run_tandem2d(ge.load_package(), orc)
+        line["d2q9_energy"] = run_energy2d(ge.load_package())
     if not args.no_cpu_baseline:
         cb = cpu_baseline_sample()
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

@@ -265,8 +265,9 @@ __device__ __forceinline__ float poly9(float cu, float usq) {
 // viscous-heating source F_l = w_l Phi / cp (1 + c_l.u (tau_g - 1/2) /
 // (cs2 tau_g)) plus half its change since the previous collision, where
 // Phi = 2 nu rho S:S and S = -sum c c (f - feq) / (2 rho tau cs2).
-// aux [4][N] keeps what the previous collision used, per cell: rho - 1, u
-// and Phi (the reference's F_vis history, F_vis = 0 before the first one).
+// aux[N] (one float4 per cell, read once at the top and written once at the
+// end) keeps what the previous collision used: rho - 1, u and Phi (the
+// reference's F_vis history, F_vis = 0 before the first one).
 // ENERGY handles keep f and g in FP32: with geq = rho w T (lbm.cpp:646-650)
 // and T = sum g, each collision scales T by 1 + (rho - 1) / tau_g, so T
 // integrates any error of rho -- with FP16 f the Couette run's T drifted by
@@ -276,7 +277,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
                                                   const float *__restrict__ GA, float *__restrict__ GB,
                                                   const __grid_constant__ Params2 P,
                                                   const __grid_constant__ Energy2 E, State2 *__restrict__ ds,
-                                                  float *__restrict__ aux, float *__restrict__ mom, int gather,
+                                                  float4 *__restrict__ aux, float *__restrict__ mom, int gather,
                                                   int first, int export_only) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
@@ -284,7 +285,8 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
     const long long cell = x + (long long)P.nx * y;
     float f[Q9], g[Q9];
     const bool face = x == 0 || x == P.nx - 1 || y == 0 || y == P.ny - 1;
-    const float drho_p = aux[cell];
+    const float4 hist = aux[cell];
+    const float drho_p = hist.x;
     if (!gather) {
 #pragma unroll
         for (int l = 0; l < Q9; l++) {
@@ -362,7 +364,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
     sxy *= sk;
     syy *= sk;
     const float phi = E.two_nu * rho * (sxx * sxx + 2.0f * sxy * sxy + syy * syy);
-    const float uxp = aux[P.N + cell], uyp = aux[2 * P.N + cell], phip = aux[3 * P.N + cell];
+    const float uxp = hist.y, uyp = hist.z, phip = hist.w;
     collide9(f, drho, ux, uy, Fx, Fy, P.omega, FORCED);
     const float a = phi * E.inv_cp, ap = phip * E.inv_cp;
 #pragma unroll
@@ -374,10 +376,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
         const float geq_s = w9f(l) * (dT + drho * Tc + rho * Tc * poly9(cu, usq));
         g[l] = g[l] - (g[l] - geq_s) * E.inv_tau_g + Fl + 0.5f * (Fl - Fb);
     }
-    aux[cell] = drho;
-    aux[P.N + cell] = ux;
-    aux[2 * P.N + cell] = uy;
-    aux[3 * P.N + cell] = phi;
+    aux[cell] = make_float4(drho, ux, uy, phi);
 #pragma unroll
     for (int l = 0; l < Q9; l++) {
         St<T>::st(B + l * P.S + cell, f[l]);
@@ -387,7 +386,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
 
 // g = geq(rho, u, T0) (LBM::Init, lbm.cpp:44-49), shifted by w T0 with T0
 // the uniform set-up T; aux = (rho - 1, u, Phi = 0).
-__global__ void k_init_energy2d(float *__restrict__ G, float *__restrict__ aux, long long N, long long S,
+__global__ void k_init_energy2d(float *__restrict__ G, float4 *__restrict__ aux, long long N, long long S,
                                 const float *__restrict__ fields, float rho0, float ux0, float uy0, float T0) {
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (c >= N) return;
@@ -399,10 +398,7 @@ __global__ void k_init_energy2d(float *__restrict__ G, float *__restrict__ aux, 
         const float cu = (float)cx9(l) * ux + (float)cy9(l) * uy;
         G[l * S + c] = w9f(l) * ((rho - 1.0f) * T0 + rho * T0 * poly9(cu, usq));
     }
-    aux[c] = rho - 1.0f;
-    aux[N + c] = ux;
-    aux[2 * N + c] = uy;
-    aux[3 * N + c] = 0.0f;
+    aux[c] = make_float4(rho - 1.0f, ux, uy, 0.0f);
 }
 
 // ---------------------------------------------------------------------------
@@ -1066,7 +1062,7 @@ struct lbm2d {
     bool energy = false;
     Energy2 E;
     float *g[2] = {nullptr, nullptr};
-    float *aux = nullptr;
+    float4 *aux = nullptr;
     // interior solid cells: the per-cell link masks, a momentum-exchange result
     uint16_t *links = nullptr;
     double *mea_out = nullptr;
@@ -1425,7 +1421,7 @@ lbm_status l2d_create(lbm_handle *h) {
     for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->f[i], (size_t)Q9 * P.S * h->esize));
     if (d->energy) {
         for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->g[i], (size_t)Q9 * P.S * sizeof(float)));
-        CK2(alloc2(h, &d->aux, (size_t)4 * P.N * sizeof(float)));
+        CK2(alloc2(h, &d->aux, (size_t)P.N * sizeof(float4)));
     }
     // moments: rho, ux, uy (ENERGY: and T, qx, qy)
     CK2(alloc2(h, &d->mom, (size_t)(d->energy ? 6 : 3) * P.N * sizeof(float)));
