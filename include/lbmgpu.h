@@ -258,6 +258,15 @@ lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int max_steps, in
  * lbmgpu_get_solid_forces sums every solid after every step). */
 lbm_status lbmgpu_mea_box(lbm_handle *h, const int box[6], double out[3]);
 
+/* Find_Nusselt_number (lbm.cpp:3538-3561) of the current state:
+ * Nu = 1 + <u_y T> / (alpha dT / (Ny + 1)), the mean over the fluid cells
+ * (interior solids excluded), Ny the reference's interior row count.  Thermal
+ * handles: D3Q7 (D3Q19) or ENERGY (D2Q9).  The reference also counts
+ * TYPE_IN / TYPE_OUT ghost cells, which are not on the device; for closed or
+ * periodic boxes (its Rayleigh-Benard, Couette and Poiseuille cases) the set
+ * of cells is the same.  Summed in FP64 in a fixed order. */
+lbm_status lbmgpu_nusselt(lbm_handle *h, double alpha, double dT, double *out);
+
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 
 /* Checkpoint and restart (no counterpart in the reference, which restarts

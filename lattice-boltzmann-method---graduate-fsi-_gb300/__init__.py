@@ -51,7 +51,7 @@ ABI_SYMBOLS = [
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
-    "lbmgpu_config_energy_2d", "lbmgpu_mea_box",
+    "lbmgpu_config_energy_2d", "lbmgpu_mea_box", "lbmgpu_nusselt",
 ]
 
 
@@ -166,6 +166,7 @@ def load(path: str | None = None):
     L.lbmgpu_config_from_types_2d.argtypes = [i, i, d, C.POINTER(C.c_uint8), dp, dp, dp, C.POINTER(Config)]
     L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
     L.lbmgpu_mea_box.argtypes = [vp, C.POINTER(C.c_int), dp]
+    L.lbmgpu_nusselt.argtypes = [vp, d, d, dp]
     L.lbmgpu_config_energy_2d.argtypes = [C.POINTER(Config), i, i, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), dp, d,
                                           d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]
@@ -333,6 +334,12 @@ class Solver:
         out = np.zeros(3)
         check(self.L.lbmgpu_mea_box(self.h, b, _dp(out)))
         return out
+
+    def nusselt(self, alpha: float, dT: float) -> float:
+        """Find_Nusselt_number of the current state: 1 + <u_y T> / (alpha dT / (Ny + 1))."""
+        out = np.zeros(1)
+        check(self.L.lbmgpu_nusselt(self.h, alpha, dT, _dp(out)))
+        return float(out[0])
 
     def output_vtk_async(self, path: str, u_ref: float = 1.0, types=None):
         """Write a .vtr of the current state in the reference's layout; returns

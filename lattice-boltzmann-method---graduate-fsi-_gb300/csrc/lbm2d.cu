@@ -1754,6 +1754,18 @@ lbm_status l2d_set_solids(lbm_handle *h, const uint8_t *mask) {
     return LBM_OK;
 }
 
+lbm_status l2d_thermal_moments(lbm_handle *h, const float **uy, const float **T, const uint16_t **links, long long *N) {
+    lbm2d *d = h->d2;
+    if (!d->energy) return f2(LBM_ERR_STATE, "nusselt: the handle has no temperature (ENERGY)");
+    lbm_status s = l2d_export(h);
+    if (s != LBM_OK) return s;
+    *uy = d->mom + 2 * d->P.N;
+    *T = d->mom + 3 * d->P.N;
+    *links = d->links;
+    *N = d->P.N;
+    return LBM_OK;
+}
+
 lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]) {
     lbm2d *d = h->d2;
     if (!d->links) return f2(LBM_ERR_STATE, "mea_box: no solid cells set");

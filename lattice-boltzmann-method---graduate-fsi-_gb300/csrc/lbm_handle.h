@@ -89,6 +89,8 @@ lbm_status l2d_get_markers(lbm_handle *h, double *xyz);
 lbm_status l2d_get_body(lbm_handle *h, double out[9]);
 lbm_status l2d_status(lbm_handle *h, uint32_t *flags);
 lbm_status l2d_set_solids(lbm_handle *h, const uint8_t *mask);
+// after an export pass: u_y and T of the current moments, the solid-cell masks, the cell count
+lbm_status l2d_thermal_moments(lbm_handle *h, const float **uy, const float **T, const uint16_t **links, long long *N);
 lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]);
 
 // Launch the gather-only export of the current state's moments into h->mom
