@@ -192,19 +192,17 @@ def run_gpu(args):
     hx = np.ctypeslib.as_array(C.cast(xyz_p, C.POINTER(C.c_double)), shape=(xyz.size + ds.size,))
     hx[: xyz.size] = xyz.ravel()
     hx[xyz.size:] = ds
-    ic = pkg.IbmConfig()
-    ic.n_markers, ic.m_max, ic.radius = N_MARKERS, M_MAX, DIAM / 2.0
-    for a in range(3):
-        ic.center[a] = CENTER[a]
     fbuf = np.zeros((LBM_PER_STEP, 8))
     nout = C.c_int()
     dp = C.POINTER(C.c_double)
 
     def e2e_step():
-        pkg.check(L.lbmgpu_set_markers(s.h, C.byref(ic), C.cast(xyz_p, dp),
-                                       C.cast(xyz_p.value + xyz.nbytes, dp), None))
+        # the step's inputs: marker positions and weights from pinned memory
+        pkg.check(L.lbmgpu_update_markers(s.h, C.cast(xyz_p, dp), C.cast(xyz_p.value + xyz.nbytes, dp)))
         pkg.check(L.lbmgpu_step(s.h, LBM_PER_STEP))
-        pkg.check(L.lbmgpu_download_all_f32(s.h, host))
+        # the step's moments to pinned host memory; the copy overlaps the
+        # next step's compute and is complete at lbmgpu_download_wait
+        pkg.check(L.lbmgpu_download_all_f32_async(s.h, host))
         pkg.check(L.lbmgpu_get_forces(s.h, fbuf.ctypes.data_as(dp), LBM_PER_STEP, C.byref(nout)))
 
     for _ in range(args.warmup):
@@ -213,10 +211,11 @@ def run_gpu(args):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         e2e_step()
+    pkg.check(L.lbmgpu_download_wait(s.h))
     s.sync()
     e2e_s = time.perf_counter() - t0
     e2e_mlups = ncell * args.steps * LBM_PER_STEP / e2e_s / 1e6
-    h2d = xyz.nbytes + ds.nbytes + 3 * N_MARKERS * 4
+    h2d = xyz.nbytes + ds.nbytes
     d2h = nf * ncell * 4 + LBM_PER_STEP * 8 * 8
     L.lbmgpu_host_free(host)
     L.lbmgpu_host_free(xyz_p)

@@ -229,6 +229,14 @@ lbm_status lbmgpu_download(lbm_handle *h, int field, double *host);
 lbm_status lbmgpu_download_f32(lbm_handle *h, int field, float *host);
 /* All of rho, ux, uy, uz (and T if thermal) in one export, FP32, [field][cells]. */
 lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host);
+/* The same read-back without waiting: the moment export runs on the handle's
+ * stream and the copy to `host` (pinned memory, e.g. lbmgpu_host_alloc, for
+ * a true overlap) on a copy stream of its own, so the steps enqueued next
+ * run while it lands.  The data are in `host` after lbmgpu_download_wait or
+ * lbmgpu_sync.  A later export waits for this copy before it rewrites the
+ * device moments.  D2Q9 handles copy synchronously. */
+lbm_status lbmgpu_download_all_f32_async(lbm_handle *h, float *host);
+lbm_status lbmgpu_download_wait(lbm_handle *h);
 
 /* IBM force history, oldest first: per step {Fx, Fy, Fz, Tx, Ty, Tz, heat,
  * step}, where F = sum over forcing iterations of -F_m ds_m (the reference's
@@ -268,6 +276,16 @@ lbm_status lbmgpu_mea_box(lbm_handle *h, const int box[6], double out[3]);
 lbm_status lbmgpu_nusselt(lbm_handle *h, double alpha, double dT, double *out);
 
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
+
+/* New positions (3 x n, x rows first) and weights (n) for the markers that
+ * lbmgpu_set_markers registered, as the caller moves the body between calls
+ * of IBLBM (its marker array is an input of every call, lbm.cpp:1135-1167).
+ * The copies are enqueued on the handle's stream ahead of the next step and
+ * nothing else is reset, so captured graphs stay valid; keep the host arrays
+ * (pinned memory for a true overlap) unchanged until the next synchronising
+ * call.  The markers must stay inside the band set up by lbmgpu_set_markers
+ * (LBM_STATUS_BAND_EDGE otherwise).  D3Q19 handles. */
+lbm_status lbmgpu_update_markers(lbm_handle *h, const double *xyz, const double *ds);
 
 /* Checkpoint and restart (no counterpart in the reference, which restarts
  * from its set-up): the current populations, the device state (step counters,

@@ -51,7 +51,8 @@ ABI_SYMBOLS = [
     "lbmgpu_output_markers_vtk", "lbmgpu_output_csv", "lbmgpu_save_state", "lbmgpu_load_state",
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
-    "lbmgpu_config_energy_2d", "lbmgpu_mea_box", "lbmgpu_nusselt",
+    "lbmgpu_config_energy_2d", "lbmgpu_mea_box", "lbmgpu_nusselt", "lbmgpu_download_all_f32_async",
+    "lbmgpu_download_wait", "lbmgpu_update_markers",
 ]
 
 
@@ -167,6 +168,9 @@ def load(path: str | None = None):
     L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
     L.lbmgpu_mea_box.argtypes = [vp, C.POINTER(C.c_int), dp]
     L.lbmgpu_nusselt.argtypes = [vp, d, d, dp]
+    L.lbmgpu_download_all_f32_async.argtypes = [vp, vp]
+    L.lbmgpu_download_wait.argtypes = [vp]
+    L.lbmgpu_update_markers.argtypes = [vp, dp, dp]
     L.lbmgpu_config_energy_2d.argtypes = [C.POINTER(Config), i, i, C.POINTER(C.c_uint8), C.POINTER(C.c_uint8), dp, d,
                                           d]
     L.lbmgpu_get_solid_forces.argtypes = [vp, dp, i, C.POINTER(C.c_int)]

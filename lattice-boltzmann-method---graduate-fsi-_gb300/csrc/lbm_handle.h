@@ -64,6 +64,11 @@ struct lbm_handle {
     cudaStream_t s2 = nullptr;            // IBM stream (overlaps the far-region streaming)
     cudaStream_t s3 = nullptr;            // force reduction, beside the last spreading and band collision
     cudaEvent_t ev_near = nullptr, ev_ibm = nullptr, ev_acc = nullptr, ev_fin = nullptr;
+    // asynchronous moment read-back (lbmgpu_download_all_f32_async): its own
+    // copy stream, ordered after the export pass
+    cudaStream_t s_dl = nullptr;
+    cudaEvent_t ev_dl_exported = nullptr, ev_dl_copied = nullptr;
+    bool dl_issued = false;
     // MORE_DETAILS mode (lbm_details.cu)
     bool details = false;
     float *det = nullptr;                 // [7][N]: p, sigma xx xy xz yy yz zz

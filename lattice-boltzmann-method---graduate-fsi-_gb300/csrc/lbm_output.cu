@@ -337,6 +337,10 @@ void write_vtk(VtkJob j, lbm_output *o) {
 }  // namespace
 
 cudaError_t lbm_mom_acquire(lbm_handle *h) {
+    if (h->dl_issued) {
+        cudaError_t e = cudaStreamWaitEvent(h->s, h->ev_dl_copied, 0);
+        if (e != cudaSuccess) return e;
+    }
     if (!h->out || !h->out->copy_issued) return cudaSuccess;
     return cudaStreamWaitEvent(h->s, h->out->copied, 0);
 }
