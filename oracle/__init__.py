@@ -738,22 +738,28 @@ class Cylinder2D:
     and Streaming.  motion(t) -> (Vx, Vy, Vz) or None for a fixed body.
     marker_dy shifts the markers (not the centre, so not the box): the
     transverse-oscillation case generates them at center_y + amplitude
-    (lbm.cpp:1966)."""
+    (lbm.cpp:1966).  at_rest: the set-up of the moving-body cases
+    (main_setup_Cylinder_InlineOscillating / _IBM_Moving, lbm.cpp:1878-1900,
+    1980-2002): TYPE_OUT on every face, fluid at rest.  center overrides
+    (Nx/5, Ny/2); area the length of C = F / (1/2 u^2 area) (D; D + dx for
+    the inline oscillation, lbm.cpp:1406-1410)."""
 
     def __init__(self, nx: int, ny: int, D: float, nodes: int, m_max: int, u_max: float = 0.1, Re: float = 40.0,
-                 scheme: int = 0, motion=None, vsolid: float | None = None, marker_dy: float = 0.0):
+                 scheme: int = 0, motion=None, vsolid: float | None = None, marker_dy: float = 0.0,
+                 at_rest: bool = False, center=None, area: float | None = None):
         tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
         lat = Lattice(9, nx, ny, 1, tau)
         t = lat.types
         t[:] = TYPE_F
-        t[:, :, 0] = TYPE_IN
+        t[:, :, 0] = TYPE_OUT if at_rest else TYPE_IN
         t[:, :, -1] = TYPE_OUT
         t[:, 0, :] = TYPE_OUT
         t[:, -1, :] = TYPE_OUT
-        lat.ux[:] = u_max
+        lat.ux[:] = 0.0 if at_rest else u_max
         lat.init()
         self.lat, self.D, self.m_max, self.u_max, self.scheme, self.motion = lat, D, m_max, u_max, scheme, motion
-        self.cx, self.cy = nx / 5.0, ny / 2.0
+        self.cx, self.cy = (nx / 5.0, ny / 2.0) if center is None else (float(center[0]), float(center[1]))
+        self.area = D if area is None else area
         self.mk = cylinder_markers_literal(nodes, D, self.cx, self.cy + marker_dy)
         self.vsolid = REF_PI * D * D * 0.25 if vsolid is None else vsolid
         self.V = [0.0, 0.0, 0.0]
@@ -784,20 +790,39 @@ class Cylinder2D:
             op.vcm_new[a] = V[a]
             op.vcm_old[a] = Vold[a]
         out = self.lat.step_ibm(mk, op, [self.cx, self.cy, 1.0])
-        q = 0.5 * 1.0 * self.u_max ** 2 * D
+        q = 0.5 * 1.0 * self.u_max ** 2 * self.area
         self.cl.append(out[1] / q)
         self.cd.append(out[0] / q)
 
 
 def cylinder2d_literal(nx: int, ny: int, D: float, nodes: int, m_max: int, steps: int, u_max: float = 0.1,
                        Re: float = 40.0, scheme: int = 0, motion=None, vsolid: float | None = None,
-                       marker_dy: float = 0.0):
+                       marker_dy: float = 0.0, at_rest: bool = False, center=None, area: float | None = None):
     """Cylinder2D run for `steps` steps: the lattice, the markers, Cl and Cd
-    per step (C = F / (1/2 u^2 D))."""
-    c = Cylinder2D(nx, ny, D, nodes, m_max, u_max, Re, scheme, motion, vsolid, marker_dy)
+    per step (C = F / (1/2 u^2 area))."""
+    c = Cylinder2D(nx, ny, D, nodes, m_max, u_max, Re, scheme, motion, vsolid, marker_dy, at_rest, center, area)
     for _ in range(steps):
         c.step()
     return c.lat, c.mk, np.array(c.cl), np.array(c.cd)
+
+
+def inline_motion(u_max: float, frequency: float):
+    """V_CM(t) of Cylinder_Inline_Oscillating (lbm.cpp:1142-1144)."""
+    import math
+
+    def v(t):
+        return (-u_max * math.cos(2 * REF_PI * frequency * t), 0.0, 0.0)
+
+    return v
+
+
+def towed_motion(u_max: float):
+    """V_CM of Cylinder_IBM_Moving_Arbie (lbm.cpp:1148-1150): -u_max along x."""
+
+    def v(t):
+        return (-u_max, 0.0, 0.0)
+
+    return v
 
 
 def transverse_motion(amplitude: float, frequency: float):

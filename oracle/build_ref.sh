@@ -13,6 +13,8 @@
 #   explicit:NX:NY:D:NODES    the same cylinder, explicit direct forcing
 #   transverse:NX:NY:D:NODES:M:AMP:FREQ  D2Q9 cylinder oscillating across the stream
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
+#   inline:NX:NY:D:NODES:M:PERIOD  D2Q9 cylinder oscillating along the stream (KC = 5)
+#   arbie:NX:NY:D:NODES:M:CX  D2Q9 cylinder towed through fluid at rest
 #   couette:NY:RE             D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls)
 #   cylbasic:NX:NY:D:RE:U     D2Q9 staircase cylinder, momentum-exchange Cl/Cd (Cylinder_Basic)
 #   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
@@ -67,6 +69,15 @@ for v in "$@"; do
         exe="$OUT/ref_transverse_${nx}_${ny}_${d}_${nodes}_${mm}_${amp}_${fr}"
         $CXX $FLAGS -DREF_TRANSVERSE -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
             -DREF_AMP=$amp -DREF_FREQ=$fr -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    inline|arbie)
+        kind=$(echo "$v" | cut -d: -f1)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
+        nodes=$(echo "$v" | cut -d: -f5); mm=$(echo "$v" | cut -d: -f6); p6=$(echo "$v" | cut -d: -f7)
+        exe="$OUT/ref_${kind}_${nx}_${ny}_${d}_${nodes}_${mm}_${p6}"
+        if [ "$kind" = inline ]; then extra="-DREF_INLINE -DREF_PERIOD=$p6"; else extra="-DREF_ARBIE -DREF_CX=$p6"; fi
+        $CXX $FLAGS $extra -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
+            -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     couette)
         ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3)

@@ -16,6 +16,11 @@
  *                 stream (the reference's Cylinder_Transverse_Oscillation),
  *                 shrunk; REF_AMP and REF_FREQ set its amplitude and
  *                 frequency.
+ *   REF_INLINE    D2Q9 implicit IBM cylinder oscillating along the stream
+ *                 in fluid at rest (Cylinder_Inline_Oscillating, KC = 5),
+ *                 REF_PERIOD steps per period.
+ *   REF_ARBIE     D2Q9 implicit IBM cylinder towed at -u through fluid at
+ *                 rest (Cylinder_IBM_Moving_Arbie), centre x = REF_CX.
  *   REF_COUETTE   D2Q9 Couette flow with the reference's own thermal model
  *                 (ENERGY: temperature populations on the flow lattice,
  *                 viscous heating, Dirichlet walls), Ny = REF_NY, Re = REF_RE.
@@ -138,6 +143,55 @@ static const int level_marker = 1;
 static int m_max = REF_MMAX;
 #define T_OUT 30000
 #define Nt 10
+#elif defined REF_INLINE
+#define IBM
+#define Implicit_Diffuse_Interface_Scheme
+#define Cylinder_Inline_Oscillating
+#define Volume_Force
+#define D2Q9
+#define Re 100.0
+#define KC 5.0
+static const double D = REF_D;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static const double period = REF_PERIOD;
+static const double frequency = 1 / period;
+static const double u_max = KC * D * frequency;
+static const double amplitude = u_max / (2 * PI * frequency);
+static double center_x = dx * (Nx / 2.0);
+static double center_y = dy * (Ny / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+static const double Vsolid = PI * D * D * 0.25 * (Nz + 2);
+static const int number_nodes = REF_NODES;
+static const int level_marker = 1;
+static int m_max = REF_MMAX;
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_ARBIE
+#define IBM
+#define Implicit_Diffuse_Interface_Scheme
+#define Cylinder_IBM_Moving_Arbie
+#define Volume_Force
+#define D2Q9
+#define Re 40.0
+static const double D = REF_D;
+static const double target_tstar = 50;
+static const int Nx = REF_NX;
+static const int Ny = REF_NY;
+static const int Nz = 1;
+static const double u_max = 0.1;
+static double center_x = REF_CX;
+static double center_y = dy * (Ny / 2.0);
+static const double nu = u_max * D / Re;
+static const double tau = 0.5 * dt + nu / cs2;
+static const int number_nodes = REF_NODES;
+static const int level_marker = 1;
+static int m_max = REF_MMAX;
+static const double Vsolid = PI * D * D * 0.25;
+#define T_OUT 30000
+#define Nt 10
 #elif defined REF_COUETTE
 #define Couette_Flow
 #define ENERGY
@@ -240,5 +294,5 @@ static const double tau = 0.5 * dt + nu / cs2;
 #define T_OUT 30000
 #define Nt 10
 #else
-#error "define REF_CAVITY, REF_CYLINDER, REF_TRANSVERSE, REF_COUETTE, REF_CYLBASIC, REF_TANDEM, REF_TRIANGLE or REF_SPHERE"
+#error "define one of the REF_* variants listed above"
 #endif

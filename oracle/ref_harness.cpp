@@ -110,9 +110,13 @@ int main(int argc, char **argv) {
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cavity\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
-#elif defined REF_CYLINDER || defined REF_TRANSVERSE
+#elif defined REF_CYLINDER || defined REF_TRANSVERSE || defined REF_INLINE || defined REF_ARBIE
 #if defined REF_TRANSVERSE
     LBM lb = main_setup_Cylinder_TransverseOscillating();
+#elif defined REF_INLINE
+    LBM lb = main_setup_Cylinder_InlineOscillating();
+#elif defined REF_ARBIE
+    LBM lb = main_setup_Cylinder_IBM_Moving();
 #else
     LBM lb = main_setup_Cylinder_IBM();
 #endif

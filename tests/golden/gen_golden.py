@@ -33,6 +33,13 @@ outputs are stored as small .npz fixtures:
                                     Re = 20, 2000 steps: rho, u, T and the
                                     heat flux q on every row of the k = 1
                                     layer, ghosts included
+  cylinder80x40_D10_n40_m5_inline_100.npz  the cylinder oscillating along the
+                                    stream in fluid at rest
+                                    (Cylinder_Inline_Oscillating, KC = 5,
+                                    period 1000 steps, centre (Nx/2, Ny/2))
+  cylinder120x40_D10_n40_m5_towed_100.npz  the cylinder towed at -0.1
+                                    through fluid at rest
+                                    (Cylinder_IBM_Moving_Arbie, centre x = 80)
   staircase2d_{cylbasic,tandem,triangle}_300.npz  the D2Q9 staircase bodies
                                     with momentum-exchange Cl/Cd
                                     (Cylinder_Basic, Cylinder_Tandem_Circle,
@@ -112,7 +119,7 @@ def main() -> None:
     a = ap.parse_args()
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
-                     "couette:30:20", *STAIRCASE_VARIANTS)
+                     "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -163,6 +170,17 @@ def main() -> None:
         np.savez_compressed(os.path.join(OUT, name), window=fl[[0, 1, 2, 4, 5], 8:33, 4:29],
                             sums=fl[[0, 1, 2, 4, 5]].reshape(5, -1).sum(axis=1), cl=r["cl"], cd=r["cd"],
                             markers=r["markers"], nx=80, ny=40, D=10.0, nodes=40, steps=100)
+
+    # moving bodies in fluid at rest: inline oscillation, towed cylinder (100 steps)
+    for exe, name, nx in (("ref_inline_80_40_10_40_5_1000", "cylinder80x40_D10_n40_m5_inline_100.npz", 80),
+                          ("ref_arbie_120_40_10_40_5_80", "cylinder120x40_D10_n40_m5_towed_100.npz", 120)):
+        p = os.path.join(tmp, name + ".bin")
+        run(exe, ["100", p])
+        r = oracle.read_ref_dump(p, nx + 2, 42, 3, 7, 100, 40)
+        fl = r["fields"][:, 1]
+        np.savez_compressed(os.path.join(OUT, name), window=fl[[0, 1, 2, 4, 5], 6:36, nx // 2 - 20:nx // 2 + 30],
+                            sums=fl[[0, 1, 2, 4, 5]].reshape(5, -1).sum(axis=1), cl=r["cl"], cd=r["cd"],
+                            markers=r["markers"], nx=nx, ny=40, D=10.0, nodes=40, steps=100)
 
     # MORE_DETAILS cavity, 200 steps (averages sampled every Nt = 10 steps)
     d = os.path.join(tmp, "det")

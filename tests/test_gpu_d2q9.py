@@ -89,20 +89,22 @@ def _cylinder_gpu(pkg, orc, g, steps, storage="f32", graph_steps=0, **kw):
     nx, ny, D, nodes = int(g["nx"]), int(g["ny"]), float(g["D"]), int(g["nodes"])
     u_max, Re = kw.pop("u_max", 0.1), kw.pop("Re", 40.0)
     marker_dy = kw.pop("marker_dy", 0.0)
+    at_rest, center, area = kw.pop("at_rest", False), kw.pop("center", None), kw.pop("area", D)
     tau = 0.5 + (u_max * D / Re) / (1.0 / 3.0)
     t = np.zeros((ny + 2, nx + 2), np.uint8)
-    t[:, 0] = orc.TYPE_IN
+    t[:, 0] = orc.TYPE_OUT if at_rest else orc.TYPE_IN
     t[:, -1] = orc.TYPE_OUT
     t[0, :] = orc.TYPE_OUT
     t[-1, :] = orc.TYPE_OUT
     ones = np.ones((ny + 2, nx + 2))
-    cfg = pkg.config_from_types_2d(nx, ny, tau, t, ones, u_max * ones, 0.0 * ones)
+    u0 = 0.0 if at_rest else u_max
+    cfg = pkg.config_from_types_2d(nx, ny, tau, t, ones, u0 * ones, 0.0 * ones)
     cfg.storage = pkg.STORAGE[storage]
     cfg.graph_steps = graph_steps
-    cfg.u0[0] = u_max
+    cfg.u0[0] = u0
     s = pkg.Solver(cfg)
     s.init()
-    cx, cy = nx / 5.0, ny / 2.0
+    cx, cy = (nx / 5.0, ny / 2.0) if center is None else center
     mk = orc.cylinder_markers_literal(nodes, D, cx, cy + marker_dy)
     xyz = np.stack([mk["x"], mk["y"], mk["z"]])
     nrm = np.stack([mk["nx"], mk["ny"], mk["nz"]])
@@ -113,7 +115,7 @@ def _cylinder_gpu(pkg, orc, g, steps, storage="f32", graph_steps=0, **kw):
     assert s.status() == 0
     rows = s.forces()
     assert rows.shape[0] == steps and np.array_equal(rows[:, 7], np.arange(1, steps + 1))
-    q = 0.5 * u_max ** 2 * D
+    q = 0.5 * u_max ** 2 * area
     return s, rows[:, 1] / q, rows[:, 0] / q
 
 
@@ -166,6 +168,36 @@ def test_d2q9_ibm_transverse_oscillation_vs_reference(pkg, orc):
     _check_fields(s.moments(), *_layer_moments(lat), 0.05)
     # the body's V_CM of the last step
     assert abs(body[4] - orc.transverse_motion(2.0, 0.005)(float(g["steps"]))[1]) < 1e-15
+
+
+@pytest.mark.parametrize("case", ["inline", "towed"])
+def test_d2q9_ibm_moving_in_fluid_at_rest_vs_reference(pkg, orc, case):
+    """The inline oscillation (V_x = -u cos 2 pi f t, Cd over D + dx) and
+    the towed cylinder (V_x = -u), both in fluid at rest with TYPE_OUT on
+    every face: Cl / Cd after every step, the markers and the fields against
+    the reference's runs.  The step-1 added-mass impulse dominates max |Cd|;
+    the later steps are held to their own scale too."""
+    from test_oracle_golden import moving_case_kwargs
+
+    name = "cylinder80x40_D10_n40_m5_inline_100.npz" if case == "inline" else "cylinder120x40_D10_n40_m5_towed_100.npz"
+    g = np.load(os.path.join(GOLDEN, name))
+    D, steps = float(g["D"]), int(g["steps"])
+    okw = moving_case_kwargs(orc, case, D)
+    kw = dict(m_max=5, u_max=okw["u_max"], Re=okw["Re"], at_rest=True, center=okw["center"],
+              area=okw.get("area", D))
+    if case == "inline":
+        kw.update(vsolid=okw["vsolid"], motion=pkg.MOTION_INLINE_OSC, motion_amp=okw["u_max"], motion_freq=1e-3)
+    else:
+        kw.update(motion=pkg.MOTION_CONSTANT, velocity=(-0.1, 0.0, 0.0))
+    s, cl, cd = _cylinder_gpu(pkg, orc, g, steps, **kw)
+    e = _coeff_err(cl, cd, g)
+    late = max(np.abs(cd - g["cd"])[1:].max(), np.abs(cl - g["cl"])[1:].max()) / np.abs(g["cd"][1:]).max()
+    print("%s Cl/Cd error / max|Cd|: %.3g (steps 2.. on their own scale: %.3g)" % (case, e, late))
+    assert e < 2e-6 and late < 2e-5
+    mk = s.markers().reshape(3, -1)
+    assert np.abs(mk[0] - g["markers"][:, 0]).max() < 1e-12
+    lat, _, _, _ = orc.cylinder2d_literal(int(g["nx"]), int(g["ny"]), D, int(g["nodes"]), steps=steps, **okw)
+    _check_fields(s.moments(), *_layer_moments(lat), okw["u_max"])
 
 
 def test_d2q9_ibm_fp16_storage(pkg, orc):

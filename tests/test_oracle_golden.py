@@ -140,15 +140,32 @@ def test_more_details_match_reference(orc):
     assert abs(g["rms_p"][0, 0, 0] - np.sqrt(190.0 / 191.0) / 3.0) < 1e-15
 
 
-@pytest.mark.parametrize("case", ["explicit", "transverse"])
+def moving_case_kwargs(orc, case, D=10.0):
+    """Cylinder2D options of the moving-body cases in fluid at rest."""
+    if case == "inline":
+        u, f = 5.0 * D * 1e-3, 1e-3
+        return dict(m_max=5, u_max=u, Re=100.0, motion=orc.inline_motion(u, f), vsolid=orc.REF_PI * D * D * 0.25 * 3,
+                    at_rest=True, center=(40.0, 20.0), area=D + 1.0)
+    return dict(m_max=5, u_max=0.1, Re=40.0, motion=orc.towed_motion(0.1), at_rest=True, center=(80.0, 20.0))
+
+
+@pytest.mark.parametrize("case", ["explicit", "transverse", "inline", "towed"])
 def test_cylinder2d_variants_match_reference(orc, case):
-    """The explicit direct-forcing scheme (lbm.cpp:1171-1258) and the
+    """The explicit direct-forcing scheme (lbm.cpp:1171-1258), the
     transversely oscillating cylinder (moving markers and box, added mass,
-    markers generated at center_y + amplitude, lbm.cpp:1966) against the
-    reference's own runs."""
+    markers generated at center_y + amplitude, lbm.cpp:1966), the inline
+    oscillation (Cd over D + dx) and the towed cylinder, the last two in fluid
+    at rest (TYPE_OUT on every face), against the reference's own runs."""
+    win = (slice(8, 33), slice(4, 29))
     if case == "explicit":
         g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_explicit_100.npz"))
         kw = dict(m_max=1, scheme=1)
+    elif case in ("inline", "towed"):
+        g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_inline_100.npz" if case == "inline"
+                                 else "cylinder120x40_D10_n40_m5_towed_100.npz"))
+        kw = moving_case_kwargs(orc, case)
+        nx = int(g["nx"])
+        win = (slice(6, 36), slice(nx // 2 - 20, nx // 2 + 30))
     else:
         g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_transverse_100.npz"))
         D = float(g["D"])
@@ -160,8 +177,9 @@ def test_cylinder2d_variants_match_reference(orc, case):
     assert np.abs(cd - g["cd"]).max() < 1e-12 * scale
     assert np.abs(cl - g["cl"]).max() < 1e-12 * scale
     assert np.abs(mk["y"] - g["markers"][:, 1]).max() == 0.0
+    assert np.abs(mk["x"] - g["markers"][:, 0]).max() == 0.0
     f = np.stack([lat.rho[1], lat.ux[1], lat.uy[1], lat.Fx[1], lat.Fy[1]])
-    assert np.abs(f[:, 8:33, 4:29] - g["window"]).max() < 1e-12
+    assert np.abs(f[(slice(None),) + win] - g["window"]).max() < 1e-12
     assert np.allclose(f.reshape(5, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
 
 
