@@ -72,6 +72,7 @@ def lib():
         L.orc_enable_thermal.argtypes = [vp, d, d, d, d, d]
         L.orc_enable_energy.argtypes = [vp, d, d, d]
         L.orc_energy_buoyancy.argtypes = [vp, d, d]
+        L.orc_force_all.argtypes = [vp, i]
         L.orc_types_energy.restype = C.POINTER(C.c_uint8)
         L.orc_types_energy.argtypes = [vp]
         L.orc_ncell.restype = l
@@ -181,6 +182,12 @@ class Lattice:
         ``types_energy`` is TYPE_T.  Set T (walls included) before init()."""
         self.L.orc_enable_energy(self.h, tau_g, cp, nu)
         self.energy = True
+
+    def force_on_every_cell(self, on: bool = True):
+        """Poiseuille_Flow's MacroProp: the body force set on every cell, walls
+        included (lbm.cpp:800-801), so walls report u = F / 2 from the second
+        MacroProp on and count as moving."""
+        self.L.orc_force_all(self.h, int(on))
 
     def energy_buoyancy(self, g_beta: float, T_star: float):
         """Rayleigh_Benard: F_y = g_beta (T - T_star) on every cell."""
@@ -523,6 +530,40 @@ def couette_energy(ny: int, Re: float, tau: float = 0.9, nx: int = 2, nz: int = 
     lat.T[:, -1, :] = Tt
     lat.init()
     return lat, dict(tau=tau, tau_g=tau_g, cp=cp, nu=nu, u_wall=uw, Tb=Tb, Tt=Tt)
+
+
+def poiseuille(ny: int, Re: float, energy: bool = False, tau: float = 0.9, nx: int = 2, nz: int = 2):
+    """main_setup_Poiseuille (lbm.cpp:1495-1535) with the constants of
+    LBM.h:116-136: walls (TYPE_S; with ENERGY Dirichlet TYPE_T at Tb = Tt =
+    1) on rows j = 0 and Ny + 1, periodic in x and z, u_max = Re nu /
+    (Ny + 1), F_x = -dp/dx = 8 rho nu u_max / (Ny + 1)^2 on the fluid at
+    set-up and, from the first MacroProp on, on every cell.  Returns the
+    initialised lattice and the constants."""
+    cs2 = 1.0 / 3.0
+    nu = cs2 * (tau - 0.5)
+    u_max = Re * nu / (ny + 1)
+    fx = 8 * nu * u_max / (ny + 1) ** 2
+    lat = Lattice(9, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    t[:, 0, :] = TYPE_S
+    t[:, -1, :] = TYPE_S
+    c = dict(tau=tau, nu=nu, u_max=u_max, fx=fx)
+    if energy:
+        alpha = nu / 0.7
+        tau_g = 0.5 + alpha / cs2
+        cp = cs2 * tau_g / alpha
+        lat.enable_energy(tau_g, cp, nu)
+        te = lat.types_energy
+        te[:, 0, :] = TYPE_T
+        te[:, -1, :] = TYPE_T
+        lat.T[:] = 1.0
+        c.update(tau_g=tau_g, cp=cp, alpha=alpha)
+    lat.set_body_force(fx, 0.0, 0.0)
+    lat.force_on_every_cell(True)
+    lat.Fx[t == TYPE_F] = fx
+    lat.init()
+    return lat, c
 
 
 def read_ref_dump(path: str, NX: int, NY: int, NZ: int, nfields: int, steps: int = 0, nodes: int = 0):

@@ -16,6 +16,7 @@
 #   inline:NX:NY:D:NODES:M:PERIOD  D2Q9 cylinder oscillating along the stream (KC = 5)
 #   arbie:NX:NY:D:NODES:M:CX  D2Q9 cylinder towed through fluid at rest
 #   couette:NY:RE             D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls)
+#   poiseuille:NY:RE[:energy] D2Q9 body-forced channel (Poiseuille_Flow), optionally with ENERGY
 #   cylbasic:NX:NY:D:RE:U     D2Q9 staircase cylinder, momentum-exchange Cl/Cd (Cylinder_Basic)
 #   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
 #   triangle:NX:NY:D:RE:U:LPD:NB  D2Q9 staircase triangles in tandem (Cylinder_Tandem_Triangle)
@@ -78,6 +79,12 @@ for v in "$@"; do
         if [ "$kind" = inline ]; then extra="-DREF_INLINE -DREF_PERIOD=$p6"; else extra="-DREF_ARBIE -DREF_CX=$p6"; fi
         $CXX $FLAGS $extra -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_NODES=$nodes -DREF_MMAX=$mm \
             -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    poiseuille)
+        ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3); en=$(echo "$v" | cut -d: -f4)
+        exe="$OUT/ref_poiseuille_${ny}_${re}${en:+_energy}"
+        $CXX $FLAGS -DREF_POISEUILLE ${en:+-DREF_ENERGY} -DREF_NY=$ny -DREF_RE=$re -o "$exe" "$REF/lbm.cpp" \
+            "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     couette)
         ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3)

@@ -102,6 +102,7 @@ typedef struct orc {
     /* the reference's own thermal model (ENERGY): temperature populations on
      * the flow lattice, viscous heating, Dirichlet walls */
     int energy, ebuoy;
+    int force_all;             /* Poiseuille_Flow: the body force is set on every cell */
     double etau_g, ecp, enu;
     double eg_beta, eT_star;   /* Rayleigh_Benard buoyancy F_y = g beta (T - T*) */
     double *eg, *egs, *fvis;   /* [q][ncell] */
@@ -177,6 +178,9 @@ void orc_free(orc *o) {
     free(o->eg); free(o->egs); free(o->fvis); free(o->hq); free(o->type_e);
     free(o);
 }
+
+/* Poiseuille_Flow's force update on every cell (lbm.cpp:800-801). */
+void orc_force_all(orc *o, int on) { o->force_all = on; }
 
 /* Rayleigh_Benard's force update (lbm.cpp:803-805). */
 void orc_energy_buoyancy(orc *o, double g_beta, double T_star) {
@@ -526,6 +530,12 @@ long orc_macro(orc *o) {
         o->ux[c] = (rho_ux + 0.5 * 1.0 * o->Fx[c]) / rho;
         o->uy[c] = (rho_uy + 0.5 * 1.0 * o->Fy[c]) / rho;
         o->uz[c] = (rho_uz + 0.5 * 1.0 * o->Fz[c]) / rho;
+        /* Poiseuille_Flow: F = -dp/dx on every cell, walls included, after u
+         * took the previous force (lbm.cpp:800-801); a wall then reports
+         * u = F / 2 rho from the second MacroProp on */
+        if (o->force_all) {
+            o->Fx[c] = o->body[0]; o->Fy[c] = o->body[1]; o->Fz[c] = o->body[2];
+        }
         /* Rayleigh_Benard: F_y = g beta (T - T*) on every cell, after u took
          * the previous force (lbm.cpp:803-805) */
         if (o->energy && o->ebuoy) o->Fy[c] = o->eg_beta * (o->T[c] - o->eT_star);

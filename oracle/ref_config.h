@@ -21,6 +21,9 @@
  *                 REF_PERIOD steps per period.
  *   REF_ARBIE     D2Q9 implicit IBM cylinder towed at -u through fluid at
  *                 rest (Cylinder_IBM_Moving_Arbie), centre x = REF_CX.
+ *   REF_POISEUILLE  D2Q9 body-forced channel (Poiseuille_Flow), Ny =
+ *                 REF_NY, Re = REF_RE; with REF_ENERGY also the reference's
+ *                 ENERGY model (walls at T = 1, viscous heating).
  *   REF_COUETTE   D2Q9 Couette flow with the reference's own thermal model
  *                 (ENERGY: temperature populations on the flow lattice,
  *                 viscous heating, Dirichlet walls), Ny = REF_NY, Re = REF_RE.
@@ -190,6 +193,34 @@ static const int number_nodes = REF_NODES;
 static const int level_marker = 1;
 static int m_max = REF_MMAX;
 static const double Vsolid = PI * D * D * 0.25;
+#define T_OUT 30000
+#define Nt 10
+#elif defined REF_POISEUILLE
+#define Poiseuille_Flow
+#define D2Q9
+#if defined REF_ENERGY
+#define ENERGY
+#endif
+#define Re REF_RE
+static const int Nx = 2;
+static const int Ny = REF_NY;
+static const int Nz = 2;
+static const double tau = 0.9;
+static const double nu = cs2 * (tau - 0.5);
+static const double u_max = Re * nu / (Ny + 1);
+static double dp_dx = -8 * rho0 * nu * u_max / pow(Ny + 1, 2);
+#define Velocity_Ratio
+#define Temperature_Ratio
+static const double Pr = 0.7;
+static const double alpha = nu / Pr;
+static const double tau_g = 0.5 + alpha / (cs2 * dx);
+static const double k = cs2 * tau_g * dx;
+static const double cp = k / (rho0 * alpha);
+static const double Tt = 1;
+static const double Tb = 1;
+static const double dT = 1;
+static const double j_dot_n = 0;
+static const double D = 1;
 #define T_OUT 30000
 #define Nt 10
 #elif defined REF_COUETTE

@@ -153,6 +153,24 @@ int main(int argc, char **argv) {
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cylinder2d\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());
+#elif defined REF_POISEUILLE
+    LBM lb = main_setup_Poiseuille();
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int s = 1; s <= steps; s++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 4; w++) dump_field(lb, fp, w);
+#if defined ENERGY
+    for (int w = 50; w <= 53; w++) dump_field(lb, fp, w);
+#endif
+    fclose(fp);
+    printf("{\"case\": \"poiseuille\", \"ny\": %d, \"steps\": %d, \"seconds\": %.6f}\n", Ny, steps, t1 - t0);
 #elif defined REF_COUETTE
     LBM lb = main_setup_Couette();
     lb.Init();

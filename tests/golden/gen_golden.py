@@ -40,6 +40,10 @@ outputs are stored as small .npz fixtures:
   cylinder120x40_D10_n40_m5_towed_100.npz  the cylinder towed at -0.1
                                     through fluid at rest
                                     (Cylinder_IBM_Moving_Arbie, centre x = 80)
+  poiseuille_ny30_re20{,_energy}_1500.npz  the body-forced channel
+                                    (Poiseuille_Flow, Ny = 30, Re = 20), with
+                                    and without the ENERGY model: rho, u (and
+                                    T, q) of every row of the k = 1 layer
   staircase2d_{cylbasic,tandem,triangle}_300.npz  the D2Q9 staircase bodies
                                     with momentum-exchange Cl/Cd
                                     (Cylinder_Basic, Cylinder_Tandem_Circle,
@@ -119,7 +123,8 @@ def main() -> None:
     a = ap.parse_args()
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
-                     "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", *STAIRCASE_VARIANTS)
+                     "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",
+                     "poiseuille:30:20:energy", *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -211,6 +216,17 @@ def main() -> None:
         assert np.array_equal(f[:, k], f[:, 1])
     np.savez_compressed(os.path.join(OUT, "couette_energy_ny30_re20_2000.npz"), rho=f[0, 1], u=f[1:4, 1],
                         T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=2000)
+    # Poiseuille channel, 1500 steps, with and without ENERGY
+    for exe, name, nf in (("ref_poiseuille_30_20", "poiseuille_ny30_re20_1500.npz", 4),
+                          ("ref_poiseuille_30_20_energy", "poiseuille_ny30_re20_energy_1500.npz", 8)):
+        p = os.path.join(tmp, name + ".bin")
+        run(exe, ["1500", p])
+        f = oracle.read_ref_dump(p, 4, 32, 4, nf)["fields"]
+        for k in range(4):
+            assert np.array_equal(f[:, k], f[:, 1])
+        extra = dict(T=f[4, 1], q=f[5:8, 1]) if nf == 8 else {}
+        np.savez_compressed(os.path.join(OUT, name), rho=f[0, 1], u=f[1:4, 1], ny=30, Re=20.0, steps=1500, **extra)
+
     # staircase 2D bodies, 300 steps
     for name, _, exe, nx, ny, nb, wr, wc in STAIRCASE:
         p = os.path.join(tmp, name + ".bin")

@@ -224,3 +224,23 @@ def test_staircase2d_matches_reference(orc, case):
     wr, wc = g["wrows"], g["wcols"]
     assert np.abs(f[:, wr[0]:wr[1], wc[0]:wc[1]] - g["window"]).max() < 1e-13
     assert np.allclose(f.reshape(3, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-10)
+
+
+@pytest.mark.parametrize("energy", [False, True], ids=["plain", "energy"])
+def test_poiseuille_matches_reference(orc, energy):
+    """The reference's Poiseuille_Flow build (lbm.cpp:1495-1535): the body
+    force -dp/dx set on the fluid at set-up and on every cell in each
+    MacroProp (lbm.cpp:800-801), so the walls report u = F/2 from the
+    second MacroProp on and bounce back as moving walls; with ENERGY also the
+    Dirichlet walls at T = 1 and the viscous heating.  Bit-exact after 1500
+    steps, ghosts included."""
+    g = np.load(os.path.join(GOLDEN, "poiseuille_ny30_re20%s_1500.npz" % ("_energy" if energy else "")))
+    lat, c = orc.poiseuille(int(g["ny"]), float(g["Re"]), energy=energy)
+    assert lat.step_plain(int(g["steps"])) == 0
+    assert np.array_equal(lat.rho[1], g["rho"])
+    assert np.array_equal(np.stack([lat.ux[1], lat.uy[1], lat.uz[1]]), g["u"])
+    # the wall rows move at F / 2
+    assert np.all(g["u"][0, 0] == 0.5 * c["fx"]) or np.allclose(g["u"][0, 0], 0.5 * c["fx"], rtol=1e-12)
+    if energy:
+        assert np.array_equal(lat.T[1], g["T"])
+        assert np.array_equal(lat.hq[:, 1], g["q"])
