@@ -107,6 +107,10 @@ typedef struct lbm_config {
                              build; nz = 1, faces 4/5 unused) */
     double cp;            /* thermal == LBM_THERMAL_ENERGY: specific heat capacity of the viscous-heating
                              source Phi / cp (LBM.h:213) */
+    int wall_force;       /* D2Q9: 1 = the body force also acts on the wall cells, as the reference's
+                             Poiseuille_Flow MacroProp sets it on every cell (lbm.cpp:800-801); the walls
+                             then report u_w + F/2 and bounce back as moving walls from the third
+                             streaming on */
 } lbm_config;
 
 /* lbm_config.thermal: 0 none; 1 a D3Q7 temperature population with a heat

@@ -68,7 +68,7 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("xface", C.c_int), ("lattice", C.c_int), ("cp", C.c_double)]
+                ("xface", C.c_int), ("lattice", C.c_int), ("cp", C.c_double), ("wall_force", C.c_int)]
 
 
 class IbmConfig(C.Structure):

@@ -83,6 +83,10 @@ struct lbm_options {
     // ENERGY builds (-DENERGY, D2Q9): LBM.h's cp = k / (rho0 alpha) of the
     // viscous-heating source; tau_g above is its tau_g = 0.5 + alpha / cs2
     double cp = 0.0;
+    // Poiseuille_Flow builds: MacroProp sets the body force on every cell,
+    // walls included (lbm.cpp:800-801); the body force itself is read from
+    // fluid[..].F of the fluid cells at Init
+    int wall_force = 0;
     int Nt = 10;                  // output cadence (LBM.h:493-496): Sup_MacroProp's told = (n - Nt) dt
     // the reference's global centre (center_x, center_y, 1): IBLBM's box is
     // [centre - D, centre + D] (lbm.cpp:1165-1166); unset, the marker centroid

@@ -133,6 +133,27 @@ void LBM::Init() {
                                                         uy.data(), uz.data(), T.data(), &cfg));
 #endif
     const lbm_options &o = g_lbm_options;
+    // a uniform force on the fluid cells of the set-up (main_setup_Poiseuille
+    // writes F[0] = -dp_dx, lbm.cpp:1518) is the body force of the run
+    {
+        bool have = false, uniform = true;
+        double F0[3] = {0, 0, 0};
+        for (int i = 0; i < NX; i++)
+            for (int j = 0; j < NY; j++)
+                for (int k = 0; k < NZ; k++) {
+                    const LATTICE &c = fluid[i][j][k];
+                    if (c.type != TYPE_F) continue;
+                    if (!have) {
+                        for (int a = 0; a < 3; a++) F0[a] = c.F[a];
+                        have = true;
+                    } else if (c.F[0] != F0[0] || c.F[1] != F0[1] || c.F[2] != F0[2]) {
+                        uniform = false;
+                    }
+                }
+        if (have && uniform && (F0[0] != 0 || F0[1] != 0 || F0[2] != 0))
+            for (int a = 0; a < 3; a++) cfg.body_force[a] = F0[a];
+    }
+    cfg.wall_force = o.wall_force;
     cfg.storage = o.storage;
     cfg.thermal = o.thermal;
     cfg.tau_g = o.tau_g;

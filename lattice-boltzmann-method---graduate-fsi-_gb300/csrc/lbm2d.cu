@@ -89,7 +89,7 @@ template <class T, bool FORCED, bool SOLID>
 __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__restrict__ B,
                                                 const __grid_constant__ Params2 P, State2 *__restrict__ ds,
                                                 float *__restrict__ mom, float *__restrict__ band, int gather,
-                                                int export_only) {
+                                                int export_only, int drift) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= P.nx || y >= P.ny) return;
@@ -117,7 +117,7 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     if (SOLID && gather && (lk & kSolidLinks)) {
         int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
         raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
-        const Class2 &ce = P.cls[raw];
+        const Class2 &ce = drift ? P.cls_w[raw] : P.cls[raw];
 #pragma unroll
         for (int l = 0; l < Q9; l++)
             f[l] = ((lk >> l) & 1u) ? St<T>::ld(A + opp9(l) * P.S + cell) : pull_link2<T>(A, l, x, y, cell, ce, P);
@@ -130,7 +130,7 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     } else {
         int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
         raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
-        const Class2 &ce = P.cls[raw];
+        const Class2 &ce = drift ? P.cls_w[raw] : P.cls[raw];
 #pragma unroll
         for (int l = 0; l < Q9; l++) f[l] = pull_link2<T>(A, l, x, y, cell, ce, P);
     }
@@ -187,7 +187,7 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
 // out = -sum (the force on the body).
 template <class T>
 __global__ void __launch_bounds__(256) k_mea2d(const T *__restrict__ A, const __grid_constant__ Params2 P, int x0,
-                                               int x1, int y0, int y1, double *__restrict__ out) {
+                                               int x1, int y0, int y1, double *__restrict__ out, int drift) {
     __shared__ double sp[2][256];
     double px = 0.0, py = 0.0;
     const int bw = x1 - x0 + 1, bh = y1 - y0 + 1;
@@ -199,7 +199,7 @@ __global__ void __launch_bounds__(256) k_mea2d(const T *__restrict__ A, const __
         if ((lk & kSolidCell) || !(lk & kSolidLinks)) continue;
         int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
         raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
-        const Class2 &ce = P.cls[raw];
+        const Class2 &ce = drift ? P.cls_w[raw] : P.cls[raw];
         float cpx = 0.0f, cpy = 0.0f;
 #pragma unroll
         for (int l = 1; l < Q9; l++) {
@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
                                                   const __grid_constant__ Params2 P,
                                                   const __grid_constant__ Energy2 E, State2 *__restrict__ ds,
                                                   float4 *__restrict__ aux, float *__restrict__ mom, int gather,
-                                                  int first, int export_only) {
+                                                  int first, int export_only, int drift) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= P.nx || y >= P.ny) return;
@@ -302,7 +302,8 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
     } else {
         int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
         raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
-        const Class2 &ce = P.cls[raw];
+        const Class2 &ce = drift ? P.cls_w[raw] : P.cls[raw];
+        const float *pm1 = drift ? E.pm1_w[raw] : E.pm1[raw];
         const int k = first ? 0 : 1;
         const float tw = E.tw[raw][k], dtw = E.dtw[raw][k];
 #pragma unroll
@@ -310,7 +311,7 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
             f[l] = pull_link2<T>(A, l, x, y, cell, ce, P);
             if ((E.dir[raw] >> l) & 1u) {
                 // 2 geq - 2 w T_ref = 2 w (rho T_w (1 + pm1) - T_ref)
-                const float wall = 2.0f * w9f(l) * (dtw + drho_p * tw + (1.0f + drho_p) * tw * E.pm1[raw][l]);
+                const float wall = 2.0f * w9f(l) * (dtw + drho_p * tw + (1.0f + drho_p) * tw * pm1[l]);
                 g[l] = wall - GA[opp9(l) * P.S + cell];
             } else {
                 // a periodic or interior source (the only other links of an
@@ -1115,7 +1116,7 @@ int face_priority2(int kind) {
 // ghost faces takes the highest-priority kind; a cell's wall velocity is the
 // mean over its moving wall neighbours, Determine_Wall_Velocity,
 // lbm.cpp:941-962).
-void build_classes2(const lbm_config &c, Params2 &P, double uwall_out[16][2] = nullptr) {
+void build_classes2(const lbm_config &c, const Params2 &P, Class2 out[16], double uwall_out[16][2]) {
     for (int cls = 0; cls < 16; cls++) {
         Class2 e;
         memset(&e, 0, sizeof(e));
@@ -1191,7 +1192,7 @@ void build_classes2(const lbm_config &c, Params2 &P, double uwall_out[16][2] = n
                 e.zg |= 1u << l;
             }
         }
-        P.cls[cls] = e;
+        out[cls] = e;
     }
 }
 
@@ -1203,7 +1204,8 @@ void build_classes2(const lbm_config &c, Params2 &P, double uwall_out[16][2] = n
 // streamed): the mean set-up T of their own solid neighbours, which for a
 // wall row wraps onto the opposite wall row.  Corner ghost cells take the T
 // of their y face.
-void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16][2], Energy2 &E) {
+void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16][2], const double uwall_w[16][2],
+                   Energy2 &E) {
     const double cs2 = 1.0 / 3.0, tg = c.tau_g;
     memset(&E, 0, sizeof(E));
     E.inv_tau_g = (float)(1.0 / tg);
@@ -1253,15 +1255,26 @@ void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16]
         E.dtw[cls][0] = (float)(t0 - c.T_init);
         E.dtw[cls][1] = (float)(t1 - c.T_init);
         E.dir[cls] = P.cls[cls].bb;
-        const double uwx = uwall[cls][0], uwy = uwall[cls][1], usq = uwx * uwx + uwy * uwy;
-        for (int l = 0; l < Q9; l++) {
-            // geq of the outgoing direction opp(l) (lbm.cpp:277-279)
-            const double cu = -(cx9(l) * uwx + cy9(l) * uwy);
-            E.pm1[cls][l] = (float)(cu / cs2 + cu * cu / (2 * cs2 * cs2) - usq / (2 * cs2) +
-                                    cu * cu * cu / (6 * cs2 * cs2 * cs2) - cu * usq / (2 * cs2 * cs2));
+        for (int w = 0; w < 2; w++) {
+            const double uwx = w ? uwall_w[cls][0] : uwall[cls][0], uwy = w ? uwall_w[cls][1] : uwall[cls][1];
+            const double usq = uwx * uwx + uwy * uwy;
+            for (int l = 0; l < Q9; l++) {
+                // geq of the outgoing direction opp(l) (lbm.cpp:277-279)
+                const double cu = -(cx9(l) * uwx + cy9(l) * uwy);
+                const float v = (float)(cu / cs2 + cu * cu / (2 * cs2 * cs2) - usq / (2 * cs2) +
+                                        cu * cu * cu / (6 * cs2 * cs2 * cs2) - cu * usq / (2 * cs2 * cs2));
+                if (w) E.pm1_w[cls][l] = v;
+                else E.pm1[cls][l] = v;
+            }
         }
     }
 }
+
+// The streaming of step s (the gather of the launch made with s steps done)
+// sees the walls moving at F/2 from s = 3 on when wall_force is set: the
+// walls' force is set by the first MacroProp and enters their velocity at
+// the second.
+int wall_drift(const lbm_handle *h, int gather) { return (h->cfg.wall_force && gather && h->steps >= 3) ? 1 : 0; }
 
 cudaError_t launch_energy2d(lbm_handle *h, int gather, float *mom, int export_only) {
     lbm2d *d = h->d2;
@@ -1272,14 +1285,16 @@ cudaError_t launch_energy2d(lbm_handle *h, int gather, float *mom, int export_on
     const float *GA = d->g[d->cur];
     float *GB = d->g[1 - d->cur];
     const int first = gather && h->steps == 1 ? 1 : 0;
+    const int drift = wall_drift(h, gather);
     const bool forced = d->P.forced != 0;
 #define L2D_ENERGY(T)                                                                                           \
     if (forced)                                                                                               \
         k_energy2d<T, true><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, GA, GB, d->P, d->E,                 \
-                                                     d->st, d->aux, mom, gather, first, export_only);          \
+                                                     d->st, d->aux, mom, gather, first, export_only, drift);   \
     else                                                                                                      \
         k_energy2d<T, false><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, GA, GB, d->P,                      \
-                                                      d->E, d->st, d->aux, mom, gather, first, export_only);
+                                                      d->E, d->st, d->aux, mom, gather, first, export_only,    \
+                                                      drift);
     L2D_ENERGY(float)
 #undef L2D_ENERGY
     return cudaGetLastError();
@@ -1293,9 +1308,10 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
     const void *A = d->f[d->cur];
     void *B = d->f[1 - d->cur];
     const bool forced = d->P.forced != 0, solid = d->P.links != nullptr;
+    const int drift = wall_drift(h, gather);
 #define L2D_LAUNCH(T, FO, SO)                                                                                  \
     k_step2d<T, FO, SO><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather,    \
-                                                 export_only)
+                                                 export_only, drift)
 #define L2D_STEP(T)                                                                                             \
     if (solid) {                                                                                              \
         if (forced) L2D_LAUNCH(T, true, true);                                                                \
@@ -1408,10 +1424,19 @@ lbm_status l2d_create(lbm_handle *h) {
     for (int a = 0; a < 2; a++)
         if (c.faces[2 * a].kind == LBM_FACE_PERIODIC) P.periodic |= 1 << a;
     for (int l = 0; l < Q9; l++) P.pofs[l] = -(cx9(l) + c.nx * cy9(l));
-    double uwall[16][2];
-    build_classes2(c, P, uwall);
+    double uwall[16][2], uwall_w[16][2];
+    build_classes2(c, P, P.cls, uwall);
+    {
+        // the walls as seen from the third streaming on under wall_force:
+        // their MacroProp velocity u_w + F / (2 rho_w), rho_w = 1
+        lbm_config cw = c;
+        for (int f = 0; f < 4; f++)
+            if (c.wall_force && cw.faces[f].kind == LBM_FACE_WALL)
+                for (int a = 0; a < 2; a++) cw.faces[f].u[a] += 0.5 * c.body_force[a];
+        build_classes2(cw, P, P.cls_w, uwall_w);
+    }
     d->energy = c.thermal == LBM_THERMAL_ENERGY;
-    if (d->energy) build_energy2(c, P, uwall, d->E);
+    if (d->energy) build_energy2(c, P, uwall, uwall_w, d->E);
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
     if (c.graph_steps > 0) d->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) d->gsteps = 0;
@@ -1604,7 +1629,8 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
     // the first step (no gather) and odd remainders run eagerly; whole
     // graphs of gsteps (even: the buffers return to the same parity) replay
     // (ENERGY: also the second, whose streaming takes the set-up wall T)
-    const long long eager = d->energy ? 2 : 1;
+    // (wall_force: also until the walls' drift has set in, at the third)
+    const long long eager = h->cfg.wall_force ? 3 : (d->energy ? 2 : 1);
     while (left > 0 && h->steps < eager) {
         CK2(enqueue_step2d(h));
         left--;
@@ -1780,12 +1806,15 @@ lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]) {
     const int y0 = std::max(box[2] - oy, 0), y1 = std::min(box[3] - oy, P.ny - 1);
     if (x0 > x1 || y0 > y1) return LBM_OK;
     const void *A = d->f[d->cur];
+    const int drift = wall_drift(h, 1);
     switch (h->cfg.storage) {
-    case LBM_STORE_F16: k_mea2d<__half><<<1, 256, 0, h->s>>>((const __half *)A, P, x0, x1, y0, y1, d->mea_out); break;
-    case LBM_STORE_BF16:
-        k_mea2d<__nv_bfloat16><<<1, 256, 0, h->s>>>((const __nv_bfloat16 *)A, P, x0, x1, y0, y1, d->mea_out);
+    case LBM_STORE_F16:
+        k_mea2d<__half><<<1, 256, 0, h->s>>>((const __half *)A, P, x0, x1, y0, y1, d->mea_out, drift);
         break;
-    default: k_mea2d<float><<<1, 256, 0, h->s>>>((const float *)A, P, x0, x1, y0, y1, d->mea_out); break;
+    case LBM_STORE_BF16:
+        k_mea2d<__nv_bfloat16><<<1, 256, 0, h->s>>>((const __nv_bfloat16 *)A, P, x0, x1, y0, y1, d->mea_out, drift);
+        break;
+    default: k_mea2d<float><<<1, 256, 0, h->s>>>((const float *)A, P, x0, x1, y0, y1, d->mea_out, drift); break;
     }
     CK2(cudaGetLastError());
     CK2(cudaMemcpyAsync(out, d->mea_out, 3 * sizeof(double), cudaMemcpyDeviceToHost, h->s));

@@ -47,6 +47,10 @@ struct Params2 {
     int periodic;   // bit 0: x, bit 1: y
     int pofs[Q9];   // plain pull offset of link l: -(cx + nx cy)
     Class2 cls[16];
+    // the classes once the walls move at F/2 (lbm_config.wall_force: the
+    // reference's Poiseuille_Flow sets the body force on every cell, walls
+    // included, lbm.cpp:800-801); used from the third streaming on
+    Class2 cls_w[16];
     int bsx, bsy;   // allocated box (band) extent; band arrays are [5][bsx * bsy]
     long long nb;
     int band_on;
@@ -74,6 +78,7 @@ struct Energy2 {
     float T_ref;         // shift of the stored g; the uniform set-up T
     uint32_t dir[16];    // links l of a class whose source is a Dirichlet wall
     float pm1[16][Q9];   // P(c_opp(l) . u_w) - 1 of the wall equilibrium
+    float pm1_w[16][Q9]; // the same with the walls moving at F/2 (cls_w)
     float tw[16][2];     // wall T (first streaming, later)
     float dtw[16][2];    // wall T - T_ref
 };

@@ -295,6 +295,8 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         if (c.faces[f].kind < 0 || c.faces[f].kind > 4) return fail(LBM_ERR_INVALID, "create: unknown face kind");
     if (c.lattice != 0 && c.lattice != LBM_LATTICE_D3Q19 && c.lattice != LBM_LATTICE_D2Q9)
         return fail(LBM_ERR_INVALID, "create: unknown lattice");
+    if (c.wall_force && c.lattice != LBM_LATTICE_D2Q9)
+        return fail(LBM_ERR_UNSUPPORTED, "create: wall_force is a D2Q9 option (the reference's Poiseuille_Flow)");
     if (c.lattice == LBM_LATTICE_D2Q9) {
         lbm_handle *h = new lbm_handle();
         h->cfg = c;

@@ -126,3 +126,45 @@ def test_energy_unsupported_calls_fail_loudly(pkg, orc):
         with pytest.raises(pkg.LbmError) as e:
             _solver(pkg, orc, 10, 20.0, storage=st)
         assert e.value.status == 7 and "FP32" in str(e.value)
+
+
+@pytest.mark.parametrize("energy", [False, True], ids=["plain", "energy"])
+def test_poiseuille_wall_force_vs_reference(pkg, orc, energy):
+    """The reference's Poiseuille_Flow build: F = -dp/dx on every cell in
+    MacroProp, so its walls move at F/2 from the third streaming on
+    (lbm_config.wall_force); with ENERGY the walls at T = 1 and viscous
+    heating.  Against the reference's own 1500-step runs."""
+    g = np.load(os.path.join(GOLDEN, "poiseuille_ny30_re20%s_1500.npz" % ("_energy" if energy else "")))
+    ny, Re = int(g["ny"]), float(g["Re"])
+    lat, c = orc.poiseuille(ny, Re, energy=energy)
+    t = lat.types[1].copy()
+    nx = t.shape[1] - 2
+    cfg = pkg.config_from_types_2d(nx, ny, c["tau"], t, np.ones(t.shape), np.zeros(t.shape), np.zeros(t.shape))
+    if energy:
+        te = np.zeros_like(t)
+        te[0, :] = te[-1, :] = orc.TYPE_T
+        cfg = pkg.config_energy_2d(cfg, nx, ny, t, te, np.ones(t.shape), c["tau_g"], c["cp"])
+    cfg.body_force[0] = c["fx"]
+    cfg.wall_force = 1
+    s = pkg.Solver(cfg)
+    s.init()
+    s.step(int(g["steps"]))
+    assert s.status() == 0
+    m = s.moments()
+    um = np.abs(g["u"][0, 1:-1]).max()
+    eu = max(np.abs(m["ux"][0] - g["u"][0, 1:-1]).max(), np.abs(m["uy"][0] - g["u"][1, 1:-1]).max()) / um
+    print("poiseuille %s u error / u_max: %.3g" % ("energy" if energy else "plain", eu))
+    # FP32 over 1500 steps: measured 1.3e-5; a run without the walls' drift
+    # is off by 5.5e-4 (checked below)
+    assert eu < 3e-5
+    if energy:
+        T = g["T"][1:-1]
+        eT = np.abs(m["T"][0] - T).max() / (T.max() - T.min())
+        print("poiseuille T error / spread: %.3g" % eT)
+        assert eT < 5e-3
+    # without the walls' drift the profile differs by about the wall speed F/2
+    cfg.wall_force = 0
+    s2 = pkg.Solver(cfg)
+    s2.init()
+    s2.step(int(g["steps"]))
+    assert np.abs(s2.moments()["ux"][0] - g["u"][0, 1:-1]).max() > 0.3 * 0.5 * c["fx"]

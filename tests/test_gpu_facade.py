@@ -156,3 +156,22 @@ def test_dropin_staircase2d_loop(drivers, tmp_path, case):
     scale = np.abs(g["cd"]).max()
     assert np.abs(a[0] - g["cl"]).max() < 2e-5 * scale
     assert np.abs(a[1] - g["cd"]).max() < 2e-5 * scale
+
+
+def test_dropin_poiseuille_energy_loop(drivers, tmp_path):
+    """The reference's Poiseuille_Flow build with ENERGY (-DD2Q9 -DENERGY):
+    main_setup_Poiseuille's set-up (F[0] = -dp/dx on the fluid cells, read
+    as the body force) and loop through the facade, the walls moving at F/2
+    from the third streaming (wall_force); rho, u, T against the reference's
+    own run."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "poiseuille_ny30_re20_energy_1500.npz"))
+    ny = int(g["ny"])
+    out = str(tmp_path / "pois.bin")
+    subprocess.check_call([drivers["dropin_poiseuille"], str(ny), str(float(g["Re"])), str(int(g["steps"])), out])
+    a = np.fromfile(out, dtype=np.float64).reshape(8, ny, 4)
+    um = np.abs(g["u"][0, 1:-1]).max()
+    assert np.abs(a[1:3] - g["u"][:2, 1:-1]).max() < 3e-5 * um
+    T = g["T"][1:-1]
+    assert np.abs(a[4] - T).max() < 5e-3 * (T.max() - T.min())
