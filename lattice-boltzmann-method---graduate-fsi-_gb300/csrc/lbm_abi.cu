@@ -666,8 +666,10 @@ static cudaError_t enqueue_ibm(lbm_handle *h, const LaunchArgs &a, cudaStream_t 
     ia.band = h->band;
     ia.thermal = h->icfg.thermal;
     ia.stream = s;
+    ia.pdl = h->cfg.storage == LBM_STORE_F32 ? 1 : 0;
     LaunchArgs b = a;
     b.stream = s;
+    b.pdl = ia.pdl;
     const float fsign = h->icfg.literal_sign ? -1.0f : 1.0f;
     if (split && (e = cudaStreamWaitEvent(s, h->ev_fin, 0)) != cudaSuccess) return e;
     for (int it = 1; it <= h->icfg.m_max; it++) {

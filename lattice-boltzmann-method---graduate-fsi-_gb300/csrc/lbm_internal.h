@@ -39,6 +39,7 @@ struct LaunchArgs {
     const StagedPlan *st;  // staged kernel plan (or null)
     int buf_a;             // index of the population buffer read (A)
     cudaStream_t stream;
+    int pdl = 0;           // band collision: programmatic dependent launch behind the IBM chain
 };
 
 cudaError_t launch_step(int storage, const LaunchArgs &a);
@@ -79,6 +80,7 @@ struct IbmArgs {
     float *band;
     int thermal;
     cudaStream_t stream;
+    int pdl = 0;  // programmatic dependent launch for the chain (FP32 storage, where the chain is the critical path)
 };
 
 // first = 1: unforced interpolation and marker density; each call computes

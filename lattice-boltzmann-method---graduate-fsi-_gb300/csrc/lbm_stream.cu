@@ -109,6 +109,8 @@ __global__ void __launch_bounds__(64, 16) k_band_collide(T *__restrict__ B, T *_
                                                       const __grid_constant__ StepParams P,
                                                       const DevState *__restrict__ ds,
                                                       const float *__restrict__ band, float fsign) {
+    // the last spreading may still be running (programmatic dependent launch)
+    cudaGridDependencySynchronize();
     const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (b >= P.nb) return;
     band_collide_cell<T, THERMAL>(B, GB, P, ds, band, fsign, b);
@@ -207,13 +209,20 @@ template <class T>
 static cudaError_t launch_band_t(const LaunchArgs &a, float fsign) {
     const int threads = 64;
     const long long blocks = (a.P->nb + threads - 1) / threads;
-    if (a.thermal)
-        k_band_collide<T, true><<<(unsigned)blocks, threads, 0, a.stream>>>((T *)a.B, (T *)a.GB, *a.P, a.ds, a.band,
-                                                                            fsign);
-    else
-        k_band_collide<T, false><<<(unsigned)blocks, threads, 0, a.stream>>>((T *)a.B, nullptr, *a.P, a.ds, a.band,
-                                                                             fsign);
-    return cudaGetLastError();
+    // programmatic dependent launch behind the last spreading of the chain
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3((unsigned)blocks);
+    c.blockDim = dim3(threads);
+    c.stream = a.stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = attr;
+    c.numAttrs = a.pdl ? 1 : 0;
+    const DevState *ds = a.ds;
+    const float *band = a.band;
+    if (a.thermal) return cudaLaunchKernelEx(&c, k_band_collide<T, true>, (T *)a.B, (T *)a.GB, *a.P, ds, band, fsign);
+    return cudaLaunchKernelEx(&c, k_band_collide<T, false>, (T *)a.B, (T *)nullptr, *a.P, ds, band, fsign);
 }
 
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign) {
