@@ -200,9 +200,6 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_interp(const __grid_con
     // launched early beside its predecessor (programmatic dependent
     // launch): wait for that grid's results before reading anything
     cudaGridDependencySynchronize();
-    // every block of this grid is resident: let the next grid of the chain
-    // launch and wait at its own dependency point
-    cudaTriggerProgrammaticLaunchCompletion();
     const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
     if (m >= mk.n) return;  // whole warp leaves together
     interp_marker(m, threadIdx.x & 31, P, mk, ds, band, first, last, thermal);
@@ -212,7 +209,6 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_spread(const __grid_con
                                                     const DevState *__restrict__ ds, float *__restrict__ band,
                                                     int thermal) {
     cudaGridDependencySynchronize();
-    cudaTriggerProgrammaticLaunchCompletion();
     const int m = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
     if (m >= mk.n) return;
     spread_marker(m, threadIdx.x & 31, P, mk, ds, band, thermal);
@@ -381,12 +377,14 @@ cudaError_t launch_mea_finish(const float *part, const int *blocks, int nblocks,
 
 // The interpolation/spreading chain of a step is a dozen short dependent
 // grids.  With a.pdl each is launched with programmatic stream
-// serialization, so its blocks are resident and waiting
-// (cudaGridDependencySynchronize) when its predecessor ends instead of being
-// launched only then.  That shortens the chain (the FP32 sphere's critical
-// path: 31.9 k -> 33.8 k MLUPS) but the waiting blocks hold SM slots the
-// far-region streaming beside them would use (FP16 sphere 40.7 k -> 38.9 k),
-// so the host enables it for FP32 storage only.
+// serialization: its launch is processed while its predecessor runs, and
+// its blocks wait (cudaGridDependencySynchronize) for that grid's results.
+// That shortens the chain, the FP32 sphere's critical path (31.9 k -> 34.5 k
+// MLUPS); with FP16 storage, where the far-region streaming beside the chain
+// is the critical path, it cost 3 % (40.7 k -> 39.6 k), so the host enables
+// it for FP32 only.  Triggering the next grid early from the top of each
+// kernel was worse for both (33.8 k, 38.9 k): its waiting blocks hold SM
+// slots.
 static cudaLaunchConfig_t pdl_config(dim3 grid, dim3 block, cudaStream_t s, cudaLaunchAttribute *attr, int pdl) {
     cudaLaunchConfig_t c = {};
     c.gridDim = grid;
