@@ -33,12 +33,19 @@ struct BatchProb {
     float lid;          // lid velocity along x
 };
 
+// tilexyz (optional): the (x, y | z << 16) of each tile's first cell, so a
+// thread finds its cell by stepping along the rows instead of dividing.  A
+// warp whose lanes all lie in rows off the y/z walls pulls plainly, the lanes
+// on x = 0 / x = nx-1 bouncing back their x-crossing links (every row of a
+// small cavity has two such lanes; a divergent boundary branch for them made
+// every warp run both paths); warps touching a y/z wall take the per-link
+// path.
 template <class T, bool EXPORT>
 __global__ void __launch_bounds__(512) k_batch_step(const T *__restrict__ A, T *__restrict__ B,
                                                     const BatchProb *__restrict__ probs,
                                                     const int2 *__restrict__ tiles, long long ntiles, int tile_cells,
                                                     int gather, uint32_t *__restrict__ status,
-                                                    float *__restrict__ mom) {
+                                                    float *__restrict__ mom, const int2 *__restrict__ tilexyz) {
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x) {
         const int2 tt = tiles[t];
         const BatchProb pr = probs[tt.x];
@@ -46,13 +53,48 @@ __global__ void __launch_bounds__(512) k_batch_step(const T *__restrict__ A, T *
         const bool valid = threadIdx.x < tile_cells && c < pr.N;
         const int nx = pr.nx, ny = pr.ny, nz = pr.nz;
         const int cc = valid ? (int)c : 0;
-        const int x = cc % nx, y = (cc / nx) % ny, z = cc / (nx * ny);
-        const bool bnd = x == 0 || x == nx - 1 || y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+        int x, y, z;
+        if (tilexyz) {
+            const int2 o = tilexyz[t];
+            x = o.x + (int)threadIdx.x;
+            y = o.y & 0xffff;
+            z = o.y >> 16;
+            while (x >= nx) {
+                x -= nx;
+                if (++y == ny) {
+                    y = 0;
+                    z++;
+                }
+            }
+            if (!valid) x = y = z = 0;
+        } else {
+            x = cc % nx;
+            y = (cc / nx) % ny;
+            z = cc / (nx * ny);
+        }
+        const bool yzb = y == 0 || y == ny - 1 || z == 0 || z == nz - 1;
+        const bool bnd = yzb || x == 0 || x == nx - 1;
+        const bool wyz = __any_sync(0xffffffffu, valid && yzb);
         const T *a = A + pr.base + cc;
         float f[Q];
         if (!gather) {
 #pragma unroll
             for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + l * pr.S) : 0.0f;
+        } else if (!wyz) {
+            // rows off the y/z walls; x-face lanes bounce their x-crossing
+            // links off the side walls (no lid there)
+            // (the plain pull of an x-crossing link reads the neighbouring row's
+            // end cell of the same population: inside the cavity's arrays,
+            // since the cell's y and z are interior; then replaced)
+#pragma unroll
+            for (int l = 0; l < Q; l++)
+                f[l] = valid ? St<T>::ld(a + l * pr.S - (cx(l) + nx * (cy(l) + ny * cz(l)))) : 0.0f;
+            if (valid && (x == 0 || x == nx - 1)) {
+                const bool xlo = x == 0;
+#pragma unroll
+                for (int l = 0; l < Q; l++)
+                    if ((cx(l) > 0 && xlo) || (cx(l) < 0 && !xlo)) f[l] = St<T>::ld(a + opp(l) * pr.S);
+            }
         } else if (!bnd) {
 #pragma unroll
             for (int l = 0; l < Q; l++)
@@ -79,7 +121,11 @@ __global__ void __launch_bounds__(512) k_batch_step(const T *__restrict__ A, T *
         const float rho = 1.0f + drho;
         const float inv = inv_one_plus(drho);
         const float ux = jx * inv, uy = jy * inv, uz = jz * inv;
-        if (valid && !(rho > 0.0f && rho < 100.0f)) atomicOr(&status[tt.x], ST_RHO_RANGE);
+        // one status update per warp (a warp lies in one tile, so one
+        // cavity): a diverged cavity would otherwise send an atomic from
+        // every cell of every step
+        const unsigned badw = __ballot_sync(0xffffffffu, valid && !(rho > 0.0f && rho < 100.0f));
+        if (badw && (threadIdx.x & 31) == 0) atomicOr(&status[tt.x], ST_RHO_RANGE);
         if (EXPORT) {
             if (valid) {
                 mom[pr.mom_base + cc] = rho;
@@ -135,6 +181,7 @@ struct lbm_batch {
     long long mom_total = 0;
     uint32_t *status = nullptr;
     int2 *tiles = nullptr;
+    int2 *tilexyz = nullptr;  // first cell (x, y | z << 16) of each tile
     long long ntiles = 0;
     int tile_cells = 256;
     int grid = 0;
@@ -153,10 +200,10 @@ static cudaError_t batch_launch(lbm_batch *b, int gather, bool exp) {
     T *B = (T *)b->f[1 - b->cur];
     if (exp)
         k_batch_step<T, true><<<b->grid, b->tile_cells, 0, b->s>>>(A, B, b->dp, b->tiles, b->ntiles, b->tile_cells,
-                                                                  gather, b->status, b->mom);
+                                                                  gather, b->status, b->mom, b->tilexyz);
     else
         k_batch_step<T, false><<<b->grid, b->tile_cells, 0, b->s>>>(A, B, b->dp, b->tiles, b->ntiles, b->tile_cells,
-                                                                   gather, b->status, nullptr);
+                                                                   gather, b->status, nullptr, b->tilexyz);
     return cudaGetLastError();
 }
 
@@ -171,15 +218,30 @@ static cudaError_t batch_enqueue(lbm_batch *b, int gather, bool exp) {
 
 static lbm_status batch_set_shape(lbm_batch *b, int tile_cells, int grid) {
     // tile table for this tile size
-    std::vector<int2> t;
+    std::vector<int2> t, txyz;
     for (int p = 0; p < b->n; p++) {
-        long long nt = (b->hp[p].N + tile_cells - 1) / tile_cells;
-        for (long long k = 0; k < nt; k++) t.push_back(make_int2(p, (int)k));
+        const BatchProb &pr = b->hp[p];
+        long long nt = (pr.N + tile_cells - 1) / tile_cells;
+        for (long long k = 0; k < nt; k++) {
+            t.push_back(make_int2(p, (int)k));
+            const long long c0 = k * tile_cells;
+            const int x0 = (int)(c0 % pr.nx), y0 = (int)((c0 / pr.nx) % pr.ny), z0 = (int)(c0 / ((long long)pr.nx * pr.ny));
+            txyz.push_back(make_int2(x0, y0 | (z0 << 16)));
+        }
     }
     if (b->tiles) cudaFree(b->tiles);
+    if (b->tilexyz) cudaFree(b->tilexyz);
     b->tiles = nullptr;
+    b->tilexyz = nullptr;
     BCUDA(cudaMalloc(&b->tiles, t.size() * sizeof(int2)));
     BCUDA(cudaMemcpyAsync(b->tiles, t.data(), t.size() * sizeof(int2), cudaMemcpyHostToDevice, b->s));
+    // y and z each fit 16 bits (cavity edges are far below 65536)
+    bool fits = true;
+    for (int p = 0; p < b->n; p++) fits = fits && b->hp[p].ny < 65536 && b->hp[p].nz < 32768;
+    if (fits) {
+        BCUDA(cudaMalloc(&b->tilexyz, txyz.size() * sizeof(int2)));
+        BCUDA(cudaMemcpyAsync(b->tilexyz, txyz.data(), txyz.size() * sizeof(int2), cudaMemcpyHostToDevice, b->s));
+    }
     b->ntiles = (long long)t.size();
     b->tile_cells = tile_cells;
     b->grid = grid;
@@ -271,6 +333,7 @@ extern "C" lbm_status lbmgpu_batch_destroy(lbm_batch *b) {
     cudaFree(b->status);
     cudaFree(b->dp);
     cudaFree(b->tiles);
+    cudaFree(b->tilexyz);
     if (b->s) cudaStreamDestroy(b->s);
     delete b;
     return LBM_OK;
@@ -508,17 +571,18 @@ extern "C" lbm_status lbmgpu_batch_step_noalloc(int n, const int *dims, const do
         switch (storage) {
         case 0:
             k_batch_step<float, false><<<grid, kNoAllocTile, 0, s>>>((const float *)A, (float *)B, sc->prob, sc->tiles,
-                                                                      ntiles, kNoAllocTile, gather, sc->status, nullptr);
+                                                                      ntiles, kNoAllocTile, gather, sc->status, nullptr,
+                                                                      nullptr);
             break;
         case 1:
             k_batch_step<__half, false><<<grid, kNoAllocTile, 0, s>>>((const __half *)A, (__half *)B, sc->prob,
                                                                        sc->tiles, ntiles, kNoAllocTile, gather,
-                                                                       sc->status, nullptr);
+                                                                       sc->status, nullptr, nullptr);
             break;
         default:
             k_batch_step<__nv_bfloat16, false><<<grid, kNoAllocTile, 0, s>>>(
                 (const __nv_bfloat16 *)A, (__nv_bfloat16 *)B, sc->prob, sc->tiles, ntiles, kNoAllocTile, gather,
-                sc->status, nullptr);
+                sc->status, nullptr, nullptr);
         }
         BCUDA(cudaGetLastError());
     }
