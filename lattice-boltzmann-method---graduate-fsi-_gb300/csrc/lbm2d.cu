@@ -42,6 +42,15 @@ constexpr double kRefPi = 3.14159265;  // the reference's truncated PI (LBM.h:74
 // ---------------------------------------------------------------------------
 // Collide-stream
 // ---------------------------------------------------------------------------
+// One status update per warp from the lanes still running (the step
+// kernels let lanes past the grid edge leave early): a diverged solve would
+// otherwise send an atomic from every cell.
+__device__ __forceinline__ void status_once(uint32_t *status, uint32_t bit, bool bad) {
+    const unsigned am = __activemask();
+    const unsigned b = __ballot_sync(am, bad);
+    if (b && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) atomicOr(status, bit);
+}
+
 template <class T>
 __device__ __forceinline__ float pull_link2(const T *__restrict__ A, int l, int x, int y, long long cell,
                                             const Class2 &ce, const Params2 &P) {
@@ -148,7 +157,7 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     // (LBM::Init, lbm.cpp:31-57); MacroProp adds F/2 afterwards (lbm.cpp:677-679)
     const float hf = gather ? 0.5f : 0.0f;
     const float ux = (jx + hf * Fx) * inv, uy = (jy + hf * Fy) * inv;
-    if (!(rho > 0.0f && rho < 100.0f)) atomicOr(&ds->status, lbmk::ST_RHO_RANGE);
+    status_once(&ds->status, lbmk::ST_RHO_RANGE, !(rho > 0.0f && rho < 100.0f));
     if (mom != nullptr) {
         mom[cell] = rho;
         mom[P.N + cell] = ux;
@@ -339,8 +348,8 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
     const float hf = gather ? 0.5f : 0.0f;
     const float ux = (jx + hf * Fx) * inv, uy = (jy + hf * Fy) * inv;
     const float Tc = E.T_ref + dT;
-    if (!(rho > 0.0f && rho < 100.0f)) atomicOr(&ds->status, lbmk::ST_RHO_RANGE);
-    if (!(Tc > 0.0f && Tc < 100.0f)) atomicOr(&ds->status, lbmk::ST_T_RANGE);
+    status_once(&ds->status, lbmk::ST_RHO_RANGE, !(rho > 0.0f && rho < 100.0f));
+    status_once(&ds->status, lbmk::ST_T_RANGE, !(Tc > 0.0f && Tc < 100.0f));
     if (mom != nullptr) {
         mom[cell] = rho;
         mom[P.N + cell] = ux;
