@@ -99,6 +99,9 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
                                                 const __grid_constant__ Params2 P, State2 *__restrict__ ds,
                                                 float *__restrict__ mom, float *__restrict__ band, int gather,
                                                 int export_only, int drift) {
+    // launched behind the previous step's IBM pass (programmatic dependent
+    // launch): wait for its results first
+    cudaGridDependencySynchronize();
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y * blockDim.y + threadIdx.y;
     if (x >= P.nx || y >= P.ny) return;
@@ -685,6 +688,8 @@ template <class T>
 __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __grid_constant__ Params2 P,
                                                      State2 *__restrict__ st, Ibm2 ib, float *__restrict__ band) {
     extern __shared__ float smem[];
+    // launched behind the collide-stream grid (programmatic dependent launch)
+    cudaGridDependencySynchronize();
     const int tid = threadIdx.x, nt = blockDim.x;
     const int n = ib.n;
     const long long nb = P.nb;
@@ -1279,6 +1284,22 @@ void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16]
     }
 }
 
+// The two launches of a D2Q9 step (collide-stream, IBM pass) go out with
+// programmatic stream serialization: each launch is processed while its
+// predecessor runs and its grid waits at cudaGridDependencySynchronize.
+cudaLaunchConfig_t pdl_config2(dim3 grid, dim3 block, size_t smem, cudaStream_t s, cudaLaunchAttribute *attr) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = grid;
+    c.blockDim = block;
+    c.dynamicSmemBytes = smem;
+    c.stream = s;
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = attr;
+    c.numAttrs = 1;
+    return c;
+}
+
 // The streaming of step s (the gather of the launch made with s steps done)
 // sees the walls moving at F/2 from s = 3 on when wall_force is set: the
 // walls' force is set by the first MacroProp and enters their velocity at
@@ -1318,9 +1339,12 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
     void *B = d->f[1 - d->cur];
     const bool forced = d->P.forced != 0, solid = d->P.links != nullptr;
     const int drift = wall_drift(h, gather);
+    cudaLaunchAttribute attr[1];
+    const cudaLaunchConfig_t lc = pdl_config2(grid, block, 0, h->s, attr);
+    cudaError_t e = cudaSuccess;
 #define L2D_LAUNCH(T, FO, SO)                                                                                  \
-    k_step2d<T, FO, SO><<<grid, block, 0, h->s>>>((const T *)A, (T *)B, d->P, d->st, mom, d->band, gather,    \
-                                                 export_only, drift)
+    e = cudaLaunchKernelEx(&lc, k_step2d<T, FO, SO>, (const T *)A, (T *)B, d->P, d->st, mom, d->band, gather, \
+                           export_only, drift)
 #define L2D_STEP(T)                                                                                             \
     if (solid) {                                                                                              \
         if (forced) L2D_LAUNCH(T, true, true);                                                                \
@@ -1336,7 +1360,7 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
     }
 #undef L2D_STEP
 #undef L2D_LAUNCH
-    return cudaGetLastError();
+    return e;
 }
 
 cudaError_t launch_ibm2d(lbm_handle *h) {
@@ -1344,14 +1368,14 @@ cudaError_t launch_ibm2d(lbm_handle *h) {
     void *B = d->f[1 - d->cur];
     const size_t sm = d->ib.fast ? ibm2d_fast_smem_bytes(d->P.nb, d->ib.n)
                                  : (d->ib.smem ? ibm2d_smem_bytes(d->P.nb, d->ib.n) : 0);
+    cudaLaunchAttribute attr[1];
+    cudaLaunchConfig_t c = pdl_config2(dim3(1), dim3(kIbmBlock), sm, h->s, attr);
     switch (h->cfg.storage) {
-    case LBM_STORE_F16: k_ibm2d<__half><<<1, kIbmBlock, sm, h->s>>>((__half *)B, d->P, d->st, d->ib, d->band); break;
+    case LBM_STORE_F16: return cudaLaunchKernelEx(&c, k_ibm2d<__half>, (__half *)B, d->P, d->st, d->ib, d->band);
     case LBM_STORE_BF16:
-        k_ibm2d<__nv_bfloat16><<<1, kIbmBlock, sm, h->s>>>((__nv_bfloat16 *)B, d->P, d->st, d->ib, d->band);
-        break;
-    default: k_ibm2d<float><<<1, kIbmBlock, sm, h->s>>>((float *)B, d->P, d->st, d->ib, d->band); break;
+        return cudaLaunchKernelEx(&c, k_ibm2d<__nv_bfloat16>, (__nv_bfloat16 *)B, d->P, d->st, d->ib, d->band);
+    default: return cudaLaunchKernelEx(&c, k_ibm2d<float>, (float *)B, d->P, d->st, d->ib, d->band);
     }
-    return cudaGetLastError();
 }
 
 // Opt the IBM kernel of this storage into the shared memory it needs.
