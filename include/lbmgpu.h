@@ -44,7 +44,7 @@ typedef enum lbm_status {
     LBM_ERR_DIVERGED = 4,    /* device status word reports an invalid state */
     LBM_ERR_TIMEOUT = 5,     /* a bounded device wait gave up */
     LBM_ERR_STATE = 6,       /* call out of order (e.g. step before init) */
-    LBM_ERR_UNSUPPORTED = 7  /* geometry this build does not handle */
+    LBM_ERR_UNSUPPORTED = 7  /* a set-up or option the library does not handle */
 } lbm_status;
 
 /* Population storage formats.  F16/BF16 store f - w (shifted) and compute in FP32. */
