@@ -1,6 +1,6 @@
 """FP64 CPU oracle for the LBM hot path (test infrastructure only).
 
-This package is the correctness checker.  The CUDA product path never imports
+This package is the test oracle the GPU results are compared with.  The CUDA product path never imports
 it; only ``tests/``, ``__graft_entry__.smoke()`` and the ``cpu_baseline`` /
 ``--impl reference`` legs of ``bench.py`` use it.
 

@@ -4,7 +4,7 @@
  * TEST INFRASTRUCTURE ONLY.  This file is the correctness oracle: the CUDA
  * product path never links, loads or calls it.  Only tests/, the smoke check
  * in __graft_entry__.py and the cpu_baseline leg of bench.py use it, and only
- * as the checker (or as the timed CPU baseline).
+ * as the reference results are compared with (or as the timed CPU baseline).
  *
  * It restates, in plain C over flat arrays, the algorithm of the reference
  * solver (DestinyFlow01/Lattice-Boltzmann-Method---Graduate-FSI-):
