@@ -1,12 +1,10 @@
 """GPU parity: the fused collide-stream kernel through the C ABI against the
 FP64 oracle and the reference's own golden output (lid-driven cavity).
 
-Tolerance: plain FP32 fields within 1e-5 of the lid velocity U for the short
-runs.  On the 64^3, 5000-step cavity the FP32 error against the reference's
-FP64 run saturates at 1.13e-5 U (max over the mid planes; the mean is 2e-6 U),
-from FP32 rounding accumulated over the ~4e4-step viscous time of the vortex
-core, so that case is bounded at 1.5e-5 U.  FP16/BF16 shifted-population
-storage errors are measured and bounded (FP16 1.5e-3 U, BF16 2e-2 U)."""
+Tolerance: plain FP32 fields within 1e-5 of the lid velocity U, also on the
+64^3, 5000-step cavity against the reference's own FP64 run (measured there:
+3.1e-6 U, max over the mid planes).  FP16/BF16 shifted-population storage
+errors are measured and bounded (FP16 1.5e-3 U, BF16 2e-2 U)."""
 import os
 
 import numpy as np
@@ -62,7 +60,7 @@ def test_cavity64_5000_vs_reference_golden(pkg):
         res[st] = (e[0], e[1:].max() / lid)
         s.close()
     print("cavity64 errors (rho abs, u / U):", res)
-    assert res["f32"][0] < TOL_F32 and res["f32"][1] < 1.5e-5
+    assert res["f32"][0] < TOL_F32 and res["f32"][1] < TOL_F32
     assert res["f16"][1] < 1.5e-3
     assert res["bf16"][1] < 2e-2
 
