@@ -111,6 +111,11 @@ typedef struct lbm_config {
                              Poiseuille_Flow MacroProp sets it on every cell (lbm.cpp:800-801); the walls
                              then report u_w + F/2 and bounce back as moving walls from the third
                              streaming on */
+    int cells_per_thread; /* D3Q19 fused step: consecutive x-cells per thread, moved as one 4-, 8- or
+                             16-byte access per population row and updated in pairs with the packed FP32
+                             instructions (FP16/BF16: 2, 4 or 8; FP32: 2 or 4); 0 = default (2 for
+                             FP16/BF16, 1 for FP32); 1 = one cell per thread.  Needs nx a multiple of it,
+                             else one cell per thread is used.  Results are identical either way. */
 } lbm_config;
 
 /* lbm_config.thermal: 0 none; 1 a D3Q7 temperature population with a heat
@@ -377,6 +382,9 @@ lbm_status lbmgpu_status(lbm_handle *h, uint32_t *flags);
 lbm_status lbmgpu_sync(lbm_handle *h);
 lbm_status lbmgpu_steps_done(lbm_handle *h, long long *steps);
 lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes);
+/* x-cells per thread the fused step uses on this handle (lbm_config.cells_per_thread after the
+ * lattice and storage checks; 1 = one cell per thread).  No counterpart in the reference. */
+lbm_status lbmgpu_cells_per_thread(lbm_handle *h, int *cells);
 
 /* Page-locked host buffers for fast host<->device copies. */
 lbm_status lbmgpu_host_alloc(size_t bytes, void **ptr);

@@ -52,7 +52,7 @@ ABI_SYMBOLS = [
     "lbmgpu_set_more_details", "lbmgpu_download_details", "lbmgpu_sup_macroprop", "lbmgpu_download_stats",
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
     "lbmgpu_config_energy_2d", "lbmgpu_mea_box", "lbmgpu_nusselt", "lbmgpu_download_all_f32_async",
-    "lbmgpu_download_wait", "lbmgpu_update_markers",
+    "lbmgpu_download_wait", "lbmgpu_update_markers", "lbmgpu_cells_per_thread",
 ]
 
 
@@ -68,7 +68,8 @@ class Config(C.Structure):
                 ("T_init", C.c_double), ("T_ref", C.c_double), ("gbeta", C.c_double * 3),
                 ("block_x", C.c_int), ("block_y", C.c_int), ("graph_steps", C.c_int), ("staged", C.c_int),
                 ("ibm_overlap", C.c_int),
-                ("xface", C.c_int), ("lattice", C.c_int), ("cp", C.c_double), ("wall_force", C.c_int)]
+                ("xface", C.c_int), ("lattice", C.c_int), ("cp", C.c_double), ("wall_force", C.c_int),
+                ("cells_per_thread", C.c_int)]
 
 
 class IbmConfig(C.Structure):
@@ -140,6 +141,7 @@ def load(path: str | None = None):
     L.lbmgpu_sync.argtypes = [vp]
     L.lbmgpu_steps_done.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.lbmgpu_device_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.lbmgpu_cells_per_thread.argtypes = [vp, C.POINTER(C.c_int)]
     L.lbmgpu_host_alloc.argtypes = [C.c_size_t, C.POINTER(vp)]
     L.lbmgpu_host_free.argtypes = [vp]
     L.lbmgpu_batch_create.argtypes = [i, C.POINTER(C.c_int), dp, d, i, C.POINTER(vp)]
@@ -195,7 +197,7 @@ def _dp(a: np.ndarray):
 
 def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0.0, 0.0), body=(0.0, 0.0, 0.0),
                 thermal=False, tau_g=0.0, T_init=0.0, T_ref=0.0, gbeta=(0.0, 0.0, 0.0), block=(0, 0),
-                graph_steps=0, staged=0, ibm_overlap=0, xface=0) -> Config:
+                graph_steps=0, staged=0, ibm_overlap=0, xface=0, cells=0) -> Config:
     c = Config()
     c.nx, c.ny, c.nz, c.tau = nx, ny, nz, tau
     c.storage = STORAGE[storage] if isinstance(storage, str) else storage
@@ -219,6 +221,7 @@ def make_config(nx, ny, nz, tau, storage="f32", faces=None, rho0=1.0, u0=(0.0, 0
     c.staged = staged
     c.ibm_overlap = ibm_overlap
     c.xface = xface
+    c.cells_per_thread = cells
     return c
 
 
@@ -458,6 +461,12 @@ class Solver:
     def device_bytes(self) -> int:
         v = C.c_size_t()
         check(self.L.lbmgpu_device_bytes(self.h, C.byref(v)))
+        return v.value
+
+    def cells_per_thread(self) -> int:
+        """x-cells per thread of the fused step on this solve (1: one cell per thread)."""
+        v = C.c_int()
+        check(self.L.lbmgpu_cells_per_thread(self.h, C.byref(v)))
         return v.value
 
 

@@ -8,6 +8,7 @@
 #include <cstring>
 #include <string>
 #include <cstddef>
+#include <numeric>
 #include <vector>
 
 #include "../../include/lbmgpu.h"
@@ -135,6 +136,56 @@ static void build_classes(const lbm_config &c, StepParams &P) {
             }
         }
         P.cls[cls] = e;
+    }
+}
+
+// The x-face table (XFix) of rows off the y/z faces: what the boundary-class
+// rule of pull_link / pull_heat_link gives for the five x-crossing links of a
+// cell on x = 0 (face 0) and x = nx-1 (face 1), as an offset from the cell,
+// a factor and a constant.
+static void build_xfix(StepParams &P) {
+    const int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
+    for (int f = 0; f < 2; f++) {
+        XFix &xf = P.xf[f];
+        memset(&xf, 0, sizeof(xf));
+        const ClassEntry &ce = P.cls[(f == 0 ? 1 : 2) & ~pm];
+        const int x = f == 0 ? 0 : P.nx - 1;
+        auto pull_ofs = [&](int l) -> long long {
+            int sx = x - cx(l);
+            if (P.periodic & 1) sx = sx < 0 ? sx + P.nx : (sx >= P.nx ? sx - P.nx : sx);
+            if ((ce.zg >> l) & 1u) sx = std::min(std::max(sx, 0), P.nx - 1);
+            return (long long)l * P.S + (sx - x) - (long long)P.nx * (cy(l) + (long long)P.ny * cz(l));
+        };
+        for (int k = 0; k < 5; k++) {
+            const int l = f == 0 ? lbmk::xpl(k) : lbmk::xml(k);
+            if ((ce.bb >> l) & 1u) {
+                xf.ofs[k] = (unsigned)((long long)opp(l) * P.S);
+                xf.sgn[k] = 1.0f;
+                xf.add[k] = ce.val[l];
+            } else if ((ce.eq >> l) & 1u) {
+                xf.eq |= 1u << k;
+                xf.ofs[k] = (unsigned)((long long)l * P.S);
+                xf.add[k] = ce.val[l];
+            } else {
+                xf.ofs[k] = (unsigned)pull_ofs(l);
+                xf.sgn[k] = 1.0f;
+                xf.add[k] = 0.0f;
+            }
+        }
+        const int lt = f == 0 ? 1 : 2;  // the D3Q7 link across this face
+        if ((ce.bb >> lt) & 1u) {
+            const bool dir = (ce.tdir >> lt) & 1u;
+            xf.tofs = (unsigned)((long long)opp(lt) * P.S);
+            xf.tsgn = dir ? -1.0f : 1.0f;
+            xf.tadd = dir ? ce.tval[lt] : 0.0f;
+        } else if ((ce.eq >> lt) & 1u) {
+            xf.teq = 1;
+            xf.tofs = (unsigned)((long long)lt * P.S);
+            xf.tadd = ce.tval[lt];
+        } else {
+            xf.tofs = (unsigned)pull_ofs(lt);
+            xf.tsgn = 1.0f;
+        }
     }
 }
 
@@ -368,10 +419,19 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     for (int l = 0; l < Q; l++) {
         P.pofs32[l] = P.idx32 ? (unsigned)P.pofs[l] : 0u;
         P.sofs32[l] = P.idx32 ? (unsigned)((long long)l * P.S) : 0u;
+        P.rofs32[l] = P.idx32 ? (unsigned)((long long)l * P.S - (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l)))
+                              : 0u;
     }
     // x-face lanes fix their own x-crossing links: warps stay on the plain
     // pull in every row that is not on a y/z face
     P.xface = (c.xface >= 0 && P.nx >= 2 && P.ny >= 3 && P.nz >= 3) ? 1 : 0;
+    if (P.idx32) build_xfix(P);
+    {
+        // two x-cells per thread (packed pair arithmetic) for FP16/BF16 storage;
+        // one for FP32, which is memory-bound with one cell per thread
+        const int v = c.cells_per_thread > 0 ? c.cells_per_thread : (c.storage == LBM_STORE_F32 ? 1 : 2);
+        h->vcells = (v > 1 && lbmk::step_vec_usable(c.storage, P, v)) ? v : 0;
+    }
     const size_t fb = ((size_t)Q * P.S + 2 * kGuard) * h->esize;
     for (int i = 0; i < 2 && st == LBM_OK; i++) {
         chk(dalloc(h, &h->fraw[i], fb), "populations");
@@ -542,7 +602,10 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     // near box: the band grown by the one-cell pull stencil, rounded out to
     // whole tiles of the staged kernel in x and y
     {
-        const int tile[3] = {h->tile_x, h->tile_y, 1};
+        // (and to whole row segments of the multi-cell kernel)
+        int tx = h->tile_x;
+        if (h->vcells > 1 && tx % h->vcells != 0) tx = tx * h->vcells / std::gcd(tx, h->vcells);
+        const int tile[3] = {tx, h->tile_y, 1};
         for (int a = 0; a < 3; a++) {
             int lo = std::max(0, org[a] - 1), hi = std::min(dims[a], org[a] + bs[a] + 1);
             lo = (lo / tile[a]) * tile[a];
@@ -651,6 +714,7 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.st = &h->stp;
     a.buf_a = h->cur;
     a.stream = h->s;
+    a.vcells = h->solids ? 0 : h->vcells;
     return a;
 }
 
@@ -1175,6 +1239,12 @@ extern "C" lbm_status lbmgpu_steps_done(lbm_handle *h, long long *steps) {
 extern "C" lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes) {
     if (!h || !bytes) return fail(LBM_ERR_INVALID, "device_bytes: null argument");
     *bytes = h->dev_bytes;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_cells_per_thread(lbm_handle *h, int *cells) {
+    if (!h || !cells) return fail(LBM_ERR_INVALID, "cells_per_thread: null argument");
+    *cells = (h->d2 || h->solids || h->stp.enabled || h->vcells <= 1) ? 1 : h->vcells;
     return LBM_OK;
 }
 

@@ -34,6 +34,16 @@ __host__ __device__ constexpr int opp(int l) {
     constexpr int v[19] = {0, 2, 1, 4, 3, 6, 5, 8, 7, 10, 9, 12, 11, 14, 13, 16, 15, 18, 17};
     return v[l];
 }
+// The links with c_x = +1 (xpl) and c_x = -1 (xml), in link order: the five
+// links a cell on x = 0, respectively x = nx-1, pulls across its x face.
+__host__ __device__ constexpr int xpl(int k) {
+    constexpr int v[5] = {1, 7, 9, 13, 15};
+    return v[k];
+}
+__host__ __device__ constexpr int xml(int k) {
+    constexpr int v[5] = {2, 8, 10, 14, 16};
+    return v[k];
+}
 __host__ __device__ constexpr float wf(int l) {
     return l == 0 ? (1.0f / 3.0f) : (l < 7 ? (1.0f / 18.0f) : (1.0f / 36.0f));
 }
@@ -78,6 +88,23 @@ struct ClassEntry {
     float tval[QT];   // thermal: eq: geq(face);  tdir: 2 w T_wall
 };
 
+// The five x-crossing links of a cell on x = 0 (face 0: links with c_x = +1)
+// or x = nx-1 (face 1: c_x = -1) in a row off the y/z faces, as the
+// boundary-class rule resolves them for that face: value = add (an
+// equilibrium ghost, bit k of eq) or sgn * A[cell + ofs] + add, rounded
+// once (bounce-back: the cell's own opposite population plus the wall term;
+// a periodic or zero-gradient pull: the wrapped or clamped source, add 0).
+// The D3Q7 link of the face likewise (t*).
+struct XFix {
+    unsigned ofs[5];
+    float sgn[5];
+    float add[5];
+    unsigned eq;
+    unsigned tofs;
+    float tsgn, tadd;
+    int teq;
+};
+
 // Per-launch parameters, passed by value as a __grid_constant__.
 struct StepParams {
     int nx, ny, nz;
@@ -87,6 +114,7 @@ struct StepParams {
     long long pofs[Q];     // l * S - (cx + nx (cy + ny cz)): pull offset of link l from the cell
     unsigned pofs32[Q];    // the same as 32-bit words when idx32 (never negative)
     unsigned sofs32[Q];    // l * S as 32-bit words when idx32
+    unsigned rofs32[Q];    // l * S - nx (cy + ny cz): the source row of link l, same x (when idx32)
     int idx32;             // 19 S < 2^31 and a safe cell exists: 32-bit element indices
     unsigned safe_cell;    // a cell whose whole pull stencil is inside the lattice: idle
                            // lanes load from it instead of being predicated off
@@ -106,6 +134,7 @@ struct StepParams {
     const uint32_t *solid;  // bit per interior cell: stationary solid (bounce-back on its links)
     const uint32_t *nearw;  // bit per interior cell: a solid, or a neighbour of one
     float *mea;             // per-block momentum-exchange partial sums [blocks][3], or null
+    XFix xf[2];             // x-face links of interior rows (when idx32)
     ClassEntry cls[64];
 };
 

@@ -48,6 +48,7 @@ struct lbm_handle {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;
     int tx = 128, ty = 2;
+    int vcells = 0;                       // x-cells per thread of gather steps (k_stepv), 0 = k_step
     StagedPlan stp;                       // staged (bulk-copy) step kernel
     // interior solid cells and their momentum exchange
     bool solids = false;

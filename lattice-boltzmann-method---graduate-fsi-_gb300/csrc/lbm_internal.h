@@ -40,9 +40,14 @@ struct LaunchArgs {
     int buf_a;             // index of the population buffer read (A)
     cudaStream_t stream;
     int pdl = 0;           // band collision: programmatic dependent launch behind the IBM chain
+    int vcells = 0;        // > 1: gather steps use k_stepv with this many x-cells per thread
 };
 
 cudaError_t launch_step(int storage, const LaunchArgs &a);
+// k_stepv (lbm_stepv.cu): whether it can run this lattice with vcells cells
+// per thread, and its launcher.
+bool step_vec_usable(int storage, const StepParams &P, int vcells);
+cudaError_t launch_step_vec(int storage, const LaunchArgs &a);
 cudaError_t plan_staged(int storage, bool thermal, const StepParams &P, void *const f[2], void *const g[2],
                         StagedPlan &sp);
 cudaError_t launch_staged(int storage, const LaunchArgs &a);

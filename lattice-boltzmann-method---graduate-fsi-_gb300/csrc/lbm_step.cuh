@@ -29,6 +29,18 @@ __device__ __forceinline__ float pull_link(const T *__restrict__ A, int l, int x
     return St<T>::ld(A + l * P.S + sx + (long long)P.nx * (sy + (long long)P.ny * sz));
 }
 
+// Link k of the x-face table (XFix) for the cell at 32-bit index c.
+template <class T>
+__device__ __forceinline__ float xfix_link(const T *__restrict__ A, unsigned c, const XFix &xf, int k) {
+    const float v = St<T>::ld(A + (c + xf.ofs[k]));
+    return ((xf.eq >> k) & 1u) ? xf.add[k] : __fmaf_rn(xf.sgn[k], v, xf.add[k]);
+}
+template <class T>
+__device__ __forceinline__ float xfix_heat(const T *__restrict__ G, unsigned c, const XFix &xf) {
+    const float v = St<T>::ld(G + (c + xf.tofs));
+    return xf.teq ? xf.tadd : __fmaf_rn(xf.tsgn, v, xf.tadd);
+}
+
 __device__ __forceinline__ int periodic_mask(const StepParams &P) {
     return ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
 }
@@ -58,11 +70,24 @@ __device__ __forceinline__ void gather_flow(const T *__restrict__ A, float f[Q],
             for (int l = 0; l < Q; l++) f[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
         }
         if (raw_cls & 3) {
-            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+            if (P.idx32) {
+                // the x-face table: the same values, without per-link branches
+                const unsigned c = (unsigned)cell;
+                if (raw_cls & 1) {
 #pragma unroll
-            for (int l = 1; l < Q; l++) {
-                if (cx(l) > 0 && (raw_cls & 1)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
-                if (cx(l) < 0 && (raw_cls & 2)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+                    for (int k = 0; k < 5; k++) f[xpl(k)] = xfix_link<T>(A, c, P.xf[0], k);
+                }
+                if (raw_cls & 2) {
+#pragma unroll
+                    for (int k = 0; k < 5; k++) f[xml(k)] = xfix_link<T>(A, c, P.xf[1], k);
+                }
+            } else {
+                const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+#pragma unroll
+                for (int l = 1; l < Q; l++) {
+                    if (cx(l) > 0 && (raw_cls & 1)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+                    if (cx(l) < 0 && (raw_cls & 2)) f[l] = pull_link<T>(A, l, x, y, z, cell, ce, P);
+                }
             }
         }
         return;
@@ -109,11 +134,16 @@ __device__ __forceinline__ void gather_heat(const T *__restrict__ G, float g[QT]
 #pragma unroll
         for (int l = 0; l < QT; l++) g[l] = valid ? St<T>::ld(a + P.pofs[l]) : 0.0f;
         if (raw_cls & 3) {
-            const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
+            if (P.idx32) {
+                if (raw_cls & 1) g[1] = xfix_heat<T>(G, (unsigned)cell, P.xf[0]);
+                if (raw_cls & 2) g[2] = xfix_heat<T>(G, (unsigned)cell, P.xf[1]);
+            } else {
+                const ClassEntry &ce = P.cls[raw_cls & 3 & ~periodic_mask(P)];
 #pragma unroll
-            for (int l = 1; l < QT; l++) {
-                if (cx(l) > 0 && (raw_cls & 1)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
-                if (cx(l) < 0 && (raw_cls & 2)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+                for (int l = 1; l < QT; l++) {
+                    if (cx(l) > 0 && (raw_cls & 1)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+                    if (cx(l) < 0 && (raw_cls & 2)) g[l] = pull_heat_link<T>(G, l, x, y, z, cell, ce, P);
+                }
             }
         }
         return;
@@ -180,6 +210,43 @@ __device__ __forceinline__ void gather_solid(const T *__restrict__ A, const T *_
     }
 }
 
+// Moments, force and velocity of one cell (F = float) or of two neighbouring
+// cells (F = float2): the part of the update every step kernel shares.
+// Body force plus Boussinesq buoyancy F = Fb + gbeta (T - T0); velocity
+// u = (j + hf F) / rho, hf = 1/2 once the populations have been streamed
+// (MacroProp, lbm.cpp:677-679) and 0 before the first streaming, when the
+// reference collides with the velocity stored at set-up (LBM::Init,
+// lbm.cpp:31-57).
+template <class F, bool THERMAL, bool FORCED>
+__device__ __forceinline__ void cell_state(const F f[Q], const F g[QT], const StepParams &P, float hf, F &drho,
+                                           F &ux, F &uy, F &uz, F &Fx, F &Fy, F &Fz, F &Tc) {
+    using A = Ar<F>;
+    F jx, jy, jz;
+    moments_pairs(f, drho, jx, jy, jz);
+    Fx = A::splat(P.body[0]);
+    Fy = A::splat(P.body[1]);
+    Fz = A::splat(P.body[2]);
+    Tc = A::splat(0.0f);
+    if constexpr (THERMAL) {
+        Tc = heat_sum(g);
+        const F dT = A::sub(Tc, A::splat(P.T0));
+        Fx = A::fma(A::splat(P.gbeta[0]), dT, Fx);
+        Fy = A::fma(A::splat(P.gbeta[1]), dT, Fy);
+        Fz = A::fma(A::splat(P.gbeta[2]), dT, Fz);
+    }
+    const F inv = inv_one_plus(drho);
+    if constexpr (FORCED) {
+        const F h = A::splat(hf);
+        ux = A::mul(A::fma(h, Fx, jx), inv);
+        uy = A::mul(A::fma(h, Fy, jy), inv);
+        uz = A::mul(A::fma(h, Fz, jz), inv);
+    } else {
+        ux = A::mul(jx, inv);
+        uy = A::mul(jy, inv);
+        uz = A::mul(jz, inv);
+    }
+}
+
 // Everything after the gather of one cell except the stores: moments,
 // optional moment output, then either the band hand-off (f, g keep the
 // pre-collision populations; the unforced moments go to the band arrays) or
@@ -190,26 +257,9 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
                                             DevState *__restrict__ ds, float *__restrict__ mom,
                                             float *__restrict__ band, bool check_band, bool frozen = false) {
     const long long N = P.N;
-    float drho, jx, jy, jz;
-    moments_pairs(f, drho, jx, jy, jz);
-    float Tc = 0.0f;
-    float Fx = P.body[0], Fy = P.body[1], Fz = P.body[2];
-    if (THERMAL) {
-#pragma unroll
-        for (int l = 0; l < QT; l++) Tc += g[l];
-        Fx += P.gbeta[0] * (Tc - P.T0);
-        Fy += P.gbeta[1] * (Tc - P.T0);
-        Fz += P.gbeta[2] * (Tc - P.T0);
-    }
-    const float rho = 1.0f + drho;
-    const float inv = inv_one_plus(drho);
-    // Before the first streaming the reference collides with the velocity
-    // stored at set-up (LBM::Init, lbm.cpp:31-57), i.e. without the F/2 shift
-    // that MacroProp applies afterwards (lbm.cpp:677-679).
-    const float hf = gather ? 0.5f : 0.0f;
-    const float ux = (jx + hf * Fx) * inv;
-    const float uy = (jy + hf * Fy) * inv;
-    const float uz = (jz + hf * Fz) * inv;
+    float drho, ux, uy, uz, Fx, Fy, Fz, Tc;
+    cell_state<float, THERMAL, FORCED>(f, g, P, gather ? 0.5f : 0.0f, drho, ux, uy, uz, Fx, Fy, Fz, Tc);
+    const float rho = __fadd_rn(1.0f, drho);
     // one status update per warp (every lane of the warp runs this): a
     // diverged solve would otherwise send an atomic from every cell
     const unsigned badw = __ballot_sync(0xffffffffu, valid && !(rho > 0.0f && rho < 100.0f));
@@ -256,8 +306,8 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
             return true;
         }
     }
-    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, FORCED, P.omega);
-    if (THERMAL) collide_heat(g, Tc, ux, uy, uz, 0.0f, P.omega_t);
+    collide_flow<float, FORCED>(f, drho, ux, uy, uz, Fx, Fy, Fz, P.omega);
+    if (THERMAL) collide_heat<float, false>(g, Tc, ux, uy, uz, 0.0f, P.omega_t);
     return true;
 }
 
@@ -321,7 +371,7 @@ __device__ __forceinline__ void band_collide_cell(T *__restrict__ B, T *__restri
         for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * P.S + cell);
         const float Qt = band[11 * nb + b];
         const float Tc = band[10 * nb + b] + 0.5f * Qt;
-        collide_heat(g, Tc, ux, uy, uz, Qt, P.omega_t);
+        collide_heat<float, true>(g, Tc, ux, uy, uz, Qt, P.omega_t);
 #pragma unroll
         for (int l = 0; l < QT; l++) St<T>::st(GB + l * P.S + cell, g[l]);
     }

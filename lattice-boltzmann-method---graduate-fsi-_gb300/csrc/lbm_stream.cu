@@ -197,6 +197,8 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
 cudaError_t launch_step(int storage, const LaunchArgs &a) {
     if (a.st && a.st->enabled && a.gather && !a.export_only && a.mom == nullptr && a.region != 2)
         return launch_staged(storage, a);
+    if (a.vcells > 1 && a.gather && !a.export_only && a.mom == nullptr && a.region != 2)
+        return launch_step_vec(storage, a);
     switch (storage) {
     case 0: return launch_step_t<float>(a);
     case 1: return launch_step_t<__half>(a);
