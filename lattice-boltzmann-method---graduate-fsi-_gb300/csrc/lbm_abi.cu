@@ -591,9 +591,12 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     if (fresh || nb != h->P.nb) {
         cudaFree(h->band);
         h->band = nullptr;
-        CUDA_TRY(dalloc(h, &h->band, (size_t)12 * nb * sizeof(float)));
-        CUDA_TRY(cudaMemsetAsync(h->band, 0, (size_t)12 * nb * sizeof(float), h->s));
+        // 12 FP32 arrays, then the 4 fixed-point force/heat accumulators
+        CUDA_TRY(dalloc(h, &h->band, (size_t)12 * nb * sizeof(float) + (size_t)4 * nb * sizeof(long long)));
+        CUDA_TRY(cudaMemsetAsync(h->band, 0, (size_t)12 * nb * sizeof(float) + (size_t)4 * nb * sizeof(long long),
+                                 h->s));
     }
+    h->P.bandq = reinterpret_cast<long long *>(h->band + (size_t)12 * nb);
     h->P.band_on = 1;
     h->P.bsx = bs[0];
     h->P.bsy = bs[1];
@@ -651,7 +654,8 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
             cudaDeviceGetAttribute(&max_persist, cudaDevAttrMaxPersistingL2CacheSize, dev) == cudaSuccess &&
             cudaDeviceGetAttribute(&max_win, cudaDevAttrMaxAccessPolicyWindowSize, dev) == cudaSuccess &&
             max_persist > 0 && max_win > 0) {
-            const size_t bytes = std::min<size_t>((size_t)12 * nb * sizeof(float), (size_t)max_win);
+            const size_t bytes =
+                std::min<size_t>((size_t)12 * nb * sizeof(float) + (size_t)4 * nb * sizeof(long long), (size_t)max_win);
             size_t cur = 0;
             cudaDeviceGetLimit(&cur, cudaLimitPersistingL2CacheSize);
             if (cur < bytes) cudaDeviceSetLimit(cudaLimitPersistingL2CacheSize, std::min<size_t>(bytes, max_persist));

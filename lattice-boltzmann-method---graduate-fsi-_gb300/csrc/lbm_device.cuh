@@ -130,6 +130,7 @@ struct StepParams {
     int bsx, bsy, bsz;     // band extent
     long long nb;          // bsx * bsy * bsz
     int nlo[3], nhi[3];    // near box of a fixed body: band grown by one cell, rounded out to tiles
+    long long *bandq;      // [4][nb] accumulated IBM force (x, y, z) and heat, fixed point (to_fx)
     // interior solid cells (staircase bodies), or null
     const uint32_t *solid;  // bit per interior cell: stationary solid (bounce-back on its links)
     const uint32_t *nearw;  // bit per interior cell: a solid, or a neighbour of one
@@ -167,6 +168,14 @@ __device__ __forceinline__ int cell_class(int x, int y, int z, const StepParams 
     int pm = ((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0) | ((P.periodic & 4) ? 48 : 0);
     return c & ~pm;
 }
+
+// The spreading accumulates in 64-bit fixed point: v * 2^44 (an exact
+// scaling) rounded to an integer, so the sum of a node's contributions is
+// the same in whatever order the atomics land; read back with one rounding
+// to FP32.  |v| stays far below 2^19 for any finite forcing.
+constexpr float kFxScale = 17592186044416.0f;  // 2^44
+__device__ __forceinline__ long long to_fx(float v) { return __float2ll_rn(v * kFxScale); }
+__device__ __forceinline__ float from_fx(long long q) { return __ll2float_rn(q) * (1.0f / kFxScale); }
 
 // 4-point Peskin delta, kernel(r) of lbm.cpp:1095-1102, in FP32.
 __device__ __forceinline__ float peskin(float r) {

@@ -108,11 +108,11 @@ __device__ __forceinline__ void interp_marker(int m, int lane, const StepParams 
             const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
             const float rho = 1.0f + band[q];
             const float hr = 0.5f / rho;
-            su += wgt * (band[nb + q] + hr * band[7 * nb + q]);
-            sv += wgt * (band[2 * nb + q] + hr * band[8 * nb + q]);
-            sw += wgt * (band[3 * nb + q] + hr * band[9 * nb + q]);
+            su += wgt * (band[nb + q] + hr * from_fx(P.bandq[q]));
+            sv += wgt * (band[2 * nb + q] + hr * from_fx(P.bandq[nb + q]));
+            sw += wgt * (band[3 * nb + q] + hr * from_fx(P.bandq[2 * nb + q]));
             if (first) sr += wgt * rho;
-            if (thermal) sT += wgt * (band[10 * nb + q] + 0.5f * band[11 * nb + q]);
+            if (thermal) sT += wgt * (band[10 * nb + q] + 0.5f * from_fx(P.bandq[3 * nb + q]));
         } else if (wgt != 0.0f) {
             edge = true;
         }
@@ -161,8 +161,10 @@ __device__ __forceinline__ void interp_marker(int m, int lane, const StepParams 
 }
 
 // Spreading of marker m (one warp): Ft(x) += F_m ds_m delta(x - X_m)
-// (lbm.cpp:1331-1360), float atomics into the band, with the stencil the
-// step's first interpolation stored.
+// (lbm.cpp:1331-1360), with the stencil the step's first interpolation
+// stored.  The contributions go into the band's 64-bit fixed-point
+// accumulators (to_fx): integer atomics, so every node's sum -- and the whole
+// solve -- is the same in whatever order the markers' warps run.
 __device__ __forceinline__ void spread_marker(int m, int lane, const StepParams &P, const MarkerDev &mk,
                                               const DevState *__restrict__ ds, float *__restrict__ band,
                                               int thermal) {
@@ -181,10 +183,11 @@ __device__ __forceinline__ void spread_marker(int m, int lane, const StepParams 
         if (wgt != 0.0f && (unsigned)bx < (unsigned)P.bsx && (unsigned)by < (unsigned)P.bsy &&
             (unsigned)bz < (unsigned)P.bsz) {
             const long long q = bx + (long long)P.bsx * (by + (long long)P.bsy * bz);
-            atomicAdd(&band[7 * nb + q], Fx * wgt);
-            atomicAdd(&band[8 * nb + q], Fy * wgt);
-            atomicAdd(&band[9 * nb + q], Fz * wgt);
-            if (thermal) atomicAdd(&band[11 * nb + q], Qm * wgt);
+            unsigned long long *acc = reinterpret_cast<unsigned long long *>(P.bandq);
+            atomicAdd(acc + q, (unsigned long long)to_fx(Fx * wgt));
+            atomicAdd(acc + nb + q, (unsigned long long)to_fx(Fy * wgt));
+            atomicAdd(acc + 2 * nb + q, (unsigned long long)to_fx(Fz * wgt));
+            if (thermal) atomicAdd(acc + 3 * nb + q, (unsigned long long)to_fx(Qm * wgt));
         }
     }
 }

@@ -303,6 +303,8 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
             band[9 * nb + b] = 0.0f;
             band[10 * nb + b] = Tc;
             band[11 * nb + b] = 0.0f;
+#pragma unroll
+            for (int k = 0; k < 4; k++) P.bandq[k * nb + b] = 0;
             return true;
         }
     }
@@ -341,7 +343,7 @@ __device__ __forceinline__ void finish_cell(float f[Q], float g[QT], int x, int 
 // T = T_unf + Qt / 2.
 template <class T, bool THERMAL>
 __device__ __forceinline__ void band_collide_cell(T *__restrict__ B, T *__restrict__ GB, const StepParams &P,
-                                                  const DevState *__restrict__ ds, const float *__restrict__ band,
+                                                  const DevState *__restrict__ ds, float *__restrict__ band,
                                                   float fsign, long long b) {
     const int bx = (int)(b % P.bsx);
     const int by = (int)((b / P.bsx) % P.bsy);
@@ -355,7 +357,12 @@ __device__ __forceinline__ void band_collide_cell(T *__restrict__ B, T *__restri
     for (int l = 0; l < Q; l++) f[l] = St<T>::ld(B + l * P.S + cell);
     const float drho = band[b];
     const float rho = 1.0f + drho;
-    const float ftx = band[7 * nb + b], fty = band[8 * nb + b], ftz = band[9 * nb + b];
+    const float ftx = from_fx(P.bandq[b]), fty = from_fx(P.bandq[nb + b]), ftz = from_fx(P.bandq[2 * nb + b]);
+    // the step's IBM force as FP32, for the VTK force density and the
+    // free body's internal-fluid momentum
+    band[7 * nb + b] = ftx;
+    band[8 * nb + b] = fty;
+    band[9 * nb + b] = ftz;
     const float ux = band[nb + b] + 0.5f * ftx / rho;
     const float uy = band[2 * nb + b] + 0.5f * fty / rho;
     const float uz = band[3 * nb + b] + 0.5f * ftz / rho;
@@ -369,7 +376,8 @@ __device__ __forceinline__ void band_collide_cell(T *__restrict__ B, T *__restri
         float g[QT];
 #pragma unroll
         for (int l = 0; l < QT; l++) g[l] = St<T>::ld(GB + l * P.S + cell);
-        const float Qt = band[11 * nb + b];
+        const float Qt = from_fx(P.bandq[3 * nb + b]);
+        band[11 * nb + b] = Qt;
         const float Tc = band[10 * nb + b] + 0.5f * Qt;
         collide_heat<float, true>(g, Tc, ux, uy, uz, Qt, P.omega_t);
 #pragma unroll

@@ -108,7 +108,7 @@ template <class T, bool THERMAL>
 __global__ void __launch_bounds__(64, 16) k_band_collide(T *__restrict__ B, T *__restrict__ GB,
                                                       const __grid_constant__ StepParams P,
                                                       const DevState *__restrict__ ds,
-                                                      const float *__restrict__ band, float fsign) {
+                                                      float *__restrict__ band, float fsign) {
     // the last spreading may still be running (programmatic dependent launch)
     cudaGridDependencySynchronize();
     const long long b = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -222,7 +222,7 @@ static cudaError_t launch_band_t(const LaunchArgs &a, float fsign) {
     c.attrs = attr;
     c.numAttrs = a.pdl ? 1 : 0;
     const DevState *ds = a.ds;
-    const float *band = a.band;
+    float *band = a.band;
     if (a.thermal) return cudaLaunchKernelEx(&c, k_band_collide<T, true>, (T *)a.B, (T *)a.GB, *a.P, ds, band, fsign);
     return cudaLaunchKernelEx(&c, k_band_collide<T, false>, (T *)a.B, (T *)nullptr, *a.P, ds, band, fsign);
 }
