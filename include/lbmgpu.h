@@ -158,6 +158,9 @@ typedef struct lbm_ibm_config {
     double motion_amp, motion_freq;
     int scheme;           /* 0: implicit multi-direct forcing (lbm.cpp:1259-1390);
                              1: explicit direct forcing (lbm.cpp:1171-1258) */
+    double virtual_mass;  /* free body: virtual-mass coefficient C_v of Schwarz, Kempe & Froehlich (2015);
+                             0 = plain explicit Newton-Euler; 1 keeps light bodies (rho_s/rho_f ~ 1.5)
+                             stable in rotation and translation */
 } lbm_ibm_config;
 
 typedef struct lbm_handle lbm_handle;

@@ -78,7 +78,8 @@ class IbmConfig(C.Structure):
                 ("density_ratio", C.c_double), ("volume", C.c_double), ("inertia", C.c_double),
                 ("gravity", C.c_double * 3), ("velocity", C.c_double * 3), ("T_body", C.c_double),
                 ("free_dofs", C.c_int), ("rho_nearest", C.c_int), ("added_mass", C.c_int), ("motion", C.c_int),
-                ("motion_amp", C.c_double), ("motion_freq", C.c_double), ("scheme", C.c_int)]
+                ("motion_amp", C.c_double), ("motion_freq", C.c_double), ("scheme", C.c_int),
+                ("virtual_mass", C.c_double)]
 
 
 class ServeRequest(C.Structure):
@@ -276,7 +277,7 @@ class Solver:
     def set_markers(self, xyz, ds, radius, center, m_max=5, literal_sign=False, free_body=False, udes=None,
                     density_ratio=0.0, volume=0.0, inertia=0.0, gravity=(0, 0, 0), velocity=(0, 0, 0),
                     thermal=False, T_body=0.0, free_dofs=0, normals=None, rho_nearest=False, added_mass=False,
-                    motion=0, motion_amp=0.0, motion_freq=0.0, scheme=0):
+                    motion=0, motion_amp=0.0, motion_freq=0.0, scheme=0, virtual_mass=0.0):
         """Markers of an immersed body.  The last group of options applies to
         D2Q9 handles (the reference's two-dimensional IBLBM): normals [3][n]
         for the nearest-node density and the added mass, the motion
@@ -296,6 +297,7 @@ class Solver:
         ic.free_dofs = free_dofs
         ic.rho_nearest, ic.added_mass, ic.motion = int(rho_nearest), int(added_mass), int(motion)
         ic.motion_amp, ic.motion_freq, ic.scheme = motion_amp, motion_freq, int(scheme)
+        ic.virtual_mass = virtual_mass
         ud = None
         if udes is not None:
             udes = np.ascontiguousarray(udes, dtype=np.float64)

@@ -637,6 +637,7 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     }
     d.have_prev = 0;
     for (int k = 0; k < 6; k++) d.internal_prev[k] = 0.0;
+    for (int a = 0; a < 3; a++) d.body_v_prev[a] = d.body_om_prev[a] = 0.0;
     CUDA_TRY(cudaMemcpyAsync(h->ds, &d, sizeof(d), cudaMemcpyHostToDevice, h->s));
     h->bp.free_body = ic->free_body;
     h->bp.radius = ic->radius;
@@ -645,6 +646,10 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     for (int a = 0; a < 3; a++)
         h->bp.gacc[a] = ic->density_ratio > 0 ? (1.0 - 1.0 / ic->density_ratio) * ic->gravity[a] : 0.0;
     h->bp.dof = ic->free_dofs ? ic->free_dofs : 63;
+    h->bp.vol = ic->volume;
+    for (int a = 0; a < 3; a++) h->bp.grav[a] = ic->gravity[a];
+    h->bp.mv = ic->virtual_mass * ic->volume;
+    h->bp.iv = ic->density_ratio > 0 ? ic->virtual_mass * ic->inertia / ic->density_ratio : 0.0;
     // Keep the band in L2 while the far-region streaming (hundreds of MB)
     // passes through it: a persisting access-policy window on the streams
     // that run the IBM phase.  A per-context limit; best effort.

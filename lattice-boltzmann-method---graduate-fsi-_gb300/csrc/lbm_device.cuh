@@ -151,6 +151,7 @@ struct DevState {
     double body_dxc[3];
     double internal_prev[6];  // fluid momentum / angular momentum inside the body, previous step
     int have_prev;
+    double body_v_prev[3], body_om_prev[3];  // previous step's velocities (virtual-mass term)
 };
 
 enum : uint32_t {

@@ -292,21 +292,35 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
     if (t == 0) {
         if (!ds->have_prev) {
             for (int k = 0; k < 6; k++) ds->internal_prev[k] = red[k][0];
+            for (int a = 0; a < 3; a++) {
+                ds->body_v_prev[a] = ds->body_v[a];
+                ds->body_om_prev[a] = ds->body_om[a];
+            }
             ds->have_prev = 1;
         }
-        // Newton-Euler, dt = 1: rho_s V dV/dt = F_h + dI/dt + (rho_s - rho_f) V g
+        // Newton-Euler, dt = 1, with the virtual mass of Schwarz, Kempe &
+        // Froehlich (2015) on both sides (mv = iv = 0: plain explicit):
+        //   (m + mv)(V' - V) = F_h + dI/dt + (rho_s - rho_f) V g + mv (V - V_prev)
+        //   (I + iv)(W' - W) = T_h + dL/dt + iv (W - W_prev)
         for (int a = 0; a < 3; a++) {
             const double dI = red[a][0] - ds->internal_prev[a];
             const double dL = red[3 + a][0] - ds->internal_prev[3 + a];
-            const double vn =
-                ((bp.dof >> a) & 1) ? ds->body_v[a] + (sh_f[a] + dI) / bp.mass + bp.gacc[a] : ds->body_v[a];
-            const double om =
-                ((bp.dof >> (3 + a)) & 1) ? ds->body_om[a] + (sh_f[3 + a] + dL) / bp.inertia : ds->body_om[a];
+            const double fb = (bp.mass - bp.vol) * bp.grav[a];
+            const double vn = ((bp.dof >> a) & 1) ? ds->body_v[a] + (sh_f[a] + dI + fb +
+                                                                    bp.mv * (ds->body_v[a] - ds->body_v_prev[a])) /
+                                                                       (bp.mass + bp.mv)
+                                                  : ds->body_v[a];
+            const double om = ((bp.dof >> (3 + a)) & 1)
+                                  ? ds->body_om[a] + (sh_f[3 + a] + dL + bp.iv * (ds->body_om[a] - ds->body_om_prev[a])) /
+                                                         (bp.inertia + bp.iv)
+                                  : ds->body_om[a];
             const double d = 0.5 * (ds->body_v[a] + vn);
             sh_dxc[a] = d;
             sh_v[a] = vn;
             sh_om[a] = om;
             sh_xc[a] = ds->body_xc[a] + d;
+            ds->body_v_prev[a] = ds->body_v[a];
+            ds->body_om_prev[a] = ds->body_om[a];
             ds->body_dxc[a] = d;
             ds->body_v[a] = vn;
             ds->body_om[a] = om;

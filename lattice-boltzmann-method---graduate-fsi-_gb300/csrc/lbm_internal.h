@@ -102,6 +102,9 @@ struct BodyParams {
     double inertia;    // I_p
     double gacc[3];    // (1 - rho_f / rho_s) g
     int dof;           // bits 0-2 translation, 3-5 rotation
+    double vol;        // V_s
+    double grav[3];    // g
+    double mv, iv;     // virtual mass C_v rho_f V_s and moment of inertia C_v 2/5 rho_f V_s R^2
 };
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap);
 

@@ -149,7 +149,8 @@ class Body(C.Structure):
     _fields_ = [("xc", C.c_double * 3), ("v", C.c_double * 3), ("om", C.c_double * 3),
                 ("rho_ratio", C.c_double), ("vol", C.c_double), ("inertia", C.c_double),
                 ("grav", C.c_double * 3), ("dof", C.c_int), ("have_prev", C.c_int),
-                ("internal_prev", C.c_double * 6)]
+                ("internal_prev", C.c_double * 6), ("cv", C.c_double), ("v_prev", C.c_double * 3),
+                ("om_prev", C.c_double * 3)]
 
 
 class Lattice:
@@ -634,8 +635,9 @@ def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, 
     equilibrium at x = 0, zero-gradient outlet, bounce-back y/z walls,
     Fibonacci markers, interpolated marker density.  thermal = dict(tau_g,
     gbeta, T_in, T_body) adds the D3Q7 population and the thermal IBM;
-    free = dict(rho_ratio, gravity[, dof]) makes the body free (Newton-Euler;
-    dof bits 0-2 translation, 3-5 rotation, default all six).
+    free = dict(rho_ratio, gravity[, dof, cv]) makes the body free (Newton-Euler;
+    dof bits 0-2 translation, 3-5 rotation, default all six; cv the
+    virtual-mass coefficient, default 0).
     Returns (lattice, markers, per-step force history [steps, 7], body)."""
     lat = Lattice(19, nx, ny, nz, tau)
     t = lat.types
@@ -665,6 +667,7 @@ def sphere_case(nx, ny, nz, tau, diameter, center, n_markers, m_max, u_in=0.05, 
         for a in range(3):
             body.grav[a] = free["gravity"][a]
         body.dof = free.get("dof", 63)
+        body.cv = free.get("cv", 0.0)
     hist = np.zeros((steps, 7))
     for s in range(steps):
         c = [body.xc[0], body.xc[1], body.xc[2]]

@@ -954,6 +954,8 @@ typedef struct orc_body {
     int dof;           /* free degrees of freedom: bits 0-2 translation x,y,z, bits 3-5 rotation */
     int have_prev;
     double internal_prev[6];
+    double cv;         /* virtual-mass coefficient C_v (0: none) */
+    double v_prev[3], om_prev[3];
 } orc_body;
 
 /* Fluid momentum and angular momentum inside the body (rho_f = 1), with the
@@ -987,24 +989,44 @@ void orc_internal_momentum(orc *o, const double xc[3], double R, const int lo[3]
  *   rho_s V_s dV/dt   = F_h + d/dt(int u dV) + (rho_s - rho_f) V_s g
  *   I_p dOmega/dt     = T_h + d/dt(int r x u dV)
  * F_h, T_h: reaction of the IBM forces (sum of -F_m ds); the internal terms
- * are differenced between consecutive steps.  Degrees of freedom not set in
- * dof keep their velocity.  x_c' = x_c + (V + V')/2; markers follow x_c and
- * rotate with Omega' (r' = r + Omega' x r, rescaled to radius R); desired
- * marker velocity V' + Omega' x r'. */
+ * are differenced between consecutive steps.  With C_v > 0 the virtual-mass
+ * scheme of Schwarz, Kempe & Froehlich (J. Comput. Phys. 281, 2015) adds a
+ * virtual mass m_v = C_v rho_f V_s (and moment of inertia
+ * I_v = C_v 2/5 rho_f V_s R^2) to both sides, the right-hand one lagged a
+ * step:
+ *   (m + m_v)(V' - V)         = F_h + dI + (rho_s - rho_f) V_s g + m_v (V - V_prev)
+ *   (I_p + I_v)(Omega' - Omega) = T_h + dL + I_v (Omega - Omega_prev),
+ * which keeps the explicit coupling stable at low density ratios (the
+ * smeared forcing drags a shell of outer fluid with the body every step).
+ * Degrees of freedom not set in dof keep their velocity.
+ * x_c' = x_c + (V + V')/2; markers follow x_c and rotate with Omega'
+ * (r' = r + Omega' x r, rescaled to radius R); desired marker velocity
+ * V' + Omega' x r'. */
 void orc_body_step(orc_body *b, orc_markers *mk, double R, const double force[6], const double internal[6]) {
     if (!b->have_prev) {
         for (int q = 0; q < 6; q++) b->internal_prev[q] = internal[q];
+        for (int a = 0; a < 3; a++) {
+            b->v_prev[a] = b->v[a];
+            b->om_prev[a] = b->om[a];
+        }
         b->have_prev = 1;
     }
-    double mass = b->rho_ratio * b->vol;
+    const double mass = b->rho_ratio * b->vol;
+    const double mv = b->cv * b->vol;
+    const double iv = b->cv * b->inertia / b->rho_ratio;
     double vn[3], dxc[3];
     for (int a = 0; a < 3; a++) {
-        double dI = internal[a] - b->internal_prev[a];
-        double dL = internal[3 + a] - b->internal_prev[3 + a];
-        vn[a] = ((b->dof >> a) & 1)
-                    ? b->v[a] + (force[a] + dI) / mass + (1.0 - 1.0 / b->rho_ratio) * b->grav[a]
-                    : b->v[a];
-        if ((b->dof >> (3 + a)) & 1) b->om[a] = b->om[a] + (force[3 + a] + dL) / b->inertia;
+        const double dI = internal[a] - b->internal_prev[a];
+        const double dL = internal[3 + a] - b->internal_prev[3 + a];
+        const double fb = (mass - b->vol) * b->grav[a];
+        vn[a] = ((b->dof >> a) & 1) ? b->v[a] + (force[a] + dI + fb + mv * (b->v[a] - b->v_prev[a])) / (mass + mv)
+                                    : b->v[a];
+        const double on = ((b->dof >> (3 + a)) & 1)
+                              ? b->om[a] + (force[3 + a] + dL + iv * (b->om[a] - b->om_prev[a])) / (b->inertia + iv)
+                              : b->om[a];
+        b->v_prev[a] = b->v[a];
+        b->om_prev[a] = b->om[a];
+        b->om[a] = on;
         dxc[a] = 0.5 * (b->v[a] + vn[a]);
         b->xc[a] += dxc[a];
         b->v[a] = vn[a];

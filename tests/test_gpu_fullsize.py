@@ -1,0 +1,158 @@
+"""Parity at the stated sizes of the sphere configurations, against the FP64
+oracle on the same inputs (the reference has no 3D IBM; its restatement,
+pinned to the reference's own builds on the cases it can run, stands in).
+
+* IBM sphere channel, 256 x 128 x 128, D = 20 at (64, 64, 64), 1257
+  Fibonacci markers, m_max = 5, tau = 0.53 (Re = 100), inlet u = 0.05:
+  plain FP32 drag/lift within 0.1 % of the drag (measured 1.2e-7) and
+  fields within 1e-5 U after 150 steps; FP16 shifted storage drag within
+  0.5 % (measured 3.9e-4).
+  Error budget of the FP32 fields: the difference to FP64 grows about
+  linearly in time (mean 1.6e-6 U at 100 steps, 4.6e-6 U at 300; maximum
+  5.1e-6 U, then 1.59e-5 U, at the outlet and beside the no-slip walls,
+  outside the sphere's acoustic reach), so after 300 steps the bound is
+  2e-5 U.  It is FP32 rounding of the conserved moments, repeated every
+  step in the impulsively started wall layers of this low-viscosity flow
+  (tau = 0.53), not sensitivity to the state: the FP64 oracle perturbed by
+  3e-9 in u at the start differs by 2.2e-7 U after 300 steps.
+  Error budget of the FP16 fields: populations are stored as f - w, about
+  9e-3 on the moving links of the u = 0.05 free stream, so each stored value
+  is rounded by up to 2^-12 of that every step; the momentum errors
+  accumulate like a random walk over the domain.  Measured 1.6e-3 U after
+  300 steps (1.0e-3 U on the 64 x 32 x 28 sphere after 150 steps), so the
+  full-size bound is 2e-3 U; the drag stays within 0.04 %.
+* Two-way FSI with heat, the same channel: the sphere free in all six
+  degrees of freedom at rho_s / rho_f = 1.5 (virtual mass C_v = 1), gravity
+  -1e-5 along y, D3Q7 temperature at Pr = 0.71 with Boussinesq buoyancy
+  gbeta = 1e-5 along y, sphere at T = 1, inflow at T = 0: trajectory within
+  1e-6 cells, sphere and volume Nusselt numbers within 0.1 %, fields within
+  1e-4 of the largest velocity and 5e-5 in T.
+
+A few hundred steps each: the oracle (OpenMP on the host cores) takes about
+a minute per case."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+NX, NY, NZ, TAU, D, CEN, NM, MMAX, U = 256, 128, 128, 0.53, 20.0, (64.0, 64.0, 64.0), 1257, 5, 0.05
+
+
+def _sphere(pkg, orc, storage, thermal=None, free=None, u_in=U):
+    kw = {}
+    if thermal:
+        kw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal["T_in"], gbeta=thermal["gbeta"],
+                  T_ref=thermal["T0"])
+    s = pkg.Solver(pkg.channel_config(NX, NY, NZ, TAU, u_in=u_in, storage=storage, **kw))
+    s.init()
+    mk = orc.fibonacci_sphere(NM, D, CEN)
+    xyz = np.stack([mk["x"], mk["y"], mk["z"]])
+    mkw = {}
+    if free:
+        vol = np.pi * D ** 3 / 6.0
+        mkw = dict(free_body=True, density_ratio=free["rho_ratio"], volume=vol,
+                   inertia=0.4 * free["rho_ratio"] * vol * (D / 2) ** 2, gravity=free["gravity"],
+                   free_dofs=free["dof"], virtual_mass=free["cv"])
+    if thermal:
+        mkw.update(thermal=True, T_body=thermal["T_body"])
+    s.set_markers(xyz, mk["ds"], D / 2.0, CEN, m_max=MMAX, **mkw)
+    return s
+
+
+@pytest.fixture(scope="module")
+def sphere_oracle(orc):
+    """The oracle's fixed sphere (sphere_case's loop), moments after 150 and
+    300 steps, and the 300-step force history."""
+    lat = orc.Lattice(19, NX, NY, NZ, TAU)
+    t = lat.types
+    t[:] = orc.TYPE_F
+    t[:, :, 0] = orc.TYPE_IN
+    t[:, :, -1] = orc.TYPE_OUTZG
+    t[:, 0, :] = orc.TYPE_S
+    t[:, -1, :] = orc.TYPE_S
+    t[0, :, :] = orc.TYPE_S
+    t[-1, :, :] = orc.TYPE_S
+    lat.ux[t != orc.TYPE_S] = U
+    lat.init()
+    mk = orc.fibonacci_sphere(NM, D, CEN)
+    lo, hi = orc.sphere_box(CEN, D, lat)
+    op = orc.ibm_opts(lo, hi, MMAX)
+    hist = np.zeros((300, 7))
+    snap = {}
+    for k in range(300):
+        hist[k] = lat.step_ibm(mk, op, CEN)
+        if k + 1 in (150, 300):
+            snap[k + 1] = orc.moments(lat)
+    return snap, hist
+
+
+def _run(pkg, orc, storage, steps):
+    s = _sphere(pkg, orc, storage)
+    s.step(1)
+    s.step(steps - 1)
+    m = s.moments()
+    fg = s.forces()
+    assert s.status() == 0
+    s.close()
+    return m, fg
+
+
+def test_sphere_fullsize_fp32_vs_oracle(pkg, orc, sphere_oracle):
+    snap, hist = sphere_oracle
+    drag = np.abs(hist[:, 0]).max()
+    for steps, bound in ((150, 1e-5), (300, 2e-5)):
+        m, fg = _run(pkg, orc, "f32", steps)
+        r = snap[steps]
+        eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / U
+        er = np.abs(m["rho"] - r["rho"]).max()
+        ef = np.abs(fg[:, :3] - hist[:steps, :3]).max() / drag
+        print("sphere 256x128x128 FP32, %d steps: |u| err %.3e U, rho err %.3e, force err %.3e of drag"
+              % (steps, eu, er, ef))
+        assert eu < bound and er < 1e-5, (steps, eu, er)
+        assert ef < 1e-3, ef
+
+
+def test_sphere_fullsize_fp16_vs_oracle(pkg, orc, sphere_oracle):
+    snap, hist = sphere_oracle
+    m, fg = _run(pkg, orc, "f16", 300)
+    r = snap[300]
+    eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / U
+    ed = abs(fg[-1, 0] - hist[-1, 0]) / abs(hist[-1, 0])
+    print("sphere 256x128x128 FP16, 300 steps: drag err %.3e, |u| err %.3e U" % (ed, eu))
+    assert ed < 5e-3 and eu < 2e-3, (ed, eu)
+
+
+def test_fsi_thermal_fullsize_vs_oracle(pkg, orc):
+    steps = 200
+    nu = (TAU - 0.5) / 3.0
+    alpha = nu / 0.71
+    th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
+    fr = dict(rho_ratio=1.5, gravity=(0.0, -1e-5, 0.0), dof=63, cv=1.0)
+    s = _sphere(pkg, orc, "f32", thermal=th, free=fr)
+    s.step(1)
+    s.step(steps - 1)
+    m = s.moments()
+    fg = s.forces()
+    body = s.body()
+    nu_vol = s.nusselt(alpha, 1.0)
+    assert s.status() == 0
+    lat, mk, hist, ob = orc.sphere_case(NX, NY, NZ, TAU, D, CEN, NM, MMAX, U, steps, thermal=th, free=fr)
+    r = orc.moments(lat, gbeta=th["gbeta"], T0=0.0)
+    vscale = max(np.abs(r[c]).max() for c in ("ux", "uy", "uz"))
+    eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / vscale
+    eT = np.abs(m["T"] - r["T"]).max()
+    oxc = np.array([ob.xc[a] for a in range(3)])
+    exc = np.abs(body[:3] - oxc).max()
+    # sphere Nusselt number from the thermal IBM's heat input, Q / (alpha pi D dT)
+    nus_g = fg[-1, 6] / (alpha * np.pi * D)
+    nus_o = hist[-1, 6] / (alpha * np.pi * D)
+    # volume Nusselt number of Find_Nusselt_number over the interior cells
+    nu_o = 1.0 + (r["uy"] * r["T"]).mean() / (alpha * 1.0 / (NY + 1))
+    print("FSI + heat 256x128x128, %d steps: |u| err %.3e of %.3e, T err %.3e, centre err %.3e, "
+          "Nu_sphere %.6f / %.6f, Nu_volume %.6f / %.6f" % (steps, eu, vscale, eT, exc, nus_g, nus_o, nu_vol, nu_o))
+    assert eu < 1e-4 and eT < 5e-5, (eu, eT)
+    assert exc < 1e-6
+    assert abs(nus_g - nus_o) < 1e-3 * abs(nus_o)
+    assert abs(nu_vol - nu_o) < 1e-3 * abs(nu_o)
+    fscale = np.abs(hist[:, :3]).max()
+    assert np.abs(fg[:, :3] - hist[:, :3]).max() / fscale < 1e-3

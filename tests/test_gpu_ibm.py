@@ -30,7 +30,7 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
         vol = np.pi * D ** 3 / 6.0
         kw = dict(free_body=True, density_ratio=free["rho_ratio"], volume=vol,
                   inertia=0.4 * free["rho_ratio"] * vol * (D / 2) ** 2, gravity=free["gravity"],
-                  free_dofs=free.get("dof", 63))
+                  free_dofs=free.get("dof", 63), virtual_mass=free.get("cv", 0.0))
     if thermal:
         kw.update(thermal=True, T_body=thermal["T_body"])
     s.set_markers(xyz, mk["ds"], D / 2.0, center, m_max=m_max, literal_sign=lit_sign, **kw)
@@ -109,6 +109,44 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, staged):
     assert np.abs(fg[:, 6] - hist[:, 6]).max() / heat < 1e-3
     oxc = np.array([ob.xc[a] for a in range(3)])
     assert np.abs(body[:3] - oxc).max() < 1e-6
+    oxyz = np.stack([mk["x"], mk["y"], mk["z"]])
+    assert np.abs(xyz - oxyz).max() < 1e-6
+
+
+def test_light_free_sphere_six_dofs_vs_oracle(pkg, orc):
+    """The configuration-3 body at reduced size: a sphere at rho_s/rho_f =
+    1.5, free in all six degrees of freedom, in the sheared channel flow
+    (placed off the centre line, so it both drifts and spins), with gravity,
+    the D3Q7 population, Boussinesq buoyancy and T_body = 1.  The explicit
+    Newton-Euler update is unstable in rotation at this density ratio; the
+    virtual-mass scheme (C_v = 1) keeps it stable, on the GPU and in the
+    oracle alike."""
+    nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 36, 0.56, 10.0, 314, 3, 120
+    center = (20.0, 14.3, 17.6)
+    nu = (tau - 0.5) / 3.0
+    th = dict(tau_g=0.5 + (nu / 0.71) / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
+    fr = dict(rho_ratio=1.5, gravity=(0.0, -1e-5, 0.0), dof=63, cv=1.0)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=U)
+    s.step(1)
+    s.step(steps - 1)
+    m = s.moments()
+    fg = s.forces()
+    body = s.body()
+    xyz = s.markers()
+    assert s.status() == 0
+    lat, mk, hist, ob = orc.sphere_case(nx, ny, nz, tau, D, center, nm, m_max, U, steps, thermal=th, free=fr)
+    r = orc.moments(lat, gbeta=th["gbeta"], T0=0.0)
+    eu = max(np.abs(m[c] - r[c]).max() for c in ("ux", "uy", "uz")) / U
+    eT = np.abs(m["T"] - r["T"]).max()
+    om = np.array([ob.om[a] for a in range(3)])
+    print("light free sphere: |u| err %.3e U, T err %.3e, omega %s" % (eu, eT, om))
+    assert np.abs(om).max() > 1e-7  # it does spin
+    assert eu < 1e-4 and eT < 5e-5, (eu, eT)
+    fscale = np.abs(hist[:, :3]).max()
+    assert np.abs(fg[:, :6] - hist[:, :6]).max() / fscale < 1e-3
+    oxc = np.array([ob.xc[a] for a in range(3)])
+    assert np.abs(body[:3] - oxc).max() < 1e-6
+    assert np.abs(body[6:9] - om).max() <= 1e-3 * np.abs(om).max()
     oxyz = np.stack([mk["x"], mk["y"], mk["z"]])
     assert np.abs(xyz - oxyz).max() < 1e-6
 
