@@ -308,6 +308,7 @@ static void free_handle(lbm_handle *h) {
     cudaFree(h->mk.acc);
     cudaFree(h->mk.sb);
     cudaFree(h->mk.sw);
+    cudaFree(h->mk.ipart);
     for (int i = 0; i < 4; i++)
         if (h->ev[i]) cudaEventDestroy(h->ev[i]);
     for (cudaEvent_t e : h->evpool) cudaEventDestroy(e);
@@ -565,6 +566,7 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         cudaFree(h->mk.acc);
         cudaFree(h->mk.sb);
         cudaFree(h->mk.sw);
+        cudaFree(h->mk.ipart);
         cudaFree(h->band);
         memset(&h->mk, 0, sizeof(h->mk));
         h->band = nullptr;
@@ -576,6 +578,7 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
         CUDA_TRY(dalloc(h, &h->mk.acc, (size_t)11 * n * sizeof(double)));
         CUDA_TRY(dalloc(h, &h->mk.sb, (size_t)3 * n * sizeof(int)));
         CUDA_TRY(dalloc(h, &h->mk.sw, (size_t)12 * n * sizeof(float)));
+        CUDA_TRY(dalloc(h, &h->mk.ipart, (size_t)6 * lbmk::kBodyBlocks * sizeof(double)));
         h->mk.n = n;
     }
     h->icfg = *ic;

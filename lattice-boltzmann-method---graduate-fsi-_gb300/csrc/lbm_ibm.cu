@@ -223,6 +223,7 @@ __global__ void __launch_bounds__(kIbmThreads, 16) k_ibm_spread(const __grid_con
 // block: its per-thread loops over the markers and the band are four times
 // shorter than with kIbmThreads.
 constexpr int kFinishThreads = 256;
+static_assert(kBodyBlocks <= kFinishThreads, "one partial per finishing thread");
 
 __device__ __forceinline__ void block_tree(double (*red)[kFinishThreads], int nq, int t) {
     __syncthreads();
@@ -238,10 +239,9 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
                                                     const float *__restrict__ band, double *__restrict__ hist,
                                                     long long hist_cap) {
     __shared__ double red[7][kFinishThreads];
-    __shared__ double sh_dxc[3], sh_om[3], sh_v[3], sh_xc[3], sh_f[7];
+    __shared__ double sh_dxc[3], sh_om[3], sh_v[3], sh_xc[3], sh_f[7];  // written and read by thread 0
     const int t = threadIdx.x;
     const int n = mk.n;
-    const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
     double s[7] = {0, 0, 0, 0, 0, 0, 0};
     // per-marker force, torque and heat of the step (the last interpolation)
     for (int m = t; m < n; m += kFinishThreads)
@@ -261,33 +261,11 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
         ds->step = step + 1;
     }
     if (!bp.free_body) return;
-    // fluid momentum and angular momentum inside the body after the forced
-    // collision, u_unf + F_b / (2 rho) + Ft / rho, volume fraction
-    // clamp(R + 1/2 - |x - xc|, 0, 1) (Kempe & Froehlich 2012)
+    // the internal-fluid momentum: the per-block partials of k_body_internal,
+    // added in block order
     __syncthreads();
-    double q[6] = {0, 0, 0, 0, 0, 0};
-    const long long nb = P.nb;
-    for (long long b = t; b < nb; b += kFinishThreads) {
-        const int bx = (int)(b % P.bsx), by = (int)((b / P.bsx) % P.bsy), bz = (int)(b / ((long long)P.bsx * P.bsy));
-        const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
-        if (x >= P.nx || y >= P.ny || z >= P.nz) continue;
-        const double rx = (x + 1) - xc0, ry = (y + 1) - xc1, rz = (z + 1) - xc2;
-        double a = bp.radius + 0.5 - sqrt(rx * rx + ry * ry + rz * rz);
-        if (a <= 0.0) continue;
-        if (a > 1.0) a = 1.0;
-        const double rho = 1.0 + (double)band[b];
-        const double ux = (double)band[nb + b] + 0.5 * band[4 * nb + b] / rho + band[7 * nb + b] / rho;
-        const double uy = (double)band[2 * nb + b] + 0.5 * band[5 * nb + b] / rho + band[8 * nb + b] / rho;
-        const double uz = (double)band[3 * nb + b] + 0.5 * band[6 * nb + b] / rho + band[9 * nb + b] / rho;
-        q[0] += a * ux;
-        q[1] += a * uy;
-        q[2] += a * uz;
-        q[3] += a * (ry * uz - rz * uy);
-        q[4] += a * (rz * ux - rx * uz);
-        q[5] += a * (rx * uy - ry * ux);
-    }
 #pragma unroll
-    for (int k = 0; k < 6; k++) red[k][t] = q[k];
+    for (int k = 0; k < 6; k++) red[k][t] = t < kBodyBlocks ? mk.ipart[6 * t + k] : 0.0;
     block_tree(red, 6, t);
     if (t == 0) {
         if (!ds->have_prev) {
@@ -335,26 +313,78 @@ __global__ void __launch_bounds__(kFinishThreads) k_ibm_finish(const __grid_cons
             ds->band_o[a] = o;
         }
     }
-    __syncthreads();
-    const double R = bp.radius;
-    for (int m = t; m < n; m += kFinishThreads) {
-        const double r0 = mk.pos[m] - (sh_xc[0] - sh_dxc[0]);
-        const double r1 = mk.pos[n + m] - (sh_xc[1] - sh_dxc[1]);
-        const double r2 = mk.pos[2 * n + m] - (sh_xc[2] - sh_dxc[2]);
-        double q0 = r0 + (sh_om[1] * r2 - sh_om[2] * r1);
-        double q1 = r1 + (sh_om[2] * r0 - sh_om[0] * r2);
-        double q2 = r2 + (sh_om[0] * r1 - sh_om[1] * r0);
-        const double sc = R / sqrt(q0 * q0 + q1 * q1 + q2 * q2);
-        q0 *= sc;
-        q1 *= sc;
-        q2 *= sc;
-        mk.pos[m] = sh_xc[0] + q0;
-        mk.pos[n + m] = sh_xc[1] + q1;
-        mk.pos[2 * n + m] = sh_xc[2] + q2;
-        mk.udes[m] = (float)(sh_v[0] + (sh_om[1] * q2 - sh_om[2] * q1));
-        mk.udes[n + m] = (float)(sh_v[1] + (sh_om[2] * q0 - sh_om[0] * q2));
-        mk.udes[2 * n + m] = (float)(sh_v[2] + (sh_om[0] * q1 - sh_om[1] * q0));
+}
+
+// Free body: fluid momentum and angular momentum inside the body after the
+// forced collision, u_unf + F_b / (2 rho) + Ft / rho, with the volume
+// fraction clamp(R + 1/2 - |x - xc|, 0, 1) (Kempe & Froehlich 2012), in
+// FP64.  Block b sums its share of the band in index order (strided over its
+// threads, then a fixed tree) into ipart[b]; k_ibm_finish adds the blocks in
+// order.  Spread over kBodyBlocks SMs: GB300's FP64 rate on one SM made this
+// sum the cost of the whole step.
+__global__ void __launch_bounds__(kFinishThreads) k_body_internal(const __grid_constant__ StepParams P, MarkerDev mk,
+                                                       const DevState *__restrict__ ds, BodyParams bp,
+                                                       const float *__restrict__ band) {
+    __shared__ double red[6][kFinishThreads];
+    const int t = threadIdx.x;
+    const long long nb = P.nb;
+    const long long chunk = (nb + kBodyBlocks - 1) / kBodyBlocks;
+    const long long b0 = blockIdx.x * chunk, b1 = min(nb, b0 + chunk);
+    const double xc0 = ds->body_xc[0], xc1 = ds->body_xc[1], xc2 = ds->body_xc[2];
+    double q[6] = {0, 0, 0, 0, 0, 0};
+    for (long long b = b0 + t; b < b1; b += kFinishThreads) {
+        const int bx = (int)(b % P.bsx), by = (int)((b / P.bsx) % P.bsy), bz = (int)(b / ((long long)P.bsx * P.bsy));
+        const int x = bx + ds->band_o[0], y = by + ds->band_o[1], z = bz + ds->band_o[2];
+        if (x >= P.nx || y >= P.ny || z >= P.nz) continue;
+        const double rx = (x + 1) - xc0, ry = (y + 1) - xc1, rz = (z + 1) - xc2;
+        double a = bp.radius + 0.5 - sqrt(rx * rx + ry * ry + rz * rz);
+        if (a <= 0.0) continue;
+        if (a > 1.0) a = 1.0;
+        const double rho = 1.0 + (double)band[b];
+        const double ux = (double)band[nb + b] + 0.5 * band[4 * nb + b] / rho + band[7 * nb + b] / rho;
+        const double uy = (double)band[2 * nb + b] + 0.5 * band[5 * nb + b] / rho + band[8 * nb + b] / rho;
+        const double uz = (double)band[3 * nb + b] + 0.5 * band[6 * nb + b] / rho + band[9 * nb + b] / rho;
+        q[0] += a * ux;
+        q[1] += a * uy;
+        q[2] += a * uz;
+        q[3] += a * (ry * uz - rz * uy);
+        q[4] += a * (rz * ux - rx * uz);
+        q[5] += a * (rx * uy - ry * ux);
     }
+#pragma unroll
+    for (int k = 0; k < 6; k++) red[k][t] = q[k];
+    block_tree(red, 6, t);
+    if (t < 6) mk.ipart[6 * blockIdx.x + t] = red[t][0];
+}
+
+// Free body: move the markers with the body k_ibm_finish just advanced
+// (x_c' = x_c + dx_c; r' = r + Omega' x r rescaled to R) and set their
+// desired velocity V' + Omega' x r'.  One thread per marker.
+__global__ void __launch_bounds__(128) k_body_markers(MarkerDev mk, const DevState *__restrict__ ds, BodyParams bp) {
+    const int m = blockIdx.x * blockDim.x + threadIdx.x;
+    const int n = mk.n;
+    if (m >= n) return;
+    const double R = bp.radius;
+    const double xc[3] = {ds->body_xc[0], ds->body_xc[1], ds->body_xc[2]};
+    const double dxc[3] = {ds->body_dxc[0], ds->body_dxc[1], ds->body_dxc[2]};
+    const double om[3] = {ds->body_om[0], ds->body_om[1], ds->body_om[2]};
+    const double v[3] = {ds->body_v[0], ds->body_v[1], ds->body_v[2]};
+    const double r0 = mk.pos[m] - (xc[0] - dxc[0]);
+    const double r1 = mk.pos[n + m] - (xc[1] - dxc[1]);
+    const double r2 = mk.pos[2 * n + m] - (xc[2] - dxc[2]);
+    double q0 = r0 + (om[1] * r2 - om[2] * r1);
+    double q1 = r1 + (om[2] * r0 - om[0] * r2);
+    double q2 = r2 + (om[0] * r1 - om[1] * r0);
+    const double sc = R / sqrt(q0 * q0 + q1 * q1 + q2 * q2);
+    q0 *= sc;
+    q1 *= sc;
+    q2 *= sc;
+    mk.pos[m] = xc[0] + q0;
+    mk.pos[n + m] = xc[1] + q1;
+    mk.pos[2 * n + m] = xc[2] + q2;
+    mk.udes[m] = (float)(v[0] + (om[1] * q2 - om[2] * q1));
+    mk.udes[n + m] = (float)(v[1] + (om[2] * q0 - om[0] * q2));
+    mk.udes[2 * n + m] = (float)(v[2] + (om[0] * q1 - om[1] * q0));
 }
 
 // One block: fixed-order FP64 sum of the per-block momentum-exchange
@@ -432,7 +462,9 @@ cudaError_t launch_ibm_spread(const IbmArgs &a) {
 }
 
 cudaError_t launch_ibm_finish(const IbmArgs &a, const BodyParams &bp, double *hist, long long hist_cap) {
+    if (bp.free_body) k_body_internal<<<kBodyBlocks, kFinishThreads, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band);
     k_ibm_finish<<<1, kFinishThreads, 0, a.stream>>>(*a.P, a.mk, a.ds, bp, a.band, hist, hist_cap);
+    if (bp.free_body) k_body_markers<<<(a.mk.n + 127) / 128, 128, 0, a.stream>>>(a.mk, a.ds, bp);
     return cudaGetLastError();
 }
 

