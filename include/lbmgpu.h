@@ -96,9 +96,8 @@ typedef struct lbm_config {
     double gbeta[3];      /* Boussinesq: F += gbeta * (T - T0)  (lbm.cpp:804-805) */
     int block_x, block_y; /* thread-block shape of the fused kernel; 0 = default */
     int graph_steps;      /* steps per captured CUDA graph; 0 = default, <0 = no graphs */
-    int staged;           /* >0: the tensor-copy (TMA) staged kernel where rows allow it (row length a
-                             multiple of 32 cells and of 16 bytes); 0: direct loads everywhere (faster
-                             as measured) */
+    int staged;           /* must be 0: reserved (a tensor-copy staged step kernel, removed after it measured
+                             slower than direct loads in every variant) */
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
                              stream); <0: serial */
     int xface;            /* 0: lanes on x = 0 / x = nx-1 keep the plain pull and redo their five

@@ -16,7 +16,7 @@ CSRC = os.path.join(HERE, "csrc")
 OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbmgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["lbm_abi.cu", "lbm_stream.cu", "lbm_stepv.cu", "lbm_staged.cu", "lbm_ibm.cu", "lbm_batch.cu", "lbm_serve.cu",
+SOURCES = ["lbm_abi.cu", "lbm_stream.cu", "lbm_stepv.cu", "lbm_ibm.cu", "lbm_batch.cu", "lbm_serve.cu",
            "lbm_output.cu", "lbm_checkpoint.cu", "lbm_details.cu", "lbm2d.cu", "lbm_nusselt.cu"]
 
 

@@ -353,6 +353,8 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         if (c.faces[f].kind < 0 || c.faces[f].kind > 4) return fail(LBM_ERR_INVALID, "create: unknown face kind");
     if (c.lattice != 0 && c.lattice != LBM_LATTICE_D3Q19 && c.lattice != LBM_LATTICE_D2Q9)
         return fail(LBM_ERR_INVALID, "create: unknown lattice");
+    if (c.staged > 0)
+        return fail(LBM_ERR_UNSUPPORTED, "create: the staged (tensor-copy) step kernel is not built (staged must be 0)");
     if (c.wall_force && c.lattice != LBM_LATTICE_D2Q9)
         return fail(LBM_ERR_UNSUPPORTED, "create: wall_force is a D2Q9 option (the reference's Poiseuille_Flow)");
     if (c.lattice == LBM_LATTICE_D2Q9) {
@@ -403,9 +405,9 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
     };
     chk(cudaStreamCreateWithFlags(&h->s, cudaStreamNonBlocking), "stream");
     // Population arrays: stride S = N plus at least two rows (and 512 cells)
-    // of slack, rounded up to 256 cells, so that a staged tile's over-read of
-    // one row and one 16-byte group past the last plane stays inside the
-    // array, and a guard of kGuard cells before the first array.
+    // of slack, rounded up to 256 cells, so that every speculative read (idle
+    // lanes, a row segment's edge word one row past the last plane) stays
+    // inside the array, and a guard of kGuard cells before the first array.
     P.S = ((P.N + std::max<long long>(512, 2LL * P.nx + 64) + 255) / 256) * 256;
     for (int l = 0; l < Q; l++)
         P.pofs[l] = (long long)l * P.S - ((long long)cx(l) + (long long)P.nx * ((long long)cy(l) + (long long)P.ny * cz(l)));
@@ -466,14 +468,6 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         chk(cudaEventCreateWithFlags(&h->ev_fin, cudaEventDisableTiming), "events");
         if (st == LBM_OK) chk(cudaEventRecord(h->ev_ibm, h->s), "events");
         if (st == LBM_OK) chk(cudaEventRecord(h->ev_fin, h->s), "events");
-    }
-    if (st == LBM_OK && c.staged > 0) {
-        void *fb[2] = {h->f[0], h->f[1]}, *gb[2] = {h->g[0], h->g[1]};
-        chk(plan_staged(c.storage, c.thermal != 0, P, fb, gb, h->stp), "staged plan");
-        if (h->stp.enabled) {
-            h->tile_x = h->stp.tx;
-            h->tile_y = h->stp.ty;
-        }
     }
     if (st == LBM_OK) chk(cudaStreamSynchronize(h->s), "sync");
     if (st != LBM_OK) {
@@ -605,8 +599,7 @@ extern "C" lbm_status lbmgpu_set_markers(lbm_handle *h, const lbm_ibm_config *ic
     h->P.bsy = bs[1];
     h->P.bsz = bs[2];
     h->P.nb = nb;
-    // near box: the band grown by the one-cell pull stencil, rounded out to
-    // whole tiles of the staged kernel in x and y
+    // near box: the band grown by the one-cell pull stencil
     {
         // (and to whole row segments of the multi-cell kernel)
         int tx = h->tile_x;
@@ -723,8 +716,6 @@ static LaunchArgs make_args(lbm_handle *h, int gather) {
     a.thermal = h->cfg.thermal;
     a.tx = h->tx;
     a.ty = h->ty;
-    a.st = &h->stp;
-    a.buf_a = h->cur;
     a.stream = h->s;
     a.vcells = h->solids ? 0 : h->vcells;
     return a;
@@ -1120,7 +1111,6 @@ extern "C" lbm_status lbmgpu_set_solids(lbm_handle *h, const uint8_t *mask) {
     h->P.nearw = h->near_d;
     h->P.mea = h->mea_part;
     h->solids = true;
-    h->stp.enabled = 0;  // the staged kernel has no solid cells
     for (int i = 0; i < 2; i++)
         if (h->gexec[i]) {
             cudaGraphExecDestroy(h->gexec[i]);
@@ -1256,7 +1246,7 @@ extern "C" lbm_status lbmgpu_device_bytes(lbm_handle *h, size_t *bytes) {
 
 extern "C" lbm_status lbmgpu_cells_per_thread(lbm_handle *h, int *cells) {
     if (!h || !cells) return fail(LBM_ERR_INVALID, "cells_per_thread: null argument");
-    *cells = (h->d2 || h->solids || h->stp.enabled || h->vcells <= 1) ? 1 : h->vcells;
+    *cells = (h->d2 || h->solids || h->vcells <= 1) ? 1 : h->vcells;
     return LBM_OK;
 }
 

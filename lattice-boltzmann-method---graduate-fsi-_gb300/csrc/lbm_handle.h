@@ -17,7 +17,6 @@ struct lbm2d;       // D2Q9 solve (lbm2d.cu)
 
 using lbmk::BodyParams;
 using lbmk::MarkerDev;
-using lbmk::StagedPlan;
 using lbmk::StepParams;
 using lbmk::DevState;
 
@@ -49,7 +48,6 @@ struct lbm_handle {
     int gsteps = 16;
     int tx = 128, ty = 2;
     int vcells = 0;                       // x-cells per thread of gather steps (k_stepv), 0 = k_step
-    StagedPlan stp;                       // staged (bulk-copy) step kernel
     // interior solid cells and their momentum exchange
     bool solids = false;
     uint32_t *solid_d = nullptr, *near_d = nullptr;
@@ -58,7 +56,7 @@ struct lbm_handle {
     int n_mea_blocks = 0;
     double *mea_ring = nullptr;
     long long mea_cap = 1 << 16;
-    int tile_x = 1, tile_y = 1;           // tile of the staged kernel (near-box rounding)
+    int tile_x = 1, tile_y = 1;           // near-box rounding in x and y
     size_t dev_bytes = 0;
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::vector<cudaEvent_t> evpool;

@@ -8,20 +8,6 @@
 
 namespace lbmk {
 
-// Launch plan of the staged (tensor-copy) step kernel k_step_st; enabled = 0
-// leaves every launch to the direct-load kernel k_step.
-struct StagedPlan {
-    int enabled = 0;
-    int tx = 0, ty = 0;            // tile of one z plane
-    int tiles_x = 0, tiles_y = 0;  // tiles per row of tiles, rows of tiles per plane
-    long long ntiles = 0;
-    int grid = 0;                  // blocks, all resident at once
-    size_t smem = 0;
-    // per population buffer (A/B ping-pong): flow narrow box, flow wide box,
-    // heat narrow box, heat wide box; the narrow maps also serve the stores
-    CUtensorMap maps[2][4];
-};
-
 struct LaunchArgs {
     const StepParams *P;
     const void *A;
@@ -36,8 +22,6 @@ struct LaunchArgs {
     int region;  // 0 all cells, 1 all but the IBM near box, 2 the near box only
     int thermal;
     int tx, ty;
-    const StagedPlan *st;  // staged kernel plan (or null)
-    int buf_a;             // index of the population buffer read (A)
     cudaStream_t stream;
     int pdl = 0;           // band collision: programmatic dependent launch behind the IBM chain
     int vcells = 0;        // > 1: gather steps use k_stepv with this many x-cells per thread
@@ -48,9 +32,6 @@ cudaError_t launch_step(int storage, const LaunchArgs &a);
 // per thread, and its launcher.
 bool step_vec_usable(int storage, const StepParams &P, int vcells);
 cudaError_t launch_step_vec(int storage, const LaunchArgs &a);
-cudaError_t plan_staged(int storage, bool thermal, const StepParams &P, void *const f[2], void *const g[2],
-                        StagedPlan &sp);
-cudaError_t launch_staged(int storage, const LaunchArgs &a);
 cudaError_t launch_band_collide(int storage, const LaunchArgs &a, float fsign);
 // Initial populations (equilibrium of the given or uniform fields) into A,
 // GA and, when non-null, also into A2 / GA2.

@@ -1,5 +1,5 @@
 // lbm_step.cuh -- per-cell pieces of the fused collide-stream step shared
-// by the direct (k_step) and the staged (k_step_st) kernels: the pull of
+// by the one-cell (k_step) and multi-cell (k_stepv) kernels: the pull of
 // the 19 (+7) populations with the boundary-class rules, and the update
 // (moments, IBM band hand-off or BGK + Guo collision).
 #pragma once

@@ -195,8 +195,6 @@ static cudaError_t launch_step_t(const LaunchArgs &a) {
 }
 
 cudaError_t launch_step(int storage, const LaunchArgs &a) {
-    if (a.st && a.st->enabled && a.gather && !a.export_only && a.mom == nullptr && a.region != 2)
-        return launch_staged(storage, a);
     if (a.vcells > 1 && a.gather && !a.export_only && a.mom == nullptr && a.region != 2)
         return launch_step_vec(storage, a);
     switch (storage) {

@@ -15,11 +15,10 @@ U = 0.05
 
 
 def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", lit_sign=0, thermal=None, free=None,
-                overlap=0, u_in=U, graph_steps=0, staged=0):
-    cfgkw = {"ibm_overlap": overlap, "graph_steps": graph_steps, "staged": staged}
+                overlap=0, u_in=U, graph_steps=0):
+    cfgkw = {"ibm_overlap": overlap, "graph_steps": graph_steps}
     if thermal:
         cfgkw = dict(thermal=True, tau_g=thermal["tau_g"], T_in=thermal.get("T_in", 0.0), graph_steps=graph_steps,
-                     staged=staged,
                      gbeta=thermal.get("gbeta", (0, 0, 0)), T_ref=thermal.get("T0", 0.0))
     s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=u_in, storage=storage, **cfgkw))
     s.init()
@@ -37,16 +36,14 @@ def _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, storage="f32", 
     return s
 
 
-@pytest.mark.parametrize("staged", [0, 1], ids=["direct", "staged"])
 @pytest.mark.parametrize("overlap", [0, -1], ids=["overlapped", "serial"])
 @pytest.mark.parametrize("lit_sign", [0, 1])
-def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap, staged):
+def test_fixed_sphere_fp32_vs_oracle(pkg, orc, lit_sign, overlap):
     """The IBM phase on its own stream overlapping the far-region streaming,
-    and in the serial order; direct-load and staged (64 x 32 rows) kernels."""
+    and in the serial order."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 32, 28, 0.56, 10.0, 314, 3, 120
     center = (16.0, 15.3, 14.6)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, overlap=overlap,
-                    staged=staged)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, lit_sign=lit_sign, overlap=overlap)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
@@ -77,8 +74,7 @@ def test_fixed_sphere_fp16_drag(pkg, orc):
     assert ed < 5e-3 and eu < 1e-3
 
 
-@pytest.mark.parametrize("staged", [0, 1], ids=["direct", "staged"])
-def test_thermal_free_sphere_vs_oracle(pkg, orc, staged):
+def test_thermal_free_sphere_vs_oracle(pkg, orc):
     """D3Q7 thermal population, Boussinesq force, thermal IBM (T_body = 1)
     and the FP64 Newton-Euler body (held in x and rotation, free in y and z)
     settling in fluid at rest, against the oracle."""
@@ -89,7 +85,7 @@ def test_thermal_free_sphere_vs_oracle(pkg, orc, staged):
     th = dict(tau_g=0.5 + alpha / 0.25, T_in=0.0, T0=0.0, gbeta=(0.0, 1e-5, 0.0), T_body=1.0)
     # rho_s/rho_f = 3: the explicit coupling of a D = 8 sphere is unstable at 1.5
     fr = dict(rho_ratio=3.0, gravity=(0.0, -1e-5, 0.0), dof=0b000110)
-    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=0.0, staged=staged)
+    s = _gpu_sphere(pkg, orc, nx, ny, nz, tau, D, center, nm, m_max, thermal=th, free=fr, u_in=0.0)
     s.step(steps)
     m = s.moments()
     fg = s.forces()
