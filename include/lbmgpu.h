@@ -358,7 +358,11 @@ lbm_status lbmgpu_download_stats(lbm_handle *h, double *host, int *samples, doub
  * array (NULL: derived from the faces and the solid mask).  Returns once the
  * snapshot is enqueued; a host thread writes the file while the device goes
  * on stepping.  One file is in flight at a time: the next call (or
- * lbmgpu_output_wait) finishes the previous one and returns its status. */
+ * lbmgpu_output_wait) finishes the previous one and returns its status.
+ * D2Q9 handles (the reference's #define D2Q9 build) write the layer k = 1 of
+ * fluid[Nx+2][Ny+2][3]: types is then that (Nx+2)(Ny+2) layer; the moments are
+ * copied out before the call returns, and an IBM body's Force density is the
+ * force its box cells collided with (IBLBM's fluid[..].F). */
 lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types);
 lbm_status lbmgpu_output_wait(lbm_handle *h);
 
@@ -370,7 +374,7 @@ lbm_status lbmgpu_output_wait(lbm_handle *h);
 lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, double u_ref, const uint8_t *types);
 
 /* OutputVTK_Marker (lbm.cpp:3033-3077): legacy ASCII POLYDATA of the markers
- * (points, closed polyline, vertices). */
+ * (points, closed polyline, vertices); D3Q19 and D2Q9 handles. */
 lbm_status lbmgpu_output_markers_vtk(lbm_handle *h, const char *path);
 
 /* OutputCSV (lbm.cpp:3169-3186): "time,error" rows, time = (i+1) time_step. */

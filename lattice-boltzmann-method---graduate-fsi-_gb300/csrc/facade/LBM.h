@@ -88,6 +88,12 @@ struct lbm_options {
     // fluid[..].F of the fluid cells at Init
     int wall_force = 0;
     int Nt = 10;                  // output cadence (LBM.h:493-496): Sup_MacroProp's told = (n - Nt) dt
+    // OutputCSV's time column, (i + 1) csv_time_step: the reference's Nt dt
+    // (Couette / Poiseuille / Rayleigh-Benard) or dt u_max / D (the IBM
+    // cylinders) (lbm.cpp:3169-3186)
+    double csv_time_step = 1.0;
+    // Find_Nusselt_number's alpha and dT (LBM.h's Rayleigh_Benard block)
+    double alpha = 0.0, dT = 1.0;
     // the reference's global centre (center_x, center_y, 1): IBLBM's box is
     // [centre - D, centre + D] (lbm.cpp:1165-1166); unset, the marker centroid
     int body_center_set = 0;
@@ -208,3 +214,15 @@ void OutputVTK_async(int &nout, LBM &lb);
 // OutputAVGVTK (LBM.h:780-782) from the device: ./avgfield.vtr
 void OutputAVGVTK(int &nout, LBM &lb);
 #endif
+// The reference's output and analysis functions (LBM.h:770-835), same
+// signatures: OutputVTK writes ./field%06d.vtr of the current state and
+// returns once it is on disk; OutputVTK_Marker "wall_t <time / Nt>.vtk" of the
+// markers on the device (or of the given vector before IBLBM registered
+// them); OutputCSV "time,error" rows with g_lbm_options.csv_time_step;
+// Find_Nusselt_number (lbmgpu_nusselt, with g_lbm_options alpha and dT) and
+// Find_Maximum_uy of the current moments.
+void OutputVTK(int &nout, LBM &lb);
+void OutputVTK_Marker(int &time, std::vector<MARKER> &marker);
+void OutputCSV(std::vector<double> &error, std::string name);
+double Find_Nusselt_number(LBM &lb);
+double Find_Maximum_uy(LBM &lb);

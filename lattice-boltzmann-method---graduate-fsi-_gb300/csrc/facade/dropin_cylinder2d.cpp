@@ -5,8 +5,12 @@
 // main.cpp:123-131 and the IBM loop of main.cpp:195-205, with the reference's
 // literal IBLBM options.  "transverse A F" runs its
 // Cylinder_Transverse_Oscillation variant instead (u = 0.05, Re = 100,
-// markers at center_y + A, V_solid = pi D^2 / 4 (Nz + 2)).
-// usage: dropin_cylinder2d NX NY D NODES M_MAX STEPS OUT.csv [storage [transverse A F]]
+// markers at center_y + A, V_solid = pi D^2 / 4 (Nz + 2)).  "vtk Nt" adds the
+// main loop's output calls (main.cpp:62-66, 205-237): OutputVTK and
+// OutputVTK_Marker of the initial state and every Nt steps, and OutputCSV of
+// Cl and Cd under the reference's file names at each output (the reference
+// rewrites the same two files after every step), into the working directory.
+// usage: dropin_cylinder2d NX NY D NODES M_MAX STEPS OUT.csv [storage [transverse A F] [vtk Nt]]
 // Writes step, Cd, Cl per step.
 #include <cmath>
 #include <cstdio>
@@ -18,7 +22,8 @@
 
 int main(int argc, char **argv) {
     if (argc < 8) {
-        fprintf(stderr, "usage: %s NX NY D NODES M_MAX STEPS OUT.csv [storage [transverse A F]]\n", argv[0]);
+        fprintf(stderr, "usage: %s NX NY D NODES M_MAX STEPS OUT.csv [storage [transverse A F] [vtk Nt]]\n",
+                argv[0]);
         return 2;
     }
     const int Nx = atoi(argv[1]), Ny = atoi(argv[2]), Nz = 1;
@@ -27,13 +32,27 @@ int main(int argc, char **argv) {
     lbm_options &o = g_lbm_options;
     o.m_max = atoi(argv[5]);
     if (argc > 8) o.storage = atoi(argv[8]);
-    const bool transverse = argc > 11 && strcmp(argv[9], "transverse") == 0;
-    const double amplitude = transverse ? atof(argv[10]) : 0.0, frequency = transverse ? atof(argv[11]) : 0.0;
+    bool transverse = false;
+    double amplitude = 0.0, frequency = 0.0;
+    int Nt = 0;
+    for (int a = 9; a < argc; a++) {
+        if (strcmp(argv[a], "transverse") == 0 && a + 2 < argc) {
+            transverse = true;
+            amplitude = atof(argv[a + 1]);
+            frequency = atof(argv[a + 2]);
+            a += 2;
+        } else if (strcmp(argv[a], "vtk") == 0 && a + 1 < argc) {
+            Nt = atoi(argv[a + 1]);
+            a += 1;
+        }
+    }
     const double u_max = transverse ? 0.05 : 0.1, Re = transverse ? 100.0 : 40.0;
     const double nu = u_max * D / Re, tau = 0.5 + nu / (1.0 / 3.0);
     const double center_x = Nx / 5.0, center_y = Ny / 2.0;
     // the reference's literal IBLBM (lbm.cpp:1259-1416)
     o.u_max = u_max;
+    if (Nt > 0) o.Nt = Nt;
+    o.csv_time_step = u_max / D;  // OutputCSV's (i + 1) dt u_max / D of the IBM cylinders
     o.ref_area = D;
     o.body_radius = D / 2;
     o.literal_sign = 1;
@@ -78,12 +97,27 @@ int main(int argc, char **argv) {
         ds.push_back(sqrt(pow(dx_, 2) + pow(dy_, 2) + pow(dz_, 2)));
     }
     lb.Init();
+    int step = 0, n = 0;
+    if (Nt > 0) {
+        OutputVTK(step, lb);
+        OutputVTK_Marker(step, marker);
+    }
     std::vector<double> CL, CD;
     double V_CM[3] = {0, 0, 0};
-    for (int step = 1; step <= steps; step++) {
+    char name[96];
+    for (step = 1; step <= steps; step++) {
         IBLBM(lb, marker, ds, CL, CD, V_CM, step * 1.0);
         lb.Collision();
         lb.Streaming();
+        if (Nt > 0 && step % Nt == 0) {
+            n++;
+            OutputVTK(n, lb);
+            OutputVTK_Marker(step, marker);
+            snprintf(name, sizeof(name), "Cl at Re = %f.csv", Re);
+            OutputCSV(CL, name);
+            snprintf(name, sizeof(name), "Cd at Re = %f.csv", Re);
+            OutputCSV(CD, name);
+        }
     }
     FILE *fp = fopen(argv[7], "w");
     if (!fp) return 3;

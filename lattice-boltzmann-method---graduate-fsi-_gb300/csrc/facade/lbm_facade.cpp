@@ -1,6 +1,9 @@
 // lbm_facade.cpp -- the reference's LBM class surface on top of liblbmgpu.
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <exception>
+#include <string>
 #include <vector>
 
 #include "LBM.h"
@@ -24,6 +27,9 @@ struct lbm_device_state {
 
 // The reference terminates on invalid state (lbm.cpp:116, 774, 796); the
 // facade does the same when the device reports an error.
+// the handle whose markers IBLBM registered last (OutputVTK_Marker)
+static lbm_handle *g_marker_handle = nullptr;
+
 static void check(const char *what, lbm_status s) {
     if (s != LBM_OK) {
         fprintf(stderr, "lbmgpu %s failed (status %d): %s\n", what, (int)s, lbmgpu_last_error());
@@ -377,7 +383,10 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
     d.cd = &Cd;
     // the markers stay on the device (a prescribed D2Q9 motion moves them
     // there: lbmgpu_get_markers reads them back)
-    if (d.markers_set) return;
+    if (d.markers_set) {
+        g_marker_handle = d.h;
+        return;
+    }
     const int n = (int)marker.size();
     std::vector<double> xyz(3 * (size_t)n), dsv(ds.begin(), ds.end());
     double c[3] = {0, 0, 0};
@@ -426,6 +435,7 @@ void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::v
     check("set_marker_normals", lbmgpu_set_marker_normals(d.h, nrm.data()));
 #endif
     d.markers_set = true;
+    g_marker_handle = d.h;
 }
 
 // Momentum-exchange coefficients of the solid cells after the latest step
@@ -465,18 +475,80 @@ double MEA_CD(LBM &lb, int xmin, int xmax, int ymin, int ymax, int zmin, int zma
 // ./field%06d.vtr of the current state from a host thread while the time
 // loop goes on.  Velocity is divided by g_lbm_options.u_max as the reference
 // does; the cell types come from fluid[..].type.
-void OutputVTK_async(int &nout, LBM &lb) {
-    lbm_handle *h = lb.handle();
-    if (!h) check("OutputVTK_async before Init", LBM_ERR_STATE);
-    const int NX = lb.getNx() + 2, NY = lb.getNy() + 2, NZ = lb.getNz() + 2;
+// fluid[..].type for the CellType array: every layer, or the layer k = 1 of
+// a D2Q9 build
+static std::vector<uint8_t> cell_types(LBM &lb) {
+    const int NX = lb.getNx() + 2, NY = lb.getNy() + 2;
+#if defined D2Q9
+    const int k0 = 1, NZ = 1;
+#else
+    const int k0 = 0, NZ = lb.getNz() + 2;
+#endif
     std::vector<uint8_t> types((size_t)NX * NY * NZ);
     for (int k = 0; k < NZ; k++)
         for (int j = 0; j < NY; j++)
             for (int i = 0; i < NX; i++)
-                types[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = (uint8_t)lb.fluid[i][j][k].type;
+                types[(size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k)] = (uint8_t)lb.fluid[i][j][k0 + k].type;
+    return types;
+}
+
+void OutputVTK_async(int &nout, LBM &lb) {
+    lbm_handle *h = lb.handle();
+    if (!h) check("OutputVTK_async before Init", LBM_ERR_STATE);
+    const std::vector<uint8_t> types = cell_types(lb);
     char name[64];
     snprintf(name, sizeof(name), "./field%06d.vtr", nout);
     check("output_vtk_async", lbmgpu_output_vtk_async(h, name, g_lbm_options.u_max, types.data()));
+}
+
+void OutputVTK(int &nout, LBM &lb) {
+    OutputVTK_async(nout, lb);
+    check("output_wait", lbmgpu_output_wait(lb.handle()));
+}
+
+void OutputVTK_Marker(int &time, std::vector<MARKER> &marker) {
+    char name[64];
+    snprintf(name, sizeof(name), "wall_t %d.vtk", time / std::max(1, g_lbm_options.Nt));
+    if (g_marker_handle) {
+        check("output_markers_vtk", lbmgpu_output_markers_vtk(g_marker_handle, name));
+        return;
+    }
+    // before IBLBM: the caller's set-up positions, in the same format
+    FILE *fp = fopen(name, "w");
+    if (!fp) check("OutputVTK_Marker: cannot open the file", LBM_ERR_INVALID);
+    const int n = (int)marker.size();
+    fprintf(fp, "# vtk DataFile Version 3.0\nwall_state\nASCII\nDATASET POLYDATA\n");
+    fprintf(fp, "POINTS %d float\n", n);
+    for (int m = 0; m < n; m++) fprintf(fp, "%g %g %g \n", marker[m].x, marker[m].y, marker[m].z);
+    fprintf(fp, "LINES %d %d\n", n, 3 * n);
+    for (int m = 0; m < n; m++) fprintf(fp, "2 %d %d\n", m % n, (m + 1) % n);
+    fprintf(fp, "VERTICES 1 %d\n", n + 1);
+    fprintf(fp, "%d ", n);
+    for (int m = 0; m < n; m++) fprintf(fp, "%d ", m);
+    fclose(fp);
+}
+
+void OutputCSV(std::vector<double> &error, std::string name) {
+    check("output_csv", lbmgpu_output_csv(name.c_str(), error.data(), (int)error.size(), g_lbm_options.csv_time_step));
+}
+
+double Find_Nusselt_number(LBM &lb) {
+    lbm_handle *h = lb.handle();
+    if (!h) check("Find_Nusselt_number before Init", LBM_ERR_STATE);
+    double nu = 0.0;
+    check("nusselt", lbmgpu_nusselt(h, g_lbm_options.alpha, g_lbm_options.dT, &nu));
+    return nu;
+}
+
+// Find_Maximum_uy (lbm.cpp:3522-3536): max |u_y| over every cell, ghosts
+// included, of the current moments
+double Find_Maximum_uy(LBM &lb) {
+    lb.sync_to_host();
+    double maximum = -99;
+    for (int i = 0; i <= lb.getNx() + 1; i++)
+        for (int j = 0; j <= lb.getNy() + 1; j++)
+            for (int k = 0; k <= lb.getNz() + 1; k++) maximum = std::max(maximum, std::fabs(lb.fluid[i][j][k].uy));
+    return maximum;
 }
 
 #if defined MORE_DETAILS

@@ -434,6 +434,8 @@ struct Ibm2 {
     float *lw;        //                         weight
     int *qnear;       // [n] nearest box node of each marker (band index), -1 for none
     uint8_t *inside;  // [nb] box node inside every marker (Calc_AverageDensity)
+    float *boxF;      // [4][nb] force and forced velocity the box cells collided with (fluid[..].F,
+                      // ux, uy after IBLBM), box order
     double *hist;     // [cap][4]: drag, lift, 0, step
     int smem;         // 1: the working fields of the pass live in shared memory
     int fast;         // 1: box nodes in registers (at most kFastNodes per thread, n <= block size)
@@ -700,6 +702,13 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     if (tid == 0) advance_body(st, ib, step);
     __syncthreads();
     const int bw = st->box_w, bh = st->box_h, nbox = bw * bh;
+    // the box this pass collides, for the force-density output (boxF)
+    if (tid == 0) {
+        st->fbox[0] = st->box_lo[0];
+        st->fbox[1] = st->box_lo[1];
+        st->fbox[2] = bw;
+        st->fbox[3] = bh;
+    }
     const int lists_ok = st->lists_ok;
     const float V0 = (float)st->V[0], V1 = (float)st->V[1];
     auto bq = [&](int o) { return (long long)(o % bw) + (long long)P.bsx * (o / bw); };
@@ -884,6 +893,10 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
 #pragma unroll
             for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
             collide9(f, band[nq[k]], vx[k], vy[k], fx[k], fy[k], P.omega, true);
+            ib.boxF[o] = fx[k];
+            ib.boxF[P.nb + o] = fy[k];
+            ib.boxF[2 * P.nb + o] = vx[k];
+            ib.boxF[3 * P.nb + o] = vy[k];
 #pragma unroll
             for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
         }
@@ -1009,6 +1022,10 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
 #pragma unroll
         for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
         collide9(f, drho[q], ux[q], uy[q], Fx[q], Fy[q], P.omega, true);
+        ib.boxF[o] = Fx[q];
+        ib.boxF[P.nb + o] = Fy[q];
+        ib.boxF[2 * P.nb + o] = ux[q];
+        ib.boxF[3 * P.nb + o] = uy[q];
 #pragma unroll
         for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
     }
@@ -1595,6 +1612,8 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     ib.dsw = dsd;
     CK2(alloc2(h, &ib.qnear, (size_t)n * sizeof(int)));
     CK2(alloc2(h, &ib.inside, (size_t)P.nb));
+    CK2(alloc2(h, &ib.boxF, (size_t)4 * P.nb * sizeof(float)));
+    CK2(cudaMemsetAsync(ib.boxF, 0, (size_t)4 * P.nb * sizeof(float), h->s));
     CK2(alloc2(h, &ib.fs, (size_t)2 * n * sizeof(float)));
     CK2(alloc2(h, &ib.rhom, (size_t)n * sizeof(float)));
     CK2(alloc2(h, &ib.s0, (size_t)2 * n * sizeof(int)));
@@ -1737,6 +1756,60 @@ lbm_status l2d_download_all_f32(lbm_handle *h, float *host) {
     memset(host + 3 * N, 0, N * sizeof(float));
     return LBM_OK;
 }
+
+// The fields OutputVTK writes.  With markers they are those of the last
+// IBLBM (lbm.cpp:1262-1285, 1342-1352): the moments of the populations the
+// last step collided -- the buffer it pulled from, still intact -- and, in
+// the box, the forced velocity and the force of that collision; without
+// markers the moments of the current state.
+lbm_status l2d_vtk_snapshot(lbm_handle *h, float *host, std::vector<float> &boxF, int box[4]) {
+    lbm2d *d = h->d2;
+    const size_t N = (size_t)d->P.N;
+    if (!h->inited) return f2(LBM_ERR_STATE, "output_vtk: call lbmgpu_init first");
+    if (d->ibm && h->steps > 0) {
+        // the export pass of the last step: its source buffer and step count
+        d->cur = 1 - d->cur;
+        h->steps--;
+        const cudaError_t e = launch_step2d(h, h->steps == 0 ? 0 : 1, d->mom, 1);
+        d->cur = 1 - d->cur;
+        h->steps++;
+        CK2(e);
+    } else {
+        lbm_status s = l2d_export(h);
+        if (s != LBM_OK) return s;
+    }
+    // the 3D moment layout: rho, u (3) [, T, q (3)]; uz and qz are zero
+    CK2(cudaMemcpyAsync(host, d->mom, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    if (d->energy) {
+        CK2(cudaMemcpyAsync(host + 4 * N, d->mom + 3 * N, N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+        CK2(cudaMemcpyAsync(host + 5 * N, d->mom + 4 * N, 2 * N * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+    }
+    box[0] = box[1] = box[2] = box[3] = 0;
+    const size_t nb = (size_t)d->P.nb;
+    if (d->ibm) {
+        State2 st;
+        boxF.resize(4 * nb);
+        CK2(cudaMemcpyAsync(boxF.data(), d->ib.boxF, boxF.size() * sizeof(float), cudaMemcpyDeviceToHost, h->s));
+        CK2(cudaMemcpyAsync(&st, d->st, sizeof(st), cudaMemcpyDeviceToHost, h->s));
+        CK2(cudaStreamSynchronize(h->s));
+        for (int k = 0; k < 4; k++) box[k] = st.fbox[k];
+    }
+    CK2(cudaStreamSynchronize(h->s));
+    if (d->ibm && h->steps > 0) {
+        for (int by = 0; by < box[3]; by++)
+            for (int bx = 0; bx < box[2]; bx++) {
+                const size_t o = (size_t)bx + (size_t)box[2] * by;
+                const size_t cell = (size_t)(box[0] + bx) + (size_t)d->P.nx * (box[1] + by);
+                host[N + cell] = boxF[2 * nb + o];
+                host[2 * N + cell] = boxF[3 * nb + o];
+            }
+    }
+    memset(host + 3 * N, 0, N * sizeof(float));
+    if (d->energy) memset(host + 7 * N, 0, N * sizeof(float));
+    return LBM_OK;
+}
+
+int l2d_marker_count(lbm_handle *h) { return h->d2->ibm ? h->d2->ib.n : 0; }
 
 lbm_status l2d_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
     lbm2d *d = h->d2;

@@ -94,6 +94,7 @@ struct State2 {
     double center[3];
     double V[3], Vold[3];
     int lists_ok;       // spreading lists valid (fixed body)
+    int fbox[4];        // box of the latest IBM pass {x0, y0, w, h}: the extent of Ibm2::boxF
     long long hist_cap;
 };
 

@@ -96,6 +96,11 @@ lbm_status l2d_set_solids(lbm_handle *h, const uint8_t *mask);
 // after an export pass: u_y and T of the current moments, the solid-cell masks, the cell count
 lbm_status l2d_thermal_moments(lbm_handle *h, const float **uy, const float **T, const uint16_t **links, long long *N);
 lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]);
+// For the VTK writer: the current moments in the 3D layout ([8][N] when ENERGY,
+// else [4][N]), and with an IBM body the force the box cells collided with
+// ([2][nb], box order) and the box {x0, y0, width, height} of that pass.
+lbm_status l2d_vtk_snapshot(lbm_handle *h, float *host, std::vector<float> &boxF, int box[4]);
+int l2d_marker_count(lbm_handle *h);
 
 // Launch the gather-only export of the current state's moments into h->mom
 // (rho, ux, uy, uz [, T]) on h->s.

@@ -131,9 +131,32 @@ VtkGrid grid_of(lbm_handle *h) {
     return g;
 }
 
+// The grid of a D2Q9 handle: the computational layer k = 1 of the
+// reference's fluid[Nx+2][Ny+2][3], written as one plane.
+VtkGrid grid_of_2d(lbm_handle *h) {
+    VtkGrid g;
+    g.cfg = h->cfg;
+    g.N = (long long)h->cfg.nx * h->cfg.ny;
+    for (int a = 0; a < 2; a++) {
+        g.dn[a] = a == 0 ? h->cfg.nx : h->cfg.ny;
+        const bool per = h->cfg.faces[2 * a].kind == LBM_FACE_PERIODIC;
+        g.off[a] = per ? 0 : 1;
+        g.nref[a] = per ? g.dn[a] - 2 : g.dn[a];
+    }
+    g.dn[2] = 1;
+    g.off[2] = 1;
+    g.nref[2] = 1;
+    return g;
+}
+
 // The caller's types array, else the device solid mask (read on h->s).
 bool grid_types(lbm_handle *h, VtkGrid &g, const uint8_t *types) {
-    if (types) {
+    if (types && h->d2) {
+        // D2Q9: the caller's (Nx+2)(Ny+2) layer k = 1
+        const size_t nt = (size_t)(g.nref[0] + 2) * (g.nref[1] + 2);
+        g.types.assign((size_t)(g.nref[0] + 2) * (g.nref[1] + 2) * 3, 0);
+        std::copy(types, types + nt, g.types.begin() + nt);
+    } else if (types) {
         const size_t nt = (size_t)(g.nref[0] + 2) * (g.nref[1] + 2) * (g.nref[2] + 2);
         g.types.assign(types, types + nt);
     } else if (h->solids) {
@@ -273,11 +296,17 @@ struct VtkJob {
     int band_o[3], bs[3];
     float fsign;
     float body[3];
-    cudaEvent_t copied;
+    cudaEvent_t copied;   // null: the host copies are complete (D2Q9)
+    // D2Q9 IBM: the force the box cells collided with (rows 0 and 1 of
+    // [4][fcap], box order) and the box {x0, y0, w, h}
+    int d2 = 0;
+    std::vector<float> boxF;
+    long long fcap = 0;
+    int fbox[4] = {0, 0, 0, 0};
 };
 
 void write_vtk(VtkJob j, lbm_output *o) {
-    if (cudaEventSynchronize(j.copied) != cudaSuccess) {
+    if (j.copied && cudaEventSynchronize(j.copied) != cudaSuccess) {
         o->result = LBM_ERR_CUDA;
         o->error = "output_vtk: copy failed";
         return;
@@ -292,7 +321,18 @@ void write_vtk(VtkJob j, lbm_output *o) {
                           for (int a = 0; a < 3; a++)
                               v[a] = c >= 0 ? (float)(j.mom[(1 + a) * N + c] / j.u_ref) : (float)(gf->u[a] / j.u_ref);
                       }});
-    if (j.force)
+    if (j.force && j.d2)
+        arrays.push_back({"Force density", 3, [&](long long c, const lbm_face *, float *v) {
+                              if (c < 0) return;
+                              for (int a = 0; a < 3; a++) v[a] = j.body[a];
+                              const int bx = (int)(c % dn[0]) - j.fbox[0], by = (int)(c / dn[0]) - j.fbox[1];
+                              if ((unsigned)bx < (unsigned)j.fbox[2] && (unsigned)by < (unsigned)j.fbox[3]) {
+                                  const long long q = bx + (long long)j.fbox[2] * by;
+                                  v[0] = j.boxF[q];
+                                  v[1] = j.boxF[j.fcap + q];
+                              }
+                          }});
+    else if (j.force)
         arrays.push_back({"Force density", 3, [&](long long c, const lbm_face *, float *v) {
                               if (c < 0) return;
                               for (int a = 0; a < 3; a++) v[a] = j.body[a];
@@ -358,10 +398,50 @@ void lbm_output_free(lbm_handle *h) {
     h->out = nullptr;
 }
 
+// D2Q9 handles: the moments (and an IBM body's box force) are copied out
+// synchronously, then the file is written by the same host thread writer.
+static lbm_status output_vtk_2d(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
+    if (!h->out) h->out = new lbm_output();
+    lbm_output *o = h->out;
+    lbm_status prev = join_writer(o);
+    if (prev != LBM_OK) return prev;
+    VtkJob j;
+    j.grid = grid_of_2d(h);
+    const long long N = j.grid.N;
+    const size_t need = (size_t)8 * N;
+    if (o->host_floats < need) {
+        if (o->host) cudaFreeHost(o->host);
+        o->host = nullptr;
+        o->host_floats = 0;
+        if (cudaMallocHost((void **)&o->host, need * sizeof(float)) != cudaSuccess)
+            return out_fail(LBM_ERR_NOMEM, "output_vtk: pinned staging allocation failed");
+        o->host_floats = need;
+    }
+    lbm_status st = l2d_vtk_snapshot(h, o->host, j.boxF, j.fbox);
+    if (st != LBM_OK) return st;
+    j.path = path;
+    for (int a = 0; a < 3; a++) j.body[a] = (float)h->cfg.body_force[a];
+    j.u_ref = u_ref;
+    j.tau = h->cfg.tau;
+    j.thermal = h->cfg.thermal;
+    j.force = l2d_marker_count(h) > 0;
+    j.details = 0;
+    j.mom = o->host;
+    j.band = nullptr;
+    j.det = nullptr;
+    j.fsign = 1.0f;
+    j.d2 = 1;
+    j.fcap = (long long)j.boxF.size() / 4;
+    j.copied = nullptr;
+    if (!grid_types(h, j.grid, types)) return out_fail(LBM_ERR_CUDA, "output_vtk: types");
+    o->writer = std::thread(write_vtk, std::move(j), o);
+    return LBM_OK;
+}
+
 extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
     if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_vtk: bad argument");
-    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_vtk: not for D2Q9 handles");
     if (!h->inited) return out_fail(LBM_ERR_STATE, "output_vtk: call lbmgpu_init first");
+    if (h->d2) return output_vtk_2d(h, path, u_ref, types);
     if (!h->out) {
         h->out = new lbm_output();
         lbm_output *o = h->out;
@@ -525,14 +605,17 @@ extern "C" lbm_status lbmgpu_output_wait(lbm_handle *h) {
 
 extern "C" lbm_status lbmgpu_output_markers_vtk(lbm_handle *h, const char *path) {
     if (!h || !path) return out_fail(LBM_ERR_INVALID, "output_markers: bad argument");
-    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_markers: not for D2Q9 handles");
-    if (!h->ibm) return out_fail(LBM_ERR_STATE, "output_markers: no markers set");
-    const int n = h->mk.n;
+    const int n = h->d2 ? l2d_marker_count(h) : (h->ibm ? h->mk.n : 0);
+    if (n == 0) return out_fail(LBM_ERR_STATE, "output_markers: no markers set");
     std::vector<double> pos(3 * (size_t)n);
-    if (cudaMemcpyAsync(pos.data(), h->mk.pos, pos.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s) !=
-            cudaSuccess ||
-        cudaStreamSynchronize(h->s) != cudaSuccess)
+    if (h->d2) {
+        const lbm_status st = lbmgpu_get_markers(h, pos.data());
+        if (st != LBM_OK) return st;
+    } else if (cudaMemcpyAsync(pos.data(), h->mk.pos, pos.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s) !=
+                   cudaSuccess ||
+               cudaStreamSynchronize(h->s) != cudaSuccess) {
         return out_fail(LBM_ERR_CUDA, "output_markers: copy failed");
+    }
     FILE *fp = fopen(path, "w");
     if (!fp) return out_fail(LBM_ERR_INVALID, std::string("output_markers: cannot open ") + path);
     // legacy ASCII POLYDATA; numbers as the reference's stream prints them

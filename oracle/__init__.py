@@ -52,9 +52,16 @@ def build(force: bool = False) -> str:
     return LIB
 
 
+# Where this build environment keeps the reference tree (read-only); the
+# environment variable REF overrides it.  Absent on hosts that only run the
+# prebuilt files.
+REF_TREE = os.environ.get("REF", "/root/reference")
+
+
 def build_ref(*variants: str) -> None:
     """Run the reference-literal recipe (no-op when the reference tree is absent)."""
-    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), *variants])
+    env = dict(os.environ, REF=REF_TREE)
+    subprocess.check_call(["sh", os.path.join(HERE, "build_ref.sh"), *variants], env=env)
 
 
 _lib = None

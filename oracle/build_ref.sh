@@ -3,8 +3,8 @@
 # lbm.cpp, unmodified and where it lies, against oracle/ref_config.h (which
 # replaces the compile-time configuration block of LBM.h) and the Vector3d
 # stand-in under oracle/shim, with the batch driver oracle/ref_harness.cpp.
-# Outputs go to oracle/_ref/ only.  Needs the reference tree (REF, default
-# /root/reference); without it this script does nothing and exits 0.
+# Outputs go to oracle/_ref/ only.  Needs the reference tree, given in the
+# environment variable REF; without it this script does nothing and exits 0.
 #
 # usage: oracle/build_ref.sh [variant ...]
 #   cavity:N[:TAU]            D3Q19 cavity, N^3 interior
@@ -22,9 +22,9 @@
 #   triangle:NX:NY:D:RE:U:LPD:NB  D2Q9 staircase triangles in tandem (Cylinder_Tandem_Triangle)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
-REF=${REF:-/root/reference}
+REF=${REF:-}
 OUT="$HERE/_ref"
-if [ ! -f "$REF/lbm.cpp" ]; then
+if [ -z "$REF" ] || [ ! -f "$REF/lbm.cpp" ]; then
     echo "build_ref: no reference tree at $REF, skipped"
     exit 0
 fi

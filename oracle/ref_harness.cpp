@@ -66,7 +66,7 @@ static void dump_field(LBM &lb, FILE *fp, int which) {
 
 int main(int argc, char **argv) {
     if (argc < 3) {
-        fprintf(stderr, "usage: %s steps out.bin [lid_velocity [vtk]]\n", argv[0]);
+        fprintf(stderr, "usage: %s steps out.bin [lid_velocity [vtk]]  (cylinders: steps out.bin [vtk])\n", argv[0]);
         return 2;
     }
     int steps = atoi(argv[1]);
@@ -150,6 +150,13 @@ int main(int argc, char **argv) {
         fwrite(v, sizeof(double), 8, fp);
     }
     fclose(fp);
+    if (argc > 3) {
+        // the reference's own writers: OutputVTK (lbm.cpp:2290-2642), ./field000000.vtr, and
+        // OutputVTK_Marker (lbm.cpp:3033-3077) of the final markers
+        int nout = 0;
+        OutputVTK(nout, lb);
+        OutputVTK_Marker(steps, marker);
+    }
     double mlups = (double)Nx * Ny * Nz * steps / (t1 - t0) / 1e6;
     printf("{\"case\": \"cylinder2d\", \"nx\": %d, \"steps\": %d, \"seconds\": %.6f, \"mlups\": %.4f, \"threads\": %d}\n",
            Nx, steps, t1 - t0, mlups, omp_get_max_threads());

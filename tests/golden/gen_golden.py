@@ -7,6 +7,7 @@ outputs are stored as small .npz fixtures:
   cavity12_tau0.8_lid0.05_200.npz   D3Q19 lid-driven cavity 12^3, 200 steps:
                                     full interior rho, ux, uy, uz
   cavity12_vtk_200.npz              the same run's OutputVTK file
+  cylinder80x40_vtk_100.npz         the D2Q9 cylinder's OutputVTK and OutputVTK_Marker files
                                     (lbm.cpp:2290-2642): header text and
                                     every appended array
   cavity64_tau0.8_lid0.05_5000.npz  the 64^3, tau = 0.8, 5000-step cavity:
@@ -112,6 +113,22 @@ STAIRCASE = (("cylbasic", "cylbasic:100:60:20:200:0.1", "ref_cylbasic_100_60_20_
 STAIRCASE_VARIANTS = tuple(v for _, v, *_ in STAIRCASE)
 
 
+def cylinder_vtk(tmp: str) -> None:
+    """The shipped D2Q9 implicit-IBM cylinder (80 x 40, D = 10, 40 markers,
+    m_max = 5), 100 steps, with the reference's own OutputVTK file of the
+    final state and its OutputVTK_Marker file."""
+    import glob
+
+    p = os.path.join(tmp, "cylvtk.bin")
+    subprocess.check_call([os.path.join(REF, "ref_cylinder_80_40_10_40_5"), "100", p, "vtk"], cwd=tmp)
+    v = read_vtr(os.path.join(tmp, "field000000.vtr"))
+    wall = glob.glob(os.path.join(tmp, "wall_t*.vtk"))
+    assert len(wall) == 1, wall
+    v["marker_file"] = open(wall[0]).read()
+    v["marker_file_name"] = os.path.basename(wall[0])
+    np.savez_compressed(os.path.join(OUT, "cylinder80x40_vtk_100.npz"), steps=100, **v)
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -120,7 +137,13 @@ def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--cav64-dump", default=None)
     ap.add_argument("--skip-cav64", action="store_true")
+    ap.add_argument("--only-cylinder-vtk", action="store_true",
+                    help="write only cylinder80x40_vtk_100.npz (the D2Q9 OutputVTK / OutputVTK_Marker files)")
     a = ap.parse_args()
+    if a.only_cylinder_vtk:
+        oracle.build_ref("cylinder:80:40:10:40:5")
+        cylinder_vtk(tempfile.mkdtemp())
+        return
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
                      "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",

@@ -224,8 +224,8 @@ def test_d2q9_unsupported_calls_fail_loudly(pkg, tmp_path):
     t[1:-1, 1:-1] = 0
     s = pkg.Solver(pkg.config_from_types_2d(10, 8, 0.8, t))
     s.init()
-    for call in (lambda: s.save_state(str(tmp_path / "x")), lambda: s.output_vtk_async(str(tmp_path / "x.vtr")),
-                 lambda: s.set_more_details(True), lambda: s.solid_forces()):
+    for call in (lambda: s.save_state(str(tmp_path / "x")), lambda: s.set_more_details(True),
+                 lambda: s.solid_forces()):
         with pytest.raises(pkg.LbmError) as e:
             call()
         assert e.value.status == 7

@@ -175,3 +175,35 @@ def test_dropin_poiseuille_energy_loop(drivers, tmp_path):
     assert np.abs(a[1:3] - g["u"][:2, 1:-1]).max() < 3e-5 * um
     T = g["T"][1:-1]
     assert np.abs(a[4] - T).max() < 5e-3 * (T.max() - T.min())
+
+
+def test_dropin_cylinder2d_outputs(drivers, pkg, tmp_path):
+    """The default build's output calls through the facade (main.cpp:62-66,
+    205-237): OutputVTK every Nt = 10 steps against the reference's own
+    field file after 100 steps, OutputVTK_Marker's wall_t file against the
+    reference's text, and OutputCSV's Cd / Cl files (time = (i + 1) u_max / D,
+    six significant digits) against the reference's coefficients."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_vtk_100.npz"))
+    c = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    steps = int(g["steps"])
+    subprocess.check_call([drivers["dropin_cylinder2d"], "80", "40", "10", "40", "5", str(steps),
+                           str(tmp_path / "cd.csv"), "0", "vtk", "10"], cwd=str(tmp_path))
+    for n in range(steps // 10 + 1):
+        assert (tmp_path / ("field%06d.vtr" % n)).exists(), n
+        assert (tmp_path / ("wall_t %d.vtk" % n)).exists(), n
+    v = pkg.read_vtr(str(tmp_path / ("field%06d.vtr" % (steps // 10))))
+    assert v["header"] == str(g["header"])
+    assert np.array_equal(v["CellType"], g["CellType"])
+    assert np.abs(v["Density"] - g["Density"]).max() < 1e-5
+    assert np.abs(v["Velocity"] - g["Velocity"]).max() * 0.1 < 1e-5  # u / u_max
+    fscale = np.abs(g["Force density"]).max()
+    assert np.abs(v["Force density"] - g["Force density"]).max() < 1e-5 * max(fscale, 1e-3) + 1e-7
+    assert (tmp_path / str(g["marker_file_name"])).read_text() == str(g["marker_file"])
+    for coef in ("cd", "cl"):
+        r = np.loadtxt(str(tmp_path / ("C%s at Re = 40.000000.csv" % coef[1])), delimiter=",", skiprows=1)
+        assert r.shape == (steps, 2)
+        assert np.allclose(r[:, 0], (np.arange(steps) + 1) * 0.1 / 10.0, rtol=1e-5)
+        scale = np.abs(c["cd"]).max()
+        assert np.abs(r[:, 1] - c[coef]).max() / scale < 1e-5

@@ -75,3 +75,37 @@ def test_vtk_thermal_ibm_arrays_and_markers(pkg, orc, tmp_path):
     pts = np.array([[float(t) for t in lines[5 + m].split()] for m in range(nm)])
     assert np.abs(pts - xyz.T).max() < 1e-4
     assert lines[5 + nm] == "LINES %d %d" % (nm, 3 * nm)
+
+
+def test_vtk_d2q9_cylinder_matches_reference_outputvtk(pkg, orc, tmp_path):
+    """The reference's default build (#define D2Q9, Cylinder_IBM): OutputVTK of
+    the state after 100 steps against the reference's own file of the same
+    run -- header byte for byte, CellType and coordinates exactly, Density,
+    Velocity / u_max and the IBM Force density within FP32 tolerance -- and
+    OutputVTK_Marker against the reference's marker file, text for text."""
+    from test_gpu_d2q9 import _cylinder_gpu
+
+    g = np.load(os.path.join(GOLDEN, "cylinder80x40_vtk_100.npz"))
+    c = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+    s, cl, cd = _cylinder_gpu(pkg, orc, c, int(g["steps"]), m_max=int(c["m_max"]))
+    types = g["CellType"].reshape(42, 82).astype(np.uint8)
+    path = str(tmp_path / "field000000.vtr")
+    s.output_vtk_async(path, u_ref=0.1, types=types)  # the reference divides by its u_max = 0.1
+    s.output_wait()
+    v = pkg.read_vtr(path)
+    assert v["header"] == str(g["header"])
+    for k in ("CellType", "CoordinateX", "CoordinateY", "CoordinateZ"):
+        assert np.array_equal(v[k], g[k]), k
+    def worst(a, b):
+        d = np.abs(a - b).reshape(42, 82, -1).max(axis=2)
+        return d.max(), np.unravel_index(np.argmax(d), d.shape)
+
+    assert worst(v["Density"], g["Density"])[0] < 1e-5, worst(v["Density"], g["Density"])
+    # Velocity is u / u_max: 1e-5 in lattice units
+    assert worst(v["Velocity"], g["Velocity"])[0] * 0.1 < 1e-5, worst(v["Velocity"], g["Velocity"])
+    fscale = np.abs(g["Force density"]).max()
+    assert fscale > 0
+    assert np.abs(v["Force density"] - g["Force density"]).max() < 1e-5 * max(fscale, 1e-3) + 1e-7
+    mpath = str(tmp_path / str(g["marker_file_name"]))
+    s.output_markers_vtk(mpath)
+    assert open(mpath).read() == str(g["marker_file"])
