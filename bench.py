@@ -548,17 +548,22 @@ def run_fsi_thermal(pkg, orc, steps: int = 20000, timed: int = 2000, sample_ever
 
         row, b = sample()
         traj = [row]
-        margin = DIAM / 2.0 + 4.0  # stop before the body's stencils reach a lattice face
+        # stop before the body's stencils reach a lattice face: the band
+        # (the stencils' box) must stay inside the lattice through the next
+        # chunk of 100 steps at the body's current velocity
+        margin = DIAM / 2.0 + 4.0
         stop = None
         while done < steps and s.status() == 0:
+            b = s.body()
+            dims = (NX, NY, NZ)
+            gap = min([b[a] - 1.0 - 100.0 * max(-b[3 + a], 0.0) for a in range(3)] +
+                      [dims[a] - b[a] - 100.0 * max(b[3 + a], 0.0) for a in range(3)])
+            if gap < margin:
+                stop = ("at step %d the next 100 steps would bring the body within %.0f cells of a lattice face "
+                        "(centre %s)" % (done, margin, [round(float(v), 1) for v in b[:3]]))
+                break
             s.step(100)
             done += 100
-            b = s.body()
-            gap = min([b[a] - 1.0 for a in range(3)] + [(NX, NY, NZ)[a] - b[a] for a in range(3)])
-            if gap < margin:
-                stop = ("at step %d the body came within %.0f cells of a lattice face (centre %s); the final "
-                        "state is the last sample before that" % (done, margin, [round(float(v), 1) for v in b[:3]]))
-                break
             if done % sample_every == 0 or done >= steps:
                 row, b = sample()
                 traj.append(row)

@@ -437,8 +437,9 @@ lbm_status lbmgpu_batch_info(lbm_batch *b, long long *total_cells, long long *st
  * exit: at most 1024 cavities and 2^20 tiles of 256 cells; larger batches are
  * rejected with LBM_ERR_INVALID.  Every call clears the status words itself
  * and rewrites the tables, so nothing in that array has to start at zero.
- * The first call on a device looks up that array's device address; make it
- * before any stream capture.  All calls share
+ * Each call copies its tables from host memory, so it cannot be captured
+ * into a CUDA graph: called on a stream that is being captured it returns
+ * LBM_ERR_STATE and enqueues nothing.  All calls share
  * the array: calls that overlap on the GPU race.  status_out (host, n words,
  * may be NULL) receives the per-cavity status words; stream may be NULL (the
  * default stream).  Allocates nothing. */

@@ -297,6 +297,7 @@ static void free_handle(lbm_handle *h) {
     }
     cudaFree(h->mom);
     cudaFree(h->band);
+    cudaFree(h->nu_scratch);
     cudaFree(h->ds);
     cudaFree(h->hist);
 

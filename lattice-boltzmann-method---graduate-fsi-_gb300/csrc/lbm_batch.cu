@@ -550,6 +550,12 @@ extern "C" lbm_status lbmgpu_batch_step_noalloc(int n, const int *dims, const do
     }
     NoAllocScratch *sc = g_noalloc_ptr[dev];
     cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+    // the tables are copied from this call's host vectors: a captured graph
+    // would replay copies from freed host memory
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    BCUDA(cudaStreamIsCapturing(s, &cap));
+    if (cap != cudaStreamCaptureStatusNone)
+        return bfail(LBM_ERR_STATE, "batch_step_noalloc: not callable while the stream is being captured");
     BCUDA(cudaMemcpyAsync(sc->prob, hp.data(), (size_t)n * sizeof(BatchProb), cudaMemcpyHostToDevice, s));
     BCUDA(cudaMemcpyAsync(sc->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice, s));
     BCUDA(cudaMemsetAsync(sc->status, 0, (size_t)n * sizeof(uint32_t), s));  // starts at zero on every call

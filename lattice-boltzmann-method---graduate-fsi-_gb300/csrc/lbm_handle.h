@@ -33,6 +33,7 @@ struct lbm_handle {
     int cur = 0;
     float *mom = nullptr;
     float *band = nullptr;
+    double *nu_scratch = nullptr;  // lbmgpu_nusselt: per-block partials, counts and result, on first use
     DevState *ds = nullptr;
     bool inited = false;
     long long steps = 0;

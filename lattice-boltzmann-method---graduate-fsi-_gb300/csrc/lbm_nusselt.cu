@@ -89,12 +89,13 @@ extern "C" lbm_status lbmgpu_nusselt(lbm_handle *h, double alpha, double dT, dou
     }
     // the reference's Ny: a periodic y axis carries its two ghost rows on the device
     const int Ny = h->cfg.faces[2].kind == LBM_FACE_PERIODIC ? ny_dev - 2 : ny_dev;
-    double *part = nullptr;
-    unsigned long long *cnt = nullptr;
-    double *res = nullptr;
-    cudaError_t e = cudaMalloc((void **)&part, kNuBlocks * sizeof(double));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&cnt, kNuBlocks * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMalloc((void **)&res, 2 * sizeof(double));
+    // partials, counts and the result: one allocation per handle, made on the
+    // first call (a cudaFree on every call would synchronise the device)
+    cudaError_t e = cudaSuccess;
+    if (!h->nu_scratch) e = cudaMalloc((void **)&h->nu_scratch, (2 * kNuBlocks + 2) * sizeof(double));
+    double *part = h->nu_scratch;
+    unsigned long long *cnt = reinterpret_cast<unsigned long long *>(h->nu_scratch + kNuBlocks);
+    double *res = h->nu_scratch + 2 * kNuBlocks;
     if (e == cudaSuccess) {
         k_nusselt_part<<<kNuBlocks, kNuThreads, 0, h->s>>>(uy, T, N, solid3, links2, part, cnt);
         k_nusselt_finish<<<1, 1, 0, h->s>>>(part, cnt, res);
@@ -103,9 +104,6 @@ extern "C" lbm_status lbmgpu_nusselt(lbm_handle *h, double alpha, double dT, dou
     double r[2] = {0.0, 0.0};
     if (e == cudaSuccess) e = cudaMemcpyAsync(r, res, sizeof(r), cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
-    cudaFree(part);
-    cudaFree(cnt);
-    cudaFree(res);
     if (e != cudaSuccess) return fail_nu(LBM_ERR_CUDA, std::string("nusselt: ") + cudaGetErrorString(e));
     if (r[1] < 1) return fail_nu(LBM_ERR_STATE, "nusselt: no fluid cell");
     out[0] = 1.0 + (r[0] / r[1]) / (alpha * dT / (Ny + 1));

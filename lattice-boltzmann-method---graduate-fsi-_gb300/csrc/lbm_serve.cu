@@ -54,7 +54,8 @@ size_t estimate_bytes(const lbm_serve_request &r, int n_markers) {
     const size_t cells = (size_t)r.nx * r.ny * r.nz;
     const size_t es = r.storage == LBM_STORE_F32 ? 4 : 2;
     size_t b = 2 * 19 * cells * es + 5 * cells * 4 + ((size_t)1 << 16) * 64 + (1 << 20);
-    if (r.kind == LBM_SERVE_SPHERE) b += (size_t)n_markers * 128 + (size_t)12 * 4 * 64 * 64 * 64;
+    // band of at most 64^3 nodes: 12 FP32 fields and 4 fixed-point accumulators a node
+    if (r.kind == LBM_SERVE_SPHERE) b += (size_t)n_markers * 128 + (size_t)(12 * 4 + 4 * 8) * 64 * 64 * 64;
     return b + b / 20;
 }
 
