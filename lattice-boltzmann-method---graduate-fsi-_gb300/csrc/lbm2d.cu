@@ -48,7 +48,7 @@ constexpr double kRefPi = 3.14159265;  // the reference's truncated PI (LBM.h:74
 __device__ __forceinline__ void status_once(uint32_t *status, uint32_t bit, bool bad) {
     const unsigned am = __activemask();
     const unsigned b = __ballot_sync(am, bad);
-    if (b && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) atomicOr(status, bit);
+    if (b && (threadIdx.x & 31) == (unsigned)(__ffs(am) - 1)) lbmk::raise_status(status, bit);
 }
 
 template <class T>

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(512) k_batch_step(const T *__restrict__ A, T *
         // cavity): a diverged cavity would otherwise send an atomic from
         // every cell of every step
         const unsigned badw = __ballot_sync(0xffffffffu, valid && !(rho > 0.0f && rho < 100.0f));
-        if (badw && (threadIdx.x & 31) == 0) atomicOr(&status[tt.x], ST_RHO_RANGE);
+        if (badw && (threadIdx.x & 31) == 0) raise_status(&status[tt.x], ST_RHO_RANGE);
         if (EXPORT) {
             if (valid) {
                 mom[pr.mom_base + cc] = rho;

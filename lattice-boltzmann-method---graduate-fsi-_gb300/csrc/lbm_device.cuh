@@ -174,6 +174,13 @@ __device__ __forceinline__ int cell_class(int x, int y, int z, const StepParams 
 // scaling) rounded to an integer, so the sum of a node's contributions is
 // the same in whatever order the atomics land; read back with one rounding
 // to FP32.  |v| stays far below 2^19 for any finite forcing.
+// Set a status bit from one lane: a plain read first, so that a diverged
+// solve, where every warp of every step finds a bad cell, sends one atomic
+// per warp only until the bit is set instead of on every step.
+__device__ __forceinline__ void raise_status(uint32_t *status, uint32_t bit) {
+    if ((*reinterpret_cast<volatile uint32_t *>(status) & bit) == 0u) atomicOr(status, bit);
+}
+
 constexpr float kFxScale = 17592186044416.0f;  // 2^44
 __device__ __forceinline__ long long to_fx(float v) { return __float2ll_rn(v * kFxScale); }
 __device__ __forceinline__ float from_fx(long long q) { return __ll2float_rn(q) * (1.0f / kFxScale); }

@@ -263,7 +263,7 @@ __device__ __forceinline__ bool update_cell(float f[Q], float g[QT], int x, int 
     // one status update per warp (every lane of the warp runs this): a
     // diverged solve would otherwise send an atomic from every cell
     const unsigned badw = __ballot_sync(0xffffffffu, valid && !(rho > 0.0f && rho < 100.0f));
-    if (badw && (threadIdx.x & 31) == 0) atomicOr(&ds->status, ST_RHO_RANGE);
+    if (badw && (threadIdx.x & 31) == 0) raise_status(&ds->status, ST_RHO_RANGE);
     if (mom != nullptr && valid) {
         mom[cell] = rho;
         mom[N + cell] = ux;

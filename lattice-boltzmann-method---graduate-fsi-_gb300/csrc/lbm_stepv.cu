@@ -282,7 +282,7 @@ __global__ void __launch_bounds__(128, (stepv_min_blocks<T, NP, THERMAL>()))
         }
     }
     const unsigned badw = __ballot_sync(0xffffffffu, valid && bad);
-    if (badw && lane == 0) atomicOr(&ds->status, ST_RHO_RANGE);
+    if (badw && lane == 0) raise_status(&ds->status, ST_RHO_RANGE);
     if (!valid) return;
     T *pb = B + c0;
 #pragma unroll

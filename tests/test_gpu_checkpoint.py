@@ -23,17 +23,26 @@ def test_cavity_restart_is_bitwise(pkg, tmp_path, storage):
         assert np.array_equal(ma[c], mb[c]), c
 
 
-def test_sphere_restart_continues(pkg, orc, tmp_path):
-    """IBM sphere (force history and markers restored); the spreading sums in
-    float atomics, so the continuation agrees to rounding."""
+@pytest.mark.parametrize("free", [False, True], ids=["fixed", "free_thermal"])
+def test_sphere_restart_is_bitwise(pkg, orc, tmp_path, free):
+    """IBM sphere, fixed or free in six degrees of freedom with the D3Q7
+    population (force history, markers and the FP64 body restored).  The
+    spreading sums in 64-bit fixed point, independent of the order of the
+    atomics, so the continuation equals the uninterrupted run bit for bit."""
     nx, ny, nz, D, nm = 48, 32, 28, 8.0, 201
     center = (14.0, 16.0, 14.0)
     mk = orc.fibonacci_sphere(nm, D, center)
     xyz = np.stack([mk["x"], mk["y"], mk["z"]])
 
     def solver():
-        s = pkg.Solver(pkg.channel_config(nx, ny, nz, 0.56, u_in=0.05))
-        s.set_markers(xyz, mk["ds"], D / 2.0, center, m_max=3)
+        kw = dict(thermal=True, tau_g=0.7, T_in=0.0, gbeta=(0.0, 1e-5, 0.0)) if free else {}
+        s = pkg.Solver(pkg.channel_config(nx, ny, nz, 0.56, u_in=0.05, **kw))
+        mkw = {}
+        if free:
+            vol = np.pi * D ** 3 / 6.0
+            mkw = dict(free_body=True, density_ratio=1.5, volume=vol, inertia=0.4 * 1.5 * vol * (D / 2) ** 2,
+                       gravity=(0.0, -1e-5, 0.0), free_dofs=63, virtual_mass=1.0, thermal=True, T_body=1.0)
+        s.set_markers(xyz, mk["ds"], D / 2.0, center, m_max=3, **mkw)
         return s
 
     path = str(tmp_path / "sph.ckpt")
@@ -45,11 +54,16 @@ def test_sphere_restart_continues(pkg, orc, tmp_path):
     b = solver()
     b.load_state(path)
     b.step(30)
+    assert a.status() == 0 and b.status() == 0
     fa, fb = a.forces(), b.forces()
     assert fa.shape == fb.shape == (60, 8)
-    assert np.array_equal(fa[:30], fb[:30])
-    assert np.abs(fa[30:, :3] - fb[30:, :3]).max() / np.abs(fa[:, 0]).max() < 1e-4
-    assert np.abs(a.moments()["ux"] - b.moments()["ux"]).max() / 0.05 < 1e-5
+    assert np.array_equal(fa, fb)
+    ma, mb = a.moments(), b.moments()
+    for c in ma:
+        assert np.array_equal(ma[c], mb[c]), c
+    if free:
+        assert np.array_equal(a.body(), b.body())
+        assert np.array_equal(a.markers(), b.markers())
 
 
 def test_restart_rejects_other_configuration(pkg, tmp_path):

@@ -82,9 +82,9 @@ def test_default_cells_per_thread(pkg):
 
 def test_multicell_sphere_matches_single_cell(pkg, orc):
     """The fixed IBM sphere with the near box carved out of the multi-cell far
-    region (its x bounds rounded to whole segments): the same drag and fields
-    as the one-cell-per-thread kernel up to the order of the float atomics of
-    the spreading (FP32 storage, where that order moves u by ~1e-7 U)."""
+    region (its x bounds rounded to whole segments): the same forces and
+    fields as the one-cell-per-thread kernel, bit for bit (the spreading sums
+    in fixed point, independent of the order of its atomics)."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
     center = (23.3, 20.2, 19.6)
     out = []
@@ -99,7 +99,6 @@ def test_multicell_sphere_matches_single_cell(pkg, orc):
         out.append((s.forces(), s.moments(), s.cells_per_thread()))
         s.close()
     assert out[0][2] == 1 and out[1][2] == 4
-    fa, fb = out[0][0], out[1][0]
-    assert np.abs(fa[:, :3] - fb[:, :3]).max() / np.abs(fa[:, 0]).max() < 1e-4
-    for c in ("ux", "uy", "uz"):
-        assert np.abs(out[0][1][c] - out[1][1][c]).max() / 0.05 < 1e-5, c
+    assert np.array_equal(out[0][0], out[1][0])
+    for c in out[0][1]:
+        assert np.array_equal(out[0][1][c], out[1][1][c]), c
