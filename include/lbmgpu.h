@@ -113,8 +113,9 @@ typedef struct lbm_config {
     int cells_per_thread; /* D3Q19 fused step: consecutive x-cells per thread, moved as one 4-, 8- or
                              16-byte access per population row and updated in pairs with the packed FP32
                              instructions (FP16/BF16: 2, 4 or 8; FP32: 2 or 4); 0 = default (2 for
-                             FP16/BF16, 1 for FP32); 1 = one cell per thread.  Needs nx a multiple of it,
-                             else one cell per thread is used.  Results are identical either way. */
+                             FP16/BF16 on lattices of 2^20 cells or more, else 1); 1 = one cell per
+                             thread.  Needs nx a multiple of it, else one cell per thread is used.
+                             Results are identical either way. */
 } lbm_config;
 
 /* lbm_config.thermal: 0 none; 1 a D3Q7 temperature population with a heat

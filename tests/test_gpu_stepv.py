@@ -70,12 +70,17 @@ def test_multicell_step_matches_single_cell_bitwise(pkg, case, storage):
 
 
 def test_default_cells_per_thread(pkg):
+    # two cells a thread for half storage on lattices of 2^20 cells or more
     for storage, v in (("f32", 1), ("f16", 2), ("bf16", 2)):
-        s = pkg.Solver(pkg.cavity_config(64, tau=0.7, lid=0.05, ny=8, nz=8, storage=storage))
+        s = pkg.Solver(pkg.cavity_config(128, tau=0.7, lid=0.05, ny=128, nz=64, storage=storage))
         assert s.cells_per_thread() == v, storage
         s.close()
+    # smaller lattices sit in L2 and run one cell a thread
+    s = pkg.Solver(pkg.cavity_config(64, tau=0.7, lid=0.05, ny=64, nz=64, storage="f16"))
+    assert s.cells_per_thread() == 1
+    s.close()
     # a row length that is not a multiple of the segment: one cell per thread
-    s = pkg.Solver(pkg.cavity_config(31, tau=0.7, lid=0.05, ny=8, nz=8, storage="f16"))
+    s = pkg.Solver(pkg.cavity_config(31, tau=0.7, lid=0.05, ny=256, nz=256, storage="f16"))
     assert s.cells_per_thread() == 1
     s.close()
 
