@@ -488,6 +488,7 @@ lbm_status lbmgpu_serve_run(const lbm_serve_request *reqs, int n, const lbm_serv
                             lbm_serve_result *out, double *lattice_updates);
 
 const char *lbmgpu_last_error(void);
+/* 2: lbm_config.cells_per_thread and lbm_ibm_config.virtual_mass appended */
 int lbmgpu_abi_version(void);
 
 #ifdef __cplusplus
