@@ -303,8 +303,9 @@ lbm_status lbmgpu_update_markers(lbm_handle *h, const double *xyz, const double 
  * from its set-up): the current populations, the device state (step counters,
  * band origin, rigid body), the markers and the force histories.  Load onto a
  * handle created with the same configuration and the same lbmgpu_set_markers /
- * lbmgpu_set_solids calls, instead of lbmgpu_init; the run then continues as
- * if never interrupted. */
+ * lbmgpu_set_solids (D2Q9: lbmgpu_set_marker_normals) calls, instead of
+ * lbmgpu_init; the run then continues as if never interrupted, bit for bit.
+ * D3Q19 and D2Q9 handles (each its own file format). */
 lbm_status lbmgpu_save_state(lbm_handle *h, const char *path);
 lbm_status lbmgpu_load_state(lbm_handle *h, const char *path);
 

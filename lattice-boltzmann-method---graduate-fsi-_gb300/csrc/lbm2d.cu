@@ -23,6 +23,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -1087,7 +1088,9 @@ struct lbm2d {
     Ibm2 ib;
     double *hist = nullptr;
     long long hist_cap = 1 << 16;
-    cudaGraphExec_t gexec = nullptr;
+    // graphs of gsteps steps, one per parity of the buffer they start from
+    // (a graph reads and writes fixed buffers)
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;
     int tx = 128, ty = 2;
     // ENERGY: g ping-pong, per-cell history of the last collision
@@ -1518,7 +1521,8 @@ lbm_status l2d_create(lbm_handle *h) {
 void l2d_free(lbm_handle *h) {
     lbm2d *d = h->d2;
     if (!d) return;
-    if (d->gexec) cudaGraphExecDestroy(d->gexec);
+    for (int i = 0; i < 2; i++)
+        if (d->gexec[i]) cudaGraphExecDestroy(d->gexec[i]);
     for (void *p : d->allocs) cudaFree(p);
     delete d;
     h->d2 = nullptr;
@@ -1561,9 +1565,10 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
     d->cur = 0;
     h->steps = 0;
     h->inited = true;
-    if (d->gexec) {
-        cudaGraphExecDestroy(d->gexec);
-        d->gexec = nullptr;
+    for (int i = 0; i < 2; i++) {
+        if (!d->gexec[i]) continue;
+        cudaGraphExecDestroy(d->gexec[i]);
+        d->gexec[i] = nullptr;
     }
     return LBM_OK;
 }
@@ -1652,9 +1657,10 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
     CK2(cudaStreamSynchronize(h->s));
     d->ibm = true;
     d->kin_ready = false;
-    if (d->gexec) {
-        cudaGraphExecDestroy(d->gexec);
-        d->gexec = nullptr;
+    for (int i = 0; i < 2; i++) {
+        if (!d->gexec[i]) continue;
+        cudaGraphExecDestroy(d->gexec[i]);
+        d->gexec[i] = nullptr;
     }
     return LBM_OK;
 }
@@ -1692,7 +1698,8 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
         left--;
     }
     if (d->gsteps > 0 && left >= d->gsteps) {
-        if (!d->gexec) {
+        cudaGraphExec_t &gx = d->gexec[d->cur];
+        if (!gx) {
             cudaGraph_t g;
             const long long s0 = h->steps;
             const int c0 = d->cur;
@@ -1702,12 +1709,12 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
             h->steps = s0;
             d->cur = c0;
             CK2(e);
-            e = cudaGraphInstantiate(&d->gexec, g, 0);
+            e = cudaGraphInstantiate(&gx, g, 0);
             cudaGraphDestroy(g);
             CK2(e);
         }
         while (left >= d->gsteps) {
-            CK2(cudaGraphLaunch(d->gexec, h->s));
+            CK2(cudaGraphLaunch(gx, h->s));
             h->steps += d->gsteps;
             left -= d->gsteps;
         }
@@ -1806,6 +1813,65 @@ lbm_status l2d_vtk_snapshot(lbm_handle *h, float *host, std::vector<float> &boxF
     }
     memset(host + 3 * N, 0, N * sizeof(float));
     if (d->energy) memset(host + 7 * N, 0, N * sizeof(float));
+    return LBM_OK;
+}
+
+// Checkpoint regions: the populations of buffer src (and the ENERGY g and
+// per-cell history), the device state (box, body, step, lists flag), the
+// force history, and the markers' positions and nearest nodes (a fixed body
+// finds them on its first step only).  The spreading lists are not saved:
+// the restore marks them stale and the next pass rebuilds the same ones.
+std::vector<l2d_region> l2d_checkpoint_regions(lbm_handle *h, int src) {
+    lbm2d *d = h->d2;
+    if (src < 0) src = d->cur;
+    std::vector<l2d_region> r;
+    const size_t es = h->cfg.storage == LBM_STORE_F32 ? 4 : 2;
+    r.push_back({d->f[src], (size_t)Q9 * d->P.S * es, 1});
+    if (d->energy) {
+        r.push_back({d->g[src], (size_t)Q9 * d->P.S * sizeof(float), 1});
+        r.push_back({d->aux, (size_t)d->P.N * sizeof(float4), 0});
+    }
+    r.push_back({d->st, sizeof(State2), 0});
+    r.push_back({d->hist, (size_t)d->hist_cap * 4 * sizeof(double), 0});
+    if (d->ibm) {
+        r.push_back({d->ib.pos, (size_t)3 * d->ib.n * sizeof(double), 0});
+        r.push_back({d->ib.qnear, (size_t)d->ib.n * sizeof(int), 0});
+    }
+    return r;
+}
+
+// lattice extents, storage, ENERGY, markers, solid cells, stride, history
+void l2d_checkpoint_shape(lbm_handle *h, int shape[8]) {
+    lbm2d *d = h->d2;
+    shape[0] = d->P.nx;
+    shape[1] = d->P.ny;
+    shape[2] = h->cfg.storage;
+    shape[3] = d->energy ? 1 : 0;
+    shape[4] = d->ibm ? d->ib.n : 0;
+    shape[5] = d->links ? 1 : 0;
+    shape[6] = (int)(d->P.S & 0x7fffffff);
+    shape[7] = (int)d->hist_cap;
+}
+
+lbm_status l2d_checkpoint_restored(lbm_handle *h, long long steps) {
+    lbm2d *d = h->d2;
+    d->cur = 0;
+    h->steps = steps;
+    h->inited = true;
+    if (d->ibm) {
+        // the lists are rebuilt by the next pass; the box of the next step is
+        // in the restored state, or made by the step-1 kinematics
+        const int zero = 0;
+        CK2(cudaMemcpyAsync(reinterpret_cast<char *>(d->st) + offsetof(State2, lists_ok), &zero, sizeof(int),
+                            cudaMemcpyHostToDevice, h->s));
+        d->kin_ready = steps > 0;
+    }
+    for (int i = 0; i < 2; i++) {
+        if (!d->gexec[i]) continue;
+        cudaGraphExecDestroy(d->gexec[i]);
+        d->gexec[i] = nullptr;
+    }
+    CK2(cudaStreamSynchronize(h->s));
     return LBM_OK;
 }
 

@@ -82,11 +82,75 @@ CkptHeader header_of(lbm_handle *h) {
     return c;
 }
 
+// D2Q9 handles: a header of the configuration's shape and the step count,
+// then the regions of l2d_checkpoint_regions.
+const char kMagic2[8] = {'L', 'B', 'M', 'G', 'P', 'U', '2', 'D'};
+
+struct Ckpt2Header {
+    char magic[8];
+    int shape[8];
+    long long steps;
+};
+
+lbm_status save_2d(lbm_handle *h, const char *path) {
+    if (!h->inited) return ck_fail(LBM_ERR_STATE, "save_state: call lbmgpu_init first");
+    if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
+    FILE *fp = fopen(path, "wb");
+    if (!fp) return ck_fail(LBM_ERR_INVALID, std::string("save_state: cannot open ") + path);
+    Ckpt2Header c;
+    memset(&c, 0, sizeof(c));
+    memcpy(c.magic, kMagic2, 8);
+    l2d_checkpoint_shape(h, c.shape);
+    c.steps = h->steps;
+    bool ok = fwrite(&c, sizeof(c), 1, fp) == 1;
+    std::vector<char> buf;
+    for (const l2d_region &r : l2d_checkpoint_regions(h, -1)) {
+        if (!ok) break;
+        buf.resize(r.bytes);
+        ok = cudaMemcpy(buf.data(), r.dev, r.bytes, cudaMemcpyDeviceToHost) == cudaSuccess &&
+             fwrite(buf.data(), 1, r.bytes, fp) == r.bytes;
+    }
+    if (fclose(fp) != 0) ok = false;
+    if (!ok) return ck_fail(LBM_ERR_CUDA, std::string("save_state: write failed: ") + path);
+    return LBM_OK;
+}
+
+lbm_status load_2d(lbm_handle *h, const char *path) {
+    if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
+    FILE *fp = fopen(path, "rb");
+    if (!fp) return ck_fail(LBM_ERR_INVALID, std::string("load_state: cannot open ") + path);
+    Ckpt2Header c;
+    int mine[8];
+    l2d_checkpoint_shape(h, mine);
+    if (fread(&c, sizeof(c), 1, fp) != 1 || memcmp(c.magic, kMagic2, 8) != 0) {
+        fclose(fp);
+        return ck_fail(LBM_ERR_INVALID, "load_state: not a D2Q9 state file");
+    }
+    if (memcmp(c.shape, mine, sizeof(mine)) != 0) {
+        fclose(fp);
+        return ck_fail(LBM_ERR_INVALID, "load_state: the file was saved from a different configuration");
+    }
+    std::vector<char> buf;
+    bool ok = true;
+    const std::vector<l2d_region> r0 = l2d_checkpoint_regions(h, 0), r1 = l2d_checkpoint_regions(h, 1);
+    for (size_t i = 0; i < r0.size() && ok; i++) {
+        buf.resize(r0[i].bytes);
+        ok = fread(buf.data(), 1, r0[i].bytes, fp) == r0[i].bytes &&
+             cudaMemcpy(r0[i].dev, buf.data(), r0[i].bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+        // both buffers alike: solid cells (never rewritten) read either
+        if (ok && r0[i].both)
+            ok = cudaMemcpy(r1[i].dev, buf.data(), r0[i].bytes, cudaMemcpyHostToDevice) == cudaSuccess;
+    }
+    fclose(fp);
+    if (!ok) return ck_fail(LBM_ERR_INVALID, std::string("load_state: read failed: ") + path);
+    return l2d_checkpoint_restored(h, c.steps);
+}
+
 }  // namespace
 
 extern "C" lbm_status lbmgpu_save_state(lbm_handle *h, const char *path) {
     if (!h || !path) return ck_fail(LBM_ERR_INVALID, "save_state: null argument");
-    if (h->d2) return ck_fail(LBM_ERR_UNSUPPORTED, "save_state: not for D2Q9 handles");
+    if (h->d2) return save_2d(h, path);
     if (!h->inited) return ck_fail(LBM_ERR_STATE, "save_state: call lbmgpu_init first");
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     FILE *fp = fopen(path, "wb");
@@ -107,7 +171,7 @@ extern "C" lbm_status lbmgpu_save_state(lbm_handle *h, const char *path) {
 
 extern "C" lbm_status lbmgpu_load_state(lbm_handle *h, const char *path) {
     if (!h || !path) return ck_fail(LBM_ERR_INVALID, "load_state: null argument");
-    if (h->d2) return ck_fail(LBM_ERR_UNSUPPORTED, "load_state: not for D2Q9 handles");
+    if (h->d2) return load_2d(h, path);
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     FILE *fp = fopen(path, "rb");
     if (!fp) return ck_fail(LBM_ERR_INVALID, std::string("load_state: cannot open ") + path);

@@ -101,6 +101,18 @@ lbm_status l2d_mea_box(lbm_handle *h, const int box[6], double out[3]);
 // else [4][N]), and with an IBM body the force the box cells collided with
 // ([2][nb], box order) and the box {x0, y0, width, height} of that pass.
 lbm_status l2d_vtk_snapshot(lbm_handle *h, float *host, std::vector<float> &boxF, int box[4]);
+// Checkpoint of a D2Q9 handle: the device regions the next step reads (the
+// populations of buffer `src`, the current one when src < 0), a description
+// of the configuration for the
+// header, and the host-side state set after the regions were written back.
+struct l2d_region {
+    void *dev;
+    size_t bytes;
+    int both;  // 1: the populations, written into both buffers on restore
+};
+std::vector<l2d_region> l2d_checkpoint_regions(lbm_handle *h, int src);
+void l2d_checkpoint_shape(lbm_handle *h, int shape[8]);
+lbm_status l2d_checkpoint_restored(lbm_handle *h, long long steps);
 int l2d_marker_count(lbm_handle *h);
 
 // Launch the gather-only export of the current state's moments into h->mom

@@ -76,3 +76,76 @@ def test_restart_rejects_other_configuration(pkg, tmp_path):
     with pytest.raises(pkg.LbmError) as e:
         b.load_state(path)
     assert e.value.status == 1
+
+
+@pytest.mark.parametrize("case", ["cylinder", "transverse", "energy", "staircase"])
+def test_d2q9_restart_is_bitwise(pkg, orc, tmp_path, case):
+    """D2Q9 handles: the reference's default cylinder (fixed body, nearest-node
+    density, added mass), its transverse oscillation (moving markers and box),
+    the ENERGY Couette channel (g and the per-cell history) and the tandem
+    staircase circles (interior solid cells); saved after 30 steps, restored
+    onto a fresh handle of the same set-up, 30 more steps equal the
+    uninterrupted run bit for bit."""
+    import os
+
+    from conftest import GOLDEN
+
+    def make():
+        if case in ("cylinder", "transverse"):
+            from test_gpu_d2q9 import _cylinder_solver
+
+            if case == "cylinder":
+                g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_100.npz"))
+                return _cylinder_solver(pkg, orc, g, m_max=int(g["m_max"]))[0]
+            g = np.load(os.path.join(GOLDEN, "cylinder80x40_D10_n40_m5_transverse_100.npz"))
+            D = float(g["D"])
+            return _cylinder_solver(pkg, orc, g, m_max=5, u_max=0.05, Re=100.0, marker_dy=2.0,
+                                    vsolid=orc.REF_PI * D * D * 0.25 * 3, motion=pkg.MOTION_TRANSVERSE_OSC,
+                                    motion_amp=2.0, motion_freq=0.005)[0]
+        if case == "energy":
+            from test_gpu_energy import _solver
+
+            return _solver(pkg, orc, 30, 20.0, tau=0.8, nx=6)[0]
+        from test_gpu_d2q9 import STAIRCASE, _staircase_gpu
+
+        return _staircase_gpu(pkg, orc, [c for c in STAIRCASE if c[0] == "tandem"][0])[0]
+
+    path = str(tmp_path / "d2.ckpt")
+    a = make()
+    a.step(30)
+    a.save_state(path)
+    a.step(30)
+    b = make()
+    b.load_state(path)
+    b.step(30)
+    assert a.status() == 0 and b.status() == 0
+    ma, mb = a.moments(), b.moments()
+    for c in ma:
+        assert np.array_equal(ma[c], mb[c]), c
+    if case in ("cylinder", "transverse"):
+        assert np.array_equal(a.forces(), b.forces())
+        assert np.array_equal(a.markers(), b.markers())
+    if case == "energy":
+        assert np.array_equal(a.download_f32(pkg.FIELD_QX), b.download_f32(pkg.FIELD_QX))
+
+
+def test_d2q9_restart_rejects_other_files(pkg, orc, tmp_path):
+    """A D3Q19 state file, or one of another D2Q9 lattice, is refused."""
+    from test_gpu_energy import _solver
+
+    p3 = str(tmp_path / "c3.ckpt")
+    a = pkg.Solver(pkg.cavity_config(16, tau=0.7))
+    a.init()
+    a.step(2)
+    a.save_state(p3)
+    s, _ = _solver(pkg, orc, 30, 20.0, tau=0.8, nx=6)
+    with pytest.raises(pkg.LbmError) as e:
+        s.load_state(p3)
+    assert e.value.status == 1
+    p2 = str(tmp_path / "c2.ckpt")
+    s.step(3)
+    s.save_state(p2)
+    t, _ = _solver(pkg, orc, 20, 20.0, tau=0.8, nx=6)
+    with pytest.raises(pkg.LbmError) as e:
+        t.load_state(p2)
+    assert e.value.status == 1
