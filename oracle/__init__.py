@@ -36,6 +36,10 @@ CX19 = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
 CY19 = np.array([0, 0, 0, 1, -1, 0, 0, 1, -1, 0, 0, 1, -1, -1, 1, 0, 0, 1, -1])
 CZ19 = np.array([0, 0, 0, 0, 0, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0, -1, 1, -1, 1])
 W19 = np.array([1 / 3] + [1 / 18] * 6 + [1 / 36] * 12)
+# D2Q9 in the reference order (LBM.h:533-537)
+CX9 = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+CY9 = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+CZ9 = np.zeros(9, dtype=np.int64)
 REF_PI = 3.14159265
 
 
@@ -708,13 +712,13 @@ def details(lat: Lattice) -> dict:
     sigma[a][b] = -(tau - 0.5) * sum_l f_l (c_la - u_a)(c_lb - u_b) / tau,
     summed over l in the reference order.  sigma is returned as the six
     distinct components (SYM6 order), shape (6, NZ, NY, NX)."""
-    c = (CX19, CY19, CZ19)
+    c = (CX19, CY19, CZ19) if lat.q == 19 else (CX9, CY9, CZ9)
     u = (lat.ux, lat.uy, lat.uz)
     f = lat.f
     sig = np.empty((6,) + lat.shape)
     for s, (a, b) in enumerate(SYM6):
         acc = np.zeros(lat.shape)
-        for l in range(19):
+        for l in range(lat.q):
             acc = acc + f[l] * (c[a][l] - u[a]) * (c[b][l] - u[b])
         sig[s] = -(lat.tau - 0.5) * acc / lat.tau
     return {"p": lat.rho / 3.0, "sigma": sig}
@@ -760,6 +764,27 @@ def cavity_details_run(n: int, tau: float, lid: float, steps: int, nt: int = 10)
     step and Sup_MacroProp every nt steps (main.cpp:214-223, 389).  Returns
     the lattice, the last details() and the statistics, ghosts included."""
     lat = cavity(n, tau, lid)
+    stats = SupStats(lat.shape)
+    det = None
+    for s in range(1, steps + 1):
+        lat.collide()
+        lat.stream()
+        lat.macro()
+        if s % nt == 0:
+            det = details(lat)
+            stats.update(s, nt, 1.0, (lat.ux, lat.uy, lat.uz), det["p"])
+    if det is None:
+        det = details(lat)
+    return lat, det, stats
+
+
+def staircase2d_details_run(kind: str, nx: int, ny: int, D: float, Re: float, u_max: float, steps: int,
+                            lpd: float = 1.5, nb: int = 1, nt: int = 10):
+    """A staircase 2D case in MORE_DETAILS mode: Collision, Streaming,
+    MacroProp every step and Sup_MacroProp every nt steps (main.cpp:214-223,
+    389).  Returns the lattice, the last details() and the statistics,
+    ghosts included (the reference's D2Q9 grid has three k layers)."""
+    lat, boxes, area = staircase2d(kind, nx, ny, D, Re, u_max, lpd, nb)
     stats = SupStats(lat.shape)
     det = None
     for s in range(1, steps + 1):

@@ -20,6 +20,7 @@
 #   cylbasic:NX:NY:D:RE:U     D2Q9 staircase cylinder, momentum-exchange Cl/Cd (Cylinder_Basic)
 #   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
 #   triangle:NX:NY:D:RE:U:LPD:NB  D2Q9 staircase triangles in tandem (Cylinder_Tandem_Triangle)
+#   triangled:NX:NY:D:RE:U:LPD:NB the same in MORE_DETAILS mode
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${REF:-}
@@ -98,12 +99,13 @@ for v in "$@"; do
         $CXX $FLAGS -DREF_CYLBASIC -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_RE=$re -DREF_U=$u -o "$exe" \
             "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
-    tandem|triangle)
+    tandem|triangle|triangled)
         kind=$(echo "$v" | cut -d: -f1)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)
         re=$(echo "$v" | cut -d: -f5); u=$(echo "$v" | cut -d: -f6); lpd=$(echo "$v" | cut -d: -f7)
         nb=$(echo "$v" | cut -d: -f8)
         flag=-DREF_TANDEM; [ "$kind" = triangle ] && flag=-DREF_TRIANGLE
+        [ "$kind" = triangled ] && flag="-DREF_TRIANGLE -DREF_DETAILS"
         exe="$OUT/ref_${kind}_${nx}_${ny}_${d}_${re}_${u}_${lpd}_${nb}"
         $CXX $FLAGS $flag -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_RE=$re -DREF_U=$u -DREF_LPD=$lpd \
             -DREF_NB=$nb -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &

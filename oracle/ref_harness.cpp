@@ -16,6 +16,8 @@
 
 #include <omp.h>
 
+#include <sys/stat.h>
+
 #include <cstdio>
 #include <cstdlib>
 #include <vector>
@@ -214,6 +216,10 @@ int main(int argc, char **argv) {
         lb.Collision();
         lb.Streaming();
         lb.MacroProp();
+#if defined MORE_DETAILS
+        // the call of main.cpp:389, made at the output cadence (main.cpp:223)
+        if (step % Nt == 0) lb.Sup_MacroProp(step);
+#endif
         for (int n = 0; n < nb; n++) {
 #if defined REF_CYLBASIC
             CL[n].push_back(MEA_CL(lb, center_x - D, center_x + D, center_y - D, center_y + D, 1, 1));
@@ -237,7 +243,27 @@ int main(int argc, char **argv) {
         fwrite(CL[n].data(), sizeof(double), CL[n].size(), fp);
         fwrite(CD[n].data(), sizeof(double), CD[n].size(), fp);
     }
+#if defined MORE_DETAILS
+    for (int w = 7; w <= 42; w++) dump_field(lb, fp, w);
+#endif
     fclose(fp);
+#if defined MORE_DETAILS && defined REF_TRIANGLE
+    // the reference's own writers, into the folders it names for this case
+    // (lbm.cpp:2299-2301, 2654-2658): Flowfield/field000000.vtr and
+    // avgfield.vtr under "./output Tandem Triangle/LpD = .. Re = ..", which
+    // must exist
+    if (argc > 4) {
+        char dir[128], sub[160];
+        snprintf(dir, sizeof(dir), "./output Tandem Triangle/LpD = %.1f Re = %.0f", LpD, Re);
+        snprintf(sub, sizeof(sub), "%s/Flowfield", dir);
+        mkdir("./output Tandem Triangle", 0755);
+        mkdir(dir, 0755);
+        mkdir(sub, 0755);
+        int nout = 0;
+        OutputVTK(nout, lb);
+        OutputAVGVTK(nout, lb);
+    }
+#endif
     // the solid cells of the set-up, layer k = 1 (x fastest)
     if (argc > 3) {
         FILE *fs = fopen(argv[3], "wb");

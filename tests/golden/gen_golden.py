@@ -129,6 +129,44 @@ def cylinder_vtk(tmp: str) -> None:
     np.savez_compressed(os.path.join(OUT, "cylinder80x40_vtk_100.npz"), steps=100, **v)
 
 
+def triangle_details(tmp: str) -> None:
+    """The reference's Cylinder_Tandem_Triangle in MORE_DETAILS mode (D2Q9,
+    60 x 40, D = 10, two triangles 1.5 D apart, Re = 100, u = 0.05), 200
+    steps with Sup_MacroProp every Nt = 10: the k = 1 layer of rho, u, the
+    pressure, the viscous stress and the running statistics, the
+    momentum-exchange Cl / Cd of both bodies after every step, the cell
+    types, and the reference's own OutputVTK and OutputAVGVTK files."""
+    nx, ny, nb, steps = 60, 40, 2, 200
+    d = os.path.join(tmp, "trid")
+    os.makedirs(d)
+    p, pt = os.path.join(d, "tri.bin"), os.path.join(d, "tri.types")
+    subprocess.check_call([os.path.join(REF, "ref_triangled_60_40_10_100.0_0.05_1.5_2"), str(steps), p, pt, "vtk"],
+                          cwd=d)
+    n3 = (nx + 2) * (ny + 2) * 3
+    a = np.fromfile(p)
+    f4 = a[:4 * n3].reshape(4, 3, ny + 2, nx + 2)[:, 1]
+    rest = a[4 * n3:4 * n3 + nb * 2 * steps].reshape(nb, 2, steps)
+    det = a[4 * n3 + nb * 2 * steps:].reshape(36, 3, ny + 2, nx + 2)[:, 1]
+    # details order: pressure, sigma[3][3], avg_velocity, avg_pressure,
+    # avg_ReynoldStress, rms_velocity, rms_pressure, rms_ReynoldStress
+    sym = {}
+    for base, name in ((1, "sigma"), (14, "avg_rs"), (27, "rms_rs")):
+        t = det[base:base + 9].reshape(3, 3, ny + 2, nx + 2)
+        for i in range(3):
+            for j in range(i):
+                assert np.array_equal(t[i, j], t[j, i]), (name, i, j)
+        sym[name] = np.stack([t[0, 0], t[0, 1], t[0, 2], t[1, 1], t[1, 2], t[2, 2]])
+    base = os.path.join(d, "output Tandem Triangle", "LpD = 1.5 Re = 100")
+    v = read_vtr(os.path.join(base, "Flowfield", "field000000.vtr"))
+    w = read_vtr(os.path.join(base, "avgfield.vtr"))
+    types = np.fromfile(pt, dtype=np.uint8).reshape(ny + 2, nx + 2)
+    np.savez_compressed(os.path.join(OUT, "triangle60x40_details_200.npz"), rho=f4[0], u=f4[1:4], p=det[0],
+                        sigma=sym["sigma"], avg_u=det[10:13], avg_p=det[13], avg_rs=sym["avg_rs"],
+                        rms_u=det[23:26], rms_p=det[26], rms_rs=sym["rms_rs"], cl=rest[:, 0], cd=rest[:, 1],
+                        types=types, nx=nx, ny=ny, D=10, Re=100.0, u_in=0.05, lpd=1.5, nb=nb, steps=steps, nt=10,
+                        **{"vtk_" + k: x for k, x in v.items()}, **{"avgvtk_" + k: x for k, x in w.items()})
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -139,7 +177,13 @@ def main() -> None:
     ap.add_argument("--skip-cav64", action="store_true")
     ap.add_argument("--only-cylinder-vtk", action="store_true",
                     help="write only cylinder80x40_vtk_100.npz (the D2Q9 OutputVTK / OutputVTK_Marker files)")
+    ap.add_argument("--only-triangle-details", action="store_true",
+                    help="write only triangle60x40_details_200.npz (D2Q9 MORE_DETAILS, both VTK files)")
     a = ap.parse_args()
+    if a.only_triangle_details:
+        oracle.build_ref("triangled:60:40:10:100.0:0.05:1.5:2")
+        triangle_details(tempfile.mkdtemp())
+        return
     if a.only_cylinder_vtk:
         oracle.build_ref("cylinder:80:40:10:40:5")
         cylinder_vtk(tempfile.mkdtemp())
@@ -147,7 +191,7 @@ def main() -> None:
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
                      "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",
-                     "poiseuille:30:20:energy", *STAIRCASE_VARIANTS)
+                     "poiseuille:30:20:energy", "triangled:60:40:10:100.0:0.05:1.5:2", *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -262,6 +306,7 @@ def main() -> None:
         np.savez_compressed(os.path.join(OUT, "staircase2d_%s_300.npz" % name), cl=rest[:, 0], cd=rest[:, 1],
                             types=types, window=fl[:, wr, wc], wrows=np.array([wr.start, wr.stop]),
                             wcols=np.array([wc.start, wc.stop]), sums=fl.reshape(3, -1).sum(axis=1), steps=300)
+    triangle_details(tmp)
     print("golden fixtures written to", OUT)
 
 

@@ -140,6 +140,25 @@ def test_more_details_match_reference(orc):
     assert abs(g["rms_p"][0, 0, 0] - np.sqrt(190.0 / 191.0) / 3.0) < 1e-15
 
 
+def test_triangle_details_matches_reference(orc):
+    """The reference's Cylinder_Tandem_Triangle in MORE_DETAILS mode (D2Q9,
+    triangled variant of oracle/build_ref.sh): after 200 steps with
+    Sup_MacroProp every 10, rho, u, the pressure, the viscous stress and the
+    running statistics of the k = 1 layer, within 1e-13 as the other staircase
+    fixtures (measured 8e-16)."""
+    g = np.load(os.path.join(GOLDEN, "triangle60x40_details_200.npz"))
+    lat, det, st = orc.staircase2d_details_run("triangle", int(g["nx"]), int(g["ny"]), float(g["D"]),
+                                               float(g["Re"]), float(g["u_in"]), int(g["steps"]), float(g["lpd"]),
+                                               int(g["nb"]), int(g["nt"]))
+    assert np.abs(lat.rho[1] - g["rho"]).max() < 1e-13
+    assert np.abs(np.stack([lat.ux[1], lat.uy[1], lat.uz[1]]) - g["u"]).max() < 1e-13
+    assert np.abs(det["p"][1] - g["p"]).max() < 1e-13
+    assert np.abs(det["sigma"][:, 1] - g["sigma"]).max() < 1e-13
+    for k in ("avg_u", "avg_p", "avg_rs", "rms_u", "rms_p", "rms_rs"):
+        a = getattr(st, k)
+        assert np.abs((a[:, 1] if a.ndim == 4 else a[1]) - g[k]).max() < 1e-13, k
+
+
 def moving_case_kwargs(orc, case, D=10.0):
     """Cylinder2D options of the moving-body cases in fluid at rest."""
     if case == "inline":
