@@ -333,7 +333,10 @@ enum { LBM_STAT_AVG_U = 0, LBM_STAT_AVG_P = 3, LBM_STAT_AVG_RS = 4, LBM_STAT_RMS
 /* on = 1: allocate the detail and statistics arrays (7 floats + 20 doubles
  * per cell), clear the statistics, and add the Pressure / Viscous Stress /
  * Vorticity arrays of the reference's MORE_DETAILS OutputVTK to
- * lbmgpu_output_vtk_async.  on = 0 frees them. */
+ * lbmgpu_output_vtk_async.  on = 0 frees them.  D2Q9 handles too (their
+ * z components are zero), except those with markers: the reference's IBM
+ * loop never calls MacroProp, which forms the details (LBM_ERR_UNSUPPORTED,
+ * in either order of this call and lbmgpu_set_markers). */
 lbm_status lbmgpu_set_more_details(lbm_handle *h, int on);
 /* Pressure and viscous stress of the current state, [LBM_DETAIL_COUNT][cells]. */
 lbm_status lbmgpu_download_details(lbm_handle *h, float *host);

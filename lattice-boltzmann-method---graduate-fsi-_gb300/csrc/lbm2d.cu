@@ -189,6 +189,105 @@ __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__re
     for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
 }
 
+// MORE_DETAILS on D2Q9 (LBM.h:55): of the current (streamed) state, the
+// pressure p = rho / 3 (lbm.cpp:683) and the viscous stress
+// sigma_ab = -(tau - 1/2)/tau sum_l f_l (c_la - u_a)(c_lb - u_b)
+// (lbm.cpp:687-705) from the raw second moment,
+//     sum f (c - u)(c - u)^T = Pi - u j^T - j u^T + rho u u^T,
+// with rho and u of the moment export that precedes it (the shifted storage
+// adds c_s^2 to Pi_xx and Pi_yy only: the D2Q9 links have c_z = 0, and u_z
+// is zero); with a sample to fold in, Sup_MacroProp's running statistics
+// (lbm.cpp:865-939) in FP64, as the D3Q19 pass keeps them.  Layouts
+// [component][cell]: details p, sigma xx, xy, xz, yy, yz, zz; statistics
+// avg u (3), avg p, avg Reynolds stress (6), rms u (3), rms p, rms Reynolds
+// stress (6).
+template <class T, bool SOLID>
+__global__ void __launch_bounds__(256) k_details2d(const T *__restrict__ A, const __grid_constant__ Params2 P,
+                                                   const float *__restrict__ mom, float *__restrict__ det,
+                                                   double *__restrict__ st, float sfac, int gather, int drift,
+                                                   int fold, double told, double dt) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (x >= P.nx || y >= P.ny) return;
+    const long long cell = x + (long long)P.nx * y;
+    float f[Q9];
+    const uint32_t lk = SOLID ? (uint32_t)P.links[cell] : 0u;
+    int raw = (x == 0 ? 1 : 0) | (x == P.nx - 1 ? 2 : 0) | (y == 0 ? 4 : 0) | (y == P.ny - 1 ? 8 : 0);
+    raw &= ~(((P.periodic & 1) ? 3 : 0) | ((P.periodic & 2) ? 12 : 0));
+    const Class2 &ce = drift ? P.cls_w[raw] : P.cls[raw];
+    if (SOLID && (lk & kSolidCell)) {
+        // a solid cell keeps its populations (they are its own moments)
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(A + l * P.S + cell);
+    } else if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(A + l * P.S + cell);
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q9; l++)
+            f[l] = (SOLID && ((lk >> l) & 1u)) ? St<T>::ld(A + opp9(l) * P.S + cell)
+                                              : pull_link2<T>(A, l, x, y, cell, ce, P);
+    }
+    float jx = 0.0f, jy = 0.0f, pxx = 0.0f, pxy = 0.0f, pyy = 0.0f;
+#pragma unroll
+    for (int l = 1; l < Q9; l++) {
+        const float v = f[l], ex = (float)cx9(l), ey = (float)cy9(l);
+        jx += ex * v;
+        jy += ey * v;
+        pxx += ex * ex * v;
+        pxy += ex * ey * v;
+        pyy += ey * ey * v;
+    }
+    const long long N = P.N;
+    const float rho = mom[cell], ux = mom[N + cell], uy = mom[2 * N + cell];
+    const float cs2 = 1.0f / 3.0f;
+    const float sxx = (pxx + cs2) - 2.0f * ux * jx + rho * ux * ux;
+    const float syy = (pyy + cs2) - 2.0f * uy * jy + rho * uy * uy;
+    const float sxy = pxy - ux * jy - jx * uy + rho * ux * uy;
+    det[cell] = rho / 3.0f;
+    det[N + cell] = sfac * sxx;
+    det[2 * N + cell] = sfac * sxy;
+    det[3 * N + cell] = 0.0f;
+    det[4 * N + cell] = sfac * syy;
+    det[5 * N + cell] = 0.0f;
+    det[6 * N + cell] = 0.0f;
+    if (!fold) return;
+    // Sup_MacroProp, in the reference's order and with its weights
+    const double w1 = told + 1.0;
+    const double u[3] = {ux, uy, 0.0};
+    const double p = (double)rho / 3.0;
+    double au[3], d[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        au[a] = (st[a * N + cell] * told + u[a] * dt) / (told + dt);
+        st[a * N + cell] = au[a];
+        d[a] = u[a] - au[a];
+    }
+    const double ap = (st[3 * N + cell] * told + p) / w1;
+    st[3 * N + cell] = ap;
+    const int ia[6] = {0, 0, 0, 1, 1, 2}, ib[6] = {0, 1, 2, 1, 2, 2};
+    double ars[6];
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        ars[s] = (st[(4 + s) * N + cell] * told + d[ia[s]] * d[ib[s]]) / w1;
+        st[(4 + s) * N + cell] = ars[s];
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+        const double r = st[(10 + a) * N + cell];
+        st[(10 + a) * N + cell] = sqrt((r * r * told + d[a] * d[a]) / w1);
+    }
+    // the pressure rms squares the current pressure (lbm.cpp:913)
+    const double dp = p - ap;
+    st[13 * N + cell] = sqrt((p * p * told + dp * dp) / w1);
+#pragma unroll
+    for (int s = 0; s < 6; s++) {
+        const double r = st[(14 + s) * N + cell];
+        const double e = u[ia[s]] * u[ib[s]] - ars[s];
+        st[(14 + s) * N + cell] = sqrt((r * r * told + e * e) / w1);
+    }
+}
+
 // Momentum exchange over a box of the current state (MEA_CL / MEA_CD,
 // lbm.cpp:3085-3163): over the fluid cells of the box, every link l whose
 // source x - c_l is a solid adds (f*_l + f_opp(l)) c_l, with f* the cell's
@@ -1576,6 +1675,9 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
 lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double *xyz, const double *dsw) {
     lbm2d *d = h->d2;
     if (d->ibm) return f2(LBM_ERR_STATE, "set_markers: markers already set");
+    if (h->details)
+        return f2(LBM_ERR_UNSUPPORTED, "set_markers: not on a D2Q9 handle in MORE_DETAILS mode (the reference's IBM "
+                                       "loop never calls MacroProp, which forms the details)");
     if (d->energy) return f2(LBM_ERR_UNSUPPORTED, "set_markers: no immersed body on ENERGY handles");
     if (d->links) return f2(LBM_ERR_UNSUPPORTED, "set_markers: a D2Q9 handle takes solid cells or markers, not both");
     if (h->steps > 0) return f2(LBM_ERR_STATE, "set_markers: call before the first step");
@@ -1874,6 +1976,41 @@ lbm_status l2d_checkpoint_restored(lbm_handle *h, long long steps) {
     CK2(cudaStreamSynchronize(h->s));
     return LBM_OK;
 }
+
+long long l2d_cells(lbm_handle *h) { return h->d2->P.N; }
+float *l2d_moments(lbm_handle *h) { return h->d2->mom; }
+
+// MORE_DETAILS of the current state (k_details2d) behind a moment export, on
+// the handle's stream; fold != 0 folds a Sup_MacroProp sample.
+cudaError_t l2d_details_async(lbm_handle *h, int fold, double told, double dt) {
+    lbm2d *d = h->d2;
+    if (!h->inited) return cudaErrorNotReady;
+    const int gather = h->steps == 0 ? 0 : 1;
+    cudaError_t e = launch_step2d(h, gather, d->mom, 1);
+    if (e != cudaSuccess) return e;
+    const float sfac = (float)(-(h->cfg.tau - 0.5) / h->cfg.tau);
+    const int drift = wall_drift(h, gather);
+    const dim3 block(d->tx, d->ty);
+    const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
+    const void *A = d->f[d->cur];
+    const bool solid = d->P.links != nullptr;
+#define L2D_DET(T)                                                                                             \
+    if (solid)                                                                                               \
+        k_details2d<T, true><<<grid, block, 0, h->s>>>((const T *)A, d->P, d->mom, h->det, h->stats, sfac,     \
+                                                       gather, drift, fold, told, dt);                        \
+    else                                                                                                     \
+        k_details2d<T, false><<<grid, block, 0, h->s>>>((const T *)A, d->P, d->mom, h->det, h->stats, sfac,    \
+                                                        gather, drift, fold, told, dt);
+    switch (h->cfg.storage) {
+    case LBM_STORE_F16: L2D_DET(__half) break;
+    case LBM_STORE_BF16: L2D_DET(__nv_bfloat16) break;
+    default: L2D_DET(float) break;
+    }
+#undef L2D_DET
+    return cudaGetLastError();
+}
+
+bool l2d_has_markers(lbm_handle *h) { return h->d2->ibm; }
 
 int l2d_marker_count(lbm_handle *h) { return h->d2->ibm ? h->d2->ib.n : 0; }
 

@@ -159,11 +159,15 @@ lbm_status det_fail(lbm_status s, const std::string &m) {
     return s;
 }
 
+// cells of the handle's lattice (D3Q19 interior or D2Q9 device grid)
+long long det_cells(lbm_handle *h) { return h->d2 ? l2d_cells(h) : h->P.N; }
+
 }  // namespace
 
 // Export the moments, then the details (and fold a statistics sample when
 // smp_fold) of the current state on h->s.
 cudaError_t lbm_details_async(lbm_handle *h, int smp_fold, double told, double dt) {
+    if (h->d2) return l2d_details_async(h, smp_fold, told, dt);
     cudaError_t e = lbm_export_moments_async(h);
     if (e != cudaSuccess) return e;
     StepParams P = h->P;
@@ -184,20 +188,22 @@ cudaError_t lbm_details_async(lbm_handle *h, int smp_fold, double told, double d
 
 extern "C" lbm_status lbmgpu_set_more_details(lbm_handle *h, int on) {
     if (!h) return det_fail(LBM_ERR_INVALID, "set_more_details: null handle");
-    if (h->d2) return det_fail(LBM_ERR_UNSUPPORTED, "set_more_details: not for D2Q9 handles");
+    if (h->d2 && l2d_has_markers(h))
+        return det_fail(LBM_ERR_UNSUPPORTED, "set_more_details: not for D2Q9 IBM handles (the reference's IBM loop "
+                                             "never calls MacroProp, which forms the details)");
     if (lbmgpu_sync(h) != LBM_OK) return LBM_ERR_CUDA;
     if (!on) {
         if (h->det) cudaFree(h->det);
         if (h->stats) cudaFree(h->stats);
-        if (h->det) h->dev_bytes -= (size_t)kDetailFields * h->P.N * sizeof(float);
-        if (h->stats) h->dev_bytes -= (size_t)kStatFields * h->P.N * sizeof(double);
+        if (h->det) h->dev_bytes -= (size_t)kDetailFields * det_cells(h) * sizeof(float);
+        if (h->stats) h->dev_bytes -= (size_t)kStatFields * det_cells(h) * sizeof(double);
         h->det = nullptr;
         h->stats = nullptr;
         h->details = false;
         return LBM_OK;
     }
     if (h->details) return LBM_OK;
-    const size_t N = (size_t)h->P.N;
+    const size_t N = (size_t)det_cells(h);
     if (cudaMalloc((void **)&h->det, kDetailFields * N * sizeof(float)) != cudaSuccess) {
         h->det = nullptr;
         return det_fail(LBM_ERR_NOMEM, "set_more_details: device allocation failed");
@@ -240,8 +246,8 @@ extern "C" lbm_status lbmgpu_download_details(lbm_handle *h, float *host) {
     if (!h->inited) return det_fail(LBM_ERR_STATE, "download_details: call lbmgpu_init first");
     cudaError_t e = lbm_details_async(h, 0, 0.0, 1.0);
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(host, h->det, (size_t)kDetailFields * h->P.N * sizeof(float), cudaMemcpyDeviceToHost,
-                            h->s);
+        e = cudaMemcpyAsync(host, h->det, (size_t)kDetailFields * det_cells(h) * sizeof(float),
+                            cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return det_fail(LBM_ERR_CUDA, std::string("download_details: ") + cudaGetErrorString(e));
     return LBM_OK;
@@ -250,7 +256,7 @@ extern "C" lbm_status lbmgpu_download_details(lbm_handle *h, float *host) {
 extern "C" lbm_status lbmgpu_download_stats(lbm_handle *h, double *host, int *samples, double *told) {
     if (!h || !host) return det_fail(LBM_ERR_INVALID, "download_stats: null argument");
     if (!h->details) return det_fail(LBM_ERR_STATE, "download_stats: call lbmgpu_set_more_details first");
-    cudaError_t e = cudaMemcpyAsync(host, h->stats, (size_t)kStatFields * h->P.N * sizeof(double),
+    cudaError_t e = cudaMemcpyAsync(host, h->stats, (size_t)kStatFields * det_cells(h) * sizeof(double),
                                     cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return det_fail(LBM_ERR_CUDA, std::string("download_stats: ") + cudaGetErrorString(e));

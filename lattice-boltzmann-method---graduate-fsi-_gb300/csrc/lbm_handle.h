@@ -111,6 +111,11 @@ struct l2d_region {
     int both;  // 1: the populations, written into both buffers on restore
 };
 std::vector<l2d_region> l2d_checkpoint_regions(lbm_handle *h, int src);
+// MORE_DETAILS of a D2Q9 handle into h->det / h->stats (cells: l2d_cells).
+long long l2d_cells(lbm_handle *h);
+float *l2d_moments(lbm_handle *h);  // the export's rows rho, ux, uy [, T, qx, qy]
+cudaError_t l2d_details_async(lbm_handle *h, int fold, double told, double dt);
+bool l2d_has_markers(lbm_handle *h);
 void l2d_checkpoint_shape(lbm_handle *h, int shape[8]);
 lbm_status l2d_checkpoint_restored(lbm_handle *h, long long steps);
 int l2d_marker_count(lbm_handle *h);

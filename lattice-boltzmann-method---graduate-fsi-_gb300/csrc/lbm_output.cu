@@ -352,10 +352,13 @@ void write_vtk(VtkJob j, lbm_output *o) {
         arrays.push_back({"Pressure", 1, [&](long long c, const lbm_face *gf, float *v) {
                               v[0] = c >= 0 ? j.det[c] : ghost_pressure(gf);
                           }});
+        // a ghost cell's stress is that of its face equilibrium: rho c_s^2 on
+        // the diagonal, on xx and yy only for D2Q9 (c_z = 0)
         arrays.push_back({"Viscous Stress", 9, [&](long long c, const lbm_face *gf, float *v) {
                               for (int q = 0; q < 9; q++)
                                   v[q] = c >= 0 ? j.det[(1 + kSym9[q]) * N + c]
-                                                : ((q % 4 == 0) ? ghost_stress_diag(gf, j.tau) : 0.0f);
+                                                : ((q % 4 == 0 && !(j.d2 && q == 8)) ? ghost_stress_diag(gf, j.tau)
+                                                                                     : 0.0f);
                           }});
         arrays.push_back({"Vorticity", 3, [&](long long, const lbm_face *, float *) {}});
     }
@@ -398,8 +401,9 @@ void lbm_output_free(lbm_handle *h) {
     h->out = nullptr;
 }
 
-// D2Q9 handles: the moments (and an IBM body's box force) are copied out
-// synchronously, then the file is written by the same host thread writer.
+// D2Q9 handles: the moments (and an IBM body's box force, or in MORE_DETAILS
+// mode the pressure and viscous stress) are copied out synchronously, then
+// the file is written by the same host thread writer.
 static lbm_status output_vtk_2d(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
     if (!h->out) h->out = new lbm_output();
     lbm_output *o = h->out;
@@ -408,7 +412,7 @@ static lbm_status output_vtk_2d(lbm_handle *h, const char *path, double u_ref, c
     VtkJob j;
     j.grid = grid_of_2d(h);
     const long long N = j.grid.N;
-    const size_t need = (size_t)8 * N;
+    const size_t need = (size_t)(h->details ? 8 + LBM_DETAIL_COUNT : 8) * N;
     if (o->host_floats < need) {
         if (o->host) cudaFreeHost(o->host);
         o->host = nullptr;
@@ -416,6 +420,14 @@ static lbm_status output_vtk_2d(lbm_handle *h, const char *path, double u_ref, c
         if (cudaMallocHost((void **)&o->host, need * sizeof(float)) != cudaSuccess)
             return out_fail(LBM_ERR_NOMEM, "output_vtk: pinned staging allocation failed");
         o->host_floats = need;
+    }
+    if (h->details) {
+        cudaError_t e = l2d_details_async(h, 0, 0.0, 1.0);
+        if (e == cudaSuccess)
+            e = cudaMemcpyAsync(o->host + 8 * N, h->det, (size_t)LBM_DETAIL_COUNT * N * sizeof(float),
+                                cudaMemcpyDeviceToHost, h->s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
+        if (e != cudaSuccess) return out_fail(LBM_ERR_CUDA, std::string("output_vtk: ") + cudaGetErrorString(e));
     }
     lbm_status st = l2d_vtk_snapshot(h, o->host, j.boxF, j.fbox);
     if (st != LBM_OK) return st;
@@ -425,10 +437,10 @@ static lbm_status output_vtk_2d(lbm_handle *h, const char *path, double u_ref, c
     j.tau = h->cfg.tau;
     j.thermal = h->cfg.thermal;
     j.force = l2d_marker_count(h) > 0;
-    j.details = 0;
+    j.details = h->details ? 1 : 0;
     j.mom = o->host;
     j.band = nullptr;
-    j.det = nullptr;
+    j.det = h->details ? o->host + 8 * N : nullptr;
     j.fsign = 1.0f;
     j.d2 = 1;
     j.fcap = (long long)j.boxF.size() / 4;
@@ -516,28 +528,32 @@ extern "C" lbm_status lbmgpu_output_vtk_async(lbm_handle *h, const char *path, d
     return LBM_OK;
 }
 
+// the moment export's buffer of the handle
+static const float *lbm_moment_buffer(lbm_handle *h) { return h->d2 ? l2d_moments(h) : h->mom; }
+
 extern "C" lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, double u_ref, const uint8_t *types) {
     if (!h || !path || !(u_ref > 0.0)) return out_fail(LBM_ERR_INVALID, "output_avg_vtk: bad argument");
-    if (h->d2) return out_fail(LBM_ERR_UNSUPPORTED, "output_avg_vtk: not for D2Q9 handles");
     if (!h->details) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_set_more_details first");
     if (!h->inited) return out_fail(LBM_ERR_STATE, "output_avg_vtk: call lbmgpu_init first");
     if (h->out) {
         lbm_status prev = join_writer(h->out);
         if (prev != LBM_OK) return prev;
     }
-    const long long N = h->P.N;
+    const long long N = h->d2 ? l2d_cells(h) : h->P.N;
     std::vector<float> mom((size_t)4 * N), det((size_t)LBM_DETAIL_COUNT * N);
     std::vector<double> st((size_t)LBM_STAT_COUNT * N);
     cudaError_t e = lbm_details_async(h, 0, 0.0, 1.0);
+    // the moments as rho, u (3): a D2Q9 export holds rho, ux, uy (uz = 0)
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(mom.data(), h->mom, mom.size() * sizeof(float), cudaMemcpyDeviceToHost, h->s);
+        e = cudaMemcpyAsync(mom.data(), lbm_moment_buffer(h), (size_t)(h->d2 ? 3 : 4) * N * sizeof(float),
+                            cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(det.data(), h->det, det.size() * sizeof(float), cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(st.data(), h->stats, st.size() * sizeof(double), cudaMemcpyDeviceToHost, h->s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(h->s);
     if (e != cudaSuccess) return out_fail(LBM_ERR_CUDA, std::string("output_avg_vtk: ") + cudaGetErrorString(e));
-    VtkGrid g = grid_of(h);
+    VtkGrid g = h->d2 ? grid_of_2d(h) : grid_of(h);
     if (!grid_types(h, g, types)) return out_fail(LBM_ERR_CUDA, "output_avg_vtk: solid mask read failed");
     const double tau = h->cfg.tau, u2 = u_ref * u_ref;
     const bool sampled = h->stat_samples > 0;
@@ -576,10 +592,11 @@ extern "C" lbm_status lbmgpu_output_avg_vtk(lbm_handle *h, const char *path, dou
                               v[0] = (float)sqrt(p * p * told / (told + 1.0));
                           }
                       }});
+    const bool d2 = h->d2 != nullptr;
     arrays.push_back({"Viscous Stress", 9, [&](long long c, const lbm_face *gf, float *v) {
                           for (int q = 0; q < 9; q++)
                               v[q] = c >= 0 ? det[(1 + kSym9[q]) * N + c]
-                                            : ((q % 4 == 0) ? ghost_stress_diag(gf, tau) : 0.0f);
+                                            : ((q % 4 == 0 && !(d2 && q == 8)) ? ghost_stress_diag(gf, tau) : 0.0f);
                       }});
     for (const char *name : {"Vorticity", "Avg vorticity", "Rms vorticity"})
         arrays.push_back({name, 3, [&](long long, const lbm_face *, float *) {}});

@@ -185,3 +185,83 @@ def test_more_details_calls_need_the_mode(pkg):
     s.set_more_details(False)
     with pytest.raises(pkg.LbmError):
         s.details()
+
+
+def _triangle(pkg, orc):
+    """The reference's Cylinder_Tandem_Triangle in MORE_DETAILS mode (D2Q9,
+    60 x 40, two triangles), 200 steps with Sup_MacroProp every 10."""
+    from test_gpu_d2q9 import _staircase_gpu
+
+    g = np.load(os.path.join(GOLDEN, "triangle60x40_details_200.npz"))
+    case = ("triangle", int(g["nx"]), int(g["ny"]), int(g["D"]), float(g["Re"]), float(g["u_in"]), int(g["nb"]))
+    s = _staircase_gpu(pkg, orc, case)[0]
+    s.set_more_details(True)
+    nt = int(g["nt"])
+    for step in range(1, int(g["steps"]) + 1):
+        s.step(1)
+        if step % nt == 0:
+            s.sup_macroprop(step, nt, 1.0)
+    assert s.status() == 0
+    return s, g
+
+
+def test_d2q9_details_vs_reference(pkg, orc):
+    """D2Q9 handles: the pressure, the viscous stress and the Sup_MacroProp
+    statistics of every interior cell against the reference's own
+    MORE_DETAILS run of its tandem-triangle case (staircase solids, inlet and
+    outlet faces, tau = 0.515).  The Reynolds-stress statistics are products
+    of velocities: their FP32 error is about 2 U times that of u, so they are
+    held to 2 U TOL_U U [measured 2.5e-6 U^2]."""
+    s, g = _triangle(pkg, orc)
+    u = float(g["u_in"])
+
+    def inner(a):
+        return a[..., 1:-1, 1:-1]
+
+    d = s.details()
+    ep = np.abs(d["p"][0] - inner(g["p"])).max()
+    es = np.abs(d["sigma"][:, 0] - inner(g["sigma"])).max()
+    st = s.stats()
+    assert st["samples"] == 20 and st["told"] == 190.0
+    err = {k: np.abs((st[k][:, 0] if st[k].ndim == 4 else st[k][0]) - inner(g[k])).max()
+           for k in ("avg_u", "rms_u", "avg_p", "rms_p", "avg_rs", "rms_rs")}
+    print("D2Q9 details errors: p %.3g sigma %.3g" % (ep, es), {k: "%.3g" % v for k, v in err.items()})
+    assert ep < TOL_P and es < TOL_P, (ep, es)
+    assert err["avg_u"] < TOL_U * u and err["rms_u"] < TOL_U * u
+    assert err["avg_p"] < TOL_P and err["rms_p"] < TOL_P
+    assert err["avg_rs"] < 2 * TOL_U * u * u and err["rms_rs"] < 2 * TOL_U * u * u
+
+
+def test_d2q9_details_vtk_files_match_reference(pkg, orc, tmp_path):
+    """OutputVTK and OutputAVGVTK of the D2Q9 MORE_DETAILS run against the
+    reference's own files of the same run: the same headers, CellType and
+    coordinates exactly, every other array within FP32 tolerance (ghost cells
+    included): the velocities within 1e-5 U as the D2Q9 staircase fields
+    [5.6e-6 U], the rest as test_d2q9_details_vs_reference."""
+    s, g = _triangle(pkg, orc)
+    u = float(g["u_in"])
+    types = g["types"]
+    path = str(tmp_path / "field000000.vtr")
+    s.output_vtk_async(path, u_ref=u, types=types)
+    s.output_wait()
+    v = pkg.read_vtr(path)
+    assert v["header"] == str(g["vtk_header"])
+    for k in ("CellType", "CoordinateX", "CoordinateY", "CoordinateZ", "Vorticity"):
+        assert np.array_equal(v[k], g["vtk_" + k]), k
+    assert np.abs(v["Density"] - g["vtk_Density"]).max() < 1e-6
+    assert np.abs(v["Velocity"] - g["vtk_Velocity"]).max() < 1e-5  # u / u_in
+    assert np.abs(v["Pressure"] - g["vtk_Pressure"]).max() < TOL_P
+    assert np.abs(v["Viscous Stress"] - g["vtk_Viscous Stress"]).max() < TOL_P
+    apath = str(tmp_path / "avgfield.vtr")
+    s.output_avg_vtk(apath, u_ref=u, types=types)
+    w = pkg.read_vtr(apath)
+    assert w["header"] == str(g["avgvtk_header"])
+    for k in ("CellType", "CoordinateX", "CoordinateY", "CoordinateZ", "Vorticity", "Avg vorticity", "Rms vorticity"):
+        assert np.array_equal(w[k], g["avgvtk_" + k]), k
+    # velocities in the file are u / u_in, Reynolds stresses u u / u_in^2
+    tol = {"Density": 1e-6, "Pressure": TOL_P, "Avg pressure": TOL_P, "Rms pressure": TOL_P,
+           "Viscous Stress": TOL_P, "Velocity": 1e-5, "Avg velocity": 1e-5, "Rms velocity": 1e-5,
+           "Avg reynolds Stress": 2e-5, "Rms reynolds Stress": 2e-5}
+    for k, t in tol.items():
+        e = np.abs(w[k] - g["avgvtk_" + k]).max()
+        assert e < t, (k, e)
