@@ -29,7 +29,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liblbm_oracle.so")
 
-TYPE_F, TYPE_S, TYPE_OUT, TYPE_IN, TYPE_P, TYPE_L, TYPE_T, TYPE_OUTZG = 0, 1, 2, 3, 4, 5, 6, 8
+TYPE_F, TYPE_S, TYPE_OUT, TYPE_IN, TYPE_P, TYPE_L, TYPE_T, TYPE_Q, TYPE_OUTZG = 0, 1, 2, 3, 4, 5, 6, 7, 8
 
 # D3Q19 in the reference order (LBM.h:542-552)
 CX19 = np.array([0, 1, -1, 0, 0, 0, 0, 1, -1, 1, -1, 0, 0, 1, -1, 1, -1, 0, 0])
@@ -513,14 +513,15 @@ def cylinder_markers_literal(nodes: int, D: float, cx: float, cy: float) -> Mark
 
 
 def couette_energy(ny: int, Re: float, tau: float = 0.9, nx: int = 2, nz: int = 2, Pr: float = 0.7,
-                   Br: float = 10.0, Tb: float = 0.5):
+                   Br: float = 10.0, Tb: float = 0.5, top: int = 6):
     """main_setup_Couette (lbm.cpp:1537-1580) with ENERGY and D2Q9: walls
     (TYPE_S, Dirichlet TYPE_T) on rows j = 0 and Ny + 1, the top one moving
     at u_wall = Re nu / (Ny + 1), periodic in x and z; T = Tb on the fluid
     and the bottom wall, Tt = Tb + u_wall^2 / (cp Ec) on the top wall.  The
     thermal constants follow LBM.h:206-219: alpha = nu / Pr, tau_g = 0.5 +
-    alpha / cs2, k = cs2 tau_g, cp = k / alpha, Ec = Br / Pr.  Returns the
-    initialised lattice and the constants."""
+    alpha / cs2, k = cs2 tau_g, cp = k / alpha, Ec = Br / Pr.  top: the top
+    wall's type_Energy (TYPE_T, or TYPE_Q for a Neumann wall with j.n = 0).
+    Returns the initialised lattice and the constants."""
     cs2 = 1.0 / 3.0
     nu = cs2 * (tau - 0.5)
     uw = Re * nu / (ny + 1)
@@ -536,7 +537,7 @@ def couette_energy(ny: int, Re: float, tau: float = 0.9, nx: int = 2, nz: int = 
     lat.enable_energy(tau_g, cp, nu)
     te = lat.types_energy
     te[:, 0, :] = TYPE_T
-    te[:, -1, :] = TYPE_T
+    te[:, -1, :] = top
     lat.ux[:, -1, :] = uw
     lat.T[:] = Tb
     lat.T[:, -1, :] = Tt

@@ -15,7 +15,8 @@
 #   sphere:NX:NY:NZ:D:RE:U    D3Q19 staircase sphere, momentum-exchange Cl/Cd
 #   inline:NX:NY:D:NODES:M:PERIOD  D2Q9 cylinder oscillating along the stream (KC = 5)
 #   arbie:NX:NY:D:NODES:M:CX  D2Q9 cylinder towed through fluid at rest
-#   couette:NY:RE             D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls)
+#   couette:NY:RE[:neumann]   D2Q9 thermal Couette flow (ENERGY: viscous heating, Dirichlet walls; the
+#                             top wall a Neumann wall with j.n = 0)
 #   poiseuille:NY:RE[:energy] D2Q9 body-forced channel (Poiseuille_Flow), optionally with ENERGY
 #   cylbasic:NX:NY:D:RE:U     D2Q9 staircase cylinder, momentum-exchange Cl/Cd (Cylinder_Basic)
 #   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
@@ -88,9 +89,10 @@ for v in "$@"; do
             "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     couette)
-        ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3)
-        exe="$OUT/ref_couette_${ny}_${re}"
-        $CXX $FLAGS -DREF_COUETTE -DREF_NY=$ny -DREF_RE=$re -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        ny=$(echo "$v" | cut -d: -f2); re=$(echo "$v" | cut -d: -f3); top=$(echo "$v" | cut -d: -f4)
+        exe="$OUT/ref_couette_${ny}_${re}"; extra=""
+        if [ "$top" = neumann ]; then exe="${exe}_neumann"; extra="-DREF_NEUMANN"; fi
+        $CXX $FLAGS -DREF_COUETTE $extra -DREF_NY=$ny -DREF_RE=$re -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     cylbasic)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); d=$(echo "$v" | cut -d: -f4)

@@ -52,7 +52,7 @@
 /* Cell types: LBM.h:505-515 (TYPE_F .. TYPE_Q).  ORC_OUTZG is new: a ghost
  * cell that repeats the post-collision populations of the interior cell next
  * to it (zero-gradient outlet). */
-enum { ORC_F = 0, ORC_S = 1, ORC_OUT = 2, ORC_IN = 3, ORC_P = 4, ORC_L = 5, ORC_T = 6, ORC_OUTZG = 8 };
+enum { ORC_F = 0, ORC_S = 1, ORC_OUT = 2, ORC_IN = 3, ORC_P = 4, ORC_L = 5, ORC_T = 6, ORC_Q = 7, ORC_OUTZG = 8 };
 
 /* D2Q9 and D3Q19 tables in the reference order: LBM.h:528-555. */
 static const int CX9[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
@@ -107,7 +107,8 @@ typedef struct orc {
     double eg_beta, eT_star;   /* Rayleigh_Benard buoyancy F_y = g beta (T - T*) */
     double *eg, *egs, *fvis;   /* [q][ncell] */
     double *hq;                /* [3][ncell] heat flux sum g c */
-    uint8_t *type_e;           /* type_Energy: ORC_T (Dirichlet) on walls */
+    uint8_t *type_e;           /* type_Energy: ORC_T (Dirichlet) or ORC_Q (Neumann) on walls */
+    double ejdn;               /* the Neumann walls' j . n (LBM.h's j_dot_n) */
 } orc;
 
 static inline long IDX(const orc *o, int i, int j, int k) {
@@ -421,69 +422,151 @@ static long zg_source(const orc *o, int i, int j, int k) {
  * of lbm.cpp:299-624 only touch ghost cells that no fluid cell reads, so they
  * are not restated.  Extension: populations arriving from a ORC_OUTZG ghost
  * take the post-collision value of the clamped interior cell. */
-void orc_stream(orc *o) {
+/* LBM::Determine_Twall_Neumann, lbm.cpp:983-1028, for cell (i, j, k) in
+ * the middle of the push: the normal is the mean of the directions of the
+ * links that face a wall (cdotn_pos, the opposites of the solid links, not
+ * normalised); the links not facing a wall contribute the cell's current g
+ * -- this sweep's value where the source was visited earlier, the previous
+ * sweep's otherwise --, the facing ones the wall equilibrium at T = 1 (cubic
+ * shape, the cell's rho and the wall velocity); T_w = (j.n - sum_notpos) /
+ * sum_pos, also written into the wall cell opposite the normal. */
+static double twall_neumann(orc *o, int i, int j, int k, long c, const double uw[3]) {
+    long n = o->ncell;
+    int pos[27], npos = 0, is_pos[27] = {0};
+    for (int l = 0; l < o->q; l++) {
+        int in = (i + o->cx[l] + o->NX) % o->NX;
+        int jn = (j + o->cy[l] + o->NY) % o->NY;
+        int kn = (k + o->cz[l] + o->NZ) % o->NZ;
+        if (o->type[IDX(o, in, jn, kn)] == ORC_S) {
+            pos[npos++] = o->opp[l];
+            is_pos[o->opp[l]] = 1;
+        }
+    }
+    double nrm[3] = {0, 0, 0};
+    for (int p = 0; p < npos; p++) {
+        nrm[0] += o->cx[pos[p]];
+        nrm[1] += o->cy[pos[p]];
+        nrm[2] += o->cz[pos[p]];
+    }
+    nrm[0] /= npos; nrm[1] /= npos; nrm[2] /= npos;
+    double sum_notpos = 0;
+    for (int l = 0; l < o->q; l++) {
+        if (is_pos[l]) continue;
+        sum_notpos += o->eg[l * n + c] * (o->cx[l] * nrm[0] + o->cy[l] * nrm[1] + o->cz[l] * nrm[2]);
+    }
+    double cs2 = o->cs2, uu = uw[0] * uw[0] + uw[1] * uw[1] + uw[2] * uw[2];
+    double sum_pos = 0;
+    for (int p = 0; p < npos; p++) {
+        int l = pos[p];
+        double uc = uw[0] * o->cx[l] + uw[1] * o->cy[l] + uw[2] * o->cz[l];
+        double eq = o->w[l] * o->rho[c] *
+                    (1 + uc / cs2 + pow(uc, 2) / (2 * cs2 * cs2) - uu / (2 * cs2) + pow(uc, 3) / (6 * pow(cs2, 3)) -
+                     uc * uu / (2 * cs2 * cs2));
+        sum_pos += eq * (o->cx[l] * nrm[0] + o->cy[l] * nrm[1] + o->cz[l] * nrm[2]);
+    }
+    double Tw = (o->ejdn - sum_notpos) / sum_pos;
+    for (int l = 0; l < o->q; l++) {
+        int m = o->opp[l];
+        if (o->cx[m] == nrm[0] && o->cy[m] == nrm[1] && o->cz[m] == nrm[2]) {
+            int in = (i + o->cx[l] + o->NX) % o->NX;
+            int jn = (j + o->cy[l] + o->NY) % o->NY;
+            int kn = (k + o->cz[l] + o->NZ) % o->NZ;
+            o->T[IDX(o, in, jn, kn)] = Tw;
+            break;
+        }
+    }
+    return Tw;
+}
+
+/* Streaming of one fluid cell (the body of orc_stream's loops). */
+static void stream_cell(orc *o, int i, int j, int k) {
     long n = o->ncell;
     double cs2 = o->cs2;
-#pragma omp parallel for collapse(2)
-    for (int k = 0; k < o->NZ; k++) {
-        for (int j = 0; j < o->NY; j++) {
-            for (int i = 0; i < o->NX; i++) {
-                long c = IDX(o, i, j, k);
-                if (o->type[c] != ORC_F) continue;
-                int have_uw = 0;
-                double uw[3] = {0, 0, 0};
-                for (int l = 0; l < o->q; l++) {
-                    int in = (i + o->cx[l] + o->NX) % o->NX;
-                    int jn = (j + o->cy[l] + o->NY) % o->NY;
-                    int kn = (k + o->cz[l] + o->NZ) % o->NZ;
-                    long nb = IDX(o, in, jn, kn);
-                    uint8_t t = o->type[nb];
-                    if (t == ORC_F) {
-                        o->f[l * n + nb] = o->fs[l * n + c];
-                        if (o->energy) o->eg[l * n + nb] = o->egs[l * n + c];
-                    } else if (t == ORC_S) {
-                        if (!have_uw) { wall_velocity(o, i, j, k, uw); have_uw = 1; }
-                        double uwall_dot_c = uw[0] * o->cx[l] + uw[1] * o->cy[l] + uw[2] * o->cz[l];
-                        o->f[o->opp[l] * n + c] = o->fs[l * n + c] - 2 * o->w[l] * uwall_dot_c / cs2;
-                        /* Dirichlet wall (type_Energy TYPE_T): anti-bounce-back
-                         * against the wall equilibrium (lbm.cpp:277-280) */
-                        if (o->energy && o->type_e[nb] == ORC_T) {
-                            double g_eq = energy_geq(o, i, j, k, l, 1, uw);
-                            o->eg[o->opp[l] * n + c] = -o->egs[l * n + c] + 2 * g_eq;
-                        }
-                    }
-                    /* Pull-side view of the zero-gradient ghost: the
-                     * population of this cell arriving from direction l's
-                     * opposite neighbour. */
-                    int m = o->opp[l];
-                    if (t == ORC_OUTZG) {
-                        /* neighbour nb = x + c_l = x - c_m is the source of population m */
-                        long src = zg_source(o, in, jn, kn);
-                        if (o->type[src] == ORC_F) o->f[m * n + c] = o->fs[m * n + src];
-                    }
-                }
-                if (o->thermal) {
-                    for (int l = 0; l < 7; l++) {
-                        int in = (i + CX7[l] + o->NX) % o->NX;
-                        int jn = (j + CY7[l] + o->NY) % o->NY;
-                        int kn = (k + CZ7[l] + o->NZ) % o->NZ;
-                        long nb = IDX(o, in, jn, kn);
-                        uint8_t t = o->type[nb];
-                        if (t == ORC_F) {
-                            o->g[l * n + nb] = o->gs[l * n + c];
-                        } else if (t == ORC_S) {
-                            /* adiabatic wall: plain bounce-back of g */
-                            o->g[OPP7[l] * n + c] = o->gs[l * n + c];
-                        } else if (t == ORC_OUTZG) {
-                            int m = OPP7[l];
-                            long src = zg_source(o, in, jn, kn);
-                            if (o->type[src] == ORC_F) o->g[m * n + c] = o->gs[m * n + src];
-                        }
-                    }
-                }
+    long c = IDX(o, i, j, k);
+    if (o->type[c] != ORC_F) return;
+    int have_uw = 0;
+    double uw[3] = {0, 0, 0};
+    for (int l = 0; l < o->q; l++) {
+        int in = (i + o->cx[l] + o->NX) % o->NX;
+        int jn = (j + o->cy[l] + o->NY) % o->NY;
+        int kn = (k + o->cz[l] + o->NZ) % o->NZ;
+        long nb = IDX(o, in, jn, kn);
+        uint8_t t = o->type[nb];
+        if (t == ORC_F) {
+            o->f[l * n + nb] = o->fs[l * n + c];
+            if (o->energy) o->eg[l * n + nb] = o->egs[l * n + c];
+        } else if (t == ORC_S) {
+            if (!have_uw) { wall_velocity(o, i, j, k, uw); have_uw = 1; }
+            double uwall_dot_c = uw[0] * o->cx[l] + uw[1] * o->cy[l] + uw[2] * o->cz[l];
+            o->f[o->opp[l] * n + c] = o->fs[l * n + c] - 2 * o->w[l] * uwall_dot_c / cs2;
+            /* Dirichlet wall (type_Energy TYPE_T): anti-bounce-back
+             * against the wall equilibrium (lbm.cpp:277-280) */
+            if (o->energy && o->type_e[nb] == ORC_T) {
+                double g_eq = energy_geq(o, i, j, k, l, 1, uw);
+                o->eg[o->opp[l] * n + c] = -o->egs[l * n + c] + 2 * g_eq;
+            } else if (o->energy && o->type_e[nb] == ORC_Q) {
+                /* Neumann wall (lbm.cpp:281-288): the wall's T from
+                 * the heat flux, and the unknown g as the
+                 * second-order equilibrium of T_w; a wall of any
+                 * other type_Energy (adiabatic) writes nothing */
+                double Tw = twall_neumann(o, i, j, k, c, uw);
+                o->T[nb] = Tw;
+                double uu = uw[0] * uw[0] + uw[1] * uw[1] + uw[2] * uw[2];
+                o->eg[o->opp[l] * n + c] =
+                    o->w[l] * o->rho[c] * Tw *
+                    (1 + uwall_dot_c / cs2 + pow(uwall_dot_c, 2) / (2 * cs2 * cs2) - uu / (2 * cs2));
+            }
+        }
+        /* Pull-side view of the zero-gradient ghost: the
+         * population of this cell arriving from direction l's
+         * opposite neighbour. */
+        int m = o->opp[l];
+        if (t == ORC_OUTZG) {
+            /* neighbour nb = x + c_l = x - c_m is the source of population m */
+            long src = zg_source(o, in, jn, kn);
+            if (o->type[src] == ORC_F) o->f[m * n + c] = o->fs[m * n + src];
+        }
+    }
+    if (o->thermal) {
+        for (int l = 0; l < 7; l++) {
+            int in = (i + CX7[l] + o->NX) % o->NX;
+            int jn = (j + CY7[l] + o->NY) % o->NY;
+            int kn = (k + CZ7[l] + o->NZ) % o->NZ;
+            long nb = IDX(o, in, jn, kn);
+            uint8_t t = o->type[nb];
+            if (t == ORC_F) {
+                o->g[l * n + nb] = o->gs[l * n + c];
+            } else if (t == ORC_S) {
+                /* adiabatic wall: plain bounce-back of g */
+                o->g[OPP7[l] * n + c] = o->gs[l * n + c];
+            } else if (t == ORC_OUTZG) {
+                int m = OPP7[l];
+                long src = zg_source(o, in, jn, kn);
+                if (o->type[src] == ORC_F) o->g[m * n + c] = o->gs[m * n + src];
             }
         }
     }
+}
+
+/* LBM::Streaming, fluid part.  With a Neumann wall the result depends on the
+ * order the cells are visited in (twall_neumann reads this sweep's pushes),
+ * so the loop runs in the reference's order, i outer, k inner, on one
+ * thread; otherwise every write has one source and the loop runs in
+ * parallel. */
+void orc_stream(orc *o) {
+    int neumann = 0;
+    if (o->energy)
+        for (long c = 0; c < o->ncell && !neumann; c++) neumann = o->type_e[c] == ORC_Q;
+    if (neumann) {
+        for (int i = 0; i < o->NX; i++)
+            for (int j = 0; j < o->NY; j++)
+                for (int k = 0; k < o->NZ; k++) stream_cell(o, i, j, k);
+        return;
+    }
+#pragma omp parallel for collapse(2)
+    for (int k = 0; k < o->NZ; k++)
+        for (int j = 0; j < o->NY; j++)
+            for (int i = 0; i < o->NX; i++) stream_cell(o, i, j, k);
 }
 
 /* LBM::MacroProp, lbm.cpp:657-679: rho = sum f, u = (sum f c + F/2) / rho on

@@ -182,6 +182,12 @@ int main(int argc, char **argv) {
     printf("{\"case\": \"poiseuille\", \"ny\": %d, \"steps\": %d, \"seconds\": %.6f}\n", Ny, steps, t1 - t0);
 #elif defined REF_COUETTE
     LBM lb = main_setup_Couette();
+#if defined REF_NEUMANN
+    // the top wall as a Neumann wall: type_Energy TYPE_Q with LBM.h's
+    // j_dot_n (Determine_Twall_Neumann, lbm.cpp:983-1028)
+    for (int i = 0; i <= Nx + 1; i++)
+        for (int k = 0; k <= Nz + 1; k++) lb.fluid[i][Ny + 1][k].type_Energy = TYPE_Q;
+#endif
     lb.Init();
     double t0 = omp_get_wtime();
     for (int s = 1; s <= steps; s++) {

@@ -167,6 +167,21 @@ def triangle_details(tmp: str) -> None:
                         **{"vtk_" + k: x for k, x in v.items()}, **{"avgvtk_" + k: x for k, x in w.items()})
 
 
+def couette_neumann(tmp: str) -> None:
+    """The ENERGY Couette flow with its top wall a Neumann wall (j.n = 0),
+    1000 steps.  The reference evaluates Neumann walls inside its push, so
+    its result depends on the order its OpenMP threads visit the cells; one
+    thread gives the serial order the oracle and the device restate."""
+    p = os.path.join(tmp, "couette_neumann.bin")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.check_call([os.path.join(REF, "ref_couette_30_20_neumann"), "1000", p], env=env)
+    f = oracle.read_ref_dump(p, 4, 32, 4, 8)["fields"]
+    for k in range(4):
+        assert np.array_equal(f[:, k], f[:, 1])
+    np.savez_compressed(os.path.join(OUT, "couette_neumann_ny30_re20_1000.npz"), rho=f[0, 1], u=f[1:4, 1],
+                        T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=1000)
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -177,9 +192,15 @@ def main() -> None:
     ap.add_argument("--skip-cav64", action="store_true")
     ap.add_argument("--only-cylinder-vtk", action="store_true",
                     help="write only cylinder80x40_vtk_100.npz (the D2Q9 OutputVTK / OutputVTK_Marker files)")
+    ap.add_argument("--only-couette-neumann", action="store_true",
+                    help="write only couette_neumann_ny30_re20_1000.npz (the ENERGY Couette, Neumann top wall)")
     ap.add_argument("--only-triangle-details", action="store_true",
                     help="write only triangle60x40_details_200.npz (D2Q9 MORE_DETAILS, both VTK files)")
     a = ap.parse_args()
+    if a.only_couette_neumann:
+        oracle.build_ref("couette:30:20:neumann")
+        couette_neumann(tempfile.mkdtemp())
+        return
     if a.only_triangle_details:
         oracle.build_ref("triangled:60:40:10:100.0:0.05:1.5:2")
         triangle_details(tempfile.mkdtemp())
@@ -190,7 +211,7 @@ def main() -> None:
         return
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
-                     "couette:30:20", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",
+                     "couette:30:20", "couette:30:20:neumann", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",
                      "poiseuille:30:20:energy", "triangled:60:40:10:100.0:0.05:1.5:2", *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
@@ -283,6 +304,7 @@ def main() -> None:
         assert np.array_equal(f[:, k], f[:, 1])
     np.savez_compressed(os.path.join(OUT, "couette_energy_ny30_re20_2000.npz"), rho=f[0, 1], u=f[1:4, 1],
                         T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=2000)
+    couette_neumann(tmp)
     # Poiseuille channel, 1500 steps, with and without ENERGY
     for exe, name, nf in (("ref_poiseuille_30_20", "poiseuille_ny30_re20_1500.npz", 4),
                           ("ref_poiseuille_30_20_energy", "poiseuille_ny30_re20_energy_1500.npz", 8)):

@@ -202,6 +202,28 @@ def test_cylinder2d_variants_match_reference(orc, case):
     assert np.allclose(f.reshape(5, -1).sum(axis=1), g["sums"], rtol=1e-12, atol=1e-12)
 
 
+def test_energy_neumann_wall_matches_reference(orc):
+    """The ENERGY Couette with its top wall a Neumann wall (type_Energy
+    TYPE_Q, j.n = 0; Determine_Twall_Neumann, lbm.cpp:983-1028): the wall
+    temperature from the cell's g in the middle of the push -- this sweep's
+    values for the links whose source comes earlier in the (i, j, k) loop,
+    last sweep's for the others --, the unknown g as the second-order
+    equilibrium of T_w (lbm.cpp:281-288), T_w written into the wall cell.
+    Against the reference run on one thread (its OpenMP split over i changes
+    the result), bit for bit after 1000 steps, ghosts included."""
+    g = np.load(os.path.join(GOLDEN, "couette_neumann_ny30_re20_1000.npz"))
+    lat, c = orc.couette_energy(int(g["ny"]), float(g["Re"]), top=orc.TYPE_Q)
+    assert lat.step_plain(int(g["steps"])) == 0
+    assert np.array_equal(lat.rho[1], g["rho"])
+    assert np.array_equal(np.stack([lat.ux[1], lat.uy[1], lat.uz[1]]), g["u"])
+    assert np.array_equal(lat.T[1], g["T"])
+    assert np.array_equal(lat.hq[:, 1], g["q"])
+    # no heat crosses the top wall: the profile flattens towards it (about a
+    # twentieth of the gradient at the Dirichlet bottom wall)
+    T = g["T"][:, 1]
+    assert abs(T[-2] - T[-3]) < 0.1 * abs(T[2] - T[1])
+
+
 def test_energy_couette_matches_reference(orc):
     """The reference's ENERGY model (LBM.h:58) on its Couette case, D2Q9:
     temperature populations on the flow lattice with the cubic equilibrium
