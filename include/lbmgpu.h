@@ -57,7 +57,15 @@ enum { LBM_STORE_F32 = 0, LBM_STORE_F16 = 1, LBM_STORE_BF16 = 2 };
 enum { LBM_FACE_WALL = 0, LBM_FACE_INLET = 1, LBM_FACE_OUTLET_EQ = 2, LBM_FACE_OUTLET_ZG = 3, LBM_FACE_PERIODIC = 4 };
 
 /* Thermal condition on a WALL face. */
-enum { LBM_TWALL_ADIABATIC = 0, LBM_TWALL_DIRICHLET = 1 };
+/* Thermal wall kinds.  NEUMANN (D2Q9 ENERGY handles only): the wall's T is
+ * set every streaming so that no heat crosses it, j . n = 0 (the reference's
+ * j_dot_n; Determine_Twall_Neumann, lbm.cpp:983-1028).  ADIABATIC on ENERGY
+ * handles: the wall's links are never streamed and keep their initial
+ * values, as a wall of any other type_Energy in the reference
+ * (lbm.cpp:276-288).  On ENERGY handles every wall face's T is its set-up
+ * temperature: the Dirichlet walls' temperature is the mean of their solid
+ * neighbours' (lbm.cpp:965-981), which wraps onto the opposite wall row. */
+enum { LBM_TWALL_ADIABATIC = 0, LBM_TWALL_DIRICHLET = 1, LBM_TWALL_NEUMANN = 2 };
 
 /* Fields for lbmgpu_download*. */
 enum { LBM_FIELD_RHO = 0, LBM_FIELD_UX = 1, LBM_FIELD_UY = 2, LBM_FIELD_UZ = 3, LBM_FIELD_T = 4,
@@ -78,7 +86,7 @@ typedef struct lbm_face {
     int thermal_kind;  /* LBM_TWALL_* for walls */
     double rho;        /* inlet/outlet-equilibrium density */
     double u[3];       /* wall velocity, or inlet/outlet-equilibrium velocity */
-    double T;          /* inlet temperature or Dirichlet wall temperature */
+    double T;          /* inlet temperature or (set-up) wall temperature */
 } lbm_face;
 
 typedef struct lbm_config {

@@ -27,7 +27,7 @@ FACE_WALL, FACE_INLET, FACE_OUTLET_EQ, FACE_OUTLET_ZG, FACE_PERIODIC = 0, 1, 2, 
 LATTICE_D3Q19, LATTICE_D2Q9 = 19, 9
 # prescribed motion of a D2Q9 IBM body (IBLBM, lbm.cpp:1140-1151)
 MOTION_FIXED, MOTION_CONSTANT, MOTION_INLINE_OSC, MOTION_TRANSVERSE_OSC = 0, 1, 2, 3
-TWALL_ADIABATIC, TWALL_DIRICHLET = 0, 1
+TWALL_ADIABATIC, TWALL_DIRICHLET, TWALL_NEUMANN = 0, 1, 2
 FIELD_RHO, FIELD_UX, FIELD_UY, FIELD_UZ, FIELD_T = 0, 1, 2, 3, 4
 FIELD_QX, FIELD_QY, FIELD_QZ = 5, 6, 7
 # lbm_config.thermal: none, D3Q7 (D3Q19 handles), the reference's ENERGY model (D2Q9 handles)

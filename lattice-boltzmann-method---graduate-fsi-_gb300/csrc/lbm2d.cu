@@ -405,6 +405,11 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
             f[l] = St<T>::ld(A + l * P.S + cell);
             g[l] = GA[l * P.S + cell];
         }
+        // Neumann and adiabatic walls: the initial values are the first kept ones
+        if (E.gold != nullptr && face && !export_only) {
+#pragma unroll
+            for (int l = 0; l < Q9; l++) E.gold[l * P.S + cell] = g[l];
+        }
     } else if (!face) {
 #pragma unroll
         for (int l = 0; l < Q9; l++) {
@@ -418,6 +423,8 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
         const float *pm1 = drift ? E.pm1_w[raw] : E.pm1[raw];
         const int k = first ? 0 : 1;
         const float tw = E.tw[raw][k], dtw = E.dtw[raw][k];
+        const uint32_t neu = E.neu[raw], adi = E.adi[raw];
+        float sn = 0.0f;  // Neumann: sum over the other links of (g - w T_ref) c.n
 #pragma unroll
         for (int l = 0; l < Q9; l++) {
             f[l] = pull_link2<T>(A, l, x, y, cell, ce, P);
@@ -425,11 +432,40 @@ __global__ void __launch_bounds__(256) k_energy2d(const T *__restrict__ A, T *__
                 // 2 geq - 2 w T_ref = 2 w (rho T_w (1 + pm1) - T_ref)
                 const float wall = 2.0f * w9f(l) * (dtw + drho_p * tw + (1.0f + drho_p) * tw * pm1[l]);
                 g[l] = wall - GA[opp9(l) * P.S + cell];
+            } else if ((adi >> l) & 1u) {
+                g[l] = E.gold[l * P.S + cell];  // never streamed: the initial value
+            } else if ((neu >> l) & 1u) {
+                g[l] = 0.0f;  // set from T_w below
             } else {
                 // a periodic or interior source (the only other links of an
                 // ENERGY handle)
                 g[l] = pull_link2<float>(GA, l, x, y, cell, ce, P);
+                if (neu) {
+                    // The reference pushes cell by cell, i outer and j inner,
+                    // and forms T_w in the middle of this cell's push: a link
+                    // whose source it visited earlier (periodic wrap included;
+                    // the rest link in this cell's own push) holds this
+                    // sweep's value, the others the previous sweep's.
+                    int sx = x - cx9(l), sy = y - cy9(l);
+                    sx += sx < 0 ? P.nx : (sx >= P.nx ? -P.nx : 0);
+                    sy += sy < 0 ? P.ny : (sy >= P.ny ? -P.ny : 0);
+                    const bool fresh = l == 0 || sx < x || (sx == x && sy < y);
+                    float *kept = E.gold + l * P.S + cell;
+                    sn += (fresh ? g[l] : *kept) * E.cn[raw][l];
+                    if (!export_only) *kept = g[l];
+                }
             }
+        }
+        if (neu) {
+            // T_w = (j.n - sum_other g c.n) / sum_wall geq(rho, T = 1, u_w) c.n
+            // with j.n = 0 (LBM.h's j_dot_n), rho of the previous MacroProp;
+            // the wall links take the second-order equilibrium of T_w
+            // (lbm.cpp:281-288)
+            const float rho_p = 1.0f + drho_p;
+            const float Tw = -(sn + E.T_ref * E.nk[raw]) / (rho_p * E.nd[raw]);
+#pragma unroll
+            for (int l = 0; l < Q9; l++)
+                if ((neu >> l) & 1u) g[l] = w9f(l) * (rho_p * Tw * E.nq[raw][l] - E.T_ref);
         }
     }
     float drho = 0.0f, jx = 0.0f, jy = 0.0f, dT = 0.0f, qx = 0.0f, qy = 0.0f;
@@ -1249,7 +1285,10 @@ int face_priority2(int kind) {
 // ghost faces takes the highest-priority kind; a cell's wall velocity is the
 // mean over its moving wall neighbours, Determine_Wall_Velocity,
 // lbm.cpp:941-962).
-void build_classes2(const lbm_config &c, const Params2 &P, Class2 out[16], double uwall_out[16][2]) {
+// lface (optional): for every class and link whose source is a wall, the
+// face that wall belongs to; -1 for the other links.
+void build_classes2(const lbm_config &c, const Params2 &P, Class2 out[16], double uwall_out[16][2],
+                    int (*lface)[Q9] = nullptr) {
     for (int cls = 0; cls < 16; cls++) {
         Class2 e;
         memset(&e, 0, sizeof(e));
@@ -1314,6 +1353,7 @@ void build_classes2(const lbm_config &c, const Params2 &P, Class2 out[16], doubl
             double uw[2];
             const int fi = resolve(fs, k, uw);
             const lbm_face &F = c.faces[fi];
+            if (lface) lface[cls][l] = F.kind == LBM_FACE_WALL ? fi : -1;
             if (F.kind == LBM_FACE_WALL) {
                 e.bb |= 1u << l;
                 // f_l = f*_opp(l) - 2 w (u_w . c_opp) / cs^2 (lbm.cpp:274)
@@ -1337,8 +1377,10 @@ void build_classes2(const lbm_config &c, const Params2 &P, Class2 out[16], doubl
 // streamed): the mean set-up T of their own solid neighbours, which for a
 // wall row wraps onto the opposite wall row.  Corner ghost cells take the T
 // of their y face.
-void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16][2], const double uwall_w[16][2],
-                   Energy2 &E) {
+// Neumann and adiabatic walls: the kind of each wall link's face; a class
+// with wall links of two kinds is refused (returns false).
+bool build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16][2], const double uwall_w[16][2],
+                   const int lface[16][Q9], Energy2 &E) {
     const double cs2 = 1.0 / 3.0, tg = c.tau_g;
     memset(&E, 0, sizeof(E));
     E.inv_tau_g = (float)(1.0 / tg);
@@ -1387,7 +1429,54 @@ void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16]
         E.tw[cls][1] = (float)t1;
         E.dtw[cls][0] = (float)(t0 - c.T_init);
         E.dtw[cls][1] = (float)(t1 - c.T_init);
-        E.dir[cls] = P.cls[cls].bb;
+        uint32_t dir = 0, neu = 0, adi = 0;
+        for (int l = 0; l < Q9; l++) {
+            if (!((P.cls[cls].bb >> l) & 1u)) continue;
+            const int kind = c.faces[lface[cls][l]].thermal_kind;
+            if (kind == LBM_TWALL_DIRICHLET) dir |= 1u << l;
+            else if (kind == LBM_TWALL_NEUMANN) neu |= 1u << l;
+            else adi |= 1u << l;
+        }
+        // classes no cell has: a periodic axis's face bits, or both faces of
+        // an axis more than one cell long
+        const bool occurs = !(((P.periodic & 1) && (cls & 3)) || ((P.periodic & 2) && (cls & 12)) ||
+                              ((cls & 3) == 3 && P.nx > 1) || ((cls & 12) == 12 && P.ny > 1));
+        if (occurs && (dir != 0) + (neu != 0) + (adi != 0) > 1) return false;
+        E.dir[cls] = dir;
+        E.neu[cls] = neu;
+        E.adi[cls] = adi;
+        if (neu) {
+            // the normal: the mean direction of the wall links (the reference's
+            // cdotn_pos, not normalised)
+            double n0 = 0.0, n1 = 0.0;
+            int np = 0;
+            for (int l = 0; l < Q9; l++)
+                if ((neu >> l) & 1u) {
+                    n0 += cx9(l);
+                    n1 += cy9(l);
+                    np++;
+                }
+            n0 /= np;
+            n1 /= np;
+            const double u0 = uwall[cls][0], u1 = uwall[cls][1], uu = u0 * u0 + u1 * u1;
+            double nk = 0.0, nd = 0.0;
+            for (int l = 0; l < Q9; l++) {
+                const double cn = cx9(l) * n0 + cy9(l) * n1;
+                E.cn[cls][l] = (float)cn;
+                const double uc = u0 * cx9(l) + u1 * cy9(l);
+                if ((neu >> l) & 1u) {
+                    nd += w9d(l) * (1 + uc / cs2 + pow(uc, 2) / (2 * cs2 * cs2) - uu / (2 * cs2) +
+                                    pow(uc, 3) / (6 * pow(cs2, 3)) - uc * uu / (2 * cs2 * cs2)) *
+                          cn;
+                    // the g of link l: w rho T_w P2 of the solid direction -c_l
+                    E.nq[cls][l] = (float)(1 - uc / cs2 + pow(uc, 2) / (2 * cs2 * cs2) - uu / (2 * cs2));
+                } else {
+                    nk += w9d(l) * cn;
+                }
+            }
+            E.nk[cls] = (float)nk;
+            E.nd[cls] = (float)nd;
+        }
         for (int w = 0; w < 2; w++) {
             const double uwx = w ? uwall_w[cls][0] : uwall[cls][0], uwy = w ? uwall_w[cls][1] : uwall[cls][1];
             const double usq = uwx * uwx + uwy * uwy;
@@ -1401,6 +1490,7 @@ void build_energy2(const lbm_config &c, const Params2 &P, const double uwall[16]
             }
         }
     }
+    return true;
 }
 
 // The two launches of a D2Q9 step (collide-stream, IBM pass) go out with
@@ -1552,8 +1642,9 @@ lbm_status l2d_create(lbm_handle *h) {
         for (int f = 0; f < 4; f++) {
             const lbm_face &F = c.faces[f];
             if (F.kind == LBM_FACE_PERIODIC) continue;
-            if (F.kind != LBM_FACE_WALL || F.thermal_kind != LBM_TWALL_DIRICHLET)
-                return f2(LBM_ERR_UNSUPPORTED, "create: ENERGY faces are periodic or Dirichlet walls (face " +
+            if (F.kind != LBM_FACE_WALL || F.thermal_kind < LBM_TWALL_ADIABATIC ||
+                F.thermal_kind > LBM_TWALL_NEUMANN)
+                return f2(LBM_ERR_UNSUPPORTED, "create: ENERGY faces are periodic or walls (face " +
                                                    std::to_string(f) + ")");
         }
     }
@@ -1577,7 +1668,10 @@ lbm_status l2d_create(lbm_handle *h) {
         if (c.faces[2 * a].kind == LBM_FACE_PERIODIC) P.periodic |= 1 << a;
     for (int l = 0; l < Q9; l++) P.pofs[l] = -(cx9(l) + c.nx * cy9(l));
     double uwall[16][2], uwall_w[16][2];
-    build_classes2(c, P, P.cls, uwall);
+    int lface[16][Q9];
+    for (int cls = 0; cls < 16; cls++)
+        for (int l = 0; l < Q9; l++) lface[cls][l] = -1;
+    build_classes2(c, P, P.cls, uwall, lface);
     {
         // the walls as seen from the third streaming on under wall_force:
         // their MacroProp velocity u_w + F / (2 rho_w), rho_w = 1
@@ -1588,7 +1682,14 @@ lbm_status l2d_create(lbm_handle *h) {
         build_classes2(cw, P, P.cls_w, uwall_w);
     }
     d->energy = c.thermal == LBM_THERMAL_ENERGY;
-    if (d->energy) build_energy2(c, P, uwall, uwall_w, d->E);
+    bool walls_kept = false;  // Neumann or adiabatic walls: the kept values
+    if (d->energy) {
+        if (!build_energy2(c, P, uwall, uwall_w, lface, d->E))
+            return f2(LBM_ERR_UNSUPPORTED, "create: a cell next to walls of two thermal kinds (ENERGY)");
+        for (int cls = 0; cls < 16; cls++) walls_kept = walls_kept || d->E.neu[cls] || d->E.adi[cls];
+        if (walls_kept && c.wall_force)
+            return f2(LBM_ERR_UNSUPPORTED, "create: Neumann or adiabatic walls with wall_force (ENERGY)");
+    }
     h->esize = c.storage == LBM_STORE_F32 ? 4 : 2;
     if (c.graph_steps > 0) d->gsteps = c.graph_steps + (c.graph_steps & 1);
     if (c.graph_steps < 0) d->gsteps = 0;
@@ -1603,6 +1704,7 @@ lbm_status l2d_create(lbm_handle *h) {
     if (d->energy) {
         for (int i = 0; i < 2; i++) CK2(alloc2(h, &d->g[i], (size_t)Q9 * P.S * sizeof(float)));
         CK2(alloc2(h, &d->aux, (size_t)P.N * sizeof(float4)));
+        if (walls_kept) CK2(alloc2(h, &d->E.gold, (size_t)Q9 * P.S * sizeof(float)));
     }
     // moments: rho, ux, uy (ENERGY: and T, qx, qy)
     CK2(alloc2(h, &d->mom, (size_t)(d->energy ? 6 : 3) * P.N * sizeof(float)));
@@ -1932,6 +2034,7 @@ std::vector<l2d_region> l2d_checkpoint_regions(lbm_handle *h, int src) {
     if (d->energy) {
         r.push_back({d->g[src], (size_t)Q9 * d->P.S * sizeof(float), 1});
         r.push_back({d->aux, (size_t)d->P.N * sizeof(float4), 0});
+        if (d->E.gold) r.push_back({d->E.gold, (size_t)Q9 * d->P.S * sizeof(float), 0});
     }
     r.push_back({d->st, sizeof(State2), 0});
     r.push_back({d->hist, (size_t)d->hist_cap * 4 * sizeof(double), 0});
@@ -1948,7 +2051,7 @@ void l2d_checkpoint_shape(lbm_handle *h, int shape[8]) {
     shape[0] = d->P.nx;
     shape[1] = d->P.ny;
     shape[2] = h->cfg.storage;
-    shape[3] = d->energy ? 1 : 0;
+    shape[3] = d->energy ? (d->E.gold ? 2 : 1) : 0;
     shape[4] = d->ibm ? d->ib.n : 0;
     shape[5] = d->links ? 1 : 0;
     shape[6] = (int)(d->P.S & 0x7fffffff);
@@ -2235,19 +2338,22 @@ extern "C" lbm_status lbmgpu_config_energy_2d(lbm_config *cfg, int nx, int ny, c
             return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: inlet/outlet faces are not supported with ENERGY");
         const int a = f / 2, side = f % 2;
         const int lim = a == 0 ? ny : nx;
+        // type_Energy TYPE_T (6): Dirichlet; TYPE_Q (7): Neumann with the
+        // reference's j_dot_n = 0 (LBM.h); any other: adiabatic
+        int kind = LBM_TWALL_ADIABATIC;
         for (int p = 1; p <= lim; p++) {
             const size_t id = a == 0 ? at(side ? nx + 1 : 0, p) : at(p, side ? ny + 1 : 0);
             const int te = types_energy[id];
-            if (te == 7)
-                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: Neumann walls (TYPE_Q) are not supported: the "
-                                               "reference's update depends on its loop order");
-            if (te != 6)
-                return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: every wall cell needs type_Energy = TYPE_T (6)");
+            const int k = te == 6 ? LBM_TWALL_DIRICHLET : (te == 7 ? LBM_TWALL_NEUMANN : LBM_TWALL_ADIABATIC);
+            if (p == 1) kind = k;
+            else if (k != kind)
+                return f2(LBM_ERR_UNSUPPORTED,
+                          "config_energy_2d: face " + std::to_string(f) + " mixes thermal wall types");
             if (p == 1) F.T = T[id];
             else if (T[id] != F.T)
                 return f2(LBM_ERR_UNSUPPORTED, "config_energy_2d: face " + std::to_string(f) + " T is not uniform");
         }
-        F.thermal_kind = LBM_TWALL_DIRICHLET;
+        F.thermal_kind = kind;
     }
     cfg->thermal = LBM_THERMAL_ENERGY;
     cfg->tau_g = tau_g;

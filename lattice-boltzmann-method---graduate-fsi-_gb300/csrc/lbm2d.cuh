@@ -81,6 +81,16 @@ struct Energy2 {
     float pm1_w[16][Q9]; // the same with the walls moving at F/2 (cls_w)
     float tw[16][2];     // wall T (first streaming, later)
     float dtw[16][2];    // wall T - T_ref
+    // Neumann walls (type_Energy TYPE_Q, j.n = 0; Determine_Twall_Neumann,
+    // lbm.cpp:983-1028) and adiabatic walls (any other type_Energy: their
+    // links are never written and keep the Init value), per class
+    uint32_t neu[16];    // links whose source is a Neumann wall
+    uint32_t adi[16];    // links whose source is an adiabatic wall
+    float cn[16][Q9];    // c_l . n, n the mean direction of the class's wall links
+    float nk[16];        // sum over the other links of w_l c_l . n (the T_ref shift)
+    float nd[16];        // sum over the wall links of w_l P3(u_w . c_l) c_l . n
+    float nq[16][Q9];    // P2(-u_w . c_l) of a wall link l: its g over w_l rho T_w
+    float *gold;         // [Q9][S] of the wall cells: last sweep's values, the Init values
 };
 
 // Device state of a D2Q9 solve.  The body kinematics are those of IBLBM

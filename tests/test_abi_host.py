@@ -135,9 +135,17 @@ def test_config_energy_2d_maps_couette_and_refuses_the_rest(pkg):
     assert cfg.thermal == pkg.THERMAL_ENERGY and cfg.cp == 2.0 and cfg.tau_g == 0.8 and cfg.T_init == 0.5
     assert [cfg.faces[f].thermal_kind for f in (2, 3)] == [pkg.TWALL_DIRICHLET] * 2
     assert (cfg.faces[2].T, cfg.faces[3].T) == (0.5, 0.625)
-    for bad_te, bad_T, word in ((7, None, "Neumann"), (0, None, "TYPE_T"), (6, "fluid", "uniform")):
+    # TYPE_Q: a Neumann wall (j.n = 0); any other type_Energy: adiabatic;
+    # both keep their set-up T
+    for top, kind in ((7, pkg.TWALL_NEUMANN), (0, pkg.TWALL_ADIABATIC)):
         te2 = te.copy()
-        te2[0] = bad_te
+        te2[-1] = top
+        c2 = pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t), nx, ny, t, te2, T, 0.8, 2.0)
+        assert (c2.faces[2].thermal_kind, c2.faces[3].thermal_kind) == (pkg.TWALL_DIRICHLET, kind)
+        assert (c2.faces[2].T, c2.faces[3].T) == (0.5, 0.625)
+    for bad_te, bad_T, word in ((7, None, "mixes"), (0, None, "mixes"), (6, "fluid", "uniform")):
+        te2 = te.copy()
+        te2[0, 2] = bad_te
         T2 = T.copy()
         if bad_T:
             T2[3, 1] = 0.51
@@ -151,6 +159,12 @@ def test_config_energy_2d_maps_couette_and_refuses_the_rest(pkg):
     with pytest.raises(pkg.LbmError) as e:
         pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t3), nx, ny, t3, te, T, 0.8, 2.0)
     assert e.value.status == 7
+    # Neumann walls are a D2Q9 ENERGY option
+    c3 = pkg.channel_config(8, 8, 8, 0.8)
+    c3.faces[2].thermal_kind = pkg.TWALL_NEUMANN
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(c3)
+    assert e.value.status == 7 and "Neumann" in str(e.value)
     # create: the D3Q7 model is not a D2Q9 option; ENERGY needs cp > 0
     c2 = pkg.config_from_types_2d(nx, ny, 0.9, t)
     c2.thermal, c2.tau_g = pkg.THERMAL_D3Q7, 0.8

@@ -21,9 +21,10 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 
-def _couette_setup(orc, ny, Re, nx=2, tau=0.9, u_bottom=0.0, Tb=0.5):
+def _couette_setup(orc, ny, Re, nx=2, tau=0.9, u_bottom=0.0, Tb=0.5, top=None, bottom=None):
     """The arrays of main_setup_Couette's k = 1 layer (lbm.cpp:1537-1580)
-    and the LBM.h constants."""
+    and the LBM.h constants; top / bottom: the walls' type_Energy (TYPE_T
+    by default)."""
     cs2 = 1.0 / 3.0
     nu = cs2 * (tau - 0.5)
     uw = Re * nu / (ny + 1)
@@ -36,8 +37,8 @@ def _couette_setup(orc, ny, Re, nx=2, tau=0.9, u_bottom=0.0, Tb=0.5):
     t[0, :] = orc.TYPE_S
     t[-1, :] = orc.TYPE_S
     te = np.zeros_like(t)
-    te[0, :] = orc.TYPE_T
-    te[-1, :] = orc.TYPE_T
+    te[0, :] = orc.TYPE_T if bottom is None else bottom
+    te[-1, :] = orc.TYPE_T if top is None else top
     ux = np.zeros(t.shape)
     ux[-1, :] = uw
     ux[0, :] = u_bottom
@@ -105,10 +106,51 @@ def test_energy_forced_moving_walls_vs_oracle(pkg, orc):
     print("forced T / u / q errors: %.3g %.3g %.3g" % e)
 
 
-def test_energy_graph_replay_matches_eager(pkg, orc):
+def test_energy_couette_neumann_vs_reference(pkg, orc):
+    """The top wall a Neumann wall (type_Energy TYPE_Q, j.n = 0): its T from
+    the cell's g in the middle of the reference's push, whose result depends
+    on the visiting order (Determine_Twall_Neumann, lbm.cpp:983-1028).
+    Against the reference's own single-thread run, 1000 steps, every fluid
+    row."""
+    g = np.load(os.path.join(GOLDEN, "couette_neumann_ny30_re20_1000.npz"))
+    s, c = _solver(pkg, orc, int(g["ny"]), float(g["Re"]), top=orc.TYPE_Q)
+    s.step(int(g["steps"]))
+    assert s.status() == 0
+    e = _check(s, pkg, g["T"][1:-1], g["u"][:2, 1:-1], g["q"][:2, 1:-1], c["u_wall"])
+    print("couette Neumann T / u / q errors: %.3g %.3g %.3g" % e)
+    # no heat crosses the top wall: the profile flattens towards it
+    T = s.moments()["T"][0][:, 1]
+    assert abs(T[-1] - T[-2]) < 0.1 * abs(T[1] - T[0])
+
+
+@pytest.mark.parametrize("case", ["neumann_bottom", "adiabatic_top"])
+def test_energy_neumann_adiabatic_vs_oracle(pkg, orc, case):
+    """A Neumann bottom wall under a moving Dirichlet top (the links from
+    above come from cells the reference's push visits later: last sweep's
+    values), and an adiabatic top wall (type_Energy TYPE_F: its links keep
+    their initial values); a wider channel, a moving bottom wall, an odd
+    step count."""
+    ny, Re, steps, nx, tau = 24, 30.0, 555, 6, 0.8
+    kw = dict(bottom=orc.TYPE_Q) if case == "neumann_bottom" else dict(top=orc.TYPE_F)
+    s, c = _solver(pkg, orc, ny, Re, nx=nx, u_bottom=-0.01, tau=tau, **kw)
+    s.step(steps)
+    assert s.status() == 0
+    lat, _ = orc.couette_energy(ny, Re, tau=tau, nx=nx, top=kw.get("top", orc.TYPE_T))
+    lat.ux[:, 0, :] = -0.01
+    if "bottom" in kw:
+        lat.types_energy[:, 0, :] = kw["bottom"]
+    lat.init()
+    assert lat.step_plain(steps) == 0
+    L = slice(1, -1)
+    e = _check(s, pkg, lat.T[1, L], np.stack([lat.ux[1, L], lat.uy[1, L]]), lat.hq[:2, 1, L], c["u_wall"])
+    print("%s T / u / q errors: %.3g %.3g %.3g" % ((case,) + e))
+
+
+@pytest.mark.parametrize("top", ["dirichlet", "neumann"])
+def test_energy_graph_replay_matches_eager(pkg, orc, top):
     out = []
     for gs in (8, -1):
-        s, _ = _solver(pkg, orc, 30, 20.0, graph_steps=gs)
+        s, _ = _solver(pkg, orc, 30, 20.0, graph_steps=gs, top=orc.TYPE_Q if top == "neumann" else None)
         s.step(203)
         m = s.moments()
         out.append((m["T"], m["ux"], s.download_f32(pkg.FIELD_QY)))
