@@ -545,6 +545,52 @@ def couette_energy(ny: int, Re: float, tau: float = 0.9, nx: int = 2, nz: int = 
     return lat, dict(tau=tau, tau_g=tau_g, cp=cp, nu=nu, u_wall=uw, Tb=Tb, Tt=Tt)
 
 
+def rayleigh_benard(nx: int = 200, ny: int = 50, nz: int = 5):
+    """main_setup_RayleighBenard1 (lbm.cpp:1585-1643) with the constants of
+    LBM.h:222-242, D3Q19 with ENERGY: walls all round; the y walls Dirichlet
+    (TYPE_T) at Tt on row j = 0 and Tb on row Ny + 1 (edges included), the
+    x and z walls Neumann (TYPE_Q, j.n = 0) at Tt; the fluid at rest at Tt
+    with F_y = g beta (T - T*), T* = (Tb + Tt) / 2, the force MacroProp
+    refreshes on every cell (lbm.cpp:803-805).  Returns the initialised
+    lattice and the constants."""
+    cs2 = 1.0 / 3.0
+    Tb, dT = 2.0, 1.0
+    Tt = Tb - dT
+    Ra, g_beta, Pr = 1710.0, 1e-5, 0.71
+    nu = np.sqrt(g_beta * dT * float((nz + 1) ** 3) * Pr / Ra)
+    tau = 0.5 + nu / cs2
+    alpha = nu / Pr
+    tau_g = 0.5 + alpha / cs2
+    k = cs2 * tau_g
+    cp = k / alpha
+    T_star = (Tb + Tt) / 2
+    lat = Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = TYPE_F
+    lat.enable_energy(tau_g, cp, nu)
+    te = lat.types_energy
+    T = lat.T
+    # the set-up's three ifs in order (z faces, x faces, y faces: the last
+    # one wins on edges), then the y rows' temperatures
+    for sl in ((0, slice(None), slice(None)), (-1, slice(None), slice(None)),
+               (slice(None), slice(None), 0), (slice(None), slice(None), -1)):
+        t[sl] = TYPE_S
+        te[sl] = TYPE_Q
+        T[sl] = Tt
+    for sl in ((slice(None), 0, slice(None)), (slice(None), -1, slice(None))):
+        t[sl] = TYPE_S
+        te[sl] = TYPE_T
+        T[sl] = Tt
+    T[:, -1, :] = Tb
+    T[:, 0, :] = Tt
+    fl = t == TYPE_F
+    T[fl] = Tt
+    lat.Fy[fl] = g_beta * (Tt - T_star)
+    lat.energy_buoyancy(g_beta, T_star)
+    lat.init()
+    return lat, dict(tau=tau, tau_g=tau_g, cp=cp, nu=nu, alpha=alpha, g_beta=g_beta, T_star=T_star, Tb=Tb, Tt=Tt)
+
+
 def poiseuille(ny: int, Re: float, energy: bool = False, tau: float = 0.9, nx: int = 2, nz: int = 2):
     """main_setup_Poiseuille (lbm.cpp:1495-1535) with the constants of
     LBM.h:116-136: walls (TYPE_S; with ENERGY Dirichlet TYPE_T at Tb = Tt =

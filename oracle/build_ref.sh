@@ -22,6 +22,7 @@
 #   tandem:NX:NY:D:RE:U:LPD:NB    D2Q9 staircase circles in tandem (Cylinder_Tandem_Circle)
 #   triangle:NX:NY:D:RE:U:LPD:NB  D2Q9 staircase triangles in tandem (Cylinder_Tandem_Triangle)
 #   triangled:NX:NY:D:RE:U:LPD:NB the same in MORE_DETAILS mode
+#   rayleigh:NX:NY:NZ         D3Q19 Rayleigh-Benard box (ENERGY, Dirichlet y walls, Neumann x and z walls)
 set -e
 HERE=$(cd "$(dirname "$0")" && pwd)
 REF=${REF:-}
@@ -111,6 +112,12 @@ for v in "$@"; do
         exe="$OUT/ref_${kind}_${nx}_${ny}_${d}_${re}_${u}_${lpd}_${nb}"
         $CXX $FLAGS $flag -DREF_NX=$nx -DREF_NY=$ny -DREF_D=$d -DREF_RE=$re -DREF_U=$u -DREF_LPD=$lpd \
             -DREF_NB=$nb -o "$exe" "$REF/lbm.cpp" "$HERE/ref_harness.cpp" &
+        pids="$pids $!" ;;
+    rayleigh)
+        nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)
+        exe="$OUT/ref_rayleigh_${nx}_${ny}_${nz}"
+        $CXX $FLAGS -DREF_RAYLEIGH -DREF_NX=$nx -DREF_NY=$ny -DREF_NZ=$nz -o "$exe" "$REF/lbm.cpp" \
+            "$HERE/ref_harness.cpp" &
         pids="$pids $!" ;;
     sphere)
         nx=$(echo "$v" | cut -d: -f2); ny=$(echo "$v" | cut -d: -f3); nz=$(echo "$v" | cut -d: -f4)

@@ -202,6 +202,23 @@ int main(int argc, char **argv) {
     for (int w = 50; w <= 53; w++) dump_field(lb, fp, w);
     fclose(fp);
     printf("{\"case\": \"couette_energy\", \"ny\": %d, \"steps\": %d, \"seconds\": %.6f}\n", Ny, steps, t1 - t0);
+#elif defined REF_RAYLEIGH
+    LBM lb = main_setup_RayleighBenard1();
+    lb.Init();
+    double t0 = omp_get_wtime();
+    for (int s = 1; s <= steps; s++) {
+        lb.Collision();
+        lb.Streaming();
+        lb.MacroProp();
+    }
+    double t1 = omp_get_wtime();
+    FILE *fp = fopen(out, "wb");
+    if (!fp) return 3;
+    for (int w = 0; w < 7; w++) dump_field(lb, fp, w);
+    for (int w = 50; w <= 53; w++) dump_field(lb, fp, w);
+    fclose(fp);
+    printf("{\"case\": \"rayleigh_benard\", \"nx\": %d, \"ny\": %d, \"nz\": %d, \"steps\": %d, \"seconds\": %.6f}\n",
+           Nx, Ny, Nz, steps, t1 - t0);
 #elif defined REF_CYLBASIC || defined REF_TANDEM || defined REF_TRIANGLE
     // the staircase 2D bodies with the momentum exchange of main.cpp:242-356,
     // taken after every step (the reference takes it every Nt steps)

@@ -182,6 +182,19 @@ def couette_neumann(tmp: str) -> None:
                         T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=1000)
 
 
+def rayleigh(tmp: str) -> None:
+    """The reference's Rayleigh_Benard case (D3Q19 ENERGY: Dirichlet y
+    walls, Neumann x and z walls, buoyancy) on a 32 x 16 x 5 box, 400 steps,
+    on one thread (its Neumann walls make the result depend on the visiting
+    order).  Every cell, ghosts included: rho, u, F, T, q."""
+    p = os.path.join(tmp, "rayleigh.bin")
+    env = dict(os.environ, OMP_NUM_THREADS="1")
+    subprocess.check_call([os.path.join(REF, "ref_rayleigh_32_16_5"), "400", p], env=env)
+    f = oracle.read_ref_dump(p, 34, 18, 7, 11)["fields"]
+    np.savez_compressed(os.path.join(OUT, "rayleigh32x16x5_400.npz"), rho=f[0], u=f[1:4], F=f[4:7], T=f[7],
+                        q=f[8:11], nx=32, ny=16, nz=5, steps=400)
+
+
 def run(exe: str, args: list[str]) -> None:
     subprocess.check_call([os.path.join(REF, exe)] + args)
 
@@ -194,12 +207,18 @@ def main() -> None:
                     help="write only cylinder80x40_vtk_100.npz (the D2Q9 OutputVTK / OutputVTK_Marker files)")
     ap.add_argument("--only-couette-neumann", action="store_true",
                     help="write only couette_neumann_ny30_re20_1000.npz (the ENERGY Couette, Neumann top wall)")
+    ap.add_argument("--only-rayleigh", action="store_true",
+                    help="write only rayleigh32x16x5_400.npz (D3Q19 ENERGY, Rayleigh-Benard)")
     ap.add_argument("--only-triangle-details", action="store_true",
                     help="write only triangle60x40_details_200.npz (D2Q9 MORE_DETAILS, both VTK files)")
     a = ap.parse_args()
     if a.only_couette_neumann:
         oracle.build_ref("couette:30:20:neumann")
         couette_neumann(tempfile.mkdtemp())
+        return
+    if a.only_rayleigh:
+        oracle.build_ref("rayleigh:32:16:5")
+        rayleigh(tempfile.mkdtemp())
         return
     if a.only_triangle_details:
         oracle.build_ref("triangled:60:40:10:100.0:0.05:1.5:2")
@@ -212,7 +231,8 @@ def main() -> None:
     oracle.build_ref("cavity:12:0.8", "cavity:64:0.8", "cylinder:80:40:10:40:5", "sphere:48:24:24:8:20:0.05",
                      "details:8:0.8", "explicit:80:40:10:40", "transverse:80:40:10:40:5:2.0:0.005",
                      "couette:30:20", "couette:30:20:neumann", "inline:80:40:10:40:5:1000", "arbie:120:40:10:40:5:80", "poiseuille:30:20",
-                     "poiseuille:30:20:energy", "triangled:60:40:10:100.0:0.05:1.5:2", *STAIRCASE_VARIANTS)
+                     "poiseuille:30:20:energy", "triangled:60:40:10:100.0:0.05:1.5:2", "rayleigh:32:16:5",
+                     *STAIRCASE_VARIANTS)
     tmp = tempfile.mkdtemp()
 
     # 12^3 cavity, 200 steps (and the reference's own VTK file of it)
@@ -305,6 +325,7 @@ def main() -> None:
     np.savez_compressed(os.path.join(OUT, "couette_energy_ny30_re20_2000.npz"), rho=f[0, 1], u=f[1:4, 1],
                         T=f[4, 1], q=f[5:8, 1], ny=30, Re=20.0, steps=2000)
     couette_neumann(tmp)
+    rayleigh(tmp)
     # Poiseuille channel, 1500 steps, with and without ENERGY
     for exe, name, nf in (("ref_poiseuille_30_20", "poiseuille_ny30_re20_1500.npz", 4),
                           ("ref_poiseuille_30_20_energy", "poiseuille_ny30_re20_energy_1500.npz", 8)):

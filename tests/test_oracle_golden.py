@@ -224,6 +224,30 @@ def test_energy_neumann_wall_matches_reference(orc):
     assert abs(T[-2] - T[-3]) < 0.1 * abs(T[2] - T[1])
 
 
+def test_energy_rayleigh_benard_matches_reference(orc):
+    """The reference's Rayleigh_Benard case (main_setup_RayleighBenard1,
+    lbm.cpp:1585-1643; LBM.h:222-242), D3Q19 with ENERGY: Dirichlet y walls,
+    Neumann x and z walls whose T the push writes into the wall cells, read
+    by the Dirichlet walls' Determine_Wall_Temperature of cells visited later
+    (edges mix both kinds), and F_y = g beta (T - T*) refreshed by MacroProp
+    on every cell, so that the walls report u = F / 2 and bounce back as
+    moving walls from the third streaming on.  Against the reference run on
+    one thread: bit for bit after 400 steps on a 32 x 16 x 5 box, ghosts
+    included."""
+    g = np.load(os.path.join(GOLDEN, "rayleigh32x16x5_400.npz"))
+    lat, c = orc.rayleigh_benard(int(g["nx"]), int(g["ny"]), int(g["nz"]))
+    assert lat.step_plain(int(g["steps"])) == 0
+    assert np.array_equal(lat.rho, g["rho"])
+    assert np.array_equal(np.stack([lat.ux, lat.uy, lat.uz]), g["u"])
+    assert np.array_equal(np.stack([lat.Fx, lat.Fy, lat.Fz]), g["F"])
+    assert np.array_equal(lat.T, g["T"])
+    assert np.array_equal(lat.hq, g["q"])
+    # the walls move at F / (2 rho_w) = g beta (T_w - T*) / 2 along y
+    w = (slice(None), 0, slice(1, -1))
+    assert np.allclose(g["u"][1][w], 0.5 * g["F"][1][w] / g["rho"][w], rtol=1e-12, atol=0)
+    assert np.abs(g["u"][1][w]).min() > 1e-7
+
+
 def test_energy_couette_matches_reference(orc):
     """The reference's ENERGY model (LBM.h:58) on its Couette case, D2Q9:
     temperature populations on the flow lattice with the cubic equilibrium
