@@ -199,8 +199,9 @@ lbm_status lbmgpu_config_from_types_2d(int nx, int ny, double tau, const uint8_t
  * each wall face and over the fluid).  tau_g and cp are LBM.h's
  * tau_g = 0.5 + alpha / cs2 and cp = k / (rho0 alpha).  Replaces the
  * LATTICE::type_Energy / T set-up of main_setup_Couette (lbm.cpp:1552-1572).
- * Fails with LBM_ERR_UNSUPPORTED for Neumann (TYPE_Q) or adiabatic walls,
- * inlet/outlet faces, or a non-uniform set-up. */
+ * type_Energy TYPE_Q (7) makes a Neumann face, any other type an adiabatic
+ * one (LBM_TWALL_*).  Fails with LBM_ERR_UNSUPPORTED for inlet/outlet faces,
+ * a face mixing thermal wall types, or a non-uniform set-up. */
 lbm_status lbmgpu_config_energy_2d(lbm_config *cfg, int nx, int ny, const uint8_t *types, const uint8_t *types_energy,
                                    const double *T, double tau_g, double cp);
 
@@ -499,8 +500,48 @@ typedef struct lbm_serve_result {
 lbm_status lbmgpu_serve_run(const lbm_serve_request *reqs, int n, const lbm_serve_options *opt,
                             lbm_serve_result *out, double *lattice_updates);
 
+/* The reference's ENERGY model on D3Q19 (#define ENERGY without D2Q9; its
+ * Rayleigh_Benard case, LBM.h:222-242, lbm.cpp:1585-1643), a solver object
+ * of its own.  It is built from the reference's ghost-inclusive cell arrays,
+ * (nx+2)(ny+2)(nz+2) cells, x fastest, indexed like LBM::fluid[i][j][k], and
+ * keeps the reference's periodic modulo over that whole grid.  f and g are
+ * FP32.  Walls: a TYPE_S cell whose type_Energy is TYPE_T is a Dirichlet
+ * wall (lbm.cpp:277-280) at Determine_Wall_Temperature's T (lbm.cpp:965-981);
+ * TYPE_Q a Neumann wall with j.n = 0 (lbm.cpp:281-288, 983-1028), evaluated
+ * in the reference's serial push order; any other type an adiabatic wall
+ * (its links keep their initial values).  With g_beta != 0, MacroProp sets
+ * F_y = g_beta (T - T_star) on every cell, walls included (lbm.cpp:803-805),
+ * so walls report u = F / (2 rho) and bounce back as moving walls from the
+ * third streaming on. */
+typedef struct lbm_energy3d lbm_energy3d;
+typedef struct lbm_energy3d_setup {
+    int nx, ny, nz;             /* interior cells */
+    double tau, tau_g, cp;      /* tau; LBM.h's tau_g = 0.5 + alpha / cs2 and cp = k / (rho0 alpha) */
+    double g_beta, T_star;      /* MacroProp's buoyancy; g_beta = 0: the set-up force stays */
+    const uint8_t *type;        /* TYPE_F (0) or TYPE_S (1) */
+    const uint8_t *type_energy; /* of TYPE_S cells: TYPE_T (6), TYPE_Q (7), other */
+    const double *T;            /* set-up temperature, walls included */
+    const double *rho;          /* set-up density; NULL: 1 */
+    const double *u;            /* set-up velocity [3][cells]; NULL: 0 */
+    const double *F;            /* set-up force [3][cells]; NULL: 0 */
+} lbm_energy3d_setup;
+/* Creates the solver and runs LBM::Init on the set-up.  LBM_ERR_UNSUPPORTED
+ * for other cell types, or a wall cell next to fluid without a solid
+ * neighbour (its Determine_Wall_Temperature would divide by zero). */
+lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *setup, lbm_energy3d **out);
+lbm_status lbmgpu_energy3d_init(lbm_energy3d *e);
+/* nsteps of Collision, Streaming, MacroProp (main.cpp:213-220). */
+lbm_status lbmgpu_energy3d_step(lbm_energy3d *e, int nsteps);
+lbm_status lbmgpu_energy3d_step_timed(lbm_energy3d *e, int nsteps, double *ms);
+/* LBM_FIELD_RHO .. LBM_FIELD_QZ after the last streaming and MacroProp, on
+ * the whole ghost-inclusive grid; NaN on TYPE_S cells. */
+lbm_status lbmgpu_energy3d_download(lbm_energy3d *e, int field, double *host);
+lbm_status lbmgpu_energy3d_status(lbm_energy3d *e, uint32_t *flags);
+lbm_status lbmgpu_energy3d_destroy(lbm_energy3d *e);
+
 const char *lbmgpu_last_error(void);
-/* 2: lbm_config.cells_per_thread and lbm_ibm_config.virtual_mass appended */
+/* 2: lbm_config.cells_per_thread and lbm_ibm_config.virtual_mass appended
+ * 3: lbm_energy3d (the ENERGY model on D3Q19) added */
 int lbmgpu_abi_version(void);
 
 #ifdef __cplusplus

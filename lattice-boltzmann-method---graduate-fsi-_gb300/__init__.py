@@ -53,7 +53,17 @@ ABI_SYMBOLS = [
     "lbmgpu_output_avg_vtk", "lbmgpu_config_from_types_2d", "lbmgpu_set_marker_normals",
     "lbmgpu_config_energy_2d", "lbmgpu_mea_box", "lbmgpu_nusselt", "lbmgpu_download_all_f32_async",
     "lbmgpu_download_wait", "lbmgpu_update_markers", "lbmgpu_cells_per_thread",
+    "lbmgpu_energy3d_create", "lbmgpu_energy3d_init", "lbmgpu_energy3d_step", "lbmgpu_energy3d_step_timed",
+    "lbmgpu_energy3d_download", "lbmgpu_energy3d_status", "lbmgpu_energy3d_destroy",
 ]
+
+
+class Energy3DSetup(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("nz", C.c_int), ("tau", C.c_double), ("tau_g", C.c_double),
+                ("cp", C.c_double), ("g_beta", C.c_double), ("T_star", C.c_double),
+                ("type", C.POINTER(C.c_uint8)), ("type_energy", C.POINTER(C.c_uint8)),
+                ("T", C.POINTER(C.c_double)), ("rho", C.POINTER(C.c_double)), ("u", C.POINTER(C.c_double)),
+                ("F", C.POINTER(C.c_double))]
 
 
 class Face(C.Structure):
@@ -171,6 +181,13 @@ def load(path: str | None = None):
     L.lbmgpu_set_marker_normals.argtypes = [vp, dp]
     L.lbmgpu_mea_box.argtypes = [vp, C.POINTER(C.c_int), dp]
     L.lbmgpu_nusselt.argtypes = [vp, d, d, dp]
+    L.lbmgpu_energy3d_create.argtypes = [C.POINTER(Energy3DSetup), C.POINTER(vp)]
+    L.lbmgpu_energy3d_init.argtypes = [vp]
+    L.lbmgpu_energy3d_step.argtypes = [vp, i]
+    L.lbmgpu_energy3d_step_timed.argtypes = [vp, i, dp]
+    L.lbmgpu_energy3d_download.argtypes = [vp, i, dp]
+    L.lbmgpu_energy3d_status.argtypes = [vp, C.POINTER(C.c_uint32)]
+    L.lbmgpu_energy3d_destroy.argtypes = [vp]
     L.lbmgpu_download_all_f32_async.argtypes = [vp, vp]
     L.lbmgpu_download_wait.argtypes = [vp]
     L.lbmgpu_update_markers.argtypes = [vp, dp, dp]
@@ -652,3 +669,68 @@ def batch_step_noalloc(dims, taus, lid, storage, pop_a_ptr, pop_b_ptr, first_ste
                                       C.c_void_p(pop_a_ptr), C.c_void_p(pop_b_ptr), int(first_step), int(nsteps),
                                       st.ctypes.data_as(C.POINTER(C.c_uint32)), C.c_void_p(stream or None)))
     return st
+
+
+class Energy3D:
+    """The reference's ENERGY model on D3Q19 (its Rayleigh_Benard case), built
+    from the reference's ghost-inclusive arrays, shaped (nz+2, ny+2, nx+2)
+    like LBM::fluid read k, j, i: type (TYPE_F / TYPE_S), type_Energy (TYPE_T
+    Dirichlet, TYPE_Q Neumann, other adiabatic), the set-up T and optionally
+    rho, u = (ux, uy, uz) and F = (Fx, Fy, Fz).  g_beta != 0 turns on
+    MacroProp's buoyancy F_y = g_beta (T - T_star) on every cell."""
+
+    FIELDS = {"rho": FIELD_RHO, "ux": FIELD_UX, "uy": FIELD_UY, "uz": FIELD_UZ, "T": FIELD_T, "qx": FIELD_QX,
+              "qy": FIELD_QY, "qz": FIELD_QZ}
+
+    def __init__(self, types, types_energy, T, tau, tau_g, cp, g_beta=0.0, T_star=0.0, rho=None, u=None, F=None):
+        self.L = load()
+        t = np.ascontiguousarray(types, dtype=np.uint8)
+        nz, ny, nx = (d - 2 for d in t.shape)
+        self.shape = t.shape
+        keep = [t, np.ascontiguousarray(types_energy, dtype=np.uint8), np.ascontiguousarray(T, dtype=np.float64)]
+        su = Energy3DSetup(nx=nx, ny=ny, nz=nz, tau=tau, tau_g=tau_g, cp=cp, g_beta=g_beta, T_star=T_star)
+        su.type = keep[0].ctypes.data_as(C.POINTER(C.c_uint8))
+        su.type_energy = keep[1].ctypes.data_as(C.POINTER(C.c_uint8))
+        su.T = _dp(keep[2])
+        for name, arr in (("rho", rho), ("u", u), ("F", F)):
+            if arr is not None:
+                a = np.ascontiguousarray(arr, dtype=np.float64)
+                keep.append(a)
+                setattr(su, name, _dp(a))
+        self.h = C.c_void_p()
+        check(self.L.lbmgpu_energy3d_create(C.byref(su), C.byref(self.h)))
+
+    def init(self):
+        check(self.L.lbmgpu_energy3d_init(self.h))
+
+    def step(self, n: int):
+        check(self.L.lbmgpu_energy3d_step(self.h, int(n)))
+
+    def step_timed(self, n: int) -> float:
+        ms = C.c_double()
+        check(self.L.lbmgpu_energy3d_step_timed(self.h, int(n), C.byref(ms)))
+        return ms.value
+
+    def download(self, field: str) -> np.ndarray:
+        out = np.empty(self.shape)
+        check(self.L.lbmgpu_energy3d_download(self.h, self.FIELDS[field], _dp(out)))
+        return out
+
+    def moments(self) -> dict:
+        return {k: self.download(k) for k in self.FIELDS}
+
+    def status(self) -> int:
+        v = C.c_uint32()
+        check(self.L.lbmgpu_energy3d_status(self.h, C.byref(v)))
+        return int(v.value)
+
+    def close(self):
+        if self.h:
+            self.L.lbmgpu_energy3d_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

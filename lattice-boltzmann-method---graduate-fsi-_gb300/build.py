@@ -17,7 +17,13 @@ OBJ = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "liblbmgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 SOURCES = ["lbm_abi.cu", "lbm_stream.cu", "lbm_stepv.cu", "lbm_ibm.cu", "lbm_batch.cu", "lbm_serve.cu",
-           "lbm_output.cu", "lbm_checkpoint.cu", "lbm_details.cu", "lbm2d.cu", "lbm_nusselt.cu"]
+           "lbm_output.cu", "lbm_checkpoint.cu", "lbm_details.cu", "lbm2d.cu", "lbm_nusselt.cu", "lbm_energy3d.cu"]
+
+
+# host code whose rounding must follow the reference's (lbm_energy3d.cu
+# decides which walls move from MacroProp's sums): no a*b+c contraction,
+# which gcc does by default on aarch64
+HOST_FLAGS = {"lbm_energy3d.cu": ["-Xcompiler", "-ffp-contract=off"]}
 
 
 def _nvcc() -> str:
@@ -50,7 +56,8 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
         obj = os.path.join(OBJ, s.replace(".cu", ".o"))
         objs.append(obj)
         if force or _stale(obj, _deps(src)):
-            cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-c", src, "-o", obj]
+            cmd = [nvcc, *ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", *HOST_FLAGS.get(s, []),
+                   "-c", src, "-o", obj]
             if ptxas_v:
                 cmd.insert(1, "-Xptxas=-v")
             jobs.append(cmd)

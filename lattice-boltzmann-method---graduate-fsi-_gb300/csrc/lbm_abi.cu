@@ -208,7 +208,7 @@ static void choose_block(lbm_handle *h) {
 // ---------------------------------------------------------------------------
 // Creation
 // ---------------------------------------------------------------------------
-extern "C" int lbmgpu_abi_version(void) { return 2; }
+extern "C" int lbmgpu_abi_version(void) { return 3; }
 
 cudaStream_t lbm_handle_stream(lbm_handle *h) { return h->s; }
 

@@ -1,0 +1,727 @@
+// lbm_energy3d.cu -- the reference's ENERGY model on D3Q19 (#define ENERGY
+// without D2Q9; its Rayleigh_Benard case, LBM.h:222-242, lbm.cpp:1585-1643):
+// temperature populations g on the flow lattice with viscous heating,
+// Dirichlet (TYPE_T), Neumann (TYPE_Q) and adiabatic walls, and the
+// Boussinesq force that MacroProp refreshes on every cell (lbm.cpp:803-805).
+//
+// The device grid is the reference's ghost-inclusive one, (Nx+2)(Ny+2)(Nz+2)
+// cells with its periodic modulo over the whole grid, so every wall rule
+// reads the cells the reference reads.  f and g are FP32, stored shifted
+// (f - w, g - w T_ref) in [19][S] arrays, two of each (pull scheme).
+//
+// The reference applies its thermal wall rules inside a serial push
+// (lbm.cpp:240-289): a Neumann wall's T (Determine_Twall_Neumann,
+// lbm.cpp:983-1028) sums the cell's g while neighbours are still pushing,
+// and is written into wall cells that Determine_Wall_Temperature
+// (lbm.cpp:965-981) of cells visited later reads for their Dirichlet links.
+// Every value such a read can see is known before the sweep: the wall T a
+// Neumann cell forms depends only on the previous collision and on its own
+// previous g.  So the host replays the visiting order once (build_records)
+// and gives each wall-adjacent fluid cell a record: its link masks, the
+// wall velocity of each phase, and for each solid neighbour the cell whose
+// Neumann write it sees (or none, then the wall's own T).  Per step a
+// pre-pass (k_e3_walls) forms the Neumann cells' T_w; the step kernel
+// (k_e3_step) pulls, applies the wall rules, takes the moments, refreshes
+// the force and collides.
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/lbmgpu.h"
+#include "lbm_collide.cuh"
+#include "lbm_device.cuh"
+
+void lbm_set_last_error(const std::string &m);
+
+namespace {
+using namespace lbmk;
+
+constexpr int kSlots = 18;       // solid neighbours a cell can have
+constexpr int kTypeF = 0, kTypeS = 1, kTypeT = 6, kTypeQ = 7;
+constexpr int kBlock = 256;
+
+// A fluid cell with at least one solid neighbour.  Links are indexed by the
+// pulled direction p (source c - c_p); the reference's push direction of
+// that wall link is opp(p).
+struct E3Rec {
+    int cell;
+    uint32_t bb;             // links whose source is solid
+    uint32_t dir, neu, adi;  // ... of type_Energy TYPE_T, TYPE_Q, any other
+    int nsol;                // solid neighbours
+    float uw[3][3];          // Determine_Wall_Velocity at streaming 1, 2, and from 3 on
+    int writer[kSlots];      // record whose Neumann push last wrote the slot's T before this cell; -1 none
+    float tsol[2][kSlots];   // the slot's own T: set-up (streaming 1), MacroProp's (later)
+    uint8_t own[kSlots];     // push index at which this cell itself writes the slot's T; 255 never
+};
+
+struct E3Params {
+    int NX, NY, NZ;
+    long long N, S;
+    int nrec;
+    float omega, inv_tau_g, tg_fac, inv_cp, two_nu, s_fac, T_ref;
+    float gbeta, T_star;
+    int buoy, forced;
+};
+
+__device__ __forceinline__ long long wrap_src(int i, int j, int k, int l, const E3Params &P) {
+    int a = i - cx(l), b = j - cy(l), c = k - cz(l);
+    a += a < 0 ? P.NX : (a >= P.NX ? -P.NX : 0);
+    b += b < 0 ? P.NY : (b >= P.NY ? -P.NY : 0);
+    c += c < 0 ? P.NZ : (c >= P.NZ ? -P.NZ : 0);
+    return a + (long long)P.NX * (b + (long long)P.NY * c);
+}
+
+// 1 + 3x + 4.5x^2 - 1.5uu (+ 4.5x(x^2 - uu) for the cubic form), x = c.u
+__device__ __forceinline__ float p2m1(float x, float uu) { return 3.0f * x + 4.5f * x * x - 1.5f * uu; }
+__device__ __forceinline__ float p3m1(float x, float uu) { return p2m1(x, uu) + 4.5f * x * (x * x - uu); }
+
+// Determine_Twall_Neumann for every record with Neumann links: the normal is
+// the mean direction of the links from walls (cdotn_pos); the other links
+// contribute this sweep's pulled value where the reference's push (i outer,
+// k inner) visits their source before the cell -- and for the rest link --,
+// else the previous sweep's, kept in gold; the wall links the equilibrium
+// at T = 1 of the cell's density (previous MacroProp) and the wall velocity.
+// With j.n = 0 (LBM.h's j_dot_n): T_w = -sum_other g c.n / sum_wall geq c.n.
+// keep: store this sweep's pulled values for the next sweep.
+__global__ void __launch_bounds__(kBlock) k_e3_walls(const float *__restrict__ GA, const float4 *__restrict__ aux,
+                                                     const E3Rec *__restrict__ recs, float *__restrict__ gold,
+                                                     float *__restrict__ tw, const __grid_constant__ E3Params P,
+                                                     int phase, int keep) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.nrec) return;
+    const E3Rec &R = recs[r];
+    if (!R.neu) return;
+    const int c = R.cell;
+    const int i = c % P.NX, j = (c / P.NX) % P.NY, k = c / (P.NX * P.NY);
+    float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
+    int np = 0;
+#pragma unroll
+    for (int p = 0; p < Q; p++)
+        if ((R.bb >> p) & 1u) {
+            n0 += cx(p);
+            n1 += cy(p);
+            n2 += cz(p);
+            np++;
+        }
+    const float inv_np = 1.0f / (float)np;
+    n0 *= inv_np;
+    n1 *= inv_np;
+    n2 *= inv_np;
+    const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
+    const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+    float other = 0.0f, wall = 0.0f;
+#pragma unroll
+    for (int p = 0; p < Q; p++) {
+        const float cn = cx(p) * n0 + cy(p) * n1 + cz(p) * n2;
+        if ((R.bb >> p) & 1u) {
+            const float x = cx(p) * u0 + cy(p) * u1 + cz(p) * u2;
+            wall += wf(p) * (1.0f + p3m1(x, uu)) * cn;
+        } else {
+            const long long s = wrap_src(i, j, k, p, P);
+            const float v = GA[p * P.S + s];
+            const int si = (int)(s % P.NX), sj = (int)((s / P.NX) % P.NY), sk = (int)(s / ((long long)P.NX * P.NY));
+            const bool fresh = p == 0 || si < i || (si == i && (sj < j || (sj == j && sk < k)));
+            float *kept = gold + (long long)p * P.nrec + r;
+            other += ((fresh ? v : *kept) + wf(p) * P.T_ref) * cn;
+            if (keep) *kept = v;
+        }
+    }
+    const float rho = 1.0f + aux[c].x;
+    tw[r] = -other / (rho * wall);
+}
+
+// One step of f and g over the whole grid (solid cells idle).  gather = 0:
+// the first collision, on the set-up state (no streaming before it).
+// aux[c] = (rho - 1, u) of the last MacroProp (the previous collision's);
+// aux2[c] = (Phi of the previous collision, the force of the last
+// MacroProp).  MacroProp (lbm.cpp:657-806): u = (j + F/2) / rho with the
+// force of the previous MacroProp, T = sum g, q = sum g c, then
+// F_y = g beta (T - T*) when the buoyancy is on.  ConvLBM (lbm.cpp:91-177):
+// f by BGK + Guo with that force; g by BGK with the viscous-heating source
+// F_l = w Phi / cp (1 + c.u (tau_g - 1/2) / (cs2 tau_g)) and half its change
+// since the previous collision.
+__global__ void __launch_bounds__(kBlock) k_e3_step(const float *__restrict__ A, float *__restrict__ B,
+                                                    const float *__restrict__ GA, float *__restrict__ GB,
+                                                    float4 *__restrict__ aux, float4 *__restrict__ aux2,
+                                                    const int *__restrict__ rec_of, const E3Rec *__restrict__ recs,
+                                                    float *__restrict__ gold, const float *__restrict__ tw,
+                                                    const __grid_constant__ E3Params P, uint32_t *__restrict__ status,
+                                                    float *__restrict__ mom, int gather, int phase, int export_only) {
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= P.N) return;
+    const int ro = rec_of[c];
+    if (ro == -2) return;  // solid
+    const int i = (int)(c % P.NX), j = (int)((c / P.NX) % P.NY), k = (int)(c / ((long long)P.NX * P.NY));
+    const float4 h1 = aux[c], h2 = aux2[c];
+    const float drho_p = h1.x;
+    float f[Q], g[Q];
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            f[l] = A[l * P.S + c];
+            g[l] = GA[l * P.S + c];
+        }
+        if (ro >= 0 && !export_only) {
+#pragma unroll
+            for (int l = 0; l < Q; l++) gold[(long long)l * P.nrec + ro] = g[l];
+        }
+    } else if (ro < 0) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            const long long s = wrap_src(i, j, k, l, P);
+            f[l] = A[l * P.S + s];
+            g[l] = GA[l * P.S + s];
+        }
+    } else {
+        const E3Rec &R = recs[ro];
+        const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
+        const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+        const float rho_p = 1.0f + drho_p;
+        const float tw_own = R.neu ? tw[ro] : 0.0f;
+        const float inv_nsol = 1.0f / (float)R.nsol;
+#pragma unroll
+        for (int p = 0; p < Q; p++) {
+            if (!((R.bb >> p) & 1u)) {
+                const long long s = wrap_src(i, j, k, p, P);
+                f[p] = A[p * P.S + s];
+                g[p] = GA[p * P.S + s];
+                continue;
+            }
+            const int q = opp(p);  // the reference's push direction, towards the wall
+            const float x = cx(q) * u0 + cy(q) * u1 + cz(q) * u2;
+            // f_opp(q) = f*_q - 2 w (u_w . c_q) / cs2 (lbm.cpp:273-274)
+            f[p] = A[q * P.S + c] - 6.0f * wf(q) * x;
+            if ((R.dir >> p) & 1u) {
+                // Determine_Wall_Temperature at this point of the push: the
+                // mean T of the solid neighbours as the sweep has left them
+                float Tsum = 0.0f;
+                for (int m = 0; m < R.nsol; m++) {
+                    float v;
+                    if (R.own[m] < q) v = tw_own;
+                    else if (R.writer[m] >= 0) v = tw[R.writer[m]];
+                    else v = R.tsol[phase == 0 ? 0 : 1][m];
+                    Tsum += v;
+                }
+                const float Tw = Tsum * inv_nsol;
+                // -g*_q + 2 geq_q(rho, T_w, u_w) (lbm.cpp:277-280)
+                g[p] = 2.0f * wf(q) * (rho_p * Tw * (1.0f + p3m1(x, uu)) - P.T_ref) - GA[q * P.S + c];
+            } else if ((R.neu >> p) & 1u) {
+                // w rho T_w times the second-order shape of the wall (lbm.cpp:281-288)
+                g[p] = wf(q) * (rho_p * tw_own * (1.0f + p2m1(x, uu)) - P.T_ref);
+            } else {
+                g[p] = gold[(long long)p * P.nrec + ro];  // never written: the initial value
+            }
+        }
+    }
+    float drho, jx, jy, jz;
+    moments_pairs(f, drho, jx, jy, jz);
+    float dT = 0.0f, qx = 0.0f, qy = 0.0f, qz = 0.0f;
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        dT += g[l];
+        if (cx(l)) qx += cx(l) * g[l];
+        if (cy(l)) qy += cy(l) * g[l];
+        if (cz(l)) qz += cz(l) * g[l];
+    }
+    const float rho = 1.0f + drho;
+    const float inv = 1.0f / rho;
+    // before the first MacroProp the collision takes the set-up state:
+    // u = j / rho, T = sum g / rho (the initial g sum to rho T)
+    const float hf = gather ? 0.5f : 0.0f;
+    const float ux = (jx + hf * h2.y) * inv, uy = (jy + hf * h2.z) * inv, uz = (jz + hf * h2.w) * inv;
+    const float Tc = gather ? P.T_ref + dT : (P.T_ref + dT) * inv;
+    // rho T - T_ref
+    const float Tdiff = gather ? dT + drho * Tc : dT;
+    float Fx = h2.y, Fy = h2.z, Fz = h2.w;
+    if (gather && P.buoy) Fy = P.gbeta * (Tc - P.T_star);
+    if (!(rho > 0.0f && rho < 100.0f)) raise_status(status, ST_RHO_RANGE);
+    if (!(Tc > 0.0f && Tc < 100.0f)) raise_status(status, ST_T_RANGE);
+    if (mom != nullptr) {
+        mom[c] = rho;
+        mom[P.N + c] = ux;
+        mom[2 * P.N + c] = uy;
+        mom[3 * P.N + c] = uz;
+        mom[4 * P.N + c] = Tc;
+        mom[5 * P.N + c] = qx;  // sum g c: the shift w T_ref carries no momentum
+        mom[6 * P.N + c] = qy;
+        mom[7 * P.N + c] = qz;
+    }
+    if (export_only) return;
+    const float usq = ux * ux + uy * uy + uz * uz;
+    float sxx = 0.0f, syy = 0.0f, szz = 0.0f, sxy = 0.0f, sxz = 0.0f, syz = 0.0f;
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
+        const float fne = f[l] - wf(l) * (drho + rho * p3m1(cu, usq));
+        sxx += (float)(cx(l) * cx(l)) * fne;
+        syy += (float)(cy(l) * cy(l)) * fne;
+        szz += (float)(cz(l) * cz(l)) * fne;
+        sxy += (float)(cx(l) * cy(l)) * fne;
+        sxz += (float)(cx(l) * cz(l)) * fne;
+        syz += (float)(cy(l) * cz(l)) * fne;
+    }
+    const float sk = P.s_fac * inv;
+    sxx *= sk;
+    syy *= sk;
+    szz *= sk;
+    sxy *= sk;
+    sxz *= sk;
+    syz *= sk;
+    const float phi =
+        P.two_nu * rho * (sxx * sxx + syy * syy + szz * szz + 2.0f * (sxy * sxy + sxz * sxz + syz * syz));
+    collide_flow(f, drho, ux, uy, uz, Fx, Fy, Fz, P.forced != 0, P.omega);
+    const float a = phi * P.inv_cp, ap = h2.x * P.inv_cp;
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
+        const float cup = cx(l) * h1.y + cy(l) * h1.z + cz(l) * h1.w;
+        const float Fl = wf(l) * a * (1.0f + cu * P.tg_fac);
+        const float Fb = wf(l) * ap * (1.0f + cup * P.tg_fac);
+        const float geq = wf(l) * (Tdiff + rho * Tc * p3m1(cu, usq));
+        g[l] = g[l] - (g[l] - geq) * P.inv_tau_g + Fl + 0.5f * (Fl - Fb);
+    }
+    aux[c] = make_float4(drho, ux, uy, uz);
+    aux2[c] = make_float4(phi, Fx, Fy, Fz);
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        B[l * P.S + c] = f[l];
+        GB[l * P.S + c] = g[l];
+    }
+}
+
+// LBM::Init (lbm.cpp:31-57) on the fluid cells: f = feq(rho, u), g =
+// rho w T P3(u) (Calc_geq, lbm.cpp:636-653), shifted; aux = (rho - 1, u),
+// aux2 = (0, F).  fields: [8][N] rho, u, T, F of the set-up.
+__global__ void k_e3_init(float *__restrict__ A, float *__restrict__ GA, float4 *__restrict__ aux,
+                          float4 *__restrict__ aux2, const int *__restrict__ rec_of, const float *__restrict__ fields,
+                          const __grid_constant__ E3Params P) {
+    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (c >= P.N || rec_of[c] == -2) return;
+    const float rho = fields[c], ux = fields[P.N + c], uy = fields[2 * P.N + c], uz = fields[3 * P.N + c];
+    const float T = fields[4 * P.N + c];
+    const float usq = ux * ux + uy * uy + uz * uz;
+#pragma unroll
+    for (int l = 0; l < Q; l++) {
+        const float cu = cx(l) * ux + cy(l) * uy + cz(l) * uz;
+        const float pm = p3m1(cu, usq);
+        A[l * P.S + c] = wf(l) * ((rho - 1.0f) + rho * pm);
+        GA[l * P.S + c] = wf(l) * ((rho * T - P.T_ref) + rho * T * pm);
+    }
+    aux[c] = make_float4(rho - 1.0f, ux, uy, uz);
+    aux2[c] = make_float4(0.0f, fields[5 * P.N + c], fields[6 * P.N + c], fields[7 * P.N + c]);
+}
+
+lbm_status fail3(lbm_status s, const std::string &m) {
+    lbm_set_last_error(m);
+    return s;
+}
+
+}  // namespace
+
+struct lbm_energy3d {
+    E3Params P{};
+    int nx = 0, ny = 0, nz = 0;
+    float *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
+    float4 *aux = nullptr, *aux2 = nullptr;
+    int *rec_of = nullptr;
+    E3Rec *recs = nullptr;
+    float *gold = nullptr, *tw = nullptr, *mom = nullptr, *fields = nullptr;
+    uint32_t *status = nullptr;
+    bool has_neu = false, inited = false;
+    int cur = 0;
+    long long steps = 0;
+    cudaStream_t s = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    std::vector<void *> allocs;
+};
+
+namespace {
+
+template <class Tp>
+cudaError_t alloc3(lbm_energy3d *e, Tp **p, size_t bytes) {
+    cudaError_t err = cudaMalloc((void **)p, bytes);
+    if (err == cudaSuccess) e->allocs.push_back((void *)*p);
+    else *p = nullptr;
+    return err;
+}
+
+void free3(lbm_energy3d *e) {
+    for (void *p : e->allocs) cudaFree(p);
+    if (e->s) cudaStreamDestroy(e->s);
+    for (cudaEvent_t v : e->ev)
+        if (v) cudaEventDestroy(v);
+    delete e;
+}
+
+int phase_of(long long steps) { return steps <= 1 ? 0 : (steps == 2 ? 1 : 2); }
+
+// The wall records.  type/te/T/rho/u/F: the set-up arrays (ghost-inclusive).
+// Replays the reference's push order (i outer, j, k inner) over the fluid
+// cells to find, for each solid neighbour of a cell, the last Neumann write
+// of its T before the cell (Determine_Twall_Neumann's write of the cell
+// opposite the normal, lbm.cpp:1021-1027, and the write of each Neumann
+// wall cell, lbm.cpp:284).
+lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, double gbeta, double T_star,
+                         bool buoy, const std::vector<double> &rho, const std::vector<double> &F,
+                         std::vector<int> &rec_of, std::vector<E3Rec> &recs) {
+    const long long N = (long long)NX * NY * NZ;
+    auto idx = [&](int i, int j, int k) { return (long long)i + (long long)NX * (j + (long long)NY * k); };
+    auto nb = [&](long long c, int l) {
+        const int i = (int)(c % NX), j = (int)((c / NX) % NY), k = (int)(c / ((long long)NX * NY));
+        return idx((i + cx(l) + NX) % NX, (j + cy(l) + NY) % NY, (k + cz(l) + NZ) % NZ);
+    };
+    auto solid = [&](long long c) { return su.type[c] == kTypeS; };
+    // A wall's g and f never change after Init, so MacroProp gives it the
+    // same T and rho every step: the sums, in the reference's order and
+    // rounding, of its initial g = rho w T_w (Calc_geq at rest, T_w the mean
+    // set-up T of its solid neighbours, Determine_Wall_Temperature) and f =
+    // rho w.  The rounding matters: Determine_Wall_Velocity counts the walls
+    // with u != 0, and a wall whose exact T is T* moves at about 1e-21
+    // (this file is compiled without floating-point contraction).
+    std::vector<double> Twall(N, 0.0), rho_w(N, 1.0);
+    for (long long c = 0; c < N; c++) {
+        if (!solid(c)) continue;
+        double s = 0.0;
+        int num = 0;
+        for (int l = 0; l < Q; l++) {
+            const long long n = nb(c, l);
+            if (solid(n)) {
+                s += su.T[n];
+                num++;
+            }
+        }
+        if (!num) {
+            Twall[c] = NAN;
+            continue;
+        }
+        const double Tw = s / num;
+        double Tm = 0.0, rm = 0.0;
+        for (int l = 0; l < Q; l++) {
+            Tm += rho[c] * wd(l) * Tw;
+            rm += rho[c] * wd(l);
+        }
+        Twall[c] = Tm;
+        rho_w[c] = rm;
+    }
+    // the walls' velocity at streaming 1 (set-up), 2 (after MacroProp 1)
+    // and later (after MacroProp 2): u_set + F / (2 rho_w), F the force of
+    // the previous MacroProp (the set-up one, then the refreshed one)
+    auto wall_u = [&](long long w, int ph, double out[3]) {
+        const double *u = su.u;
+        for (int a = 0; a < 3; a++) {
+            double v = u ? u[a * N + w] : 0.0;
+            if (ph >= 1) {
+                double Fa = F[a * N + w];
+                if (ph == 2 && buoy && a == 1) Fa = gbeta * (Twall[w] - T_star);
+                v += 0.5 * Fa / rho_w[w];
+            }
+            out[a] = v;
+        }
+    };
+    rec_of.assign(N, -2);
+    recs.clear();
+    for (long long c = 0; c < N; c++) {
+        if (su.type[c] != kTypeF) continue;
+        bool any = false;
+        for (int l = 1; l < Q && !any; l++) any = solid(nb(c, l));
+        if (!any) {
+            rec_of[c] = -1;
+            continue;
+        }
+        E3Rec R;
+        memset(&R, 0, sizeof(R));
+        R.cell = (int)c;
+        for (int m = 0; m < kSlots; m++) {
+            R.writer[m] = -1;
+            R.own[m] = 255;
+        }
+        for (int ph = 0; ph < 3; ph++) {
+            double s[3] = {0, 0, 0};
+            int num = 0;
+            for (int l = 0; l < Q; l++) {
+                const long long w = nb(c, l);
+                if (!solid(w)) continue;
+                double uw[3];
+                wall_u(w, ph, uw);
+                if (uw[0] != 0 || uw[1] != 0 || uw[2] != 0) {
+                    for (int a = 0; a < 3; a++) s[a] += uw[a];
+                    num++;
+                }
+            }
+            for (int a = 0; a < 3; a++) R.uw[ph][a] = (float)(num ? s[a] / num : 0.0);
+        }
+        for (int l = 0; l < Q; l++) {
+            const long long w = nb(c, l);
+            if (!solid(w)) continue;
+            const int p = opp(l);
+            R.bb |= 1u << p;
+            const int te = su.type_energy[w];
+            if (te == kTypeT) R.dir |= 1u << p;
+            else if (te == kTypeQ) R.neu |= 1u << p;
+            else R.adi |= 1u << p;
+            if (!(std::isfinite(Twall[w])))
+                return fail3(LBM_ERR_UNSUPPORTED, "energy3d_create: a wall cell next to fluid has no solid "
+                                                  "neighbour (Determine_Wall_Temperature divides by zero)");
+            R.tsol[0][R.nsol] = (float)su.T[w];
+            R.tsol[1][R.nsol] = (float)Twall[w];
+            R.nsol++;
+        }
+        rec_of[c] = (int)recs.size();
+        recs.push_back(R);
+    }
+    // the push order, replayed: last_writer[w] = record of the last
+    // Neumann write of solid w so far
+    std::vector<int> last_writer(N, -1);
+    for (int i = 0; i < NX; i++)
+        for (int j = 0; j < NY; j++)
+            for (int k = 0; k < NZ; k++) {
+                const long long c = idx(i, j, k);
+                const int r = rec_of[c];
+                if (r < 0) continue;
+                E3Rec &R = recs[r];
+                // the slots in push-direction order, as built above
+                long long slot_cell[kSlots];
+                int m = 0;
+                for (int l = 0; l < Q; l++) {
+                    const long long w = nb(c, l);
+                    if (solid(w)) slot_cell[m++] = w;
+                }
+                for (m = 0; m < R.nsol; m++) R.writer[m] = last_writer[slot_cell[m]];
+                if (!R.neu) continue;
+                // this cell's writes: at its first Neumann link the cell
+                // opposite the normal (when the normal is a lattice
+                // direction), at each Neumann link that link's wall cell
+                double n[3] = {0, 0, 0};
+                int np = 0;
+                for (int l = 0; l < Q; l++)
+                    if (solid(nb(c, l))) {
+                        n[0] += cx(opp(l));
+                        n[1] += cy(opp(l));
+                        n[2] += cz(opp(l));
+                        np++;
+                    }
+                for (int a = 0; a < 3; a++) n[a] /= np;
+                long long wn = -1;
+                for (int l = 0; l < Q; l++) {
+                    const int o = opp(l);
+                    if (cx(o) == n[0] && cy(o) == n[1] && cz(o) == n[2]) {
+                        wn = nb(c, l);
+                        break;
+                    }
+                }
+                bool first = true;
+                std::vector<long long> written;
+                for (int l = 0; l < Q; l++) {
+                    const long long w = nb(c, l);
+                    if (!solid(w) || su.type_energy[w] != kTypeQ) continue;
+                    const long long targets[2] = {first ? wn : -1, w};
+                    first = false;
+                    for (long long t : targets) {
+                        if (t < 0) continue;
+                        for (int s = 0; s < R.nsol; s++)
+                            if (slot_cell[s] == t && R.own[s] == 255) R.own[s] = (uint8_t)l;
+                        written.push_back(t);
+                    }
+                }
+                for (long long t : written) last_writer[t] = r;
+            }
+    return LBM_OK;
+}
+
+#define CK3(expr)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) return fail3(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
+    const E3Params &P = e->P;
+    const int gather = e->steps > 0 ? 1 : 0;
+    const int phase = phase_of(e->steps);
+    if (gather && e->has_neu) {
+        const unsigned nb = (unsigned)((P.nrec + kBlock - 1) / kBlock);
+        k_e3_walls<<<nb, kBlock, 0, e->s>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
+                                           export_only ? 0 : 1);
+    }
+    const unsigned blocks = (unsigned)((P.N + kBlock - 1) / kBlock);
+    k_e3_step<<<blocks, kBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
+                                          e->aux2, e->rec_of, e->recs, e->gold, e->tw, P, e->status, mom, gather,
+                                          phase, export_only);
+    return cudaGetLastError();
+}
+
+}  // namespace
+
+extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_energy3d **out) {
+    if (!su || !out || !su->type || !su->type_energy || !su->T || su->nx < 1 || su->ny < 1 || su->nz < 1)
+        return fail3(LBM_ERR_INVALID, "energy3d_create: bad arguments");
+    if (!(su->tau > 0.5) || !(su->tau_g > 0.5) || !(su->cp > 0))
+        return fail3(LBM_ERR_INVALID, "energy3d_create: needs tau > 0.5, tau_g > 0.5 and cp > 0");
+    *out = nullptr;
+    const int NX = su->nx + 2, NY = su->ny + 2, NZ = su->nz + 2;
+    const long long N = (long long)NX * NY * NZ;
+    if (N > (1LL << 30)) return fail3(LBM_ERR_INVALID, "energy3d_create: more than 2^30 cells");
+    double Tsum = 0.0;
+    long long nf = 0;
+    for (long long c = 0; c < N; c++) {
+        if (su->type[c] == kTypeF) {
+            Tsum += su->T[c];
+            nf++;
+        } else if (su->type[c] != kTypeS) {
+            return fail3(LBM_ERR_UNSUPPORTED, "energy3d_create: cell types other than TYPE_F and TYPE_S");
+        }
+    }
+    if (!nf) return fail3(LBM_ERR_INVALID, "energy3d_create: no fluid cell");
+    std::vector<double> rho(N, 1.0), F(3 * N, 0.0);
+    if (su->rho)
+        for (long long c = 0; c < N; c++) rho[c] = su->rho[c];
+    if (su->F)
+        for (long long c = 0; c < 3 * N; c++) F[c] = su->F[c];
+    bool forced = su->g_beta != 0.0;
+    for (long long c = 0; c < 3 * N && !forced; c++) forced = su->type[c % N] == kTypeF && F[c] != 0.0;
+    std::vector<int> rec_of;
+    std::vector<E3Rec> recs;
+    const bool buoy = su->g_beta != 0.0;
+    lbm_status st = build_records(*su, NX, NY, NZ, su->g_beta, su->T_star, buoy, rho, F, rec_of, recs);
+    if (st != LBM_OK) return st;
+
+    lbm_energy3d *e = new lbm_energy3d();
+    e->nx = su->nx;
+    e->ny = su->ny;
+    e->nz = su->nz;
+    E3Params &P = e->P;
+    P.NX = NX;
+    P.NY = NY;
+    P.NZ = NZ;
+    P.N = N;
+    P.S = ((N + 255) / 256) * 256;
+    P.nrec = (int)recs.size();
+    const double cs2 = 1.0 / 3.0, tg = su->tau_g;
+    P.omega = (float)(1.0 / su->tau);
+    P.inv_tau_g = (float)(1.0 / tg);
+    P.tg_fac = (float)((tg - 0.5) / (cs2 * tg));
+    P.inv_cp = (float)(1.0 / su->cp);
+    P.two_nu = (float)(2.0 * cs2 * (su->tau - 0.5));
+    P.s_fac = (float)(-1.0 / (2.0 * su->tau * cs2));
+    P.T_ref = (float)(Tsum / nf);
+    P.gbeta = (float)su->g_beta;
+    P.T_star = (float)su->T_star;
+    P.buoy = buoy ? 1 : 0;
+    P.forced = forced ? 1 : 0;
+    for (const E3Rec &R : recs) e->has_neu = e->has_neu || R.neu != 0;
+    auto bail = [&](lbm_status s) {
+        free3(e);
+        return s;
+    };
+#define CKE(expr)                                                                                          \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess)                                                                            \
+            return bail(fail3(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)));        \
+    } while (0)
+    CKE(cudaStreamCreateWithFlags(&e->s, cudaStreamNonBlocking));
+    for (int i = 0; i < 2; i++) CKE(cudaEventCreate(&e->ev[i]));
+    for (int i = 0; i < 2; i++) {
+        CKE(alloc3(e, &e->f[i], (size_t)Q * P.S * sizeof(float)));
+        CKE(alloc3(e, &e->g[i], (size_t)Q * P.S * sizeof(float)));
+    }
+    CKE(alloc3(e, &e->aux, (size_t)P.S * sizeof(float4)));
+    CKE(alloc3(e, &e->aux2, (size_t)P.S * sizeof(float4)));
+    CKE(alloc3(e, &e->rec_of, (size_t)N * sizeof(int)));
+    CKE(alloc3(e, &e->recs, std::max<size_t>(1, recs.size()) * sizeof(E3Rec)));
+    CKE(alloc3(e, &e->gold, (size_t)Q * std::max(1, P.nrec) * sizeof(float)));
+    CKE(alloc3(e, &e->tw, (size_t)std::max(1, P.nrec) * sizeof(float)));
+    CKE(alloc3(e, &e->mom, (size_t)8 * N * sizeof(float)));
+    CKE(alloc3(e, &e->fields, (size_t)8 * N * sizeof(float)));
+    CKE(alloc3(e, &e->status, sizeof(uint32_t)));
+    CKE(cudaMemcpy(e->rec_of, rec_of.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice));
+    if (!recs.empty())
+        CKE(cudaMemcpy(e->recs, recs.data(), recs.size() * sizeof(E3Rec), cudaMemcpyHostToDevice));
+    std::vector<float> fl((size_t)8 * N);
+    for (long long c = 0; c < N; c++) {
+        fl[c] = (float)rho[c];
+        for (int a = 0; a < 3; a++) fl[(1 + a) * N + c] = (float)(su->u ? su->u[a * N + c] : 0.0);
+        fl[4 * N + c] = (float)su->T[c];
+        for (int a = 0; a < 3; a++) fl[(5 + a) * N + c] = (float)F[a * N + c];
+    }
+    CKE(cudaMemcpy(e->fields, fl.data(), fl.size() * sizeof(float), cudaMemcpyHostToDevice));
+#undef CKE
+    *out = e;
+    return lbmgpu_energy3d_init(e);
+}
+
+extern "C" lbm_status lbmgpu_energy3d_init(lbm_energy3d *e) {
+    if (!e) return fail3(LBM_ERR_INVALID, "energy3d_init: null handle");
+    const E3Params &P = e->P;
+    CK3(cudaMemsetAsync(e->status, 0, sizeof(uint32_t), e->s));
+    // NaN on the solid cells of the exported moments
+    CK3(cudaMemsetAsync(e->mom, 0xff, (size_t)8 * P.N * sizeof(float), e->s));
+    for (int i = 0; i < 2; i++) {
+        CK3(cudaMemsetAsync(e->f[i], 0, (size_t)Q * P.S * sizeof(float), e->s));
+        CK3(cudaMemsetAsync(e->g[i], 0, (size_t)Q * P.S * sizeof(float), e->s));
+    }
+    const unsigned blocks = (unsigned)((P.N + kBlock - 1) / kBlock);
+    k_e3_init<<<blocks, kBlock, 0, e->s>>>(e->f[0], e->g[0], e->aux, e->aux2, e->rec_of, e->fields, P);
+    CK3(cudaGetLastError());
+    CK3(cudaStreamSynchronize(e->s));
+    e->cur = 0;
+    e->steps = 0;
+    e->inited = true;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_energy3d_step(lbm_energy3d *e, int nsteps) {
+    if (!e) return fail3(LBM_ERR_INVALID, "energy3d_step: null handle");
+    if (!e->inited) return fail3(LBM_ERR_STATE, "energy3d_step: not initialised");
+    if (nsteps < 0) return fail3(LBM_ERR_INVALID, "energy3d_step: negative count");
+    for (int n = 0; n < nsteps; n++) {
+        CK3(enqueue3(e, nullptr, 0));
+        e->cur = 1 - e->cur;
+        e->steps++;
+    }
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_energy3d_step_timed(lbm_energy3d *e, int nsteps, double *ms) {
+    if (!e || !ms) return fail3(LBM_ERR_INVALID, "energy3d_step_timed: bad arguments");
+    CK3(cudaEventRecord(e->ev[0], e->s));
+    lbm_status st = lbmgpu_energy3d_step(e, nsteps);
+    if (st != LBM_OK) return st;
+    CK3(cudaEventRecord(e->ev[1], e->s));
+    CK3(cudaEventSynchronize(e->ev[1]));
+    float t = 0.0f;
+    CK3(cudaEventElapsedTime(&t, e->ev[0], e->ev[1]));
+    *ms = t;
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_energy3d_download(lbm_energy3d *e, int field, double *host) {
+    if (!e || !host || field < LBM_FIELD_RHO || field > LBM_FIELD_QZ)
+        return fail3(LBM_ERR_INVALID, "energy3d_download: bad arguments");
+    if (!e->inited) return fail3(LBM_ERR_STATE, "energy3d_download: not initialised");
+    // a gather-only pass over the current state (no collision, no store)
+    CK3(enqueue3(e, e->mom, 1));
+    const long long N = e->P.N;
+    std::vector<float> buf(N);
+    CK3(cudaMemcpyAsync(buf.data(), e->mom + (long long)field * N, N * sizeof(float), cudaMemcpyDeviceToHost, e->s));
+    CK3(cudaStreamSynchronize(e->s));
+    for (long long c = 0; c < N; c++) host[c] = buf[c];
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_energy3d_status(lbm_energy3d *e, uint32_t *flags) {
+    if (!e || !flags) return fail3(LBM_ERR_INVALID, "energy3d_status: bad arguments");
+    CK3(cudaMemcpyAsync(flags, e->status, sizeof(uint32_t), cudaMemcpyDeviceToHost, e->s));
+    CK3(cudaStreamSynchronize(e->s));
+    return LBM_OK;
+}
+
+extern "C" lbm_status lbmgpu_energy3d_destroy(lbm_energy3d *e) {
+    if (!e) return LBM_OK;
+    if (e->s) cudaStreamSynchronize(e->s);
+    free3(e);
+    return LBM_OK;
+}

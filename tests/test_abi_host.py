@@ -23,7 +23,7 @@ def test_exports_every_declared_symbol(pkg):
     for name in declared:
         assert hasattr(L, name), name
     assert sorted(pkg.ABI_SYMBOLS) == declared
-    assert L.lbmgpu_abi_version() == 2
+    assert L.lbmgpu_abi_version() == 3
 
 
 def _ref_geometry(nx, ny, nz):
