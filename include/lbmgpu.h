@@ -534,7 +534,9 @@ lbm_status lbmgpu_energy3d_init(lbm_energy3d *e);
 lbm_status lbmgpu_energy3d_step(lbm_energy3d *e, int nsteps);
 lbm_status lbmgpu_energy3d_step_timed(lbm_energy3d *e, int nsteps, double *ms);
 /* LBM_FIELD_RHO .. LBM_FIELD_QZ after the last streaming and MacroProp, on
- * the whole ghost-inclusive grid; NaN on TYPE_S cells. */
+ * the whole ghost-inclusive grid, walls included: MacroProp's values on a
+ * wall (lbm.cpp:657-806) are the sums of its initial populations, with
+ * u = u_set + F / (2 rho) and q = 0. */
 lbm_status lbmgpu_energy3d_download(lbm_energy3d *e, int field, double *host);
 lbm_status lbmgpu_energy3d_status(lbm_energy3d *e, uint32_t *flags);
 lbm_status lbmgpu_energy3d_destroy(lbm_energy3d *e);

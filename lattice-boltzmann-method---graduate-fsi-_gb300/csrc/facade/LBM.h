@@ -80,9 +80,12 @@ struct lbm_options {
     double body_radius = 0.0;     // IBM body radius (0: from the marker cloud)
     int thermal = 0;              // D3Q7 temperature population
     double tau_g = 0.0, T_ref = 0.0, gbeta[3] = {0, 0, 0};
-    // ENERGY builds (-DENERGY, D2Q9): LBM.h's cp = k / (rho0 alpha) of the
+    // ENERGY builds (-DENERGY): LBM.h's cp = k / (rho0 alpha) of the
     // viscous-heating source; tau_g above is its tau_g = 0.5 + alpha / cs2
     double cp = 0.0;
+    // Rayleigh_Benard's MacroProp force F_y = g_beta (T - T_star) on every
+    // cell (lbm.cpp:803-805), D3Q19 ENERGY builds; 0: the set-up force stays
+    double g_beta = 0.0, T_star = 0.0;
     // Poiseuille_Flow builds: MacroProp sets the body force on every cell,
     // walls included (lbm.cpp:800-801); the body force itself is read from
     // fluid[..].F of the fluid cells at Init
@@ -191,6 +194,7 @@ class LBM {
     // GB300 additions
     void sync_to_host();        // MacroProp moments (MORE_DETAILS: and details, statistics) into fluid[..]
     lbm_handle *handle() const; // the device solve (nullptr before Init)
+    lbm_energy3d *energy3d() const; // the D3Q19 ENERGY solve (-DENERGY without -DD2Q9 builds)
     long long steps() const;
     friend void IBLBM(LBM &lb, std::vector<MARKER> &marker, std::vector<double> &ds, std::vector<double> &Cl,
                       std::vector<double> &Cd, double V_CM[], double t);

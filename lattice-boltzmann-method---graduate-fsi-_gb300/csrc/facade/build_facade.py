@@ -11,11 +11,11 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PKG = os.path.dirname(os.path.dirname(HERE))
 OUT = os.path.join(HERE, "_build")
 DRIVERS = ["dropin_cavity", "dropin_sphere", "dropin_sphere_bb", "dropin_details", "dropin_cylinder2d",
-           "dropin_couette", "dropin_staircase2d", "dropin_poiseuille"]
+           "dropin_couette", "dropin_staircase2d", "dropin_poiseuille", "dropin_rayleigh"]
 # compile-time switches of the reference a driver is built with
 DRIVER_FLAGS = {"dropin_details": ["-DMORE_DETAILS"], "dropin_cylinder2d": ["-DD2Q9"],
                 "dropin_couette": ["-DD2Q9", "-DENERGY"], "dropin_staircase2d": ["-DD2Q9"],
-                "dropin_poiseuille": ["-DD2Q9", "-DENERGY"]}
+                "dropin_poiseuille": ["-DD2Q9", "-DENERGY"], "dropin_rayleigh": ["-DENERGY"]}
 
 
 def build(force: bool = False) -> list:

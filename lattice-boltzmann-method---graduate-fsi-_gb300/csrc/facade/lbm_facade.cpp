@@ -12,6 +12,7 @@ lbm_options g_lbm_options;
 
 struct lbm_device_state {
     lbm_handle *h = nullptr;
+    lbm_energy3d *e3 = nullptr;  // D3Q19 ENERGY builds (-DENERGY without -DD2Q9)
     bool collision_pending = false;
     bool mirror_stale = false;
     bool markers_set = false;
@@ -22,6 +23,7 @@ struct lbm_device_state {
     int dn[3] = {0, 0, 0};
     ~lbm_device_state() {
         if (h) lbmgpu_destroy(h);
+        if (e3) lbmgpu_energy3d_destroy(e3);
     }
 };
 
@@ -62,6 +64,7 @@ int LBM::getNy() const { return Ny; }
 int LBM::getNz() const { return Nz; }
 double LBM::getTAU() const { return tau; }
 lbm_handle *LBM::handle() const { return dev->h; }
+lbm_energy3d *LBM::energy3d() const { return dev->e3; }
 long long LBM::steps() const { return dev->steps; }
 
 double LBM::Calc_feq(int i, int j, int k, int l) {
@@ -107,9 +110,70 @@ void LBM::Determine_Wall_Velocity(int i, int j, int k, std::vector<double> &uwal
     }
 }
 
+#if defined ENERGY && !defined D2Q9
+// D3Q19 with ENERGY (the reference's Rayleigh_Benard build): the whole
+// ghost-inclusive set-up goes to lbmgpu_energy3d, which keeps the
+// reference's grid.
+static void init_energy3d(LBM &lb, lbm_device_state &d, double tau) {
+    const int Nx = lb.getNx(), Ny = lb.getNy(), Nz = lb.getNz();
+    const int NX = Nx + 2, NY = Ny + 2, NZ = Nz + 2;
+    const size_t n = (size_t)NX * NY * NZ;
+    std::vector<uint8_t> t(n), te(n);
+    std::vector<double> T(n), rho(n), u(3 * n), F(3 * n);
+    for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+            for (int i = 0; i < NX; i++) {
+                const LATTICE &c = lb.fluid[i][j][k];
+                const size_t id = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k);
+                t[id] = (uint8_t)c.type;
+                te[id] = (uint8_t)c.type_Energy;
+                T[id] = c.T;
+                rho[id] = c.density;
+                u[id] = c.ux;
+                u[n + id] = c.uy;
+                u[2 * n + id] = c.uz;
+                for (int a = 0; a < 3; a++) F[a * n + id] = c.F[a];
+            }
+    const lbm_options &o = g_lbm_options;
+    lbm_energy3d_setup su = {};
+    su.nx = Nx;
+    su.ny = Ny;
+    su.nz = Nz;
+    su.tau = tau;
+    su.tau_g = o.tau_g;
+    su.cp = o.cp;
+    su.g_beta = o.g_beta;
+    su.T_star = o.T_star;
+    su.type = t.data();
+    su.type_energy = te.data();
+    su.T = T.data();
+    su.rho = rho.data();
+    su.u = u.data();
+    su.F = F.data();
+    if (d.e3) lbmgpu_energy3d_destroy(d.e3);
+    d.e3 = nullptr;
+    check("energy3d_create", lbmgpu_energy3d_create(&su, &d.e3));
+}
+#endif
+
 void LBM::Init() {
     const int NX = Nx + 2, NY = Ny + 2, NZ = Nz + 2;
     const size_t n = (size_t)NX * NY * NZ;
+#if defined ENERGY && !defined D2Q9
+    (void)n;
+    init_energy3d(*this, *dev, tau);
+    for (int i = 0; i < NX; i++)
+        for (int j = 0; j < NY; j++)
+            for (int k = 0; k < NZ; k++)
+                for (int l = 0; l < npop; l++) {
+                    double fe = Calc_feq(i, j, k, l);
+                    fluid[i][j][k].f[l] = fe;
+                    fluid[i][j][k].f_star[l] = fe;
+                }
+    dev->steps = 0;
+    dev->mirror_stale = false;
+    return;
+#endif
     std::vector<uint8_t> types(n);
     std::vector<double> rho(n), ux(n), uy(n), uz(n), T(n);
     for (int k = 0; k < NZ; k++)
@@ -176,8 +240,6 @@ void LBM::Init() {
         check("config_energy_2d", lbmgpu_config_energy_2d(&cfg, Nx, Ny, types.data() + layer, te.data(),
                                                           T.data() + layer, o.tau_g, o.cp));
     }
-#elif defined ENERGY
-#error "the ENERGY model runs on D2Q9 builds (-DD2Q9)"
 #endif
     const int dims[3] = {Nx, Ny, Nz};
     const int ddims[3] = {cfg.nx, cfg.ny, cfg.nz};
@@ -245,6 +307,13 @@ void LBM::Init() {
 void LBM::Collision() { dev->collision_pending = true; }
 
 void LBM::Streaming() {
+    if (dev->e3) {
+        check("energy3d_step", lbmgpu_energy3d_step(dev->e3, 1));
+        dev->collision_pending = false;
+        dev->mirror_stale = true;
+        dev->steps++;
+        return;
+    }
     if (!dev->h) check("Streaming before Init", LBM_ERR_STATE);
     check("step", lbmgpu_step(dev->h, 1));
     dev->collision_pending = false;
@@ -264,6 +333,30 @@ void LBM::Streaming() {
 void LBM::MacroProp() { dev->mirror_stale = true; }
 
 void LBM::sync_to_host() {
+    if (dev->e3) {
+        // every cell, ghosts included (the walls as MacroProp leaves them)
+        const int NX = Nx + 2, NY = Ny + 2, NZ = Nz + 2;
+        const size_t n = (size_t)NX * NY * NZ;
+        std::vector<double> v(8 * n);
+        for (int f = 0; f < 8; f++)
+            check("energy3d_download", lbmgpu_energy3d_download(dev->e3, f, v.data() + (size_t)f * n));
+        for (int k = 0; k < NZ; k++)
+            for (int j = 0; j < NY; j++)
+                for (int i = 0; i < NX; i++) {
+                    const size_t id = (size_t)i + (size_t)NX * ((size_t)j + (size_t)NY * k);
+                    LATTICE &c = fluid[i][j][k];
+                    c.density = v[id];
+                    c.ux = v[n + id];
+                    c.uy = v[2 * n + id];
+                    c.uz = v[3 * n + id];
+                    c.T = v[4 * n + id];
+#if defined ENERGY
+                    for (int a = 0; a < 3; a++) c.q[a] = v[(5 + a) * n + id];
+#endif
+                }
+        dev->mirror_stale = false;
+        return;
+    }
     if (!dev->h) return;
     const size_t nd = (size_t)dev->dn[0] * dev->dn[1] * dev->dn[2];
 #if defined ENERGY
@@ -533,6 +626,22 @@ void OutputCSV(std::vector<double> &error, std::string name) {
 }
 
 double Find_Nusselt_number(LBM &lb) {
+    if (lb.energy3d()) {
+        // lbm.cpp:3538-3561 on the mirror, summed in the serial order
+        lb.sync_to_host();
+        double s = 0.0;
+        long long number = 0;
+        for (int i = 0; i <= lb.getNx() + 1; i++)
+            for (int j = 0; j <= lb.getNy() + 1; j++)
+                for (int k = 0; k <= lb.getNz() + 1; k++) {
+                    const LATTICE &c = lb.fluid[i][j][k];
+                    if (c.type == TYPE_F || c.type == TYPE_OUT || c.type == TYPE_IN) {
+                        s += c.uy * c.T;
+                        number++;
+                    }
+                }
+        return 1 + (s / number) / (g_lbm_options.alpha * g_lbm_options.dT / (lb.getNy() + 1));
+    }
     lbm_handle *h = lb.handle();
     if (!h) check("Find_Nusselt_number before Init", LBM_ERR_STATE);
     double nu = 0.0;

@@ -314,6 +314,17 @@ __global__ void k_e3_init(float *__restrict__ A, float *__restrict__ GA, float4 
     aux2[c] = make_float4(0.0f, fields[5 * P.N + c], fields[6 * P.N + c], fields[7 * P.N + c]);
 }
 
+// What MacroProp leaves on a wall cell (its f and g never change after
+// Init): the set-up values before the first MacroProp, then the sums of
+// its initial populations, with u = u_set + F / (2 rho) for the force of the
+// previous MacroProp (the set-up one at MacroProp 1, the refreshed one
+// later); q = sum g c = 0 (Init puts the walls' g at rest).
+struct E3Wall {
+    long long cell;
+    double rho0, rhom, T0, Tm;
+    double u[3][3];  // after 0, 1, >= 2 MacroProps
+};
+
 lbm_status fail3(lbm_status s, const std::string &m) {
     lbm_set_last_error(m);
     return s;
@@ -336,6 +347,7 @@ struct lbm_energy3d {
     cudaStream_t s = nullptr;
     cudaEvent_t ev[2] = {nullptr, nullptr};
     std::vector<void *> allocs;
+    std::vector<E3Wall> walls;
 };
 
 namespace {
@@ -366,7 +378,7 @@ int phase_of(long long steps) { return steps <= 1 ? 0 : (steps == 2 ? 1 : 2); }
 // wall cell, lbm.cpp:284).
 lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, double gbeta, double T_star,
                          bool buoy, const std::vector<double> &rho, const std::vector<double> &F,
-                         std::vector<int> &rec_of, std::vector<E3Rec> &recs) {
+                         std::vector<int> &rec_of, std::vector<E3Rec> &recs, std::vector<E3Wall> &walls) {
     const long long N = (long long)NX * NY * NZ;
     auto idx = [&](int i, int j, int k) { return (long long)i + (long long)NX * (j + (long long)NY * k); };
     auto nb = [&](long long c, int l) {
@@ -421,6 +433,18 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
             out[a] = v;
         }
     };
+    walls.clear();
+    for (long long c = 0; c < N; c++) {
+        if (!solid(c)) continue;
+        E3Wall W;
+        W.cell = c;
+        W.rho0 = rho[c];
+        W.rhom = rho_w[c];
+        W.T0 = su.T[c];
+        W.Tm = Twall[c];
+        for (int ph = 0; ph < 3; ph++) wall_u(c, ph, W.u[ph]);
+        walls.push_back(W);
+    }
     rec_of.assign(N, -2);
     recs.clear();
     for (long long c = 0; c < N; c++) {
@@ -584,11 +608,13 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
     for (long long c = 0; c < 3 * N && !forced; c++) forced = su->type[c % N] == kTypeF && F[c] != 0.0;
     std::vector<int> rec_of;
     std::vector<E3Rec> recs;
+    std::vector<E3Wall> walls;
     const bool buoy = su->g_beta != 0.0;
-    lbm_status st = build_records(*su, NX, NY, NZ, su->g_beta, su->T_star, buoy, rho, F, rec_of, recs);
+    lbm_status st = build_records(*su, NX, NY, NZ, su->g_beta, su->T_star, buoy, rho, F, rec_of, recs, walls);
     if (st != LBM_OK) return st;
 
     lbm_energy3d *e = new lbm_energy3d();
+    e->walls.swap(walls);
     e->nx = su->nx;
     e->ny = su->ny;
     e->nz = su->nz;
@@ -709,6 +735,19 @@ extern "C" lbm_status lbmgpu_energy3d_download(lbm_energy3d *e, int field, doubl
     CK3(cudaMemcpyAsync(buf.data(), e->mom + (long long)field * N, N * sizeof(float), cudaMemcpyDeviceToHost, e->s));
     CK3(cudaStreamSynchronize(e->s));
     for (long long c = 0; c < N; c++) host[c] = buf[c];
+    const int ph = e->steps < 2 ? (int)e->steps : 2;
+    for (const E3Wall &W : e->walls) {
+        double v = 0.0;
+        switch (field) {
+        case LBM_FIELD_RHO: v = e->steps ? W.rhom : W.rho0; break;
+        case LBM_FIELD_UX: v = W.u[ph][0]; break;
+        case LBM_FIELD_UY: v = W.u[ph][1]; break;
+        case LBM_FIELD_UZ: v = W.u[ph][2]; break;
+        case LBM_FIELD_T: v = e->steps ? W.Tm : W.T0; break;
+        default: v = 0.0; break;
+        }
+        host[W.cell] = v;
+    }
     return LBM_OK;
 }
 

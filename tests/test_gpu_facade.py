@@ -207,3 +207,42 @@ def test_dropin_cylinder2d_outputs(drivers, pkg, tmp_path):
         assert np.allclose(r[:, 0], (np.arange(steps) + 1) * 0.1 / 10.0, rtol=1e-5)
         scale = np.abs(c["cd"]).max()
         assert np.abs(r[:, 1] - c[coef]).max() / scale < 1e-5
+
+
+def test_dropin_rayleigh_benard_loop(drivers, tmp_path):
+    """The reference's Rayleigh_Benard build (-DENERGY on D3Q19):
+    main_setup_RayleighBenard1 and the main loop with Find_Maximum_uy and
+    Find_Nusselt_number every step (main.cpp:308-321) through the facade,
+    which hands the set-up to lbm_energy3d; every cell, ghosts included,
+    against the reference's own run (FP32: T within 1e-5 of the spread, u
+    within 1e-4 of its largest value), and the last step's maximum |uy| and
+    Nusselt number against the same formulas on the reference's fields."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "rayleigh32x16x5_400.npz"))
+    nx, ny, nz, steps = int(g["nx"]), int(g["ny"]), int(g["nz"]), int(g["steps"])
+    out = str(tmp_path / "rb.bin")
+    subprocess.check_call([drivers["dropin_rayleigh"], str(nx), str(ny), str(nz), str(steps), out],
+                          cwd=str(tmp_path))
+    shape = (nz + 2, ny + 2, nx + 2)
+    n = int(np.prod(shape))
+    raw = np.fromfile(out, dtype=np.float64)
+    a = raw[:8 * n].reshape((8,) + shape)
+    uy_max, nus = raw[8 * n:8 * n + steps], raw[8 * n + steps:]
+    assert uy_max.shape == (steps,) and nus.shape == (steps,)
+    T = g["T"]
+    assert np.abs(a[4] - T).max() < 1e-5 * (T.max() - T.min())
+    us = np.abs(g["u"]).max()
+    assert np.abs(a[1:4] - g["u"]).max() < 1e-4 * us
+    assert np.abs(a[0] - g["rho"]).max() < 1e-6
+    assert np.abs(a[5:8] - g["q"]).max() < 1e-4 * np.abs(g["q"]).max()
+    # Find_Maximum_uy: every cell, ghosts included (lbm.cpp:3522-3536)
+    assert abs(uy_max[-1] - np.abs(g["u"][1]).max()) < 1e-4 * np.abs(g["u"][1]).max()
+    # Find_Nusselt_number (lbm.cpp:3538-3561) on the reference's fields
+    cs2, Pr, Ra, gb = 1.0 / 3.0, 0.71, 1710.0, 1e-5
+    nu = np.sqrt(gb * 1.0 * (nz + 1) ** 3 * Pr / Ra)
+    alpha = nu / Pr
+    fl = np.zeros(shape, bool)
+    fl[1:-1, 1:-1, 1:-1] = True
+    nu_ref = 1 + (g["u"][1][fl] * T[fl]).mean() / (alpha * 1.0 / (ny + 1))
+    assert abs(nus[-1] - nu_ref) < 1e-4 * abs(nu_ref - 1.0), (nus[-1], nu_ref)
