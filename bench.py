@@ -425,6 +425,64 @@ def run_tandem2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 6.0):
             "speedup_vs_cpu_port": gpu / cpu}
 
 
+def rayleigh_setup(nx: int, ny: int, nz: int):
+    """main_setup_RayleighBenard1 (lbm.cpp:1585-1643) with the constants of
+    LBM.h:222-242 as ghost-inclusive arrays (z, y, x): Neumann x and z walls,
+    Dirichlet y walls (Tt at j = 0, Tb at j = Ny + 1), the fluid at rest at
+    Tt with F_y = g beta (T - T*)."""
+    cs2, Tb, dT, Ra, gb, Pr = 1.0 / 3.0, 2.0, 1.0, 1710.0, 1e-5, 0.71
+    Tt = Tb - dT
+    nu = np.sqrt(gb * dT * float((nz + 1) ** 3) * Pr / Ra)
+    tau = 0.5 + nu / cs2
+    alpha = nu / Pr
+    tau_g = 0.5 + alpha / cs2
+    cp = cs2 * tau_g / alpha
+    T_star = (Tb + Tt) / 2
+    shape = (nz + 2, ny + 2, nx + 2)
+    t = np.zeros(shape, np.uint8)
+    te = np.zeros(shape, np.uint8)
+    T = np.full(shape, Tt)
+    for sl in ((0,), (-1,), (slice(None), slice(None), 0), (slice(None), slice(None), -1)):
+        t[sl] = 1
+        te[sl] = 7
+    t[:, 0, :] = t[:, -1, :] = 1
+    te[:, 0, :] = te[:, -1, :] = 6
+    T[:, -1, :] = Tb
+    F = np.zeros((3,) + shape)
+    F[1][t == 0] = gb * (Tt - T_star)
+    return t, te, T, F, dict(tau=tau, tau_g=tau_g, cp=cp, g_beta=gb, T_star=T_star, alpha=alpha)
+
+
+def run_energy3d(pkg):
+    """The reference's Rayleigh_Benard case (D3Q19 ENERGY) through
+    lbm_energy3d: at its own size (200 x 50 x 5, launch-bound: two launches
+    a step) and on a 384 x 192 x 96 box of the same set-up for the HBM
+    roofline.  k_e3_step reads f, g (19 FP32 each), two float4 of history
+    and the record index and writes f, g and the history: 372 B per cell
+    of the ghost-inclusive grid."""
+    out = {}
+    for name, (nx, ny, nz), steps in (("own_size", (200, 50, 5), 2000), ("large", (384, 192, 96), 60)):
+        t, te, T, F, c = rayleigh_setup(nx, ny, nz)
+        s = pkg.Energy3D(t, te, T, c["tau"], c["tau_g"], c["cp"], g_beta=c["g_beta"], T_star=c["T_star"], F=F)
+        s.step(5)
+        ms = s.step_timed(steps)
+        st = s.status()
+        uy = s.download("uy")
+        s.close()
+        interior = nx * ny * nz
+        grid = t.size
+        achieved = 372.0 * grid * steps / (ms * 1e-3) / 1e9
+        peak, peak_kind = measured_peak()
+        out[name] = {"workload": "Rayleigh-Benard %dx%dx%d (D3Q19 ENERGY, Neumann x/z and Dirichlet y walls, "
+                                 "buoyancy), FP32 f and g" % (nx, ny, nz),
+                     "value": interior * steps / (ms * 1e-3) / 1e6, "unit": "MLUPS", "ms_per_lbm_step": ms / steps,
+                     "steps_timed": steps, "status": int(st), "max_abs_uy": float(np.nanmax(np.abs(uy))),
+                     "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                  "frac": achieved / peak, "peak_kind": peak_kind, "bytes_per_cell": 372,
+                                  "note": "eager steps: k_e3_walls + k_e3_step per step"}}
+    return out
+
+
 def run_energy2d(pkg, steps: int = 2000, nx: int = 2046, ny: int = 1024):
     """The reference's ENERGY model on a wide Couette channel (its
     main_setup_Couette geometry, periodic x, Dirichlet walls, the top one
@@ -753,6 +811,7 @@ def main():
         line["d2q9_cylinder"] = run_cylinder2d(ge.load_package(), orc)
         line["d2q9_tandem"] = run_tandem2d(ge.load_package(), orc)
         line["d2q9_energy"] = run_energy2d(ge.load_package())
+        line["d3q19_energy_rayleigh"] = run_energy3d(ge.load_package())
     if not args.no_cpu_baseline:
         cb = cpu_baseline_sample()
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores", "kind", "sample")}

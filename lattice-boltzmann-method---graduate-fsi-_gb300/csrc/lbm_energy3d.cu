@@ -21,8 +21,9 @@
 // wall velocity of each phase, and for each solid neighbour the cell whose
 // Neumann write it sees (or none, then the wall's own T).  Per step a
 // pre-pass (k_e3_walls) forms the Neumann cells' T_w; the step kernel
-// (k_e3_step) pulls, applies the wall rules, takes the moments, refreshes
-// the force and collides.
+// (k_e3_bulk for the other fluid cells, k_e3_rec for the records) pulls,
+// applies the wall rules, takes the moments, refreshes the force and
+// collides.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -42,36 +43,64 @@ using namespace lbmk;
 constexpr int kSlots = 18;       // solid neighbours a cell can have
 constexpr int kTypeF = 0, kTypeS = 1, kTypeT = 6, kTypeQ = 7;
 constexpr int kBlock = 256;
+constexpr int kRecBlock = 64;  // the record kernels: latency-bound, spread over every SM
 
 // A fluid cell with at least one solid neighbour.  Links are indexed by the
 // pulled direction p (source c - c_p); the reference's push direction of
-// that wall link is opp(p).
+// that wall link is opp(p).  Its Dirichlet links' wall T is the mean over
+// its solid neighbours: the ones no Neumann write reaches are summed once
+// (ssum); the others ("dynamic") are listed with the record whose write the
+// cell sees and the push index of the cell's own write.
 struct E3Rec {
     int cell;
+    int i, j, k;             // its coordinates
     uint32_t bb;             // links whose source is solid
     uint32_t dir, neu, adi;  // ... of type_Energy TYPE_T, TYPE_Q, any other
-    int nsol;                // solid neighbours
+    int ndyn;                // dynamic solid neighbours
+    float inv_nsol;          // 1 / solid neighbours
+    float ssum[2];           // T of the other solid neighbours: set-up (streaming 1), MacroProp's (later)
     float uw[3][3];          // Determine_Wall_Velocity at streaming 1, 2, and from 3 on
-    int writer[kSlots];      // record whose Neumann push last wrote the slot's T before this cell; -1 none
-    float tsol[2][kSlots];   // the slot's own T: set-up (streaming 1), MacroProp's (later)
-    uint8_t own[kSlots];     // push index at which this cell itself writes the slot's T; 255 never
+    int dwriter[kSlots];     // record whose Neumann push last wrote its T before this cell; -1 none
+    float dt[2][kSlots];     // its own T, as ssum
+    uint8_t down[kSlots];    // push index at which this cell itself writes its T; 255 never
 };
+
+// The solid neighbours of a record while the host builds it.
+struct E3Slots {
+    int nsol = 0;
+    long long cell[kSlots];
+    int writer[kSlots];
+    float tsol[2][kSlots];
+    uint8_t own[kSlots];
+};
+
+// rec_of: a record index, or one of these
+constexpr int kSolid = -2, kBulk = -1, kBulkWrap = -3;
 
 struct E3Params {
     int NX, NY, NZ;
     long long N, S;
+    int offs[Q];  // source of link l: c - offs[l] away from the grid's faces
     int nrec;
     float omega, inv_tau_g, tg_fac, inv_cp, two_nu, s_fac, T_ref;
     float gbeta, T_star;
     int buoy, forced;
 };
 
-__device__ __forceinline__ long long wrap_src(int i, int j, int k, int l, const E3Params &P) {
-    int a = i - cx(l), b = j - cy(l), c = k - cz(l);
+// The source c - c_l of cell (i, j, k) under the reference's periodic
+// modulo over the whole grid (lbm.cpp:252-255); its coordinates in a, b, d.
+__device__ __forceinline__ int wrap_src(int i, int j, int k, int l, const E3Params &P, int &a, int &b, int &d) {
+    a = i - cx(l);
+    b = j - cy(l);
+    d = k - cz(l);
     a += a < 0 ? P.NX : (a >= P.NX ? -P.NX : 0);
     b += b < 0 ? P.NY : (b >= P.NY ? -P.NY : 0);
-    c += c < 0 ? P.NZ : (c >= P.NZ ? -P.NZ : 0);
-    return a + (long long)P.NX * (b + (long long)P.NY * c);
+    d += d < 0 ? P.NZ : (d >= P.NZ ? -P.NZ : 0);
+    return a + P.NX * (b + P.NY * d);
+}
+__device__ __forceinline__ int wrap_src(int i, int j, int k, int l, const E3Params &P) {
+    int a, b, d;
+    return wrap_src(i, j, k, l, P, a, b, d);
 }
 
 // 1 + 3x + 4.5x^2 - 1.5uu (+ 4.5x(x^2 - uu) for the cubic form), x = c.u
@@ -86,7 +115,7 @@ __device__ __forceinline__ float p3m1(float x, float uu) { return p2m1(x, uu) + 
 // at T = 1 of the cell's density (previous MacroProp) and the wall velocity.
 // With j.n = 0 (LBM.h's j_dot_n): T_w = -sum_other g c.n / sum_wall geq c.n.
 // keep: store this sweep's pulled values for the next sweep.
-__global__ void __launch_bounds__(kBlock) k_e3_walls(const float *__restrict__ GA, const float4 *__restrict__ aux,
+__global__ void __launch_bounds__(kRecBlock) k_e3_walls(const float *__restrict__ GA, const float4 *__restrict__ aux,
                                                      const E3Rec *__restrict__ recs, float *__restrict__ gold,
                                                      float *__restrict__ tw, const __grid_constant__ E3Params P,
                                                      int phase, int keep) {
@@ -94,8 +123,7 @@ __global__ void __launch_bounds__(kBlock) k_e3_walls(const float *__restrict__ G
     if (r >= P.nrec) return;
     const E3Rec &R = recs[r];
     if (!R.neu) return;
-    const int c = R.cell;
-    const int i = c % P.NX, j = (c / P.NX) % P.NY, k = c / (P.NX * P.NY);
+    const int c = R.cell, i = R.i, j = R.j, k = R.k;
     float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
     int np = 0;
 #pragma unroll
@@ -112,6 +140,19 @@ __global__ void __launch_bounds__(kBlock) k_e3_walls(const float *__restrict__ G
     n2 *= inv_np;
     const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
     const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+    // every load first (the kept values are rewritten below)
+    float v[Q];
+    uint32_t fresh = 0u;
+#pragma unroll
+    for (int p = 0; p < Q; p++) {
+        if ((R.bb >> p) & 1u) continue;
+        int si, sj, sk;
+        const int s = wrap_src(i, j, k, p, P, si, sj, sk);
+        const bool fr = p == 0 || si < i || (si == i && (sj < j || (sj == j && sk < k)));
+        v[p] = fr ? GA[p * P.S + s] : gold[(long long)p * P.nrec + r];
+        if (fr) fresh |= 1u << p;
+    }
+    const float rho = 1.0f + aux[c].x;
     float other = 0.0f, wall = 0.0f;
 #pragma unroll
     for (int p = 0; p < Q; p++) {
@@ -120,102 +161,34 @@ __global__ void __launch_bounds__(kBlock) k_e3_walls(const float *__restrict__ G
             const float x = cx(p) * u0 + cy(p) * u1 + cz(p) * u2;
             wall += wf(p) * (1.0f + p3m1(x, uu)) * cn;
         } else {
-            const long long s = wrap_src(i, j, k, p, P);
-            const float v = GA[p * P.S + s];
-            const int si = (int)(s % P.NX), sj = (int)((s / P.NX) % P.NY), sk = (int)(s / ((long long)P.NX * P.NY));
-            const bool fresh = p == 0 || si < i || (si == i && (sj < j || (sj == j && sk < k)));
-            float *kept = gold + (long long)p * P.nrec + r;
-            other += ((fresh ? v : *kept) + wf(p) * P.T_ref) * cn;
-            if (keep) *kept = v;
+            other += (v[p] + wf(p) * P.T_ref) * cn;
         }
     }
-    const float rho = 1.0f + aux[c].x;
     tw[r] = -other / (rho * wall);
+    if (!keep) return;
+    // this sweep's pulled values for the next sweep's stale links
+#pragma unroll
+    for (int p = 0; p < Q; p++) {
+        if (((R.bb | fresh) >> p) & 1u) continue;
+        gold[(long long)p * P.nrec + r] = GA[p * P.S + wrap_src(i, j, k, p, P)];
+    }
 }
 
-// One step of f and g over the whole grid (solid cells idle).  gather = 0:
-// the first collision, on the set-up state (no streaming before it).
-// aux[c] = (rho - 1, u) of the last MacroProp (the previous collision's);
-// aux2[c] = (Phi of the previous collision, the force of the last
-// MacroProp).  MacroProp (lbm.cpp:657-806): u = (j + F/2) / rho with the
-// force of the previous MacroProp, T = sum g, q = sum g c, then
-// F_y = g beta (T - T*) when the buoyancy is on.  ConvLBM (lbm.cpp:91-177):
+// MacroProp and the collision of one fluid cell whose pulled populations
+// are f and g (lbm.cpp:657-806, 91-177).  gather = 0: the first collision,
+// on the set-up state (no streaming before it).  aux[c] = (rho - 1, u) of
+// the last MacroProp (the previous collision's); aux2[c] = (Phi of the
+// previous collision, the force of the last MacroProp).  MacroProp:
+// u = (j + F/2) / rho with the force of the previous MacroProp, T = sum g,
+// q = sum g c, then F_y = g beta (T - T*) when the buoyancy is on.  ConvLBM:
 // f by BGK + Guo with that force; g by BGK with the viscous-heating source
 // F_l = w Phi / cp (1 + c.u (tau_g - 1/2) / (cs2 tau_g)) and half its change
 // since the previous collision.
-__global__ void __launch_bounds__(kBlock) k_e3_step(const float *__restrict__ A, float *__restrict__ B,
-                                                    const float *__restrict__ GA, float *__restrict__ GB,
-                                                    float4 *__restrict__ aux, float4 *__restrict__ aux2,
-                                                    const int *__restrict__ rec_of, const E3Rec *__restrict__ recs,
-                                                    float *__restrict__ gold, const float *__restrict__ tw,
-                                                    const __grid_constant__ E3Params P, uint32_t *__restrict__ status,
-                                                    float *__restrict__ mom, int gather, int phase, int export_only) {
-    const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (c >= P.N) return;
-    const int ro = rec_of[c];
-    if (ro == -2) return;  // solid
-    const int i = (int)(c % P.NX), j = (int)((c / P.NX) % P.NY), k = (int)(c / ((long long)P.NX * P.NY));
-    const float4 h1 = aux[c], h2 = aux2[c];
-    const float drho_p = h1.x;
-    float f[Q], g[Q];
-    if (!gather) {
-#pragma unroll
-        for (int l = 0; l < Q; l++) {
-            f[l] = A[l * P.S + c];
-            g[l] = GA[l * P.S + c];
-        }
-        if (ro >= 0 && !export_only) {
-#pragma unroll
-            for (int l = 0; l < Q; l++) gold[(long long)l * P.nrec + ro] = g[l];
-        }
-    } else if (ro < 0) {
-#pragma unroll
-        for (int l = 0; l < Q; l++) {
-            const long long s = wrap_src(i, j, k, l, P);
-            f[l] = A[l * P.S + s];
-            g[l] = GA[l * P.S + s];
-        }
-    } else {
-        const E3Rec &R = recs[ro];
-        const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
-        const float uu = u0 * u0 + u1 * u1 + u2 * u2;
-        const float rho_p = 1.0f + drho_p;
-        const float tw_own = R.neu ? tw[ro] : 0.0f;
-        const float inv_nsol = 1.0f / (float)R.nsol;
-#pragma unroll
-        for (int p = 0; p < Q; p++) {
-            if (!((R.bb >> p) & 1u)) {
-                const long long s = wrap_src(i, j, k, p, P);
-                f[p] = A[p * P.S + s];
-                g[p] = GA[p * P.S + s];
-                continue;
-            }
-            const int q = opp(p);  // the reference's push direction, towards the wall
-            const float x = cx(q) * u0 + cy(q) * u1 + cz(q) * u2;
-            // f_opp(q) = f*_q - 2 w (u_w . c_q) / cs2 (lbm.cpp:273-274)
-            f[p] = A[q * P.S + c] - 6.0f * wf(q) * x;
-            if ((R.dir >> p) & 1u) {
-                // Determine_Wall_Temperature at this point of the push: the
-                // mean T of the solid neighbours as the sweep has left them
-                float Tsum = 0.0f;
-                for (int m = 0; m < R.nsol; m++) {
-                    float v;
-                    if (R.own[m] < q) v = tw_own;
-                    else if (R.writer[m] >= 0) v = tw[R.writer[m]];
-                    else v = R.tsol[phase == 0 ? 0 : 1][m];
-                    Tsum += v;
-                }
-                const float Tw = Tsum * inv_nsol;
-                // -g*_q + 2 geq_q(rho, T_w, u_w) (lbm.cpp:277-280)
-                g[p] = 2.0f * wf(q) * (rho_p * Tw * (1.0f + p3m1(x, uu)) - P.T_ref) - GA[q * P.S + c];
-            } else if ((R.neu >> p) & 1u) {
-                // w rho T_w times the second-order shape of the wall (lbm.cpp:281-288)
-                g[p] = wf(q) * (rho_p * tw_own * (1.0f + p2m1(x, uu)) - P.T_ref);
-            } else {
-                g[p] = gold[(long long)p * P.nrec + ro];  // never written: the initial value
-            }
-        }
-    }
+__device__ __forceinline__ void macro_collide(int c, float f[Q], float g[Q], float4 h1, float4 h2,
+                                              const E3Params &P, float *__restrict__ B, float *__restrict__ GB,
+                                              float4 *__restrict__ aux, float4 *__restrict__ aux2,
+                                              uint32_t *__restrict__ status, float *__restrict__ mom, int gather,
+                                              int export_only) {
     float drho, jx, jy, jz;
     moments_pairs(f, drho, jx, jy, jz);
     float dT = 0.0f, qx = 0.0f, qy = 0.0f, qz = 0.0f;
@@ -292,6 +265,127 @@ __global__ void __launch_bounds__(kBlock) k_e3_step(const float *__restrict__ A,
     }
 }
 
+// The fluid cells without a solid neighbour (solid cells and wall records
+// idle): a plain pull, offsets away from the grid's faces, the reference's
+// periodic modulo on them.
+__global__ void __launch_bounds__(kBlock) k_e3_bulk(const float *__restrict__ A, float *__restrict__ B,
+                                                    const float *__restrict__ GA, float *__restrict__ GB,
+                                                    float4 *__restrict__ aux, float4 *__restrict__ aux2,
+                                                    const int *__restrict__ rec_of, const __grid_constant__ E3Params P,
+                                                    uint32_t *__restrict__ status, float *__restrict__ mom,
+                                                    int gather, int export_only) {
+    const int c = blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= P.N) return;
+    const int ro = rec_of[c];
+    if (ro != kBulk && ro != kBulkWrap) return;
+    const float4 h1 = aux[c], h2 = aux2[c];
+    float f[Q], g[Q];
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            f[l] = A[l * P.S + c];
+            g[l] = GA[l * P.S + c];
+        }
+    } else if (ro == kBulk) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            const int s = c - P.offs[l];
+            f[l] = A[l * P.S + s];
+            g[l] = GA[l * P.S + s];
+        }
+    } else {
+        const int i = c % P.NX, j = (c / P.NX) % P.NY, k = c / (P.NX * P.NY);
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            const int s = wrap_src(i, j, k, l, P);
+            f[l] = A[l * P.S + s];
+            g[l] = GA[l * P.S + s];
+        }
+    }
+    macro_collide(c, f, g, h1, h2, P, B, GB, aux, aux2, status, mom, gather, export_only);
+}
+
+// The wall records, one thread each: the pull with the reference's wall
+// rules (lbm.cpp:266-288).  f: bounce-back with Determine_Wall_Velocity;
+// g: Dirichlet anti-bounce-back at Determine_Wall_Temperature's T as the
+// sweep has left the solid neighbours, Neumann the equilibrium of the
+// pre-pass's T_w, adiabatic the kept initial value.
+__global__ void __launch_bounds__(kRecBlock) k_e3_rec(const float *__restrict__ A, float *__restrict__ B,
+                                                   const float *__restrict__ GA, float *__restrict__ GB,
+                                                   float4 *__restrict__ aux, float4 *__restrict__ aux2,
+                                                   const E3Rec *__restrict__ recs, float *__restrict__ gold,
+                                                   const float *__restrict__ tw, const __grid_constant__ E3Params P,
+                                                   uint32_t *__restrict__ status, float *__restrict__ mom, int gather,
+                                                   int phase, int export_only) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.nrec) return;
+    const E3Rec &R = recs[r];
+    const int c = R.cell;
+    const float4 h1 = aux[c], h2 = aux2[c];
+    float f[Q], g[Q];
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            f[l] = A[l * P.S + c];
+            g[l] = GA[l * P.S + c];
+        }
+        if (!export_only) {
+#pragma unroll
+            for (int l = 0; l < Q; l++) gold[(long long)l * P.nrec + r] = g[l];
+        }
+    } else {
+        const int i = R.i, j = R.j, k = R.k;
+        const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
+        const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+        const float rho_p = 1.0f + h1.x;
+        const float tw_own = R.neu ? tw[r] : 0.0f;
+        const int ph = phase == 0 ? 0 : 1;
+        // the dynamic solid neighbours' T as this cell's push starts: the
+        // last Neumann write before the cell, or the wall's own T
+        float vd[kSlots];
+        float vsum = R.ssum[ph];
+        const int ndyn = R.ndyn;
+#pragma unroll 6
+        for (int m = 0; m < ndyn; m++) {
+            const int w = R.dwriter[m];
+            vd[m] = w >= 0 ? tw[w] : R.dt[ph][m];
+        }
+#pragma unroll 1
+        for (int m = 0; m < ndyn; m++) vsum += vd[m];
+#pragma unroll
+        for (int p = 0; p < Q; p++) {
+            if (!((R.bb >> p) & 1u)) {
+                const int s = wrap_src(i, j, k, p, P);
+                f[p] = A[p * P.S + s];
+                g[p] = GA[p * P.S + s];
+                continue;
+            }
+            const int q = opp(p);  // the reference's push direction, towards the wall
+            const float x = cx(q) * u0 + cy(q) * u1 + cz(q) * u2;
+            // f_opp(q) = f*_q - 2 w (u_w . c_q) / cs2 (lbm.cpp:273-274)
+            f[p] = A[q * P.S + c] - 6.0f * wf(q) * x;
+            if ((R.dir >> p) & 1u) {
+                // Determine_Wall_Temperature at this point of the push: the
+                // neighbours this cell's own Neumann links wrote earlier in
+                // its push hold its T_w
+                float Tsum = vsum;
+#pragma unroll 1
+                for (int m = 0; m < ndyn; m++)
+                    if (R.down[m] < q) Tsum += tw_own - vd[m];
+                const float Tw = Tsum * R.inv_nsol;
+                // -g*_q + 2 geq_q(rho, T_w, u_w) (lbm.cpp:277-280)
+                g[p] = 2.0f * wf(q) * (rho_p * Tw * (1.0f + p3m1(x, uu)) - P.T_ref) - GA[q * P.S + c];
+            } else if ((R.neu >> p) & 1u) {
+                // w rho T_w times the second-order shape of the wall (lbm.cpp:281-288)
+                g[p] = wf(q) * (rho_p * tw_own * (1.0f + p2m1(x, uu)) - P.T_ref);
+            } else {
+                g[p] = gold[(long long)p * P.nrec + r];  // never written: the initial value
+            }
+        }
+    }
+    macro_collide(c, f, g, h1, h2, P, B, GB, aux, aux2, status, mom, gather, export_only);
+}
+
 // LBM::Init (lbm.cpp:31-57) on the fluid cells: f = feq(rho, u), g =
 // rho w T P3(u) (Calc_geq, lbm.cpp:636-653), shifted; aux = (rho - 1, u),
 // aux2 = (0, F).  fields: [8][N] rho, u, T, F of the set-up.
@@ -299,7 +393,7 @@ __global__ void k_e3_init(float *__restrict__ A, float *__restrict__ GA, float4 
                           float4 *__restrict__ aux2, const int *__restrict__ rec_of, const float *__restrict__ fields,
                           const __grid_constant__ E3Params P) {
     const long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-    if (c >= P.N || rec_of[c] == -2) return;
+    if (c >= P.N || rec_of[c] == kSolid) return;
     const float rho = fields[c], ux = fields[P.N + c], uy = fields[2 * P.N + c], uz = fields[3 * P.N + c];
     const float T = fields[4 * P.N + c];
     const float usq = ux * ux + uy * uy + uz * uz;
@@ -445,22 +539,29 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
         for (int ph = 0; ph < 3; ph++) wall_u(c, ph, W.u[ph]);
         walls.push_back(W);
     }
-    rec_of.assign(N, -2);
+    rec_of.assign(N, kSolid);
     recs.clear();
+    std::vector<E3Slots> slots;
     for (long long c = 0; c < N; c++) {
         if (su.type[c] != kTypeF) continue;
         bool any = false;
         for (int l = 1; l < Q && !any; l++) any = solid(nb(c, l));
         if (!any) {
-            rec_of[c] = -1;
+            const int i = (int)(c % NX), j = (int)((c / NX) % NY), k = (int)(c / ((long long)NX * NY));
+            const bool face = i == 0 || i == NX - 1 || j == 0 || j == NY - 1 || k == 0 || k == NZ - 1;
+            rec_of[c] = face ? kBulkWrap : kBulk;
             continue;
         }
         E3Rec R;
         memset(&R, 0, sizeof(R));
         R.cell = (int)c;
+        R.i = (int)(c % NX);
+        R.j = (int)((c / NX) % NY);
+        R.k = (int)(c / ((long long)NX * NY));
+        E3Slots L;
         for (int m = 0; m < kSlots; m++) {
-            R.writer[m] = -1;
-            R.own[m] = 255;
+            L.writer[m] = -1;
+            L.own[m] = 255;
         }
         for (int ph = 0; ph < 3; ph++) {
             double s[3] = {0, 0, 0};
@@ -489,12 +590,14 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
             if (!(std::isfinite(Twall[w])))
                 return fail3(LBM_ERR_UNSUPPORTED, "energy3d_create: a wall cell next to fluid has no solid "
                                                   "neighbour (Determine_Wall_Temperature divides by zero)");
-            R.tsol[0][R.nsol] = (float)su.T[w];
-            R.tsol[1][R.nsol] = (float)Twall[w];
-            R.nsol++;
+            L.cell[L.nsol] = w;
+            L.tsol[0][L.nsol] = (float)su.T[w];
+            L.tsol[1][L.nsol] = (float)Twall[w];
+            L.nsol++;
         }
         rec_of[c] = (int)recs.size();
         recs.push_back(R);
+        slots.push_back(L);
     }
     // the push order, replayed: last_writer[w] = record of the last
     // Neumann write of solid w so far
@@ -505,15 +608,9 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
                 const long long c = idx(i, j, k);
                 const int r = rec_of[c];
                 if (r < 0) continue;
-                E3Rec &R = recs[r];
-                // the slots in push-direction order, as built above
-                long long slot_cell[kSlots];
-                int m = 0;
-                for (int l = 0; l < Q; l++) {
-                    const long long w = nb(c, l);
-                    if (solid(w)) slot_cell[m++] = w;
-                }
-                for (m = 0; m < R.nsol; m++) R.writer[m] = last_writer[slot_cell[m]];
+                const E3Rec &R = recs[r];
+                E3Slots &L = slots[r];
+                for (int m = 0; m < L.nsol; m++) L.writer[m] = last_writer[L.cell[m]];
                 if (!R.neu) continue;
                 // this cell's writes: at its first Neumann link the cell
                 // opposite the normal (when the normal is a lattice
@@ -545,13 +642,34 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
                     first = false;
                     for (long long t : targets) {
                         if (t < 0) continue;
-                        for (int s = 0; s < R.nsol; s++)
-                            if (slot_cell[s] == t && R.own[s] == 255) R.own[s] = (uint8_t)l;
+                        for (int s = 0; s < L.nsol; s++)
+                            if (L.cell[s] == t && L.own[s] == 255) L.own[s] = (uint8_t)l;
                         written.push_back(t);
                     }
                 }
                 for (long long t : written) last_writer[t] = r;
             }
+    // the compact form: static neighbours summed, dynamic ones listed
+    for (size_t r = 0; r < recs.size(); r++) {
+        E3Rec &R = recs[r];
+        const E3Slots &L = slots[r];
+        R.inv_nsol = 1.0f / (float)L.nsol;
+        double s0 = 0.0, s1 = 0.0;
+        for (int m = 0; m < L.nsol; m++) {
+            if (L.writer[m] < 0 && L.own[m] == 255) {
+                s0 += L.tsol[0][m];
+                s1 += L.tsol[1][m];
+                continue;
+            }
+            const int d = R.ndyn++;
+            R.dwriter[d] = L.writer[m];
+            R.down[d] = L.own[m];
+            R.dt[0][d] = L.tsol[0][m];
+            R.dt[1][d] = L.tsol[1][m];
+        }
+        R.ssum[0] = (float)s0;
+        R.ssum[1] = (float)s1;
+    }
     return LBM_OK;
 }
 
@@ -566,14 +684,19 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
     const int gather = e->steps > 0 ? 1 : 0;
     const int phase = phase_of(e->steps);
     if (gather && e->has_neu) {
-        const unsigned nb = (unsigned)((P.nrec + kBlock - 1) / kBlock);
-        k_e3_walls<<<nb, kBlock, 0, e->s>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
+        const unsigned nb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
+        k_e3_walls<<<nb, kRecBlock, 0, e->s>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
                                            export_only ? 0 : 1);
     }
     const unsigned blocks = (unsigned)((P.N + kBlock - 1) / kBlock);
-    k_e3_step<<<blocks, kBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
-                                          e->aux2, e->rec_of, e->recs, e->gold, e->tw, P, e->status, mom, gather,
-                                          phase, export_only);
+    k_e3_bulk<<<blocks, kBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
+                                          e->aux2, e->rec_of, P, e->status, mom, gather, export_only);
+    if (P.nrec) {
+        const unsigned rb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
+        k_e3_rec<<<rb, kRecBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
+                                         e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather, phase,
+                                         export_only);
+    }
     return cudaGetLastError();
 }
 
@@ -625,6 +748,7 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
     P.N = N;
     P.S = ((N + 255) / 256) * 256;
     P.nrec = (int)recs.size();
+    for (int l = 0; l < Q; l++) P.offs[l] = cx(l) + NX * (cy(l) + NY * cz(l));
     const double cs2 = 1.0 / 3.0, tg = su->tau_g;
     P.omega = (float)(1.0 / su->tau);
     P.inv_tau_g = (float)(1.0 / tg);
