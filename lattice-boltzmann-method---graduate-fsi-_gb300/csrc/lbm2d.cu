@@ -995,6 +995,9 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
             for (int k = 0; k < kFastNodes; k++) {
                 if (nq[k] < 0) continue;
                 float sx = 0.0f, sy = 0.0f;
+                // unrolled: the list entries' loads overlap (the sum keeps
+                // its ascending marker order)
+#pragma unroll 4
                 for (int i = la[k]; i < la[k] + lc[k]; i++) {
                     const int2 e = lst[i];
                     const float2 f = fsp[e.x];
