@@ -583,9 +583,9 @@ constexpr int kFastNodes = 4;
 // Shared-memory words of the register-resident pass: u at the box nodes
 // (2 nb), the marker forces (2 n), the stencils as (node, weight) pairs
 // (32 n), the spreading lists as (marker, weight) pairs (32 n), the marker
-// densities (n).
+// densities (n), the box nodes with a spreading list (nb).
 __host__ __device__ inline size_t ibm2d_fast_smem_bytes(long long nb, int n) {
-    return (size_t)4 * (2 * (size_t)nb + 67 * (size_t)n);
+    return (size_t)4 * (3 * (size_t)nb + 67 * (size_t)n);
 }
 
 // 4-point Peskin delta (lbm.cpp:1095-1102).
@@ -907,25 +907,38 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     const float sgn = ib.lit_sign ? -1.0f : 1.0f;
     double drag, lift;
     if (ib.fast) {
-        // Register-resident pass: every thread keeps its box nodes' index,
-        // 1 / (2 rho), u, F and list span in registers for the m_max
-        // iterations; shared memory holds u (read by the interpolation), the
-        // marker forces, the stencils and the lists as packed pairs.
+        // Register-resident pass over the box nodes some marker spreads to
+        // (the others keep their u and F through the iterations): every
+        // thread keeps its nodes' index, 1 / (2 rho), u, F and list span in
+        // registers for the m_max iterations; shared memory holds u (read by
+        // the interpolation, which reads only these nodes), the marker
+        // forces, the stencils and the lists as packed pairs.
         float2 *uxy = reinterpret_cast<float2 *>(smem);
         float2 *fsp = uxy + nb;
         float2 *mst = fsp + n;                               // [16][n] (node as int bits, weight)
         int2 *lst = reinterpret_cast<int2 *>(mst + 16 * n);  // (marker, weight as int bits)
         float *rhm = reinterpret_cast<float *>(lst + 16 * n);
+        int *act = reinterpret_cast<int *>(rhm + n);         // box order of the nodes with a list
+        int nact;
+        {
+            const int chunk = (nbox + nt - 1) / nt, o0 = tid * chunk, o1 = min(nbox, o0 + chunk);
+            int mine = 0;
+            for (int o = o0; o < o1; o++) mine += ib.cnt[bq(o)] > 0 ? 1 : 0;
+            int run = block_scan(mine, &nact);
+            for (int o = o0; o < o1; o++)
+                if (ib.cnt[bq(o)] > 0) act[run++] = o;
+        }
+        __syncthreads();
         int nq[kFastNodes], la[kFastNodes], lc[kFastNodes];
         float hr[kFastNodes], fx[kFastNodes], fy[kFastNodes], vx[kFastNodes], vy[kFastNodes];
 #pragma unroll
         for (int k = 0; k < kFastNodes; k++) {
-            const int o = tid + k * nt;
+            const int a = tid + k * nt;
             nq[k] = -1;
             la[k] = lc[k] = 0;
             hr[k] = fx[k] = fy[k] = vx[k] = vy[k] = 0.0f;
-            if (o < nbox) {
-                const int q = (int)bq(o);
+            if (a < nact) {
+                const int q = (int)bq(act[a]);
                 nq[k] = q;
                 hr[k] = 0.5f / (1.0f + band[q]);
                 vx[k] = band[nb + q];
@@ -1022,20 +1035,29 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
         }
         drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
         lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
-        // collision of this thread's box cells
+        // the forced nodes' u and F back into the box fields, then the
+        // collision of every box cell
 #pragma unroll
         for (int k = 0; k < kFastNodes; k++) {
             if (nq[k] < 0) continue;
-            const int o = tid + k * nt;
+            band[nb + nq[k]] = vx[k];
+            band[2 * nb + nq[k]] = vy[k];
+            band[3 * nb + nq[k]] = fx[k];
+            band[4 * nb + nq[k]] = fy[k];
+        }
+        __syncthreads();
+        for (int o = tid; o < nbox; o += nt) {
+            const long long q = bq(o);
+            const float ux = band[nb + q], uy = band[2 * nb + q], Fx = band[3 * nb + q], Fy = band[4 * nb + q];
             const long long cell = (st->box_lo[0] + o % bw) + (long long)P.nx * (st->box_lo[1] + o / bw);
             float f[Q9];
 #pragma unroll
             for (int l = 0; l < Q9; l++) f[l] = St<T>::ld(B + l * P.S + cell);
-            collide9(f, band[nq[k]], vx[k], vy[k], fx[k], fy[k], P.omega, true);
-            ib.boxF[o] = fx[k];
-            ib.boxF[P.nb + o] = fy[k];
-            ib.boxF[2 * P.nb + o] = vx[k];
-            ib.boxF[3 * P.nb + o] = vy[k];
+            collide9(f, band[q], ux, uy, Fx, Fy, P.omega, true);
+            ib.boxF[o] = Fx;
+            ib.boxF[P.nb + o] = Fy;
+            ib.boxF[2 * P.nb + o] = ux;
+            ib.boxF[3 * P.nb + o] = uy;
 #pragma unroll
             for (int l = 0; l < Q9; l++) St<T>::st(B + l * P.S + cell, f[l]);
         }
