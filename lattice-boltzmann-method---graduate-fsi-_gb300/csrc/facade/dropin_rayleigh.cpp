@@ -1,16 +1,18 @@
 // dropin_rayleigh.cpp -- the reference's Rayleigh_Benard build (#define
 // ENERGY on D3Q19): main_setup_RayleighBenard1 (lbm.cpp:1585-1643) and the
-// main loop with its per-step maximum vertical velocity and Nusselt number
-// (main.cpp:212-223, 308-321) through the LBM.h facade built with -DENERGY.
+// main loop with its maximum vertical velocity and Nusselt number every Nt
+// = 10 steps, each time rewritten to its two CSV files (main.cpp:212-226,
+// 308-321), through the LBM.h facade built with -DENERGY.
 // The constants are those of LBM.h's Rayleigh_Benard section
 // (LBM.h:222-242) on an NX x NY x NZ box (the reference's is 200 x 50 x 5).
 // usage: dropin_rayleigh NX NY NZ STEPS OUT.bin
 // Writes, for every cell (ghosts included, x fastest, then y, then z), as
-// doubles: density, ux, uy, uz, T, q[0], q[1], q[2]; then per step the
-// maximum |uy| and the Nusselt number.
+// doubles: density, ux, uy, uz, T, q[0], q[1], q[2]; then the recorded
+// maximum |uy| and Nusselt numbers.
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 #include <vector>
 
 #include "LBM.h"
@@ -37,6 +39,9 @@ int main(int argc, char **argv) {
     g_lbm_options.T_star = T_star;
     g_lbm_options.alpha = alpha;
     g_lbm_options.dT = dT;
+    const int Nt = 10;
+    g_lbm_options.Nt = Nt;
+    g_lbm_options.csv_time_step = Nt * 1.0;  // OutputCSV's (i + 1) Nt dt (lbm.cpp:3174-3175)
     LBM lb(Nx, Ny, Nz, tau);
     for (int i = 0; i <= Nx + 1; i++)
         for (int j = 0; j <= Ny + 1; j++)
@@ -67,8 +72,14 @@ int main(int argc, char **argv) {
         lb.Collision();
         lb.Streaming();
         lb.MacroProp();
-        uy_max.push_back(Find_Maximum_uy(lb));
-        Nusselt_number.push_back(Find_Nusselt_number(lb));
+        if (step % Nt == 0) {
+            uy_max.push_back(Find_Maximum_uy(lb));
+            Nusselt_number.push_back(Find_Nusselt_number(lb));
+            std::string name = "Maximum velocity in y direction at Ra = " + std::to_string(Ra) + ".csv";
+            OutputCSV(uy_max, name);
+            name = "Nusselt number at Ra = " + std::to_string(Ra) + ".csv";
+            OutputCSV(Nusselt_number, name);
+        }
     }
     lb.sync_to_host();
     FILE *fp = fopen(argv[5], "wb");

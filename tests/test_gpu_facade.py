@@ -212,10 +212,11 @@ def test_dropin_cylinder2d_outputs(drivers, pkg, tmp_path):
 def test_dropin_rayleigh_benard_loop(drivers, tmp_path):
     """The reference's Rayleigh_Benard build (-DENERGY on D3Q19):
     main_setup_RayleighBenard1 and the main loop with Find_Maximum_uy and
-    Find_Nusselt_number every step (main.cpp:308-321) through the facade,
+    Find_Nusselt_number every Nt steps, each time rewritten to the loop's CSV
+    files (main.cpp:226, 308-321), through the facade,
     which hands the set-up to lbm_energy3d; every cell, ghosts included,
     against the reference's own run (FP32: T within 1e-5 of the spread, u
-    within 1e-4 of its largest value), and the last step's maximum |uy| and
+    within 1e-4 of its largest value), and the last recorded maximum |uy| and
     Nusselt number against the same formulas on the reference's fields."""
     from conftest import GOLDEN
 
@@ -228,8 +229,16 @@ def test_dropin_rayleigh_benard_loop(drivers, tmp_path):
     n = int(np.prod(shape))
     raw = np.fromfile(out, dtype=np.float64)
     a = raw[:8 * n].reshape((8,) + shape)
-    uy_max, nus = raw[8 * n:8 * n + steps], raw[8 * n + steps:]
-    assert uy_max.shape == (steps,) and nus.shape == (steps,)
+    rec = steps // 10
+    uy_max, nus = raw[8 * n:8 * n + rec], raw[8 * n + rec:]
+    assert uy_max.shape == (rec,) and nus.shape == (rec,)
+    # the loop's CSV files, rewritten every Nt = 10 steps: time (i + 1) Nt dt
+    for name, series in (("Maximum velocity in y direction at Ra = 1710.000000.csv", uy_max),
+                         ("Nusselt number at Ra = 1710.000000.csv", nus)):
+        r = np.loadtxt(str(tmp_path / name), delimiter=",", skiprows=1)
+        assert (tmp_path / name).read_text().startswith("time,error\n")
+        assert np.array_equal(r[:, 0], 10.0 * (np.arange(rec) + 1))
+        assert np.allclose(r[:, 1], series, rtol=1e-5, atol=0)
     T = g["T"]
     assert np.abs(a[4] - T).max() < 1e-5 * (T.max() - T.min())
     us = np.abs(g["u"]).max()
