@@ -358,6 +358,11 @@ extern "C" lbm_status lbmgpu_create(const lbm_config *cfg, lbm_handle **out) {
         return fail(LBM_ERR_UNSUPPORTED, "create: the staged (tensor-copy) step kernel is not built (staged must be 0)");
     if (c.wall_force && c.lattice != LBM_LATTICE_D2Q9)
         return fail(LBM_ERR_UNSUPPORTED, "create: wall_force is a D2Q9 option (the reference's Poiseuille_Flow)");
+    if (c.thermal < LBM_THERMAL_NONE || c.thermal > LBM_THERMAL_ENERGY)
+        return fail(LBM_ERR_INVALID, "create: unknown thermal model");
+    if (c.lattice != LBM_LATTICE_D2Q9 && c.thermal == LBM_THERMAL_ENERGY)
+        return fail(LBM_ERR_UNSUPPORTED, "create: the ENERGY model on D3Q19 is its own solver object "
+                                         "(lbmgpu_energy3d_create)");
     for (int f = 0; f < 6; f++)
         if (c.lattice != LBM_LATTICE_D2Q9 && c.faces[f].kind == LBM_FACE_WALL &&
             c.faces[f].thermal_kind == LBM_TWALL_NEUMANN)

@@ -159,12 +159,21 @@ def test_config_energy_2d_maps_couette_and_refuses_the_rest(pkg):
     with pytest.raises(pkg.LbmError) as e:
         pkg.config_energy_2d(pkg.config_from_types_2d(nx, ny, 0.9, t3), nx, ny, t3, te, T, 0.8, 2.0)
     assert e.value.status == 7
-    # Neumann walls are a D2Q9 ENERGY option
+    # Neumann walls are a D2Q9 ENERGY option; ENERGY on D3Q19 is lbm_energy3d
     c3 = pkg.channel_config(8, 8, 8, 0.8)
     c3.faces[2].thermal_kind = pkg.TWALL_NEUMANN
     with pytest.raises(pkg.LbmError) as e:
         pkg.Solver(c3)
     assert e.value.status == 7 and "Neumann" in str(e.value)
+    c4 = pkg.channel_config(8, 8, 8, 0.8)
+    c4.thermal, c4.tau_g, c4.cp = pkg.THERMAL_ENERGY, 0.8, 2.0
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(c4)
+    assert e.value.status == 7 and "energy3d" in str(e.value)
+    c4.thermal = 5
+    with pytest.raises(pkg.LbmError) as e:
+        pkg.Solver(c4)
+    assert e.value.status == 1
     # create: the D3Q7 model is not a D2Q9 option; ENERGY needs cp > 0
     c2 = pkg.config_from_types_2d(nx, ny, 0.9, t)
     c2.thermal, c2.tau_g = pkg.THERMAL_D3Q7, 0.8
