@@ -179,6 +179,17 @@ class LBM {
     void ConvLBM(int i, int j, int k);          // host collision of one mirror cell (lbm.cpp:75-119)
     double Calc_feq(int i, int j, int k, int l); // third-order equilibrium (lbm.cpp:628-633)
     void Determine_Wall_Velocity(int i, int j, int k, std::vector<double> &uwall);  // lbm.cpp:941-962
+#if defined ENERGY
+    // ENERGY host helpers on the mirror (the device keeps g; the mirror's g
+    // holds Init's equilibrium): Calc_geq (lbm.cpp:636-653), the wall T of
+    // Determine_Wall_Temperature (lbm.cpp:965-981) and of
+    // Determine_Twall_Neumann (lbm.cpp:983-1028), which also writes it into
+    // the mirror's wall cell opposite the normal
+    double Calc_geq(int i, int j, int k, int l, short type, std::vector<double> uwall);
+    double Determine_Wall_Temperature(int i, int j, int k);
+    double Determine_Twall_Neumann(int i, int j, int k, std::vector<double> uwall, std::vector<int> cdotn_pos,
+                                   std::vector<int> cdotn_notpos, double j_dot_n);
+#endif
 
     int getNx() const;
     int getNy() const;

@@ -95,7 +95,12 @@ int main(int argc, char **argv) {
     fwrite(uy_max.data(), sizeof(double), uy_max.size(), fp);
     fwrite(Nusselt_number.data(), sizeof(double), Nusselt_number.size(), fp);
     fclose(fp);
-    printf("{\"steps\": %lld, \"uy_max\": %.9g, \"nusselt\": %.9g}\n", lb.steps(), uy_max.back(),
-           Nusselt_number.back());
+    // the per-cell ENERGY helpers on the synced mirror: the bottom wall's T
+    // seen from the first fluid cell, and the cell's equilibrium along +y
+    const std::vector<double> rest(3, 0.0);
+    printf("{\"steps\": %lld, \"uy_max\": %.17g, \"nusselt\": %.17g, \"wall_T_1_1_1\": %.17g, "
+           "\"geq_1_1_1_3\": %.17g}\n",
+           lb.steps(), uy_max.back(), Nusselt_number.back(), lb.Determine_Wall_Temperature(1, 1, 1),
+           lb.Calc_geq(1, 1, 1, 3, TYPE_F, rest));
     return 0;
 }

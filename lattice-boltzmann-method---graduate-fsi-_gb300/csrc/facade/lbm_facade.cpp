@@ -110,6 +110,77 @@ void LBM::Determine_Wall_Velocity(int i, int j, int k, std::vector<double> &uwal
     }
 }
 
+#if defined ENERGY
+// rho w T times the cubic shape of c.u: the cell's own T and u, or for a
+// solid type the wall T of the cell and the given wall velocity
+double LBM::Calc_geq(int i, int j, int k, int l, short type, std::vector<double> uwall) {
+    const LATTICE &c = fluid[i][j][k];
+    const double cs2 = 1.0 / 3.0;
+    double T = c.T, u[3] = {c.ux, c.uy, c.uz};
+    if (type == TYPE_S) {
+        T = Determine_Wall_Temperature(i, j, k);
+        for (int a = 0; a < 3; a++) u[a] = uwall[a];
+    }
+    const double uu = u[0] * u[0] + u[1] * u[1] + u[2] * u[2];
+    const double cu = u[0] * cx[l] + u[1] * cy[l] + u[2] * cz[l];
+    return c.density * w[l] * T *
+           (1 + cu / cs2 + cu * cu / (2 * cs2 * cs2) - uu / (2 * cs2) + std::pow(cu, 3) / (6 * std::pow(cs2, 3)) -
+            cu * uu / (2 * cs2 * cs2));
+}
+
+// the mean T of the solid neighbours (periodic modulo over the whole grid)
+double LBM::Determine_Wall_Temperature(int i, int j, int k) {
+    double s = 0.0;
+    int num = 0;
+    for (int l = 0; l < npop; l++) {
+        const LATTICE &nb = fluid[(i + cx[l] + Nx + 2) % (Nx + 2)][(j + cy[l] + Ny + 2) % (Ny + 2)]
+                                 [(k + cz[l] + Nz + 2) % (Nz + 2)];
+        if (nb.type == TYPE_S) {
+            s += nb.T;
+            num++;
+        }
+    }
+    return s / num;
+}
+
+// T_w = (j.n - sum over the links facing away from the walls of g c.n) /
+// sum over the wall links of geq(rho, T = 1, u_w) c.n, n the mean wall-link
+// direction (not normalised)
+double LBM::Determine_Twall_Neumann(int i, int j, int k, std::vector<double> uwall, std::vector<int> cdotn_pos,
+                                   std::vector<int> cdotn_notpos, double j_dot_n) {
+    const LATTICE &c = fluid[i][j][k];
+    const double cs2 = 1.0 / 3.0;
+    double n[3] = {0, 0, 0};
+    for (int l : cdotn_pos) {
+        n[0] += cx[l];
+        n[1] += cy[l];
+        n[2] += cz[l];
+    }
+    for (int a = 0; a < 3; a++) n[a] /= (double)cdotn_pos.size();
+    double other = 0.0;
+    for (int l : cdotn_notpos) other += c.g[l] * (cx[l] * n[0] + cy[l] * n[1] + cz[l] * n[2]);
+    const double uu = uwall[0] * uwall[0] + uwall[1] * uwall[1] + uwall[2] * uwall[2];
+    double wall = 0.0;
+    for (int l : cdotn_pos) {
+        const double cu = uwall[0] * cx[l] + uwall[1] * cy[l] + uwall[2] * cz[l];
+        const double eq = w[l] * c.density *
+                          (1 + cu / cs2 + cu * cu / (2 * cs2 * cs2) - uu / (2 * cs2) +
+                           std::pow(cu, 3) / (6 * std::pow(cs2, 3)) - cu * uu / (2 * cs2 * cs2));
+        wall += eq * (cx[l] * n[0] + cy[l] * n[1] + cz[l] * n[2]);
+    }
+    const double Tw = (j_dot_n - other) / wall;
+    for (int l = 0; l < npop; l++) {
+        const int o = opposite[l];
+        if (cx[o] == n[0] && cy[o] == n[1] && cz[o] == n[2]) {
+            fluid[(i + cx[l] + Nx + 2) % (Nx + 2)][(j + cy[l] + Ny + 2) % (Ny + 2)][(k + cz[l] + Nz + 2) % (Nz + 2)]
+                .T = Tw;
+            break;
+        }
+    }
+    return Tw;
+}
+#endif
+
 #if defined ENERGY && !defined D2Q9
 // D3Q19 with ENERGY (the reference's Rayleigh_Benard build): the whole
 // ghost-inclusive set-up goes to lbmgpu_energy3d, which keeps the
@@ -162,6 +233,9 @@ void LBM::Init() {
 #if defined ENERGY && !defined D2Q9
     (void)n;
     init_energy3d(*this, *dev, tau);
+    // host mirror as LBM::Init leaves it (lbm.cpp:31-57): f = feq, g = geq of
+    // the cell type with the walls at rest
+    const std::vector<double> rest(3, 0.0);
     for (int i = 0; i < NX; i++)
         for (int j = 0; j < NY; j++)
             for (int k = 0; k < NZ; k++)
@@ -169,6 +243,9 @@ void LBM::Init() {
                     double fe = Calc_feq(i, j, k, l);
                     fluid[i][j][k].f[l] = fe;
                     fluid[i][j][k].f_star[l] = fe;
+                    double ge = Calc_geq(i, j, k, l, fluid[i][j][k].type, rest);
+                    fluid[i][j][k].g[l] = ge;
+                    fluid[i][j][k].g_star[l] = ge;
                 }
     dev->steps = 0;
     dev->mirror_stale = false;

@@ -1,5 +1,6 @@
 """The C++ drop-in facade (csrc/facade/LBM.h): the reference's own time loops
 (main.cpp:195-221) driving the GPU through the C ABI, against the oracle."""
+import json
 import os
 import subprocess
 
@@ -223,8 +224,9 @@ def test_dropin_rayleigh_benard_loop(drivers, tmp_path):
     g = np.load(os.path.join(GOLDEN, "rayleigh32x16x5_400.npz"))
     nx, ny, nz, steps = int(g["nx"]), int(g["ny"]), int(g["nz"]), int(g["steps"])
     out = str(tmp_path / "rb.bin")
-    subprocess.check_call([drivers["dropin_rayleigh"], str(nx), str(ny), str(nz), str(steps), out],
-                          cwd=str(tmp_path))
+    r = subprocess.run([drivers["dropin_rayleigh"], str(nx), str(ny), str(nz), str(steps), out],
+                       cwd=str(tmp_path), capture_output=True, text=True, check=True)
+    info = json.loads(r.stdout.strip().splitlines()[-1])
     shape = (nz + 2, ny + 2, nx + 2)
     n = int(np.prod(shape))
     raw = np.fromfile(out, dtype=np.float64)
@@ -255,3 +257,16 @@ def test_dropin_rayleigh_benard_loop(drivers, tmp_path):
     fl[1:-1, 1:-1, 1:-1] = True
     nu_ref = 1 + (g["u"][1][fl] * T[fl]).mean() / (alpha * 1.0 / (ny + 1))
     assert abs(nus[-1] - nu_ref) < 1e-4 * abs(nu_ref - 1.0), (nus[-1], nu_ref)
+    # the ENERGY helpers on the mirror (fields from the dump, k, j, i order):
+    # Determine_Wall_Temperature of cell (1, 1, 1), the mean T of its solid
+    # neighbours (the walls as MacroProp leaves them), and Calc_geq along +y
+    cxyz = [(0, 0, 0), (1, 0, 0), (-1, 0, 0), (0, 1, 0), (0, -1, 0), (0, 0, 1), (0, 0, -1), (1, 1, 0), (-1, -1, 0),
+            (1, 0, 1), (-1, 0, -1), (0, 1, 1), (0, -1, -1), (1, -1, 0), (-1, 1, 0), (1, 0, -1), (-1, 0, 1),
+            (0, 1, -1), (0, -1, 1)]
+    solid = ~fl
+    Ts = [a[4][1 + c[2], 1 + c[1], 1 + c[0]] for c in cxyz if solid[1 + c[2], 1 + c[1], 1 + c[0]]]
+    assert abs(info["wall_T_1_1_1"] - np.mean(Ts)) < 1e-12
+    rho, uy, Tc = a[0][1, 1, 1], a[2][1, 1, 1], a[4][1, 1, 1]
+    uu = a[1][1, 1, 1] ** 2 + uy ** 2 + a[3][1, 1, 1] ** 2
+    geq = rho / 18 * Tc * (1 + 3 * uy + 4.5 * uy ** 2 - 1.5 * uu + 4.5 * uy ** 3 - 4.5 * uy * uu)
+    assert abs(info["geq_1_1_1_3"] - geq) < 1e-12 * abs(geq)
