@@ -3,12 +3,14 @@
 // and the main loop (main.cpp:212-223) through the LBM.h facade built with
 // -DD2Q9 -DENERGY.  The constants are those of LBM.h's Couette section
 // (LBM.h:206-219), on a strip Nx = 2 wide.
-// usage: dropin_couette NY RE STEPS OUT.bin
+// usage: dropin_couette NY RE STEPS OUT.bin [neumann]
+// neumann: the top wall's type_Energy is TYPE_Q (a Neumann wall, j.n = 0).
 // Writes, for the interior rows j = 1..Ny of the layer k = 1 (x fastest over
 // i = 0..Nx+1, the periodic ghost columns included), as doubles: density, ux,
 // uy, uz, T, q[0], q[1], q[2].
 #include <cstdio>
 #include <cstdlib>
+#include <string>
 
 #include "LBM.h"
 
@@ -20,6 +22,7 @@ int main(int argc, char **argv) {
     const int Nx = 2, Ny = atoi(argv[1]), Nz = 2;
     const double Re = atof(argv[2]);
     const int steps = atoi(argv[3]);
+    const bool neumann = argc > 5 && std::string(argv[5]) == "neumann";
     const double cs2 = 1.0 / 3.0, tau = 0.9, rho0 = 1.0;
     const double nu = cs2 * (tau - 0.5);
     const double u_wall = Re * nu / (Ny + 1);
@@ -41,7 +44,7 @@ int main(int argc, char **argv) {
                 if (j == 0 || j == Ny + 1) c.type = TYPE_S;
                 if (j == Ny + 1) c.ux = u_wall;
                 if (j == 0 || j == Ny + 1) {
-                    c.type_Energy = TYPE_T;
+                    c.type_Energy = (neumann && j == Ny + 1) ? TYPE_Q : TYPE_T;
                     lb.fluid[i][0][kk].T = Tb;
                     lb.fluid[i][Ny + 1][kk].T = Tt;
                 }

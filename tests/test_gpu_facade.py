@@ -115,6 +115,26 @@ def test_dropin_cylinder2d_loop(drivers, tmp_path, case):
     assert np.abs(r[:, 2] - g["cl"]).max() / scale < 2e-6
 
 
+def test_dropin_couette_neumann_loop(drivers, tmp_path):
+    """The same build with the top wall's type_Energy TYPE_Q (a Neumann wall,
+    j.n = 0): every fluid row against the reference's own single-thread run
+    (1000 steps)."""
+    from conftest import GOLDEN
+
+    g = np.load(os.path.join(GOLDEN, "couette_neumann_ny30_re20_1000.npz"))
+    ny = int(g["ny"])
+    out = str(tmp_path / "couette_neumann.bin")
+    subprocess.check_call([drivers["dropin_couette"], str(ny), str(float(g["Re"])), str(int(g["steps"])), out,
+                           "neumann"], cwd=str(tmp_path))
+    a = np.fromfile(out, dtype=np.float64).reshape(8, ny, 4)
+    T = g["T"][1:-1]
+    assert np.abs(a[4] - T).max() < 1e-3 * (T.max() - T.min())
+    uw = np.abs(g["u"][0]).max()
+    assert np.abs(a[1:4] - g["u"][:, 1:-1]).max() < 1e-5 * uw
+    q = g["q"][:, 1:-1]
+    assert np.abs(a[5:8] - q).max() < 1e-5 * np.abs(q).max()
+
+
 def test_dropin_couette_energy_loop(drivers, tmp_path):
     """The reference's Couette_Flow build with its ENERGY model (-DD2Q9
     -DENERGY): main_setup_Couette's type_Energy / T set-up and the main loop
