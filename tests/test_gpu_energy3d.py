@@ -135,6 +135,47 @@ def test_lid_box_periodic_adiabatic_vs_oracle(pkg, orc):
     assert eT < 2e-5 and eu < 1e-5 and er < 1e-6 and eq < 2e-5, (eT, eu, er, eq)
 
 
+def test_moving_interior_solid_vs_oracle(pkg, orc):
+    """A 2 x 2 x 2 solid block inside the fluid, moving with u_x = 0.02
+    (Determine_Wall_Velocity's moving solid neighbours, lbm.cpp:941-962) and
+    held at T = 1.1 (type_Energy TYPE_T), in a channel with Dirichlet y walls
+    and fluid ghost layers in x and z (the periodic modulo over the whole
+    grid); 250 steps against the oracle."""
+    nx, ny, nz, steps, tau = 16, 12, 8, 250, 0.75
+    cs2 = 1.0 / 3.0
+    nu = cs2 * (tau - 0.5)
+    alpha = nu / 0.71
+    tau_g = 0.5 + alpha / cs2
+    cp = cs2 * tau_g / alpha
+    lat = orc.Lattice(19, nx, ny, nz, tau)
+    t = lat.types
+    t[:] = orc.TYPE_F
+    lat.enable_energy(tau_g, cp, nu)
+    te = lat.types_energy
+    T = lat.T
+    T[:] = 1.0
+    t[:, 0, :] = t[:, -1, :] = orc.TYPE_S
+    te[:, 0, :] = te[:, -1, :] = orc.TYPE_T
+    blk = (slice(4, 6), slice(5, 7), slice(7, 9))  # k, j, i
+    t[blk] = orc.TYPE_S
+    te[blk] = orc.TYPE_T
+    T[blk] = 1.1
+    lat.ux[blk] = 0.02
+    s = pkg.Energy3D(t.copy(), te.copy(), T.copy(), tau, tau_g, cp, u=np.stack([lat.ux, lat.uy, lat.uz]).copy())
+    lat.init()
+    s.step(steps)
+    assert s.status() == 0
+    m = s.moments()
+    assert lat.step_plain(steps) == 0
+    fl = t == orc.TYPE_F
+    ref = dict(rho=lat.rho, ux=lat.ux, uy=lat.uy, uz=lat.uz, T=lat.T, qx=lat.hq[0], qy=lat.hq[1], qz=lat.hq[2])
+    eT, eu, er, eq = _errors(m, ref, fl)
+    print("moving block 16x12x8, %d steps: T %.3g of spread, u %.3g of max, rho %.3g, q %.3g" % (steps, eT, eu, er, eq))
+    assert eT < 2e-5 and eu < 1e-5 and er < 1e-6 and eq < 2e-5, (eT, eu, er, eq)
+    # the block drags the fluid along x
+    assert m["ux"][fl].max() > 1e-3
+
+
 def test_energy3d_rejects_other_cell_types(pkg, orc):
     lat, c = orc.rayleigh_benard(8, 6, 4)
     t = lat.types.copy()
