@@ -439,7 +439,9 @@ struct lbm_energy3d {
     int cur = 0;
     long long steps = 0;
     cudaStream_t s = nullptr;
+    cudaStream_t s2 = nullptr;  // the wall records, beside the bulk kernel (high priority)
     cudaEvent_t ev[2] = {nullptr, nullptr};
+    cudaEvent_t fork = nullptr, join = nullptr;
     std::vector<void *> allocs;
     std::vector<E3Wall> walls;
 };
@@ -457,6 +459,9 @@ cudaError_t alloc3(lbm_energy3d *e, Tp **p, size_t bytes) {
 void free3(lbm_energy3d *e) {
     for (void *p : e->allocs) cudaFree(p);
     if (e->s) cudaStreamDestroy(e->s);
+    if (e->s2) cudaStreamDestroy(e->s2);
+    if (e->fork) cudaEventDestroy(e->fork);
+    if (e->join) cudaEventDestroy(e->join);
     for (cudaEvent_t v : e->ev)
         if (v) cudaEventDestroy(v);
     delete e;
@@ -679,24 +684,35 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
         if (e_ != cudaSuccess) return fail3(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// One step: the Neumann pre-pass and the wall records on the second stream,
+// beside the bulk kernel (they write disjoint cells and read only the
+// previous step's arrays); the next step waits for both.
 cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
     const E3Params &P = e->P;
     const int gather = e->steps > 0 ? 1 : 0;
     const int phase = phase_of(e->steps);
-    if (gather && e->has_neu) {
-        const unsigned nb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
-        k_e3_walls<<<nb, kRecBlock, 0, e->s>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
-                                           export_only ? 0 : 1);
+    cudaError_t err = cudaSuccess;
+    if (P.nrec) {
+        err = cudaEventRecord(e->fork, e->s);
+        if (err == cudaSuccess) err = cudaStreamWaitEvent(e->s2, e->fork, 0);
+        if (err != cudaSuccess) return err;
+        if (gather && e->has_neu) {
+            const unsigned nb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
+            k_e3_walls<<<nb, kRecBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
+                                                export_only ? 0 : 1);
+        }
+        const unsigned rb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
+        k_e3_rec<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur],
+                                          e->aux, e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather,
+                                          phase, export_only);
+        err = cudaEventRecord(e->join, e->s2);
+        if (err != cudaSuccess) return err;
     }
     const unsigned blocks = (unsigned)((P.N + kBlock - 1) / kBlock);
     k_e3_bulk<<<blocks, kBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
                                           e->aux2, e->rec_of, P, e->status, mom, gather, export_only);
-    if (P.nrec) {
-        const unsigned rb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
-        k_e3_rec<<<rb, kRecBlock, 0, e->s>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur], e->aux,
-                                         e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather, phase,
-                                         export_only);
-    }
+    if (P.nrec) err = cudaStreamWaitEvent(e->s, e->join, 0);
+    if (err != cudaSuccess) return err;
     return cudaGetLastError();
 }
 
@@ -773,7 +789,14 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
             return bail(fail3(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)));        \
     } while (0)
     CKE(cudaStreamCreateWithFlags(&e->s, cudaStreamNonBlocking));
+    {
+        int lo = 0, hi = 0;
+        CKE(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+        CKE(cudaStreamCreateWithPriority(&e->s2, cudaStreamNonBlocking, hi));
+    }
     for (int i = 0; i < 2; i++) CKE(cudaEventCreate(&e->ev[i]));
+    CKE(cudaEventCreateWithFlags(&e->fork, cudaEventDisableTiming));
+    CKE(cudaEventCreateWithFlags(&e->join, cudaEventDisableTiming));
     for (int i = 0; i < 2; i++) {
         CKE(alloc3(e, &e->f[i], (size_t)Q * P.S * sizeof(float)));
         CKE(alloc3(e, &e->g[i], (size_t)Q * P.S * sizeof(float)));
