@@ -99,13 +99,21 @@ template <class T, bool FORCED, bool SOLID>
 __global__ void __launch_bounds__(256) k_step2d(const T *__restrict__ A, T *__restrict__ B,
                                                 const __grid_constant__ Params2 P, State2 *__restrict__ ds,
                                                 float *__restrict__ mom, float *__restrict__ band, int gather,
-                                                int export_only, int drift) {
+                                                int export_only, int drift, int region, int4 nbx) {
     // launched behind the previous step's IBM pass (programmatic dependent
     // launch): wait for its results first
     cudaGridDependencySynchronize();
-    const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y;
+    // region 0: every cell; 1: all but the near box nbx (x0, y0, w, h: the IBM
+    // box and one cell around it); 2: the near box only, over a grid of its size
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    int y = blockIdx.y * blockDim.y + threadIdx.y;
+    if (region == 2) {
+        if (x >= nbx.z || y >= nbx.w) return;
+        x += nbx.x;
+        y += nbx.y;
+    }
     if (x >= P.nx || y >= P.ny) return;
+    if (region == 1 && (unsigned)(x - nbx.x) < (unsigned)nbx.z && (unsigned)(y - nbx.y) < (unsigned)nbx.w) return;
     const long long cell = x + (long long)P.nx * y;
     float f[Q9];
     const bool face = x == 0 || x == P.nx - 1 || y == 0 || y == P.ny - 1;
@@ -1261,6 +1269,12 @@ struct lbm2d {
     // interior solid cells: the per-cell link masks, a momentum-exchange result
     uint16_t *links = nullptr;
     double *mea_out = nullptr;
+    // a fixed IBM body: the next step's cells away from the box ("far") run
+    // beside the IBM pass, which with the near box goes on a second stream
+    bool overlap = false, overlap_known = false;
+    int4 nbox = make_int4(0, 0, 0, 0);  // near box: x0, y0, w, h
+    cudaStream_t s2 = nullptr;
+    cudaEvent_t ev_far = nullptr, ev_near = nullptr, ev_join = nullptr;
     std::vector<void *> allocs;
 };
 
@@ -1564,21 +1578,26 @@ cudaError_t launch_energy2d(lbm_handle *h, int gather, float *mom, int export_on
     return cudaGetLastError();
 }
 
-cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only) {
+cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only, int region = 0,
+                          cudaStream_t stream = nullptr) {
     lbm2d *d = h->d2;
     if (d->energy) return launch_energy2d(h, gather, mom, export_only);
     const dim3 block(d->tx, d->ty);
-    const dim3 grid((d->P.nx + d->tx - 1) / d->tx, (d->P.ny + d->ty - 1) / d->ty);
+    const int gw = region == 2 ? d->nbox.z : d->P.nx, gh = region == 2 ? d->nbox.w : d->P.ny;
+    const dim3 grid((gw + d->tx - 1) / d->tx, (gh + d->ty - 1) / d->ty);
+    const int4 nbx = d->nbox;
     const void *A = d->f[d->cur];
     void *B = d->f[1 - d->cur];
     const bool forced = d->P.forced != 0, solid = d->P.links != nullptr;
     const int drift = wall_drift(h, gather);
     cudaLaunchAttribute attr[1];
-    const cudaLaunchConfig_t lc = pdl_config2(grid, block, 0, h->s, attr);
+    cudaLaunchConfig_t lc = pdl_config2(grid, block, 0, region ? stream : h->s, attr);
+    // the split launches follow event waits: plain launches
+    if (region) lc.numAttrs = 0;
     cudaError_t e = cudaSuccess;
 #define L2D_LAUNCH(T, FO, SO)                                                                                  \
     e = cudaLaunchKernelEx(&lc, k_step2d<T, FO, SO>, (const T *)A, (T *)B, d->P, d->st, mom, d->band, gather, \
-                           export_only, drift)
+                           export_only, drift, region, nbx)
 #define L2D_STEP(T)                                                                                             \
     if (solid) {                                                                                              \
         if (forced) L2D_LAUNCH(T, true, true);                                                                \
@@ -1597,13 +1616,13 @@ cudaError_t launch_step2d(lbm_handle *h, int gather, float *mom, int export_only
     return e;
 }
 
-cudaError_t launch_ibm2d(lbm_handle *h) {
+cudaError_t launch_ibm2d(lbm_handle *h, cudaStream_t stream) {
     lbm2d *d = h->d2;
     void *B = d->f[1 - d->cur];
     const size_t sm = d->ib.fast ? ibm2d_fast_smem_bytes(d->P.nb, d->ib.n)
                                  : (d->ib.smem ? ibm2d_smem_bytes(d->P.nb, d->ib.n) : 0);
     cudaLaunchAttribute attr[1];
-    cudaLaunchConfig_t c = pdl_config2(dim3(1), dim3(kIbmBlock), sm, h->s, attr);
+    cudaLaunchConfig_t c = pdl_config2(dim3(1), dim3(kIbmBlock), sm, stream, attr);
     switch (h->cfg.storage) {
     case LBM_STORE_F16: return cudaLaunchKernelEx(&c, k_ibm2d<__half>, (__half *)B, d->P, d->st, d->ib, d->band);
     case LBM_STORE_BF16:
@@ -1643,11 +1662,68 @@ cudaError_t enqueue_step2d(lbm_handle *h) {
             e = cudaGetLastError();
         }
     }
-    if (e == cudaSuccess) e = launch_step2d(h, gather, nullptr, 0);
-    if (e == cudaSuccess && d->ibm) e = launch_ibm2d(h);
+    if (e == cudaSuccess && d->overlap && gather) {
+        // second stream: the near box (after the previous step's far cells)
+        // and the IBM pass; this stream: the far cells, after the near box
+        // (they read the previous state only) and beside the IBM pass
+        e = cudaStreamWaitEvent(d->s2, d->ev_far, 0);
+        if (e == cudaSuccess) e = launch_step2d(h, gather, nullptr, 0, 2, d->s2);
+        if (e == cudaSuccess) e = cudaEventRecord(d->ev_near, d->s2);
+        if (e == cudaSuccess) e = launch_ibm2d(h, d->s2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(h->s, d->ev_near, 0);
+        if (e == cudaSuccess) e = launch_step2d(h, gather, nullptr, 0, 1, h->s);
+        if (e == cudaSuccess) e = cudaEventRecord(d->ev_far, h->s);
+    } else {
+        if (e == cudaSuccess) e = launch_step2d(h, gather, nullptr, 0);
+        if (e == cudaSuccess && d->ibm) e = launch_ibm2d(h, h->s);
+        if (e == cudaSuccess && d->overlap) e = cudaEventRecord(d->ev_far, h->s);
+    }
     d->cur = 1 - d->cur;
     h->steps++;
     return e;
+}
+
+// A run of steps on the split streams starts from this stream's work and
+// ends with the second stream joined back into it.
+cudaError_t seq_begin2d(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    return d->overlap ? cudaEventRecord(d->ev_far, h->s) : cudaSuccess;
+}
+cudaError_t seq_end2d(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    if (!d->overlap) return cudaSuccess;
+    cudaError_t e = cudaEventRecord(d->ev_join, d->s2);
+    return e == cudaSuccess ? cudaStreamWaitEvent(h->s, d->ev_join, 0) : e;
+}
+
+// Whether the split applies: a fixed IBM body on plain cells whose near box
+// (the IBM box of the step and one cell around it) lies inside the lattice,
+// so that no periodic wrap reaches it.  The box is read back once.
+lbm_status decide_overlap2d(lbm_handle *h) {
+    lbm2d *d = h->d2;
+    if (d->overlap_known) return LBM_OK;
+    d->overlap = false;
+    if (d->ibm && d->ib.motion == LBM_MOTION_FIXED && !d->links && !d->energy) {
+        State2 st;
+        CK2(cudaStreamSynchronize(h->s));
+        CK2(cudaMemcpy(&st, d->st, sizeof(State2), cudaMemcpyDeviceToHost));
+        const int4 nb = make_int4(st.box_lo[0] - 1, st.box_lo[1] - 1, st.box_w + 2, st.box_h + 2);
+        if (nb.x >= 0 && nb.y >= 0 && nb.x + nb.z <= d->P.nx && nb.y + nb.w <= d->P.ny && st.box_w > 0 &&
+            st.box_h > 0) {
+            if (!d->s2) {
+                int lo = 0, hi = 0;
+                CK2(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+                CK2(cudaStreamCreateWithPriority(&d->s2, cudaStreamNonBlocking, hi));
+                CK2(cudaEventCreateWithFlags(&d->ev_far, cudaEventDisableTiming));
+                CK2(cudaEventCreateWithFlags(&d->ev_near, cudaEventDisableTiming));
+                CK2(cudaEventCreateWithFlags(&d->ev_join, cudaEventDisableTiming));
+            }
+            d->nbox = nb;
+            d->overlap = true;
+        }
+    }
+    d->overlap_known = true;
+    return LBM_OK;
 }
 
 }  // namespace
@@ -1749,6 +1825,12 @@ void l2d_free(lbm_handle *h) {
     if (!d) return;
     for (int i = 0; i < 2; i++)
         if (d->gexec[i]) cudaGraphExecDestroy(d->gexec[i]);
+    if (d->s2) {
+        cudaStreamSynchronize(d->s2);
+        cudaStreamDestroy(d->s2);
+    }
+    for (cudaEvent_t ev : {d->ev_far, d->ev_near, d->ev_join})
+        if (ev) cudaEventDestroy(ev);
     for (void *p : d->allocs) cudaFree(p);
     delete d;
     h->d2 = nullptr;
@@ -1796,6 +1878,7 @@ lbm_status l2d_init(lbm_handle *h, const double *rho, const double *ux, const do
         cudaGraphExecDestroy(d->gexec[i]);
         d->gexec[i] = nullptr;
     }
+    d->overlap_known = false;
     return LBM_OK;
 }
 
@@ -1891,6 +1974,7 @@ lbm_status l2d_set_markers(lbm_handle *h, const lbm_ibm_config *ic, const double
         cudaGraphExecDestroy(d->gexec[i]);
         d->gexec[i] = nullptr;
     }
+    d->overlap_known = false;
     return LBM_OK;
 }
 
@@ -1916,16 +2000,22 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
         CK2(cudaGetLastError());
         d->kin_ready = true;
     }
+    if (d->ibm) {
+        const lbm_status so = decide_overlap2d(h);
+        if (so != LBM_OK) return so;
+    }
     int left = nsteps;
     // the first step (no gather) and odd remainders run eagerly; whole
     // graphs of gsteps (even: the buffers return to the same parity) replay
     // (ENERGY: also the second, whose streaming takes the set-up wall T)
     // (wall_force: also until the walls' drift has set in, at the third)
     const long long eager = h->cfg.wall_force ? 3 : (d->energy ? 2 : 1);
+    CK2(seq_begin2d(h));
     while (left > 0 && h->steps < eager) {
         CK2(enqueue_step2d(h));
         left--;
     }
+    CK2(seq_end2d(h));
     if (d->gsteps > 0 && left >= d->gsteps) {
         cudaGraphExec_t &gx = d->gexec[d->cur];
         if (!gx) {
@@ -1933,7 +2023,9 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
             const long long s0 = h->steps;
             const int c0 = d->cur;
             CK2(cudaStreamBeginCapture(h->s, cudaStreamCaptureModeThreadLocal));
+            seq_begin2d(h);
             for (int i = 0; i < d->gsteps; i++) enqueue_step2d(h);
+            seq_end2d(h);
             cudaError_t e = cudaStreamEndCapture(h->s, &g);
             h->steps = s0;
             d->cur = c0;
@@ -1948,10 +2040,12 @@ lbm_status l2d_step(lbm_handle *h, int nsteps) {
             left -= d->gsteps;
         }
     }
+    CK2(seq_begin2d(h));
     while (left > 0) {
         CK2(enqueue_step2d(h));
         left--;
     }
+    CK2(seq_end2d(h));
     return LBM_OK;
 }
 
@@ -2101,6 +2195,7 @@ lbm_status l2d_checkpoint_restored(lbm_handle *h, long long steps) {
         cudaGraphExecDestroy(d->gexec[i]);
         d->gexec[i] = nullptr;
     }
+    d->overlap_known = false;
     CK2(cudaStreamSynchronize(h->s));
     return LBM_OK;
 }
