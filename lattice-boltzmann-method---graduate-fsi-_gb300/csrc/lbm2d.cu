@@ -692,19 +692,30 @@ __device__ int block_scan(int v, int *total) {
     return before;
 }
 
-// FP64 block sum in a fixed order.
-__device__ double block_sum_d(double v) {
-    __shared__ double part[32];
+// Two FP64 block sums in a fixed order (warp shuffles, then thread 0 over the
+// warps' partials, the two sums as independent chains).
+__device__ void block_sum_d2(double a, double b, double &sa, double &sb) {
+    __shared__ double part[2][32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    if (lane == 0) part[w] = v;
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+        part[0][w] = a;
+        part[1][w] = b;
+    }
     __syncthreads();
-    double s = 0.0;
+    double x = 0.0, y = 0.0;
     if (threadIdx.x == 0)
-        for (int i = 0; i < (int)(blockDim.x >> 5); i++) s += part[i];
+        for (int i = 0; i < (int)(blockDim.x >> 5); i++) {
+            x += part[0][i];
+            y += part[1][i];
+        }
     __syncthreads();
-    return s;  // valid in thread 0
+    sa = x;  // valid in thread 0
+    sb = y;
 }
 
 // Marker m's stencil: origin (box coordinates) and the 16 weights
@@ -1041,8 +1052,7 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
             }
             __syncthreads();
         }
-        drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
-        lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
+        block_sum_d2(ib.scheme == 0 ? mk_drag : node_drag, ib.scheme == 0 ? mk_lift : node_lift, drag, lift);
         // the forced nodes' u and F back into the box fields, then the
         // collision of every box cell
 #pragma unroll
@@ -1180,8 +1190,7 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
     }
 
     // the pass's force: sum over markers (implicit) or box nodes (explicit)
-    drag = block_sum_d(ib.scheme == 0 ? mk_drag : node_drag);
-    lift = block_sum_d(ib.scheme == 0 ? mk_lift : node_lift);
+    block_sum_d2(ib.scheme == 0 ? mk_drag : node_drag, ib.scheme == 0 ? mk_lift : node_lift, drag, lift);
 
     // collision of the box cells with the forced velocity and the force
     for (int o = tid; o < nbox; o += nt) {
@@ -1214,7 +1223,8 @@ __global__ void __launch_bounds__(kIbmBlock) k_ibm2d(T *__restrict__ B, const __
                 cn += 1.0;
             }
         }
-        const double tr = block_sum_d(rs), tc = block_sum_d(cn);
+        double tr, tc;
+        block_sum_d2(rs, cn, tr, tc);
         if (tid == 0) {
             const double ravg = tr / tc;
             sam[0] = ravg * ib.vsolid * dV0 / 1.0;
