@@ -165,16 +165,19 @@ __device__ __forceinline__ void shift_rows(const uint32_t (&w)[NL][NW], const ui
 
 // Resident blocks per SM asked of the compiler: the register budget that
 // measured fastest for each segment width (an FP16 channel 256x128x128:
-// two cells at 8 blocks 53.7 k MLUPS against 44.4 k unbounded).
-template <class T, int NP, bool THERMAL>
+// two cells at 8 blocks 53.7 k MLUPS against 44.4 k unbounded).  BESIDE:
+// the far region that runs beside the IBM kernels, where 7 blocks (more
+// registers, fewer spills) measured faster on the sphere channel.
+template <class T, int NP, bool THERMAL, bool BESIDE = false>
 constexpr int stepv_min_blocks() {
     if constexpr (sizeof(T) == 4) return NP == 1 ? 6 : 1;
     if constexpr (THERMAL) return NP == 1 ? 4 : 1;
+    if constexpr (BESIDE && NP == 1) return 7;
     return NP == 1 ? 8 : (NP == 2 ? 4 : 1);
 }
 
-template <class T, int NP, bool THERMAL, bool FORCED>
-__global__ void __launch_bounds__(128, (stepv_min_blocks<T, NP, THERMAL>()))
+template <class T, int NP, bool THERMAL, bool FORCED, bool BESIDE = false>
+__global__ void __launch_bounds__(128, (stepv_min_blocks<T, NP, THERMAL, BESIDE>()))
     k_stepv(const T *__restrict__ A, T *__restrict__ B, const T *__restrict__ GA, T *__restrict__ GB,
             const __grid_constant__ StepParams P, DevState *__restrict__ ds, float *__restrict__ band, int region) {
     using A2 = Ar<float2>;
@@ -306,6 +309,17 @@ static cudaError_t launch_t(const LaunchArgs &a) {
     const dim3 grd((per_row + bx - 1) / bx, (P.ny + blk.y - 1) / blk.y, P.nz);
     const T *A = (const T *)a.A, *GA = (const T *)a.GA;
     T *B = (T *)a.B, *GB = (T *)a.GB;
+    if constexpr (sizeof(T) == 2 && NP == 1) {
+        if (a.region == 1 && !a.thermal) {
+            if (P.forced)
+                k_stepv<T, NP, false, true, true><<<grd, blk, 0, a.stream>>>(A, B, nullptr, nullptr, P, a.ds,
+                                                                           a.band, a.region);
+            else
+                k_stepv<T, NP, false, false, true><<<grd, blk, 0, a.stream>>>(A, B, nullptr, nullptr, P, a.ds,
+                                                                            a.band, a.region);
+            return cudaGetLastError();
+        }
+    }
     if (a.thermal)
         k_stepv<T, NP, true, true><<<grd, blk, 0, a.stream>>>(A, B, GA, GB, P, a.ds, a.band, a.region);
     else if (P.forced)
