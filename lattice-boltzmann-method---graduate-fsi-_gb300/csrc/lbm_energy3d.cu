@@ -74,6 +74,20 @@ struct E3Slots {
     uint8_t own[kSlots];
 };
 
+// The records on the device, one array per field (a warp's load of a field
+// reads 32 consecutive records).
+struct E3Recs {
+    const int *cell, *ci, *cj, *ck;
+    const uint32_t *bb, *dir, *neu;
+    const int *ndyn;
+    const float *inv_nsol;
+    const float *ssum;     // [2][nrec]
+    const float *uw;       // [3 phases][3][nrec]
+    const int *dwriter;    // [kSlots][nrec]
+    const float *dt;       // [2][kSlots][nrec]
+    const uint8_t *down;   // [kSlots][nrec]
+};
+
 // rec_of: a record index, or one of these
 constexpr int kSolid = -2, kBulk = -1, kBulkWrap = -3;
 
@@ -107,6 +121,85 @@ __device__ __forceinline__ int wrap_src(int i, int j, int k, int l, const E3Para
 __device__ __forceinline__ float p2m1(float x, float uu) { return 3.0f * x + 4.5f * x * x - 1.5f * uu; }
 __device__ __forceinline__ float p3m1(float x, float uu) { return p2m1(x, uu) + 4.5f * x * (x * x - uu); }
 
+// The D3Q19 link vectors as 2-bit fields (c + 1) of one word per axis, for a
+// link index that differs across the lanes of a warp.
+__host__ __device__ constexpr unsigned long long pack_axis(int a) {
+    unsigned long long v = 0;
+    for (int l = 0; l < Q; l++) v |= (unsigned long long)((a == 0 ? cx(l) : (a == 1 ? cy(l) : cz(l))) + 1) << (2 * l);
+    return v;
+}
+__device__ __forceinline__ int lane_c(unsigned long long packed, int l) { return (int)((packed >> (2 * l)) & 3ull) - 1; }
+__device__ __forceinline__ float lane_w(int l) { return l == 0 ? 1.0f / 3.0f : (l < 7 ? 1.0f / 18.0f : 1.0f / 36.0f); }
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Determine_Twall_Neumann for every record with Neumann links, one warp a
+// record and one lane a link: the normal is the mean direction of the links
+// from walls (cdotn_pos); the other links contribute this sweep's pulled
+// value where the reference's push (i outer, k inner) visits their source
+// before the cell -- and for the rest link --, else the previous sweep's,
+// kept in gold; the wall links the equilibrium at T = 1 of the cell's
+// density (previous MacroProp) and the wall velocity.  With j.n = 0
+// (LBM.h's j_dot_n): T_w = -sum_other g c.n / sum_wall geq c.n, the sums
+// over the lanes.  keep: store this sweep's pulled values for the next
+// sweep's stale links.
+constexpr int kWallBlock = 128;
+__global__ void __launch_bounds__(kWallBlock) k_e3_walls(const float *__restrict__ GA, const float4 *__restrict__ aux,
+                                                         const __grid_constant__ E3Recs R, float *__restrict__ gold,
+                                                         float *__restrict__ tw, const __grid_constant__ E3Params P,
+                                                         int phase, int keep) {
+    const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    if (r >= P.nrec) return;  // whole warps
+    if (!R.neu[r]) return;    // uniform over the warp
+    constexpr unsigned long long PX = pack_axis(0), PY = pack_axis(1), PZ = pack_axis(2);
+    const int lane = threadIdx.x & 31;
+    const bool act = lane < Q;
+    const int p = act ? lane : 0;
+    const int ex = lane_c(PX, p), ey = lane_c(PY, p), ez = lane_c(PZ, p);
+    const uint32_t bb = R.bb[r];
+    const bool wl = act && ((bb >> p) & 1u);
+    const int c = R.cell[r], i = R.ci[r], j = R.cj[r], k = R.ck[r];
+    // the other links' loads first
+    float vnew = 0.0f, vold = 0.0f;
+    bool fresh = true;
+    int s = 0;
+    if (act && !wl) {
+        int a = i - ex, b = j - ey, d = k - ez;
+        a += a < 0 ? P.NX : (a >= P.NX ? -P.NX : 0);
+        b += b < 0 ? P.NY : (b >= P.NY ? -P.NY : 0);
+        d += d < 0 ? P.NZ : (d >= P.NZ ? -P.NZ : 0);
+        s = a + P.NX * (b + P.NY * d);
+        fresh = p == 0 || a < i || (a == i && (b < j || (b == j && d < k)));
+        vnew = GA[p * P.S + s];
+        if (!fresh) vold = gold[(long long)p * P.nrec + r];
+    }
+    const float u0 = R.uw[(3 * phase) * P.nrec + r], u1 = R.uw[(3 * phase + 1) * P.nrec + r],
+                u2 = R.uw[(3 * phase + 2) * P.nrec + r];
+    const float rho = 1.0f + aux[c].x;
+    // the normal: the mean wall-link direction (sums of small integers, exact)
+    const float nw = warp_sum(wl ? 1.0f : 0.0f);
+    const float n0 = warp_sum(wl ? (float)ex : 0.0f) / nw, n1 = warp_sum(wl ? (float)ey : 0.0f) / nw,
+                n2 = warp_sum(wl ? (float)ez : 0.0f) / nw;
+    const float cn = ex * n0 + ey * n1 + ez * n2;
+    float wall = 0.0f, other = 0.0f;
+    if (wl) {
+        const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+        const float x = ex * u0 + ey * u1 + ez * u2;
+        wall = lane_w(p) * (1.0f + p3m1(x, uu)) * cn;
+    } else if (act) {
+        other = ((fresh ? vnew : vold) + lane_w(p) * P.T_ref) * cn;
+    }
+    wall = warp_sum(wall);
+    other = warp_sum(other);
+    if (lane == 0) tw[r] = -other / (rho * wall);
+    if (keep && act && !wl && !fresh) gold[(long long)p * P.nrec + r] = vnew;
+}
+
+// The same, one thread a record: the form for grids whose wall records are a
+// small share, where it does not crowd the bulk kernel beside it.
 // Determine_Twall_Neumann for every record with Neumann links: the normal is
 // the mean direction of the links from walls (cdotn_pos); the other links
 // contribute this sweep's pulled value where the reference's push (i outer,
@@ -115,20 +208,20 @@ __device__ __forceinline__ float p3m1(float x, float uu) { return p2m1(x, uu) + 
 // at T = 1 of the cell's density (previous MacroProp) and the wall velocity.
 // With j.n = 0 (LBM.h's j_dot_n): T_w = -sum_other g c.n / sum_wall geq c.n.
 // keep: store this sweep's pulled values for the next sweep.
-__global__ void __launch_bounds__(kRecBlock) k_e3_walls(const float *__restrict__ GA, const float4 *__restrict__ aux,
-                                                     const E3Rec *__restrict__ recs, float *__restrict__ gold,
+__global__ void __launch_bounds__(kRecBlock) k_e3_walls_t(const float *__restrict__ GA, const float4 *__restrict__ aux,
+                                                     const __grid_constant__ E3Recs R, float *__restrict__ gold,
                                                      float *__restrict__ tw, const __grid_constant__ E3Params P,
                                                      int phase, int keep) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= P.nrec) return;
-    const E3Rec &R = recs[r];
-    if (!R.neu) return;
-    const int c = R.cell, i = R.i, j = R.j, k = R.k;
+    if (!R.neu[r]) return;
+    const uint32_t bb = R.bb[r];
+    const int c = R.cell[r], i = R.ci[r], j = R.cj[r], k = R.ck[r];
     float n0 = 0.0f, n1 = 0.0f, n2 = 0.0f;
     int np = 0;
 #pragma unroll
     for (int p = 0; p < Q; p++)
-        if ((R.bb >> p) & 1u) {
+        if ((bb >> p) & 1u) {
             n0 += cx(p);
             n1 += cy(p);
             n2 += cz(p);
@@ -138,14 +231,15 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_walls(const float *__restrict_
     n0 *= inv_np;
     n1 *= inv_np;
     n2 *= inv_np;
-    const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
+    const float u0 = R.uw[(3 * phase) * P.nrec + r], u1 = R.uw[(3 * phase + 1) * P.nrec + r],
+                u2 = R.uw[(3 * phase + 2) * P.nrec + r];
     const float uu = u0 * u0 + u1 * u1 + u2 * u2;
     // every load first (the kept values are rewritten below)
     float v[Q];
     uint32_t fresh = 0u;
 #pragma unroll
     for (int p = 0; p < Q; p++) {
-        if ((R.bb >> p) & 1u) continue;
+        if ((bb >> p) & 1u) continue;
         int si, sj, sk;
         const int s = wrap_src(i, j, k, p, P, si, sj, sk);
         const bool fr = p == 0 || si < i || (si == i && (sj < j || (sj == j && sk < k)));
@@ -157,7 +251,7 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_walls(const float *__restrict_
 #pragma unroll
     for (int p = 0; p < Q; p++) {
         const float cn = cx(p) * n0 + cy(p) * n1 + cz(p) * n2;
-        if ((R.bb >> p) & 1u) {
+        if ((bb >> p) & 1u) {
             const float x = cx(p) * u0 + cy(p) * u1 + cz(p) * u2;
             wall += wf(p) * (1.0f + p3m1(x, uu)) * cn;
         } else {
@@ -169,7 +263,7 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_walls(const float *__restrict_
     // this sweep's pulled values for the next sweep's stale links
 #pragma unroll
     for (int p = 0; p < Q; p++) {
-        if (((R.bb | fresh) >> p) & 1u) continue;
+        if (((bb | fresh) >> p) & 1u) continue;
         gold[(long long)p * P.nrec + r] = GA[p * P.S + wrap_src(i, j, k, p, P)];
     }
 }
@@ -313,14 +407,13 @@ __global__ void __launch_bounds__(kBlock) k_e3_bulk(const float *__restrict__ A,
 __global__ void __launch_bounds__(kRecBlock) k_e3_rec(const float *__restrict__ A, float *__restrict__ B,
                                                    const float *__restrict__ GA, float *__restrict__ GB,
                                                    float4 *__restrict__ aux, float4 *__restrict__ aux2,
-                                                   const E3Rec *__restrict__ recs, float *__restrict__ gold,
+                                                   const __grid_constant__ E3Recs R, float *__restrict__ gold,
                                                    const float *__restrict__ tw, const __grid_constant__ E3Params P,
                                                    uint32_t *__restrict__ status, float *__restrict__ mom, int gather,
                                                    int phase, int export_only) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= P.nrec) return;
-    const E3Rec &R = recs[r];
-    const int c = R.cell;
+    const int c = R.cell[r];
     const float4 h1 = aux[c], h2 = aux2[c];
     float f[Q], g[Q];
     if (!gather) {
@@ -334,27 +427,29 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_rec(const float *__restrict__ 
             for (int l = 0; l < Q; l++) gold[(long long)l * P.nrec + r] = g[l];
         }
     } else {
-        const int i = R.i, j = R.j, k = R.k;
-        const float u0 = R.uw[phase][0], u1 = R.uw[phase][1], u2 = R.uw[phase][2];
+        const int i = R.ci[r], j = R.cj[r], k = R.ck[r];
+        const uint32_t bb = R.bb[r], dir = R.dir[r], neu = R.neu[r];
+        const float u0 = R.uw[(3 * phase) * P.nrec + r], u1 = R.uw[(3 * phase + 1) * P.nrec + r],
+                    u2 = R.uw[(3 * phase + 2) * P.nrec + r];
         const float uu = u0 * u0 + u1 * u1 + u2 * u2;
         const float rho_p = 1.0f + h1.x;
-        const float tw_own = R.neu ? tw[r] : 0.0f;
+        const float tw_own = neu ? tw[r] : 0.0f;
         const int ph = phase == 0 ? 0 : 1;
         // the dynamic solid neighbours' T as this cell's push starts: the
         // last Neumann write before the cell, or the wall's own T
         float vd[kSlots];
-        float vsum = R.ssum[ph];
-        const int ndyn = R.ndyn;
+        float vsum = R.ssum[ph * P.nrec + r];
+        const int ndyn = R.ndyn[r];
 #pragma unroll 6
         for (int m = 0; m < ndyn; m++) {
-            const int w = R.dwriter[m];
-            vd[m] = w >= 0 ? tw[w] : R.dt[ph][m];
+            const int w = R.dwriter[m * P.nrec + r];
+            vd[m] = w >= 0 ? tw[w] : R.dt[(ph * kSlots + m) * P.nrec + r];
         }
 #pragma unroll 1
         for (int m = 0; m < ndyn; m++) vsum += vd[m];
 #pragma unroll
         for (int p = 0; p < Q; p++) {
-            if (!((R.bb >> p) & 1u)) {
+            if (!((bb >> p) & 1u)) {
                 const int s = wrap_src(i, j, k, p, P);
                 f[p] = A[p * P.S + s];
                 g[p] = GA[p * P.S + s];
@@ -364,18 +459,18 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_rec(const float *__restrict__ 
             const float x = cx(q) * u0 + cy(q) * u1 + cz(q) * u2;
             // f_opp(q) = f*_q - 2 w (u_w . c_q) / cs2 (lbm.cpp:273-274)
             f[p] = A[q * P.S + c] - 6.0f * wf(q) * x;
-            if ((R.dir >> p) & 1u) {
+            if ((dir >> p) & 1u) {
                 // Determine_Wall_Temperature at this point of the push: the
                 // neighbours this cell's own Neumann links wrote earlier in
                 // its push hold its T_w
                 float Tsum = vsum;
 #pragma unroll 1
                 for (int m = 0; m < ndyn; m++)
-                    if (R.down[m] < q) Tsum += tw_own - vd[m];
-                const float Tw = Tsum * R.inv_nsol;
+                    if (R.down[m * P.nrec + r] < q) Tsum += tw_own - vd[m];
+                const float Tw = Tsum * R.inv_nsol[r];
                 // -g*_q + 2 geq_q(rho, T_w, u_w) (lbm.cpp:277-280)
                 g[p] = 2.0f * wf(q) * (rho_p * Tw * (1.0f + p3m1(x, uu)) - P.T_ref) - GA[q * P.S + c];
-            } else if ((R.neu >> p) & 1u) {
+            } else if ((neu >> p) & 1u) {
                 // w rho T_w times the second-order shape of the wall (lbm.cpp:281-288)
                 g[p] = wf(q) * (rho_p * tw_own * (1.0f + p2m1(x, uu)) - P.T_ref);
             } else {
@@ -432,7 +527,8 @@ struct lbm_energy3d {
     float *f[2] = {nullptr, nullptr}, *g[2] = {nullptr, nullptr};
     float4 *aux = nullptr, *aux2 = nullptr;
     int *rec_of = nullptr;
-    E3Rec *recs = nullptr;
+    void *recbuf = nullptr;  // the records' field arrays
+    E3Recs recs{};
     float *gold = nullptr, *tw = nullptr, *mom = nullptr, *fields = nullptr;
     uint32_t *status = nullptr;
     bool has_neu = false, inited = false;
@@ -697,9 +793,17 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
         if (err == cudaSuccess) err = cudaStreamWaitEvent(e->s2, e->fork, 0);
         if (err != cudaSuccess) return err;
         if (gather && e->has_neu) {
-            const unsigned nb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
-            k_e3_walls<<<nb, kRecBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
-                                                export_only ? 0 : 1);
+            // a warp a record where the records are a large share of the
+            // grid (their chain is the step), else a thread a record
+            if ((long long)P.nrec * 8 >= P.N) {
+                const unsigned nb = (unsigned)(((long long)P.nrec * 32 + kWallBlock - 1) / kWallBlock);
+                k_e3_walls<<<nb, kWallBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
+                                                    export_only ? 0 : 1);
+            } else {
+                const unsigned nb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
+                k_e3_walls_t<<<nb, kRecBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
+                                                     export_only ? 0 : 1);
+            }
         }
         const unsigned rb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
         k_e3_rec<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur],
@@ -804,15 +908,67 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
     CKE(alloc3(e, &e->aux, (size_t)P.S * sizeof(float4)));
     CKE(alloc3(e, &e->aux2, (size_t)P.S * sizeof(float4)));
     CKE(alloc3(e, &e->rec_of, (size_t)N * sizeof(int)));
-    CKE(alloc3(e, &e->recs, std::max<size_t>(1, recs.size()) * sizeof(E3Rec)));
+    // the records, one array per field, each at a 256-byte boundary
+    const size_t nr = std::max<size_t>(1, recs.size());
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        const size_t at = off;
+        off += (bytes + 255) / 256 * 256;
+        return at;
+    };
+    const size_t o_cell = take(4 * nr), o_ci = take(4 * nr), o_cj = take(4 * nr), o_ck = take(4 * nr);
+    const size_t o_bb = take(4 * nr), o_dir = take(4 * nr), o_neu = take(4 * nr), o_ndyn = take(4 * nr);
+    const size_t o_inv = take(4 * nr), o_ssum = take(8 * nr), o_uw = take(36 * nr);
+    const size_t o_dw = take(4 * kSlots * nr), o_dt = take(8 * kSlots * nr), o_down = take(kSlots * nr);
+    std::vector<uint8_t> hb(off, 0);
+    auto put = [&](size_t at, size_t idx, const void *v, size_t sz) { memcpy(hb.data() + at + idx * sz, v, sz); };
+    for (size_t r = 0; r < recs.size(); r++) {
+        const E3Rec &R = recs[r];
+        put(o_cell, r, &R.cell, 4);
+        put(o_ci, r, &R.i, 4);
+        put(o_cj, r, &R.j, 4);
+        put(o_ck, r, &R.k, 4);
+        put(o_bb, r, &R.bb, 4);
+        put(o_dir, r, &R.dir, 4);
+        put(o_neu, r, &R.neu, 4);
+        put(o_ndyn, r, &R.ndyn, 4);
+        put(o_inv, r, &R.inv_nsol, 4);
+        for (int ph = 0; ph < 2; ph++) put(o_ssum, ph * nr + r, &R.ssum[ph], 4);
+        for (int ph = 0; ph < 3; ph++)
+            for (int a = 0; a < 3; a++) put(o_uw, (3 * ph + a) * nr + r, &R.uw[ph][a], 4);
+        for (int m = 0; m < kSlots; m++) {
+            put(o_dw, m * nr + r, &R.dwriter[m], 4);
+            put(o_down, m * nr + r, &R.down[m], 1);
+            for (int ph = 0; ph < 2; ph++) put(o_dt, (ph * kSlots + m) * nr + r, &R.dt[ph][m], 4);
+        }
+    }
+    CKE(alloc3(e, &e->recbuf, off));
+    CKE(cudaMemcpy(e->recbuf, hb.data(), off, cudaMemcpyHostToDevice));
+    {
+        const uint8_t *b = (const uint8_t *)e->recbuf;
+        E3Recs &D = e->recs;
+        D.cell = (const int *)(b + o_cell);
+        D.ci = (const int *)(b + o_ci);
+        D.cj = (const int *)(b + o_cj);
+        D.ck = (const int *)(b + o_ck);
+        D.bb = (const uint32_t *)(b + o_bb);
+        D.dir = (const uint32_t *)(b + o_dir);
+        D.neu = (const uint32_t *)(b + o_neu);
+        D.ndyn = (const int *)(b + o_ndyn);
+        D.inv_nsol = (const float *)(b + o_inv);
+        D.ssum = (const float *)(b + o_ssum);
+        D.uw = (const float *)(b + o_uw);
+        D.dwriter = (const int *)(b + o_dw);
+        D.dt = (const float *)(b + o_dt);
+        D.down = (const uint8_t *)(b + o_down);
+    }
     CKE(alloc3(e, &e->gold, (size_t)Q * std::max(1, P.nrec) * sizeof(float)));
     CKE(alloc3(e, &e->tw, (size_t)std::max(1, P.nrec) * sizeof(float)));
     CKE(alloc3(e, &e->mom, (size_t)8 * N * sizeof(float)));
     CKE(alloc3(e, &e->fields, (size_t)8 * N * sizeof(float)));
     CKE(alloc3(e, &e->status, sizeof(uint32_t)));
     CKE(cudaMemcpy(e->rec_of, rec_of.data(), (size_t)N * sizeof(int), cudaMemcpyHostToDevice));
-    if (!recs.empty())
-        CKE(cudaMemcpy(e->recs, recs.data(), recs.size() * sizeof(E3Rec), cudaMemcpyHostToDevice));
+
     std::vector<float> fl((size_t)8 * N);
     for (long long c = 0; c < N; c++) {
         fl[c] = (float)rho[c];

@@ -88,6 +88,25 @@ def test_rayleigh_benard_fullsize_vs_oracle(pkg, orc):
     assert abs(uy_g - uy_o) < 1e-4 * uy_o and abs(nu_g - nu_o) < 1e-4 * abs(nu_o - 1.0)
 
 
+def test_rayleigh_benard_larger_box_vs_oracle(pkg, orc):
+    """The same set-up on a 128 x 64 x 32 box, where the wall records are
+    under an eighth of the grid and the Neumann pre-pass runs one thread a
+    record (the warp-a-record form serves the smaller boxes above); 60 steps
+    against the oracle."""
+    steps = 60
+    lat, c = orc.rayleigh_benard(128, 64, 32)
+    s = _rb_gpu(pkg, lat, c)
+    s.step(steps)
+    assert s.status() == 0
+    m = s.moments()
+    assert lat.step_plain(steps) == 0
+    fluid = lat.types == orc.TYPE_F
+    ref = dict(rho=lat.rho, ux=lat.ux, uy=lat.uy, uz=lat.uz, T=lat.T, qx=lat.hq[0], qy=lat.hq[1], qz=lat.hq[2])
+    eT, eu, er, eq = _errors(m, ref, fluid)
+    print("rayleigh 128x64x32, %d steps: T %.3g of spread, u %.3g of max, rho %.3g, q %.3g" % (steps, eT, eu, er, eq))
+    assert eT < 1e-5 and eu < 1e-4 and er < 1e-6 and eq < 1e-4, (eT, eu, er, eq)
+
+
 def test_lid_box_periodic_adiabatic_vs_oracle(pkg, orc):
     """A box with a moving lid (the y+ wall, u_x = 0.05, Dirichlet at T = 1.2),
     a Dirichlet floor at 1, Neumann x walls, an adiabatic wall
