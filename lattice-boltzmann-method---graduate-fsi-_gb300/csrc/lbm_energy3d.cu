@@ -21,9 +21,9 @@
 // wall velocity of each phase, and for each solid neighbour the cell whose
 // Neumann write it sees (or none, then the wall's own T).  Per step a
 // pre-pass (k_e3_walls) forms the Neumann cells' T_w; the step kernel
-// (k_e3_bulk for the other fluid cells, k_e3_rec for the records) pulls,
-// applies the wall rules, takes the moments, refreshes the force and
-// collides.
+// (k_e3_bulk for the other fluid cells; k_e3_rgather and k_e3_rcollide for
+// the records) pulls, applies the wall rules, takes the moments, refreshes
+// the force and collides.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -399,7 +399,125 @@ __global__ void __launch_bounds__(kBlock) k_e3_bulk(const float *__restrict__ A,
     macro_collide(c, f, g, h1, h2, P, B, GB, aux, aux2, status, mom, gather, export_only);
 }
 
-// The wall records, one thread each: the pull with the reference's wall
+// The wall records' pull, one warp a record and one lane a link, into the
+// scratch array (f then g, [2 Q][records]): the reference's wall rules
+// (lbm.cpp:266-288).  f: bounce-back with Determine_Wall_Velocity; g:
+// Dirichlet anti-bounce-back at Determine_Wall_Temperature's T as the sweep
+// has left the solid neighbours (the lanes load the dynamic neighbours'
+// values; a link's own-write corrections come by shuffles), Neumann the
+// equilibrium of the pre-pass's T_w, adiabatic the kept initial value.
+__global__ void __launch_bounds__(kWallBlock) k_e3_rgather(const float *__restrict__ A, const float *__restrict__ GA,
+                                                           const float4 *__restrict__ aux,
+                                                           const __grid_constant__ E3Recs R,
+                                                           const float *__restrict__ gold, const float *__restrict__ tw,
+                                                           float *__restrict__ scr, const __grid_constant__ E3Params P,
+                                                           int phase) {
+    const int r = (int)((blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5);
+    if (r >= P.nrec) return;  // whole warps
+    constexpr unsigned long long PX = pack_axis(0), PY = pack_axis(1), PZ = pack_axis(2);
+    const int lane = threadIdx.x & 31;
+    const bool act = lane < Q;
+    const int p = act ? lane : 0;
+    const int ex = lane_c(PX, p), ey = lane_c(PY, p), ez = lane_c(PZ, p);
+    const int c = R.cell[r], i = R.ci[r], j = R.cj[r], k = R.ck[r];
+    const uint32_t bb = R.bb[r], dir = R.dir[r], neu = R.neu[r];
+    const bool wl = act && ((bb >> p) & 1u);
+    float fv = 0.0f, gv = 0.0f;
+    if (act && !wl) {
+        int sa = i - ex, sb = j - ey, sc = k - ez;
+        sa += sa < 0 ? P.NX : (sa >= P.NX ? -P.NX : 0);
+        sb += sb < 0 ? P.NY : (sb >= P.NY ? -P.NY : 0);
+        sc += sc < 0 ? P.NZ : (sc >= P.NZ ? -P.NZ : 0);
+        const int src = sa + P.NX * (sb + P.NY * sc);
+        fv = A[p * P.S + src];
+        gv = GA[p * P.S + src];
+    }
+    const int ph = phase == 0 ? 0 : 1;
+    const float tw_own = neu ? tw[r] : 0.0f;
+    // the dynamic solid neighbours' T as this cell's push starts (the last
+    // Neumann write before the cell, or the wall's own T), one lane each
+    const int ndyn = R.ndyn[r];
+    float vdl = 0.0f;
+    int dl = 255;
+    if (lane < ndyn) {
+        const int w = R.dwriter[lane * P.nrec + r];
+        vdl = w >= 0 ? tw[w] : R.dt[(ph * kSlots + lane) * P.nrec + r];
+        dl = R.down[lane * P.nrec + r];
+    }
+    const float vsum = R.ssum[ph * P.nrec + r] + warp_sum(vdl);
+    // the reference's push direction of this link, towards the wall
+    const int q = p == 0 ? 0 : ((p & 1) ? p + 1 : p - 1);
+    // the neighbours this cell's own Neumann links wrote before push index q
+    float corr = 0.0f;
+    for (int m = 0; m < ndyn; m++) {
+        const float vm = __shfl_sync(0xffffffffu, vdl, m);
+        const int dm = __shfl_sync(0xffffffffu, dl, m);
+        if (dm < q) corr += tw_own - vm;
+    }
+    if (wl) {
+        const float u0 = R.uw[(3 * phase) * P.nrec + r], u1 = R.uw[(3 * phase + 1) * P.nrec + r],
+                    u2 = R.uw[(3 * phase + 2) * P.nrec + r];
+        const float uu = u0 * u0 + u1 * u1 + u2 * u2;
+        const float rho_p = 1.0f + aux[c].x;
+        const float w = lane_w(p);
+        const float x = -(ex * u0 + ey * u1 + ez * u2);  // c_q . u_w
+        // f_opp(q) = f*_q - 2 w (u_w . c_q) / cs2 (lbm.cpp:273-274)
+        fv = A[q * P.S + c] - 6.0f * w * x;
+        if ((dir >> p) & 1u) {
+            const float Tw = (vsum + corr) * R.inv_nsol[r];
+            // -g*_q + 2 geq_q(rho, T_w, u_w) (lbm.cpp:277-280)
+            gv = 2.0f * w * (rho_p * Tw * (1.0f + p3m1(x, uu)) - P.T_ref) - GA[q * P.S + c];
+        } else if ((neu >> p) & 1u) {
+            // w rho T_w times the second-order shape of the wall (lbm.cpp:281-288)
+            gv = w * (rho_p * tw_own * (1.0f + p2m1(x, uu)) - P.T_ref);
+        } else {
+            gv = gold[(long long)p * P.nrec + r];  // never written: the initial value
+        }
+    }
+    if (act) {
+        scr[(long long)p * P.nrec + r] = fv;
+        scr[(long long)(Q + p) * P.nrec + r] = gv;
+    }
+}
+
+// MacroProp and the collision of the wall records, one thread each, from the
+// gathered populations (the first collision: from the set-up state, whose g
+// become the kept initial values).
+__global__ void __launch_bounds__(kRecBlock) k_e3_rcollide(const float *__restrict__ A, float *__restrict__ B,
+                                                           const float *__restrict__ GA, float *__restrict__ GB,
+                                                           float4 *__restrict__ aux, float4 *__restrict__ aux2,
+                                                           const __grid_constant__ E3Recs R, float *__restrict__ gold,
+                                                           const float *__restrict__ scr,
+                                                           const __grid_constant__ E3Params P,
+                                                           uint32_t *__restrict__ status, float *__restrict__ mom,
+                                                           int gather, int export_only) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= P.nrec) return;
+    const int c = R.cell[r];
+    const float4 h1 = aux[c], h2 = aux2[c];
+    float f[Q], g[Q];
+    if (!gather) {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            f[l] = A[l * P.S + c];
+            g[l] = GA[l * P.S + c];
+        }
+        if (!export_only) {
+#pragma unroll
+            for (int l = 0; l < Q; l++) gold[(long long)l * P.nrec + r] = g[l];
+        }
+    } else {
+#pragma unroll
+        for (int l = 0; l < Q; l++) {
+            f[l] = scr[(long long)l * P.nrec + r];
+            g[l] = scr[(long long)(Q + l) * P.nrec + r];
+        }
+    }
+    macro_collide(c, f, g, h1, h2, P, B, GB, aux, aux2, status, mom, gather, export_only);
+}
+
+// The wall records in one pass, one thread each (the form for grids whose
+// records are a small share): the pull with the reference's wall
 // rules (lbm.cpp:266-288).  f: bounce-back with Determine_Wall_Velocity;
 // g: Dirichlet anti-bounce-back at Determine_Wall_Temperature's T as the
 // sweep has left the solid neighbours, Neumann the equilibrium of the
@@ -530,6 +648,7 @@ struct lbm_energy3d {
     void *recbuf = nullptr;  // the records' field arrays
     E3Recs recs{};
     float *gold = nullptr, *tw = nullptr, *mom = nullptr, *fields = nullptr;
+    float *scr = nullptr;  // the records' gathered f and g, [2 Q][records]
     uint32_t *status = nullptr;
     bool has_neu = false, inited = false;
     int cur = 0;
@@ -792,10 +911,12 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
         err = cudaEventRecord(e->fork, e->s);
         if (err == cudaSuccess) err = cudaStreamWaitEvent(e->s2, e->fork, 0);
         if (err != cudaSuccess) return err;
+        // a warp a record where the records are a large share of the grid
+        // (their chain is the step), else a thread a record (a warp each
+        // would crowd the bulk kernel beside them)
+        const bool wide = (long long)P.nrec * 8 >= P.N;
         if (gather && e->has_neu) {
-            // a warp a record where the records are a large share of the
-            // grid (their chain is the step), else a thread a record
-            if ((long long)P.nrec * 8 >= P.N) {
+            if (wide) {
                 const unsigned nb = (unsigned)(((long long)P.nrec * 32 + kWallBlock - 1) / kWallBlock);
                 k_e3_walls<<<nb, kWallBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
                                                     export_only ? 0 : 1);
@@ -806,9 +927,20 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
             }
         }
         const unsigned rb = (unsigned)((P.nrec + kRecBlock - 1) / kRecBlock);
-        k_e3_rec<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur],
-                                          e->aux, e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather,
-                                          phase, export_only);
+        if (wide) {
+            if (gather) {
+                const unsigned gb = (unsigned)(((long long)P.nrec * 32 + kWallBlock - 1) / kWallBlock);
+                k_e3_rgather<<<gb, kWallBlock, 0, e->s2>>>(e->f[e->cur], e->g[e->cur], e->aux, e->recs, e->gold,
+                                                         e->tw, e->scr, P, phase);
+            }
+            k_e3_rcollide<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur],
+                                                      e->g[1 - e->cur], e->aux, e->aux2, e->recs, e->gold, e->scr,
+                                                      P, e->status, mom, gather, export_only);
+        } else {
+            k_e3_rec<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur],
+                                                 e->aux, e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather,
+                                                 phase, export_only);
+        }
         err = cudaEventRecord(e->join, e->s2);
         if (err != cudaSuccess) return err;
     }
@@ -964,6 +1096,7 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
     }
     CKE(alloc3(e, &e->gold, (size_t)Q * std::max(1, P.nrec) * sizeof(float)));
     CKE(alloc3(e, &e->tw, (size_t)std::max(1, P.nrec) * sizeof(float)));
+    CKE(alloc3(e, &e->scr, (size_t)2 * Q * std::max(1, P.nrec) * sizeof(float)));
     CKE(alloc3(e, &e->mom, (size_t)8 * N * sizeof(float)));
     CKE(alloc3(e, &e->fields, (size_t)8 * N * sizeof(float)));
     CKE(alloc3(e, &e->status, sizeof(uint32_t)));
