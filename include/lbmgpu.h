@@ -129,8 +129,9 @@ typedef struct lbm_config {
 /* lbm_config.thermal: 0 none; 1 a D3Q7 temperature population with a heat
  * source and Boussinesq buoyancy (D3Q19 handles); 2 the reference's own
  * ENERGY model (LBM.h:58): temperature populations on the flow lattice with
- * the cubic equilibrium, viscous heating and anti-bounce-back Dirichlet walls
- * (D2Q9 handles; faces periodic or Dirichlet walls). */
+ * the cubic equilibrium, viscous heating, and Dirichlet, Neumann or adiabatic
+ * walls (D2Q9 handles; faces periodic or walls).  The ENERGY model on D3Q19
+ * is a solver object of its own: lbmgpu_energy3d_create. */
 enum { LBM_THERMAL_NONE = 0, LBM_THERMAL_D3Q7 = 1, LBM_THERMAL_ENERGY = 2 };
 
 enum { LBM_LATTICE_D3Q19 = 19, LBM_LATTICE_D2Q9 = 9 };
