@@ -1007,8 +1007,10 @@ extern "C" lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host) {
 // MB) would sit in front of every small read-back the caller makes meanwhile
 // (force rows, status words); these stores leave the copy engines free and
 // run beside the next steps.  16 blocks reach the same host-link rate as 64
-// (67 MB in about 0.38 ms on a GB300) and take fewer SM slots from the steps
-// they overlap; 4 blocks halve the rate.
+// (67 MB in about 0.38 ms on a GB300); fewer take fewer SM slots from the
+// steps they overlap, until the copy no longer ends within them.  Measured
+// end to end on the FP16 sphere channel (10 steps per call): 4 blocks 31.1 k,
+// 6 36.1 k, 8 36.2 k, 10 36.5 k, 12 35.2 k, 16 34.2 k MLUPS.
 __global__ void __launch_bounds__(512) k_copy_out(const float *__restrict__ src, float *__restrict__ dst, long long n) {
     const long long n4 = n >> 2;
     const long long stride = (long long)gridDim.x * blockDim.x;
@@ -1042,7 +1044,7 @@ extern "C" lbm_status lbmgpu_download_all_f32_async(lbm_handle *h, float *host) 
         dptr = pa.devicePointer;
     cudaGetLastError();
     if (dptr) {
-        k_copy_out<<<16, 512, 0, h->s_dl>>>(h->mom, (float *)dptr, n);
+        k_copy_out<<<10, 512, 0, h->s_dl>>>(h->mom, (float *)dptr, n);
         CUDA_TRY(cudaGetLastError());
     } else {
         CUDA_TRY(cudaMemcpyAsync(host, h->mom, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, h->s_dl));
