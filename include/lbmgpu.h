@@ -107,7 +107,7 @@ typedef struct lbm_config {
     int staged;           /* must be 0: reserved (a tensor-copy staged step kernel, removed after it measured
                              slower than direct loads in every variant) */
     int ibm_overlap;      /* 0: a fixed body's IBM phase overlaps the far-region streaming (second
-                             stream); <0: serial */
+                             stream; D3Q19 and D2Q9); <0: serial */
     int xface;            /* 0: lanes on x = 0 / x = nx-1 keep the plain pull and redo their five
                              x-crossing links; <0: their whole warp takes the boundary-class path */
     int lattice;          /* LBM_LATTICE_*: 0 or 19 = D3Q19; 9 = D2Q9 (the reference's #define D2Q9
@@ -525,6 +525,8 @@ typedef struct lbm_energy3d_setup {
     const double *rho;          /* set-up density; NULL: 1 */
     const double *u;            /* set-up velocity [3][cells]; NULL: 0 */
     const double *F;            /* set-up force [3][cells]; NULL: 0 */
+    int graph_steps;            /* steps per captured CUDA graph from the third step on (rounded up to
+                                   even, at most 1000); 0 = 10, <0 = every step launched on its own */
 } lbm_energy3d_setup;
 /* Creates the solver and runs LBM::Init on the set-up.  LBM_ERR_UNSUPPORTED
  * for other cell types, or a wall cell next to fluid without a solid

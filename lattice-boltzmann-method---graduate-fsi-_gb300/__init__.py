@@ -63,7 +63,7 @@ class Energy3DSetup(C.Structure):
                 ("cp", C.c_double), ("g_beta", C.c_double), ("T_star", C.c_double),
                 ("type", C.POINTER(C.c_uint8)), ("type_energy", C.POINTER(C.c_uint8)),
                 ("T", C.POINTER(C.c_double)), ("rho", C.POINTER(C.c_double)), ("u", C.POINTER(C.c_double)),
-                ("F", C.POINTER(C.c_double))]
+                ("F", C.POINTER(C.c_double)), ("graph_steps", C.c_int)]
 
 
 class Face(C.Structure):
@@ -682,13 +682,15 @@ class Energy3D:
     FIELDS = {"rho": FIELD_RHO, "ux": FIELD_UX, "uy": FIELD_UY, "uz": FIELD_UZ, "T": FIELD_T, "qx": FIELD_QX,
               "qy": FIELD_QY, "qz": FIELD_QZ}
 
-    def __init__(self, types, types_energy, T, tau, tau_g, cp, g_beta=0.0, T_star=0.0, rho=None, u=None, F=None):
+    def __init__(self, types, types_energy, T, tau, tau_g, cp, g_beta=0.0, T_star=0.0, rho=None, u=None, F=None,
+                 graph_steps=0):
         self.L = load()
         t = np.ascontiguousarray(types, dtype=np.uint8)
         nz, ny, nx = (d - 2 for d in t.shape)
         self.shape = t.shape
         keep = [t, np.ascontiguousarray(types_energy, dtype=np.uint8), np.ascontiguousarray(T, dtype=np.float64)]
-        su = Energy3DSetup(nx=nx, ny=ny, nz=nz, tau=tau, tau_g=tau_g, cp=cp, g_beta=g_beta, T_star=T_star)
+        su = Energy3DSetup(nx=nx, ny=ny, nz=nz, tau=tau, tau_g=tau_g, cp=cp, g_beta=g_beta, T_star=T_star,
+                           graph_steps=graph_steps)
         su.type = keep[0].ctypes.data_as(C.POINTER(C.c_uint8))
         su.type_energy = keep[1].ctypes.data_as(C.POINTER(C.c_uint8))
         su.T = _dp(keep[2])

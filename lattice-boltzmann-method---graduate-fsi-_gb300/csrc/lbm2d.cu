@@ -1708,12 +1708,13 @@ cudaError_t seq_end2d(lbm_handle *h) {
 
 // Whether the split applies: a fixed IBM body on plain cells whose near box
 // (the IBM box of the step and one cell around it) lies inside the lattice,
-// so that no periodic wrap reaches it.  The box is read back once.
+// so that no periodic wrap reaches it, unless the configuration asks for the
+// serial order (ibm_overlap < 0).  The box is read back once.
 lbm_status decide_overlap2d(lbm_handle *h) {
     lbm2d *d = h->d2;
     if (d->overlap_known) return LBM_OK;
     d->overlap = false;
-    if (d->ibm && d->ib.motion == LBM_MOTION_FIXED && !d->links && !d->energy) {
+    if (d->ibm && d->ib.motion == LBM_MOTION_FIXED && !d->links && !d->energy && h->cfg.ibm_overlap >= 0) {
         State2 st;
         CK2(cudaStreamSynchronize(h->s));
         CK2(cudaMemcpy(&st, d->st, sizeof(State2), cudaMemcpyDeviceToHost));

@@ -26,6 +26,7 @@
 // the force and collides.
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -657,6 +658,10 @@ struct lbm_energy3d {
     cudaStream_t s2 = nullptr;  // the wall records, beside the bulk kernel (high priority)
     cudaEvent_t ev[2] = {nullptr, nullptr};
     cudaEvent_t fork = nullptr, join = nullptr;
+    // steps per captured graph (even, so that a replay ends on the buffer it
+    // started from); 0: every step launched on its own
+    int graph_steps = 0;
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // by the starting buffer
     std::vector<void *> allocs;
     std::vector<E3Wall> walls;
 };
@@ -672,6 +677,8 @@ cudaError_t alloc3(lbm_energy3d *e, Tp **p, size_t bytes) {
 }
 
 void free3(lbm_energy3d *e) {
+    for (cudaGraphExec_t g : e->gexec)
+        if (g) cudaGraphExecDestroy(g);
     for (void *p : e->allocs) cudaFree(p);
     if (e->s) cudaStreamDestroy(e->s);
     if (e->s2) cudaStreamDestroy(e->s2);
@@ -952,6 +959,37 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
     return cudaGetLastError();
 }
 
+// From the third step on every step enqueues the same launches (gather on,
+// phase 2) on alternating buffers: graph_steps of them are captured once per
+// starting buffer, the second stream's records joining the capture through
+// the fork and join events, and replayed as one launch.
+cudaError_t replay3(lbm_energy3d *e) {
+    cudaGraphExec_t &x = e->gexec[e->cur];
+    if (!x) {
+        const int cur0 = e->cur;
+        const long long steps0 = e->steps;
+        cudaError_t err = cudaStreamBeginCapture(e->s, cudaStreamCaptureModeThreadLocal);
+        if (err != cudaSuccess) return err;
+        for (int n = 0; n < e->graph_steps && err == cudaSuccess; n++) {
+            err = enqueue3(e, nullptr, 0);
+            e->cur = 1 - e->cur;
+            e->steps++;
+        }
+        e->cur = cur0;
+        e->steps = steps0;
+        cudaGraph_t g = nullptr;
+        const cudaError_t end = cudaStreamEndCapture(e->s, &g);
+        if (err == cudaSuccess) err = end;
+        if (err == cudaSuccess) err = cudaGraphInstantiate(&x, g, 0);
+        if (g) cudaGraphDestroy(g);
+        if (err != cudaSuccess) {
+            x = nullptr;
+            return err;
+        }
+    }
+    return cudaGraphLaunch(x, e->s);
+}
+
 }  // namespace
 
 extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_energy3d **out) {
@@ -990,6 +1028,11 @@ extern "C" lbm_status lbmgpu_energy3d_create(const lbm_energy3d_setup *su, lbm_e
 
     lbm_energy3d *e = new lbm_energy3d();
     e->walls.swap(walls);
+    // 0: ten steps a graph; odd counts round up to the next even one
+    if (su->graph_steps >= 0) {
+        const int gs = su->graph_steps ? std::min(su->graph_steps, 1000) : 10;
+        e->graph_steps = gs + (gs & 1);
+    }
     e->nx = su->nx;
     e->ny = su->ny;
     e->nz = su->nz;
@@ -1139,10 +1182,17 @@ extern "C" lbm_status lbmgpu_energy3d_step(lbm_energy3d *e, int nsteps) {
     if (!e) return fail3(LBM_ERR_INVALID, "energy3d_step: null handle");
     if (!e->inited) return fail3(LBM_ERR_STATE, "energy3d_step: not initialised");
     if (nsteps < 0) return fail3(LBM_ERR_INVALID, "energy3d_step: negative count");
-    for (int n = 0; n < nsteps; n++) {
+    for (int n = 0; n < nsteps;) {
+        if (e->graph_steps > 0 && e->steps >= 3 && nsteps - n >= e->graph_steps) {
+            CK3(replay3(e));
+            e->steps += e->graph_steps;
+            n += e->graph_steps;
+            continue;
+        }
         CK3(enqueue3(e, nullptr, 0));
         e->cur = 1 - e->cur;
         e->steps++;
+        n++;
     }
     return LBM_OK;
 }

@@ -21,11 +21,12 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 
-def _rb_gpu(pkg, lat, c):
+def _rb_gpu(pkg, lat, c, graph_steps=0):
     """The GPU solver on the oracle lattice's set-up arrays (the oracle's
     restatement of main_setup_RayleighBenard1, before any step)."""
     return pkg.Energy3D(lat.types.copy(), lat.types_energy.copy(), lat.T.copy(), c["tau"], c["tau_g"], c["cp"],
-                        g_beta=c["g_beta"], T_star=c["T_star"], F=np.stack([lat.Fx, lat.Fy, lat.Fz]).copy())
+                        g_beta=c["g_beta"], T_star=c["T_star"], F=np.stack([lat.Fx, lat.Fy, lat.Fz]).copy(),
+                        graph_steps=graph_steps)
 
 
 def _errors(m, ref, fluid):
@@ -193,6 +194,23 @@ def test_moving_interior_solid_vs_oracle(pkg, orc):
     assert eT < 2e-5 and eu < 1e-5 and er < 1e-6 and eq < 2e-5, (eT, eu, er, eq)
     # the block drags the fluid along x
     assert m["ux"][fl].max() > 1e-3
+
+
+@pytest.mark.parametrize("graph_steps", [0, 3])
+def test_energy3d_graph_replay_matches_eager(pkg, orc, graph_steps):
+    """Steps replayed from captured graphs (the default ten, and an odd
+    request rounded up to four), between eager ones and across both starting
+    buffers, give the same bits as every step launched on its own."""
+    lat, c = orc.rayleigh_benard(200, 50, 5)
+    out = []
+    for gs in (graph_steps, -1):
+        s = _rb_gpu(pkg, lat, c, graph_steps=gs)
+        for n in (2, 11, 1, 24, 5):
+            s.step(n)
+        assert s.status() == 0
+        out.append(s.moments())
+    for k in out[1]:
+        assert np.array_equal(out[0][k], out[1][k], equal_nan=True), k
 
 
 def test_energy3d_rejects_other_cell_types(pkg, orc):
