@@ -1266,6 +1266,9 @@ struct lbm2d {
     Ibm2 ib;
     double *hist = nullptr;
     long long hist_cap = 1 << 16;
+    // lbmgpu_get_forces: pinned, device-mapped rows, grown on demand
+    double *fstage = nullptr;
+    long long fstage_rows = 0;
     // graphs of gsteps steps, one per parity of the buffer they start from
     // (a graph reads and writes fixed buffers)
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
@@ -1843,6 +1846,7 @@ void l2d_free(lbm_handle *h) {
     for (cudaEvent_t ev : {d->ev_far, d->ev_near, d->ev_join})
         if (ev) cudaEventDestroy(ev);
     for (void *p : d->allocs) cudaFree(p);
+    if (d->fstage) cudaFreeHost(d->fstage);
     delete d;
     h->d2 = nullptr;
 }
@@ -2248,25 +2252,45 @@ bool l2d_has_markers(lbm_handle *h) { return h->d2->ibm; }
 
 int l2d_marker_count(lbm_handle *h) { return h->d2->ibm ? h->d2->ib.n : 0; }
 
+// The last `take` rows of the force ring (drag, lift, 0, step) as the rows
+// of lbmgpu_get_forces (Fx, Fy, 0, 0, 0, 0, 0, step), stored into pinned,
+// device-mapped host memory: one launch and one synchronisation for a read
+// the reference's loop makes every step, however long the ring.
+__global__ void k_forces2d_out(const double *__restrict__ hist, long long cap, long long steps, long long take,
+                               double *__restrict__ dst) {
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < take * 8;
+         e += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(e & 7);
+        // reference step steps - take + 1 + (e >> 3), 1-based
+        const double *r = hist + 4 * ((steps - take + (e >> 3)) % cap);
+        dst[e] = k < 2 ? r[k] : (k == 7 ? r[3] : 0.0);
+    }
+}
+
 lbm_status l2d_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
     lbm2d *d = h->d2;
     if (!d->ibm) return f2(LBM_ERR_STATE, "get_forces: no markers set");
-    CK2(cudaStreamSynchronize(h->s));
-    const long long have = std::min<long long>(h->steps, d->hist_cap);
-    const long long take = std::min<long long>(have, max_steps);
-    std::vector<double> ring((size_t)d->hist_cap * 4);
-    CK2(cudaMemcpy(ring.data(), d->hist, ring.size() * sizeof(double), cudaMemcpyDeviceToHost));
-    for (long long i = 0; i < take; i++) {
-        const long long s = h->steps - take + 1 + i;  // reference step, 1-based
-        const double *r = &ring[(size_t)(4 * ((s - 1) % d->hist_cap))];
-        double *o = out + 8 * i;
-        o[0] = r[0];
-        o[1] = r[1];
-        o[2] = 0.0;
-        o[3] = o[4] = o[5] = 0.0;
-        o[6] = 0.0;
-        o[7] = r[3];
+    const long long take = std::min<long long>(std::min<long long>(h->steps, d->hist_cap), max_steps);
+    if (take > d->fstage_rows) {
+        if (d->fstage) {
+            CK2(cudaStreamSynchronize(h->s));
+            CK2(cudaFreeHost(d->fstage));
+            d->fstage = nullptr;
+            d->fstage_rows = 0;
+        }
+        const long long cap = std::max<long long>(take, 64);
+        CK2(cudaHostAlloc((void **)&d->fstage, (size_t)cap * 8 * sizeof(double), cudaHostAllocMapped));
+        d->fstage_rows = cap;
     }
+    if (take > 0) {
+        double *dst = nullptr;
+        CK2(cudaHostGetDevicePointer((void **)&dst, d->fstage, 0));
+        const unsigned blocks = (unsigned)std::min<long long>((take * 8 + 255) / 256, 64);
+        k_forces2d_out<<<blocks, 256, 0, h->s>>>(d->hist, d->hist_cap, h->steps, take, dst);
+        CK2(cudaGetLastError());
+    }
+    CK2(cudaStreamSynchronize(h->s));
+    if (take > 0) std::memcpy(out, d->fstage, (size_t)take * 8 * sizeof(double));
     if (n_out) *n_out = (int)take;
     return LBM_OK;
 }

@@ -328,6 +328,7 @@ static void free_handle(lbm_handle *h) {
     if (h->s2) cudaStreamDestroy(h->s2);
     if (h->s3) cudaStreamDestroy(h->s3);
     if (h->s) cudaStreamDestroy(h->s);
+    if (h->fstage) cudaFreeHost(h->fstage);
     delete h;
 }
 
@@ -1002,6 +1003,17 @@ extern "C" lbm_status lbmgpu_download_all_f32(lbm_handle *h, float *host) {
     return LBM_OK;
 }
 
+// The device address of pinned, device-mapped host memory (lbmgpu_host_alloc),
+// else null.
+static const void *mapped_device_ptr(const void *host) {
+    cudaPointerAttributes pa;
+    const void *d = nullptr;
+    if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer)
+        d = pa.devicePointer;
+    cudaGetLastError();
+    return d;
+}
+
 // Device-to-host copy done by a few blocks that store straight into pinned,
 // device-mapped host memory.  A copy-engine transfer of the moments (tens of
 // MB) would sit in front of every small read-back the caller makes meanwhile
@@ -1037,12 +1049,8 @@ extern "C" lbm_status lbmgpu_download_all_f32_async(lbm_handle *h, float *host) 
     const long long n = (long long)nf * h->P.N;
     // pinned memory the device can address (lbmgpu_host_alloc): stored by a
     // kernel; anything else: a copy-engine transfer
-    cudaPointerAttributes pa;
-    void *dptr = nullptr;
-    if (cudaPointerGetAttributes(&pa, host) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer &&
-        ((uintptr_t)pa.devicePointer & 15u) == 0)
-        dptr = pa.devicePointer;
-    cudaGetLastError();
+    void *dptr = const_cast<void *>(mapped_device_ptr(host));
+    if (((uintptr_t)dptr & 15u) != 0) dptr = nullptr;
     if (dptr) {
         k_copy_out<<<10, 512, 0, h->s_dl>>>(h->mom, (float *)dptr, n);
         CUDA_TRY(cudaGetLastError());
@@ -1175,25 +1183,46 @@ extern "C" lbm_status lbmgpu_get_solid_forces(lbm_handle *h, double *out, int ma
     return LBM_OK;
 }
 
+// The last n = min(steps done, ring size, rows) rows of the force ring, in
+// step order, and n after them, stored into pinned, device-mapped host memory.
+// The device knows the step count, so the read-back is one launch and one
+// synchronisation, and it takes no copy engine (a moments download may hold
+// one for a few hundred microseconds).
+__global__ void k_forces_out(const DevState *__restrict__ ds, const double *__restrict__ hist, long long cap,
+                             long long rows, double *__restrict__ dst) {
+    const long long step = ds->step;
+    const long long n = min(min(step, cap), rows);
+    const long long first = step - n;
+    for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < n * 8;
+         e += (long long)gridDim.x * blockDim.x)
+        dst[e] = hist[((first + (e >> 3)) % cap) * 8 + (e & 7)];
+    if (blockIdx.x == 0 && threadIdx.x == 0) dst[rows * 8] = (double)n;
+}
+
 extern "C" lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out) {
     if (!h || !out || max_steps < 0) return fail(LBM_ERR_INVALID, "get_forces: bad argument");
     if (h->d2) return l2d_get_forces(h, out, max_steps, n_out);
     if (!h->ibm) return fail(LBM_ERR_STATE, "get_forces: no markers set");
-    DevState d;
-    CUDA_TRY(cudaMemcpyAsync(&d, h->ds, sizeof(d), cudaMemcpyDeviceToHost, h->s));
+    const long long rows = std::min<long long>(max_steps, h->hist_cap);
+    if (rows > h->fstage_rows || !h->fstage) {
+        if (h->fstage) {
+            CUDA_TRY(cudaStreamSynchronize(h->s));
+            CUDA_TRY(cudaFreeHost(h->fstage));
+            h->fstage = nullptr;
+            h->fstage_rows = 0;
+        }
+        const long long cap = std::max<long long>(rows, 64);
+        CUDA_TRY(cudaHostAlloc((void **)&h->fstage, (size_t)(cap * 8 + 1) * sizeof(double), cudaHostAllocMapped));
+        h->fstage_rows = cap;
+    }
+    double *dst = nullptr;
+    CUDA_TRY(cudaHostGetDevicePointer((void **)&dst, h->fstage, 0));
+    const unsigned blocks = (unsigned)std::min<long long>((rows * 8 + 255) / 256 + 1, 64);
+    k_forces_out<<<blocks, 256, 0, h->s>>>(h->ds, h->hist, h->hist_cap, rows, dst);
+    CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(h->s));
-    long long avail = std::min<long long>(d.step, h->hist_cap);
-    long long n = std::min<long long>(avail, max_steps);
-    // the last n entries of the ring, in at most two contiguous pieces
-    long long first = (d.step - n) % h->hist_cap;
-    long long n1 = std::min(n, h->hist_cap - first);
-    if (n1 > 0)
-        CUDA_TRY(cudaMemcpyAsync(out, h->hist + first * 8, (size_t)n1 * 8 * sizeof(double), cudaMemcpyDeviceToHost,
-                                 h->s));
-    if (n > n1)
-        CUDA_TRY(cudaMemcpyAsync(out + n1 * 8, h->hist, (size_t)(n - n1) * 8 * sizeof(double),
-                                 cudaMemcpyDeviceToHost, h->s));
-    CUDA_TRY(cudaStreamSynchronize(h->s));
+    const long long n = (long long)h->fstage[rows * 8];
+    std::memcpy(out, h->fstage, (size_t)n * 8 * sizeof(double));
     if (n_out) *n_out = (int)n;
     return LBM_OK;
 }

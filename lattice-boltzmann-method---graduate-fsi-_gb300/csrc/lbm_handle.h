@@ -44,6 +44,10 @@ struct lbm_handle {
     BodyParams bp;
     double *hist = nullptr;
     long long hist_cap = 1 << 16;
+    // lbmgpu_get_forces: pinned, device-mapped rows of the ring and their
+    // count, written by a kernel (grown on demand)
+    double *fstage = nullptr;
+    long long fstage_rows = 0;
     // graphs
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};
     int gsteps = 16;

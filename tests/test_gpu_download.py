@@ -48,16 +48,30 @@ def test_async_download_equals_sync_and_pipelines(pkg):
         b.close()
 
 
-def test_update_markers_keeps_graphs_and_moves_the_body(pkg, orc):
-    """lbmgpu_update_markers: the same positions change nothing (graphs kept;
-    the spreading's float atomics make two runs agree to rounding, not bit
-    for bit); shifted positions before the first step give the run of a body
-    registered there."""
+@pytest.mark.parametrize("memory", ["pageable", "pinned"])
+def test_update_markers_keeps_graphs_and_moves_the_body(pkg, orc, memory):
+    """lbmgpu_update_markers: the same positions change nothing (graphs kept);
+    shifted positions before the first step give the run of a body
+    registered there; from pageable memory and from pinned memory
+    (lbmgpu_host_alloc)."""
     L = pkg.load()
     n, D, c = 200, 8.0, (20.0, 12.0, 10.0)
     mk = orc.fibonacci_sphere(n, D, c)
-    xyz = np.ascontiguousarray(np.stack([mk["x"], mk["y"], mk["z"]]))
-    ds = np.ascontiguousarray(mk["ds"])
+    bufs = []
+
+    def host(a):
+        a = np.ascontiguousarray(a, dtype=np.float64)
+        if memory == "pageable":
+            return a
+        p = C.c_void_p()
+        pkg.check(L.lbmgpu_host_alloc(a.nbytes, C.byref(p)))
+        bufs.append(p)
+        h = np.ctypeslib.as_array(C.cast(p, C.POINTER(C.c_double)), shape=a.shape)
+        h[...] = a
+        return h
+
+    xyz = host(np.stack([mk["x"], mk["y"], mk["z"]]))
+    ds = host(mk["ds"])
 
     def solver(pos):
         s = pkg.Solver(pkg.channel_config(48, 24, 20, 0.6, u_in=0.05, graph_steps=4))
@@ -75,7 +89,7 @@ def test_update_markers_keeps_graphs_and_moves_the_body(pkg, orc):
     fa, fb = a.forces(), b.forces()
     assert np.array_equal(fa[:, 7], fb[:, 7]) and np.abs(fa[:, :3] - fb[:, :3]).max() < 1e-5 * np.abs(fa[:, :3]).max()
     # a small move that keeps every stencil inside the band set up for xyz
-    shifted = np.ascontiguousarray(xyz + np.array([[0.1], [0.0], [0.0]]))
+    shifted = host(xyz + np.array([[0.1], [0.0], [0.0]]))
     d, e = solver(shifted), solver(xyz)
     pkg.check(L.lbmgpu_update_markers(e.h, shifted.ctypes.data_as(dp), ds.ctypes.data_as(dp)))
     d.step(16)
@@ -85,6 +99,8 @@ def test_update_markers_keeps_graphs_and_moves_the_body(pkg, orc):
     assert np.abs(fd[:, :3] - fe[:, :3]).max() < 1e-5 * np.abs(fd[:, :3]).max()
     for x in (a, b, d, e):
         x.close()
+    for p in bufs:
+        L.lbmgpu_host_free(p)
     with pytest.raises(pkg.LbmError):
         s = pkg.Solver(pkg.channel_config(16, 8, 8, 0.6))
         s.init()

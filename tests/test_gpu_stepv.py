@@ -89,11 +89,13 @@ def test_multicell_sphere_matches_single_cell(pkg, orc):
     """The fixed IBM sphere with the near box carved out of the multi-cell far
     region (its x bounds rounded to whole segments): the same forces and
     fields as the one-cell-per-thread kernel, bit for bit (the spreading sums
-    in fixed point, independent of the order of its atomics)."""
+    in fixed point, independent of the order of its atomics); with two cells
+    a thread the moment export runs on the multi-cell kernel too, its band
+    segments on the one-cell path."""
     nx, ny, nz, tau, D, nm, m_max, steps = 64, 40, 40, 0.53, 20.0, 1257, 5, 40
     center = (23.3, 20.2, 19.6)
     out = []
-    for cells in (1, 4):
+    for cells in (1, 2, 4):
         s = pkg.Solver(pkg.channel_config(nx, ny, nz, tau, u_in=0.05, storage="f32", cells=cells))
         s.init()
         mk = orc.fibonacci_sphere(nm, D, center)
@@ -103,7 +105,8 @@ def test_multicell_sphere_matches_single_cell(pkg, orc):
         assert s.status() == 0
         out.append((s.forces(), s.moments(), s.cells_per_thread()))
         s.close()
-    assert out[0][2] == 1 and out[1][2] == 4
-    assert np.array_equal(out[0][0], out[1][0])
-    for c in out[0][1]:
-        assert np.array_equal(out[0][1][c], out[1][1][c]), c
+    assert [o[2] for o in out] == [1, 2, 4]
+    for o in out[1:]:
+        assert np.array_equal(out[0][0], o[0])
+        for c in out[0][1]:
+            assert np.array_equal(out[0][1][c], o[1][c]), (o[2], c)
