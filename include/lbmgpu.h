@@ -297,6 +297,15 @@ lbm_status lbmgpu_mea_box(lbm_handle *h, const int box[6], double out[3]);
  * of cells is the same.  Summed in FP64 in a fixed order. */
 lbm_status lbmgpu_nusselt(lbm_handle *h, double alpha, double dT, double *out);
 
+/* The IBM body's force rows of the last min(steps done, 65536, max_steps)
+ * steps, oldest first, 8 doubles a row into out; *n_out = the rows written.
+ * D3Q19: the FP64 sums over the markers of -F_m ds_m (x, y, z), their torque
+ * about the body centre (x, y, z), the heat exchange, and the step's index
+ * (the steps done before it).  D2Q9: drag and lift (IBLBM's sums,
+ * lbm.cpp:1392-1416, with the added-mass term when set), five zeros, and the
+ * reference's 1-based step.  Cl/Cd = row / (0.5 u^2 area).  One kernel copies
+ * the rows into pinned, device-mapped host memory; the call synchronises the
+ * handle's stream once. */
 lbm_status lbmgpu_get_forces(lbm_handle *h, double *out, int max_steps, int *n_out);
 
 /* New positions (3 x n, x rows first) and weights (n) for the markers that
