@@ -189,3 +189,37 @@ def test_config_energy_2d_maps_couette_and_refuses_the_rest(pkg):
     with pytest.raises(pkg.LbmError) as e:
         pkg.Solver(cfg)
     assert e.value.status == 1
+
+
+def test_ctypes_mirrors_match_the_header_layouts(pkg, tmp_path):
+    """Every public struct of include/lbmgpu.h has the size and field offsets
+    of its ctypes mirror in the package, as a C compiler lays it out."""
+    import ctypes as C
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    mirrors = {"lbm_face": pkg.Face, "lbm_config": pkg.Config, "lbm_ibm_config": pkg.IbmConfig,
+               "lbm_serve_request": pkg.ServeRequest, "lbm_serve_options": pkg.ServeOptions,
+               "lbm_serve_result": pkg.ServeResult, "lbm_energy3d_setup": pkg.Energy3DSetup}
+    txt = open(os.path.join(ROOT, "include", "lbmgpu.h")).read()
+    assert sorted(mirrors) == sorted(re.findall(r"typedef struct (lbm_\w+) \{", txt))
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "lbmgpu.h"', "int main(void) {"]
+    expect = []
+    for name, cls in mirrors.items():
+        lines.append('    printf("%%zu\\n", sizeof(%s));' % name)
+        expect.append(("sizeof " + name, C.sizeof(cls)))
+        for field, _ in cls._fields_:
+            lines.append('    printf("%%zu\\n", offsetof(%s, %s));' % (name, field))
+            expect.append((name + "." + field, getattr(cls, field).offset))
+    lines += ["    return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.check_call([cc, "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)])
+    got = [int(v) for v in subprocess.check_output([str(exe)], text=True).split()]
+    assert len(got) == len(expect)
+    for (what, want), have in zip(expect, got):
+        assert have == want, (what, have, want)
