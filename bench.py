@@ -369,6 +369,15 @@ def run_cylinder2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 10.0):
     s.step(100)
     ms = s.step_timed(steps)
     cd = s.forces(1)[0, 0] / (0.5 * u * u * D)
+    # the reference's loop through the C ABI: one step a call and that
+    # step's drag / lift read back after it (main.cpp:195-211), host clock
+    loop_steps = 500
+    s.sync()
+    t0 = time.perf_counter()
+    for _ in range(loop_steps):
+        s.step(1)
+        s.forces(1)
+    loop_s = time.perf_counter() - t0
     st = s.status()
     s.close()
     gpu = nx * ny * steps / (ms * 1e-3) / 1e6
@@ -382,6 +391,9 @@ def run_cylinder2d(pkg, orc, steps: int = 2000, cpu_seconds: float = 10.0):
     return {"workload": "D2Q9 implicit-IBM cylinder 800x400, D=20, 200 markers, m_max=20 (the reference's "
                         "default build)", "value": gpu, "unit": "MLUPS", "ms_per_lbm_step": ms / steps,
             "steps_timed": steps, "cd_last": float(cd), "status": int(st),
+            "step_loop": {"value": nx * ny * loop_steps / loop_s / 1e6, "unit": "MLUPS",
+                          "us_per_step": loop_s / loop_steps * 1e6, "steps": loop_steps,
+                          "note": "one lbmgpu_step(1) and one lbmgpu_get_forces(1) a step, host clock"},
             "cpu_port": {"value": cpu, "unit": "MLUPS", "cores": os.cpu_count() or 1, "kind": "port",
                          "sample": "%d steps of the same case, FP64 oracle (OpenMP)" % n},
             "speedup_vs_cpu_port": gpu / cpu}
