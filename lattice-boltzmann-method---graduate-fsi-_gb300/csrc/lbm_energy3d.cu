@@ -30,6 +30,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/lbmgpu.h"
@@ -422,6 +423,9 @@ __global__ void __launch_bounds__(kWallBlock) k_e3_rgather(const float *__restri
     const int ex = lane_c(PX, p), ey = lane_c(PY, p), ez = lane_c(PZ, p);
     const int c = R.cell[r], i = R.ci[r], j = R.cj[r], k = R.ck[r];
     const uint32_t bb = R.bb[r], dir = R.dir[r], neu = R.neu[r];
+    // launched early behind the pre-pass (programmatic dependent launch):
+    // the record's fields above never change; wait before the populations
+    cudaGridDependencySynchronize();
     const bool wl = act && ((bb >> p) & 1u);
     float fv = 0.0f, gv = 0.0f;
     if (act && !wl) {
@@ -495,6 +499,7 @@ __global__ void __launch_bounds__(kRecBlock) k_e3_rcollide(const float *__restri
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= P.nrec) return;
     const int c = R.cell[r];
+    cudaGridDependencySynchronize();  // behind the gather (programmatic dependent launch)
     const float4 h1 = aux[c], h2 = aux2[c];
     float f[Q], g[Q];
     if (!gather) {
@@ -906,6 +911,23 @@ lbm_status build_records(const lbm_energy3d_setup &su, int NX, int NY, int NZ, d
         if (e_ != cudaSuccess) return fail3(LBM_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
     } while (0)
 
+// A launch on stream s that may begin while the stream's previous kernel
+// finishes (programmatic dependent launch, when pdl): the kernel waits for
+// that grid's results with cudaGridDependencySynchronize.
+template <class... K, class... A>
+cudaError_t launch3(bool pdl, unsigned grid, unsigned block, cudaStream_t s, void (*kern)(K...), A &&...args) {
+    cudaLaunchConfig_t c = {};
+    c.gridDim = dim3(grid);
+    c.blockDim = dim3(block);
+    c.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    c.attrs = at;
+    c.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&c, kern, std::forward<A>(args)...);
+}
+
 // One step: the Neumann pre-pass and the wall records on the second stream,
 // beside the bulk kernel (they write disjoint cells and read only the
 // previous step's arrays); the next step waits for both.
@@ -922,7 +944,12 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
         // (their chain is the step), else a thread a record (a warp each
         // would crowd the bulk kernel beside them)
         const bool wide = (long long)P.nrec * 8 >= P.N;
+        // the record chain's later kernels start behind the earlier ones
+        // where the chain is the step (the warp forms); on large grids their
+        // early blocks would take slots from the bulk kernel beside them
+        bool behind = false;
         if (gather && e->has_neu) {
+            behind = true;
             if (wide) {
                 const unsigned nb = (unsigned)(((long long)P.nrec * 32 + kWallBlock - 1) / kWallBlock);
                 k_e3_walls<<<nb, kWallBlock, 0, e->s2>>>(e->g[e->cur], e->aux, e->recs, e->gold, e->tw, P, phase,
@@ -937,17 +964,21 @@ cudaError_t enqueue3(lbm_energy3d *e, float *mom, int export_only) {
         if (wide) {
             if (gather) {
                 const unsigned gb = (unsigned)(((long long)P.nrec * 32 + kWallBlock - 1) / kWallBlock);
-                k_e3_rgather<<<gb, kWallBlock, 0, e->s2>>>(e->f[e->cur], e->g[e->cur], e->aux, e->recs, e->gold,
-                                                         e->tw, e->scr, P, phase);
+                err = launch3(behind, gb, kWallBlock, e->s2, k_e3_rgather, (const float *)e->f[e->cur],
+                              (const float *)e->g[e->cur], (const float4 *)e->aux, e->recs, (const float *)e->gold,
+                              (const float *)e->tw, e->scr, P, phase);
+                if (err != cudaSuccess) return err;
+                behind = true;
             }
-            k_e3_rcollide<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur],
-                                                      e->g[1 - e->cur], e->aux, e->aux2, e->recs, e->gold, e->scr,
-                                                      P, e->status, mom, gather, export_only);
+            err = launch3(behind, rb, kRecBlock, e->s2, k_e3_rcollide, (const float *)e->f[e->cur],
+                          e->f[1 - e->cur], (const float *)e->g[e->cur], e->g[1 - e->cur], e->aux, e->aux2, e->recs,
+                          e->gold, (const float *)e->scr, P, e->status, mom, gather, export_only);
         } else {
-            k_e3_rec<<<rb, kRecBlock, 0, e->s2>>>(e->f[e->cur], e->f[1 - e->cur], e->g[e->cur], e->g[1 - e->cur],
-                                                 e->aux, e->aux2, e->recs, e->gold, e->tw, P, e->status, mom, gather,
-                                                 phase, export_only);
+            err = launch3(false, rb, kRecBlock, e->s2, k_e3_rec, (const float *)e->f[e->cur], e->f[1 - e->cur],
+                          (const float *)e->g[e->cur], e->g[1 - e->cur], e->aux, e->aux2, e->recs, e->gold,
+                          (const float *)e->tw, P, e->status, mom, gather, phase, export_only);
         }
+        if (err != cudaSuccess) return err;
         err = cudaEventRecord(e->join, e->s2);
         if (err != cudaSuccess) return err;
     }
